@@ -1,0 +1,215 @@
+/*
+ * pathguide.h - C ABI of the GB300 path-guiding library (libpathguide.so).
+ *
+ * Plain C: pointers, sizes and integer status codes; no CUDA or torch types.
+ * Streams are passed as `void*` holding a cudaStream_t (NULL = legacy default
+ * stream).  Every entry point returns a pg_status; the text of the last error
+ * of a context is available from pg_last_error().
+ *
+ * Each entry point names the reference interface it stands in for
+ * (paths relative to the rtx-pathtracer source tree).
+ */
+#ifndef PATHGUIDE_H
+#define PATHGUIDE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* MAX_DISTRIBUTIONS in shaders/limits.glsl:6; four 4-wide lightpmm kernels
+ * (src/PathGuiding.h:28-30). */
+#define PG_MAX_COMPONENTS 16u
+/* INVALID region id of a sample slot (src/SampleCollector.h:13). */
+#define PG_INVALID_REGION 0xFFFFFFFFu
+
+typedef enum pg_status {
+    PG_OK = 0,
+    PG_ERR_ARG = 1,      /* bad argument (null pointer, size out of range)   */
+    PG_ERR_CUDA = 2,     /* a CUDA runtime call failed                        */
+    PG_ERR_TIMEOUT = 3,  /* a bounded device-side wait ran out               */
+    PG_ERR_NUMERIC = 4,  /* non-finite result detected                        */
+    PG_ERR_NOMEM = 5,    /* capacity of the context exceeded                  */
+    PG_ERR_IO = 6,       /* file could not be read or written                 */
+    PG_ERR_PARSE = 7,    /* scene file malformed                              */
+    PG_ERR_STATE = 8     /* call made in the wrong order                      */
+} pg_status;
+
+/* Fit modes of pg_fit_regions. */
+typedef enum pg_fit_mode {
+    /* VMMFactory::initialize + VMMFactory::fit(..., initialize=false)
+     * (external/lightpmm/include/pmm/VMMFactory.h:132-216), which is what
+     * PathGuiding::createPMMs + the first updateRegion do
+     * (src/PathGuiding.cpp:42-51, 357-359). */
+    PG_FIT_INIT = 0,
+    /* VMMFactory::fit(..., initialize=false) from the current state. */
+    PG_FIT_CONTINUE = 1,
+    /* VMMFactory::updateFit: stepwise EM that adds the statistics recovered
+     * from the current parameters (VMMFactory.h:305-362, 543-555); used by
+     * PathGuiding::updateRegion on every pass after the first
+     * (src/PathGuiding.cpp:360-363). */
+    PG_FIT_UPDATE = 2
+} pg_fit_mode;
+
+/* lightpmm::DirectionalData (external/lightpmm/include/pmm/DirectionalData.h:44-101)
+ * and the GLSL record (shaders/guiding.glsl:99-111): 40 bytes, AoS.
+ * `flags` holds the guiding region id or PG_INVALID_REGION. */
+typedef struct pg_directional_data {
+    float position[3];
+    float direction[3];
+    float weight;
+    float pdf;
+    float distance;
+    uint32_t flags;
+} pg_directional_data;
+
+/* lightpmm::VMMFactoryProperties (VMMFactory.h:45-61) with the overrides of
+ * PathGuiding::configureVMMFactory (src/PathGuiding.cpp:33-40), plus the
+ * parallax switch of PathGuiding (src/PathGuiding.h:103). */
+typedef struct pg_fit_config {
+    uint32_t min_itr;
+    uint32_t max_itr;
+    float rel_ll_threshold;
+    uint32_t num_initial_components; /* 1..16 */
+    float init_kappa;
+    float max_kappa;
+    float v_prior;
+    float r_prior;
+    float r_prior_weight;
+    uint32_t use_parallax;
+} pg_fit_config;
+
+/* Per-region mixture state held in device memory (one 704-byte record per
+ * region).  It carries what lightpmm::ParametricMixtureModel
+ * (ParametricMixtureModel.h:69-81), its VMFKernel lanes (VMFKernel.h:75-86)
+ * and PMM_ExtraData's parallax fields (src/PathGuiding.h:77-84) hold, in
+ * structure-of-arrays form over the 16 components. */
+typedef struct pg_region_state {
+    float weight[16];      /* mixture weights (weight prior applied)          */
+    float mu_x[16];        /* mean directions                                 */
+    float mu_y[16];
+    float mu_z[16];
+    float kappa[16];       /* concentrations                                  */
+    float r[16];           /* mean cosines                                    */
+    float norm[16];        /* kappa / (2 pi (1 - exp(-2 kappa)))              */
+    float e_min2k[16];     /* exp(-2 kappa)                                   */
+    float distance[16];    /* parallax distance per lobe (+inf: unknown)      */
+    float dist_sum_w[16];  /* accumulated weight of the distance estimate     */
+    float parallax_mean[3];
+    float last_parallax_mean[3];
+    uint32_t k;            /* active components                               */
+    float sample_weight;   /* m_sampleWeight                                  */
+    float num_samples;     /* m_numSamples                                    */
+    uint32_t num_em_iterations;
+    uint64_t total_num_samples;
+    float ll_last;         /* weighted log-likelihood of the last E-step      */
+    uint32_t iters_last;   /* EM iterations run by the last fit               */
+    uint32_t flags;        /* PG_STATE_* bits                                 */
+    uint32_t reserved;
+} pg_region_state;
+
+#define PG_STATE_FITTED 1u     /* region has been fitted at least once        */
+#define PG_STATE_NONFINITE 2u  /* last fit produced a non-finite parameter    */
+
+/* VMF_Theta / VMM_Theta as uploaded to the tracer (src/PathGuiding.h:36-75,
+ * shaders/guiding.glsl:14-51): 40 and 720 bytes, scalar layout. */
+typedef struct pg_vmf_theta {
+    float mu[3];
+    float k;
+    float norm;
+    float e_min2k;
+    float distance;
+    float target[3];
+} pg_vmf_theta;
+
+typedef struct pg_vmm_theta {
+    pg_vmf_theta thetas[16];
+    float pi[16];
+    float mean_position[3];
+    int32_t used_distributions;
+} pg_vmm_theta;
+
+typedef struct pg_ctx pg_ctx;
+
+/* ------------------------------------------------------------------ */
+/* Context                                                             */
+/* ------------------------------------------------------------------ */
+
+/* Reference defaults: VMMFactoryProperties (VMMFactory.h:45-61) overridden by
+ * PathGuiding::configureVMMFactory (src/PathGuiding.cpp:33-40): K=8,
+ * maxItr=100, maxKappa=50000; parallax on (src/RayTracingApp.h:117). */
+void pg_default_fit_config(pg_fit_config *out);
+
+/* Creates a context on the current CUDA device.  The context owns the
+ * per-region mixture states (max_regions records) and the scratch of the
+ * fit (work queues, region order) and of the sample sort (max_samples
+ * records).  Replaces the constructor PathGuiding::PathGuiding
+ * (src/PathGuiding.cpp:11-24) minus its Vulkan objects. */
+int pg_ctx_create(const pg_fit_config *cfg, uint32_t max_regions, uint64_t max_samples,
+                  pg_ctx **out);
+int pg_ctx_destroy(pg_ctx *ctx);
+const char *pg_last_error(const pg_ctx *ctx);
+const char *pg_status_string(int status);
+int pg_get_fit_config(const pg_ctx *ctx, pg_fit_config *out);
+int pg_set_fit_config(pg_ctx *ctx, const pg_fit_config *cfg);
+
+/* ------------------------------------------------------------------ */
+/* Mixture state                                                       */
+/* ------------------------------------------------------------------ */
+
+/* Initialises n_regions mixtures as VMMFactory::initialize does
+ * (VMMFactory.h:132-148): K components, weights 1/K, kappa = init_kappa,
+ * means on the spherical Fibonacci set (VMMFactory.h:594-632); distances
+ * +inf (external/guiding/incrementaldistance.h:52-55).  Device-side. */
+int pg_init_regions(pg_ctx *ctx, uint32_t n_regions, void *stream);
+
+/* Host copies of the device states (ParametricMixtureModel::serialize /
+ * deserialize, ParametricMixtureModel.h:373-397, in this layout). */
+int pg_get_region_states(pg_ctx *ctx, pg_region_state *host_out, uint32_t first,
+                         uint32_t count, void *stream);
+int pg_set_region_states(pg_ctx *ctx, const pg_region_state *host_in, uint32_t first,
+                         uint32_t count, void *stream);
+/* Device pointer to the state array (valid until pg_ctx_destroy). */
+int pg_region_states_device(pg_ctx *ctx, pg_region_state **dev_out);
+
+/* ------------------------------------------------------------------ */
+/* Batched weighted EM                                                 */
+/* ------------------------------------------------------------------ */
+
+/* Fits the mixtures of regions [0, n_regions) to their samples in one
+ * launch.  `dirw` (device, 16-byte aligned) holds one float4
+ * {direction.xyz, weight} per sample, grouped by region; `offsets` (device)
+ * holds n_regions+1 sample offsets.  Regions run different iteration counts
+ * (relative log-likelihood test per region).  Replaces the serial loop
+ * PathGuiding::update -> updateRegion -> VMMFactory::fit / updateFit
+ * (src/PathGuiding.cpp:281-288, 350-368; VMMFactory.h:157-216, 305-362). */
+int pg_fit_regions(pg_ctx *ctx, const float *dirw, const uint32_t *offsets,
+                   uint32_t n_regions, int mode, void *stream);
+
+/* Weighted log-likelihood sum_n w_n log p(d_n) of each region's samples under
+ * the current mixtures (the quantity of VMMFactory.h:531-532), written as
+ * double to ll_out (device, n_regions entries). */
+int pg_eval_loglik(pg_ctx *ctx, const float *dirw, const uint32_t *offsets,
+                   uint32_t n_regions, double *ll_out, void *stream);
+
+/* Tuning of the fit launch (chosen by the autotuner; 0 = default). */
+typedef struct pg_fit_tuning {
+    uint32_t threads_per_cta;     /* 64, 128, 256                            */
+    uint32_t smem_samples;        /* samples kept in shared memory per CTA   */
+    uint32_t ctas_per_sm;         /* resident CTAs per SM for the grid size  */
+    uint32_t reserved;
+} pg_fit_tuning;
+int pg_set_fit_tuning(pg_ctx *ctx, const pg_fit_tuning *t);
+int pg_get_fit_tuning(const pg_ctx *ctx, pg_fit_tuning *t);
+
+/* Device kernels launched by the last pg_fit_regions call (for counting
+ * launches in benchmarks). */
+int pg_last_launch_count(const pg_ctx *ctx, uint32_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PATHGUIDE_H */

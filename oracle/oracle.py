@@ -1,0 +1,189 @@
+"""ctypes bindings of the oracle libraries (TEST INFRASTRUCTURE).
+
+Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference
+legs import this module, and only as the checker or the timed CPU baseline.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import importlib.util
+import os
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent
+
+
+def _load_abi():
+    spec = importlib.util.spec_from_file_location("_pg_abi", ROOT / "rtx-pathtracer_gb300" / "abi.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+abi = _load_abi()
+_P = C.c_void_p
+_U32 = C.c_uint32
+_I = C.c_int
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class Oracle:
+    """The plain-C restatement (liboracle.so)."""
+
+    def __init__(self, path: Path | None = None):
+        path = path or HERE / "liboracle.so"
+        self.lib = C.CDLL(str(path))
+        L = self.lib
+        L.pgo_fit_lpmm32.argtypes = [C.POINTER(abi.FitConfig), _I, _U32, _P, _P, _P, _P, _I]
+        L.pgo_fit_f64.argtypes = [C.POINTER(abi.FitConfig), _I, _U32, _P, _P, _P, _P, _I]
+        L.pgo_init_states.argtypes = [C.POINTER(abi.FitConfig), _U32, _P, _I]
+        L.pgo_initial_mus.argtypes = [_U32, _P]
+        L.pgo_eval_ll_f64.argtypes = [_U32, _P, _P, _P, _P]
+        L.pgo_fastexp.argtypes = [C.c_float]
+        L.pgo_fastexp.restype = C.c_float
+        L.pgo_prefit_parallax.argtypes = [_U32, _P, _P, _P, _P, _P]
+        L.pgo_update_distances.argtypes = [_U32, _P, _P, _P, _P]
+        L.pgo_reposition.argtypes = [_P, _P]
+        L.pgo_pack_vmm_theta.argtypes = [_U32, _P, _I, _P]
+        L.pgo_region_aabbs.argtypes = [_U32, _P, _P]
+        L.pgo_sort_samples.argtypes = [_P, C.c_uint64, _U32, _P, _P]
+        L.pgo_sort_samples.restype = C.c_uint64
+
+    def init_states(self, cfg, n, exact=True):
+        s = np.zeros(n, dtype=abi.STATE_DTYPE)
+        self.lib.pgo_init_states(C.byref(cfg), n, abi.ptr(s), int(exact))
+        return s
+
+    def fit(self, cfg, dirw, offsets, states=None, mode=abi.PG_FIT_INIT, f64=True, threads=None):
+        dirw = _f32(dirw)
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint32)
+        R = offsets.shape[0] - 1
+        st = np.zeros(R, dtype=abi.STATE_DTYPE) if states is None else states.copy()
+        threads = threads or (os.cpu_count() or 1)
+        if f64:
+            ll = np.zeros(R, dtype=np.float64)
+            self.lib.pgo_fit_f64(C.byref(cfg), mode, R, abi.ptr(dirw), abi.ptr(offsets), abi.ptr(st),
+                                 abi.ptr(ll), threads)
+        else:
+            ll = np.zeros(R, dtype=np.float32)
+            self.lib.pgo_fit_lpmm32(C.byref(cfg), mode, R, abi.ptr(dirw), abi.ptr(offsets),
+                                    abi.ptr(st), abi.ptr(ll), threads)
+        return st, ll
+
+    def eval_ll(self, dirw, offsets, states):
+        dirw = _f32(dirw)
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint32)
+        R = offsets.shape[0] - 1
+        ll = np.zeros(R, dtype=np.float64)
+        self.lib.pgo_eval_ll_f64(R, abi.ptr(dirw), abi.ptr(offsets), abi.ptr(states), abi.ptr(ll))
+        return ll
+
+    def initial_mus(self, K):
+        out = np.zeros(48, dtype=np.float32)
+        self.lib.pgo_initial_mus(K, abi.ptr(out))
+        return out.reshape(3, 16)
+
+    def fastexp(self, x):
+        return np.array([self.lib.pgo_fastexp(float(v)) for v in np.ravel(x)], dtype=np.float32)
+
+    def prefit_parallax(self, sorted_records, offsets, means):
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint32)
+        R = offsets.shape[0] - 1
+        N = sorted_records.shape[0]
+        dirw = np.zeros((N, 4), dtype=np.float32)
+        dist = np.zeros(N, dtype=np.float32)
+        means = _f32(means)
+        self.lib.pgo_prefit_parallax(R, abi.ptr(sorted_records), abi.ptr(offsets), abi.ptr(means),
+                                     abi.ptr(dirw), abi.ptr(dist))
+        return dirw, dist
+
+    def update_distances(self, dirw, dist, offsets, states):
+        st = states.copy()
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint32)
+        self.lib.pgo_update_distances(offsets.shape[0] - 1, abi.ptr(_f32(dirw)), abi.ptr(_f32(dist)),
+                                      abi.ptr(offsets), abi.ptr(st))
+        return st
+
+    def reposition(self, state, new_to_old):
+        s = np.array(state, dtype=abi.STATE_DTYPE).reshape(1).copy()
+        v = _f32(new_to_old)
+        self.lib.pgo_reposition(abi.ptr(s), abi.ptr(v))
+        return s[0]
+
+    def pack_vmm_theta(self, states, use_parallax=True):
+        out = np.zeros(states.shape[0], dtype=abi.VMM_THETA_DTYPE)
+        self.lib.pgo_pack_vmm_theta(states.shape[0], abi.ptr(states), int(use_parallax), abi.ptr(out))
+        return out
+
+    def region_aabbs(self, split_count, scene_aabb):
+        out = np.zeros((1 << split_count, 6), dtype=np.float32)
+        a = _f32(scene_aabb)
+        self.lib.pgo_region_aabbs(split_count, abi.ptr(a), abi.ptr(out))
+        return out
+
+    def sort_samples(self, records, n_regions):
+        sorted_out = np.zeros_like(records)
+        offsets = np.zeros(n_regions + 1, dtype=np.uint32)
+        n = self.lib.pgo_sort_samples(abi.ptr(records), records.shape[0], n_regions,
+                                      abi.ptr(sorted_out), abi.ptr(offsets))
+        return sorted_out[:n], offsets
+
+
+class ReferenceFit:
+    """The reference's own lightpmm fit compiled in place (oracle/_ref)."""
+
+    PATH = HERE / "_ref" / "liblightpmm_ref.so"
+
+    @classmethod
+    def available(cls) -> bool:
+        return cls.PATH.exists()
+
+    def __init__(self):
+        self.lib = C.CDLL(str(self.PATH))
+        L = self.lib
+        L.lpmm_ref_init.argtypes = [C.POINTER(abi.FitConfig), _U32, _P]
+        L.lpmm_ref_fit.argtypes = [C.POINTER(abi.FitConfig), _I, _U32, _P, _P, _P, _P]
+        L.lpmm_ref_update_distances.argtypes = [_U32, _P, _P, _P, _P]
+        L.lpmm_ref_reposition.argtypes = [_P, _P]
+        L.lpmm_ref_fastexp.argtypes = [_P, _P, _U32]
+        L.lpmm_ref_state_size.restype = _U32
+        assert L.lpmm_ref_state_size() == abi.STATE_DTYPE.itemsize
+
+    def init_states(self, cfg, n):
+        s = np.zeros(n, dtype=abi.STATE_DTYPE)
+        self.lib.lpmm_ref_init(C.byref(cfg), n, abi.ptr(s))
+        return s
+
+    def fit(self, cfg, dirw, offsets, states=None, mode=abi.PG_FIT_INIT):
+        dirw = _f32(dirw)
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint32)
+        R = offsets.shape[0] - 1
+        st = np.zeros(R, dtype=abi.STATE_DTYPE) if states is None else states.copy()
+        ll = np.zeros(R, dtype=np.float32)
+        self.lib.lpmm_ref_fit(C.byref(cfg), mode, R, abi.ptr(dirw), abi.ptr(offsets), abi.ptr(st),
+                              abi.ptr(ll))
+        return st, ll
+
+    def update_distances(self, dirw, dist, offsets, states):
+        st = states.copy()
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint32)
+        self.lib.lpmm_ref_update_distances(offsets.shape[0] - 1, abi.ptr(_f32(dirw)),
+                                           abi.ptr(_f32(dist)), abi.ptr(offsets), abi.ptr(st))
+        return st
+
+    def reposition(self, state, new_to_old):
+        s = np.array(state, dtype=abi.STATE_DTYPE).reshape(1).copy()
+        self.lib.lpmm_ref_reposition(abi.ptr(s), abi.ptr(_f32(new_to_old)))
+        return s[0]
+
+    def fastexp(self, x):
+        x = _f32(x)
+        y = np.zeros_like(x)
+        self.lib.lpmm_ref_fastexp(abi.ptr(x), abi.ptr(y), x.size)
+        return y

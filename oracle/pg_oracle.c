@@ -1,0 +1,778 @@
+/*
+ * pg_oracle.c - TEST INFRASTRUCTURE (see pg_oracle.h).  Plain-C restatement of
+ * the reference's guiding-fit arithmetic.  Compiled with -ffp-contract=off so
+ * that every product and sum rounds the way the reference's SSE2 build does.
+ *
+ * Citations are to the rtx-pathtracer tree: lightpmm is vendored under
+ * external/lightpmm/include/pmm, the guiding statistics under external/guiding.
+ */
+#include "pg_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define INV_4PI_F ((float)(1.0 / (4.0 * 3.14159265358979323846)))
+#define TWO_PI_F ((float)(2.0 * 3.14159265358979323846))
+#define PMM_EPS 1.0e-8f       /* PMM_EPSILON, pmm.h:40 */
+#define VMF_MIN_KAPPA 1e-3f   /* VMF_MinKappa, VMFKernel.h:42 */
+
+static float bits_to_float(int32_t i) {
+    float f;
+    memcpy(&f, &i, sizeof f);
+    return f;
+}
+
+/* SSE2 cvtps2dq: round to nearest even, out of range or NaN -> INT32_MIN. */
+static int32_t cvt_rne(float v) {
+    if (!(v >= -2147483648.0f && v < 2147483648.0f)) return INT32_MIN;
+    return (int32_t)nearbyintf(v);
+}
+
+/* fastpow2 (pmm-vcl.h:161-176): Mineiro's rational approximation of 2^p,
+ * with the clip at -126 and truncation of the SSE2 build (INSTRSET 2). */
+static float fastpow2_f(float p) {
+    const float clipp = (-126.0f > p) ? -126.0f : p; /* _mm_max_ps(-126, p) */
+    float w;
+    {
+        /* vcl::truncate, SSE2 path: cvttps2dq, back to float, keep input on overflow */
+        if (clipp >= -2147483648.0f && clipp < 2147483648.0f)
+            w = (float)(int32_t)clipp;
+        else
+            w = clipp;
+    }
+    const float z = (clipp - w) + 1.0f;
+    const float t = ((clipp + 121.2740575f) + (27.7280233f / (4.84252568f - z))) - (1.49012907f * z);
+    return bits_to_float(cvt_rne(8388608.0f * t));
+}
+
+float pgo_fastexp(float x) { return fastpow2_f(1.442695040f * x); }
+
+/* fasttanh (pmm-vcl.h:187-222) for one lane. */
+static float fasttanh_f(float x0) {
+    const float r0 = -3.33332819422E-1f, r1 = 1.33314422036E-1f, r2 = -5.37397155531E-2f,
+                r3 = 2.06390887954E-2f, r4 = -5.70498872745E-3f;
+    const float x = fabsf(x0);
+    float y;
+    if (x <= 0.625f) {
+        const float x2 = x * x;
+        /* polynomial_4(x2, r0..r4) (vectormath_common.h:136-143), mul_add = a*b+c */
+        const float X2 = x2 * x2;
+        const float X4 = X2 * X2;
+        const float p = (r3 * x2 + r2) * X2 + ((r1 * x2 + r0) + r4 * X4);
+        y = p * (x2 * x) + x;
+    } else {
+        float e = pgo_fastexp(x + x);
+        y = 1.0f - 2.0f / (e + 1.0f);
+    }
+    if (x > 44.4f) y = 1.0f;
+    return copysignf(y, x0);
+}
+
+/* kappaToMeanCosine (VMFKernel.h:47-55) on one 4-lane group: the cheap
+ * 1 - 1/kappa form only when all four lanes exceed 5. */
+static void kappa_to_mean_cosine4(const float *kappa, float *r) {
+    int all = 1;
+    for (int i = 0; i < 4; ++i) all &= (kappa[i] > 5.0f);
+    for (int i = 0; i < 4; ++i) {
+        if (all) {
+            r[i] = 1.0f - 1.0f / kappa[i];
+        } else {
+            const float v = 1.0f / fasttanh_f(kappa[i]) - 1.0f / kappa[i];
+            r[i] = (kappa[i] > 0.0f) ? v : 0.0f;
+        }
+    }
+}
+
+void pgo_initial_mus(uint32_t num_components, float *out) {
+    /* computeUniformMus (VMMFactory.h:594-632) for l = K-1, in the reference's
+     * float arithmetic: phi is formed in double (2.0f*M_PI is a double) and
+     * stored as float; acos/sin/cos are the float functions. */
+    const float gr = 1.618033988749895f;
+    for (uint32_t n = 0; n < 16; ++n) {
+        float x = 0.0f, y = 0.0f, z = 1.0f;
+        if (n < num_components) {
+            const float phi = (float)(2.0f * M_PI * (double)((float)n / gr));
+            const float zz = 1.0f - ((2.0f * (float)n + 1.0f) / (float)num_components);
+            const float theta = acosf(zz);
+            const float st = sinf(theta);
+            x = st * cosf(phi);
+            y = st * sinf(phi);
+            z = cosf(theta);
+        }
+        out[n] = x;
+        out[16 + n] = y;
+        out[32 + n] = z;
+    }
+}
+
+/* reset of an inactive lane (VMFKernel.h:554-568) */
+static void reset_lane(pg_region_state *s, int c) {
+    s->weight[c] = 0.0f;
+    s->kappa[c] = 0.0f;
+    s->r[c] = 0.0f;
+    s->mu_x[c] = 0.0f;
+    s->mu_y[c] = 0.0f;
+    s->mu_z[c] = 1.0f;
+    s->norm[c] = INV_4PI_F;
+    s->e_min2k[c] = 1.0f;
+}
+
+static void cal_normalization_f32(pg_region_state *s, int c) {
+    /* VMFKernel::calNormalization (VMFKernel.h:620-628) */
+    const float k = s->kappa[c];
+    const float e = pgo_fastexp(-2.0f * k);
+    s->e_min2k[c] = e;
+    const float norm = k / (TWO_PI_F * (1.0f - e));
+    s->norm[c] = (k > 0.0f) ? norm : INV_4PI_F;
+}
+
+static void cal_normalization_f64(double k, double *norm, double *em2k) {
+    *em2k = exp(-2.0 * k);
+    *norm = (k > 0.0) ? k / (2.0 * M_PI * (-expm1(-2.0 * k))) : 1.0 / (4.0 * M_PI);
+}
+
+void pgo_init_states(const pg_fit_config *cfg, uint32_t n, pg_region_state *states, int exact) {
+    const uint32_t K = cfg->num_initial_components;
+    float mus[48];
+    pgo_initial_mus(K, mus);
+    for (uint32_t rg = 0; rg < n; ++rg) {
+        pg_region_state *s = &states[rg];
+        memset(s, 0, sizeof *s);
+        s->k = K;
+        const float w0 = 1.0f / (float)K;
+        float kap = cfg->init_kappa;
+        if (kap < VMF_MIN_KAPPA) kap = 0.0f;
+        for (int c = 0; c < 16; ++c) {
+            s->distance[c] = INFINITY;
+            s->dist_sum_w[c] = 0.0f;
+            if ((uint32_t)c >= K) {
+                reset_lane(s, c);
+                continue;
+            }
+            s->weight[c] = w0;
+            s->mu_x[c] = mus[c];
+            s->mu_y[c] = mus[16 + c];
+            s->mu_z[c] = mus[32 + c];
+            s->kappa[c] = kap;
+        }
+        for (int g = 0; g < 4; ++g) {
+            if ((uint32_t)(4 * g) >= K) break;
+            float kk[4] = {kap, kap, kap, kap};
+            float rr[4];
+            if (exact) {
+                for (int i = 0; i < 4; ++i) {
+                    const double kd = kap;
+                    rr[i] = kd > 0.0 ? (float)(1.0 / tanh(kd) - 1.0 / kd) : 0.0f;
+                }
+            } else {
+                kappa_to_mean_cosine4(kk, rr);
+            }
+            for (int i = 0; i < 4; ++i) {
+                const int c = 4 * g + i;
+                if ((uint32_t)c >= K) continue;
+                s->r[c] = rr[i];
+                if (exact) {
+                    double nm, em;
+                    cal_normalization_f64(kap, &nm, &em);
+                    s->norm[c] = (float)nm;
+                    s->e_min2k[c] = (float)em;
+                } else {
+                    cal_normalization_f32(s, c);
+                }
+            }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* lightpmm-faithful FP32 fit                                          */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+    float sx[16], sy[16], sz[16], w[16];
+} stats32;
+
+/* computeSufficentStatsFromSamples (VMMFactory.h:497-536) with
+ * SoftAssignmentWeights (ParametricMixtureModel.h:501-522). */
+static void estep32(const pg_region_state *s, const float *dirw, uint32_t b, uint32_t e,
+                    stats32 *st, float *sum_w, float *ll) {
+    const uint32_t K = s->k;
+    const uint32_t nk = (K + 3) / 4;
+    memset(st, 0, sizeof *st);
+    if (sum_w) *sum_w = 0.0f;
+    if (ll) *ll = 0.0f;
+    for (uint32_t n = b; n < e; ++n) {
+        const float dx = dirw[4 * (size_t)n], dy = dirw[4 * (size_t)n + 1],
+                    dz = dirw[4 * (size_t)n + 2], wt = dirw[4 * (size_t)n + 3];
+        float sa[16];
+        float part[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        for (uint32_t k = 0; k < nk; ++k) {
+            for (int i = 0; i < 4; ++i) {
+                const int c = 4 * k + i;
+                const float cs = (s->mu_x[c] * dx + s->mu_y[c] * dy) + s->mu_z[c] * dz;
+                const float tm = cs - 1.0f;
+                const float t = (tm < 0.0f) ? tm : 0.0f; /* _mm_min_ps(cos-1, 0) */
+                const float ex = pgo_fastexp(s->kappa[c] * t);
+                const float pdf = s->norm[c] * ex;
+                sa[c] = s->weight[c] * pdf;
+                part[i] = part[i] + sa[c];
+            }
+        }
+        const float mix = (part[0] + part[2]) + (part[1] + part[3]);
+        const float inv = 1.0f / mix;
+        if (!(mix > PMM_EPS)) continue;
+        for (uint32_t k = 0; k < nk; ++k)
+            for (int i = 0; i < 4; ++i) {
+                const int c = 4 * k + i;
+                const float a = sa[c] * inv;
+                const float sw = a * wt;
+                st->sx[c] = st->sx[c] + dx * sw;
+                st->sy[c] = st->sy[c] + dy * sw;
+                st->sz[c] = st->sz[c] + dz * sw;
+                st->w[c] = st->w[c] + sw;
+            }
+        if (sum_w) *sum_w = *sum_w + wt;
+        if (ll) *ll = *ll + wt * logf(mix);
+    }
+}
+
+/* parameterUpdate (VMMFactory.h:436-455) with the priors of :385-420. */
+static void mstep32(const pg_fit_config *cfg, pg_region_state *s, const stats32 *st) {
+    const uint32_t K = s->k;
+    const uint32_t nk = (K + 3) / 4;
+    float mk[4] = {cfg->max_kappa, cfg->max_kappa, cfg->max_kappa, cfg->max_kappa};
+    float maxr[4];
+    kappa_to_mean_cosine4(mk, maxr);
+    const float inv_wpn = cfg->v_prior * (float)K + 1.0f;
+    const float wpn = 1.0f / inv_wpn;
+    const float wptn = cfg->v_prior * wpn;
+    const float rptw = cfg->r_prior * cfg->r_prior_weight;
+    for (uint32_t c = 0; c < 4 * nk; ++c) {
+        const float mw = (st->w[c] / s->sample_weight) * wpn + wptn;
+        const float rl = sqrtf((st->sx[c] * st->sx[c] + st->sy[c] * st->sy[c]) + st->sz[c] * st->sz[c]);
+        float mx = s->mu_x[c], my = s->mu_y[c], mz = s->mu_z[c];
+        if (rl > 0.0f) {
+            mx = st->sx[c] / rl;
+            my = st->sy[c] / rl;
+            mz = st->sz[c] / rl;
+        }
+        const float avg = rl / st->w[c];
+        const float ns = (float)s->total_num_samples * mw;
+        float rp = (avg * ns + rptw) / (ns + cfg->r_prior_weight);
+        rp = (rp < maxr[c & 3]) ? rp : maxr[c & 3]; /* _mm_min_ps: NaN -> second operand */
+        float kap = (rp * 3.0f - ((rp * rp) * rp)) / (1.0f - rp * rp);
+        const int small = kap < VMF_MIN_KAPPA;
+        s->weight[c] = mw;
+        s->mu_x[c] = mx;
+        s->mu_y[c] = my;
+        s->mu_z[c] = mz;
+        s->kappa[c] = small ? 0.0f : kap;
+        s->r[c] = small ? 0.0f : rp;
+        cal_normalization_f32(s, (int)c);
+    }
+    /* resetInactiveComponents (VMMFactory.h:110-118) */
+    for (uint32_t c = K; c < 4 * nk; ++c) reset_lane(s, (int)c);
+}
+
+/* computeSufficentStatsFromMixture (VMMFactory.h:543-555) */
+static void stats_from_mixture32(const pg_fit_config *cfg, const pg_region_state *s, stats32 *st) {
+    const uint32_t K = s->k;
+    const uint32_t nk = (K + 3) / 4;
+    const float inv_wpn = cfg->v_prior * (float)K + 1.0f;
+    const float wpn = 1.0f / inv_wpn;
+    const float wptn = cfg->v_prior * wpn;
+    const float rptw = cfg->r_prior * cfg->r_prior_weight;
+    memset(st, 0, sizeof *st);
+    for (uint32_t c = 0; c < 4 * nk; ++c) {
+        const float w = s->weight[c];
+        const float wnp = (w > wptn) ? (w - wptn) * inv_wpn : 0.0f;
+        const float sw = wnp * s->sample_weight;
+        const float n = (float)s->total_num_samples * w;
+        const float rr = (s->r[c] * (n + cfg->r_prior_weight) - rptw) / n;
+        const float f = rr * sw;
+        st->w[c] = sw;
+        st->sx[c] = s->mu_x[c] * f;
+        st->sy[c] = s->mu_y[c] * f;
+        st->sz[c] = s->mu_z[c] * f;
+    }
+}
+
+static void fit_region32(const pg_fit_config *cfg, int mode, const float *dirw, uint32_t b,
+                         uint32_t e, pg_region_state *s, float *ll_final) {
+    if (mode == PG_FIT_INIT) pgo_init_states(cfg, 1, s, 0);
+    const uint32_t K = s->k;
+    const uint32_t nk = (K + 3) / 4;
+    for (uint32_t c = K; c < 4 * nk; ++c) reset_lane(s, (int)c);
+    stats32 old;
+    const int update = (mode == PG_FIT_UPDATE);
+    if (update) stats_from_mixture32(cfg, s, &old);
+    const uint32_t N = e - b;
+    const uint32_t max_itr = (N > 2 * K) ? cfg->max_itr : 0;
+    float sum_w = 0.0f, ll = 0.0f, last_ll = 0.0f, abs_inv_last = 0.0f;
+    uint32_t i = 0;
+    for (; i < max_itr; ++i) {
+        stats32 st;
+        estep32(s, dirw, b, e, &st, i == 0 ? &sum_w : NULL, i >= cfg->min_itr ? &ll : NULL);
+        if (i == 0) {
+            if (update) {
+                s->sample_weight += sum_w;
+                s->num_samples += (float)N;
+                s->total_num_samples += N;
+            } else {
+                s->sample_weight = sum_w;
+                s->num_samples = (float)N;
+                s->total_num_samples = N;
+            }
+        }
+        if (update)
+            for (int c = 0; c < 16; ++c) {
+                st.sx[c] = old.sx[c] + st.sx[c];
+                st.sy[c] = old.sy[c] + st.sy[c];
+                st.sz[c] = old.sz[c] + st.sz[c];
+                st.w[c] = old.w[c] + st.w[c];
+            }
+        mstep32(cfg, s, &st);
+        if (i >= cfg->min_itr) {
+            if (i > cfg->min_itr) {
+                const float rel = (ll - last_ll) * abs_inv_last;
+                if (rel < cfg->rel_ll_threshold) break;
+            }
+            last_ll = ll;
+            abs_inv_last = 1.0f / fabsf(ll);
+        }
+    }
+    s->num_em_iterations += i;
+    s->iters_last = i;
+    s->ll_last = ll;
+    s->flags |= PG_STATE_FITTED;
+    if (ll_final) {
+        stats32 st;
+        float l = 0.0f;
+        if (e > b) estep32(s, dirw, b, e, &st, NULL, &l);
+        *ll_final = l;
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* FP64 fit                                                            */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+    double sx[16], sy[16], sz[16], w[16];
+} stats64;
+
+typedef struct {
+    double w[16], mx[16], my[16], mz[16], kappa[16], r[16], norm[16];
+    double sample_weight;
+} mix64;
+
+static void load64(const pg_region_state *s, mix64 *m) {
+    for (int c = 0; c < 16; ++c) {
+        m->w[c] = s->weight[c];
+        m->mx[c] = s->mu_x[c];
+        m->my[c] = s->mu_y[c];
+        m->mz[c] = s->mu_z[c];
+        m->kappa[c] = s->kappa[c];
+        m->r[c] = s->r[c];
+        m->norm[c] = s->norm[c];
+    }
+    m->sample_weight = s->sample_weight;
+}
+
+static void estep64(const mix64 *m, uint32_t K, const float *dirw, uint32_t b, uint32_t e,
+                    stats64 *st, double *sum_w, double *ll) {
+    memset(st, 0, sizeof *st);
+    if (sum_w) *sum_w = 0.0;
+    if (ll) *ll = 0.0;
+    for (uint32_t n = b; n < e; ++n) {
+        const double dx = dirw[4 * (size_t)n], dy = dirw[4 * (size_t)n + 1],
+                     dz = dirw[4 * (size_t)n + 2], wt = dirw[4 * (size_t)n + 3];
+        double v[16];
+        double p = 0.0;
+        for (uint32_t c = 0; c < K; ++c) {
+            double cs = m->mx[c] * dx + m->my[c] * dy + m->mz[c] * dz;
+            double t = cs - 1.0;
+            if (t > 0.0) t = 0.0;
+            v[c] = m->w[c] * m->norm[c] * exp(m->kappa[c] * t);
+            p += v[c];
+        }
+        if (!(p > (double)PMM_EPS)) continue;
+        const double sc = wt / p;
+        for (uint32_t c = 0; c < K; ++c) {
+            const double g = v[c] * sc;
+            st->sx[c] += g * dx;
+            st->sy[c] += g * dy;
+            st->sz[c] += g * dz;
+            st->w[c] += g;
+        }
+        if (sum_w) *sum_w += wt;
+        if (ll) *ll += wt * log(p);
+    }
+}
+
+static void mstep64(const pg_fit_config *cfg, mix64 *m, uint32_t K, double total, const stats64 *st) {
+    const double maxk = cfg->max_kappa;
+    const double maxr = maxk > 0.0 ? 1.0 / tanh(maxk) - 1.0 / maxk : 0.0;
+    const double inv_wpn = (double)cfg->v_prior * K + 1.0;
+    const double wpn = 1.0 / inv_wpn;
+    const double wptn = cfg->v_prior * wpn;
+    const double rptw = (double)cfg->r_prior * cfg->r_prior_weight;
+    for (uint32_t c = 0; c < K; ++c) {
+        const double mw = (st->w[c] / m->sample_weight) * wpn + wptn;
+        const double rl = sqrt(st->sx[c] * st->sx[c] + st->sy[c] * st->sy[c] + st->sz[c] * st->sz[c]);
+        if (rl > 0.0) {
+            m->mx[c] = st->sx[c] / rl;
+            m->my[c] = st->sy[c] / rl;
+            m->mz[c] = st->sz[c] / rl;
+        }
+        const double avg = rl / st->w[c];
+        const double ns = total * mw;
+        double rp = (avg * ns + rptw) / (ns + cfg->r_prior_weight);
+        if (!(rp < maxr)) rp = maxr; /* min with NaN taking the bound */
+        const double kap = (3.0 * rp - rp * rp * rp) / (1.0 - rp * rp);
+        const int small = kap < (double)VMF_MIN_KAPPA;
+        m->w[c] = mw;
+        m->kappa[c] = small ? 0.0 : kap;
+        m->r[c] = small ? 0.0 : rp;
+        double em;
+        cal_normalization_f64(m->kappa[c], &m->norm[c], &em);
+    }
+}
+
+static void fit_region64(const pg_fit_config *cfg, int mode, const float *dirw, uint32_t b,
+                         uint32_t e, pg_region_state *s, double *ll_final) {
+    if (mode == PG_FIT_INIT) pgo_init_states(cfg, 1, s, 1);
+    const uint32_t K = s->k;
+    for (uint32_t c = K; c < 16; ++c) reset_lane(s, (int)c);
+    mix64 m;
+    load64(s, &m);
+    const int update = (mode == PG_FIT_UPDATE);
+    stats64 old;
+    memset(&old, 0, sizeof old);
+    double total = (double)s->total_num_samples;
+    if (update) {
+        const double inv_wpn = (double)cfg->v_prior * K + 1.0;
+        const double wptn = cfg->v_prior / inv_wpn;
+        const double rptw = (double)cfg->r_prior * cfg->r_prior_weight;
+        for (uint32_t c = 0; c < K; ++c) {
+            const double w = m.w[c];
+            const double sw = (w > wptn ? (w - wptn) * inv_wpn : 0.0) * m.sample_weight;
+            const double n = total * w;
+            const double rr = (m.r[c] * (n + cfg->r_prior_weight) - rptw) / n;
+            old.w[c] = sw;
+            old.sx[c] = m.mx[c] * rr * sw;
+            old.sy[c] = m.my[c] * rr * sw;
+            old.sz[c] = m.mz[c] * rr * sw;
+        }
+    }
+    const uint32_t N = e - b;
+    const uint32_t max_itr = (N > 2 * K) ? cfg->max_itr : 0;
+    double sum_w = 0.0, ll = 0.0, last_ll = 0.0, abs_inv_last = 0.0;
+    double num_samples = s->num_samples;
+    uint32_t i = 0;
+    for (; i < max_itr; ++i) {
+        stats64 st;
+        estep64(&m, K, dirw, b, e, &st, i == 0 ? &sum_w : NULL, i >= cfg->min_itr ? &ll : NULL);
+        if (i == 0) {
+            if (update) {
+                m.sample_weight += sum_w;
+                num_samples += N;
+                total += N;
+            } else {
+                m.sample_weight = sum_w;
+                num_samples = N;
+                total = N;
+            }
+        }
+        if (update)
+            for (uint32_t c = 0; c < K; ++c) {
+                st.sx[c] += old.sx[c];
+                st.sy[c] += old.sy[c];
+                st.sz[c] += old.sz[c];
+                st.w[c] += old.w[c];
+            }
+        mstep64(cfg, &m, K, total, &st);
+        if (i >= cfg->min_itr) {
+            if (i > cfg->min_itr) {
+                const double rel = (ll - last_ll) * abs_inv_last;
+                if (rel < (double)cfg->rel_ll_threshold) break;
+            }
+            last_ll = ll;
+            abs_inv_last = 1.0 / fabs(ll);
+        }
+    }
+    for (uint32_t c = 0; c < K; ++c) {
+        s->weight[c] = (float)m.w[c];
+        s->mu_x[c] = (float)m.mx[c];
+        s->mu_y[c] = (float)m.my[c];
+        s->mu_z[c] = (float)m.mz[c];
+        s->kappa[c] = (float)m.kappa[c];
+        s->r[c] = (float)m.r[c];
+        double nm, em;
+        cal_normalization_f64(m.kappa[c], &nm, &em);
+        s->norm[c] = (float)nm;
+        s->e_min2k[c] = (float)em;
+    }
+    s->sample_weight = (float)m.sample_weight;
+    s->num_samples = (float)num_samples;
+    s->total_num_samples = (uint64_t)total;
+    s->num_em_iterations += i;
+    s->iters_last = i;
+    s->ll_last = (float)ll;
+    s->flags |= PG_STATE_FITTED;
+    if (ll_final) {
+        stats64 st;
+        double l = 0.0;
+        if (e > b) estep64(&m, K, dirw, b, e, &st, NULL, &l);
+        *ll_final = l;
+    }
+}
+
+void pgo_eval_ll_f64(uint32_t n_regions, const float *dirw, const uint32_t *offsets,
+                     const pg_region_state *states, double *ll_out) {
+    for (uint32_t r = 0; r < n_regions; ++r) {
+        mix64 m;
+        load64(&states[r], &m);
+        stats64 st;
+        double l = 0.0;
+        estep64(&m, states[r].k, dirw, offsets[r], offsets[r + 1], &st, NULL, &l);
+        ll_out[r] = l;
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* Region-parallel driver                                              */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+    const pg_fit_config *cfg;
+    int mode;
+    uint32_t n_regions;
+    const float *dirw;
+    const uint32_t *offsets;
+    pg_region_state *states;
+    float *ll32;
+    double *ll64;
+    int f64;
+    uint32_t next; /* atomic */
+} job_t;
+
+static void *worker(void *arg) {
+    job_t *j = (job_t *)arg;
+    for (;;) {
+        const uint32_t r = __atomic_fetch_add(&j->next, 1u, __ATOMIC_RELAXED);
+        if (r >= j->n_regions) break;
+        if (j->f64)
+            fit_region64(j->cfg, j->mode, j->dirw, j->offsets[r], j->offsets[r + 1], &j->states[r],
+                         j->ll64 ? &j->ll64[r] : NULL);
+        else
+            fit_region32(j->cfg, j->mode, j->dirw, j->offsets[r], j->offsets[r + 1], &j->states[r],
+                         j->ll32 ? &j->ll32[r] : NULL);
+    }
+    return NULL;
+}
+
+static int run_job(job_t *j, int n_threads) {
+    if (n_threads <= 1) {
+        worker(j);
+        return 0;
+    }
+    if (n_threads > 256) n_threads = 256;
+    pthread_t th[256];
+    int started = 0;
+    for (int t = 0; t < n_threads; ++t)
+        if (pthread_create(&th[t], NULL, worker, j) == 0) ++started;
+    if (started == 0) worker(j);
+    for (int t = 0; t < started; ++t) pthread_join(th[t], NULL);
+    return 0;
+}
+
+int pgo_fit_lpmm32(const pg_fit_config *cfg, int mode, uint32_t n_regions, const float *dirw,
+                   const uint32_t *offsets, pg_region_state *states, float *ll_final, int n_threads) {
+    job_t j = {cfg, mode, n_regions, dirw, offsets, states, ll_final, NULL, 0, 0};
+    return run_job(&j, n_threads);
+}
+
+int pgo_fit_f64(const pg_fit_config *cfg, int mode, uint32_t n_regions, const float *dirw,
+                const uint32_t *offsets, pg_region_state *states, double *ll_final, int n_threads) {
+    job_t j = {cfg, mode, n_regions, dirw, offsets, states, NULL, ll_final, 1, 0};
+    return run_job(&j, n_threads);
+}
+
+/* ------------------------------------------------------------------ */
+/* Parallax, distances, packing, regions, sort                         */
+/* ------------------------------------------------------------------ */
+
+void pgo_prefit_parallax(uint32_t n_regions, const pg_directional_data *sorted,
+                         const uint32_t *offsets, const float *means, float *dirw_out,
+                         float *dist_out) {
+    for (uint32_t r = 0; r < n_regions; ++r) {
+        const float *m = means + 3 * (size_t)r;
+        for (uint32_t i = offsets[r]; i < offsets[r + 1]; ++i) {
+            const pg_directional_data *d = &sorted[i];
+            float dx = d->direction[0], dy = d->direction[1], dz = d->direction[2];
+            float dist;
+            if (d->distance > 0.0f) {
+                /* pos + distance*direction - parallaxMean, then glm::normalize / length */
+                const float nx = (d->position[0] + d->distance * dx) - m[0];
+                const float ny = (d->position[1] + d->distance * dy) - m[1];
+                const float nz = (d->position[2] + d->distance * dz) - m[2];
+                const float l2 = (nx * nx + ny * ny) + nz * nz;
+                const float inv = 1.0f / sqrtf(l2);
+                dx = nx * inv;
+                dy = ny * inv;
+                dz = nz * inv;
+                dist = sqrtf(l2);
+            } else {
+                dist = INFINITY;
+            }
+            dirw_out[4 * (size_t)i] = dx;
+            dirw_out[4 * (size_t)i + 1] = dy;
+            dirw_out[4 * (size_t)i + 2] = dz;
+            dirw_out[4 * (size_t)i + 3] = d->weight;
+            dist_out[i] = dist;
+        }
+    }
+}
+
+void pgo_update_distances(uint32_t n_regions, const float *dirw, const float *dist,
+                          const uint32_t *offsets, pg_region_state *states) {
+    for (uint32_t r = 0; r < n_regions; ++r) {
+        pg_region_state *s = &states[r];
+        const uint32_t K = s->k;
+        double bw[16] = {0}, bwd[16] = {0};
+        for (uint32_t i = offsets[r]; i < offsets[r + 1]; ++i) {
+            const double t_n = dist[i];
+            if (!(t_n > 0.0)) continue;
+            const double dx = dirw[4 * (size_t)i], dy = dirw[4 * (size_t)i + 1],
+                         dz = dirw[4 * (size_t)i + 2], wt = dirw[4 * (size_t)i + 3];
+            double pdf[16], v[16], p = 0.0;
+            for (uint32_t c = 0; c < K; ++c) {
+                double t = s->mu_x[c] * dx + s->mu_y[c] * dy + s->mu_z[c] * dz - 1.0;
+                if (t > 0.0) t = 0.0;
+                pdf[c] = s->norm[c] * exp((double)s->kappa[c] * t);
+                v[c] = s->weight[c] * pdf[c];
+                p += v[c];
+            }
+            if (!(p > (double)PMM_EPS)) continue;
+            const double sc = wt / p;
+            for (uint32_t c = 0; c < K; ++c) {
+                const double a = v[c] * pdf[c] * sc;
+                bw[c] += a;
+                bwd[c] += a / t_n;
+            }
+        }
+        for (uint32_t c = 0; c < K; ++c) {
+            const float nw = (float)((double)s->dist_sum_w[c] + bw[c]);
+            const float den = (float)((double)s->dist_sum_w[c] / (double)s->distance[c] + bwd[c]);
+            s->distance[c] = nw / den;
+            s->dist_sum_w[c] = nw;
+        }
+    }
+}
+
+void pgo_reposition(pg_region_state *s, const float d[3]) {
+    for (uint32_t c = 0; c < s->k; ++c) {
+        const int invalid = isinf(s->distance[c]) || s->dist_sum_w[c] <= 0.0f;
+        if (invalid) continue;
+        const float x = s->mu_x[c] * s->distance[c] + d[0];
+        const float y = s->mu_y[c] * s->distance[c] + d[1];
+        const float z = s->mu_z[c] * s->distance[c] + d[2];
+        const float l = sqrtf((x * x + y * y) + z * z);
+        s->distance[c] = l;
+        s->mu_x[c] = x / l;
+        s->mu_y[c] = y / l;
+        s->mu_z[c] = z / l;
+    }
+}
+
+void pgo_pack_vmm_theta(uint32_t n_regions, const pg_region_state *states, int use_parallax,
+                        pg_vmm_theta *out) {
+    for (uint32_t r = 0; r < n_regions; ++r) {
+        const pg_region_state *s = &states[r];
+        pg_vmm_theta *v = &out[r];
+        memset(v, 0, sizeof *v);
+        for (int c = 0; c < 16; ++c) v->thetas[c].distance = -1.0f;
+        v->used_distributions = (int32_t)s->k;
+        for (uint32_t c = 0; c < s->k; ++c) {
+            v->pi[c] = s->weight[c];
+            v->thetas[c].mu[0] = s->mu_x[c];
+            v->thetas[c].mu[1] = s->mu_y[c];
+            v->thetas[c].mu[2] = s->mu_z[c];
+            /* VMF_Theta::setK (src/PathGuiding.h:44-50), evaluated in double */
+            float k = s->kappa[c];
+            k = k < VMF_MIN_KAPPA ? 0.0f : k;
+            v->thetas[c].k = k;
+            v->thetas[c].norm = (float)((double)k / (2.0 * M_PI * (1.0 - exp(-2.0 * (double)k))));
+            v->thetas[c].e_min2k = (float)exp(-2.0 * (double)k);
+        }
+        if (use_parallax) {
+            for (int i = 0; i < 3; ++i) v->mean_position[i] = s->parallax_mean[i];
+            for (int c = 0; c < 16; ++c) {
+                float dd = s->distance[c];
+                dd = (dd == INFINITY) ? -1.0f : dd;
+                v->thetas[c].distance = dd;
+                for (int i = 0; i < 3; ++i) {
+                    const float mu = v->thetas[c].mu[i];
+                    v->thetas[c].target[i] = s->parallax_mean[i] + dd * mu;
+                }
+            }
+        }
+    }
+}
+
+void pgo_region_aabbs(uint32_t split_count, const float a[6], float *out) {
+    /* Aabb::addEpsilon (src/Shapes.h:48-53) */
+    float mn[3], mx[3];
+    for (int i = 0; i < 3; ++i) {
+        const float ext = a[3 + i] - a[i];
+        const float cen = a[i] + 0.5f * ext;
+        mn[i] = cen - 0.50001f * ext;
+        mx[i] = cen + 0.50001f * ext;
+    }
+    const uint32_t n = 1u << split_count;
+    float *cur = (float *)malloc(sizeof(float) * 6 * n);
+    float *nxt = (float *)malloc(sizeof(float) * 6 * n);
+    for (int i = 0; i < 3; ++i) {
+        cur[i] = mn[i];
+        cur[3 + i] = mx[i];
+    }
+    uint32_t count = 1;
+    for (uint32_t s = 0; s < split_count; ++s) {
+        for (uint32_t b = 0; b < count; ++b) {
+            const float *bx = cur + 6 * b;
+            float size[3];
+            for (int i = 0; i < 3; ++i) size[i] = bx[3 + i] - bx[i];
+            const int axis = size[0] > size[1] ? (size[0] > size[2] ? 0 : 2) : (size[1] > size[2] ? 1 : 2);
+            float *L = nxt + 6 * (2 * b), *R = nxt + 6 * (2 * b + 1);
+            memcpy(L, bx, sizeof(float) * 6);
+            memcpy(R, bx, sizeof(float) * 6);
+            L[3 + axis] -= 0.5f * size[axis];
+            R[axis] += 0.5f * size[axis];
+        }
+        count *= 2;
+        float *t = cur;
+        cur = nxt;
+        nxt = t;
+    }
+    memcpy(out, cur, sizeof(float) * 6 * n);
+    free(cur);
+    free(nxt);
+}
+
+uint64_t pgo_sort_samples(const pg_directional_data *rec, uint64_t n, uint32_t n_regions,
+                          pg_directional_data *sorted, uint32_t *offsets) {
+    memset(offsets, 0, sizeof(uint32_t) * (n_regions + 1));
+    for (uint64_t i = 0; i < n; ++i)
+        if (rec[i].flags < n_regions) offsets[rec[i].flags + 1]++;
+    for (uint32_t r = 0; r < n_regions; ++r) offsets[r + 1] += offsets[r];
+    uint32_t *cursor = (uint32_t *)malloc(sizeof(uint32_t) * (n_regions + 1));
+    memcpy(cursor, offsets, sizeof(uint32_t) * (n_regions + 1));
+    for (uint64_t i = 0; i < n; ++i)
+        if (rec[i].flags < n_regions) sorted[cursor[rec[i].flags]++] = rec[i];
+    free(cursor);
+    return offsets[n_regions];
+}
