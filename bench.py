@@ -1,0 +1,307 @@
+"""Benchmark of the path-guiding hot path on one GB300.
+
+Workload (the batched uneven guiding fit): 4096 regions, per-region sample
+counts lognormal (median 2048, sigma 1.0, clipped to 64..262144), samples
+drawn from seeded 1-6-lobe vMF mixtures (kappa log-uniform 2..2000), weights
+lognormal(0, 1.5); each region is fitted with a 16-component vMF mixture by 20
+EM iterations.  A step is one batched fit of all regions (pg_fit_regions).
+The sample set (~13.8 M samples, 221 MB of float4) is larger than L2, so no
+flush is needed between steps.
+
+Metric: EM sample-iterations per second (whole job).  `e2e` is the same metric
+through the public API with host buffers: every step copies the step's samples
+and offsets host->device from pinned memory and reads the fitted region states
+back.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "EM samples/s (sample-iterations per second, batched uneven guiding fit)"
+UNIT = "Msample-iter/s"
+ITERS = 20
+K = 16
+WORKLOAD = ("batched uneven guiding fit: 4096 regions, lognormal counts (median 2048, sigma 1.0, "
+            "clip 64-262144), 1-6 lobe vMF mixtures kappa 2-2000, weights lognormal(0,1.5), "
+            "K=16, 20 EM iterations")
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        try:
+            for line in Path(self.path).read_text().splitlines():
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx.append(float(f[2]))
+                except ValueError:
+                    continue
+                for name, val in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                                      "sw_power_cap"), f[5:9]):
+                    if val.lower() == "active":
+                        reasons.add(name)
+        except Exception:
+            pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload(small: bool):
+    import __graft_entry__ as entry
+    wl = entry.load_submodule("workloads")
+    if small:
+        return wl.fit_batched(seed=3, n_regions=512)
+    return wl.fit_batched(seed=3)
+
+
+def cpu_baseline(w, seconds: float = 12.0, threads: int | None = None):
+    """The reference's CPU fit (bit-exact C restatement of lightpmm, oracle/)
+    on a bounded sample of the workload's regions, over `threads` host threads."""
+    from oracle.oracle import Oracle, abi
+    o = Oracle()
+    threads = threads or (os.cpu_count() or 1)
+    offsets = w["offsets"].astype(np.int64)
+    counts = np.diff(offsets)
+    cfg = abi.forced_iterations(ITERS, num_initial_components=K)
+    # calibrate on a small prefix, then run a sample sized for ~`seconds`
+    n_try = 64
+    t0 = time.perf_counter()
+    sub = slice(0, n_try)
+    o.fit(cfg, w["dirw"][offsets[0]:offsets[n_try]], (offsets[:n_try + 1] - offsets[0]).astype(np.uint32),
+          f64=False, threads=threads)
+    dt = time.perf_counter() - t0
+    rate = counts[sub].sum() * ITERS / max(dt, 1e-6)
+    target = rate * seconds / ITERS
+    n = int(np.searchsorted(np.cumsum(counts), target)) + 1
+    n = max(n_try, min(n, len(counts)))
+    t0 = time.perf_counter()
+    o.fit(cfg, w["dirw"][:offsets[n]], offsets[:n + 1].astype(np.uint32), f64=False, threads=threads)
+    dt = time.perf_counter() - t0
+    si = counts[:n].sum() * ITERS
+    return {"value": si / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {n} of {len(counts)} regions ({int(counts[:n].sum())} samples), {ITERS} iterations",
+            "seconds": dt}
+
+
+def traffic_per_launch():
+    p = ROOT / "profiles" / "em_fit_traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            return None
+    return None
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    w = make_workload(args.small)
+    times = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(w, seconds=args.ref_seconds)
+        if i >= args.warmup:
+            times.append(r)
+    v = float(np.median([t["value"] for t in times]))
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": float(np.median([t["seconds"] for t in times]) * 1e3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded vMF mixtures)", "impl": "reference",
+            "config": {"workload": WORKLOAD, "sample": times[-1]["sample"]},
+            "cpu_baseline": {k: times[-1][k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line["cpu_baseline"]["value"] = v
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--small", action="store_true", help="512-region case (for ncu captures)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-seconds", type=float, default=None,
+                    help="CPU seconds per reference step (default: ~100 s over the whole run)")
+    args = ap.parse_args()
+    if args.ref_seconds is None:
+        args.ref_seconds = max(2.0, min(12.0, 100.0 / max(1, args.steps + args.warmup)))
+    args.warmup = max(args.warmup, 0)
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    import __graft_entry__ as entry
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    pkg = entry.load_package()
+    abi = pkg.abi
+    w = make_workload(args.small)
+    R = len(w["offsets"]) - 1
+    counts = np.diff(w["offsets"].astype(np.int64))
+    n_samples = int(counts.sum())
+    cfg = abi.forced_iterations(ITERS, num_initial_components=K)
+    ctx = pkg.FitContext(cfg, max_regions=R)
+    stream = torch.cuda.Stream()
+    dirw_h = torch.from_numpy(w["dirw"]).pin_memory()
+    offs_h = torch.from_numpy(w["offsets"].view(np.int32)).pin_memory()
+    dirw_d = dirw_h.to("cuda", non_blocking=False)
+    offs_d = offs_h.to("cuda", non_blocking=False)
+    fitted = counts > 2 * K
+    si_per_step = int(counts[fitted].sum()) * ITERS  # regions with N <= 2K are not fitted
+
+    def step():
+        ctx.fit(dirw_d, offs_d, R, abi.PG_FIT_INIT, stream=stream)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    torch.cuda.synchronize()
+    ctx.sync(stream)
+    launches = ctx.last_launch_count()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sampler = ClockSampler(local)
+    barrier()
+    with sampler:
+        time.sleep(0.3)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        barrier()
+    ms = ev0.elapsed_time(ev1) / max(args.steps, 1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = si_per_step * world / (ms * 1e-3) / 1e6
+
+    # e2e through the public API: H2D of the step's inputs, fit, D2H of the states
+    h2d = dirw_h.numel() * 4 + offs_h.numel() * 4
+    d2h = R * abi.STATE_DTYPE.itemsize
+    with torch.cuda.stream(stream):
+        for _ in range(max(1, args.warmup)):
+            dirw_d.copy_(dirw_h, non_blocking=True)
+            offs_d.copy_(offs_h, non_blocking=True)
+            ctx.fit(dirw_d, offs_d, R, abi.PG_FIT_INIT, stream=stream)
+            ctx.states(R, stream=stream)
+    torch.cuda.synchronize()
+    e2e_steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for _ in range(e2e_steps):
+            dirw_d.copy_(dirw_h, non_blocking=True)
+            offs_d.copy_(offs_h, non_blocking=True)
+            ctx.fit(dirw_d, offs_d, R, abi.PG_FIT_INIT, stream=stream)
+            ctx.states(R, stream=stream)  # D2H of the fitted states + stream sync
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+    e2e_value = si_per_step * world / (e2e_ms * 1e-3) / 1e6
+
+    hbm, peak_src = measured_peaks()
+    alg_bytes = 16.0 * si_per_step
+    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    tr = traffic_per_launch()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": (tr or {}).get("bytes_per_launch"),
+                "peak_source": peak_src,
+                "algorithmic_bytes_per_launch": alg_bytes}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded vMF mixtures)",
+            "config": {"workload": WORKLOAD if not args.small else "512-region case of: " + WORKLOAD,
+                       "regions": R, "samples": n_samples, "em_iterations": ITERS, "components": K,
+                       "l2": "inputs larger than L2 (221 MB of float4 samples), no flush",
+                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+            "gpu_launches": launches * args.steps,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": roofline, "clocks": sampler.summary()}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = {k: v for k, v in cpu_baseline(w).items() if k != "seconds"}
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -204,6 +204,12 @@ typedef struct pg_fit_tuning {
 int pg_set_fit_tuning(pg_ctx *ctx, const pg_fit_tuning *t);
 int pg_get_fit_tuning(const pg_ctx *ctx, pg_fit_tuning *t);
 
+/* Synchronises `stream` and reports errors recorded by device code since the
+ * last pg_fit_regions: PG_ERR_TIMEOUT (a bounded wait ran out),
+ * PG_ERR_NUMERIC (a fit produced a non-finite parameter, e.g. from corrupt
+ * samples; the region's state carries PG_STATE_NONFINITE). */
+int pg_sync_status(pg_ctx *ctx, void *stream);
+
 /* Device kernels launched by the last pg_fit_regions call (for counting
  * launches in benchmarks). */
 int pg_last_launch_count(const pg_ctx *ctx, uint32_t *count);

@@ -6,7 +6,6 @@ legs import this module, and only as the checker or the timed CPU baseline.
 from __future__ import annotations
 
 import ctypes as C
-import importlib.util
 import os
 from pathlib import Path
 
@@ -17,10 +16,12 @@ ROOT = HERE.parent
 
 
 def _load_abi():
-    spec = importlib.util.spec_from_file_location("_pg_abi", ROOT / "rtx-pathtracer_gb300" / "abi.py")
-    mod = importlib.util.module_from_spec(spec)
-    spec.loader.exec_module(mod)
-    return mod
+    """The package's own abi module, so ctypes structures are shared with it."""
+    import sys
+    if str(ROOT) not in sys.path:
+        sys.path.insert(0, str(ROOT))
+    import __graft_entry__ as entry
+    return entry.load_package().abi
 
 
 abi = _load_abi()

@@ -1,0 +1,163 @@
+"""GB300 path-guiding library: Python mirror of the C ABI (include/pathguide.h).
+
+The compute lives in libpathguide.so (hand-written sm_103a CUDA kernels behind
+a C ABI).  This module only declares the ABI for ctypes and wraps device
+pointers; there is no Python or CPU fallback - if the shared library is
+missing, importing the bindings raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import abi
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "libpathguide.so"
+
+_P = C.c_void_p
+_U32 = C.c_uint32
+_U64 = C.c_uint64
+_I = C.c_int
+
+
+class PathGuideError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{status_string(status)}: {message}")
+        self.status = status
+
+
+# name -> (restype, argtypes); one entry per function declared in include/*.h
+SIGNATURES = {
+    "pg_default_fit_config": (None, [C.POINTER(abi.FitConfig)]),
+    "pg_ctx_create": (_I, [C.POINTER(abi.FitConfig), _U32, _U64, C.POINTER(_P)]),
+    "pg_ctx_destroy": (_I, [_P]),
+    "pg_last_error": (C.c_char_p, [_P]),
+    "pg_status_string": (C.c_char_p, [_I]),
+    "pg_get_fit_config": (_I, [_P, C.POINTER(abi.FitConfig)]),
+    "pg_set_fit_config": (_I, [_P, C.POINTER(abi.FitConfig)]),
+    "pg_init_regions": (_I, [_P, _U32, _P]),
+    "pg_get_region_states": (_I, [_P, _P, _U32, _U32, _P]),
+    "pg_set_region_states": (_I, [_P, _P, _U32, _U32, _P]),
+    "pg_region_states_device": (_I, [_P, C.POINTER(_P)]),
+    "pg_fit_regions": (_I, [_P, _P, _P, _U32, _I, _P]),
+    "pg_eval_loglik": (_I, [_P, _P, _P, _U32, _P, _P]),
+    "pg_set_fit_tuning": (_I, [_P, C.POINTER(abi.FitTuning)]),
+    "pg_get_fit_tuning": (_I, [_P, C.POINTER(abi.FitTuning)]),
+    "pg_sync_status": (_I, [_P, _P]),
+    "pg_last_launch_count": (_I, [_P, C.POINTER(_U32)]),
+}
+
+_LIB = None
+
+
+def library() -> C.CDLL:
+    """Loads libpathguide.so (raises if it has not been built)."""
+    global _LIB
+    if _LIB is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with __graft_entry__.build()")
+        lib = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            if hasattr(lib, name):
+                f = getattr(lib, name)
+                f.restype = res
+                f.argtypes = args
+        _LIB = lib
+    return _LIB
+
+
+def status_string(status: int) -> str:
+    try:
+        return library().pg_status_string(status).decode()
+    except Exception:  # library not loadable: still report the number
+        return f"status {status}"
+
+
+def _stream_handle(stream) -> int:
+    if stream is None:
+        return 0
+    if isinstance(stream, int):
+        return stream
+    return int(getattr(stream, "cuda_stream", stream))
+
+
+def _dptr(x) -> int:
+    """Device address of a torch tensor (or an int address)."""
+    if isinstance(x, int):
+        return x
+    return int(x.data_ptr())
+
+
+class FitContext:
+    """A pg_ctx: per-region mixture states and the batched EM fit on one GPU."""
+
+    def __init__(self, cfg: abi.FitConfig | None = None, max_regions: int = 4096, max_samples: int = 0):
+        self.lib = library()
+        self.cfg = cfg if cfg is not None else abi.default_fit_config()
+        h = C.c_void_p()
+        st = self.lib.pg_ctx_create(C.byref(self.cfg), max_regions, max_samples, C.byref(h))
+        if st != abi.PG_OK:
+            raise PathGuideError(st, self.lib.pg_last_error(None).decode())
+        self.h = h
+        self.max_regions = max_regions
+
+    def _check(self, st: int):
+        if st != abi.PG_OK:
+            raise PathGuideError(st, self.lib.pg_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_config(self, cfg: abi.FitConfig):
+        self._check(self.lib.pg_set_fit_config(self.h, C.byref(cfg)))
+        self.cfg = cfg
+
+    def set_tuning(self, threads_per_cta=0, smem_samples=0, ctas_per_sm=0):
+        t = abi.FitTuning(threads_per_cta, smem_samples, ctas_per_sm, 0)
+        self._check(self.lib.pg_set_fit_tuning(self.h, C.byref(t)))
+
+    def init_regions(self, n_regions: int, stream=None):
+        self._check(self.lib.pg_init_regions(self.h, n_regions, _stream_handle(stream)))
+
+    def fit(self, dirw, offsets, n_regions: int, mode: int = abi.PG_FIT_INIT, stream=None):
+        """Fits regions [0, n_regions).  dirw: device float4 per sample; offsets: device uint32 (n+1)."""
+        self._check(self.lib.pg_fit_regions(self.h, _dptr(dirw), _dptr(offsets), n_regions, mode,
+                                            _stream_handle(stream)))
+
+    def eval_loglik(self, dirw, offsets, n_regions: int, ll_out, stream=None):
+        self._check(self.lib.pg_eval_loglik(self.h, _dptr(dirw), _dptr(offsets), n_regions, _dptr(ll_out),
+                                            _stream_handle(stream)))
+
+    def sync(self, stream=None):
+        self._check(self.lib.pg_sync_status(self.h, _stream_handle(stream)))
+
+    def states(self, n: int, first: int = 0, stream=None) -> np.ndarray:
+        out = np.zeros(n, dtype=abi.STATE_DTYPE)
+        self._check(self.lib.pg_get_region_states(self.h, out.ctypes.data, first, n, _stream_handle(stream)))
+        return out
+
+    def set_states(self, states: np.ndarray, first: int = 0, stream=None):
+        s = np.ascontiguousarray(states, dtype=abi.STATE_DTYPE)
+        self._check(self.lib.pg_set_region_states(self.h, s.ctypes.data, first, s.shape[0],
+                                                  _stream_handle(stream)))
+
+    def states_device_ptr(self) -> int:
+        p = C.c_void_p()
+        self._check(self.lib.pg_region_states_device(self.h, C.byref(p)))
+        return int(p.value or 0)
+
+    def last_launch_count(self) -> int:
+        n = C.c_uint32()
+        self._check(self.lib.pg_last_launch_count(self.h, C.byref(n)))
+        return int(n.value)

@@ -1,0 +1,130 @@
+// pg_internal.cuh - shared declarations of the CUDA library (context, error
+// reporting, small device helpers written as inline PTX).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "pathguide.h"
+
+static_assert(sizeof(pg_region_state) == 704, "pg_region_state layout");
+static_assert(sizeof(pg_directional_data) == 40, "DirectionalData layout");
+static_assert(sizeof(pg_vmm_theta) == 720, "VMM_Theta layout");
+
+// Device-side error word bits (ORed by kernels, read back by the host).
+#define PG_DEV_ERR_TIMEOUT 1u   // a bounded wait ran out
+#define PG_DEV_ERR_NUMERIC 2u   // non-finite parameter produced
+#define PG_DEV_ERR_BOUNDS 4u    // an index check failed (access skipped)
+
+struct pg_ctx {
+    int device = 0;
+    int sm_count = 0;
+    pg_fit_config cfg{};
+    pg_fit_tuning tuning{};
+    uint32_t max_regions = 0;
+    uint64_t max_samples = 0;
+    pg_region_state *d_states = nullptr;
+    uint32_t *d_order = nullptr;     // region ids, largest sample count first
+    uint32_t *d_counters = nullptr;  // [0] fit work queue, [1] eval queue, [2] error word, ...
+    float *d_init = nullptr;         // initial means x[16] y[16] z[16], initial r[16]
+    uint32_t *d_zero_offsets = nullptr;  // max_regions+1 zeros (initialisation-only fits)
+    uint32_t init_k = 0;             // K the table was computed for
+    float init_kappa = -1.0f;
+    uint32_t last_launches = 0;
+    std::string last_error;
+};
+
+namespace pg {
+
+int set_error(pg_ctx *ctx, int status, const std::string &msg);
+int check_cuda(pg_ctx *ctx, cudaError_t e, const char *what);
+int upload_init_table(pg_ctx *ctx, cudaStream_t s);
+
+constexpr float kLog2e = 1.4426950408889634f;
+constexpr float kLn2 = 0.6931471805599453f;
+constexpr float kInv4Pi = 0.0795774715459476679f;
+constexpr float kTwoPi = 6.2831853071795865f;
+constexpr float kPmmEps = 1.0e-8f;      // PMM_EPSILON (pmm.h:40)
+constexpr float kVmfMinKappa = 1e-3f;   // VMF_MinKappa (VMFKernel.h:42)
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ float ex2_approx(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float lg2_approx(float x) {
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// mbarrier + 1-D TMA bulk copy (cp.async.bulk) helpers.
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void tma_bulk_g2s(void *smem_dst, const void *gmem_src, uint32_t bytes,
+                                             uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(smem_dst)),
+        "l"(gmem_src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait on an mbarrier phase: gives up after `max_cycles` SM clocks
+// and reports PG_DEV_ERR_TIMEOUT instead of spinning forever.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t *err,
+                                                  long long max_cycles = 4000000000LL) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (clock64() - t0 > max_cycles) {
+            atomicOr(err, PG_DEV_ERR_TIMEOUT);
+            return false;
+        }
+    }
+    return true;
+}
+
+// Neumaier compensated accumulation of x into (s, c).
+__device__ __forceinline__ void neumaier_add(float &s, float &c, float x) {
+    const float t = s + x;
+    if (fabsf(s) >= fabsf(x))
+        c += (s - t) + x;
+    else
+        c += (x - t) + s;
+    s = t;
+}
+
+}  // namespace pg

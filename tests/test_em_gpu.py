@@ -1,0 +1,179 @@
+"""GPU parity of the batched EM fit (pg_fit_regions) through the C ABI.
+
+Tolerances, GPU vs the FP64 oracle (GPU_TOL): the GPU E-step evaluates the
+exponent kappa log2(e) mu.d + log2(pi norm) - kappa log2(e) with three FP32 FMAs
+whose intermediates are of size kappa log2(e), so each responsibility carries a
+relative error up to ~2.4e-7 kappa (plus 2^-22 from ex2); the reference's own
+FP32 cos(theta) rounding is ~1.2e-7 kappa.  These per-sample errors average
+out in the sufficient statistics; GPU_TOL bounds what is left after 20 EM
+iterations.  GPU vs the reference itself uses the FP64-vs-reference bound
+REF_TOL of test_oracle.py (lightpmm's fastexp dominates).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from test_oracle import FIT_SETS, REF_TOL, assert_params_close, cfg_from, mu_angle
+
+pytestmark = pytest.mark.gpu
+
+GPU_TOL = {"weight_rtol": 5e-4, "kappa_rtol": 1e-3, "r_atol": 1e-4, "mu_angle": 5e-4,
+           "ll_rtol": 2e-5, "ll_per_weight": 2e-5}
+
+
+def run_fit(cuda, pkg, cfg, dirw, offsets, mode=None, states=None, tuning=None, ctx=None):
+    torch = cuda
+    abi = pkg.abi
+    R = len(offsets) - 1
+    own = ctx is None
+    if own:
+        ctx = pkg.FitContext(cfg, max_regions=max(R, 1))
+    if tuning:
+        ctx.set_tuning(**tuning)
+    if states is not None:
+        ctx.set_states(states)
+    d = torch.from_numpy(np.ascontiguousarray(dirw, dtype=np.float32)).cuda()
+    o = torch.from_numpy(np.asarray(offsets, dtype=np.uint32).view(np.int32)).cuda()
+    ctx.fit(d, o, R, abi.PG_FIT_INIT if mode is None else mode)
+    ctx.sync()
+    st = ctx.states(R)
+    ll = torch.zeros(R, dtype=torch.float64, device="cuda")
+    ctx.eval_loglik(d, o, R, ll)
+    ctx.sync()
+    out = (st, ll.cpu().numpy())
+    if own:
+        ctx.close()
+    return out
+
+
+def ll_close(got, want, dirw, offsets, tol):
+    sw = np.array([dirw[offsets[r]:offsets[r + 1], 3].astype(np.float64).sum() for r in range(len(offsets) - 1)])
+    d = np.abs(got - want)
+    bound = tol["ll_per_weight"] * sw + tol["ll_rtol"] * np.abs(want) + 1e-4
+    assert np.all(d <= bound), f"log-likelihood off by {d.max():.3g}"
+
+
+@pytest.mark.parametrize("name", FIT_SETS)
+def test_fit_matches_fp64_oracle(name, cuda, pkg, golden, oracle, abi):
+    g = golden(name)
+    cfg = cfg_from(abi, g["cfg"])
+    K = cfg.num_initial_components
+    mode = abi.PG_FIT_UPDATE if "states_in" in g else abi.PG_FIT_INIT
+    st, ll = run_fit(cuda, pkg, cfg, g["dirw"], g["offsets"], mode=mode, states=g.get("states_in"))
+    want, want_ll = oracle.fit(cfg, g["dirw"], g["offsets"], states=g.get("states_in"), mode=mode, f64=True)
+    np.testing.assert_array_equal(st["iters_last"], want["iters_last"])
+    np.testing.assert_array_equal(st["total_num_samples"], want["total_num_samples"])
+    fitted = want["iters_last"] > 0
+    assert_params_close(st, want, K, GPU_TOL, fitted)
+    np.testing.assert_allclose(st["sample_weight"], want["sample_weight"], rtol=1e-5)
+    ll_close(ll, oracle.eval_ll(g["dirw"], g["offsets"], st), g["dirw"], g["offsets"], GPU_TOL)
+    ll_close(ll, want_ll, g["dirw"], g["offsets"], REF_TOL)
+
+
+@pytest.mark.parametrize("name", FIT_SETS)
+def test_fit_within_stated_tolerance_of_reference(name, cuda, pkg, golden, abi):
+    g = golden(name)
+    cfg = cfg_from(abi, g["cfg"])
+    K = cfg.num_initial_components
+    mode = abi.PG_FIT_UPDATE if "states_in" in g else abi.PG_FIT_INIT
+    st, ll = run_fit(cuda, pkg, cfg, g["dirw"], g["offsets"], mode=mode, states=g.get("states_in"))
+    ref = g["states"]
+    np.testing.assert_array_equal(st["iters_last"], ref["iters_last"])
+    assert_params_close(st, ref, K, REF_TOL, ref["iters_last"] > 0)
+    ll_close(ll, g["ll_final"].astype(np.float64), g["dirw"], g["offsets"], REF_TOL)
+
+
+@pytest.mark.parametrize("K", [8, 16])
+@pytest.mark.parametrize("tuning", [{}, {"threads_per_cta": 64}, {"threads_per_cta": 256},
+                                    {"smem_samples": 256}])
+def test_uneven_batch_and_launch_shapes(K, tuning, cuda, pkg, oracle, abi, workloads):
+    """Uneven regions (64..20000 samples), resident and streamed staging paths."""
+    w = workloads.fit_batched(seed=11, n_regions=24, median=1500, sigma=1.2, lo=64, hi=20000)
+    cfg = abi.forced_iterations(20, num_initial_components=K)
+    st, ll = run_fit(cuda, pkg, cfg, w["dirw"], w["offsets"], tuning=tuning)
+    want, _ = oracle.fit(cfg, w["dirw"], w["offsets"], f64=True)
+    assert_params_close(st, want, K, GPU_TOL, want["iters_last"] > 0)
+    ll_close(ll, oracle.eval_ll(w["dirw"], w["offsets"], st), w["dirw"], w["offsets"], GPU_TOL)
+
+
+def test_fit_is_deterministic(cuda, pkg, abi, workloads):
+    w = workloads.fit_batched(seed=4, n_regions=16, median=1200, sigma=1.0, lo=64, hi=9000)
+    cfg = abi.forced_iterations(20, num_initial_components=16)
+    a, _ = run_fit(cuda, pkg, cfg, w["dirw"], w["offsets"])
+    b, _ = run_fit(cuda, pkg, cfg, w["dirw"], w["offsets"])
+    assert a.tobytes() == b.tobytes()
+
+
+def test_init_regions_matches_oracle(cuda, pkg, oracle, abi):
+    cfg = abi.default_fit_config(num_initial_components=12)
+    ctx = pkg.FitContext(cfg, max_regions=5)
+    ctx.init_regions(5)
+    ctx.sync()
+    got = ctx.states(5)
+    want = oracle.init_states(cfg, 5, exact=True)
+    for f in ("weight", "mu_x", "mu_y", "mu_z", "kappa"):
+        np.testing.assert_array_equal(got[f], want[f])
+    np.testing.assert_allclose(got["norm"], want["norm"], rtol=2e-6)
+    np.testing.assert_allclose(got["r"], want["r"], rtol=1e-6)
+    assert np.all(np.isinf(got["distance"]))
+    ctx.close()
+
+
+def test_edge_cases(cuda, pkg, oracle, abi):
+    """Empty regions, too few samples, one repeated direction (kappa clamps at
+    maxKappa), zero-weight samples."""
+    rng = np.random.default_rng(3)
+    d = rng.normal(size=(3000, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    same = np.tile(np.array([[0.0, 0.6, 0.8]]), (500, 1))
+    counts = [0, 16, 17, 500, 1000, 0]
+    dirs = np.concatenate([d[:16], d[16:33], same, d[33:1033]])
+    w = np.ones(len(dirs))
+    w[-1000:-500] = 0.0
+    dirw = np.concatenate([dirs, w[:, None]], axis=1).astype(np.float32)
+    offsets = np.concatenate([[0], np.cumsum(counts)]).astype(np.uint32)
+    cfg = abi.forced_iterations(15, num_initial_components=8)
+    st, _ = run_fit(cuda, pkg, cfg, dirw, offsets)
+    want, _ = oracle.fit(cfg, dirw, offsets, f64=True)
+    np.testing.assert_array_equal(st["iters_last"], [0, 0, 15, 15, 15, 0])
+    np.testing.assert_array_equal(st["iters_last"], want["iters_last"])
+    assert np.all(np.isfinite(st["kappa"])) and np.all(np.isfinite(st["weight"]))
+    # the concentrated region reaches the maxKappa clamp like the oracle
+    top = np.argmax(want["weight"][3, :8])
+    np.testing.assert_allclose(st["kappa"][3, top], want["kappa"][3, top], rtol=2e-3)
+    assert st["kappa"][3, top] > 1e4
+    assert_params_close(st, want, 8, GPU_TOL, np.array([False, False, True, False, True, False]))
+
+
+def test_nonfinite_samples_are_reported(cuda, pkg, abi):
+    torch = cuda
+    dirw = np.tile(np.array([[0.0, 0.0, 1.0, 1.0]], dtype=np.float32), (400, 1))
+    dirw[5, 0] = np.nan
+    offsets = np.array([0, 200, 400], dtype=np.uint32)
+    cfg = abi.forced_iterations(5, num_initial_components=8)
+    ctx = pkg.FitContext(cfg, max_regions=2)
+    d = torch.from_numpy(dirw).cuda()
+    o = torch.from_numpy(offsets.view(np.int32)).cuda()
+    ctx.fit(d, o, 2, abi.PG_FIT_INIT)
+    with pytest.raises(pkg.PathGuideError) as e:
+        ctx.sync()
+    assert e.value.status == abi.PG_ERR_NUMERIC
+    st = ctx.states(2)
+    assert st["flags"][0] & 2 and not (st["flags"][1] & 2)
+    ctx.close()
+
+
+def test_argument_errors(cuda, pkg, abi):
+    torch = cuda
+    ctx = pkg.FitContext(abi.default_fit_config(), max_regions=4)
+    d = torch.zeros(64, dtype=torch.float32, device="cuda")
+    o = torch.zeros(8, dtype=torch.int32, device="cuda")
+    with pytest.raises(pkg.PathGuideError) as e:
+        ctx.fit(d, o, 5)  # more regions than the context holds
+    assert e.value.status == abi.PG_ERR_ARG
+    with pytest.raises(pkg.PathGuideError):
+        ctx.fit(d.data_ptr() + 4, o, 2)  # misaligned float4 array
+    with pytest.raises(pkg.PathGuideError):
+        ctx.fit(d, o, 2, mode=7)
+    ctx.close()
