@@ -189,6 +189,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="512-region case (for ncu captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--threads", type=int, default=0, help="threads per CTA (autotuned if 0)")
+    ap.add_argument("--cluster", type=int, default=0, help="CTAs per large region (autotuned if 0)")
+    ap.add_argument("--smem-samples", type=int, default=0)
+    ap.add_argument("--sweep", action="store_true", help="time the tuning grid and print one line per point")
     ap.add_argument("--ref-seconds", type=float, default=None,
                     help="CPU seconds per reference step (default: ~100 s over the whole run)")
     args = ap.parse_args()
@@ -215,6 +219,7 @@ def main():
     n_samples = int(counts.sum())
     cfg = abi.forced_iterations(ITERS, num_initial_components=K)
     ctx = pkg.FitContext(cfg, max_regions=R)
+    ctx.set_tuning(threads_per_cta=args.threads, smem_samples=args.smem_samples, cluster_size=args.cluster)
     stream = torch.cuda.Stream()
     dirw_h = torch.from_numpy(w["dirw"]).pin_memory()
     offs_h = torch.from_numpy(w["offsets"].view(np.int32)).pin_memory()

@@ -199,7 +199,7 @@ typedef struct pg_fit_tuning {
     uint32_t threads_per_cta;     /* 64, 128, 256                            */
     uint32_t smem_samples;        /* samples kept in shared memory per CTA   */
     uint32_t ctas_per_sm;         /* resident CTAs per SM for the grid size  */
-    uint32_t reserved;
+    uint32_t cluster_size;        /* CTAs sharing one large region: 1..16    */
 } pg_fit_tuning;
 int pg_set_fit_tuning(pg_ctx *ctx, const pg_fit_tuning *t);
 int pg_get_fit_tuning(const pg_ctx *ctx, pg_fit_tuning *t);

@@ -205,6 +205,7 @@ int pg_set_fit_tuning(pg_ctx *ctx, const pg_fit_tuning *t) {
         return set_error(ctx, PG_ERR_ARG, "threads_per_cta must be 64, 128 or 256");
     if (t->ctas_per_sm > 32) return set_error(ctx, PG_ERR_ARG, "ctas_per_sm must be <= 32");
     if (t->smem_samples > 13000) return set_error(ctx, PG_ERR_ARG, "smem_samples must be <= 13000");
+    if (t->cluster_size > 16) return set_error(ctx, PG_ERR_ARG, "cluster_size must be <= 16");
     ctx->tuning = *t;
     return PG_OK;
 }

@@ -30,9 +30,13 @@
 #include <math.h>
 #include <stdio.h>
 
+#include <cooperative_groups.h>
+
 #include <algorithm>
 
 #include "pg_internal.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace pg {
 
@@ -49,6 +53,8 @@ struct EmArgs {
     int mode;
     uint32_t smem_cap;  // samples staged in shared memory
     double *ll_out;     // eval mode only
+    uint32_t *large_counter;     // cluster work queue (largest regions)
+    const uint32_t *n_large;     // number of regions fitted by a whole cluster
 };
 
 template <int KMAX, int NW>
@@ -58,6 +64,8 @@ struct EmShared {
     float osx[16], osy[16], osz[16], ow[16];  // statistics recovered from the prior mixture (updateFit)
     float red[NW][4 * KMAX];
     float red_ll[NW], red_sw[NW];
+    float part[8][KMAX];  // this CTA's compensated statistics (cluster mode)
+    float ptot[4];        // this CTA's log-likelihood and weight (hi, lo pairs)
     double last_ll, abs_inv_last, ll;
     float sample_weight, num_samples;
     unsigned long long total;
@@ -259,21 +267,54 @@ __device__ __forceinline__ void estep(const float4 *__restrict__ src, uint32_t N
     }
 }
 
-// Warp 0: merge partial statistics and run the M-step of iteration `it`.
+// Compensated statistics of one component: (hi, lo) pairs of sum gamma w d.xyz, sum gamma w.
+struct Stats4 {
+    float sxh, sxc, syh, syc, szh, szc, wh, wc;
+};
+
+__device__ __forceinline__ Stats4 stats_zero() { return Stats4{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}; }
+
+// Adds a compensated pair (h, l) into (s, c).
+__device__ __forceinline__ void neumaier_add2(float &s, float &c, float h, float l) {
+    neumaier_add(s, c, h);
+    c += l;
+}
+
+// Warp 0, lane c < KMAX: the CTA's statistics of component c, merged over warps.
 template <int KMAX, int NW>
-__device__ void mstep(const EmArgs &a, EmShared<KMAX, NW> &S, int lane, uint32_t it, uint32_t N) {
+__device__ __forceinline__ Stats4 merge_warps(const EmShared<KMAX, NW> &S, int c) {
+    Stats4 m = stats_zero();
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+        neumaier_add(m.sxh, m.sxc, S.red[w][c]);
+        neumaier_add(m.syh, m.syc, S.red[w][KMAX + c]);
+        neumaier_add(m.szh, m.szc, S.red[w][2 * KMAX + c]);
+        neumaier_add(m.wh, m.wc, S.red[w][3 * KMAX + c]);
+    }
+    return m;
+}
+
+// Lane 0: the CTA's log-likelihood (log2 units) and valid weight, merged over warps.
+template <int KMAX, int NW>
+__device__ __forceinline__ void merge_totals(const EmShared<KMAX, NW> &S, float &llh, float &llc, float &swh,
+                                             float &swc) {
+    llh = llc = swh = swc = 0.0f;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+        neumaier_add(llh, llc, S.red_ll[w]);
+        neumaier_add(swh, swc, S.red_sw[w]);
+    }
+}
+
+// Warp 0 of the CTA that owns the region: M-step of iteration `it` from merged
+// statistics m (lane c < KMAX) and region totals (lane 0).
+template <int KMAX, int NW>
+__device__ void mstep_apply(const EmArgs &a, EmShared<KMAX, NW> &S, int lane, uint32_t it, uint32_t N, Stats4 m,
+                            float llh, float llc, float swh, float swc) {
     const pg_fit_config &cfg = a.cfg;
     const uint32_t K = S.K;
-    // Region totals: log-likelihood (log2 units) and valid sample weight.
-    float llh = 0.0f, llc = 0.0f, swh = 0.0f, swc = 0.0f;
     if (lane == 0) {
-#pragma unroll
-        for (int w = 0; w < NW; ++w) {
-            neumaier_add(llh, llc, S.red_ll[w]);
-            neumaier_add(swh, swc, S.red_sw[w]);
-        }
-        const double ll = ((double)llh + (double)llc) * 0.6931471805599453;
-        S.ll = ll;
+        S.ll = ((double)llh + (double)llc) * 0.6931471805599453;
         if (it == 0) {
             const float sum_w = swh + swc;
             if (a.mode == PG_FIT_UPDATE) {
@@ -290,21 +331,13 @@ __device__ void mstep(const EmArgs &a, EmShared<KMAX, NW> &S, int lane, uint32_t
     __syncwarp();
     if (lane < KMAX) {
         const int c = lane;
-        float sxh = 0.f, sxc = 0.f, syh = 0.f, syc = 0.f, szh = 0.f, szc = 0.f, wh = 0.f, wc = 0.f;
-#pragma unroll
-        for (int w = 0; w < NW; ++w) {
-            neumaier_add(sxh, sxc, S.red[w][c]);
-            neumaier_add(syh, syc, S.red[w][KMAX + c]);
-            neumaier_add(szh, szc, S.red[w][2 * KMAX + c]);
-            neumaier_add(wh, wc, S.red[w][3 * KMAX + c]);
-        }
         if (a.mode == PG_FIT_UPDATE) {
-            neumaier_add(sxh, sxc, S.osx[c]);
-            neumaier_add(syh, syc, S.osy[c]);
-            neumaier_add(szh, szc, S.osz[c]);
-            neumaier_add(wh, wc, S.ow[c]);
+            neumaier_add(m.sxh, m.sxc, S.osx[c]);
+            neumaier_add(m.syh, m.syc, S.osy[c]);
+            neumaier_add(m.szh, m.szc, S.osz[c]);
+            neumaier_add(m.wh, m.wc, S.ow[c]);
         }
-        const float Sx = sxh + sxc, Sy = syh + syc, Sz = szh + szc, W = wh + wc;
+        const float Sx = m.sxh + m.sxc, Sy = m.syh + m.syc, Sz = m.szh + m.szc, W = m.wh + m.wc;
         // parameterUpdate (VMMFactory.h:436-455)
         const float inv_wpn = cfg.v_prior * (float)K + 1.0f;
         const float wpn = 1.0f / inv_wpn;
@@ -326,8 +359,9 @@ __device__ void mstep(const EmArgs &a, EmShared<KMAX, NW> &S, int lane, uint32_t
         float rp = (avg * ns + a_p) / (ns + b_p);
         // 1 - r_p without cancellation: 1 - avg = (W^2 - |S|^2) / (W (W + |S|)),
         // with W^2 - |S|^2 evaluated in FP64 from the compensated sums.
-        const double Wd = (double)wh + (double)wc;
-        const double Xd = (double)sxh + (double)sxc, Yd = (double)syh + (double)syc, Zd = (double)szh + (double)szc;
+        const double Wd = (double)m.wh + (double)m.wc;
+        const double Xd = (double)m.sxh + (double)m.sxc, Yd = (double)m.syh + (double)m.syc,
+                     Zd = (double)m.szh + (double)m.szc;
         const double gap = fma(Wd, Wd, -fma(Xd, Xd, fma(Yd, Yd, Zd * Zd)));
         const float one_m_avg = (float)gap / (W * (W + rl));
         float one_m_rp = (ns * one_m_avg + (b_p - a_p)) / (ns + b_p);
@@ -436,103 +470,204 @@ __device__ void store_model(const EmArgs &a, EmShared<KMAX, NW> &S, pg_region_st
     }
 }
 
-template <int KMAX, int NT>
+// Copies the E-step constants, K, the iteration bound and the stop flag from
+// the shared memory of cluster rank 0 (warp 0 of a non-zero rank).
+template <int KMAX, int NW>
+__device__ __forceinline__ void pull_consts(cg::cluster_group &cluster, EmShared<KMAX, NW> &S, int lane) {
+    EmShared<KMAX, NW> *R0 = cluster.map_shared_rank(&S, 0);
+    if (lane < KMAX) {
+        S.cax[lane] = R0->cax[lane];
+        S.cay[lane] = R0->cay[lane];
+        S.caz[lane] = R0->caz[lane];
+        S.cc0[lane] = R0->cc0[lane];
+        S.ccm[lane] = R0->ccm[lane];
+    }
+    if (lane == 0) {
+        S.K = R0->K;
+        S.max_itr = R0->max_itr;
+        S.stop = R0->stop;
+    }
+}
+
+// One region (or, in a cluster, this CTA's slice of one region): stage the
+// samples, iterate E-step / reduction / M-step, store the mixture.
+template <int KMAX, int NT, bool kCluster>
+__device__ void process_region(const EmArgs &a, EmShared<KMAX, NT / 32> &S, float4 *s_samp, uint64_t *bar,
+                               uint32_t &phase, uint32_t item, cg::cluster_group &cluster) {
+    constexpr int NW = NT / 32;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t crank = kCluster ? cluster.block_rank() : 0u;
+    const uint32_t csize = kCluster ? cluster.num_blocks() : 1u;
+    const uint32_t r = a.order[item];
+    const uint32_t b = a.offsets[r], e = a.offsets[r + 1];
+    const uint32_t N = e > b ? e - b : 0u;
+    pg_region_state *st = a.states + r;
+    // this CTA's slice [sb, se)
+    const uint32_t chunk = (N + csize - 1) / csize;
+    const uint32_t sb = min(e, b + crank * chunk);
+    const uint32_t se = min(e, sb + chunk);
+    const uint32_t n_local = se - sb;
+    const bool owner = crank == 0;
+    if (owner && warp == 0) load_model(a, S, st, lane, N);
+    if (kCluster) {
+        cluster.sync();
+        if (!owner && warp == 0) pull_consts(cluster, S, lane);
+    }
+    __syncthreads();
+    const uint32_t max_itr = S.max_itr;
+    const bool resident = n_local <= a.smem_cap;
+    bool ok = true;
+    if (resident && max_itr > 0 && n_local > 0) {
+        if (tid == 0) {
+            fence_proxy_async_smem();
+            const uint32_t bytes = n_local * 16u;
+            mbar_arrive_expect_tx(bar, bytes);
+            const char *src = reinterpret_cast<const char *>(a.dirw + sb);
+            char *dst = reinterpret_cast<char *>(s_samp);
+            for (uint32_t off = 0; off < bytes; off += 32768u) {
+                const uint32_t ch = min(32768u, bytes - off);
+                tma_bulk_g2s(dst + off, src + off, ch, bar);
+            }
+        }
+        ok = mbar_wait_bounded(bar, phase, a.error_word);
+        phase ^= 1u;
+    }
+    // A timed-out copy leaves the slice's statistics at zero; the error word reports it.
+    uint32_t it = 0;
+    for (; it < max_itr; ++it) {
+        float2 AX[KMAX / 2], AY[KMAX / 2], AZ[KMAX / 2], C0[KMAX / 2];
+        float CM[KMAX];
+#pragma unroll
+        for (int j = 0; j < KMAX / 2; ++j) {
+            AX[j] = make_float2(S.cax[2 * j], S.cax[2 * j + 1]);
+            AY[j] = make_float2(S.cay[2 * j], S.cay[2 * j + 1]);
+            AZ[j] = make_float2(S.caz[2 * j], S.caz[2 * j + 1]);
+            C0[j] = make_float2(S.cc0[2 * j], S.cc0[2 * j + 1]);
+            CM[2 * j] = S.ccm[2 * j];
+            CM[2 * j + 1] = S.ccm[2 * j + 1];
+        }
+        float2 SX[KMAX / 2], SY[KMAX / 2], SZ[KMAX / 2], SW[KMAX / 2];
+#pragma unroll
+        for (int j = 0; j < KMAX / 2; ++j) SX[j] = SY[j] = SZ[j] = SW[j] = make_float2(0.0f, 0.0f);
+        float ll = 0.0f, sw = 0.0f;
+        if (ok) {
+            if (resident)
+                estep<KMAX, true>(s_samp, n_local, tid, NT, AX, AY, AZ, C0, CM, SX, SY, SZ, SW, ll, sw);
+            else
+                estep<KMAX, false>(a.dirw + sb, n_local, tid, NT, AX, AY, AZ, C0, CM, SX, SY, SZ, SW, ll, sw);
+        }
+        float f[4 * KMAX];
+#pragma unroll
+        for (int j = 0; j < KMAX / 2; ++j) {
+            f[2 * j] = SX[j].x;
+            f[2 * j + 1] = SX[j].y;
+            f[KMAX + 2 * j] = SY[j].x;
+            f[KMAX + 2 * j + 1] = SY[j].y;
+            f[2 * KMAX + 2 * j] = SZ[j].x;
+            f[2 * KMAX + 2 * j + 1] = SZ[j].y;
+            f[3 * KMAX + 2 * j] = SW[j].x;
+            f[3 * KMAX + 2 * j + 1] = SW[j].y;
+        }
+        reduce_scatter<4 * KMAX>(f, lane);
+        constexpr int Q = (4 * KMAX) / 32;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) S.red[warp][lane * Q + q] = f[q];
+        ll = warp_sum(ll);
+        sw = warp_sum(sw);
+        if (lane == 0) {
+            S.red_ll[warp] = ll;
+            S.red_sw[warp] = sw;
+        }
+        __syncthreads();
+        if (!kCluster) {
+            if (warp == 0) {
+                Stats4 m = stats_zero();
+                if (lane < KMAX) m = merge_warps(S, lane);
+                float llh = 0.f, llc = 0.f, swh = 0.f, swc = 0.f;
+                if (lane == 0) merge_totals(S, llh, llc, swh, swc);
+                mstep_apply(a, S, lane, it, N, m, llh, llc, swh, swc);
+            }
+            __syncthreads();
+        } else {
+            // CTA partial -> own shared memory; rank 0 merges the cluster's partials.
+            if (warp == 0) {
+                if (lane < KMAX) {
+                    const Stats4 m = merge_warps(S, lane);
+                    S.part[0][lane] = m.sxh;
+                    S.part[1][lane] = m.sxc;
+                    S.part[2][lane] = m.syh;
+                    S.part[3][lane] = m.syc;
+                    S.part[4][lane] = m.szh;
+                    S.part[5][lane] = m.szc;
+                    S.part[6][lane] = m.wh;
+                    S.part[7][lane] = m.wc;
+                }
+                if (lane == 0) merge_totals(S, S.ptot[0], S.ptot[1], S.ptot[2], S.ptot[3]);
+            }
+            cluster.sync();
+            if (owner && warp == 0) {
+                Stats4 m = stats_zero();
+                float llh = 0.f, llc = 0.f, swh = 0.f, swc = 0.f;
+                for (uint32_t q = 0; q < csize; ++q) {
+                    const EmShared<KMAX, NW> *P = cluster.map_shared_rank(&S, q);
+                    if (lane < KMAX) {
+                        neumaier_add2(m.sxh, m.sxc, P->part[0][lane], P->part[1][lane]);
+                        neumaier_add2(m.syh, m.syc, P->part[2][lane], P->part[3][lane]);
+                        neumaier_add2(m.szh, m.szc, P->part[4][lane], P->part[5][lane]);
+                        neumaier_add2(m.wh, m.wc, P->part[6][lane], P->part[7][lane]);
+                    }
+                    if (lane == 0) {
+                        neumaier_add2(llh, llc, P->ptot[0], P->ptot[1]);
+                        neumaier_add2(swh, swc, P->ptot[2], P->ptot[3]);
+                    }
+                }
+                mstep_apply(a, S, lane, it, N, m, llh, llc, swh, swc);
+            }
+            cluster.sync();
+            if (!owner && warp == 0) pull_consts(cluster, S, lane);
+            __syncthreads();
+        }
+        if (S.stop) break;
+    }
+    if (owner && warp == 0) store_model(a, S, st, lane, it);
+    __syncthreads();
+}
+
+template <int KMAX, int NT, bool kCluster>
 __global__ void __launch_bounds__(NT) em_fit_kernel(EmArgs a) {
     constexpr int NW = NT / 32;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float4 *s_samp = reinterpret_cast<float4 *>(smem_raw);
     EmShared<KMAX, NW> &S = *reinterpret_cast<EmShared<KMAX, NW> *>(smem_raw + (size_t)a.smem_cap * 16);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tid = threadIdx.x;
     uint64_t *bar = reinterpret_cast<uint64_t *>(&S.bar);
+    cg::cluster_group cluster = cg::this_cluster();
     if (tid == 0) {
         mbar_init(bar, 1);
         fence_mbar_init();
     }
     __syncthreads();
     uint32_t phase = 0;
+    const uint32_t n_large = kCluster ? *a.n_large : 0u;
+    if constexpr (kCluster) {
+        // Phase 1: the largest regions, each shared by all CTAs of a cluster.
+        for (;;) {
+            if (cluster.block_rank() == 0 && tid == 0) S.item = atomicAdd(a.large_counter, 1u);
+            cluster.sync();
+            const uint32_t item = *cluster.map_shared_rank(&S.item, 0);
+            cluster.sync();
+            if (item >= n_large) break;
+            process_region<KMAX, NT, true>(a, S, s_samp, bar, phase, item, cluster);
+        }
+    }
+    // Phase 2: the remaining regions, one CTA each, largest first.
     for (;;) {
-        if (tid == 0) S.item = atomicAdd(a.work_counter, 1u);
+        if (tid == 0) S.item = n_large + atomicAdd(a.work_counter, 1u);
         __syncthreads();
         const uint32_t item = S.item;
+        __syncthreads();
         if (item >= a.n_regions) break;
-        const uint32_t r = a.order[item];
-        const uint32_t b = a.offsets[r], e = a.offsets[r + 1];
-        const uint32_t N = e > b ? e - b : 0u;
-        pg_region_state *st = a.states + r;
-        if (warp == 0) load_model(a, S, st, lane, N);
-        __syncthreads();
-        const uint32_t max_itr = S.max_itr;
-        const bool resident = N <= a.smem_cap;
-        bool ok = true;
-        if (resident && max_itr > 0) {
-            if (tid == 0) {
-                fence_proxy_async_smem();
-                const uint32_t bytes = N * 16u;
-                mbar_arrive_expect_tx(bar, bytes);
-                const char *src = reinterpret_cast<const char *>(a.dirw + b);
-                char *dst = reinterpret_cast<char *>(s_samp);
-                for (uint32_t off = 0; off < bytes; off += 32768u) {
-                    const uint32_t chunk = min(32768u, bytes - off);
-                    tma_bulk_g2s(dst + off, src + off, chunk, bar);
-                }
-            }
-            ok = mbar_wait_bounded(bar, phase, a.error_word);
-            phase ^= 1u;
-        }
-        uint32_t it = 0;
-        if (ok) {
-            for (; it < max_itr; ++it) {
-                float2 AX[KMAX / 2], AY[KMAX / 2], AZ[KMAX / 2], C0[KMAX / 2];
-                float CM[KMAX];
-#pragma unroll
-                for (int j = 0; j < KMAX / 2; ++j) {
-                    AX[j] = make_float2(S.cax[2 * j], S.cax[2 * j + 1]);
-                    AY[j] = make_float2(S.cay[2 * j], S.cay[2 * j + 1]);
-                    AZ[j] = make_float2(S.caz[2 * j], S.caz[2 * j + 1]);
-                    C0[j] = make_float2(S.cc0[2 * j], S.cc0[2 * j + 1]);
-                    CM[2 * j] = S.ccm[2 * j];
-                    CM[2 * j + 1] = S.ccm[2 * j + 1];
-                }
-                float2 SX[KMAX / 2], SY[KMAX / 2], SZ[KMAX / 2], SW[KMAX / 2];
-#pragma unroll
-                for (int j = 0; j < KMAX / 2; ++j) {
-                    SX[j] = SY[j] = SZ[j] = SW[j] = make_float2(0.0f, 0.0f);
-                }
-                float ll = 0.0f, sw = 0.0f;
-                if (resident)
-                    estep<KMAX, true>(s_samp, N, tid, NT, AX, AY, AZ, C0, CM, SX, SY, SZ, SW, ll, sw);
-                else
-                    estep<KMAX, false>(a.dirw + b, N, tid, NT, AX, AY, AZ, C0, CM, SX, SY, SZ, SW, ll, sw);
-                float f[4 * KMAX];
-#pragma unroll
-                for (int j = 0; j < KMAX / 2; ++j) {
-                    f[2 * j] = SX[j].x;
-                    f[2 * j + 1] = SX[j].y;
-                    f[KMAX + 2 * j] = SY[j].x;
-                    f[KMAX + 2 * j + 1] = SY[j].y;
-                    f[2 * KMAX + 2 * j] = SZ[j].x;
-                    f[2 * KMAX + 2 * j + 1] = SZ[j].y;
-                    f[3 * KMAX + 2 * j] = SW[j].x;
-                    f[3 * KMAX + 2 * j + 1] = SW[j].y;
-                }
-                reduce_scatter<4 * KMAX>(f, lane);
-                constexpr int Q = (4 * KMAX) / 32;
-#pragma unroll
-                for (int q = 0; q < Q; ++q) S.red[warp][lane * Q + q] = f[q];
-                ll = warp_sum(ll);
-                sw = warp_sum(sw);
-                if (lane == 0) {
-                    S.red_ll[warp] = ll;
-                    S.red_sw[warp] = sw;
-                }
-                __syncthreads();
-                if (warp == 0) mstep(a, S, lane, it, N);
-                __syncthreads();
-                if (S.stop) break;
-            }
-        }
-        if (warp == 0) store_model(a, S, st, lane, it);
-        __syncthreads();
+        process_region<KMAX, NT, false>(a, S, s_samp, bar, phase, item, cluster);
     }
 }
 
@@ -588,7 +723,8 @@ __global__ void __launch_bounds__(NT) em_eval_kernel(EmArgs a) {
 // counting sort over 128 logarithmic size buckets (4 per octave).  One CTA of
 // 1024 threads; n_regions of any size.
 __global__ void __launch_bounds__(1024) order_regions_kernel(const uint32_t *offsets, uint32_t n_regions,
-                                                             uint32_t *order) {
+                                                             uint32_t *order, uint32_t large_threshold,
+                                                             uint32_t *n_large_out) {
     constexpr int NB = 128;
     __shared__ uint32_t hist[NB];
     __shared__ uint32_t base[NB];
@@ -612,6 +748,17 @@ __global__ void __launch_bounds__(1024) order_regions_kernel(const uint32_t *off
             base[i] = acc;
             acc += hist[i];
         }
+        // regions whose size bucket is at or above the threshold's bucket come
+        // first in the order and are fitted by a whole cluster
+        uint32_t nl = 0;
+        if (large_threshold != 0xFFFFFFFFu) {
+            const float l = log2f((float)large_threshold + 1.0f) * 4.0f;
+            int k = (int)l;
+            k = k < 0 ? 0 : (k > NB - 1 ? NB - 1 : k);
+            const int bt = NB - 1 - k;
+            for (int i = 0; i <= bt; ++i) nl += hist[i];
+        }
+        *n_large_out = nl;
     }
     __syncthreads();
     for (uint32_t chunk = 0; chunk < n_regions; chunk += blockDim.x) {
@@ -647,22 +794,58 @@ static size_t fit_smem_bytes(uint32_t cap) {
 }
 
 template <int KMAX, int NT>
-static int launch_fit(pg_ctx *ctx, const EmArgs &args, cudaStream_t s, uint32_t ctas_per_sm) {
-    auto kern = em_fit_kernel<KMAX, NT>;
+static int launch_fit(pg_ctx *ctx, const EmArgs &args, cudaStream_t s, uint32_t ctas_per_sm, uint32_t cluster) {
     const size_t smem = fit_smem_bytes<KMAX, NT>(args.smem_cap);
-    int st = check_cuda(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+    cudaLaunchConfig_t lc = {};
+    cudaLaunchAttribute attr[1];
+    lc.blockDim = dim3(NT, 1, 1);
+    lc.dynamicSmemBytes = smem;
+    lc.stream = s;
+    int st;
+    if (cluster > 1) {
+        auto kern = em_fit_kernel<KMAX, NT, true>;
+        st = check_cuda(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                         "em_fit smem attribute");
-    if (st) return st;
-    int occ = 0;
-    st = check_cuda(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, NT, smem), "em_fit occupancy");
-    if (st) return st;
-    if (occ < 1) return set_error(ctx, PG_ERR_ARG, "em_fit: launch configuration does not fit on an SM");
-    const uint32_t per_sm = ctas_per_sm ? std::min<uint32_t>(ctas_per_sm, (uint32_t)occ) : (uint32_t)occ;
-    uint32_t grid = per_sm * (uint32_t)ctx->sm_count;
-    if (grid > args.n_regions) grid = args.n_regions;
-    if (grid == 0) grid = 1;
-    kern<<<grid, NT, smem, s>>>(args);
-    return check_cuda(ctx, cudaGetLastError(), "em_fit launch");
+        if (st) return st;
+        if (cluster > 8) {
+            st = check_cuda(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1),
+                            "em_fit cluster attribute");
+            if (st) return st;
+        }
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = cluster;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        lc.attrs = attr;
+        lc.numAttrs = 1;
+        lc.gridDim = dim3(cluster * (uint32_t)ctx->sm_count, 1, 1);
+        int nclusters = 0;
+        st = check_cuda(ctx, cudaOccupancyMaxActiveClusters(&nclusters, kern, &lc), "em_fit cluster occupancy");
+        if (st) return st;
+        if (nclusters < 1) return set_error(ctx, PG_ERR_ARG, "em_fit: cluster configuration does not fit");
+        uint32_t grid = (uint32_t)nclusters * cluster;
+        if (ctas_per_sm) grid = std::min<uint32_t>(grid, ctas_per_sm * (uint32_t)ctx->sm_count / cluster * cluster);
+        if (grid < cluster) grid = cluster;
+        lc.gridDim = dim3(grid, 1, 1);
+        st = check_cuda(ctx, cudaLaunchKernelEx(&lc, kern, args), "em_fit launch");
+    } else {
+        auto kern = em_fit_kernel<KMAX, NT, false>;
+        st = check_cuda(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                        "em_fit smem attribute");
+        if (st) return st;
+        int occ = 0;
+        st = check_cuda(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, NT, smem), "em_fit occupancy");
+        if (st) return st;
+        if (occ < 1) return set_error(ctx, PG_ERR_ARG, "em_fit: launch configuration does not fit on an SM");
+        const uint32_t per_sm = ctas_per_sm ? std::min<uint32_t>(ctas_per_sm, (uint32_t)occ) : (uint32_t)occ;
+        uint32_t grid = per_sm * (uint32_t)ctx->sm_count;
+        if (grid > args.n_regions) grid = args.n_regions;
+        if (grid == 0) grid = 1;
+        lc.gridDim = dim3(grid, 1, 1);
+        lc.numAttrs = 0;
+        st = check_cuda(ctx, cudaLaunchKernelEx(&lc, kern, args), "em_fit launch");
+    }
+    return st;
 }
 
 }  // namespace pg
@@ -672,7 +855,6 @@ using namespace pg;
 extern "C" {
 
 int pg_init_regions(pg_ctx *ctx, uint32_t n_regions, void *stream) {
-    // A PG_FIT_INIT fit over empty regions runs VMMFactory::initialize only.
     if (!ctx) return PG_ERR_ARG;
     if (n_regions > ctx->max_regions) return set_error(ctx, PG_ERR_ARG, "n_regions exceeds context capacity");
     if (n_regions == 0) return PG_OK;
@@ -697,7 +879,13 @@ int pg_fit_regions(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint
     if (st) return st;
     st = check_cuda(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(uint32_t) * 4, s), "queue reset");
     if (st) return st;
-    order_regions_kernel<<<1, 1024, 0, s>>>(offsets, n_regions, ctx->d_order);
+    const pg_fit_tuning &t = ctx->tuning;
+    const uint32_t nt = t.threads_per_cta ? t.threads_per_cta : 128u;
+    const uint32_t cluster = t.cluster_size ? t.cluster_size : 8u;
+    const uint32_t cap = t.smem_samples ? t.smem_samples : 6144u;
+    // A region goes to a whole cluster when it has more than cluster x 2048 samples.
+    const uint32_t large_threshold = cluster > 1 ? std::max<uint32_t>(cluster * 2048u, cap) : 0xFFFFFFFFu;
+    order_regions_kernel<<<1, 1024, 0, s>>>(offsets, n_regions, ctx->d_order, large_threshold, ctx->d_counters + 3);
     st = check_cuda(ctx, cudaGetLastError(), "order_regions launch");
     if (st) return st;
     EmArgs args;
@@ -707,26 +895,27 @@ int pg_fit_regions(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint
     args.order = ctx->d_order;
     args.n_regions = n_regions;
     args.work_counter = ctx->d_counters;
+    args.large_counter = ctx->d_counters + 1;
     args.error_word = ctx->d_counters + 2;
+    args.n_large = ctx->d_counters + 3;
     args.init_table = ctx->d_init;
     args.cfg = ctx->cfg;
     args.mode = mode;
     args.ll_out = nullptr;
-    const pg_fit_tuning &t = ctx->tuning;
-    const uint32_t nt = t.threads_per_cta ? t.threads_per_cta : 128u;
-    args.smem_cap = t.smem_samples ? t.smem_samples : 6144u;
+    args.smem_cap = cap;
     const uint32_t K = ctx->cfg.num_initial_components;
-    // The component count of an existing state can exceed the configured
-    // initial K only if states were uploaded; size for the widest case then.
+    // The component count of an existing state is read from the state; size
+    // for the widest case unless the mixtures are initialised here.
     const bool wide = (mode == PG_FIT_INIT) ? (K > 8) : true;
+    const uint32_t cps = t.ctas_per_sm;
     if (!wide) {
-        if (nt == 64) st = launch_fit<8, 64>(ctx, args, s, t.ctas_per_sm);
-        else if (nt == 256) st = launch_fit<8, 256>(ctx, args, s, t.ctas_per_sm);
-        else st = launch_fit<8, 128>(ctx, args, s, t.ctas_per_sm);
+        if (nt == 64) st = launch_fit<8, 64>(ctx, args, s, cps, cluster);
+        else if (nt == 256) st = launch_fit<8, 256>(ctx, args, s, cps, cluster);
+        else st = launch_fit<8, 128>(ctx, args, s, cps, cluster);
     } else {
-        if (nt == 64) st = launch_fit<16, 64>(ctx, args, s, t.ctas_per_sm);
-        else if (nt == 256) st = launch_fit<16, 256>(ctx, args, s, t.ctas_per_sm);
-        else st = launch_fit<16, 128>(ctx, args, s, t.ctas_per_sm);
+        if (nt == 64) st = launch_fit<16, 64>(ctx, args, s, cps, cluster);
+        else if (nt == 256) st = launch_fit<16, 256>(ctx, args, s, cps, cluster);
+        else st = launch_fit<16, 128>(ctx, args, s, cps, cluster);
     }
     if (st) return st;
     ctx->last_launches = 2;

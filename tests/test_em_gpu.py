@@ -86,9 +86,11 @@ def test_fit_within_stated_tolerance_of_reference(name, cuda, pkg, golden, abi):
 
 @pytest.mark.parametrize("K", [8, 16])
 @pytest.mark.parametrize("tuning", [{}, {"threads_per_cta": 64}, {"threads_per_cta": 256},
-                                    {"smem_samples": 256}])
+                                    {"smem_samples": 256}, {"cluster_size": 1}, {"cluster_size": 2},
+                                    {"cluster_size": 16}, {"cluster_size": 4, "smem_samples": 512}])
 def test_uneven_batch_and_launch_shapes(K, tuning, cuda, pkg, oracle, abi, workloads):
-    """Uneven regions (64..20000 samples), resident and streamed staging paths."""
+    """Uneven regions (64..20000 samples): resident and streamed staging, regions
+    shared by a cluster of 2..16 CTAs and regions fitted by one CTA."""
     w = workloads.fit_batched(seed=11, n_regions=24, median=1500, sigma=1.2, lo=64, hi=20000)
     cfg = abi.forced_iterations(20, num_initial_components=K)
     st, ll = run_fit(cuda, pkg, cfg, w["dirw"], w["offsets"], tuning=tuning)
@@ -139,10 +141,11 @@ def test_edge_cases(cuda, pkg, oracle, abi):
     np.testing.assert_array_equal(st["iters_last"], [0, 0, 15, 15, 15, 0])
     np.testing.assert_array_equal(st["iters_last"], want["iters_last"])
     assert np.all(np.isfinite(st["kappa"])) and np.all(np.isfinite(st["weight"]))
-    # the concentrated region reaches the maxKappa clamp like the oracle
+    # one repeated direction: the mean-cosine prior r n/(n+1) (VMMFactory.h:415-420),
+    # n = N pi, bounds kappa near n; the GPU lands where the oracle does
     top = np.argmax(want["weight"][3, :8])
     np.testing.assert_allclose(st["kappa"][3, top], want["kappa"][3, top], rtol=2e-3)
-    assert st["kappa"][3, top] > 1e4
+    assert st["kappa"][3, top] > 100.0
     assert_params_close(st, want, 8, GPU_TOL, np.array([False, False, True, False, True, False]))
 
 
