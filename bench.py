@@ -231,6 +231,29 @@ def main():
     def step():
         ctx.fit(dirw_d, offs_d, R, abi.PG_FIT_INIT, stream=stream)
 
+    if args.sweep:
+        for threads in (128, 256, 64):
+            for cluster in (1, 2, 4, 8, 16):
+                for cap in (0, 4096, 8192):
+                    try:
+                        ctx.set_tuning(threads_per_cta=threads, smem_samples=cap, cluster_size=cluster)
+                        with torch.cuda.stream(stream):
+                            step()
+                        torch.cuda.synchronize()
+                        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                        e0.record(stream)
+                        for _ in range(3):
+                            step()
+                        e1.record(stream)
+                        torch.cuda.synchronize()
+                        t = e0.elapsed_time(e1) / 3
+                        print(json.dumps({"threads": threads, "cluster": cluster, "smem_samples": cap, "ms": t,
+                                          "gsi_s": si_per_step / t / 1e6}), flush=True)
+                    except pkg.PathGuideError as ex:
+                        print(json.dumps({"threads": threads, "cluster": cluster, "smem_samples": cap,
+                                          "error": str(ex)}), flush=True)
+        return
+
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             step()
