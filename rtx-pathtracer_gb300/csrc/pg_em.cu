@@ -338,6 +338,9 @@ __device__ void mstep_apply(const EmArgs &a, EmShared<KMAX, NW> &S, int lane, ui
             neumaier_add(m.wh, m.wc, S.ow[c]);
         }
         const float Sx = m.sxh + m.sxc, Sy = m.syh + m.syc, Sz = m.szh + m.szc, W = m.wh + m.wc;
+        // Non-finite statistics (corrupt samples) keep the reference's arithmetic
+        // but are reported: the region is flagged and pg_sync_status fails.
+        if (!(isfinite(Sx) && isfinite(Sy) && isfinite(Sz) && isfinite(W))) S.nonfinite = 1;
         // parameterUpdate (VMMFactory.h:436-455)
         const float inv_wpn = cfg.v_prior * (float)K + 1.0f;
         const float wpn = 1.0f / inv_wpn;
