@@ -192,6 +192,8 @@ def main():
     ap.add_argument("--threads", type=int, default=0, help="threads per CTA (autotuned if 0)")
     ap.add_argument("--cluster", type=int, default=0, help="CTAs per large region (autotuned if 0)")
     ap.add_argument("--smem-samples", type=int, default=0)
+    ap.add_argument("--cpt", type=int, default=0, help="components per thread (8 or 16)")
+    ap.add_argument("--unroll", type=int, default=0)
     ap.add_argument("--sweep", action="store_true", help="time the tuning grid and print one line per point")
     ap.add_argument("--ref-seconds", type=float, default=None,
                     help="CPU seconds per reference step (default: ~100 s over the whole run)")
@@ -219,7 +221,8 @@ def main():
     n_samples = int(counts.sum())
     cfg = abi.forced_iterations(ITERS, num_initial_components=K)
     ctx = pkg.FitContext(cfg, max_regions=R)
-    ctx.set_tuning(threads_per_cta=args.threads, smem_samples=args.smem_samples, cluster_size=args.cluster)
+    ctx.set_tuning(threads_per_cta=args.threads, smem_samples=args.smem_samples, cluster_size=args.cluster,
+                   components_per_thread=args.cpt, unroll=args.unroll)
     stream = torch.cuda.Stream()
     dirw_h = torch.from_numpy(w["dirw"]).pin_memory()
     offs_h = torch.from_numpy(w["offsets"].view(np.int32)).pin_memory()
@@ -232,26 +235,27 @@ def main():
         ctx.fit(dirw_d, offs_d, R, abi.PG_FIT_INIT, stream=stream)
 
     if args.sweep:
-        for threads in (128, 256, 64):
-            for cluster in (1, 2, 4, 8, 16):
-                for cap in (0, 4096, 8192):
-                    try:
-                        ctx.set_tuning(threads_per_cta=threads, smem_samples=cap, cluster_size=cluster)
-                        with torch.cuda.stream(stream):
-                            step()
-                        torch.cuda.synchronize()
-                        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                        e0.record(stream)
-                        for _ in range(3):
-                            step()
-                        e1.record(stream)
-                        torch.cuda.synchronize()
-                        t = e0.elapsed_time(e1) / 3
-                        print(json.dumps({"threads": threads, "cluster": cluster, "smem_samples": cap, "ms": t,
-                                          "gsi_s": si_per_step / t / 1e6}), flush=True)
-                    except pkg.PathGuideError as ex:
-                        print(json.dumps({"threads": threads, "cluster": cluster, "smem_samples": cap,
-                                          "error": str(ex)}), flush=True)
+        grid = [(nt, cl, cap, cpt, u) for nt in (128, 256) for cpt in (8, 16) for u in (1, 2)
+                for cl in (1, 2, 4) for cap in (2048, 3072, 4096, 6144)]
+        for nt, cl, cap, cpt, u in grid:
+            point = {"threads": nt, "cluster": cl, "smem_samples": cap, "cpt": cpt, "unroll": u}
+            try:
+                ctx.set_tuning(threads_per_cta=nt, smem_samples=cap, cluster_size=cl, components_per_thread=cpt,
+                               unroll=u)
+                with torch.cuda.stream(stream):
+                    step()
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(3):
+                    step()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                t = e0.elapsed_time(e1) / 3
+                point.update(ms=t, gsi_s=si_per_step / t / 1e6)
+            except pkg.PathGuideError as ex:
+                point["error"] = str(ex)
+            print(json.dumps(point), flush=True)
         return
 
     with torch.cuda.stream(stream):

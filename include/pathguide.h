@@ -196,10 +196,12 @@ int pg_eval_loglik(pg_ctx *ctx, const float *dirw, const uint32_t *offsets,
 
 /* Tuning of the fit launch (chosen by the autotuner; 0 = default). */
 typedef struct pg_fit_tuning {
-    uint32_t threads_per_cta;     /* 64, 128, 256                            */
-    uint32_t smem_samples;        /* samples kept in shared memory per CTA   */
-    uint32_t ctas_per_sm;         /* resident CTAs per SM for the grid size  */
-    uint32_t cluster_size;        /* CTAs sharing one large region: 1..16    */
+    uint32_t threads_per_cta;       /* 128 or 256                               */
+    uint32_t smem_samples;          /* samples kept in shared memory per CTA    */
+    uint32_t ctas_per_sm;           /* cap on resident CTAs per SM (0: maximum) */
+    uint32_t cluster_size;          /* CTAs sharing one large region: 1..16     */
+    uint32_t components_per_thread; /* 8 or 16: K=16 mixtures use 2 or 1 threads per sample */
+    uint32_t unroll;                /* samples per loop trip: 1 or 2            */
 } pg_fit_tuning;
 int pg_set_fit_tuning(pg_ctx *ctx, const pg_fit_tuning *t);
 int pg_get_fit_tuning(const pg_ctx *ctx, pg_fit_tuning *t);

@@ -201,11 +201,14 @@ int pg_region_states_device(pg_ctx *ctx, pg_region_state **dev_out) {
 
 int pg_set_fit_tuning(pg_ctx *ctx, const pg_fit_tuning *t) {
     if (!ctx || !t) return PG_ERR_ARG;
-    if (t->threads_per_cta && t->threads_per_cta != 64 && t->threads_per_cta != 128 && t->threads_per_cta != 256)
-        return set_error(ctx, PG_ERR_ARG, "threads_per_cta must be 64, 128 or 256");
+    if (t->threads_per_cta && t->threads_per_cta != 128 && t->threads_per_cta != 256)
+        return set_error(ctx, PG_ERR_ARG, "threads_per_cta must be 128 or 256");
     if (t->ctas_per_sm > 32) return set_error(ctx, PG_ERR_ARG, "ctas_per_sm must be <= 32");
     if (t->smem_samples > 13000) return set_error(ctx, PG_ERR_ARG, "smem_samples must be <= 13000");
     if (t->cluster_size > 16) return set_error(ctx, PG_ERR_ARG, "cluster_size must be <= 16");
+    if (t->components_per_thread && t->components_per_thread != 8 && t->components_per_thread != 16)
+        return set_error(ctx, PG_ERR_ARG, "components_per_thread must be 8 or 16");
+    if (t->unroll > 2) return set_error(ctx, PG_ERR_ARG, "unroll must be 1 or 2");
     ctx->tuning = *t;
     return PG_OK;
 }

@@ -1,678 +1,8 @@
-// pg_em.cu - batched weighted EM fit of the per-region vMF mixtures.
-//
-// One persistent launch fits every region.  CTAs pull regions from a device
-// work queue ordered largest-first (LPT), so regions with uneven sample counts
-// and uneven iteration counts (per-region relative log-likelihood test) share
-// the GPU without a host round trip.  Per region, a CTA:
-//   1. stages the region's float4 {direction.xyz, weight} samples into shared
-//      memory with 1-D TMA bulk copies (cp.async.bulk, mbarrier completion) and
-//      keeps them resident across all EM iterations (regions larger than the
-//      staging capacity stream through L2 with 128-bit loads each iteration);
-//   2. E-step: every thread evaluates all K components for its samples with
-//      packed FP32x2 FMAs - the exponent of pi_k * vMF_k(d) is folded into one
-//      affine form kappa_k log2(e) mu_k.d + log2(pi_k norm_k) - kappa_k log2(e),
-//      clamped as the reference clamps cos(theta) <= 1, and fed to ex2 - then
-//      accumulates the sufficient statistics sum gamma w d and sum gamma w in
-//      FP32 registers;
-//   3. reduces them with a warp reduce-scatter (shuffles) and merges the warps'
-//      partial sums with Neumaier compensation;
-//   4. M-step in one warp (lane = component): priors, mean direction, and the
-//      kappa-from-mean-cosine inversion, whose 1 - r^2 cancellation is taken in
-//      FP64; the log-likelihood convergence test runs in FP64.
-//
-// Reference: VMMFactory::fit / updateFit (external/lightpmm/include/pmm/
-// VMMFactory.h:157-216, 305-362), computeSufficentStatsFromSamples (:497-536),
-// parameterUpdate (:436-455), priors (:385-420), computeSufficentStatsFromMixture
-// (:543-555); SoftAssignmentWeights (ParametricMixtureModel.h:501-522);
-// VMFKernel::pdf / calNormalization / meanCosineToKappa (VMFKernel.h:57-66,
-// 103-112, 620-628); the serial region loop of PathGuiding::update
-// (src/PathGuiding.cpp:281-288).
-#include <math.h>
-#include <stdio.h>
-
-#include <cooperative_groups.h>
-
-#include <algorithm>
-
-#include "pg_internal.cuh"
-
-namespace cg = cooperative_groups;
+// pg_em.cu - host side of the batched EM fit (C ABI entry points), the
+// largest-first region ordering and the log-likelihood evaluation kernel.
+#include "pg_em_kernels.cuh"
 
 namespace pg {
-
-struct EmArgs {
-    pg_region_state *states;
-    const float4 *dirw;
-    const uint32_t *offsets;
-    const uint32_t *order;
-    uint32_t n_regions;
-    uint32_t *work_counter;
-    uint32_t *error_word;
-    const float *init_table;
-    pg_fit_config cfg;
-    int mode;
-    uint32_t smem_cap;  // samples staged in shared memory
-    double *ll_out;     // eval mode only
-    uint32_t *large_counter;     // cluster work queue (largest regions)
-    const uint32_t *n_large;     // number of regions fitted by a whole cluster
-};
-
-template <int KMAX, int NW>
-struct EmShared {
-    float cax[KMAX], cay[KMAX], caz[KMAX], cc0[KMAX], ccm[KMAX];  // E-step constants
-    float w[16], mx[16], my[16], mz[16], kap[16], rr[16], nrm[16], em2k[16];
-    float osx[16], osy[16], osz[16], ow[16];  // statistics recovered from the prior mixture (updateFit)
-    float red[NW][4 * KMAX];
-    float red_ll[NW], red_sw[NW];
-    float part[8][KMAX];  // this CTA's compensated statistics (cluster mode)
-    float ptot[4];        // this CTA's log-likelihood and weight (hi, lo pairs)
-    double last_ll, abs_inv_last, ll;
-    float sample_weight, num_samples;
-    unsigned long long total;
-    uint32_t K, max_itr, item, stop, nonfinite;
-    unsigned long long bar;
-};
-
-// E-step constants of component c from the model held in shared memory.
-template <int KMAX, int NW>
-__device__ __forceinline__ void make_consts(EmShared<KMAX, NW> &S, int c, uint32_t K) {
-    if (c >= KMAX) return;
-    const float kl = S.kap[c] * kLog2e;
-    const float pn = S.w[c] * S.nrm[c];
-    const float lw = (c < (int)K && pn > 0.0f) ? log2f(pn) : -INFINITY;
-    S.cax[c] = kl * S.mx[c];
-    S.cay[c] = kl * S.my[c];
-    S.caz[c] = kl * S.mz[c];
-    S.cc0[c] = lw - kl;
-    S.ccm[c] = lw;
-}
-
-__device__ __forceinline__ void reset_component(float &w, float &mx, float &my, float &mz, float &k, float &r,
-                                                float &n, float &e) {
-    w = 0.0f;
-    mx = 0.0f;
-    my = 0.0f;
-    mz = 1.0f;
-    k = 0.0f;
-    r = 0.0f;
-    n = kInv4Pi;
-    e = 1.0f;
-}
-
-__device__ __forceinline__ void normalization(float kappa, float &norm, float &em2k) {
-    // VMFKernel::calNormalization (VMFKernel.h:620-628), with 1 - e^{-2k} as -expm1(-2k).
-    em2k = expf(-2.0f * kappa);
-    norm = kappa > 0.0f ? kappa / (kTwoPi * (-expm1f(-2.0f * kappa))) : kInv4Pi;
-}
-
-// Warp 0: load (or initialise) the region's mixture into shared memory.
-template <int KMAX, int NW>
-__device__ void load_model(const EmArgs &a, EmShared<KMAX, NW> &S, pg_region_state *st, int lane, uint32_t N) {
-    const pg_fit_config &cfg = a.cfg;
-    float w, mx, my, mz, k, r, n, e;
-    uint32_t K;
-    if (a.mode == PG_FIT_INIT) {
-        // VMMFactory::initialize (VMMFactory.h:132-148)
-        K = cfg.num_initial_components;
-        if (lane < (int)K) {
-            w = 1.0f / (float)K;
-            mx = a.init_table[lane];
-            my = a.init_table[16 + lane];
-            mz = a.init_table[32 + lane];
-            k = cfg.init_kappa < kVmfMinKappa ? 0.0f : cfg.init_kappa;
-            r = a.init_table[48 + lane];
-            normalization(k, n, e);
-        } else if (lane < 16) {
-            reset_component(w, mx, my, mz, k, r, n, e);
-        }
-        if (lane == 0) {
-            S.sample_weight = 0.0f;
-            S.num_samples = 0.0f;
-            S.total = 0ull;
-        }
-    } else {
-        K = st->k;
-        if (K > 16) K = 16;
-        if (lane < 16) {
-            w = st->weight[lane];
-            mx = st->mu_x[lane];
-            my = st->mu_y[lane];
-            mz = st->mu_z[lane];
-            k = st->kappa[lane];
-            r = st->r[lane];
-            n = st->norm[lane];
-            e = st->e_min2k[lane];
-            if (lane >= (int)K) reset_component(w, mx, my, mz, k, r, n, e);  // resetInactiveComponents
-        }
-        if (lane == 0) {
-            S.sample_weight = st->sample_weight;
-            S.num_samples = st->num_samples;
-            S.total = st->total_num_samples;
-        }
-    }
-    if (lane < 16) {
-        S.w[lane] = w;
-        S.mx[lane] = mx;
-        S.my[lane] = my;
-        S.mz[lane] = mz;
-        S.kap[lane] = k;
-        S.rr[lane] = r;
-        S.nrm[lane] = n;
-        S.em2k[lane] = e;
-        // computeSufficentStatsFromMixture (VMMFactory.h:543-555) for updateFit
-        float ow = 0.0f, osx = 0.0f, osy = 0.0f, osz = 0.0f;
-        if (a.mode == PG_FIT_UPDATE && lane < (int)K) {
-            const float inv_wpn = cfg.v_prior * (float)K + 1.0f;
-            const float wpn = 1.0f / inv_wpn;
-            const float wptn = cfg.v_prior * wpn;
-            const float rptw = cfg.r_prior * cfg.r_prior_weight;
-            const float wnp = (w > wptn) ? (w - wptn) * inv_wpn : 0.0f;
-            ow = wnp * st->sample_weight;
-            const float nn = (float)st->total_num_samples * w;
-            const float rr = (r * (nn + cfg.r_prior_weight) - rptw) / nn;
-            const float f = rr * ow;
-            osx = mx * f;
-            osy = my * f;
-            osz = mz * f;
-        }
-        S.ow[lane] = ow;
-        S.osx[lane] = osx;
-        S.osy[lane] = osy;
-        S.osz[lane] = osz;
-    }
-    __syncwarp();
-    make_consts(S, lane, K);
-    if (lane == 0) {
-        S.K = K;
-        // maxItr = 0 unless N > 2K (VMMFactory.h:175-177)
-        S.max_itr = (N > 2u * K) ? cfg.max_itr : 0u;
-        S.stop = 0;
-        S.nonfinite = 0;
-        S.last_ll = 0.0;
-        S.abs_inv_last = 0.0;
-        S.ll = 0.0;
-    }
-}
-
-// Warp reduce-scatter of M floats (M a multiple of 32): afterwards lane L
-// holds the warp sums of elements [L*M/32, (L+1)*M/32) in v[0 .. M/32).
-template <int M>
-__device__ __forceinline__ void reduce_scatter(float (&v)[M], int lane) {
-#pragma unroll
-    for (int s = 0; s < 5; ++s) {
-        const int o = 16 >> s;
-        const int half = M >> (s + 1);
-        const bool upper = (lane & o) != 0;
-#pragma unroll
-        for (int j = 0; j < half; ++j) {
-            const float send = upper ? v[j] : v[j + half];
-            const float keep = upper ? v[j + half] : v[j];
-            v[j] = keep + __shfl_xor_sync(0xffffffffu, send, o);
-        }
-    }
-}
-
-__device__ __forceinline__ float warp_sum(float x) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    return x;
-}
-
-// E-step over this thread's samples: accumulates sum v_k s d, sum v_k s with
-// s = w / p (p = mixture pdf), plus sum w log2 p and sum w over valid samples.
-template <int KMAX, bool kShared>
-__device__ __forceinline__ void estep(const float4 *__restrict__ src, uint32_t N, int tid, int nt,
-                                      const float2 (&AX)[KMAX / 2], const float2 (&AY)[KMAX / 2],
-                                      const float2 (&AZ)[KMAX / 2], const float2 (&C0)[KMAX / 2],
-                                      const float (&CM)[KMAX], float2 (&SX)[KMAX / 2], float2 (&SY)[KMAX / 2],
-                                      float2 (&SZ)[KMAX / 2], float2 (&SW)[KMAX / 2], float &ll, float &sw) {
-    for (uint32_t n = tid; n < N; n += nt) {
-        float4 s;
-        if (kShared)
-            s = src[n];
-        else
-            s = __ldg(src + n);
-        const float2 dx2 = make_float2(s.x, s.x);
-        const float2 dy2 = make_float2(s.y, s.y);
-        const float2 dz2 = make_float2(s.z, s.z);
-        float v[KMAX];
-        float2 p2 = make_float2(0.0f, 0.0f);
-#pragma unroll
-        for (int j = 0; j < KMAX / 2; ++j) {
-            float2 t = __ffma2_rn(AZ[j], dz2, C0[j]);
-            t = __ffma2_rn(AY[j], dy2, t);
-            t = __ffma2_rn(AX[j], dx2, t);
-            v[2 * j] = ex2_approx(fminf(t.x, CM[2 * j]));
-            v[2 * j + 1] = ex2_approx(fminf(t.y, CM[2 * j + 1]));
-            p2 = __fadd2_rn(p2, make_float2(v[2 * j], v[2 * j + 1]));
-        }
-        const float p = p2.x + p2.y;
-        const bool valid = p > kPmmEps;
-        const float wt = s.w;
-        const float sc = valid ? wt * rcp_approx(p) : 0.0f;
-        ll = valid ? fmaf(wt, lg2_approx(p), ll) : ll;
-        sw = valid ? sw + wt : sw;
-        const float2 sx = make_float2(sc * s.x, sc * s.x);
-        const float2 sy = make_float2(sc * s.y, sc * s.y);
-        const float2 sz = make_float2(sc * s.z, sc * s.z);
-        const float2 s2 = make_float2(sc, sc);
-#pragma unroll
-        for (int j = 0; j < KMAX / 2; ++j) {
-            const float2 vv = make_float2(v[2 * j], v[2 * j + 1]);
-            SX[j] = __ffma2_rn(vv, sx, SX[j]);
-            SY[j] = __ffma2_rn(vv, sy, SY[j]);
-            SZ[j] = __ffma2_rn(vv, sz, SZ[j]);
-            SW[j] = __ffma2_rn(vv, s2, SW[j]);
-        }
-    }
-}
-
-// Compensated statistics of one component: (hi, lo) pairs of sum gamma w d.xyz, sum gamma w.
-struct Stats4 {
-    float sxh, sxc, syh, syc, szh, szc, wh, wc;
-};
-
-__device__ __forceinline__ Stats4 stats_zero() { return Stats4{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}; }
-
-// Adds a compensated pair (h, l) into (s, c).
-__device__ __forceinline__ void neumaier_add2(float &s, float &c, float h, float l) {
-    neumaier_add(s, c, h);
-    c += l;
-}
-
-// Warp 0, lane c < KMAX: the CTA's statistics of component c, merged over warps.
-template <int KMAX, int NW>
-__device__ __forceinline__ Stats4 merge_warps(const EmShared<KMAX, NW> &S, int c) {
-    Stats4 m = stats_zero();
-#pragma unroll
-    for (int w = 0; w < NW; ++w) {
-        neumaier_add(m.sxh, m.sxc, S.red[w][c]);
-        neumaier_add(m.syh, m.syc, S.red[w][KMAX + c]);
-        neumaier_add(m.szh, m.szc, S.red[w][2 * KMAX + c]);
-        neumaier_add(m.wh, m.wc, S.red[w][3 * KMAX + c]);
-    }
-    return m;
-}
-
-// Lane 0: the CTA's log-likelihood (log2 units) and valid weight, merged over warps.
-template <int KMAX, int NW>
-__device__ __forceinline__ void merge_totals(const EmShared<KMAX, NW> &S, float &llh, float &llc, float &swh,
-                                             float &swc) {
-    llh = llc = swh = swc = 0.0f;
-#pragma unroll
-    for (int w = 0; w < NW; ++w) {
-        neumaier_add(llh, llc, S.red_ll[w]);
-        neumaier_add(swh, swc, S.red_sw[w]);
-    }
-}
-
-// Warp 0 of the CTA that owns the region: M-step of iteration `it` from merged
-// statistics m (lane c < KMAX) and region totals (lane 0).
-template <int KMAX, int NW>
-__device__ void mstep_apply(const EmArgs &a, EmShared<KMAX, NW> &S, int lane, uint32_t it, uint32_t N, Stats4 m,
-                            float llh, float llc, float swh, float swc) {
-    const pg_fit_config &cfg = a.cfg;
-    const uint32_t K = S.K;
-    if (lane == 0) {
-        S.ll = ((double)llh + (double)llc) * 0.6931471805599453;
-        if (it == 0) {
-            const float sum_w = swh + swc;
-            if (a.mode == PG_FIT_UPDATE) {
-                S.sample_weight += sum_w;
-                S.num_samples += (float)N;
-                S.total += N;
-            } else {
-                S.sample_weight = sum_w;
-                S.num_samples = (float)N;
-                S.total = N;
-            }
-        }
-    }
-    __syncwarp();
-    if (lane < KMAX) {
-        const int c = lane;
-        if (a.mode == PG_FIT_UPDATE) {
-            neumaier_add(m.sxh, m.sxc, S.osx[c]);
-            neumaier_add(m.syh, m.syc, S.osy[c]);
-            neumaier_add(m.szh, m.szc, S.osz[c]);
-            neumaier_add(m.wh, m.wc, S.ow[c]);
-        }
-        const float Sx = m.sxh + m.sxc, Sy = m.syh + m.syc, Sz = m.szh + m.szc, W = m.wh + m.wc;
-        // Non-finite statistics (corrupt samples) keep the reference's arithmetic
-        // but are reported: the region is flagged and pg_sync_status fails.
-        if (!(isfinite(Sx) && isfinite(Sy) && isfinite(Sz) && isfinite(W))) S.nonfinite = 1;
-        // parameterUpdate (VMMFactory.h:436-455)
-        const float inv_wpn = cfg.v_prior * (float)K + 1.0f;
-        const float wpn = 1.0f / inv_wpn;
-        const float wptn = cfg.v_prior * wpn;
-        const float mw = (W / S.sample_weight) * wpn + wptn;
-        const float rl2 = fmaf(Sx, Sx, fmaf(Sy, Sy, Sz * Sz));
-        const float rl = sqrtf(rl2);
-        float mx = S.mx[c], my = S.my[c], mz = S.mz[c];
-        if (rl > 0.0f) {
-            const float inv = 1.0f / rl;
-            mx = Sx * inv;
-            my = Sy * inv;
-            mz = Sz * inv;
-        }
-        const float avg = rl / W;
-        const float ns = (float)S.total * mw;
-        const float a_p = cfg.r_prior * cfg.r_prior_weight;
-        const float b_p = cfg.r_prior_weight;
-        float rp = (avg * ns + a_p) / (ns + b_p);
-        // 1 - r_p without cancellation: 1 - avg = (W^2 - |S|^2) / (W (W + |S|)),
-        // with W^2 - |S|^2 evaluated in FP64 from the compensated sums.
-        const double Wd = (double)m.wh + (double)m.wc;
-        const double Xd = (double)m.sxh + (double)m.sxc, Yd = (double)m.syh + (double)m.syc,
-                     Zd = (double)m.szh + (double)m.szc;
-        const double gap = fma(Wd, Wd, -fma(Xd, Xd, fma(Yd, Yd, Zd * Zd)));
-        const float one_m_avg = (float)gap / (W * (W + rl));
-        float one_m_rp = (ns * one_m_avg + (b_p - a_p)) / (ns + b_p);
-        // kappaToMeanCosine(maxKappa) (VMFKernel.h:47-55)
-        const float maxk = cfg.max_kappa;
-        float maxr, one_m_maxr;
-        if (maxk > 5.0f) {
-            one_m_maxr = 1.0f / maxk;
-            maxr = 1.0f - one_m_maxr;
-        } else {
-            maxr = 1.0f / tanhf(maxk) - 1.0f / maxk;
-            one_m_maxr = 1.0f - maxr;
-        }
-        if (!(rp < maxr) || !(one_m_rp > one_m_maxr)) {  // min(r, maxr); NaN takes the bound
-            rp = maxr;
-            one_m_rp = one_m_maxr;
-        }
-        // meanCosineToKappa (VMFKernel.h:57-66): (3r - r^3) / (1 - r^2)
-        float kap = rp * (3.0f - rp * rp) / (one_m_rp * (1.0f + rp));
-        const bool small = kap < kVmfMinKappa;
-        kap = small ? 0.0f : kap;
-        rp = small ? 0.0f : rp;
-        float nrm, em2k;
-        normalization(kap, nrm, em2k);
-        const bool active = c < (int)K;
-        float w_ = mw, r_ = rp;
-        if (!active) reset_component(w_, mx, my, mz, kap, r_, nrm, em2k);
-        if (!(isfinite(kap) && isfinite(mx) && isfinite(my) && isfinite(mz) && isfinite(w_))) S.nonfinite = 1;
-        S.w[c] = w_;
-        S.mx[c] = mx;
-        S.my[c] = my;
-        S.mz[c] = mz;
-        S.kap[c] = kap;
-        S.rr[c] = r_;
-        S.nrm[c] = nrm;
-        S.em2k[c] = em2k;
-        make_consts(S, c, K);
-    }
-    if (lane == 0) {
-        // relative log-likelihood test (VMMFactory.h:201-212), FP64
-        uint32_t stop = 0;
-        if (it >= cfg.min_itr) {
-            if (it > cfg.min_itr) {
-                const double rel = (S.ll - S.last_ll) * S.abs_inv_last;
-                if (rel < (double)cfg.rel_ll_threshold) stop = 1;
-            }
-            if (!stop) {
-                S.last_ll = S.ll;
-                S.abs_inv_last = 1.0 / fabs(S.ll);
-            }
-        }
-        S.stop = stop;
-    }
-}
-
-template <int KMAX, int NW>
-__device__ void store_model(const EmArgs &a, EmShared<KMAX, NW> &S, pg_region_state *st, int lane, uint32_t iters) {
-    if (lane < 16) {
-        float w, mx, my, mz, k, r, n, e;
-        if (lane < KMAX) {
-            w = S.w[lane];
-            mx = S.mx[lane];
-            my = S.my[lane];
-            mz = S.mz[lane];
-            k = S.kap[lane];
-            r = S.rr[lane];
-            n = S.nrm[lane];
-            e = S.em2k[lane];
-        } else {
-            reset_component(w, mx, my, mz, k, r, n, e);
-        }
-        st->weight[lane] = w;
-        st->mu_x[lane] = mx;
-        st->mu_y[lane] = my;
-        st->mu_z[lane] = mz;
-        st->kappa[lane] = k;
-        st->r[lane] = r;
-        st->norm[lane] = n;
-        st->e_min2k[lane] = e;
-        if (a.mode == PG_FIT_INIT) {
-            st->distance[lane] = INFINITY;
-            st->dist_sum_w[lane] = 0.0f;
-        }
-    }
-    if (lane == 0) {
-        const uint32_t prev_iters = (a.mode == PG_FIT_INIT) ? 0u : st->num_em_iterations;
-        st->k = S.K;
-        st->sample_weight = S.sample_weight;
-        st->num_samples = S.num_samples;
-        st->total_num_samples = S.total;
-        st->num_em_iterations = prev_iters + iters;
-        st->iters_last = iters;
-        st->ll_last = (float)S.ll;
-        uint32_t flags = (a.mode == PG_FIT_INIT) ? 0u : st->flags;
-        flags &= ~PG_STATE_NONFINITE;
-        if (iters > 0) flags |= PG_STATE_FITTED;
-        if (S.nonfinite) flags |= PG_STATE_NONFINITE;
-        st->flags = flags;
-        if (a.mode == PG_FIT_INIT) {
-            for (int i = 0; i < 3; ++i) {
-                st->parallax_mean[i] = 0.0f;
-                st->last_parallax_mean[i] = 0.0f;
-            }
-        }
-        if (S.nonfinite) atomicOr(a.error_word, PG_DEV_ERR_NUMERIC);
-    }
-}
-
-// Copies the E-step constants, K, the iteration bound and the stop flag from
-// the shared memory of cluster rank 0 (warp 0 of a non-zero rank).
-template <int KMAX, int NW>
-__device__ __forceinline__ void pull_consts(cg::cluster_group &cluster, EmShared<KMAX, NW> &S, int lane) {
-    EmShared<KMAX, NW> *R0 = cluster.map_shared_rank(&S, 0);
-    if (lane < KMAX) {
-        S.cax[lane] = R0->cax[lane];
-        S.cay[lane] = R0->cay[lane];
-        S.caz[lane] = R0->caz[lane];
-        S.cc0[lane] = R0->cc0[lane];
-        S.ccm[lane] = R0->ccm[lane];
-    }
-    if (lane == 0) {
-        S.K = R0->K;
-        S.max_itr = R0->max_itr;
-        S.stop = R0->stop;
-    }
-}
-
-// One region (or, in a cluster, this CTA's slice of one region): stage the
-// samples, iterate E-step / reduction / M-step, store the mixture.
-template <int KMAX, int NT, bool kCluster>
-__device__ void process_region(const EmArgs &a, EmShared<KMAX, NT / 32> &S, float4 *s_samp, uint64_t *bar,
-                               uint32_t &phase, uint32_t item, cg::cluster_group &cluster) {
-    constexpr int NW = NT / 32;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t crank = kCluster ? cluster.block_rank() : 0u;
-    const uint32_t csize = kCluster ? cluster.num_blocks() : 1u;
-    const uint32_t r = a.order[item];
-    const uint32_t b = a.offsets[r], e = a.offsets[r + 1];
-    const uint32_t N = e > b ? e - b : 0u;
-    pg_region_state *st = a.states + r;
-    // this CTA's slice [sb, se)
-    const uint32_t chunk = (N + csize - 1) / csize;
-    const uint32_t sb = min(e, b + crank * chunk);
-    const uint32_t se = min(e, sb + chunk);
-    const uint32_t n_local = se - sb;
-    const bool owner = crank == 0;
-    if (owner && warp == 0) load_model(a, S, st, lane, N);
-    if (kCluster) {
-        cluster.sync();
-        if (!owner && warp == 0) pull_consts(cluster, S, lane);
-    }
-    __syncthreads();
-    const uint32_t max_itr = S.max_itr;
-    const bool resident = n_local <= a.smem_cap;
-    bool ok = true;
-    if (resident && max_itr > 0 && n_local > 0) {
-        if (tid == 0) {
-            fence_proxy_async_smem();
-            const uint32_t bytes = n_local * 16u;
-            mbar_arrive_expect_tx(bar, bytes);
-            const char *src = reinterpret_cast<const char *>(a.dirw + sb);
-            char *dst = reinterpret_cast<char *>(s_samp);
-            for (uint32_t off = 0; off < bytes; off += 32768u) {
-                const uint32_t ch = min(32768u, bytes - off);
-                tma_bulk_g2s(dst + off, src + off, ch, bar);
-            }
-        }
-        ok = mbar_wait_bounded(bar, phase, a.error_word);
-        phase ^= 1u;
-    }
-    // A timed-out copy leaves the slice's statistics at zero; the error word reports it.
-    uint32_t it = 0;
-    for (; it < max_itr; ++it) {
-        float2 AX[KMAX / 2], AY[KMAX / 2], AZ[KMAX / 2], C0[KMAX / 2];
-        float CM[KMAX];
-#pragma unroll
-        for (int j = 0; j < KMAX / 2; ++j) {
-            AX[j] = make_float2(S.cax[2 * j], S.cax[2 * j + 1]);
-            AY[j] = make_float2(S.cay[2 * j], S.cay[2 * j + 1]);
-            AZ[j] = make_float2(S.caz[2 * j], S.caz[2 * j + 1]);
-            C0[j] = make_float2(S.cc0[2 * j], S.cc0[2 * j + 1]);
-            CM[2 * j] = S.ccm[2 * j];
-            CM[2 * j + 1] = S.ccm[2 * j + 1];
-        }
-        float2 SX[KMAX / 2], SY[KMAX / 2], SZ[KMAX / 2], SW[KMAX / 2];
-#pragma unroll
-        for (int j = 0; j < KMAX / 2; ++j) SX[j] = SY[j] = SZ[j] = SW[j] = make_float2(0.0f, 0.0f);
-        float ll = 0.0f, sw = 0.0f;
-        if (ok) {
-            if (resident)
-                estep<KMAX, true>(s_samp, n_local, tid, NT, AX, AY, AZ, C0, CM, SX, SY, SZ, SW, ll, sw);
-            else
-                estep<KMAX, false>(a.dirw + sb, n_local, tid, NT, AX, AY, AZ, C0, CM, SX, SY, SZ, SW, ll, sw);
-        }
-        float f[4 * KMAX];
-#pragma unroll
-        for (int j = 0; j < KMAX / 2; ++j) {
-            f[2 * j] = SX[j].x;
-            f[2 * j + 1] = SX[j].y;
-            f[KMAX + 2 * j] = SY[j].x;
-            f[KMAX + 2 * j + 1] = SY[j].y;
-            f[2 * KMAX + 2 * j] = SZ[j].x;
-            f[2 * KMAX + 2 * j + 1] = SZ[j].y;
-            f[3 * KMAX + 2 * j] = SW[j].x;
-            f[3 * KMAX + 2 * j + 1] = SW[j].y;
-        }
-        reduce_scatter<4 * KMAX>(f, lane);
-        constexpr int Q = (4 * KMAX) / 32;
-#pragma unroll
-        for (int q = 0; q < Q; ++q) S.red[warp][lane * Q + q] = f[q];
-        ll = warp_sum(ll);
-        sw = warp_sum(sw);
-        if (lane == 0) {
-            S.red_ll[warp] = ll;
-            S.red_sw[warp] = sw;
-        }
-        __syncthreads();
-        if (!kCluster) {
-            if (warp == 0) {
-                Stats4 m = stats_zero();
-                if (lane < KMAX) m = merge_warps(S, lane);
-                float llh = 0.f, llc = 0.f, swh = 0.f, swc = 0.f;
-                if (lane == 0) merge_totals(S, llh, llc, swh, swc);
-                mstep_apply(a, S, lane, it, N, m, llh, llc, swh, swc);
-            }
-            __syncthreads();
-        } else {
-            // CTA partial -> own shared memory; rank 0 merges the cluster's partials.
-            if (warp == 0) {
-                if (lane < KMAX) {
-                    const Stats4 m = merge_warps(S, lane);
-                    S.part[0][lane] = m.sxh;
-                    S.part[1][lane] = m.sxc;
-                    S.part[2][lane] = m.syh;
-                    S.part[3][lane] = m.syc;
-                    S.part[4][lane] = m.szh;
-                    S.part[5][lane] = m.szc;
-                    S.part[6][lane] = m.wh;
-                    S.part[7][lane] = m.wc;
-                }
-                if (lane == 0) merge_totals(S, S.ptot[0], S.ptot[1], S.ptot[2], S.ptot[3]);
-            }
-            cluster.sync();
-            if (owner && warp == 0) {
-                Stats4 m = stats_zero();
-                float llh = 0.f, llc = 0.f, swh = 0.f, swc = 0.f;
-                for (uint32_t q = 0; q < csize; ++q) {
-                    const EmShared<KMAX, NW> *P = cluster.map_shared_rank(&S, q);
-                    if (lane < KMAX) {
-                        neumaier_add2(m.sxh, m.sxc, P->part[0][lane], P->part[1][lane]);
-                        neumaier_add2(m.syh, m.syc, P->part[2][lane], P->part[3][lane]);
-                        neumaier_add2(m.szh, m.szc, P->part[4][lane], P->part[5][lane]);
-                        neumaier_add2(m.wh, m.wc, P->part[6][lane], P->part[7][lane]);
-                    }
-                    if (lane == 0) {
-                        neumaier_add2(llh, llc, P->ptot[0], P->ptot[1]);
-                        neumaier_add2(swh, swc, P->ptot[2], P->ptot[3]);
-                    }
-                }
-                mstep_apply(a, S, lane, it, N, m, llh, llc, swh, swc);
-            }
-            cluster.sync();
-            if (!owner && warp == 0) pull_consts(cluster, S, lane);
-            __syncthreads();
-        }
-        if (S.stop) break;
-    }
-    if (owner && warp == 0) store_model(a, S, st, lane, it);
-    __syncthreads();
-}
-
-template <int KMAX, int NT, bool kCluster>
-__global__ void __launch_bounds__(NT) em_fit_kernel(EmArgs a) {
-    constexpr int NW = NT / 32;
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    float4 *s_samp = reinterpret_cast<float4 *>(smem_raw);
-    EmShared<KMAX, NW> &S = *reinterpret_cast<EmShared<KMAX, NW> *>(smem_raw + (size_t)a.smem_cap * 16);
-    const int tid = threadIdx.x;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(&S.bar);
-    cg::cluster_group cluster = cg::this_cluster();
-    if (tid == 0) {
-        mbar_init(bar, 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
-    uint32_t phase = 0;
-    const uint32_t n_large = kCluster ? *a.n_large : 0u;
-    if constexpr (kCluster) {
-        // Phase 1: the largest regions, each shared by all CTAs of a cluster.
-        for (;;) {
-            if (cluster.block_rank() == 0 && tid == 0) S.item = atomicAdd(a.large_counter, 1u);
-            cluster.sync();
-            const uint32_t item = *cluster.map_shared_rank(&S.item, 0);
-            cluster.sync();
-            if (item >= n_large) break;
-            process_region<KMAX, NT, true>(a, S, s_samp, bar, phase, item, cluster);
-        }
-    }
-    // Phase 2: the remaining regions, one CTA each, largest first.
-    for (;;) {
-        if (tid == 0) S.item = n_large + atomicAdd(a.work_counter, 1u);
-        __syncthreads();
-        const uint32_t item = S.item;
-        __syncthreads();
-        if (item >= a.n_regions) break;
-        process_region<KMAX, NT, false>(a, S, s_samp, bar, phase, item, cluster);
-    }
-}
 
 // Weighted log-likelihood of each region under its current mixture (FP32
 // E-step arithmetic, compensated merge, FP64 result).
@@ -791,66 +121,6 @@ __global__ void __launch_bounds__(1024) order_regions_kernel(const uint32_t *off
     }
 }
 
-template <int KMAX, int NT>
-static size_t fit_smem_bytes(uint32_t cap) {
-    return (size_t)cap * 16 + sizeof(EmShared<KMAX, NT / 32>);
-}
-
-template <int KMAX, int NT>
-static int launch_fit(pg_ctx *ctx, const EmArgs &args, cudaStream_t s, uint32_t ctas_per_sm, uint32_t cluster) {
-    const size_t smem = fit_smem_bytes<KMAX, NT>(args.smem_cap);
-    cudaLaunchConfig_t lc = {};
-    cudaLaunchAttribute attr[1];
-    lc.blockDim = dim3(NT, 1, 1);
-    lc.dynamicSmemBytes = smem;
-    lc.stream = s;
-    int st;
-    if (cluster > 1) {
-        auto kern = em_fit_kernel<KMAX, NT, true>;
-        st = check_cuda(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                        "em_fit smem attribute");
-        if (st) return st;
-        if (cluster > 8) {
-            st = check_cuda(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1),
-                            "em_fit cluster attribute");
-            if (st) return st;
-        }
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = cluster;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        lc.attrs = attr;
-        lc.numAttrs = 1;
-        lc.gridDim = dim3(cluster * (uint32_t)ctx->sm_count, 1, 1);
-        int nclusters = 0;
-        st = check_cuda(ctx, cudaOccupancyMaxActiveClusters(&nclusters, kern, &lc), "em_fit cluster occupancy");
-        if (st) return st;
-        if (nclusters < 1) return set_error(ctx, PG_ERR_ARG, "em_fit: cluster configuration does not fit");
-        uint32_t grid = (uint32_t)nclusters * cluster;
-        if (ctas_per_sm) grid = std::min<uint32_t>(grid, ctas_per_sm * (uint32_t)ctx->sm_count / cluster * cluster);
-        if (grid < cluster) grid = cluster;
-        lc.gridDim = dim3(grid, 1, 1);
-        st = check_cuda(ctx, cudaLaunchKernelEx(&lc, kern, args), "em_fit launch");
-    } else {
-        auto kern = em_fit_kernel<KMAX, NT, false>;
-        st = check_cuda(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                        "em_fit smem attribute");
-        if (st) return st;
-        int occ = 0;
-        st = check_cuda(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, NT, smem), "em_fit occupancy");
-        if (st) return st;
-        if (occ < 1) return set_error(ctx, PG_ERR_ARG, "em_fit: launch configuration does not fit on an SM");
-        const uint32_t per_sm = ctas_per_sm ? std::min<uint32_t>(ctas_per_sm, (uint32_t)occ) : (uint32_t)occ;
-        uint32_t grid = per_sm * (uint32_t)ctx->sm_count;
-        if (grid > args.n_regions) grid = args.n_regions;
-        if (grid == 0) grid = 1;
-        lc.gridDim = dim3(grid, 1, 1);
-        lc.numAttrs = 0;
-        st = check_cuda(ctx, cudaLaunchKernelEx(&lc, kern, args), "em_fit launch");
-    }
-    return st;
-}
-
 }  // namespace pg
 
 using namespace pg;
@@ -883,9 +153,8 @@ int pg_fit_regions(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint
     st = check_cuda(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(uint32_t) * 4, s), "queue reset");
     if (st) return st;
     const pg_fit_tuning &t = ctx->tuning;
-    const uint32_t nt = t.threads_per_cta ? t.threads_per_cta : 128u;
-    const uint32_t cluster = t.cluster_size ? t.cluster_size : 8u;
-    const uint32_t cap = t.smem_samples ? t.smem_samples : 6144u;
+    const uint32_t cluster = t.cluster_size ? t.cluster_size : 2u;
+    const uint32_t cap = t.smem_samples ? t.smem_samples : 3072u;
     // A region goes to a whole cluster when it has more than cluster x 2048 samples.
     const uint32_t large_threshold = cluster > 1 ? std::max<uint32_t>(cluster * 2048u, cap) : 0xFFFFFFFFu;
     order_regions_kernel<<<1, 1024, 0, s>>>(offsets, n_regions, ctx->d_order, large_threshold, ctx->d_counters + 3);
@@ -910,16 +179,7 @@ int pg_fit_regions(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint
     // The component count of an existing state is read from the state; size
     // for the widest case unless the mixtures are initialised here.
     const bool wide = (mode == PG_FIT_INIT) ? (K > 8) : true;
-    const uint32_t cps = t.ctas_per_sm;
-    if (!wide) {
-        if (nt == 64) st = launch_fit<8, 64>(ctx, args, s, cps, cluster);
-        else if (nt == 256) st = launch_fit<8, 256>(ctx, args, s, cps, cluster);
-        else st = launch_fit<8, 128>(ctx, args, s, cps, cluster);
-    } else {
-        if (nt == 64) st = launch_fit<16, 64>(ctx, args, s, cps, cluster);
-        else if (nt == 256) st = launch_fit<16, 256>(ctx, args, s, cps, cluster);
-        else st = launch_fit<16, 128>(ctx, args, s, cps, cluster);
-    }
+    st = wide ? launch_fit_k16(ctx, args, s, t, cluster) : launch_fit_k8(ctx, args, s, t, cluster);
     if (st) return st;
     ctx->last_launches = 2;
     return PG_OK;

@@ -85,7 +85,8 @@ def test_fit_within_stated_tolerance_of_reference(name, cuda, pkg, golden, abi):
 
 
 @pytest.mark.parametrize("K", [8, 16])
-@pytest.mark.parametrize("tuning", [{}, {"threads_per_cta": 64}, {"threads_per_cta": 256},
+@pytest.mark.parametrize("tuning", [{}, {"components_per_thread": 16}, {"unroll": 2}, {"threads_per_cta": 256},
+                                    {"threads_per_cta": 256, "components_per_thread": 16, "unroll": 2},
                                     {"smem_samples": 256}, {"cluster_size": 1}, {"cluster_size": 2},
                                     {"cluster_size": 16}, {"cluster_size": 4, "smem_samples": 512}])
 def test_uneven_batch_and_launch_shapes(K, tuning, cuda, pkg, oracle, abi, workloads):
