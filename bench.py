@@ -112,9 +112,12 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_workload(small: bool):
+def make_workload(small: bool, args=None):
     import __graft_entry__ as entry
     wl = entry.load_submodule("workloads")
+    if args is not None and (args.regions or args.median or args.sigma >= 0):
+        return wl.fit_batched(seed=3, n_regions=args.regions or 4096, median=args.median or 2048.0,
+                              sigma=args.sigma if args.sigma >= 0 else 1.0)
     if small:
         return wl.fit_batched(seed=3, n_regions=512)
     return wl.fit_batched(seed=3)
@@ -194,6 +197,10 @@ def main():
     ap.add_argument("--smem-samples", type=int, default=0)
     ap.add_argument("--cpt", type=int, default=0, help="components per thread (8 or 16)")
     ap.add_argument("--unroll", type=int, default=0)
+    ap.add_argument("--large", type=int, default=0, help="samples above which a cluster shares a region")
+    ap.add_argument("--regions", type=int, default=0, help="override the region count (experiments)")
+    ap.add_argument("--median", type=float, default=0.0, help="override the median region size")
+    ap.add_argument("--sigma", type=float, default=-1.0, help="override the region-size sigma")
     ap.add_argument("--sweep", action="store_true", help="time the tuning grid and print one line per point")
     ap.add_argument("--ref-seconds", type=float, default=None,
                     help="CPU seconds per reference step (default: ~100 s over the whole run)")
@@ -215,14 +222,14 @@ def main():
     torch.cuda.set_device(local)
     pkg = entry.load_package()
     abi = pkg.abi
-    w = make_workload(args.small)
+    w = make_workload(args.small, args)
     R = len(w["offsets"]) - 1
     counts = np.diff(w["offsets"].astype(np.int64))
     n_samples = int(counts.sum())
     cfg = abi.forced_iterations(ITERS, num_initial_components=K)
     ctx = pkg.FitContext(cfg, max_regions=R)
     ctx.set_tuning(threads_per_cta=args.threads, smem_samples=args.smem_samples, cluster_size=args.cluster,
-                   components_per_thread=args.cpt, unroll=args.unroll)
+                   components_per_thread=args.cpt, unroll=args.unroll, large_threshold=args.large)
     stream = torch.cuda.Stream()
     dirw_h = torch.from_numpy(w["dirw"]).pin_memory()
     offs_h = torch.from_numpy(w["offsets"].view(np.int32)).pin_memory()
@@ -235,13 +242,13 @@ def main():
         ctx.fit(dirw_d, offs_d, R, abi.PG_FIT_INIT, stream=stream)
 
     if args.sweep:
-        grid = [(nt, cl, cap, cpt, u) for nt in (128, 256) for cpt in (8, 16) for u in (1, 2)
-                for cl in (1, 2, 4) for cap in (2048, 3072, 4096, 6144)]
-        for nt, cl, cap, cpt, u in grid:
-            point = {"threads": nt, "cluster": cl, "smem_samples": cap, "cpt": cpt, "unroll": u}
+        grid = [(128, cl, cap, cpt, 2, T) for cpt in (16, 8) for cl in (2, 4, 8, 16)
+                for cap in (3072, 6144) for T in (0, 2048, 12288)]
+        for nt, cl, cap, cpt, u, T in grid:
+            point = {"threads": nt, "cluster": cl, "smem_samples": cap, "cpt": cpt, "unroll": u, "large": T}
             try:
                 ctx.set_tuning(threads_per_cta=nt, smem_samples=cap, cluster_size=cl, components_per_thread=cpt,
-                               unroll=u)
+                               unroll=u, large_threshold=T)
                 with torch.cuda.stream(stream):
                     step()
                 torch.cuda.synchronize()

@@ -202,6 +202,8 @@ typedef struct pg_fit_tuning {
     uint32_t cluster_size;          /* CTAs sharing one large region: 1..16     */
     uint32_t components_per_thread; /* 8 or 16: K=16 mixtures use 2 or 1 threads per sample */
     uint32_t unroll;                /* samples per loop trip: 1 or 2            */
+    uint32_t large_threshold;       /* regions with more samples are shared by a
+                                       cluster (0: smem_samples)                */
 } pg_fit_tuning;
 int pg_set_fit_tuning(pg_ctx *ctx, const pg_fit_tuning *t);
 int pg_get_fit_tuning(const pg_ctx *ctx, pg_fit_tuning *t);

@@ -156,7 +156,9 @@ int pg_fit_regions(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint
     const uint32_t cluster = t.cluster_size ? t.cluster_size : 2u;
     const uint32_t cap = t.smem_samples ? t.smem_samples : 3072u;
     // A region goes to a whole cluster when it has more than cluster x 2048 samples.
-    const uint32_t large_threshold = cluster > 1 ? std::max<uint32_t>(cluster * 2048u, cap) : 0xFFFFFFFFu;
+    // Regions with more samples than the threshold are shared by a cluster.
+    const uint32_t large_threshold =
+        cluster > 1 ? (t.large_threshold ? t.large_threshold : cap) : 0xFFFFFFFFu;
     order_regions_kernel<<<1, 1024, 0, s>>>(offsets, n_regions, ctx->d_order, large_threshold, ctx->d_counters + 3);
     st = check_cuda(ctx, cudaGetLastError(), "order_regions launch");
     if (st) return st;

@@ -82,7 +82,7 @@ __device__ __forceinline__ void make_consts(EmShared<KMAX, NW> &S, int c, uint32
     if (c >= KMAX) return;
     const float kl = S.kap[c] * kLog2e;
     const float pn = S.w[c] * S.nrm[c];
-    const float lw = (c < (int)K && pn > 0.0f) ? log2f(pn) : -INFINITY;
+    const float lw = (c < (int)K && pn > 0.0f) ? lg2_approx(pn) : -INFINITY;
     S.cax[c] = kl * S.mx[c];
     S.cay[c] = kl * S.my[c];
     S.caz[c] = kl * S.mz[c];
@@ -103,9 +103,15 @@ __device__ __forceinline__ void reset_component(float &w, float &mx, float &my, 
 }
 
 __device__ __forceinline__ void normalization(float kappa, float &norm, float &em2k) {
-    // VMFKernel::calNormalization (VMFKernel.h:620-628), with 1 - e^{-2k} as -expm1(-2k).
-    em2k = expf(-2.0f * kappa);
-    norm = kappa > 0.0f ? kappa / (kTwoPi * (-expm1f(-2.0f * kappa))) : kInv4Pi;
+    // VMFKernel::calNormalization (VMFKernel.h:620-628), with 1 - e^{-2k} as -expm1(-2k);
+    // for kappa >= 10, e^{-2k} < 2.1e-9 and 1 - e^{-2k} rounds to 1 in FP32.
+    if (kappa >= 10.0f) {
+        em2k = ex2_approx(-2.0f * kLog2e * kappa);
+        norm = kappa * (1.0f / kTwoPi);
+    } else {
+        em2k = expf(-2.0f * kappa);
+        norm = kappa > 0.0f ? kappa / (kTwoPi * (-expm1f(-2.0f * kappa))) : kInv4Pi;
+    }
 }
 
 // Warp 0: load (or initialise) the region's mixture into shared memory.
@@ -378,29 +384,32 @@ __device__ void mstep_apply(const EmArgs &a, EmShared<KMAX, NW> &S, int lane, ui
         const float inv_wpn = cfg.v_prior * (float)K + 1.0f;
         const float wpn = 1.0f / inv_wpn;
         const float wptn = cfg.v_prior * wpn;
-        const float mw = (W / S.sample_weight) * wpn + wptn;
+        // Quotients use the fast reciprocal (within 2 ulp): the M-step is on the
+        // critical path of every iteration.
+        const float mw = __fdividef(W, S.sample_weight) * wpn + wptn;
         const float rl2 = fmaf(Sx, Sx, fmaf(Sy, Sy, Sz * Sz));
-        const float rl = sqrtf(rl2);
+        const float irl = rsqrtf(rl2);
+        const float rl = rl2 > 0.0f ? rl2 * irl : 0.0f;
         float mx = S.mx[c], my = S.my[c], mz = S.mz[c];
-        if (rl > 0.0f) {
-            const float inv = 1.0f / rl;
-            mx = Sx * inv;
-            my = Sy * inv;
-            mz = Sz * inv;
+        if (rl2 > 0.0f) {
+            mx = Sx * irl;
+            my = Sy * irl;
+            mz = Sz * irl;
         }
-        const float avg = rl / W;
+        const float avg = __fdividef(rl, W);
         const float ns = (float)S.total * mw;
         const float a_p = cfg.r_prior * cfg.r_prior_weight;
         const float b_p = cfg.r_prior_weight;
-        float rp = (avg * ns + a_p) / (ns + b_p);
+        const float inv_nb = __fdividef(1.0f, ns + b_p);
+        float rp = (avg * ns + a_p) * inv_nb;
         // 1 - r_p without cancellation: 1 - avg = (W^2 - |S|^2) / (W (W + |S|)),
         // with W^2 - |S|^2 evaluated in FP64 from the compensated sums.
         const double Wd = (double)m.wh + (double)m.wc;
         const double Xd = (double)m.sxh + (double)m.sxc, Yd = (double)m.syh + (double)m.syc,
                      Zd = (double)m.szh + (double)m.szc;
         const double gap = fma(Wd, Wd, -fma(Xd, Xd, fma(Yd, Yd, Zd * Zd)));
-        const float one_m_avg = (float)gap / (W * (W + rl));
-        float one_m_rp = (ns * one_m_avg + (b_p - a_p)) / (ns + b_p);
+        const float one_m_avg = __fdividef((float)gap, W * (W + rl));
+        float one_m_rp = (ns * one_m_avg + (b_p - a_p)) * inv_nb;
         // kappaToMeanCosine(maxKappa) (VMFKernel.h:47-55)
         const float maxk = cfg.max_kappa;
         float maxr, one_m_maxr;
@@ -416,7 +425,7 @@ __device__ void mstep_apply(const EmArgs &a, EmShared<KMAX, NW> &S, int lane, ui
             one_m_rp = one_m_maxr;
         }
         // meanCosineToKappa (VMFKernel.h:57-66): (3r - r^3) / (1 - r^2)
-        float kap = rp * (3.0f - rp * rp) / (one_m_rp * (1.0f + rp));
+        float kap = __fdividef(rp * (3.0f - rp * rp), one_m_rp * (1.0f + rp));
         const bool small = kap < kVmfMinKappa;
         kap = small ? 0.0f : kap;
         rp = small ? 0.0f : rp;
@@ -441,13 +450,12 @@ __device__ void mstep_apply(const EmArgs &a, EmShared<KMAX, NW> &S, int lane, ui
         uint32_t stop = 0;
         if (it >= cfg.min_itr) {
             if (it > cfg.min_itr) {
-                const double rel = (S.ll - S.last_ll) * S.abs_inv_last;
-                if (rel < (double)cfg.rel_ll_threshold) stop = 1;
+                // (LL - last) * (1/|last|) < thr, evaluated without the division:
+                // (LL - last) < thr * |last| gives the same decision for every
+                // finite or infinite operand (|last| = 0 included).
+                if ((S.ll - S.last_ll) < (double)cfg.rel_ll_threshold * fabs(S.last_ll)) stop = 1;
             }
-            if (!stop) {
-                S.last_ll = S.ll;
-                S.abs_inv_last = 1.0 / fabs(S.ll);
-            }
+            if (!stop) S.last_ll = S.ll;
         }
         S.stop = stop;
     }
