@@ -153,12 +153,13 @@ int pg_fit_regions(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint
     st = check_cuda(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(uint32_t) * 4, s), "queue reset");
     if (st) return st;
     const pg_fit_tuning &t = ctx->tuning;
+    // Defaults: the best point of the tuning sweep on the 4096-region K=16
+    // workload (pairs of CTAs share regions above 12288 samples, 6144 samples
+    // staged per CTA, one thread per sample, two samples per loop trip).
     const uint32_t cluster = t.cluster_size ? t.cluster_size : 2u;
-    const uint32_t cap = t.smem_samples ? t.smem_samples : 3072u;
-    // A region goes to a whole cluster when it has more than cluster x 2048 samples.
-    // Regions with more samples than the threshold are shared by a cluster.
+    const uint32_t cap = t.smem_samples ? t.smem_samples : 6144u;
     const uint32_t large_threshold =
-        cluster > 1 ? (t.large_threshold ? t.large_threshold : cap) : 0xFFFFFFFFu;
+        cluster > 1 ? (t.large_threshold ? t.large_threshold : 12288u) : 0xFFFFFFFFu;
     order_regions_kernel<<<1, 1024, 0, s>>>(offsets, n_regions, ctx->d_order, large_threshold, ctx->d_counters + 3);
     st = check_cuda(ctx, cudaGetLastError(), "order_regions launch");
     if (st) return st;
