@@ -787,6 +787,76 @@ static int launch_fit(pg_ctx *ctx, const EmArgs &args, cudaStream_t s, uint32_t 
 }
 
 
+// Orders region ids by sample count, largest first (LPT), with a stable
+// counting sort over 128 logarithmic size buckets (4 per octave).  One CTA of
+// 1024 threads; n_regions of any size.  NB = 128 buckets.
+template <int NB>
+__global__ void __launch_bounds__(1024) order_regions_kernel(const uint32_t *offsets, uint32_t n_regions,
+                                                             uint32_t *order, uint32_t large_threshold,
+                                                             uint32_t *n_large_out) {
+    __shared__ uint32_t hist[NB];
+    __shared__ uint32_t base[NB];
+    __shared__ uint32_t warp_cnt[32][NB];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    auto bucket_of = [&](uint32_t r) -> int {
+        const uint32_t n = offsets[r + 1] - offsets[r];
+        // descending: bucket 0 = largest
+        const float l = log2f((float)n + 1.0f) * 4.0f;
+        int k = (int)l;
+        k = k < 0 ? 0 : (k > NB - 1 ? NB - 1 : k);
+        return NB - 1 - k;
+    };
+    for (int i = tid; i < NB; i += blockDim.x) hist[i] = 0;
+    __syncthreads();
+    for (uint32_t r = tid; r < n_regions; r += blockDim.x) atomicAdd(&hist[bucket_of(r)], 1u);
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t acc = 0;
+        for (int i = 0; i < NB; ++i) {
+            base[i] = acc;
+            acc += hist[i];
+        }
+        // regions whose size bucket is at or above the threshold's bucket come
+        // first in the order and are fitted by a whole cluster
+        uint32_t nl = 0;
+        if (large_threshold != 0xFFFFFFFFu) {
+            const float l = log2f((float)large_threshold + 1.0f) * 4.0f;
+            int k = (int)l;
+            k = k < 0 ? 0 : (k > NB - 1 ? NB - 1 : k);
+            const int bt = NB - 1 - k;
+            for (int i = 0; i <= bt; ++i) nl += hist[i];
+        }
+        *n_large_out = nl;
+    }
+    __syncthreads();
+    for (uint32_t chunk = 0; chunk < n_regions; chunk += blockDim.x) {
+        const uint32_t r = chunk + tid;
+        const bool valid = r < n_regions;
+        const int bk = valid ? bucket_of(r) : -1;
+        for (int i = lane; i < NB; i += 32) warp_cnt[warp][i] = 0;
+        __syncwarp();
+        const unsigned mask = __match_any_sync(0xffffffffu, bk);
+        const unsigned lt = mask & ((1u << lane) - 1u);
+        const uint32_t rank_in_warp = __popc(lt);
+        if (valid && lt == 0) warp_cnt[warp][bk] = __popc(mask);
+        __syncthreads();
+        if (valid) {
+            uint32_t before = 0;
+            for (int w = 0; w < warp; ++w) before += warp_cnt[w][bk];
+            order[base[bk] + before + rank_in_warp] = r;
+        }
+        __syncthreads();
+        // advance bucket bases by this chunk's counts
+        for (int i = tid; i < NB; i += blockDim.x) {
+            uint32_t add = 0;
+            for (int w = 0; w < 32; ++w) add += warp_cnt[w][i];
+            base[i] += add;
+        }
+        __syncthreads();
+    }
+}
+
+
 // Launchers of one component bound (pg_em_k8.cu / pg_em_k16.cu): pick the
 // instantiation for the tuning's threads per CTA, components per thread and
 // unroll, and launch it (clustered when cluster > 1).
