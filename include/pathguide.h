@@ -218,6 +218,32 @@ int pg_sync_status(pg_ctx *ctx, void *stream);
  * launches in benchmarks). */
 int pg_last_launch_count(const pg_ctx *ctx, uint32_t *count);
 
+/* ------------------------------------------------------------------ */
+/* Allocation-free fit                                                 */
+/* ------------------------------------------------------------------ */
+
+/* No counterpart in the reference: the reference fits on the host.
+ *
+ * pg_fit_regions_noalloc runs the same batched fit as pg_fit_regions for
+ * callers that cannot allocate device memory - renderers that own all device
+ * memory through their own arena, code recording a CUDA graph (a cudaMalloc
+ * breaks the capture), or plugin hosts that hand the guiding step only its own
+ * buffers.  It needs no pg_ctx: the caller passes the fit properties, the
+ * device array of n_regions mixture states (read and written in place) and the
+ * samples and offsets as for pg_fit_regions.  The fit's scratch lives in one
+ * static device array of the library, sized for PG_NOALLOC_MAX_REGIONS
+ * regions (about 257 KB per GPU, held until the process exits); nothing is
+ * allocated.  The first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress), so make it before any stream capture.  All calls
+ * share the array: calls whose work may overlap on the GPU race and must be
+ * ordered (same stream or events).  Returns PG_ERR_NOMEM when n_regions
+ * exceeds PG_NOALLOC_MAX_REGIONS, PG_ERR_ARG for bad arguments, PG_ERR_CUDA
+ * when a CUDA call fails; non-finite results are flagged in the states
+ * (PG_STATE_NONFINITE). */
+#define PG_NOALLOC_MAX_REGIONS 65536u
+int pg_fit_regions_noalloc(const pg_fit_config *cfg, pg_region_state *states, const float *dirw,
+                           const uint32_t *offsets, uint32_t n_regions, int mode, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -48,6 +48,7 @@ SIGNATURES = {
     "pg_get_fit_tuning": (_I, [_P, C.POINTER(abi.FitTuning)]),
     "pg_sync_status": (_I, [_P, _P]),
     "pg_last_launch_count": (_I, [_P, C.POINTER(_U32)]),
+    "pg_fit_regions_noalloc": (_I, [C.POINTER(abi.FitConfig), _P, _P, _P, _U32, _I, _P]),
 }
 
 _LIB = None
@@ -163,3 +164,16 @@ class FitContext:
         n = C.c_uint32()
         self._check(self.lib.pg_last_launch_count(self.h, C.byref(n)))
         return int(n.value)
+
+
+NOALLOC_MAX_REGIONS = 65536
+
+
+def fit_regions_noalloc(cfg: abi.FitConfig, states_dev, dirw, offsets, n_regions: int,
+                        mode: int = abi.PG_FIT_INIT, stream=None) -> int:
+    """pg_fit_regions_noalloc: the batched fit without a context and without any
+    device allocation, for callers that may not allocate (own memory arenas,
+    graph capture, plugin hosts).  states_dev is the caller's device array of
+    n_regions pg_region_state records, updated in place.  Returns the status."""
+    return library().pg_fit_regions_noalloc(C.byref(cfg), _dptr(states_dev), _dptr(dirw), _dptr(offsets),
+                                            n_regions, mode, _stream_handle(stream))
