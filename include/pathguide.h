@@ -219,6 +219,54 @@ int pg_sync_status(pg_ctx *ctx, void *stream);
 int pg_last_launch_count(const pg_ctx *ctx, uint32_t *count);
 
 /* ------------------------------------------------------------------ */
+/* Regions, sample bucketing, parallax, distances, VMM_Theta            */
+/* ------------------------------------------------------------------ */
+
+/* Builds 2^split_count regions by repeated midpoint splits of the padded scene
+ * box along its largest axis (PathGuiding::createRegions,
+ * src/PathGuiding.cpp:81-104; Aabb::splitAabb / addEpsilon, src/Shapes.h:32-53)
+ * and initialises their mixtures (pg_init_regions).  scene_aabb = min xyz, max xyz. */
+int pg_set_regions(pg_ctx *ctx, uint32_t split_count, const float scene_aabb[6], void *stream);
+/* PathGuiding::getRegionCount (src/PathGuiding.h:136). */
+int pg_region_count(const pg_ctx *ctx, uint32_t *out);
+/* The region boxes, 6 floats each (host copy / device pointer). */
+int pg_get_region_aabbs(pg_ctx *ctx, float *host_out, uint32_t count);
+int pg_region_aabbs_device(pg_ctx *ctx, const float **dev_out);
+
+/* SampleCollector::getSortedData (src/SampleCollector.cpp:76-131) on the
+ * device: buckets n_records records by region id (flags), stably (equal ids
+ * keep their order); INVALID or out-of-range ids are dropped.  offsets_out
+ * (device, n_regions+1) receives the region offsets; sorted_out (device, may
+ * be NULL) the bucketed records. */
+int pg_sort_samples(pg_ctx *ctx, const pg_directional_data *records, uint64_t n_records, uint32_t n_regions,
+                    pg_directional_data *sorted_out, uint32_t *offsets_out, void *stream);
+
+/* PathGuiding::preFit (src/PathGuiding.cpp:370-411): sets each region's
+ * parallax mean to its box centre, re-aims its lobes at the new mean after the
+ * first fit (incrementaldistance.h:109-131), and writes for each bucketed
+ * record the float4 {direction, weight} seen from the mean and the distance
+ * (+inf for misses).  Without parallax the directions pass through. */
+int pg_prefit_parallax(pg_ctx *ctx, const pg_directional_data *sorted, const uint32_t *offsets,
+                       uint32_t n_regions, uint64_t n_valid, float *dirw_out, float *dist_out, void *stream);
+
+/* Harmonic-mean lobe distances over one pass of samples (the statistic of
+ * external/guiding/incrementaldistance.h:57-107, PathGuiding::postFit,
+ * src/PathGuiding.cpp:445-448). */
+int pg_update_distances(pg_ctx *ctx, const float *dirw, const float *dist, const uint32_t *offsets,
+                        uint32_t n_regions, void *stream);
+
+/* PathGuiding::pmmToVMM_Theta + syncPMMsToVMM_Thetas (src/PathGuiding.cpp:53-69,
+ * 106-132): the tracer's per-region VMM_Theta (device, n_regions x 720 B). */
+int pg_pack_vmm_theta(pg_ctx *ctx, uint32_t n_regions, pg_vmm_theta *out, void *stream);
+
+/* PathGuiding::update (src/PathGuiding.cpp:276-312) as one device-resident
+ * pass: bucket the tracer's records by region, parallax pre-pass, fit
+ * (VMMFactory::fit on the first pass after pg_set_regions, updateFit after),
+ * distance update, and - when vmm_out is not NULL - VMM_Theta packing. */
+int pg_update(pg_ctx *ctx, const pg_directional_data *records, uint64_t n_records, pg_vmm_theta *vmm_out,
+              void *stream);
+
+/* ------------------------------------------------------------------ */
 /* Allocation-free fit                                                 */
 /* ------------------------------------------------------------------ */
 

@@ -49,6 +49,15 @@ SIGNATURES = {
     "pg_sync_status": (_I, [_P, _P]),
     "pg_last_launch_count": (_I, [_P, C.POINTER(_U32)]),
     "pg_fit_regions_noalloc": (_I, [C.POINTER(abi.FitConfig), _P, _P, _P, _U32, _I, _P]),
+    "pg_set_regions": (_I, [_P, _U32, _P, _P]),
+    "pg_region_count": (_I, [_P, C.POINTER(_U32)]),
+    "pg_get_region_aabbs": (_I, [_P, _P, _U32]),
+    "pg_region_aabbs_device": (_I, [_P, C.POINTER(_P)]),
+    "pg_sort_samples": (_I, [_P, _P, _U64, _U32, _P, _P, _P]),
+    "pg_prefit_parallax": (_I, [_P, _P, _P, _U32, _U64, _P, _P, _P]),
+    "pg_update_distances": (_I, [_P, _P, _P, _P, _U32, _P]),
+    "pg_pack_vmm_theta": (_I, [_P, _U32, _P, _P]),
+    "pg_update": (_I, [_P, _P, _U64, _P, _P]),
 }
 
 _LIB = None
@@ -159,6 +168,43 @@ class FitContext:
         p = C.c_void_p()
         self._check(self.lib.pg_region_states_device(self.h, C.byref(p)))
         return int(p.value or 0)
+
+    # ---- regions, bucketing, parallax, distances, VMM_Theta ----
+    def set_regions(self, split_count: int, scene_aabb, stream=None):
+        a = np.ascontiguousarray(scene_aabb, dtype=np.float32)
+        self._check(self.lib.pg_set_regions(self.h, split_count, a.ctypes.data, _stream_handle(stream)))
+
+    def region_count(self) -> int:
+        n = C.c_uint32()
+        self._check(self.lib.pg_region_count(self.h, C.byref(n)))
+        return int(n.value)
+
+    def region_aabbs(self) -> np.ndarray:
+        n = self.region_count()
+        out = np.zeros((n, 6), dtype=np.float32)
+        self._check(self.lib.pg_get_region_aabbs(self.h, out.ctypes.data, n))
+        return out
+
+    def sort_samples(self, records, n_records: int, n_regions: int, sorted_out, offsets_out, stream=None):
+        self._check(self.lib.pg_sort_samples(self.h, _dptr(records), n_records, n_regions,
+                                             _dptr(sorted_out) if sorted_out is not None else None,
+                                             _dptr(offsets_out), _stream_handle(stream)))
+
+    def prefit_parallax(self, sorted_records, offsets, n_regions: int, n_valid: int, dirw_out, dist_out, stream=None):
+        self._check(self.lib.pg_prefit_parallax(self.h, _dptr(sorted_records), _dptr(offsets), n_regions, n_valid,
+                                                _dptr(dirw_out), _dptr(dist_out), _stream_handle(stream)))
+
+    def update_distances(self, dirw, dist, offsets, n_regions: int, stream=None):
+        self._check(self.lib.pg_update_distances(self.h, _dptr(dirw), _dptr(dist), _dptr(offsets), n_regions,
+                                                 _stream_handle(stream)))
+
+    def pack_vmm_theta(self, n_regions: int, out, stream=None):
+        self._check(self.lib.pg_pack_vmm_theta(self.h, n_regions, _dptr(out), _stream_handle(stream)))
+
+    def update(self, records, n_records: int, vmm_out=None, stream=None):
+        """PathGuiding::update: one device-resident guiding pass over the tracer's records."""
+        self._check(self.lib.pg_update(self.h, _dptr(records), n_records,
+                                       _dptr(vmm_out) if vmm_out is not None else None, _stream_handle(stream)))
 
     def last_launch_count(self) -> int:
         n = C.c_uint32()

@@ -1,0 +1,732 @@
+// pg_guide.cu - the guiding steps around the fit, all device-resident:
+//   * region tree (PathGuiding::createRegions, src/PathGuiding.cpp:81-104)
+//   * stable bucket of the tracer's sample records by region
+//     (SampleCollector::getSortedData, src/SampleCollector.cpp:76-131)
+//   * parallax pre-pass (PathGuiding::preFit, src/PathGuiding.cpp:370-411)
+//   * harmonic-mean lobe distances (the statistic of
+//     external/guiding/incrementaldistance.h:57-107, PathGuiding::postFit :445-448)
+//   * VMM_Theta packing (PathGuiding::pmmToVMM_Theta / syncPMMsToVMM_Thetas,
+//     src/PathGuiding.cpp:53-69, 106-132)
+//   * pg_update: the whole training pass (PathGuiding::update, :276-312).
+//
+// The sort is an LSD radix sort of 8-bit region-id digits over (id, index)
+// pairs.  Each pass: per-tile digit histograms, a scan over (digit, tile),
+// then a stable scatter whose in-tile ranks come from warp match masks in
+// index order, so equal ids keep their original order (the reference's
+// std::sort by flags leaves that order unspecified).
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "pg_internal.cuh"
+
+namespace pg {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;                          // keys per thread
+constexpr int kSortTile = kSortThreads * kSortItems;    // 4096 keys per tile
+constexpr int kScanThreads = 1024;
+
+// Pass 0 input: the region id of each record (ids >= n_regions and INVALID
+// become the sentinel n_regions, sorted last and dropped).
+__global__ void sort_extract_keys(const pg_directional_data *rec, uint64_t n, uint32_t n_regions,
+                                  uint32_t *keys, uint32_t *vals) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t f = rec[i].flags;
+        keys[i] = f < n_regions ? f : n_regions;
+        vals[i] = (uint32_t)i;
+    }
+}
+
+__global__ void __launch_bounds__(kSortThreads) sort_histogram(const uint32_t *keys, uint32_t n, int shift,
+                                                               uint32_t n_tiles, uint32_t *tile_counts) {
+    __shared__ uint32_t h[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    const uint32_t base = blockIdx.x * (uint32_t)kSortTile;
+    for (int j = 0; j < kSortItems; ++j) {
+        const uint32_t idx = base + j * kSortThreads + threadIdx.x;
+        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    // digit-major layout: counts[d * n_tiles + tile]
+    for (int d = threadIdx.x; d < 256; d += blockDim.x) tile_counts[(size_t)d * n_tiles + blockIdx.x] = h[d];
+}
+
+// Exclusive scan of n values in place (three launches: chunk sums, scan of
+// the sums in one CTA, rescan of each chunk with its offset).
+__global__ void __launch_bounds__(kScanThreads) scan_chunk_sums(const uint32_t *v, uint32_t n, uint32_t *sums) {
+    __shared__ uint32_t w[32];
+    const uint32_t i = blockIdx.x * kScanThreads + threadIdx.x;
+    uint32_t x = i < n ? v[i] : 0u;
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) w[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        uint32_t y = w[threadIdx.x];
+        for (int o = 16; o > 0; o >>= 1) y += __shfl_xor_sync(0xffffffffu, y, o);
+        if (threadIdx.x == 0) sums[blockIdx.x] = y;
+    }
+}
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t x, uint32_t *total) {
+    __shared__ uint32_t w[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = x;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) w[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        uint32_t v = lane < nw ? w[lane] : 0u;
+        uint32_t vi = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, vi, o);
+            if (lane >= o) vi += y;
+        }
+        if (lane < nw) w[lane] = vi - v;
+        if (lane == nw - 1) *total = vi;
+    }
+    __syncthreads();
+    const uint32_t r = w[warp] + incl - x;
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_sums_single(uint32_t *sums, uint32_t n) {
+    __shared__ uint32_t carry, tot;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < n; base += kScanThreads) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t x = i < n ? sums[i] : 0u;
+        const uint32_t e = block_exclusive_scan(x, &tot);
+        if (i < n) sums[i] = carry + e;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_chunks_apply(uint32_t *v, uint32_t n, const uint32_t *sums) {
+    __shared__ uint32_t tot;
+    const uint32_t i = blockIdx.x * kScanThreads + threadIdx.x;
+    const uint32_t x = i < n ? v[i] : 0u;
+    const uint32_t e = block_exclusive_scan(x, &tot);
+    if (i < n) v[i] = sums[blockIdx.x] + e;
+}
+
+// Stable scatter of one digit pass.  Warp w of the tile owns keys
+// [base + w*512, base + (w+1)*512) in 16 groups of 32 consecutive keys; ranks
+// follow index order within the group (match masks), then across groups, then
+// across warps, so the scatter is stable.
+__global__ void __launch_bounds__(kSortThreads) sort_scatter(const uint32_t *keys_in, const uint32_t *vals_in,
+                                                             uint32_t n, int shift, uint32_t n_tiles,
+                                                             const uint32_t *tile_offsets, uint32_t *keys_out,
+                                                             uint32_t *vals_out) {
+    constexpr int NW = kSortThreads / 32;
+    __shared__ uint32_t wcount[NW][256];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int d = lane; d < 256; d += 32) wcount[warp][d] = 0;
+    __syncwarp();
+    const uint32_t base = blockIdx.x * (uint32_t)kSortTile + (uint32_t)warp * 32u * kSortItems;
+    uint32_t k[kSortItems], v[kSortItems], pos[kSortItems];
+#pragma unroll
+    for (int j = 0; j < kSortItems; ++j) {
+        const uint32_t idx = base + j * 32 + lane;
+        const bool ok = idx < n;
+        k[j] = ok ? keys_in[idx] : 0xFFFFFFFFu;
+        v[j] = ok ? vals_in[idx] : 0u;
+        const int d = ok ? (int)((k[j] >> shift) & 255u) : -1;
+        const unsigned m = __match_any_sync(0xffffffffu, d);
+        const unsigned lt = m & ((1u << lane) - 1u);
+        const uint32_t before = (d >= 0) ? wcount[warp][d] : 0u;
+        pos[j] = before + __popc(lt);
+        __syncwarp();
+        if (d >= 0 && lt == 0) wcount[warp][d] = before + __popc(m);
+        __syncwarp();
+    }
+    __syncthreads();
+    // per digit: warps' exclusive prefix (warp order = index order)
+    for (int d = threadIdx.x; d < 256; d += blockDim.x) {
+        uint32_t acc = tile_offsets[(size_t)d * n_tiles + blockIdx.x];
+        for (int w = 0; w < NW; ++w) {
+            const uint32_t c = wcount[w][d];
+            wcount[w][d] = acc;
+            acc += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kSortItems; ++j) {
+        const uint32_t idx = base + j * 32 + lane;
+        if (idx < n) {
+            const uint32_t d = (k[j] >> shift) & 255u;
+            const uint32_t dst = wcount[warp][d] + pos[j];
+            keys_out[dst] = k[j];
+            vals_out[dst] = v[j];
+        }
+    }
+}
+
+// offsets[r] = first sorted position with key >= r (r = 0..n_regions).
+__global__ void sort_offsets(const uint32_t *keys, uint32_t n, uint32_t n_regions, uint32_t *offsets) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r <= n_regions; r += gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = n;
+        while (lo < hi) {
+            const uint32_t mid = lo + (hi - lo) / 2;
+            if (keys[mid] < r)
+                lo = mid + 1;
+            else
+                hi = mid;
+        }
+        offsets[r] = lo;
+    }
+}
+
+// Gathers the sorted records (valid ones only).
+__global__ void gather_records(const pg_directional_data *rec, const uint32_t *order, const uint32_t *offsets,
+                               uint32_t n_regions, pg_directional_data *out) {
+    const uint32_t n = offsets[n_regions];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = rec[order[i]];
+}
+
+// ---------------------------------------------------------------------------
+// Parallax pre-pass, distances, reposition, packing
+// ---------------------------------------------------------------------------
+
+// PathGuiding::preFit (src/PathGuiding.cpp:370-402) for every sorted sample:
+// the region's parallax mean is its box centre; a sample with distance > 0 is
+// re-aimed from the mean at the point it saw, others get distance +inf.
+// Reads the records through the sort order (gather) and writes the fit's
+// float4 {direction, weight} and the re-centred distance.
+// The sample count is n_valid, or *n_valid_dev when given (the sort's valid
+// count, which only the device knows); records with an out-of-range region id
+// are written with zero weight.
+__global__ void prefit_parallax_kernel(const pg_directional_data *rec, const uint32_t *order, uint32_t n_valid,
+                                       const uint32_t *n_valid_dev, uint32_t n_regions, const float *means,
+                                       int use_parallax, float4 *dirw, float *dist) {
+    const uint32_t n = n_valid_dev ? *n_valid_dev : n_valid;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const pg_directional_data d = rec[order ? order[i] : i];
+        float dx = d.direction[0], dy = d.direction[1], dz = d.direction[2];
+        float t = d.distance;
+        if (d.flags >= n_regions) {
+            dirw[i] = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
+            dist[i] = INFINITY;
+            continue;
+        }
+        if (use_parallax) {
+            const float *m = means + 3 * (size_t)d.flags;
+            if (d.distance > 0.0f) {
+                const float nx = __fsub_rn(__fadd_rn(d.position[0], __fmul_rn(d.distance, dx)), m[0]);
+                const float ny = __fsub_rn(__fadd_rn(d.position[1], __fmul_rn(d.distance, dy)), m[1]);
+                const float nz = __fsub_rn(__fadd_rn(d.position[2], __fmul_rn(d.distance, dz)), m[2]);
+                const float l2 = __fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)), __fmul_rn(nz, nz));
+                const float l = __fsqrt_rn(l2);
+                const float inv = __fdiv_rn(1.0f, l);
+                dx = __fmul_rn(nx, inv);
+                dy = __fmul_rn(ny, inv);
+                dz = __fmul_rn(nz, inv);
+                t = l;
+            } else {
+                t = INFINITY;
+            }
+        }
+        dirw[i] = make_float4(dx, dy, dz, d.weight);
+        dist[i] = t;
+    }
+}
+
+// Per region: record the previous parallax mean, set the new one (box centre,
+// src/PathGuiding.cpp:380-383) and, after the first fit, re-aim the lobes with a
+// finite distance at the new mean (IncrementalDistance::reposition,
+// external/guiding/incrementaldistance.h:109-131).
+__global__ void parallax_means_kernel(pg_region_state *states, const float *aabbs, uint32_t n_regions,
+                                      int reposition, float *means_out) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_regions) return;
+    pg_region_state *s = states + r;
+    const float *b = aabbs + 6 * (size_t)r;
+    float m[3];
+    for (int i = 0; i < 3; ++i) {
+        m[i] = __fadd_rn(b[i], __fmul_rn(0.5f, __fsub_rn(b[3 + i], b[i])));
+        s->last_parallax_mean[i] = s->parallax_mean[i];
+        s->parallax_mean[i] = m[i];
+        means_out[3 * (size_t)r + i] = m[i];
+    }
+    if (!reposition) return;
+    const float d0 = __fsub_rn(s->last_parallax_mean[0], m[0]);
+    const float d1 = __fsub_rn(s->last_parallax_mean[1], m[1]);
+    const float d2 = __fsub_rn(s->last_parallax_mean[2], m[2]);
+    for (uint32_t c = 0; c < s->k && c < 16; ++c) {
+        const float dist = s->distance[c];
+        if (isinf(dist) || s->dist_sum_w[c] <= 0.0f) continue;
+        const float x = __fadd_rn(__fmul_rn(s->mu_x[c], dist), d0);
+        const float y = __fadd_rn(__fmul_rn(s->mu_y[c], dist), d1);
+        const float z = __fadd_rn(__fmul_rn(s->mu_z[c], dist), d2);
+        const float l = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
+        s->distance[c] = l;
+        s->mu_x[c] = __fdiv_rn(x, l);
+        s->mu_y[c] = __fdiv_rn(y, l);
+        s->mu_z[c] = __fdiv_rn(z, l);
+    }
+}
+
+// Harmonic-mean distance per lobe, weighted by w * gamma_k * pdf_k over the
+// samples with distance > 0 (the statistic of incrementaldistance.h:57-107),
+// merged with the previous estimate.  One CTA per region; per-thread FP32
+// partial sums, warp shuffles, Neumaier merge across warps.
+template <int NT>
+__global__ void __launch_bounds__(NT) distance_kernel(pg_region_state *states, const float4 *dirw,
+                                                      const float *dist, const uint32_t *offsets,
+                                                      uint32_t n_regions) {
+    constexpr int NW = NT / 32;
+    __shared__ float c_ax[16], c_ay[16], c_az[16], c_c0[16], c_cm[16], c_lk[16];
+    __shared__ float red[NW][32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (uint32_t r = blockIdx.x; r < n_regions; r += gridDim.x) {
+        pg_region_state *s = states + r;
+        const uint32_t K = min(s->k, 16u);
+        if (tid < 16) {
+            const int c = tid;
+            // log2 of pdf_k = kl (mu.d - 1) + log2(norm); log2 of pi_k pdf_k adds log2(pi)
+            const float kl = s->kappa[c] * kLog2e;
+            const float ln = (c < (int)K && s->norm[c] > 0.0f) ? log2f(s->norm[c]) : -INFINITY;
+            const float lw = (c < (int)K && s->weight[c] > 0.0f) ? log2f(s->weight[c]) : -INFINITY;
+            c_ax[c] = kl * s->mu_x[c];
+            c_ay[c] = kl * s->mu_y[c];
+            c_az[c] = kl * s->mu_z[c];
+            c_c0[c] = ln - kl;  // log2 pdf_k before the clamp
+            c_cm[c] = ln;       // clamp: cos <= 1
+            c_lk[c] = lw;
+        }
+        __syncthreads();
+        float bw[16], bwd[16];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) bw[c] = bwd[c] = 0.0f;
+        const uint32_t b = offsets[r], e = offsets[r + 1];
+        for (uint32_t i = b + tid; i < e; i += NT) {
+            const float t = dist[i];
+            if (!(t > 0.0f)) continue;
+            const float4 d = dirw[i];
+            float lp[16];
+            float p = 0.0f;
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+                float a = fmaf(c_az[c], d.z, c_c0[c]);
+                a = fmaf(c_ay[c], d.y, a);
+                a = fmaf(c_ax[c], d.x, a);
+                lp[c] = fminf(a, c_cm[c]);
+                p += exp2f(lp[c] + c_lk[c]);
+            }
+            if (!(p > kPmmEps)) continue;
+            const float sc = d.w / p;
+            const float it = 1.0f / t;
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+                // w * gamma_k * pdf_k = w/p * pi_k pdf_k * pdf_k
+                const float a = exp2f(2.0f * lp[c] + c_lk[c]) * sc;
+                bw[c] += a;
+                bwd[c] += a * it;
+            }
+        }
+        // reduce: lanes hold 32 values (bw[16], bwd[16]); warp sums then Neumaier over warps
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+            float x = bw[c], y = bwd[c];
+            for (int o = 16; o > 0; o >>= 1) {
+                x += __shfl_xor_sync(0xffffffffu, x, o);
+                y += __shfl_xor_sync(0xffffffffu, y, o);
+            }
+            if (lane == 0) {
+                red[warp][c] = x;
+                red[warp][16 + c] = y;
+            }
+        }
+        __syncthreads();
+        // every lane of the active 4-lane groups, as the reference's SIMD update does
+        if (tid < 16 && tid < (int)((K + 3u) & ~3u)) {
+            const int c = tid;
+            float wh = 0.f, wl = 0.f, dh = 0.f, dl = 0.f;
+            for (int w = 0; w < NW; ++w) {
+                neumaier_add(wh, wl, red[w][c]);
+                neumaier_add(dh, dl, red[w][16 + c]);
+            }
+            const float batch_w = wh + wl, batch_wd = dh + dl;
+            const float old_w = s->dist_sum_w[c];
+            const float new_w = old_w + batch_w;
+            s->distance[c] = new_w / (old_w / s->distance[c] + batch_wd);
+            s->dist_sum_w[c] = new_w;
+        }
+        __syncthreads();
+    }
+}
+
+// PathGuiding::pmmToVMM_Theta + syncPMMsToVMM_Thetas; norm and e^{-2k} of
+// VMF_Theta::setK are evaluated in double as the reference does.
+__global__ void pack_vmm_theta_kernel(const pg_region_state *states, uint32_t n_regions, int use_parallax,
+                                      pg_vmm_theta *out) {
+    const uint32_t r = blockIdx.x;
+    const int c = threadIdx.x;  // 16 threads
+    if (r >= n_regions || c >= 16) return;
+    const pg_region_state *s = states + r;
+    pg_vmm_theta *v = out + r;
+    const uint32_t K = min(s->k, 16u);
+    pg_vmf_theta th;
+    th.mu[0] = th.mu[1] = th.mu[2] = 0.0f;
+    th.k = 0.0f;
+    th.norm = 0.0f;
+    th.e_min2k = 0.0f;
+    th.distance = -1.0f;
+    th.target[0] = th.target[1] = th.target[2] = 0.0f;
+    float pi = 0.0f;
+    if (c < (int)K) {
+        pi = s->weight[c];
+        th.mu[0] = s->mu_x[c];
+        th.mu[1] = s->mu_y[c];
+        th.mu[2] = s->mu_z[c];
+        float k = s->kappa[c];
+        k = k < kVmfMinKappa ? 0.0f : k;
+        th.k = k;
+        const double kd = (double)k;
+        th.norm = (float)(kd / (2.0 * 3.14159265358979323846 * (1.0 - exp(-2.0 * kd))));
+        th.e_min2k = (float)exp(-2.0 * kd);
+    }
+    if (use_parallax) {
+        float dd = s->distance[c];
+        dd = (dd == INFINITY) ? -1.0f : dd;
+        th.distance = dd;
+        for (int i = 0; i < 3; ++i) th.target[i] = __fadd_rn(s->parallax_mean[i], __fmul_rn(dd, th.mu[i]));
+    }
+    v->thetas[c] = th;
+    v->pi[c] = pi;
+    if (c == 0) {
+        for (int i = 0; i < 3; ++i) v->mean_position[i] = use_parallax ? s->parallax_mean[i] : 0.0f;
+        v->used_distributions = (int32_t)K;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host helpers
+// ---------------------------------------------------------------------------
+
+// Region boxes: Aabb::addEpsilon then split_count rounds of midpoint splits
+// along the largest axis, breadth first (src/Shapes.h:32-53,
+// src/PathGuiding.cpp:81-104), in the reference's float arithmetic.
+void region_boxes(uint32_t split_count, const float a[6], std::vector<float> &out) {
+    float mn[3], mx[3];
+    for (int i = 0; i < 3; ++i) {
+        const float ext = a[3 + i] - a[i];
+        const float cen = a[i] + 0.5f * ext;
+        mn[i] = cen - 0.50001f * ext;
+        mx[i] = cen + 0.50001f * ext;
+    }
+    std::vector<float> cur = {mn[0], mn[1], mn[2], mx[0], mx[1], mx[2]};
+    for (uint32_t s = 0; s < split_count; ++s) {
+        std::vector<float> nxt;
+        nxt.reserve(cur.size() * 2);
+        for (size_t b = 0; b < cur.size() / 6; ++b) {
+            const float *bx = &cur[6 * b];
+            float size[3];
+            for (int i = 0; i < 3; ++i) size[i] = bx[3 + i] - bx[i];
+            const int axis = size[0] > size[1] ? (size[0] > size[2] ? 0 : 2) : (size[1] > size[2] ? 1 : 2);
+            float L[6], R[6];
+            memcpy(L, bx, sizeof L);
+            memcpy(R, bx, sizeof R);
+            L[3 + axis] -= 0.5f * size[axis];
+            R[axis] += 0.5f * size[axis];
+            nxt.insert(nxt.end(), L, L + 6);
+            nxt.insert(nxt.end(), R, R + 6);
+        }
+        cur.swap(nxt);
+    }
+    out.swap(cur);
+}
+
+}  // namespace pg
+
+using namespace pg;
+
+namespace pg {
+
+// Scratch of the sort and of the guiding pass, grown on demand and owned by the context.
+struct GuideScratch {
+    uint32_t *keys[2] = {nullptr, nullptr};
+    uint32_t *vals[2] = {nullptr, nullptr};
+    uint32_t *tile_counts = nullptr;
+    uint32_t *scan_sums = nullptr;
+    uint64_t cap_n = 0;
+    uint64_t cap_tiles = 0;
+    float4 *dirw = nullptr;
+    float *dist = nullptr;
+    uint32_t *offsets = nullptr;
+    uint32_t *order = nullptr;
+    float *means = nullptr;
+    float *aabbs = nullptr;
+    uint32_t n_regions = 0;
+    uint32_t split_count = 0;
+    uint64_t cap_samples = 0;
+    bool fitted = false;
+};
+
+static GuideScratch &guide(pg_ctx *ctx) {
+    if (!ctx->guide) ctx->guide = new GuideScratch();
+    return *static_cast<GuideScratch *>(ctx->guide);
+}
+
+void guide_release(pg_ctx *ctx) {
+    if (!ctx || !ctx->guide) return;
+    GuideScratch &g = *static_cast<GuideScratch *>(ctx->guide);
+    for (int i = 0; i < 2; ++i) {
+        cudaFree(g.keys[i]);
+        cudaFree(g.vals[i]);
+    }
+    cudaFree(g.tile_counts);
+    cudaFree(g.scan_sums);
+    cudaFree(g.dirw);
+    cudaFree(g.dist);
+    cudaFree(g.offsets);
+    cudaFree(g.order);
+    cudaFree(g.means);
+    cudaFree(g.aabbs);
+    delete static_cast<GuideScratch *>(ctx->guide);
+    ctx->guide = nullptr;
+}
+
+}  // namespace pg
+
+static int ensure_sort_capacity(pg_ctx *ctx, uint64_t n) {
+    GuideScratch &g = guide(ctx);
+    const uint64_t tiles = (n + kSortTile - 1) / kSortTile;
+    if (n > g.cap_n) {
+        for (int i = 0; i < 2; ++i) {
+            cudaFree(g.keys[i]);
+            cudaFree(g.vals[i]);
+            g.keys[i] = g.vals[i] = nullptr;
+        }
+        for (int i = 0; i < 2; ++i) {
+            int st = check_cuda(ctx, cudaMalloc(&g.keys[i], sizeof(uint32_t) * n), "sort keys");
+            if (!st) st = check_cuda(ctx, cudaMalloc(&g.vals[i], sizeof(uint32_t) * n), "sort values");
+            if (st) return st;
+        }
+        g.cap_n = n;
+    }
+    if (tiles > g.cap_tiles) {
+        cudaFree(g.tile_counts);
+        cudaFree(g.scan_sums);
+        g.tile_counts = g.scan_sums = nullptr;
+        const uint64_t cnt = 256 * tiles;
+        int st = check_cuda(ctx, cudaMalloc(&g.tile_counts, sizeof(uint32_t) * cnt), "sort tile counts");
+        if (!st)
+            st = check_cuda(ctx, cudaMalloc(&g.scan_sums, sizeof(uint32_t) * ((cnt + kScanThreads - 1) / kScanThreads + 1)),
+                            "sort scan sums");
+        if (st) return st;
+        g.cap_tiles = tiles;
+    }
+    return PG_OK;
+}
+
+static void exclusive_scan(uint32_t *v, uint32_t n, uint32_t *sums, cudaStream_t s) {
+    const uint32_t chunks = (n + kScanThreads - 1) / kScanThreads;
+    scan_chunk_sums<<<chunks, kScanThreads, 0, s>>>(v, n, sums);
+    scan_sums_single<<<1, kScanThreads, 0, s>>>(sums, chunks);
+    scan_chunks_apply<<<chunks, kScanThreads, 0, s>>>(v, n, sums);
+}
+
+// Sorts the (region id, index) pairs of n records; leaves the sorted indices in
+// *order_out (a scratch buffer) and the region offsets in offsets (device).
+static int sort_records(pg_ctx *ctx, const pg_directional_data *rec, uint64_t n, uint32_t n_regions,
+                        uint32_t *offsets, uint32_t **order_out, cudaStream_t s) {
+    if (n > 0xFFFFFFFFull - kSortTile) return set_error(ctx, PG_ERR_ARG, "too many sample records");
+    int st = ensure_sort_capacity(ctx, n ? n : 1);
+    if (st) return st;
+    GuideScratch &g = guide(ctx);
+    const uint32_t nn = (uint32_t)n;
+    const uint32_t tiles = (nn + kSortTile - 1) / kSortTile;
+    if (nn > 0) {
+        sort_extract_keys<<<std::min<uint32_t>((nn + 255) / 256, 8192u), 256, 0, s>>>(rec, n, n_regions, g.keys[0],
+                                                                                     g.vals[0]);
+        int passes = 0;
+        for (uint32_t m = n_regions; m > 0; m >>= 8) ++passes;  // digits of the sentinel n_regions
+        int cur = 0;
+        for (int p = 0; p < passes; ++p) {
+            const int shift = 8 * p;
+            sort_histogram<<<tiles, kSortThreads, 0, s>>>(g.keys[cur], nn, shift, tiles, g.tile_counts);
+            exclusive_scan(g.tile_counts, 256u * tiles, g.scan_sums, s);
+            sort_scatter<<<tiles, kSortThreads, 0, s>>>(g.keys[cur], g.vals[cur], nn, shift, tiles, g.tile_counts,
+                                                        g.keys[cur ^ 1], g.vals[cur ^ 1]);
+            cur ^= 1;
+        }
+        sort_offsets<<<(n_regions + 256) / 256, 256, 0, s>>>(g.keys[cur], nn, n_regions, offsets);
+        *order_out = g.vals[cur];
+    } else {
+        st = check_cuda(ctx, cudaMemsetAsync(offsets, 0, sizeof(uint32_t) * (n_regions + 1), s), "offsets");
+        if (st) return st;
+        *order_out = g.vals[0];
+    }
+    return check_cuda(ctx, cudaGetLastError(), "sort launch");
+}
+
+extern "C" {
+
+int pg_set_regions(pg_ctx *ctx, uint32_t split_count, const float scene_aabb[6], void *stream) {
+    if (!ctx || !scene_aabb) return PG_ERR_ARG;
+    if (split_count > 24) return set_error(ctx, PG_ERR_ARG, "split_count must be <= 24");
+    const uint32_t n = 1u << split_count;
+    if (n > ctx->max_regions) return set_error(ctx, PG_ERR_ARG, "2^split_count exceeds the context's regions");
+    GuideScratch &g = guide(ctx);
+    std::vector<float> boxes;
+    region_boxes(split_count, scene_aabb, boxes);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (g.n_regions < n || !g.aabbs) {
+        cudaFree(g.aabbs);
+        cudaFree(g.means);
+        g.aabbs = g.means = nullptr;
+        int st = check_cuda(ctx, cudaMalloc(&g.aabbs, sizeof(float) * 6 * n), "region boxes");
+        if (!st) st = check_cuda(ctx, cudaMalloc(&g.means, sizeof(float) * 3 * n), "region means");
+        if (st) return st;
+    }
+    g.n_regions = n;
+    g.split_count = split_count;
+    g.fitted = false;
+    int st = check_cuda(ctx, cudaMemcpyAsync(g.aabbs, boxes.data(), sizeof(float) * 6 * n, cudaMemcpyHostToDevice, s),
+                        "region boxes upload");
+    if (!st) st = check_cuda(ctx, cudaStreamSynchronize(s), "region boxes sync");
+    if (st) return st;
+    return pg_init_regions(ctx, n, stream);
+}
+
+int pg_region_count(const pg_ctx *ctx, uint32_t *out) {
+    if (!ctx || !out) return PG_ERR_ARG;
+    *out = ctx->guide ? static_cast<const GuideScratch *>(ctx->guide)->n_regions : 0u;
+    return PG_OK;
+}
+
+int pg_get_region_aabbs(pg_ctx *ctx, float *host_out, uint32_t count) {
+    if (!ctx || !host_out) return PG_ERR_ARG;
+    GuideScratch &g = guide(ctx);
+    if (!g.aabbs || count > g.n_regions) return set_error(ctx, PG_ERR_STATE, "regions not set");
+    return check_cuda(ctx, cudaMemcpy(host_out, g.aabbs, sizeof(float) * 6 * count, cudaMemcpyDeviceToHost),
+                      "region boxes download");
+}
+
+int pg_region_aabbs_device(pg_ctx *ctx, const float **dev_out) {
+    if (!ctx || !dev_out) return PG_ERR_ARG;
+    GuideScratch &g = guide(ctx);
+    *dev_out = g.aabbs;
+    return g.aabbs ? PG_OK : set_error(ctx, PG_ERR_STATE, "regions not set");
+}
+
+int pg_sort_samples(pg_ctx *ctx, const pg_directional_data *records, uint64_t n_records, uint32_t n_regions,
+                    pg_directional_data *sorted_out, uint32_t *offsets_out, void *stream) {
+    if (!ctx || (!records && n_records) || !offsets_out) return PG_ERR_ARG;
+    if (n_regions == 0 || n_regions >= 0xFFFFFF00u) return set_error(ctx, PG_ERR_ARG, "bad region count");
+    cudaStream_t s = (cudaStream_t)stream;
+    uint32_t *order = nullptr;
+    int st = sort_records(ctx, records, n_records, n_regions, offsets_out, &order, s);
+    if (st) return st;
+    if (sorted_out && n_records) {
+        gather_records<<<std::min<uint64_t>((n_records + 255) / 256, 8192u), 256, 0, s>>>(records, order, offsets_out,
+                                                                                         n_regions, sorted_out);
+        st = check_cuda(ctx, cudaGetLastError(), "gather launch");
+    }
+    return st;
+}
+
+int pg_prefit_parallax(pg_ctx *ctx, const pg_directional_data *sorted, const uint32_t *offsets, uint32_t n_regions,
+                       uint64_t n_valid, float *dirw_out, float *dist_out, void *stream) {
+    if (!ctx || !offsets || !dirw_out || !dist_out || (!sorted && n_valid)) return PG_ERR_ARG;
+    GuideScratch &g = guide(ctx);
+    if (ctx->cfg.use_parallax && (!g.aabbs || n_regions > g.n_regions))
+        return set_error(ctx, PG_ERR_STATE, "pg_set_regions must run before the parallax pre-pass");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (ctx->cfg.use_parallax) {
+        parallax_means_kernel<<<(n_regions + 127) / 128, 128, 0, s>>>(ctx->d_states, g.aabbs, n_regions,
+                                                                       g.fitted ? 1 : 0, g.means);
+    }
+    if (n_valid)
+        prefit_parallax_kernel<<<std::min<uint64_t>((n_valid + 255) / 256, 16384u), 256, 0, s>>>(
+            sorted, nullptr, (uint32_t)n_valid, nullptr, n_regions, g.means, ctx->cfg.use_parallax ? 1 : 0,
+            reinterpret_cast<float4 *>(dirw_out), dist_out);
+    return check_cuda(ctx, cudaGetLastError(), "prefit launch");
+}
+
+int pg_update_distances(pg_ctx *ctx, const float *dirw, const float *dist, const uint32_t *offsets,
+                        uint32_t n_regions, void *stream) {
+    if (!ctx || !dirw || !dist || !offsets) return PG_ERR_ARG;
+    if (n_regions > ctx->max_regions) return set_error(ctx, PG_ERR_ARG, "n_regions exceeds context capacity");
+    if (n_regions == 0) return PG_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    distance_kernel<256><<<std::min<uint32_t>(n_regions, (uint32_t)ctx->sm_count * 8u), 256, 0, s>>>(
+        ctx->d_states, reinterpret_cast<const float4 *>(dirw), dist, offsets, n_regions);
+    return check_cuda(ctx, cudaGetLastError(), "distance launch");
+}
+
+int pg_pack_vmm_theta(pg_ctx *ctx, uint32_t n_regions, pg_vmm_theta *out, void *stream) {
+    if (!ctx || !out) return PG_ERR_ARG;
+    if (n_regions > ctx->max_regions) return set_error(ctx, PG_ERR_ARG, "n_regions exceeds context capacity");
+    if (n_regions == 0) return PG_OK;
+    pack_vmm_theta_kernel<<<n_regions, 16, 0, (cudaStream_t)stream>>>(ctx->d_states, n_regions,
+                                                                       ctx->cfg.use_parallax ? 1 : 0, out);
+    return check_cuda(ctx, cudaGetLastError(), "pack launch");
+}
+
+int pg_update(pg_ctx *ctx, const pg_directional_data *records, uint64_t n_records, pg_vmm_theta *vmm_out,
+              void *stream) {
+    if (!ctx || (!records && n_records)) return PG_ERR_ARG;
+    GuideScratch &g = guide(ctx);
+    if (!g.aabbs || g.n_regions == 0) return set_error(ctx, PG_ERR_STATE, "pg_set_regions must run before pg_update");
+    const uint32_t R = g.n_regions;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (n_records > g.cap_samples || !g.dirw) {
+        cudaFree(g.dirw);
+        cudaFree(g.dist);
+        g.dirw = nullptr;
+        g.dist = nullptr;
+        const uint64_t cap = std::max<uint64_t>(n_records, 1);
+        int st = check_cuda(ctx, cudaMalloc(&g.dirw, sizeof(float4) * cap), "fit samples");
+        if (!st) st = check_cuda(ctx, cudaMalloc(&g.dist, sizeof(float) * cap), "fit distances");
+        if (st) return st;
+        g.cap_samples = cap;
+    }
+    if (!g.offsets) {
+        int st = check_cuda(ctx, cudaMalloc(&g.offsets, sizeof(uint32_t) * ((size_t)ctx->max_regions + 1)), "offsets");
+        if (st) return st;
+    }
+    // 1. bucket by region (SampleCollector::getSortedData)
+    uint32_t *order = nullptr;
+    int st = sort_records(ctx, records, n_records, R, g.offsets, &order, s);
+    if (st) return st;
+    // 2. parallax pre-pass (PathGuiding::preFit), gathering through the sort order
+    const int par = ctx->cfg.use_parallax ? 1 : 0;
+    if (par)
+        parallax_means_kernel<<<(R + 127) / 128, 128, 0, s>>>(ctx->d_states, g.aabbs, R, g.fitted ? 1 : 0, g.means);
+    if (n_records)
+        prefit_parallax_kernel<<<std::min<uint64_t>((n_records + 255) / 256, 16384u), 256, 0, s>>>(
+            records, order, (uint32_t)n_records, g.offsets + R, R, g.means, par, g.dirw, g.dist);
+    st = check_cuda(ctx, cudaGetLastError(), "prefit launch");
+    if (st) return st;
+    // Records past the valid count (invalid slots) are never read by the fit:
+    // offsets[R] bounds every region.
+    // 3. fit (VMMFactory::fit on the first pass, updateFit afterwards)
+    st = pg_fit_regions(ctx, reinterpret_cast<const float *>(g.dirw), g.offsets, R,
+                        g.fitted ? PG_FIT_UPDATE : PG_FIT_CONTINUE, stream);
+    if (st) return st;
+    // 4. parallax distances (PathGuiding::postFit)
+    if (par) {
+        st = pg_update_distances(ctx, reinterpret_cast<const float *>(g.dirw), g.dist, g.offsets, R, stream);
+        if (st) return st;
+    }
+    g.fitted = true;
+    // 5. VMM_Theta for the tracer
+    if (vmm_out) st = pg_pack_vmm_theta(ctx, R, vmm_out, stream);
+    return st;
+}
+
+}  // extern "C"

@@ -33,6 +33,7 @@ struct pg_ctx {
     uint32_t init_k = 0;             // K the table was computed for
     float init_kappa = -1.0f;
     uint32_t last_launches = 0;
+    void *guide = nullptr;           // sort / parallax / distance scratch (pg_guide.cu)
     std::string last_error;
 };
 
@@ -41,6 +42,7 @@ namespace pg {
 int set_error(pg_ctx *ctx, int status, const std::string &msg);
 int check_cuda(pg_ctx *ctx, cudaError_t e, const char *what);
 int upload_init_table(pg_ctx *ctx, cudaStream_t s);
+void guide_release(pg_ctx *ctx);
 
 constexpr float kLog2e = 1.4426950408889634f;
 constexpr float kLn2 = 0.6931471805599453f;
