@@ -267,6 +267,145 @@ int pg_update(pg_ctx *ctx, const pg_directional_data *records, uint64_t n_record
               void *stream);
 
 /* ------------------------------------------------------------------ */
+/* Scenes, traversal and the wavefront path tracer                       */
+/* ------------------------------------------------------------------ */
+
+/* Material types: MAT_DIFFUSE, MAT_SPECULAR, MAT_DIELECTRIC, MAT_LIGHT of
+ * shaders/raytrace.rgen:21-27.  PG_MAT_GGX is a GGX microfacet conductor; it
+ * takes the place of the reference's Beckmann MAT_ROUGH_CONDUCTOR
+ * (raytrace.rgen:222-236). */
+enum { PG_MAT_DIFFUSE = 0, PG_MAT_SPECULAR = 1, PG_MAT_DIELECTRIC = 2, PG_MAT_LIGHT = 3, PG_MAT_GGX = 6 };
+
+typedef struct pg_material {
+    int32_t type;
+    float albedo[3];    /* diffuse reflectance; specular / GGX tint (Fresnel F0) */
+    float emission[3];  /* radiance of a light (lightColor) */
+    float roughness;    /* GGX alpha */
+    float ior;          /* dielectric index of refraction */
+    int32_t reserved[3];
+} pg_material;
+
+typedef struct pg_sphere {
+    float center[3];
+    float radius;
+    uint32_t material;
+    uint32_t reserved[3];
+} pg_sphere;
+
+typedef struct pg_camera {
+    float origin[3];
+    float target[3];
+    float up[3];
+    float vfov_deg;
+    uint32_t width, height;
+} pg_camera;
+
+/* One ray: origin, t_min, direction, t_max (32 B). */
+typedef struct pg_ray {
+    float org[3];
+    float tmin;
+    float dir[3];
+    float tmax;
+} pg_ray;
+
+#define PG_NO_HIT 0xFFFFFFFFu
+#define PG_SPHERE_BIT 0x80000000u
+/* Closest hit: t, barycentrics (u, v) and the original triangle id, or
+ * PG_SPHERE_BIT | sphere index, or PG_NO_HIT. */
+typedef struct pg_hit {
+    float t;
+    float u, v;
+    uint32_t prim;
+} pg_hit;
+
+/* Procedural Cornell box: five walls (10 triangles, albedo 0.7 / red /
+ * green), a 0.25 x 0.25 area light on the ceiling, and a dielectric icosphere
+ * with 20 * 4^ico_level triangles. */
+typedef struct pg_cornell_params {
+    uint32_t width, height;
+    int32_t ico_level;
+    float light_radiance;
+    float ior;
+} pg_cornell_params;
+
+/* Multi-light glossy scene: four GGX plates (roughness 0.005, 0.02, 0.07,
+ * 0.2) facing four spherical lights (radii 0.03, 0.1, 0.3, 1.0, power
+ * proportional to 1/r^2) over a diffuse floor, plus a seeded displaced plane of
+ * 2 * grid^2 triangles between lights and plates. */
+typedef struct pg_plates_params {
+    uint32_t width, height;
+    uint32_t occluder_grid;
+    uint32_t seed;
+} pg_plates_params;
+
+typedef struct pg_scene_info {
+    uint32_t n_triangles, n_spheres, n_materials, n_nodes, n_lights;
+    float aabb[6];       /* SceneLoader::getSceneSize (src/SceneLoader.h:118) */
+    pg_camera camera;
+} pg_scene_info;
+
+/* Render settings: the push constants of the reference's ray-generation
+ * shader that this path uses (src/RayTracingApp.h:81-130). */
+typedef struct pg_render_params {
+    uint32_t spp;
+    uint32_t max_depth;
+    uint32_t seed;
+    uint32_t use_nee;          /* next-event estimation */
+    uint32_t use_mis;          /* power-heuristic MIS of NEE and BSDF samples */
+    uint32_t use_guiding;      /* sample directions from the context's mixtures */
+    float guiding_prob;        /* one-sample mixture weight of the guide (0.5) */
+    uint32_t record_samples;   /* write DirectionalData records for the next fit */
+    uint32_t reserved[4];
+} pg_render_params;
+
+typedef struct pg_render_stats {
+    uint64_t extension_rays;
+    uint64_t shadow_rays;
+    uint64_t samples_recorded;
+    uint64_t paths;
+} pg_render_stats;
+
+typedef struct pg_scene pg_scene;
+
+/* SceneLoader(filepath) (src/SceneLoader.cpp:29-65): Mitsuba-XML subset
+ * (sensor lookAt/fov, bsdf diffuse/dielectric/conductor/roughconductor,
+ * shape obj/sphere/rectangle/cube, area emitters).  Builds the BVH on the host;
+ * the device copy is made on first use.  On failure the message is in
+ * pg_last_error(NULL) (PG_ERR_IO: unreadable file, PG_ERR_PARSE: malformed). */
+int pg_scene_load(const char *path, uint32_t width, uint32_t height, pg_scene **out);
+int pg_scene_create_cornell(const pg_cornell_params *p, pg_scene **out);
+int pg_scene_create_plates(const pg_plates_params *p, pg_scene **out);
+int pg_scene_destroy(pg_scene *scene);
+int pg_scene_get_info(const pg_scene *scene, pg_scene_info *out);
+/* Host copies of the built scene: BVH nodes (64 B each), triangles in BVH
+ * order (12 floats each), their original ids, per-triangle materials, the
+ * materials and the spheres.  Any pointer may be NULL. */
+int pg_scene_export(const pg_scene *scene, void *nodes, float *tri_verts, uint32_t *tri_order,
+                    uint32_t *tri_material, pg_material *materials, pg_sphere *spheres);
+/* Host copies of the vertex positions (3 floats each, n_vertices of them) and
+ * triangle indices (3 per triangle, original order). */
+int pg_scene_export_mesh(const pg_scene *scene, float *positions, uint32_t *indices, uint32_t *n_vertices);
+/* Replaces the camera (SceneLoader origin/target/upDir/vfov, src/SceneLoader.h:147-150)
+ * and the image size. */
+int pg_scene_set_camera(pg_scene *scene, const pg_camera *cam);
+
+/* Closest hit / any hit of n rays (device arrays).  Traversal: two-wide BVH,
+ * near child first, watertight FP32 ray-triangle test (Woop, Benthin and
+ * Wald 2013); ties in t go to the lower triangle id. */
+int pg_trace_closest(pg_scene *scene, const pg_ray *rays, uint32_t n, pg_hit *hits, void *stream);
+int pg_trace_any(pg_scene *scene, const pg_ray *rays, uint32_t n, uint32_t *occluded, void *stream);
+
+/* Renders params->spp samples per pixel with the wavefront integrator and
+ * adds the radiance sums into image (device, width * height * 3 floats).
+ * With `guide` (a context after pg_set_regions / pg_update) and
+ * use_guiding, BSDF sampling is mixed with the regions' vMF mixtures
+ * (shaders/guiding.glsl:32-96, raytrace.rgen:923-960).  With record_samples,
+ * up to 16 guiding records per pixel (raytrace.rgen:966-990, 1179-1200) are
+ * written to records (device, width * height * 16), INVALID where empty. */
+int pg_render(pg_scene *scene, const pg_render_params *params, pg_ctx *guide, float *image,
+              pg_directional_data *records, pg_render_stats *stats, void *stream);
+
+/* ------------------------------------------------------------------ */
 /* Allocation-free fit                                                 */
 /* ------------------------------------------------------------------ */
 

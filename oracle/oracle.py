@@ -188,3 +188,73 @@ class ReferenceFit:
         y = np.zeros_like(x)
         self.lib.lpmm_ref_fastexp(abi.ptr(x), abi.ptr(y), x.size)
         return y
+
+
+class PgoScene(C.Structure):
+    _fields_ = [("nodes", _P), ("n_nodes", _U32), ("tri_verts", _P), ("n_tris", _U32), ("pos", _P),
+                ("n_vertices", _U32), ("idx", _P), ("tri_mat", _P), ("mats", _P), ("n_mats", _U32),
+                ("spheres", _P), ("n_spheres", _U32), ("camera", abi.Camera)]
+
+
+class PgoGuide(C.Structure):
+    _fields_ = [("root", C.c_float * 6), ("split_count", _U32), ("vmm", _P), ("use_parallax", C.c_int32)]
+
+
+class TraceOracle:
+    """CPU twins of the tracer (oracle/pg_oracle_trace.cpp, in liboracle.so)."""
+
+    def __init__(self, path: Path | None = None):
+        path = path or HERE / "liboracle.so"
+        self.lib = C.CDLL(str(path))
+        L = self.lib
+        L.pgo_trace_closest.argtypes = [C.POINTER(PgoScene), _P, _U32, _P, _I]
+        L.pgo_trace_any.argtypes = [C.POINTER(PgoScene), _P, _U32, _P, _I]
+        L.pgo_render_f64.argtypes = [C.POINTER(PgoScene), C.POINTER(abi.RenderParams), C.POINTER(PgoGuide), _P, _U32,
+                                     _U32, _I]
+        L.pgo_rnd.argtypes = [_U32, _U32, _U32, _U32]
+        L.pgo_rnd.restype = C.c_float
+
+    @staticmethod
+    def scene(exp: dict, camera: "abi.Camera | None" = None) -> tuple:
+        keep = {k: np.ascontiguousarray(v) for k, v in exp.items() if isinstance(v, np.ndarray)}
+        s = PgoScene(keep["nodes"].ctypes.data, keep["nodes"].shape[0], keep["tri_verts"].ctypes.data,
+                     keep["tri_verts"].shape[0], keep["pos"].ctypes.data, keep["pos"].shape[0],
+                     keep["idx"].ctypes.data, keep["tri_mat"].ctypes.data, keep["mats"].ctypes.data,
+                     keep["mats"].shape[0], keep["spheres"].ctypes.data, keep["spheres"].shape[0],
+                     camera if camera is not None else exp["info"].camera)
+        return s, keep
+
+    def closest(self, exp, rays, threads=None):
+        s, keep = self.scene(exp)
+        rays = np.ascontiguousarray(rays)
+        hits = np.zeros(rays.shape[0], dtype=abi.HIT_DTYPE)
+        self.lib.pgo_trace_closest(C.byref(s), rays.ctypes.data, rays.shape[0], hits.ctypes.data,
+                                   threads or (os.cpu_count() or 1))
+        return hits
+
+    def any(self, exp, rays, threads=None):
+        s, keep = self.scene(exp)
+        rays = np.ascontiguousarray(rays)
+        occ = np.zeros(rays.shape[0], dtype=np.uint32)
+        self.lib.pgo_trace_any(C.byref(s), rays.ctypes.data, rays.shape[0], occ.ctypes.data,
+                               threads or (os.cpu_count() or 1))
+        return occ
+
+    def render(self, exp, params, guide=None, rows=None, threads=None, camera=None):
+        """FP64 render: returns (H, W, 3) radiance sums over params.spp samples."""
+        s, keep = self.scene(exp, camera)
+        W, H = s.camera.width, s.camera.height
+        img = np.zeros((H, W, 3), dtype=np.float64)
+        r0, r1 = rows if rows is not None else (0, H)
+        g = None
+        if guide is not None:
+            vmm = np.ascontiguousarray(guide["vmm"])
+            keep["_vmm"] = vmm
+            g = PgoGuide((C.c_float * 6)(*[float(x) for x in guide["root"]]), guide["split_count"],
+                         vmm.ctypes.data, int(guide.get("use_parallax", 1)))
+        self.lib.pgo_render_f64(C.byref(s), C.byref(params), C.byref(g) if g is not None else None, img.ctypes.data,
+                                r0, r1, threads or (os.cpu_count() or 1))
+        return img
+
+    def rnd(self, seed, pixel, sample, dim):
+        return self.lib.pgo_rnd(seed, pixel, sample, dim)

@@ -58,6 +58,17 @@ SIGNATURES = {
     "pg_update_distances": (_I, [_P, _P, _P, _P, _U32, _P]),
     "pg_pack_vmm_theta": (_I, [_P, _U32, _P, _P]),
     "pg_update": (_I, [_P, _P, _U64, _P, _P]),
+    "pg_scene_load": (_I, [C.c_char_p, _U32, _U32, C.POINTER(_P)]),
+    "pg_scene_create_cornell": (_I, [C.POINTER(abi.CornellParams), C.POINTER(_P)]),
+    "pg_scene_create_plates": (_I, [C.POINTER(abi.PlatesParams), C.POINTER(_P)]),
+    "pg_scene_destroy": (_I, [_P]),
+    "pg_scene_get_info": (_I, [_P, C.POINTER(abi.SceneInfo)]),
+    "pg_scene_export": (_I, [_P, _P, _P, _P, _P, _P, _P]),
+    "pg_scene_export_mesh": (_I, [_P, _P, _P, C.POINTER(_U32)]),
+    "pg_scene_set_camera": (_I, [_P, C.POINTER(abi.Camera)]),
+    "pg_trace_closest": (_I, [_P, _P, _U32, _P, _P]),
+    "pg_trace_any": (_I, [_P, _P, _U32, _P, _P]),
+    "pg_render": (_I, [_P, C.POINTER(abi.RenderParams), _P, _P, _P, C.POINTER(abi.RenderStats), _P]),
 }
 
 _LIB = None
@@ -223,3 +234,91 @@ def fit_regions_noalloc(cfg: abi.FitConfig, states_dev, dirw, offsets, n_regions
     n_regions pg_region_state records, updated in place.  Returns the status."""
     return library().pg_fit_regions_noalloc(C.byref(cfg), _dptr(states_dev), _dptr(dirw), _dptr(offsets),
                                             n_regions, mode, _stream_handle(stream))
+
+
+class Scene:
+    """A pg_scene: geometry, materials, lights and camera with its BVH (SceneLoader)."""
+
+    def __init__(self, handle):
+        self.lib = library()
+        self.h = handle
+
+    @classmethod
+    def _make(cls, fn, *args):
+        lib = library()
+        h = C.c_void_p()
+        st = getattr(lib, fn)(*args, C.byref(h))
+        if st != abi.PG_OK:
+            raise PathGuideError(st, lib.pg_last_error(None).decode())
+        return cls(h)
+
+    @classmethod
+    def cornell(cls, width=1280, height=720, ico_level=5, light_radiance=15.0, ior=1.5):
+        p = abi.CornellParams(width, height, ico_level, light_radiance, ior)
+        return cls._make("pg_scene_create_cornell", C.byref(p))
+
+    @classmethod
+    def plates(cls, width=1920, height=1080, occluder_grid=707, seed=4):
+        p = abi.PlatesParams(width, height, occluder_grid, seed)
+        return cls._make("pg_scene_create_plates", C.byref(p))
+
+    @classmethod
+    def load(cls, path, width, height):
+        return cls._make("pg_scene_load", str(path).encode(), width, height)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pg_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != abi.PG_OK:
+            raise PathGuideError(st, self.lib.pg_last_error(None).decode())
+
+    def info(self) -> abi.SceneInfo:
+        i = abi.SceneInfo()
+        self._check(self.lib.pg_scene_get_info(self.h, C.byref(i)))
+        return i
+
+    def set_camera(self, cam: abi.Camera):
+        self._check(self.lib.pg_scene_set_camera(self.h, C.byref(cam)))
+
+    def export(self) -> dict:
+        """Host copies of the built scene (BVH, triangles, materials, spheres, mesh)."""
+        i = self.info()
+        nodes = np.zeros(i.n_nodes, dtype=abi.NODE_DTYPE)
+        tv = np.zeros((i.n_triangles, 12), dtype=np.float32)
+        order = np.zeros(i.n_triangles, dtype=np.uint32)
+        tmat = np.zeros(i.n_triangles, dtype=np.uint32)
+        mats = np.zeros(i.n_materials, dtype=abi.MATERIAL_DTYPE)
+        sph = np.zeros(i.n_spheres, dtype=abi.SPHERE_DTYPE)
+        self._check(self.lib.pg_scene_export(self.h, nodes.ctypes.data, tv.ctypes.data, order.ctypes.data,
+                                             tmat.ctypes.data, mats.ctypes.data, sph.ctypes.data))
+        nv = C.c_uint32()
+        self._check(self.lib.pg_scene_export_mesh(self.h, None, None, C.byref(nv)))
+        pos = np.zeros((nv.value, 3), dtype=np.float32)
+        idx = np.zeros((i.n_triangles, 3), dtype=np.uint32)
+        self._check(self.lib.pg_scene_export_mesh(self.h, pos.ctypes.data, idx.ctypes.data, C.byref(nv)))
+        return {"nodes": nodes, "tri_verts": tv, "tri_order": order, "tri_mat": tmat, "mats": mats,
+                "spheres": sph, "pos": pos, "idx": idx, "info": i}
+
+    def trace_closest(self, rays_dev, n, hits_dev, stream=None):
+        self._check(self.lib.pg_trace_closest(self.h, _dptr(rays_dev), n, _dptr(hits_dev), _stream_handle(stream)))
+
+    def trace_any(self, rays_dev, n, occ_dev, stream=None):
+        self._check(self.lib.pg_trace_any(self.h, _dptr(rays_dev), n, _dptr(occ_dev), _stream_handle(stream)))
+
+    def render(self, params: abi.RenderParams, image_dev, guide: "FitContext | None" = None, records_dev=None,
+               stream=None) -> abi.RenderStats:
+        """Adds params.spp samples per pixel of radiance into image_dev (float32, H*W*3)."""
+        st = abi.RenderStats()
+        self._check(self.lib.pg_render(self.h, C.byref(params), guide.h if guide is not None else None,
+                                       _dptr(image_dev), _dptr(records_dev) if records_dev is not None else None,
+                                       C.byref(st), _stream_handle(stream)))
+        return st

@@ -70,3 +70,53 @@ def forced_iterations(n: int, **kw) -> FitConfig:
 
 def ptr(a: np.ndarray) -> C.c_void_p:
     return C.c_void_p(a.ctypes.data)
+
+# ---- tracer -------------------------------------------------------------
+PG_MAT_DIFFUSE, PG_MAT_SPECULAR, PG_MAT_DIELECTRIC, PG_MAT_LIGHT, PG_MAT_GGX = 0, 1, 2, 3, 6
+NO_HIT = 0xFFFFFFFF
+SPHERE_BIT = 0x80000000
+
+MATERIAL_DTYPE = np.dtype([("type", "<i4"), ("albedo", "<f4", (3,)), ("emission", "<f4", (3,)),
+                           ("roughness", "<f4"), ("ior", "<f4"), ("reserved", "<i4", (3,))])
+SPHERE_DTYPE = np.dtype([("center", "<f4", (3,)), ("radius", "<f4"), ("material", "<u4"), ("reserved", "<u4", (3,))])
+RAY_DTYPE = np.dtype([("org", "<f4", (3,)), ("tmin", "<f4"), ("dir", "<f4", (3,)), ("tmax", "<f4")])
+HIT_DTYPE = np.dtype([("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("prim", "<u4")])
+NODE_DTYPE = np.dtype([("lo0", "<f4", (3,)), ("hi0", "<f4", (3,)), ("lo1", "<f4", (3,)), ("hi1", "<f4", (3,)),
+                       ("child", "<i4", (2,)), ("count", "<i4", (2,))])
+assert MATERIAL_DTYPE.itemsize == 48 and SPHERE_DTYPE.itemsize == 32 and RAY_DTYPE.itemsize == 32
+assert HIT_DTYPE.itemsize == 16 and NODE_DTYPE.itemsize == 64
+
+
+class Camera(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("target", C.c_float * 3), ("up", C.c_float * 3),
+                ("vfov_deg", C.c_float), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+class CornellParams(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("ico_level", C.c_int32),
+                ("light_radiance", C.c_float), ("ior", C.c_float)]
+
+
+class PlatesParams(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("occluder_grid", C.c_uint32), ("seed", C.c_uint32)]
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [("n_triangles", C.c_uint32), ("n_spheres", C.c_uint32), ("n_materials", C.c_uint32),
+                ("n_nodes", C.c_uint32), ("n_lights", C.c_uint32), ("aabb", C.c_float * 6), ("camera", Camera)]
+
+
+class RenderParams(C.Structure):
+    _fields_ = [("spp", C.c_uint32), ("max_depth", C.c_uint32), ("seed", C.c_uint32), ("use_nee", C.c_uint32),
+                ("use_mis", C.c_uint32), ("use_guiding", C.c_uint32), ("guiding_prob", C.c_float),
+                ("record_samples", C.c_uint32), ("reserved", C.c_uint32 * 4)]
+
+
+class RenderStats(C.Structure):
+    _fields_ = [("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("samples_recorded", C.c_uint64),
+                ("paths", C.c_uint64)]
+
+
+def render_params(spp=1, max_depth=8, seed=1, use_nee=1, use_mis=1, use_guiding=0, guiding_prob=0.5,
+                  record_samples=0) -> RenderParams:
+    return RenderParams(spp, max_depth, seed, use_nee, use_mis, use_guiding, guiding_prob, record_samples)

@@ -473,6 +473,9 @@ struct GuideScratch {
     uint32_t split_count = 0;
     uint64_t cap_samples = 0;
     bool fitted = false;
+    pg_vmm_theta *vmm = nullptr;   // packed mixtures for the renderer
+    bool vmm_fresh = false;
+    float root[6] = {0, 0, 0, 0, 0, 0};
 };
 
 static GuideScratch &guide(pg_ctx *ctx) {
@@ -495,6 +498,7 @@ void guide_release(pg_ctx *ctx) {
     cudaFree(g.order);
     cudaFree(g.means);
     cudaFree(g.aabbs);
+    cudaFree(g.vmm);
     delete static_cast<GuideScratch *>(ctx->guide);
     ctx->guide = nullptr;
 }
@@ -573,6 +577,24 @@ static int sort_records(pg_ctx *ctx, const pg_directional_data *rec, uint64_t n,
     return check_cuda(ctx, cudaGetLastError(), "sort launch");
 }
 
+namespace pg {
+int guide_view(pg_ctx *ctx, GuideView *out, cudaStream_t s) {
+    GuideScratch &g = guide(ctx);
+    if (!g.aabbs || !g.vmm) return set_error(ctx, PG_ERR_STATE, "pg_set_regions must run before guided rendering");
+    if (!g.vmm_fresh) {
+        int st = pg_pack_vmm_theta(ctx, g.n_regions, g.vmm, s);
+        if (st) return st;
+        g.vmm_fresh = true;
+    }
+    for (int i = 0; i < 6; ++i) out->root[i] = g.root[i];
+    out->split_count = g.split_count;
+    out->n_regions = g.n_regions;
+    out->vmm = g.vmm;
+    out->use_parallax = ctx->cfg.use_parallax ? 1 : 0;
+    return PG_OK;
+}
+}  // namespace pg
+
 extern "C" {
 
 int pg_set_regions(pg_ctx *ctx, uint32_t split_count, const float scene_aabb[6], void *stream) {
@@ -595,12 +617,26 @@ int pg_set_regions(pg_ctx *ctx, uint32_t split_count, const float scene_aabb[6],
     g.n_regions = n;
     g.split_count = split_count;
     g.fitted = false;
+    g.vmm_fresh = false;
+    for (int i = 0; i < 3; ++i) {  // Aabb::addEpsilon (src/Shapes.h:48-53)
+        const float ext = scene_aabb[3 + i] - scene_aabb[i];
+        const float cen = scene_aabb[i] + 0.5f * ext;
+        g.root[i] = cen - 0.50001f * ext;
+        g.root[3 + i] = cen + 0.50001f * ext;
+    }
+    cudaFree(g.vmm);
+    g.vmm = nullptr;
+    {
+        int st0 = check_cuda(ctx, cudaMalloc(&g.vmm, sizeof(pg_vmm_theta) * n), "packed mixtures");
+        if (st0) return st0;
+    }
     int st = check_cuda(ctx, cudaMemcpyAsync(g.aabbs, boxes.data(), sizeof(float) * 6 * n, cudaMemcpyHostToDevice, s),
                         "region boxes upload");
     if (!st) st = check_cuda(ctx, cudaStreamSynchronize(s), "region boxes sync");
     if (st) return st;
     return pg_init_regions(ctx, n, stream);
 }
+
 
 int pg_region_count(const pg_ctx *ctx, uint32_t *out) {
     if (!ctx || !out) return PG_ERR_ARG;
@@ -724,8 +760,12 @@ int pg_update(pg_ctx *ctx, const pg_directional_data *records, uint64_t n_record
         if (st) return st;
     }
     g.fitted = true;
-    // 5. VMM_Theta for the tracer
-    if (vmm_out) st = pg_pack_vmm_theta(ctx, R, vmm_out, stream);
+    // 5. VMM_Theta for the tracer (the context's copy, and the caller's if asked)
+    st = pg_pack_vmm_theta(ctx, R, g.vmm, stream);
+    if (st) return st;
+    g.vmm_fresh = true;
+    if (vmm_out) st = check_cuda(ctx, cudaMemcpyAsync(vmm_out, g.vmm, sizeof(pg_vmm_theta) * R,
+                                                      cudaMemcpyDeviceToDevice, s), "VMM_Theta copy");
     return st;
 }
 

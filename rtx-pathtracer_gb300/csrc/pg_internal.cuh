@@ -44,6 +44,18 @@ int check_cuda(pg_ctx *ctx, cudaError_t e, const char *what);
 int upload_init_table(pg_ctx *ctx, cudaStream_t s);
 void guide_release(pg_ctx *ctx);
 
+// What the renderer needs from a guiding context: the padded root box and
+// split count of the region tree (point -> region by descent) and the packed
+// VMM_Theta of every region.
+struct GuideView {
+    float root[6];
+    uint32_t split_count;
+    uint32_t n_regions;
+    const pg_vmm_theta *vmm;
+    int use_parallax;
+};
+int guide_view(pg_ctx *ctx, GuideView *out, cudaStream_t s);
+
 constexpr float kLog2e = 1.4426950408889634f;
 constexpr float kLn2 = 0.6931471805599453f;
 constexpr float kInv4Pi = 0.0795774715459476679f;

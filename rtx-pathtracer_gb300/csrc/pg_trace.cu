@@ -1,0 +1,1109 @@
+// pg_trace.cu - scenes on the device, ray queries, and the wavefront path
+// tracer with NEE, MIS, vMF-mixture guiding and guiding-sample recording.
+//
+// The reference traces one megakernel per pixel on RT cores (shaders/
+// raytrace.rgen:1623-1827, raytrace :992-1226).  Here each bounce of all pixels'
+// paths runs as separate stages over compacted queues:
+//   extend  - closest hit of every active path (BVH traversal, pg_traverse.cuh)
+//   shade   - emission with MIS, next-event estimation (a shadow-ray entry in
+//             a queue), BSDF or guided sampling of the continuation, guiding
+//             record bookkeeping; survivors are appended to the next queue
+//   shadow  - any hit of every shadow ray; unoccluded NEE is added to the
+//             image and to the path's guiding records
+//   commit  - after the last bounce, record weights |L| / pdf
+//             (raytrace.rgen:980-990)
+// Path state is structure-of-arrays indexed by pixel (one path per pixel per
+// sample), so every stage reads coalesced rows.
+//
+// Estimator (ours, restated in FP64 by oracle/pg_oracle_trace.cpp):
+//   lights are picked uniformly (getLightSamplingVector gives every light power
+//   1, src/SceneLoader.cpp:923-944), mesh lights sample a triangle by area and
+//   a uniform point on it (raytrace.rgen:436-472), sphere lights a uniform
+//   point on the sphere (random.glsl:108-115); NEE and BSDF-sampled emission
+//   are combined with the power heuristic (raytrace.rgen:488-493); BSDFs:
+//   Lambert (cosine sampling), GGX conductor (Smith G, Schlick F, NDF
+//   sampling), smooth dielectric (exact Fresnel, raytrace.rgen:145-160,
+//   reflect/refract choice by Fresnel, raytrace.rgen:526-541), mirror.
+//   Guided vertices draw from the region's vMF mixture with probability
+//   guiding_prob and use the one-sample mixture pdf (raytrace.rgen:923-960).
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../host/pg_scene.h"
+#include "pg_internal.cuh"
+#include "pg_traverse.cuh"
+
+namespace pg {
+
+constexpr float kPi = 3.14159265358979323846f;
+constexpr float kTMin = 0.001f;    // tMin of raytrace.rgen:51
+constexpr float kTMax = 1.0e6f;    // tMax of raytrace.rgen:52
+constexpr int kMaxRecords = 16;    // MAX_DIRECTIONAL_DATA_PER_PIXEL (shaders/limits.glsl:7)
+
+struct DevLight {
+    int32_t type;      // 0: triangle mesh, 1: sphere
+    uint32_t first;    // into light_tris / light_cdf
+    uint32_t count;
+    uint32_t sphere;
+    float area;
+    float emission[3];
+};
+
+// ---------------------------------------------------------------------------
+// Random numbers: stateless hash of (seed, pixel, sample, dimension), so the
+// FP64 oracle draws the same numbers.
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ uint32_t fmix32(uint32_t h) {
+    h ^= h >> 16;
+    h *= 0x85ebca6bu;
+    h ^= h >> 13;
+    h *= 0xc2b2ae35u;
+    h ^= h >> 16;
+    return h;
+}
+__host__ __device__ __forceinline__ float rnd(uint32_t seed, uint32_t pixel, uint32_t sample, uint32_t dim) {
+    const uint32_t h = fmix32(seed + fmix32(pixel + fmix32(sample * 1024u + dim)));
+    return (float)(h >> 8) * (1.0f / 16777216.0f);
+}
+// dimension of the d-th number at bounce b
+__host__ __device__ __forceinline__ uint32_t dimb(int b, int d) { return 2u + 16u * (uint32_t)b + (uint32_t)d; }
+
+struct V {
+    float x, y, z;
+};
+__device__ __forceinline__ V mk(float x, float y, float z) { return V{x, y, z}; }
+__device__ __forceinline__ V add(V a, V b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V sub(V a, V b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ V mul(V a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ V hmul(V a, V b) { return mk(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ float dot3(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V cross3(V a, V b) { return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+__device__ __forceinline__ V nrm(V a) { return mul(a, rsqrtf(dot3(a, a))); }
+__device__ __forceinline__ float maxc(V a) { return fmaxf(a.x, fmaxf(a.y, a.z)); }
+
+// Orthonormal frame around n (transform.glsl:7-16, coordinateAxis).
+__device__ __forceinline__ void frame(V n, V &x, V &y) {
+    if (fabsf(n.x) > fabsf(n.y)) {
+        const float inv = rsqrtf(n.x * n.x + n.z * n.z);
+        y = mk(n.z * inv, 0.0f, -n.x * inv);
+    } else {
+        const float inv = rsqrtf(n.y * n.y + n.z * n.z);
+        y = mk(0.0f, n.z * inv, -n.y * inv);
+    }
+    x = cross3(y, n);
+}
+__device__ __forceinline__ V to_world(V l, V n) {
+    V x, y;
+    frame(n, x, y);
+    return add(add(mul(x, l.x), mul(y, l.y)), mul(n, l.z));
+}
+__device__ __forceinline__ V reflect3(V i, V n) { return sub(i, mul(n, 2.0f * dot3(n, i))); }
+
+// Fresnel of a dielectric (raytrace.rgen:145-160); eta = n_i / n_t.
+__device__ __forceinline__ float fresnel_dielectric(float eta, float cos_i) {
+    const float s2 = eta * eta * (1.0f - cos_i * cos_i);
+    if (s2 > 1.0f) return 1.0f;
+    const float cos_t = sqrtf(1.0f - s2);
+    const float rs = (eta * cos_i - cos_t) / (eta * cos_i + cos_t);
+    const float rp = (cos_i - eta * cos_t) / (cos_i + eta * cos_t);
+    return 0.5f * (rs * rs + rp * rp);
+}
+
+// GGX microfacet conductor.
+__device__ __forceinline__ float ggx_D(float a2, float cos_m) {
+    const float c2 = cos_m * cos_m;
+    const float d = c2 * (a2 - 1.0f) + 1.0f;
+    return a2 / (kPi * d * d);
+}
+__device__ __forceinline__ float ggx_G1(float a2, float cos_v) {
+    const float c = fabsf(cos_v);
+    return 2.0f * c / (c + sqrtf(a2 + (1.0f - a2) * c * c));
+}
+
+struct MatEval {
+    V f;        // BSDF * cos(theta_o)
+    float pdf;  // solid-angle pdf of sampling wo
+};
+
+// BSDF value times cosine and sampling pdf for a non-delta material.
+__device__ __forceinline__ MatEval bsdf_eval(const pg_material &m, V n, V wi, V wo) {
+    MatEval r{mk(0, 0, 0), 0.0f};
+    const float co = dot3(n, wo), ci = dot3(n, wi);
+    if (co <= 0.0f || ci <= 0.0f) return r;
+    if (m.type == PG_MAT_DIFFUSE) {
+        r.f = mul(mk(m.albedo[0], m.albedo[1], m.albedo[2]), co / kPi);
+        r.pdf = co / kPi;
+    } else if (m.type == PG_MAT_GGX) {
+        const V h = nrm(add(wi, wo));
+        const float a2 = fmaxf(m.roughness * m.roughness, 1e-12f);
+        const float ch = dot3(n, h), hi = dot3(wi, h);
+        const float D = ggx_D(a2, ch);
+        const float G = ggx_G1(a2, ci) * ggx_G1(a2, co);
+        const float w = powf(1.0f - fmaxf(hi, 0.0f), 5.0f);
+        const V F = mk(m.albedo[0] + (1.0f - m.albedo[0]) * w, m.albedo[1] + (1.0f - m.albedo[1]) * w,
+                       m.albedo[2] + (1.0f - m.albedo[2]) * w);
+        r.f = mul(F, D * G / (4.0f * ci));
+        r.pdf = D * ch / (4.0f * fabsf(hi));
+    }
+    return r;
+}
+
+__device__ __forceinline__ bool is_delta(const pg_material &m) {
+    return m.type == PG_MAT_DIELECTRIC || m.type == PG_MAT_SPECULAR;  // hasDiscreteDirection
+}
+// isMatAlmostDiscrete (raytrace.rgen:962-964): glossy lobes that are not recorded
+__device__ __forceinline__ bool almost_delta(const pg_material &m) {
+    return m.type == PG_MAT_GGX && m.roughness <= 0.3f;
+}
+
+// ---------------------------------------------------------------------------
+// Guiding: region lookup and the vMF mixture (shaders/guiding.glsl:32-96)
+// ---------------------------------------------------------------------------
+struct DevGuide {
+    float root[6];
+    uint32_t split_count;
+    const pg_vmm_theta *vmm;
+    int use_parallax;
+};
+
+// Point -> region by descending the midpoint split tree with the same float
+// arithmetic that built it; points outside the root box (or in a rounding gap)
+// have no region (getGuidingRegion returns -1, raytrace.rgen:904-921).
+__device__ __forceinline__ uint32_t region_of(const DevGuide &g, V p) {
+    float lo[3] = {g.root[0], g.root[1], g.root[2]}, hi[3] = {g.root[3], g.root[4], g.root[5]};
+    const float pp[3] = {p.x, p.y, p.z};
+    for (int i = 0; i < 3; ++i)
+        if (!(pp[i] >= lo[i] && pp[i] <= hi[i])) return PG_INVALID_REGION;
+    uint32_t id = 0;
+    for (uint32_t l = 0; l < g.split_count; ++l) {
+        float size[3];
+        for (int i = 0; i < 3; ++i) size[i] = __fsub_rn(hi[i], lo[i]);
+        const int ax = size[0] > size[1] ? (size[0] > size[2] ? 0 : 2) : (size[1] > size[2] ? 1 : 2);
+        const float lhi = __fsub_rn(hi[ax], __fmul_rn(0.5f, size[ax]));
+        const float rlo = __fadd_rn(lo[ax], __fmul_rn(0.5f, size[ax]));
+        if (pp[ax] <= lhi) {
+            hi[ax] = lhi;
+            id = 2u * id;
+        } else if (pp[ax] >= rlo) {
+            lo[ax] = rlo;
+            id = 2u * id + 1u;
+        } else {
+            return PG_INVALID_REGION;
+        }
+    }
+    return id;
+}
+
+__device__ __forceinline__ V lobe_mu(const pg_vmf_theta &t, V x, int par) {
+    V mu = mk(t.mu[0], t.mu[1], t.mu[2]);
+    if (par && t.distance > 0.0f) mu = nrm(sub(mk(t.target[0], t.target[1], t.target[2]), x));
+    return mu;
+}
+
+// VMM pdf (guiding.glsl:32-60)
+__device__ float vmm_pdf(const pg_vmm_theta &v, V wo, V x, int par) {
+    float res = 0.0f;
+    const int K = min(v.used_distributions, 16);
+    for (int i = 0; i < K; ++i) {
+        const pg_vmf_theta &t = v.thetas[i];
+        float f;
+        if (t.k == 0.0f) {
+            f = 1.0f / (4.0f * kPi);
+        } else {
+            const V mu = lobe_mu(t, x, par);
+            f = t.norm * expf(t.k * (dot3(mu, wo) - 1.0f));
+        }
+        res += v.pi[i] * f;
+    }
+    return res;
+}
+
+// sampleVMM (guiding.glsl:62-96): pick a lobe by walking the weights, then
+// invert the vMF cosine CDF.
+__device__ V vmm_sample(const pg_vmm_theta &v, V x, int par, float u_lobe, float u1, float u2) {
+    const int K = min(v.used_distributions, 16);
+    int i = 0;
+    float acc = v.pi[0];
+    while (acc < u_lobe && i < K - 1) {
+        ++i;
+        acc += v.pi[i];
+    }
+    const pg_vmf_theta &t = v.thetas[i];
+    if (t.k > 0.0f) {
+        const float ct = 1.0f + logf(1.0f + t.e_min2k * u1 - u1) / t.k;
+        const float st = 1.0f - ct * ct <= 0.0f ? 0.0f : sqrtf(1.0f - ct * ct);
+        const float ph = 2.0f * kPi * u2;
+        return to_world(mk(st * cosf(ph), st * sinf(ph), ct), lobe_mu(t, x, par));
+    }
+    const float z = 1.0f - 2.0f * u1;  // uniform sphere
+    const float r = sqrtf(fmaxf(0.0f, 1.0f - z * z));
+    const float ph = 2.0f * kPi * u2;
+    return mk(r * cosf(ph), r * sinf(ph), z);
+}
+
+// ---------------------------------------------------------------------------
+// Device scene and render state
+// ---------------------------------------------------------------------------
+struct DevRender {
+    DevScene S;
+    const float *pos;            // 3 per vertex (original)
+    const uint32_t *idx;         // 3 per triangle (original)
+    const uint32_t *tri_mat;     // per original triangle
+    const pg_material *mats;
+    const DevLight *lights;
+    uint32_t n_lights;
+    const uint32_t *light_tris;  // original triangle ids of mesh lights
+    const float *light_cdf;      // per light, cumulative area fraction
+    const int32_t *tri_light;    // light index of each original triangle, -1 if none
+    unsigned long long *stats;   // [0] extension rays, [1] shadow rays
+    pg_camera cam;
+    float cam_fwd[3], cam_right[3], cam_up[3], tan_half;
+    pg_render_params rp;
+    uint32_t sample;             // sample index of this pass
+    DevGuide guide;
+    int guiding;
+    int recording;
+    // path state (indexed by pixel)
+    float *ro, *rd, *thr;        // 3 per path
+    float *prev_pdf;             // pdf of the sampled direction (0: camera or delta)
+    uint8_t *alive;
+    uint8_t *found;              // radiance reached the camera on this path
+    pg_hit *hits;
+    uint32_t *q_cur, *q_next;
+    uint32_t *counters;          // [0] next queue, [1] shadow queue, [2] ext rays, [3] shadow rays, [4] records
+    // shadow queue
+    float *sh_o, *sh_d, *sh_tmax, *sh_c, *sh_l;  // origin, dir, tmax, contribution (thr * L), radiance L
+    uint32_t *sh_pix, *sh_nrec;
+    // guiding records
+    pg_directional_data *rec;    // 16 per pixel
+    float *rec_lsum, *rec_tc;    // 3 floats per slot: radiance sum, throughput change
+    uint32_t *rec_count, *rec_start;
+    int32_t *rec_pending;        // slot awaiting its distance, -1 if none
+    float *rec_factor;           // apparent-distance factor through refraction
+    float *image;
+};
+
+__device__ __forceinline__ V ld3(const float *a, uint32_t i) { return mk(a[3 * i], a[3 * i + 1], a[3 * i + 2]); }
+__device__ __forceinline__ void st3(float *a, uint32_t i, V v) {
+    a[3 * i] = v.x;
+    a[3 * i + 1] = v.y;
+    a[3 * i + 2] = v.z;
+}
+
+__device__ __forceinline__ void warp_append(uint32_t *counter, uint32_t *queue, uint32_t value, bool pred) {
+    const unsigned m = __ballot_sync(__activemask(), pred);
+    if (!pred) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+    base = __shfl_sync(m, base, leader);
+    queue[base + __popc(m & ((1u << lane) - 1u))] = value;
+}
+
+// updateSamples (raytrace.rgen:973-978): radiance L arriving at the vertex
+// after record slot n-1 flows back through the recorded throughput changes.
+__device__ __forceinline__ void update_records(const DevRender &R, uint32_t pix, uint32_t n, V L) {
+    const uint32_t start = R.rec_start[pix];
+    for (int i = (int)n - 1; i >= (int)start; --i) {
+        const uint32_t s = pix * kMaxRecords + (uint32_t)i;
+        R.rec_lsum[3 * s] += L.x;
+        R.rec_lsum[3 * s + 1] += L.y;
+        R.rec_lsum[3 * s + 2] += L.z;
+        L = hmul(L, ld3(R.rec_tc, s));
+    }
+}
+
+// Solid-angle pdf of NEE picking the emitter point hit at distance t with
+// surface normal nl, seen along direction d.
+__device__ __forceinline__ float light_pdf(const DevRender &R, uint32_t light, float t, float cos_l) {
+    const DevLight &L = R.lights[light];
+    return (t * t) / (fmaxf(cos_l, 1e-12f) * L.area) / (float)R.n_lights;
+}
+
+__global__ void k_camera(DevRender R) {
+    const uint32_t W = R.cam.width, H = R.cam.height;
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= W * H) return;
+    const uint32_t px = pix % W, py = pix / W;
+    // getCameraRay (raytrace.rgen:1487-1494): jitter within the pixel
+    const float jx = rnd(R.rp.seed, pix, R.sample, 0) - 0.5f, jy = rnd(R.rp.seed, pix, R.sample, 1) - 0.5f;
+    const float aspect = (float)W / (float)H;
+    const float sx = (2.0f * ((float)px + 0.5f + jx) / (float)W - 1.0f) * R.tan_half * aspect;
+    const float sy = (1.0f - 2.0f * ((float)py + 0.5f + jy) / (float)H) * R.tan_half;
+    const V f = mk(R.cam_fwd[0], R.cam_fwd[1], R.cam_fwd[2]);
+    const V r = mk(R.cam_right[0], R.cam_right[1], R.cam_right[2]);
+    const V u = mk(R.cam_up[0], R.cam_up[1], R.cam_up[2]);
+    const V d = nrm(add(add(f, mul(r, sx)), mul(u, sy)));
+    st3(R.ro, pix, mk(R.cam.origin[0], R.cam.origin[1], R.cam.origin[2]));
+    st3(R.rd, pix, d);
+    st3(R.thr, pix, mk(1, 1, 1));
+    R.prev_pdf[pix] = 0.0f;
+    R.alive[pix] = 1;
+    R.found[pix] = 0;
+    R.q_cur[pix] = pix;
+    if (pix == 0) {
+        R.counters[0] = W * H;
+        R.counters[1] = 0;
+        R.counters[2] = 0;
+    }
+    if (R.recording) {
+        R.rec_count[pix] = R.rec_start[pix];
+        R.rec_pending[pix] = -1;
+        R.rec_factor[pix] = 1.0f;
+    }
+}
+
+// Queue lengths live on the device (counters[0]: current queue, [1]: next
+// queue being appended, [2]: shadow queue); kernels are launched over all
+// pixels and threads past the length return, so a render needs no host sync.
+__global__ void k_extend(DevRender R) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= R.counters[0]) return;
+    const uint32_t p = R.q_cur[i];
+    const float o[3] = {R.ro[3 * p], R.ro[3 * p + 1], R.ro[3 * p + 2]};
+    const float d[3] = {R.rd[3 * p], R.rd[3 * p + 1], R.rd[3 * p + 2]};
+    pg_hit h;
+    trace_closest(R.S, o, d, kTMin, kTMax, h);
+    R.hits[p] = h;
+}
+
+__global__ void k_shade(DevRender R, int bounce, int last) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= R.counters[0]) return;
+    const uint32_t p = R.q_cur[i];
+    const pg_hit h = R.hits[p];
+    const V d = ld3(R.rd, p);
+    V thr = ld3(R.thr, p);
+    bool cont = false;
+    const bool rec_on = R.recording != 0;
+    if (h.prim == PG_NO_HIT) {
+        // miss: black environment; a pending record saw infinity (distance 0)
+        if (rec_on && R.rec_pending[p] >= 0) {
+            R.rec[p * kMaxRecords + (uint32_t)R.rec_pending[p]].distance = 0.0f;
+            R.rec_pending[p] = -1;
+        }
+    } else {
+        const V o = ld3(R.ro, p);
+        const V x = add(o, mul(d, h.t));
+        V ng;
+        uint32_t mat_id;
+        uint32_t light_id = 0xFFFFFFFFu;
+        if (h.prim & PG_SPHERE_BIT) {
+            const pg_sphere &sp = R.S.spheres[h.prim & ~PG_SPHERE_BIT];
+            ng = mul(sub(x, mk(sp.center[0], sp.center[1], sp.center[2])), 1.0f / sp.radius);
+            mat_id = sp.material;
+        } else {
+            const uint32_t t = h.prim;
+            const V v0 = ld3(R.pos, R.idx[3 * t]), v1 = ld3(R.pos, R.idx[3 * t + 1]), v2 = ld3(R.pos, R.idx[3 * t + 2]);
+            ng = nrm(cross3(sub(v1, v0), sub(v2, v0)));
+            mat_id = R.tri_mat[t];
+        }
+        const pg_material m = R.mats[mat_id];
+        const bool front = dot3(d, ng) < 0.0f;  // raytrace.rchit:42-48
+        const V n = front ? ng : mul(ng, -1.0f);
+        const V wi = mul(d, -1.0f);
+        // distance of a pending record (raytrace.rgen:1149-1156, 1201-1212)
+        if (rec_on && R.rec_pending[p] >= 0) {
+            pg_directional_data &rd = R.rec[p * kMaxRecords + (uint32_t)R.rec_pending[p]];
+            rd.distance += h.t * R.rec_factor[p];
+            if (!is_delta(m) && !almost_delta(m)) R.rec_pending[p] = -1;
+        }
+        if (m.type == PG_MAT_LIGHT) {
+            // emission, MIS-weighted against NEE unless seen from the camera or a delta bounce
+            float w = 1.0f;
+            const float pp = R.prev_pdf[p];
+            if (R.rp.use_nee && pp > 0.0f) {
+                if (!R.rp.use_mis) {
+                    w = 0.0f;
+                } else {
+                    // the light of this emitter
+                    if (h.prim & PG_SPHERE_BIT) {
+                        for (uint32_t l = 0; l < R.n_lights; ++l)
+                            if (R.lights[l].type == 1 && R.lights[l].sphere == (h.prim & ~PG_SPHERE_BIT)) light_id = l;
+                    } else if (R.tri_light[h.prim] >= 0) {
+                        light_id = (uint32_t)R.tri_light[h.prim];
+                    }
+                    if (light_id != 0xFFFFFFFFu) {
+                        const float cl = fabsf(dot3(ng, d));
+                        const float pl = light_pdf(R, light_id, h.t, cl);
+                        w = pp * pp / (pp * pp + pl * pl);
+                    }
+                }
+            }
+            if (front || (h.prim & PG_SPHERE_BIT) == 0) {
+                const V Le = mul(mk(m.emission[0], m.emission[1], m.emission[2]), w);
+                if (maxc(Le) > 0.0f) {
+                    const V c = hmul(thr, Le);
+                    atomicAdd(&R.image[3 * p], c.x);
+                    atomicAdd(&R.image[3 * p + 1], c.y);
+                    atomicAdd(&R.image[3 * p + 2], c.z);
+                    R.found[p] = 1;
+                    if (rec_on) update_records(R, p, R.rec_count[p], Le);
+                }
+            }
+        } else if (!last) {
+            const int b = bounce;
+            // --- next-event estimation (raytrace.rgen:601-731)
+            if (R.rp.use_nee && !is_delta(m) && R.n_lights > 0) {
+                const uint32_t l =
+                    min((uint32_t)(rnd(R.rp.seed, p, R.sample, dimb(b, 0)) * (float)R.n_lights), R.n_lights - 1);
+                const DevLight &L = R.lights[l];
+                const float u1 = rnd(R.rp.seed, p, R.sample, dimb(b, 1)), u2 = rnd(R.rp.seed, p, R.sample, dimb(b, 2));
+                V lp, ln;
+                if (L.type == 1) {
+                    const pg_sphere &sp = R.S.spheres[L.sphere];
+                    const float z = 1.0f - 2.0f * u1, rr = sqrtf(fmaxf(0.0f, 1.0f - z * z)), ph = 2.0f * kPi * u2;
+                    ln = mk(rr * cosf(ph), rr * sinf(ph), z);
+                    lp = add(mk(sp.center[0], sp.center[1], sp.center[2]), mul(ln, sp.radius));
+                } else {
+                    // triangle by area, then a uniform point (raytrace.rgen:445-456)
+                    uint32_t lo = 0, hi = L.count - 1;
+                    const float uc = u1;
+                    while (lo < hi) {
+                        const uint32_t mid = (lo + hi) / 2;
+                        if (R.light_cdf[L.first + mid] < uc)
+                            lo = mid + 1;
+                        else
+                            hi = mid;
+                    }
+                    const float c0 = lo == 0 ? 0.0f : R.light_cdf[L.first + lo - 1];
+                    const float c1 = R.light_cdf[L.first + lo];
+                    const float ur = c1 > c0 ? fminf((uc - c0) / (c1 - c0), 0.99999994f) : 0.5f;
+                    const uint32_t t = R.light_tris[L.first + lo];
+                    const V a = ld3(R.pos, R.idx[3 * t]), bb = ld3(R.pos, R.idx[3 * t + 1]), c = ld3(R.pos, R.idx[3 * t + 2]);
+                    const float sx = sqrtf(ur);
+                    lp = add(add(mul(a, 1.0f - sx), mul(bb, sx * (1.0f - u2))), mul(c, u2 * sx));
+                    ln = nrm(cross3(sub(bb, a), sub(c, a)));
+                }
+                V tl = sub(lp, x);
+                const float dist2 = dot3(tl, tl), dist = sqrtf(dist2);
+                const V wl = mul(tl, 1.0f / dist);
+                float cl = -dot3(wl, ln);
+                if (L.type == 0) cl = fabsf(cl);  // two-sided mesh lights (raytrace.rgen:463-466)
+                if (cl > 0.0f && dot3(n, wl) > 0.0f) {
+                    const float pl = dist2 / (cl * L.area) / (float)R.n_lights;
+                    const MatEval me = bsdf_eval(m, n, wi, wl);
+                    if (maxc(me.f) > 0.0f) {
+                        float pb = me.pdf;
+                        if (R.guiding) {
+                            const uint32_t reg = region_of(R.guide, x);
+                            if (reg != PG_INVALID_REGION) {
+                                const float pg = vmm_pdf(R.guide.vmm[reg], wl, x, R.guide.use_parallax);
+                                pb = (1.0f - R.rp.guiding_prob) * pb + R.rp.guiding_prob * pg;
+                            }
+                        }
+                        const float w = R.rp.use_mis ? pl * pl / (pl * pl + pb * pb) : 1.0f;
+                        const V Lnee = mul(hmul(me.f, mk(L.emission[0], L.emission[1], L.emission[2])), w / pl);
+                        const uint32_t s = atomicAdd(&R.counters[2], 1u);
+                        st3(R.sh_o, s, x);
+                        st3(R.sh_d, s, wl);
+                        R.sh_tmax[s] = dist * (1.0f - 0.0001f);
+                        st3(R.sh_c, s, hmul(thr, Lnee));
+                        st3(R.sh_l, s, Lnee);
+                        R.sh_pix[s] = p;
+                        R.sh_nrec[s] = rec_on ? R.rec_count[p] : 0u;
+                    }
+                }
+            }
+            // --- continuation (getNewDirection, raytrace.rgen:923-960)
+            V wo = mk(0, 0, 1);
+            float pdf = 0.0f;
+            V tc = mk(0, 0, 0);  // throughput change f cos / pdf
+            bool delta = false;
+            const float uch = rnd(R.rp.seed, p, R.sample, dimb(b, 3));
+            const float ul = rnd(R.rp.seed, p, R.sample, dimb(b, 4));
+            const float u1 = rnd(R.rp.seed, p, R.sample, dimb(b, 5)), u2 = rnd(R.rp.seed, p, R.sample, dimb(b, 6));
+            if (m.type == PG_MAT_DIELECTRIC) {
+                const float eta = front ? 1.0f / m.ior : m.ior;  // refractionIndexInv in front
+                const float ci = dot3(wi, n);
+                const float F = fresnel_dielectric(eta, ci);
+                if (ul > F) {
+                    // refract(-wi, n, eta)
+                    const float k = 1.0f - eta * eta * (1.0f - ci * ci);
+                    wo = k < 0.0f ? reflect3(d, n) : sub(mul(d, eta), mul(n, eta * (-ci) + sqrtf(fmaxf(k, 0.0f))));
+                    wo = nrm(wo);
+                } else {
+                    wo = reflect3(d, n);
+                }
+                pdf = 1.0f;
+                tc = mk(m.albedo[0], m.albedo[1], m.albedo[2]);
+                delta = true;
+            } else if (m.type == PG_MAT_SPECULAR) {
+                wo = reflect3(d, n);
+                pdf = 1.0f;
+                tc = mk(m.albedo[0], m.albedo[1], m.albedo[2]);
+                delta = true;
+            } else {
+                bool use_guide = false;
+                uint32_t reg = PG_INVALID_REGION;
+                bool terminate = false;
+                if (R.guiding) {
+                    reg = region_of(R.guide, x);
+                    if (reg == PG_INVALID_REGION) terminate = true;  // no region: the path ends
+                    use_guide = uch < R.rp.guiding_prob;
+                }
+                if (!terminate) {
+                    if (use_guide) {
+                        const float ua = rnd(R.rp.seed, p, R.sample, dimb(b, 7));
+                        wo = vmm_sample(R.guide.vmm[reg], x, R.guide.use_parallax, ua, u1, u2);
+                    } else if (m.type == PG_MAT_DIFFUSE) {
+                        const float sr = sqrtf(u1), ph = 2.0f * kPi * u2;
+                        wo = to_world(mk(sr * cosf(ph), sr * sinf(ph), sqrtf(fmaxf(0.0f, 1.0f - u1))), n);
+                    } else {  // GGX: sample the normal distribution, reflect
+                        const float a2 = fmaxf(m.roughness * m.roughness, 1e-12f);
+                        const float t2 = a2 * u1 / fmaxf(1.0f - u1, 1e-12f);
+                        const float cm = rsqrtf(1.0f + t2), sm = sqrtf(fmaxf(0.0f, 1.0f - cm * cm));
+                        const float ph = 2.0f * kPi * u2;
+                        const V mh = to_world(mk(sm * cosf(ph), sm * sinf(ph), cm), n);
+                        wo = reflect3(d, mh);
+                    }
+                    const MatEval me = bsdf_eval(m, n, wi, wo);
+                    pdf = me.pdf;
+                    if (R.guiding && dot3(wo, n) > 0.0f && me.pdf > 0.0f) {
+                        const float pg = vmm_pdf(R.guide.vmm[reg], wo, x, R.guide.use_parallax);
+                        if (!isnan(pg)) pdf = (1.0f - R.rp.guiding_prob) * me.pdf + R.rp.guiding_prob * pg;
+                    }
+                    if (dot3(wo, n) > 0.0f && pdf > 0.0f && me.pdf > 0.0f) tc = mul(me.f, 1.0f / pdf);
+                    else pdf = 0.0f;
+                }
+            }
+            if (pdf > 0.0f && maxc(tc) > 0.0f) {
+                thr = hmul(thr, tc);
+                cont = true;
+                // guiding record of this vertex (raytrace.rgen:1179-1200)
+                if (rec_on) {
+                    const uint32_t cnt = R.rec_count[p];
+                    if (cnt < (uint32_t)kMaxRecords) {
+                        const uint32_t s = p * kMaxRecords + cnt;
+                        pg_directional_data rd;
+                        rd.position[0] = x.x;
+                        rd.position[1] = x.y;
+                        rd.position[2] = x.z;
+                        rd.direction[0] = wo.x;
+                        rd.direction[1] = wo.y;
+                        rd.direction[2] = wo.z;
+                        rd.weight = 0.0f;
+                        rd.pdf = pdf;
+                        rd.distance = 0.0f;
+                        if (delta || almost_delta(m)) {
+                            rd.flags = PG_INVALID_REGION;
+                        } else {
+                            rd.flags = region_of(R.guide, x);
+                            R.rec_pending[p] = (int32_t)cnt;
+                            R.rec_factor[p] = 1.0f;
+                        }
+                        R.rec[s] = rd;
+                        st3(R.rec_lsum, s, mk(0, 0, 0));
+                        st3(R.rec_tc, s, tc);
+                        R.rec_count[p] = cnt + 1;
+                    } else if (R.rec_pending[p] >= 0 && m.type == PG_MAT_DIELECTRIC && dot3(wo, n) < 0.0f) {
+                        const float eta = front ? m.ior : 1.0f / m.ior;
+                        R.rec_factor[p] = fabsf(dot3(n, d) / dot3(n, wo)) * eta;
+                    }
+                }
+                st3(R.ro, p, x);
+                st3(R.rd, p, wo);
+                st3(R.thr, p, thr);
+                R.prev_pdf[p] = delta ? 0.0f : pdf;
+            }
+        }
+    }
+    warp_append(&R.counters[1], R.q_next, p, cont);
+}
+
+__global__ void k_shadow(DevRender R) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= R.counters[2]) return;
+    const float o[3] = {R.sh_o[3 * i], R.sh_o[3 * i + 1], R.sh_o[3 * i + 2]};
+    const float d[3] = {R.sh_d[3 * i], R.sh_d[3 * i + 1], R.sh_d[3 * i + 2]};
+    if (trace_any(R.S, o, d, kTMin, R.sh_tmax[i])) return;
+    const uint32_t p = R.sh_pix[i];
+    atomicAdd(&R.image[3 * p], R.sh_c[3 * i]);
+    atomicAdd(&R.image[3 * p + 1], R.sh_c[3 * i + 1]);
+    atomicAdd(&R.image[3 * p + 2], R.sh_c[3 * i + 2]);
+    R.found[p] = 1;
+    if (R.recording) update_records(R, p, R.sh_nrec[i], ld3(R.sh_l, i));
+}
+
+// commitSamples (raytrace.rgen:980-990) and slot reuse when the path found no light
+__global__ void k_commit(DevRender R, uint32_t n_pix) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_pix) return;
+    const uint32_t start = R.rec_start[p], cnt = R.rec_count[p];
+    uint32_t valid = 0;
+    for (uint32_t k = start; k < cnt; ++k) {
+        const uint32_t s = p * kMaxRecords + k;
+        pg_directional_data &rd = R.rec[s];
+        const V L = ld3(R.rec_lsum, s);
+        const float w = sqrtf(dot3(L, L)) / rd.pdf;
+        if (!(w > 0.0f) || rd.flags == PG_INVALID_REGION) {
+            rd.flags = PG_INVALID_REGION;
+        } else {
+            rd.weight = w;
+            ++valid;
+        }
+    }
+    if (R.found[p]) {
+        R.rec_start[p] = cnt;
+        if (valid) atomicAdd(&R.counters[4], valid);
+    } else {
+        for (uint32_t k = start; k < cnt; ++k) R.rec[p * kMaxRecords + k].flags = PG_INVALID_REGION;
+        R.rec_count[p] = start;
+    }
+}
+
+// After a bounce: count the rays, make the next queue current.
+__global__ void k_advance(DevRender R) {
+    R.stats[0] += R.counters[0];
+    R.stats[1] += R.counters[2];
+    R.counters[0] = R.counters[1];
+    R.counters[1] = 0;
+    R.counters[2] = 0;
+}
+
+__global__ void k_reset_records(pg_directional_data *rec, uint32_t n_slots, uint32_t *rec_start, uint32_t n_pix) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_slots) rec[i].flags = PG_INVALID_REGION;
+    if (i < n_pix) rec_start[i] = 0;
+}
+
+__global__ void k_trace_closest(DevScene S, const pg_ray *rays, uint32_t n, pg_hit *hits) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const pg_ray r = rays[i];
+    pg_hit h;
+    trace_closest(S, r.org, r.dir, r.tmin, r.tmax, h);
+    hits[i] = h;
+}
+
+__global__ void k_trace_any(DevScene S, const pg_ray *rays, uint32_t n, uint32_t *occ) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const pg_ray r = rays[i];
+    occ[i] = trace_any(S, r.org, r.dir, r.tmin, r.tmax) ? 1u : 0u;
+}
+
+}  // namespace pg
+
+using namespace pg;
+
+// ---------------------------------------------------------------------------
+// Scene object
+// ---------------------------------------------------------------------------
+struct pg_scene {
+    SceneData host;
+    DevBvhNode *d_nodes = nullptr;
+    float4 *d_tris = nullptr;
+    pg_sphere *d_spheres = nullptr;
+    float *d_pos = nullptr;
+    uint32_t *d_idx = nullptr;
+    uint32_t *d_tri_mat = nullptr;
+    pg_material *d_mats = nullptr;
+    DevLight *d_lights = nullptr;
+    uint32_t *d_light_tris = nullptr;
+    float *d_light_cdf = nullptr;
+    int32_t *d_tri_light = nullptr;
+    unsigned long long *d_stats = nullptr;
+    uint32_t n_lights = 0;
+    bool uploaded = false;
+    std::vector<DevLight> h_lights;
+    std::vector<uint32_t> h_light_tris;
+    std::vector<float> h_light_cdf;
+    std::vector<int32_t> h_tri_light;
+    float aabb[6] = {0, 0, 0, 0, 0, 0};
+    // render scratch
+    uint32_t cap_pix = 0;
+    std::vector<void *> bufs;
+    DevRender R{};
+    uint32_t *d_counters = nullptr;
+};
+
+namespace {
+
+int scene_error(int st, const std::string &m) { return set_error(nullptr, st, m); }
+
+template <typename T>
+int upload(T **dst, const std::vector<T> &src) {
+    if (src.empty()) {
+        *dst = nullptr;
+        return PG_OK;
+    }
+    if (cudaMalloc(dst, sizeof(T) * src.size()) != cudaSuccess) return PG_ERR_CUDA;
+    if (cudaMemcpy(*dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice) != cudaSuccess) return PG_ERR_CUDA;
+    return PG_OK;
+}
+
+// Host side of scene creation: BVH, scene box and light tables.
+void build_host(pg_scene *sc) {
+    SceneData &s = sc->host;
+    build_bvh(s, 4);
+    // scene box (SceneLoader::calculateSceneSize, src/SceneLoader.cpp:350-368)
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (size_t v = 0; v < s.pos.size() / 3; ++v)
+        for (int i = 0; i < 3; ++i) {
+            lo[i] = std::min(lo[i], s.pos[3 * v + i]);
+            hi[i] = std::max(hi[i], s.pos[3 * v + i]);
+        }
+    for (const auto &sp : s.spheres)
+        for (int i = 0; i < 3; ++i) {
+            lo[i] = std::min(lo[i], sp.center[i] - sp.radius);
+            hi[i] = std::max(hi[i], sp.center[i] + sp.radius);
+        }
+    for (int i = 0; i < 3; ++i) {
+        sc->aabb[i] = lo[i];
+        sc->aabb[3 + i] = hi[i];
+    }
+    // lights: one per emissive material over triangles, one per emissive sphere
+    auto &lights = sc->h_lights;
+    auto &ltris = sc->h_light_tris;
+    auto &lcdf = sc->h_light_cdf;
+    auto &tri_light = sc->h_tri_light;
+    lights.clear();
+    ltris.clear();
+    lcdf.clear();
+    tri_light.assign(s.tri_mat.size(), -1);
+    for (uint32_t m = 0; m < s.mats.size(); ++m) {
+        if (s.mats[m].type != PG_MAT_LIGHT) continue;
+        DevLight L{};
+        L.type = 0;
+        L.first = (uint32_t)ltris.size();
+        double acc = 0.0;
+        std::vector<double> areas;
+        for (uint32_t t = 0; t < s.tri_mat.size(); ++t) {
+            if (s.tri_mat[t] != m) continue;
+            const float *a = &s.pos[3 * (size_t)s.idx[3 * t]], *b = &s.pos[3 * (size_t)s.idx[3 * t + 1]],
+                        *c = &s.pos[3 * (size_t)s.idx[3 * t + 2]];
+            const double e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+            const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
+                         cz = e1[0] * e2[1] - e1[1] * e2[0];
+            const double ar = 0.5 * sqrt(cx * cx + cy * cy + cz * cz);
+            ltris.push_back(t);
+            tri_light[t] = (int32_t)lights.size();
+            areas.push_back(ar);
+            acc += ar;
+        }
+        L.count = (uint32_t)(ltris.size() - L.first);
+        if (L.count == 0) continue;
+        double run = 0.0;
+        for (double ar : areas) {
+            run += ar;
+            lcdf.push_back((float)(run / acc));
+        }
+        lcdf.back() = 1.0f;
+        L.area = (float)acc;
+        for (int i = 0; i < 3; ++i) L.emission[i] = s.mats[m].emission[i];
+        lights.push_back(L);
+    }
+    for (uint32_t i = 0; i < s.spheres.size(); ++i) {
+        const pg_material &m = s.mats[s.spheres[i].material];
+        if (m.type != PG_MAT_LIGHT) continue;
+        DevLight L{};
+        L.type = 1;
+        L.sphere = i;
+        L.area = 4.0f * 3.14159265f * s.spheres[i].radius * s.spheres[i].radius;
+        for (int k = 0; k < 3; ++k) L.emission[k] = m.emission[k];
+        lights.push_back(L);
+    }
+    sc->n_lights = (uint32_t)lights.size();
+}
+
+// Device copy of the scene, made on first use (so scenes can be built and
+// inspected on a machine without a GPU).
+int ensure_uploaded(pg_scene *sc) {
+    if (sc->uploaded) return PG_OK;
+    const SceneData &s = sc->host;
+    std::vector<DevBvhNode> dn(s.nodes.size());
+    for (size_t i = 0; i < s.nodes.size(); ++i) {
+        const BvhNode &n = s.nodes[i];
+        dn[i].a = make_float4(n.lo0[0], n.lo0[1], n.lo0[2], n.hi0[0]);
+        dn[i].b = make_float4(n.hi0[1], n.hi0[2], n.lo1[0], n.lo1[1]);
+        dn[i].c = make_float4(n.lo1[2], n.hi1[0], n.hi1[1], n.hi1[2]);
+        dn[i].d = make_int4(n.child[0], n.child[1], n.count[0], n.count[1]);
+    }
+    std::vector<float4> tv(s.tri_verts.size() / 4);
+    memcpy(tv.data(), s.tri_verts.data(), sizeof(float) * s.tri_verts.size());
+    int st = upload(&sc->d_nodes, dn);
+    if (!st) st = upload(&sc->d_tris, tv);
+    if (!st) st = upload(&sc->d_spheres, s.spheres);
+    if (!st) st = upload(&sc->d_pos, s.pos);
+    if (!st) st = upload(&sc->d_idx, s.idx);
+    if (!st) st = upload(&sc->d_tri_mat, s.tri_mat);
+    if (!st) st = upload(&sc->d_mats, s.mats);
+    if (!st) st = upload(&sc->d_lights, sc->h_lights);
+    if (!st) st = upload(&sc->d_light_tris, sc->h_light_tris);
+    if (!st) st = upload(&sc->d_light_cdf, sc->h_light_cdf);
+    if (!st) st = upload(&sc->d_tri_light, sc->h_tri_light);
+    if (!st && cudaMalloc(&sc->d_counters, sizeof(uint32_t) * 16) != cudaSuccess) st = PG_ERR_CUDA;
+    if (!st && cudaMalloc(&sc->d_stats, sizeof(unsigned long long) * 4) != cudaSuccess) st = PG_ERR_CUDA;
+    if (st) return scene_error(st, "scene upload failed (CUDA)");
+    sc->uploaded = true;
+    return PG_OK;
+}
+
+DevScene dev_scene(const pg_scene *sc) {
+    DevScene S;
+    S.nodes = sc->d_nodes;
+    S.tris = sc->d_tris;
+    S.spheres = sc->d_spheres;
+    S.n_spheres = (uint32_t)sc->host.spheres.size();
+    S.n_triangles = (uint32_t)sc->host.tri_mat.size();
+    return S;
+}
+
+int create_common(pg_scene *sc, pg_scene **out) {
+    build_host(sc);
+    *out = sc;
+    return PG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pg_scene_create_cornell(const pg_cornell_params *p, pg_scene **out) {
+    if (!p || !out) return PG_ERR_ARG;
+    if (p->width == 0 || p->height == 0 || p->ico_level < 0 || p->ico_level > 8)
+        return scene_error(PG_ERR_ARG, "bad Cornell box parameters");
+    pg_scene *sc = new pg_scene();
+    make_cornell(sc->host, *p);
+    return create_common(sc, out);
+}
+
+int pg_scene_create_plates(const pg_plates_params *p, pg_scene **out) {
+    if (!p || !out) return PG_ERR_ARG;
+    if (p->width == 0 || p->height == 0 || p->occluder_grid > 4096)
+        return scene_error(PG_ERR_ARG, "bad plates-scene parameters");
+    pg_scene *sc = new pg_scene();
+    make_glossy_plates(sc->host, *p);
+    return create_common(sc, out);
+}
+
+int pg_scene_load(const char *path, uint32_t width, uint32_t height, pg_scene **out) {
+    if (!path || !out || width == 0 || height == 0) return PG_ERR_ARG;
+    pg_scene *sc = new pg_scene();
+    if (!load_mitsuba(sc->host, path, width, height)) {
+        const std::string msg = sc->host.error;
+        delete sc;
+        const bool io = msg.rfind("cannot open", 0) == 0;
+        return scene_error(io ? PG_ERR_IO : PG_ERR_PARSE, msg);
+    }
+    return create_common(sc, out);
+}
+
+int pg_scene_destroy(pg_scene *sc) {
+    if (!sc) return PG_OK;
+    cudaFree(sc->d_nodes);
+    cudaFree(sc->d_tris);
+    cudaFree(sc->d_spheres);
+    cudaFree(sc->d_pos);
+    cudaFree(sc->d_idx);
+    cudaFree(sc->d_tri_mat);
+    cudaFree(sc->d_mats);
+    cudaFree(sc->d_lights);
+    cudaFree(sc->d_light_tris);
+    cudaFree(sc->d_light_cdf);
+    cudaFree(sc->d_tri_light);
+    cudaFree(sc->d_stats);
+    cudaFree(sc->d_counters);
+    for (void *b : sc->bufs) cudaFree(b);
+    delete sc;
+    return PG_OK;
+}
+
+int pg_scene_get_info(const pg_scene *sc, pg_scene_info *out) {
+    if (!sc || !out) return PG_ERR_ARG;
+    out->n_triangles = (uint32_t)sc->host.tri_mat.size();
+    out->n_spheres = (uint32_t)sc->host.spheres.size();
+    out->n_materials = (uint32_t)sc->host.mats.size();
+    out->n_nodes = (uint32_t)sc->host.nodes.size();
+    out->n_lights = sc->n_lights;
+    for (int i = 0; i < 6; ++i) out->aabb[i] = sc->aabb[i];
+    out->camera = sc->host.camera;
+    return PG_OK;
+}
+
+int pg_scene_export(const pg_scene *sc, void *nodes, float *tri_verts, uint32_t *tri_order, uint32_t *tri_material,
+                    pg_material *materials, pg_sphere *spheres) {
+    if (!sc) return PG_ERR_ARG;
+    const SceneData &s = sc->host;
+    if (nodes) memcpy(nodes, s.nodes.data(), sizeof(BvhNode) * s.nodes.size());
+    if (tri_verts) memcpy(tri_verts, s.tri_verts.data(), sizeof(float) * s.tri_verts.size());
+    if (tri_order) memcpy(tri_order, s.tri_order.data(), sizeof(uint32_t) * s.tri_order.size());
+    if (tri_material) memcpy(tri_material, s.tri_mat.data(), sizeof(uint32_t) * s.tri_mat.size());
+    if (materials) memcpy(materials, s.mats.data(), sizeof(pg_material) * s.mats.size());
+    if (spheres) memcpy(spheres, s.spheres.data(), sizeof(pg_sphere) * s.spheres.size());
+    return PG_OK;
+}
+
+int pg_scene_set_camera(pg_scene *sc, const pg_camera *cam) {
+    if (!sc || !cam || cam->width == 0 || cam->height == 0) return PG_ERR_ARG;
+    sc->host.camera = *cam;
+    return PG_OK;
+}
+
+int pg_scene_export_mesh(const pg_scene *sc, float *positions, uint32_t *indices, uint32_t *n_vertices) {
+    if (!sc) return PG_ERR_ARG;
+    const SceneData &s = sc->host;
+    if (n_vertices) *n_vertices = (uint32_t)(s.pos.size() / 3);
+    if (positions) memcpy(positions, s.pos.data(), sizeof(float) * s.pos.size());
+    if (indices) memcpy(indices, s.idx.data(), sizeof(uint32_t) * s.idx.size());
+    return PG_OK;
+}
+
+int pg_trace_closest(pg_scene *sc, const pg_ray *rays, uint32_t n, pg_hit *hits, void *stream) {
+    if (!sc || (!rays && n) || (!hits && n)) return PG_ERR_ARG;
+    if (n == 0) return PG_OK;
+    if (int st = ensure_uploaded(sc)) return st;
+    k_trace_closest<<<(n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(dev_scene(sc), rays, n, hits);
+    return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ERR_CUDA;
+}
+
+int pg_trace_any(pg_scene *sc, const pg_ray *rays, uint32_t n, uint32_t *occluded, void *stream) {
+    if (!sc || (!rays && n) || (!occluded && n)) return PG_ERR_ARG;
+    if (n == 0) return PG_OK;
+    if (int st = ensure_uploaded(sc)) return st;
+    k_trace_any<<<(n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(dev_scene(sc), rays, n, occluded);
+    return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ERR_CUDA;
+}
+
+int pg_render(pg_scene *sc, const pg_render_params *rp, pg_ctx *guide, float *image, pg_directional_data *records,
+              pg_render_stats *stats, void *stream) {
+    if (!sc || !rp || !image) return PG_ERR_ARG;
+    if (rp->max_depth == 0 || rp->max_depth > 64) return scene_error(PG_ERR_ARG, "max_depth must be in [1, 64]");
+    if (rp->record_samples && !records) return scene_error(PG_ERR_ARG, "record_samples needs a records buffer");
+    if ((rp->use_guiding || rp->record_samples) && !guide)
+        return scene_error(PG_ERR_ARG, "guiding and sample recording need a guiding context (pg_set_regions)");
+    if (int st = ensure_uploaded(sc)) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    const pg_camera cam = sc->host.camera;
+    const uint32_t P = cam.width * cam.height;
+    // grow the path and queue buffers
+    if (P > sc->cap_pix) {
+        for (void *b : sc->bufs) cudaFree(b);
+        sc->bufs.clear();
+        auto alloc = [&](size_t bytes) -> void * {
+            void *p = nullptr;
+            if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+            sc->bufs.push_back(p);
+            return p;
+        };
+        DevRender &R = sc->R;
+        R.ro = (float *)alloc(12ull * P);
+        R.rd = (float *)alloc(12ull * P);
+        R.thr = (float *)alloc(12ull * P);
+        R.prev_pdf = (float *)alloc(4ull * P);
+        R.alive = (uint8_t *)alloc(P);
+        R.found = (uint8_t *)alloc(P);
+        R.hits = (pg_hit *)alloc(sizeof(pg_hit) * (size_t)P);
+        R.q_cur = (uint32_t *)alloc(4ull * P);
+        R.q_next = (uint32_t *)alloc(4ull * P);
+        R.sh_o = (float *)alloc(12ull * P);
+        R.sh_d = (float *)alloc(12ull * P);
+        R.sh_tmax = (float *)alloc(4ull * P);
+        R.sh_c = (float *)alloc(12ull * P);
+        R.sh_l = (float *)alloc(12ull * P);
+        R.sh_pix = (uint32_t *)alloc(4ull * P);
+        R.sh_nrec = (uint32_t *)alloc(4ull * P);
+        R.rec_lsum = (float *)alloc(12ull * P * kMaxRecords);
+        R.rec_tc = (float *)alloc(12ull * P * kMaxRecords);
+        R.rec_count = (uint32_t *)alloc(4ull * P);
+        R.rec_start = (uint32_t *)alloc(4ull * P);
+        R.rec_pending = (int32_t *)alloc(4ull * P);
+        R.rec_factor = (float *)alloc(4ull * P);
+        for (void *b : sc->bufs)
+            if (!b) return scene_error(PG_ERR_NOMEM, "render buffers: out of device memory");
+        if (sc->bufs.size() != 22) return scene_error(PG_ERR_NOMEM, "render buffers: out of device memory");
+        sc->cap_pix = P;
+    }
+    DevRender R = sc->R;
+    R.S = dev_scene(sc);
+    R.pos = sc->d_pos;
+    R.idx = sc->d_idx;
+    R.tri_mat = sc->d_tri_mat;
+    R.mats = sc->d_mats;
+    R.lights = sc->d_lights;
+    R.n_lights = sc->n_lights;
+    R.light_tris = sc->d_light_tris;
+    R.light_cdf = sc->d_light_cdf;
+    R.tri_light = sc->d_tri_light;
+    R.cam = cam;
+    {
+        float f[3] = {cam.target[0] - cam.origin[0], cam.target[1] - cam.origin[1], cam.target[2] - cam.origin[2]};
+        float l = sqrtf(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+        for (int i = 0; i < 3; ++i) f[i] /= l;
+        float r[3] = {f[1] * cam.up[2] - f[2] * cam.up[1], f[2] * cam.up[0] - f[0] * cam.up[2],
+                      f[0] * cam.up[1] - f[1] * cam.up[0]};
+        l = sqrtf(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+        for (int i = 0; i < 3; ++i) r[i] /= l;
+        const float u[3] = {r[1] * f[2] - r[2] * f[1], r[2] * f[0] - r[0] * f[2], r[0] * f[1] - r[1] * f[0]};
+        for (int i = 0; i < 3; ++i) {
+            R.cam_fwd[i] = f[i];
+            R.cam_right[i] = r[i];
+            R.cam_up[i] = u[i];
+        }
+        R.tan_half = tanf(cam.vfov_deg * 0.5f * 3.14159265f / 180.0f);
+    }
+    R.rp = *rp;
+    R.image = image;
+    R.counters = sc->d_counters;
+    R.guiding = rp->use_guiding ? 1 : 0;
+    R.recording = rp->record_samples ? 1 : 0;
+    R.rec = records;
+    memset(&R.guide, 0, sizeof R.guide);
+    if (guide) {
+        GuideView gv;
+        const int st = guide_view(guide, &gv, s);
+        if (st) return scene_error(st, pg_last_error(guide));
+        for (int i = 0; i < 6; ++i) R.guide.root[i] = gv.root[i];
+        R.guide.split_count = gv.split_count;
+        R.guide.vmm = gv.vmm;
+        R.guide.use_parallax = gv.use_parallax;
+    }
+    if (cudaMemsetAsync(sc->d_counters, 0, sizeof(uint32_t) * 16, s) != cudaSuccess)
+        return scene_error(PG_ERR_CUDA, "counter reset");
+    if (R.recording) {
+        const uint32_t slots = P * kMaxRecords;
+        k_reset_records<<<(slots + 255) / 256, 256, 0, s>>>(records, slots, R.rec_start, P);
+    }
+    R.stats = sc->d_stats;
+    if (cudaMemsetAsync(sc->d_stats, 0, sizeof(unsigned long long) * 4, s) != cudaSuccess)
+        return scene_error(PG_ERR_CUDA, "stats reset");
+    const uint32_t T = 128;
+    const uint32_t G = (P + T - 1) / T;
+    for (uint32_t smp = 0; smp < rp->spp; ++smp) {
+        R.sample = smp;
+        DevRender Rb = R;
+        k_camera<<<G, T, 0, s>>>(Rb);
+        for (uint32_t b = 0; b < rp->max_depth; ++b) {
+            k_extend<<<G, T, 0, s>>>(Rb);
+            const int last = (b + 1 == rp->max_depth) ? 1 : 0;
+            k_shade<<<G, T, 0, s>>>(Rb, (int)b, last);
+            k_shadow<<<G, T, 0, s>>>(Rb);
+            k_advance<<<1, 1, 0, s>>>(Rb);
+            std::swap(Rb.q_cur, Rb.q_next);
+        }
+        if (R.recording) k_commit<<<G, T, 0, s>>>(R, P);
+    }
+    if (cudaGetLastError() != cudaSuccess) return scene_error(PG_ERR_CUDA, "render launch failed");
+    if (stats) {
+        uint32_t c[16];
+        unsigned long long st2[4];
+        if (cudaMemcpyAsync(c, sc->d_counters, sizeof c, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaMemcpyAsync(st2, sc->d_stats, sizeof st2, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return scene_error(PG_ERR_CUDA, "render stats");
+        stats->extension_rays = st2[0];
+        stats->shadow_rays = st2[1];
+        stats->samples_recorded = c[4];
+        stats->paths = (uint64_t)P * rp->spp;
+    }
+    return PG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,273 @@
+// pg_traverse.cuh - BVH traversal and ray-primitive tests on the device.
+//
+// Closest hit and any hit over the two-wide BVH of host/pg_scene.cpp.  The
+// triangle test is the watertight algorithm of Woop, Benthin and Wald (JCGT
+// 2013).  Every product, sum and quotient of the triangle and box tests is an
+// explicit round-to-nearest operation (__fmul_rn, __fadd_rn, __fdiv_rn, ...),
+// so no FMA contraction happens and a CPU restatement with the same operation
+// order reproduces the hit (triangle id and t) bit for bit.  Ties in t go to
+// the lower triangle id.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pathguide.h"
+
+namespace pg {
+
+struct DevBvhNode {
+    float4 a;  // lo0.xyz, hi0.x
+    float4 b;  // hi0.yz, lo1.xy
+    float4 c;  // lo1.z, hi1.xyz
+    int4 d;    // child0, child1, count0, count1
+};
+
+struct DevScene {
+    const DevBvhNode *nodes;
+    const float4 *tris;           // 3 float4 per triangle in BVH order; tris[3i].w = original id (bits)
+    const pg_sphere *spheres;
+    uint32_t n_spheres;
+    uint32_t n_triangles;
+};
+
+struct RayPre {
+    float org[3], dir[3], inv[3];
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+};
+
+__device__ __forceinline__ RayPre ray_setup(const float o[3], const float d[3]) {
+    RayPre r;
+    for (int i = 0; i < 3; ++i) {
+        r.org[i] = o[i];
+        r.dir[i] = d[i];
+        r.inv[i] = __fdiv_rn(1.0f, d[i]);
+    }
+    const float ax = fabsf(d[0]), ay = fabsf(d[1]), az = fabsf(d[2]);
+    int kz = 0;
+    if (ay > ax) kz = 1;
+    if (az > fmaxf(ax, ay)) kz = 2;
+    int kx = kz + 1 == 3 ? 0 : kz + 1;
+    int ky = kx + 1 == 3 ? 0 : kx + 1;
+    if (d[kz] < 0.0f) {
+        const int t = kx;
+        kx = ky;
+        ky = t;
+    }
+    r.kx = kx;
+    r.ky = ky;
+    r.kz = kz;
+    r.Sx = __fdiv_rn(d[kx], d[kz]);
+    r.Sy = __fdiv_rn(d[ky], d[kz]);
+    r.Sz = __fdiv_rn(1.0f, d[kz]);
+    return r;
+}
+
+__device__ __forceinline__ float comp(const float4 &v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+// Watertight ray-triangle test; on a hit in (tmin, tmax) returns t and the
+// barycentrics of v1 (u) and v2 (v).
+__device__ __forceinline__ bool tri_intersect(const RayPre &r, const float4 &v0, const float4 &v1, const float4 &v2,
+                                              float tmin, float tmax, float &t_out, float &u_out, float &v_out) {
+    const float A[3] = {__fsub_rn(v0.x, r.org[0]), __fsub_rn(v0.y, r.org[1]), __fsub_rn(v0.z, r.org[2])};
+    const float B[3] = {__fsub_rn(v1.x, r.org[0]), __fsub_rn(v1.y, r.org[1]), __fsub_rn(v1.z, r.org[2])};
+    const float C[3] = {__fsub_rn(v2.x, r.org[0]), __fsub_rn(v2.y, r.org[1]), __fsub_rn(v2.z, r.org[2])};
+    const float Akz = A[r.kz], Bkz = B[r.kz], Ckz = C[r.kz];
+    const float Ax = __fsub_rn(A[r.kx], __fmul_rn(r.Sx, Akz));
+    const float Ay = __fsub_rn(A[r.ky], __fmul_rn(r.Sy, Akz));
+    const float Bx = __fsub_rn(B[r.kx], __fmul_rn(r.Sx, Bkz));
+    const float By = __fsub_rn(B[r.ky], __fmul_rn(r.Sy, Bkz));
+    const float Cx = __fsub_rn(C[r.kx], __fmul_rn(r.Sx, Ckz));
+    const float Cy = __fsub_rn(C[r.ky], __fmul_rn(r.Sy, Ckz));
+    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        // edge functions exactly zero: redo them in double (exact products)
+        U = (float)__dsub_rn(__dmul_rn((double)Cx, (double)By), __dmul_rn((double)Cy, (double)Bx));
+        V = (float)__dsub_rn(__dmul_rn((double)Ax, (double)Cy), __dmul_rn((double)Ay, (double)Cx));
+        W = (float)__dsub_rn(__dmul_rn((double)Bx, (double)Ay), __dmul_rn((double)By, (double)Ax));
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = __fadd_rn(__fadd_rn(U, V), W);
+    if (det == 0.0f) return false;
+    const float Az = __fmul_rn(r.Sz, Akz);
+    const float Bz = __fmul_rn(r.Sz, Bkz);
+    const float Cz = __fmul_rn(r.Sz, Ckz);
+    const float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
+    const float t = __fdiv_rn(T, det);
+    if (!(t > tmin && t < tmax)) return false;
+    t_out = t;
+    u_out = __fdiv_rn(V, det);
+    v_out = __fdiv_rn(W, det);
+    return true;
+}
+
+// Slab test with the exit distance widened by 4e-7 > 2 gamma_3 (Ize 2013) so the
+// box test never rejects a triangle the triangle test would accept.
+__device__ __forceinline__ float box_enter(const RayPre &r, float lx, float ly, float lz, float hx, float hy, float hz,
+                                           float tmin, float tmax) {
+    const float tx0 = __fmul_rn(__fsub_rn(lx, r.org[0]), r.inv[0]);
+    const float tx1 = __fmul_rn(__fsub_rn(hx, r.org[0]), r.inv[0]);
+    const float ty0 = __fmul_rn(__fsub_rn(ly, r.org[1]), r.inv[1]);
+    const float ty1 = __fmul_rn(__fsub_rn(hy, r.org[1]), r.inv[1]);
+    const float tz0 = __fmul_rn(__fsub_rn(lz, r.org[2]), r.inv[2]);
+    const float tz1 = __fmul_rn(__fsub_rn(hz, r.org[2]), r.inv[2]);
+    const float te = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
+    float tx = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
+    tx = __fmul_rn(tx, 1.0000004f);
+    return te <= tx ? te : INFINITY;
+}
+
+// Analytic sphere (raytrace.sphere.rint:11-29 solves the same quadratic).
+__device__ __forceinline__ bool sphere_intersect(const RayPre &r, const pg_sphere &s, float tmin, float tmax,
+                                                 float &t_out) {
+    const float oc[3] = {__fsub_rn(r.org[0], s.center[0]), __fsub_rn(r.org[1], s.center[1]),
+                         __fsub_rn(r.org[2], s.center[2])};
+    const float a = __fadd_rn(__fadd_rn(__fmul_rn(r.dir[0], r.dir[0]), __fmul_rn(r.dir[1], r.dir[1])),
+                              __fmul_rn(r.dir[2], r.dir[2]));
+    const float b = __fadd_rn(__fadd_rn(__fmul_rn(r.dir[0], oc[0]), __fmul_rn(r.dir[1], oc[1])),
+                              __fmul_rn(r.dir[2], oc[2]));
+    const float c = __fsub_rn(__fadd_rn(__fadd_rn(__fmul_rn(oc[0], oc[0]), __fmul_rn(oc[1], oc[1])),
+                                        __fmul_rn(oc[2], oc[2])),
+                              __fmul_rn(s.radius, s.radius));
+    const float disc = __fsub_rn(__fmul_rn(b, b), __fmul_rn(a, c));
+    if (disc < 0.0f) return false;
+    const float sq = __fsqrt_rn(disc);
+    const float t1 = __fdiv_rn(__fsub_rn(-b, sq), a);
+    if (t1 > tmin && t1 < tmax) {
+        t_out = t1;
+        return true;
+    }
+    const float t2 = __fdiv_rn(__fadd_rn(-b, sq), a);
+    if (t2 > tmin && t2 < tmax) {
+        t_out = t2;
+        return true;
+    }
+    return false;
+}
+
+constexpr int kStackSize = 64;
+
+// Closest hit.  Returns false if nothing is hit in (tmin, tmax).
+__device__ __forceinline__ bool trace_closest(const DevScene &S, const float o[3], const float d[3], float tmin,
+                                              float tmax, pg_hit &hit) {
+    const RayPre r = ray_setup(o, d);
+    float best_t = tmax;
+    uint32_t best_id = PG_NO_HIT;
+    float best_u = 0.0f, best_v = 0.0f;
+    for (uint32_t i = 0; i < S.n_spheres; ++i) {
+        float t;
+        if (sphere_intersect(r, S.spheres[i], tmin, best_t, t)) {
+            best_t = t;
+            best_id = PG_SPHERE_BIT | i;
+        }
+    }
+    int stack[kStackSize];
+    int sp = 0;
+    int node = 0;
+    for (;;) {
+        const DevBvhNode n = S.nodes[node];
+        const float e0 = box_enter(r, n.a.x, n.a.y, n.a.z, n.a.w, n.b.x, n.b.y, tmin, best_t);
+        const float e1 = box_enter(r, n.b.z, n.b.w, n.c.x, n.c.y, n.c.z, n.c.w, tmin, best_t);
+        int nn = 0;
+        // leaves are tested immediately; inner children are visited near first
+        int cand[2] = {-1, -1};
+        float ce[2] = {INFINITY, INFINITY};
+        for (int c = 0; c < 2; ++c) {
+            const float e = c == 0 ? e0 : e1;
+            if (e == INFINITY) continue;
+            const int child = c == 0 ? n.d.x : n.d.y;
+            const int count = c == 0 ? n.d.z : n.d.w;
+            if (count > 0) {
+                for (int k = 0; k < count; ++k) {
+                    const uint32_t ti = (uint32_t)(child + k);
+                    const float4 v0 = S.tris[3 * ti], v1 = S.tris[3 * ti + 1], v2 = S.tris[3 * ti + 2];
+                    float t, u, v;
+                    const uint32_t id = __float_as_uint(v0.w);
+                    // one ulp above the best t, so an equal t is seen and the lower id wins
+                    const float lim = best_id == PG_NO_HIT ? best_t : __uint_as_float(__float_as_uint(best_t) + 1u);
+                    if (tri_intersect(r, v0, v1, v2, tmin, lim, t, u, v) &&
+                        (t < best_t || (t == best_t && id < best_id))) {
+                        best_t = t;
+                        best_id = id;
+                        best_u = u;
+                        best_v = v;
+                    }
+                }
+            } else if (child >= 0) {
+                cand[nn] = child;
+                ce[nn] = e;
+                ++nn;
+            }
+        }
+        if (nn == 2) {
+            const int near_i = ce[1] < ce[0] ? 1 : 0;
+            if (sp < kStackSize) stack[sp++] = cand[1 - near_i];
+            node = cand[near_i];
+            continue;
+        }
+        if (nn == 1) {
+            node = cand[0];
+            continue;
+        }
+        if (sp == 0) break;
+        node = stack[--sp];
+    }
+    hit.t = best_t;
+    hit.u = best_u;
+    hit.v = best_v;
+    hit.prim = best_id;
+    return best_id != PG_NO_HIT;
+}
+
+// Any hit in (tmin, tmax).
+__device__ __forceinline__ bool trace_any(const DevScene &S, const float o[3], const float d[3], float tmin,
+                                          float tmax) {
+    const RayPre r = ray_setup(o, d);
+    for (uint32_t i = 0; i < S.n_spheres; ++i) {
+        float t;
+        if (sphere_intersect(r, S.spheres[i], tmin, tmax, t)) return true;
+    }
+    int stack[kStackSize];
+    int sp = 0;
+    int node = 0;
+    for (;;) {
+        const DevBvhNode n = S.nodes[node];
+        const float e0 = box_enter(r, n.a.x, n.a.y, n.a.z, n.a.w, n.b.x, n.b.y, tmin, tmax);
+        const float e1 = box_enter(r, n.b.z, n.b.w, n.c.x, n.c.y, n.c.z, n.c.w, tmin, tmax);
+        int cand[2];
+        int nn = 0;
+        for (int c = 0; c < 2; ++c) {
+            const float e = c == 0 ? e0 : e1;
+            if (e == INFINITY) continue;
+            const int child = c == 0 ? n.d.x : n.d.y;
+            const int count = c == 0 ? n.d.z : n.d.w;
+            if (count > 0) {
+                for (int k = 0; k < count; ++k) {
+                    const uint32_t ti = (uint32_t)(child + k);
+                    float t, u, v;
+                    if (tri_intersect(r, S.tris[3 * ti], S.tris[3 * ti + 1], S.tris[3 * ti + 2], tmin, tmax, t, u, v))
+                        return true;
+                }
+            } else if (child >= 0) {
+                cand[nn++] = child;
+            }
+        }
+        if (nn == 2) {
+            if (sp < kStackSize) stack[sp++] = cand[1];
+            node = cand[0];
+            continue;
+        }
+        if (nn == 1) {
+            node = cand[0];
+            continue;
+        }
+        if (sp == 0) break;
+        node = stack[--sp];
+    }
+    return false;
+}
+
+}  // namespace pg

@@ -1,0 +1,66 @@
+// pg_scene.h - host-side scene: triangle meshes, analytic spheres, materials,
+// lights, camera, and the binned-SAH BVH the traversal kernels walk.
+//
+// The reference keeps the same information in SceneLoader (src/SceneLoader.h:
+// 118-162: vertices, indices, materials, spheres, lights, camera) and builds
+// Vulkan BLAS/TLAS from it (src/SceneLoader.cpp:1101-1194); here the
+// acceleration structure is our own BVH in device memory.
+#pragma once
+
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "pathguide.h"
+
+namespace pg {
+
+// Node of the two-wide BVH: both children's boxes live in the parent, so one
+// 64-byte fetch tests two boxes.  child[i] >= 0: inner node index; count[i] > 0:
+// leaf with triangles [child[i], child[i] + count[i]) of the reordered list.
+struct BvhNode {
+    float lo0[3], hi0[3];
+    float lo1[3], hi1[3];
+    int32_t child[2];
+    int32_t count[2];
+};
+static_assert(sizeof(BvhNode) == 64, "BvhNode is 64 bytes");
+
+struct SceneData {
+    std::vector<float> pos;        // 3 per vertex
+    std::vector<float> nrm;        // 3 per vertex (shading normals; empty = geometric)
+    std::vector<uint32_t> idx;     // 3 per triangle
+    std::vector<uint32_t> tri_mat; // material per triangle
+    std::vector<pg_material> mats;
+    std::vector<pg_sphere> spheres;
+    pg_camera camera{};
+    // built
+    std::vector<BvhNode> nodes;
+    std::vector<float> tri_verts;  // 12 floats per triangle in BVH order: v0.xyz id, v1.xyz 0, v2.xyz 0
+    std::vector<uint32_t> tri_order;  // BVH order -> original triangle id
+    std::string error;
+};
+
+// Binned SAH build (32 bins on centroid extents, leaves of at most max_leaf
+// triangles).  Deterministic: same input, same tree.
+void build_bvh(SceneData &s, int max_leaf = 4);
+
+// Procedural scenes of the benchmark workloads.
+void make_cornell(SceneData &s, const pg_cornell_params &p);
+void make_glossy_plates(SceneData &s, const pg_plates_params &p);
+
+// Mitsuba-XML subset (SceneLoader::parseMitsubaSceneFile,
+// src/SceneLoader.cpp:329-648): sensor (lookAt, fov), bsdf
+// diffuse / dielectric / conductor / roughconductor / plastic-as-diffuse,
+// shape obj / sphere / rectangle / cube with toWorld transforms, area emitters.
+// Returns false and sets s.error on malformed input.
+bool load_mitsuba(SceneData &s, const std::string &path, uint32_t width, uint32_t height);
+bool load_obj(SceneData &s, const std::string &path, const float *to_world, uint32_t material);
+
+// Icosphere: 20 * 4^level triangles, projected on the sphere.
+void add_icosphere(SceneData &s, const float center[3], float radius, int level, uint32_t material);
+void add_quad(SceneData &s, const float p0[3], const float p1[3], const float p2[3], const float p3[3],
+              uint32_t material);
+
+}  // namespace pg

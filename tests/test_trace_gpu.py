@@ -1,0 +1,236 @@
+"""GPU parity of the tracer through the C ABI, against the CPU twins in
+oracle/pg_oracle_trace.cpp.
+
+- Ray queries (the BVH walk and the watertight triangle test that stand in for
+  the reference's traceRayEXT, shaders/raytrace.rgen:1623-1827) are FP32 on
+  both sides with the same operation order: closest hits (t, u, v, primitive)
+  and any-hit flags must be bit-exact.
+- The renderer (NEE + MIS path tracing with optional vMF-mixture guiding,
+  raytrace.rgen:601-731, 923-960) is FP32 on the GPU and FP64 in the oracle,
+  with the same hashed random numbers: a path takes the same decisions on
+  both sides unless a rounding difference flips one, so most pixels agree to
+  1e-3 relative and the whole image to 1e-3 relative; converged images of
+  different strategies agree within their noise.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+# same-seed image parity (FP32 GPU vs FP64 oracle)
+PIX_RTOL = 1e-3          # a pixel agrees when |gpu - f64| <= PIX_RTOL * (|f64| + 1e-2 * mean)
+PIX_AGREE_MIN = 0.97     # fraction of pixels that must agree
+IMAGE_MEAN_RTOL = 2e-3   # whole-image mean radiance
+
+
+@pytest.fixture(scope="module")
+def tracer(oracle):
+    from oracle.oracle import TraceOracle
+    return TraceOracle()
+
+
+def dev(torch, arr):
+    a = np.ascontiguousarray(arr)
+    return torch.from_numpy(a.view(np.uint8).reshape(-1).copy()).cuda()
+
+
+def host(t, dtype):
+    return np.frombuffer(t.cpu().numpy().tobytes(), dtype=dtype).copy()
+
+
+def make_rays(abi, rng, exp, n):
+    """Rays from random points in the scene box, from the camera, and a few
+    with empty [tmin, tmax] intervals."""
+    aabb = np.array(exp["info"].aabb, dtype=np.float64)
+    lo, hi = aabb[:3], aabb[3:]
+    rays = np.zeros(n, dtype=abi.RAY_DTYPE)
+    half = n // 2
+    rays["org"][:half] = lo + (hi - lo) * rng.random((half, 3))
+    rays["org"][half:] = np.array(exp["info"].camera.origin)
+    tgt = lo + (hi - lo) * rng.random((n, 3))
+    d = rng.normal(size=(n, 3))
+    d[half:] = tgt[half:] - rays["org"][half:]
+    rays["dir"] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rays["tmin"] = 1e-3
+    rays["tmax"] = 1e30
+    rays["tmax"][:16] = rng.uniform(0.05, 1.0, 16)
+    rays["tmax"][16:24] = 0.0  # empty interval
+    return rays
+
+
+SCENES = {
+    "cornell": lambda pkg: pkg.Scene.cornell(64, 48, ico_level=5),
+    "plates": lambda pkg: pkg.Scene.plates(64, 36, occluder_grid=64, seed=4),
+}
+
+
+@pytest.mark.parametrize("name", sorted(SCENES))
+def test_closest_hit_bit_exact(name, cuda, pkg, abi, tracer):
+    torch = cuda
+    sc = SCENES[name](pkg)
+    exp = sc.export()
+    rays = make_rays(abi, np.random.default_rng(7), exp, 200000)
+    d_rays = dev(torch, rays)
+    d_hits = torch.zeros(rays.shape[0] * abi.HIT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    sc.trace_closest(d_rays, rays.shape[0], d_hits)
+    torch.cuda.synchronize()
+    got = host(d_hits, abi.HIT_DTYPE)
+    want = tracer.closest(exp, rays)
+    assert (want["prim"] != 0xFFFFFFFF).mean() > 0.3
+    same = got.view(np.uint32).reshape(-1, 4) == want.view(np.uint32).reshape(-1, 4)
+    bad = np.where(~same.all(axis=1))[0]
+    assert bad.size == 0, f"{bad.size} hits differ; first {bad[:5]}: gpu {got[bad[:3]]} cpu {want[bad[:3]]}"
+
+
+@pytest.mark.parametrize("name", sorted(SCENES))
+def test_any_hit_matches(name, cuda, pkg, abi, tracer):
+    torch = cuda
+    sc = SCENES[name](pkg)
+    exp = sc.export()
+    rng = np.random.default_rng(8)
+    rays = make_rays(abi, rng, exp, 100000)
+    rays["tmax"][24:] = rng.uniform(0.01, 4.0, rays.shape[0] - 24)
+    d_rays = dev(torch, rays)
+    d_occ = torch.zeros(rays.shape[0], dtype=torch.int32, device="cuda")
+    sc.trace_any(d_rays, rays.shape[0], d_occ)
+    torch.cuda.synchronize()
+    got = d_occ.cpu().numpy().view(np.uint32)
+    want = tracer.any(exp, rays)
+    assert 0.05 < want.mean() < 0.95
+    assert np.array_equal(got, want)
+    closest = tracer.closest(exp, rays)
+    assert np.array_equal(got.astype(bool), closest["prim"] != 0xFFFFFFFF)
+
+
+def test_trace_empty_batch(cuda, pkg, abi):
+    sc = pkg.Scene.cornell(8, 8, ico_level=1)
+    sc.trace_closest(0, 0, 0)
+    sc.trace_any(0, 0, 0)
+    cuda.cuda.synchronize()
+
+
+def render_gpu(torch, sc, params, guide=None, records=None):
+    i = sc.info()
+    H, W = i.camera.height, i.camera.width
+    img = torch.zeros(H * W * 3, dtype=torch.float32, device="cuda")
+    st = sc.render(params, img, guide=guide, records_dev=records)
+    torch.cuda.synchronize()
+    return img.cpu().numpy().reshape(H, W, 3).astype(np.float64), st
+
+
+def assert_same_seed_parity(got, want, what):
+    mean = want.mean()
+    err = np.abs(got - want) / (np.abs(want) + 1e-2 * mean)
+    agree = (err <= PIX_RTOL).all(axis=2).mean()
+    rel_mean = abs(got.mean() - mean) / mean
+    assert agree >= PIX_AGREE_MIN, f"{what}: {agree:.4f} of pixels agree (mean rel {rel_mean:.2e})"
+    assert rel_mean <= IMAGE_MEAN_RTOL, f"{what}: image mean {got.mean()} vs {mean}"
+
+
+@pytest.mark.parametrize("nee,mis,depth", [(1, 1, 8), (0, 0, 8), (1, 0, 8), (1, 1, 1), (1, 1, 3)])
+def test_render_same_seed_cornell(nee, mis, depth, cuda, pkg, abi, tracer):
+    sc = pkg.Scene.cornell(48, 32, ico_level=4)
+    params = abi.render_params(spp=4, max_depth=depth, seed=11, use_nee=nee, use_mis=mis)
+    got, st = render_gpu(cuda, sc, params)
+    want = tracer.render(sc.export(), params)
+    assert want.mean() > 0
+    assert st.paths == 48 * 32 * 4 and st.extension_rays >= st.paths
+    assert_same_seed_parity(got, want, f"cornell nee={nee} mis={mis} depth={depth}")
+
+
+def test_render_same_seed_plates(cuda, pkg, abi, tracer):
+    sc = pkg.Scene.plates(64, 36, occluder_grid=32, seed=4)
+    params = abi.render_params(spp=4, max_depth=6, seed=3)
+    got, _ = render_gpu(cuda, sc, params)
+    want = tracer.render(sc.export(), params)
+    assert_same_seed_parity(got, want, "plates")
+
+
+def test_render_deterministic_and_accumulates(cuda, pkg, abi):
+    torch = cuda
+    sc = pkg.Scene.cornell(40, 30, ico_level=3)
+    p = abi.render_params(spp=2, max_depth=5, seed=5)
+    a, _ = render_gpu(torch, sc, p)
+    b, _ = render_gpu(torch, sc, p)
+    assert np.array_equal(a, b)
+    img = torch.zeros(40 * 30 * 3, dtype=torch.float32, device="cuda")
+    sc.render(p, img)
+    sc.render(p, img)
+    torch.cuda.synchronize()
+    assert np.allclose(img.cpu().numpy().reshape(30, 40, 3), 2 * a, rtol=1e-6, atol=0)
+
+
+def test_strategies_converge_to_f64_reference(cuda, pkg, abi, tracer):
+    """BSDF-only, NEE-only and MIS estimators are unbiased: their converged
+    images agree with each other and with an FP64 render at another seed."""
+    sc = pkg.Scene.cornell(32, 24, ico_level=4)
+    spp = 2048
+    imgs = {}
+    for name, nee, mis in (("bsdf", 0, 0), ("nee", 1, 0), ("mis", 1, 1)):
+        imgs[name], _ = render_gpu(cuda, sc, abi.render_params(spp=spp, max_depth=8, seed=21, use_nee=nee,
+                                                               use_mis=mis))
+        imgs[name] /= spp
+    ref = tracer.render(sc.export(), abi.render_params(spp=512, max_depth=8, seed=99)) / 512
+    m = ref.mean()
+    for name, img in imgs.items():
+        assert abs(img.mean() - m) / m < 0.02, f"{name}: mean {img.mean()} vs f64 {m}"
+        # 8x8 blocks average out the noise
+        blk = lambda x: x.reshape(3, 8, 4, 8, 3).mean(axis=(1, 3))
+        rel = np.abs(blk(img) - blk(ref)) / (blk(ref) + 0.05 * m)
+        assert rel.max() < 0.08, f"{name}: block rel err {rel.max():.3f}"
+    # MIS has the lowest variance of the three against the converged mean
+    assert ((imgs["mis"] - ref) ** 2).mean() <= ((imgs["bsdf"] - ref) ** 2).mean()
+
+
+def guided_setup(torch, pkg, abi, sc, split_count=6, spp=4, seed=1):
+    """Render with recording, then one PathGuiding::update pass."""
+    i = sc.info()
+    P = i.camera.width * i.camera.height
+    ctx = pkg.FitContext(abi.default_fit_config(), max_regions=1 << split_count)
+    ctx.set_regions(split_count, np.array(i.aabb, dtype=np.float32))
+    rec = torch.zeros(P * 16 * 40, dtype=torch.uint8, device="cuda")
+    _, st = render_gpu(torch, sc, abi.render_params(spp=spp, max_depth=8, seed=seed, record_samples=1), guide=ctx,
+                       records=rec)
+    R = ctx.region_count()
+    vmm = torch.zeros(R * 720, dtype=torch.uint8, device="cuda")
+    ctx.update(rec, P * 16, vmm)
+    torch.cuda.synchronize()
+    return ctx, rec, st, vmm
+
+
+def test_recorded_samples_are_well_formed(cuda, pkg, abi, workloads):
+    torch = cuda
+    sc = pkg.Scene.cornell(48, 32, ico_level=3)
+    ctx, rec, st, _ = guided_setup(torch, pkg, abi, sc)
+    r = host(rec, workloads.RECORD_DTYPE)
+    valid = r["flags"] != 0xFFFFFFFF
+    assert valid.sum() == st.samples_recorded > 1000
+    v = r[valid]
+    boxes = ctx.region_aabbs()
+    assert (v["flags"] < boxes.shape[0]).all()
+    assert np.isfinite(v["weight"]).all() and (v["weight"] > 0).all()
+    assert (v["pdf"] > 0).all() and (v["distance"] >= 0).all() and np.isfinite(v["distance"]).all()
+    assert np.allclose(np.linalg.norm(v["direction"], axis=1), 1.0, atol=1e-5)
+    b = boxes[v["flags"]]
+    assert ((v["position"] >= b[:, :3]) & (v["position"] <= b[:, 3:])).all(), "record lies in its region"
+
+
+def test_guided_render_same_seed_and_unbiased(cuda, pkg, abi, tracer):
+    torch = cuda
+    sc = pkg.Scene.cornell(48, 32, ico_level=4)
+    ctx, _, _, vmm = guided_setup(torch, pkg, abi, sc, spp=8)
+    boxes = ctx.region_aabbs()
+    guide = {"vmm": vmm.cpu().numpy(), "root": np.concatenate([boxes[:, :3].min(0), boxes[:, 3:].max(0)]),
+             "split_count": 6, "use_parallax": int(abi.default_fit_config().use_parallax)}
+    params = abi.render_params(spp=4, max_depth=8, seed=17, use_guiding=1, guiding_prob=0.5)
+    got, _ = render_gpu(torch, sc, params, guide=ctx)
+    want = tracer.render(sc.export(), params, guide=guide)
+    assert_same_seed_parity(got, want, "guided cornell")
+    # guiding changes the sampling, not the expectation
+    spp = 1024
+    g, _ = render_gpu(torch, sc, abi.render_params(spp=spp, max_depth=8, seed=5, use_guiding=1, guiding_prob=0.5),
+                      guide=ctx)
+    u, _ = render_gpu(torch, sc, abi.render_params(spp=spp, max_depth=8, seed=6))
+    assert abs(g.mean() - u.mean()) / u.mean() < 0.02
