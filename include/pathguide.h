@@ -355,14 +355,33 @@ typedef struct pg_render_params {
     uint32_t use_guiding;      /* sample directions from the context's mixtures */
     float guiding_prob;        /* one-sample mixture weight of the guide (0.5) */
     uint32_t record_samples;   /* write DirectionalData records for the next fit */
-    uint32_t reserved[4];
+    uint32_t flags;            /* PG_RENDER_* instrumentation bits (0 for plain rendering) */
+    uint32_t reserved[3];
 } pg_render_params;
+
+/* Count BVH node visits and triangle tests of every ray into the stats (a
+ * separately compiled traversal; the image is unchanged). */
+#define PG_RENDER_COUNT_WORK 1u
+/* Time each stage with CUDA events on the render stream (the call then
+ * synchronises the stream before returning). */
+#define PG_RENDER_TIME_STAGES 2u
+
+enum pg_render_stage {
+    PG_STAGE_CAMERA = 0, PG_STAGE_EXTEND, PG_STAGE_SHADE, PG_STAGE_SHADOW, PG_STAGE_ADVANCE, PG_STAGE_COMMIT,
+    PG_STAGE_COUNT
+};
 
 typedef struct pg_render_stats {
     uint64_t extension_rays;
     uint64_t shadow_rays;
     uint64_t samples_recorded;
     uint64_t paths;
+    /* with PG_RENDER_COUNT_WORK: traversal work of extension and shadow rays */
+    uint64_t extension_node_visits, extension_triangle_tests;
+    uint64_t shadow_node_visits, shadow_triangle_tests;
+    /* with PG_RENDER_TIME_STAGES: summed duration and launch count per stage */
+    float stage_ms[PG_STAGE_COUNT];
+    uint32_t stage_launches[PG_STAGE_COUNT];
 } pg_render_stats;
 
 typedef struct pg_scene pg_scene;
@@ -394,6 +413,11 @@ int pg_scene_set_camera(pg_scene *scene, const pg_camera *cam);
  * Wald 2013); ties in t go to the lower triangle id. */
 int pg_trace_closest(pg_scene *scene, const pg_ray *rays, uint32_t n, pg_hit *hits, void *stream);
 int pg_trace_any(pg_scene *scene, const pg_ray *rays, uint32_t n, uint32_t *occluded, void *stream);
+/* pg_trace_closest that also writes, per ray, the BVH nodes visited and the
+ * triangles tested (device arrays of n).  The traversal order is that of
+ * pg_trace_closest, so the counts are the algorithm's work for those rays. */
+int pg_trace_closest_counted(pg_scene *scene, const pg_ray *rays, uint32_t n, pg_hit *hits, uint32_t *node_visits,
+                             uint32_t *triangle_tests, void *stream);
 
 /* Renders params->spp samples per pixel with the wavefront integrator and
  * adds the radiance sums into image (device, width * height * 3 floats).

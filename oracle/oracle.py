@@ -209,6 +209,7 @@ class TraceOracle:
         L = self.lib
         L.pgo_trace_closest.argtypes = [C.POINTER(PgoScene), _P, _U32, _P, _I]
         L.pgo_trace_any.argtypes = [C.POINTER(PgoScene), _P, _U32, _P, _I]
+        L.pgo_trace_closest_counted.argtypes = [C.POINTER(PgoScene), _P, _U32, _P, _P, _P, _I]
         L.pgo_render_f64.argtypes = [C.POINTER(PgoScene), C.POINTER(abi.RenderParams), C.POINTER(PgoGuide), _P, _U32,
                                      _U32, _I]
         L.pgo_rnd.argtypes = [_U32, _U32, _U32, _U32]
@@ -231,6 +232,18 @@ class TraceOracle:
         self.lib.pgo_trace_closest(C.byref(s), rays.ctypes.data, rays.shape[0], hits.ctypes.data,
                                    threads or (os.cpu_count() or 1))
         return hits
+
+    def closest_counted(self, exp, rays, threads=None):
+        """Closest hits plus per-ray BVH node fetches and triangle tests."""
+        s, keep = self.scene(exp)
+        rays = np.ascontiguousarray(rays)
+        n = rays.shape[0]
+        hits = np.zeros(n, dtype=abi.HIT_DTYPE)
+        nodes = np.zeros(n, dtype=np.uint32)
+        tris = np.zeros(n, dtype=np.uint32)
+        self.lib.pgo_trace_closest_counted(C.byref(s), rays.ctypes.data, n, hits.ctypes.data, nodes.ctypes.data,
+                                           tris.ctypes.data, threads or (os.cpu_count() or 1))
+        return hits, nodes, tris
 
     def any(self, exp, rays, threads=None):
         s, keep = self.scene(exp)

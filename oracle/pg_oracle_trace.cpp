@@ -127,7 +127,9 @@ float bitsf(uint32_t u) {
     return f;
 }
 
-void closest32(const pgo_scene &S, const pg_ray &ray, pg_hit &hit) {
+// cnt (optional): [0] BVH nodes fetched, [1] triangles tested
+void closest32(const pgo_scene &S, const pg_ray &ray, pg_hit &hit, uint32_t *cnt = nullptr) {
+    uint32_t n_nodes = 0, n_tris = 0;
     const RayPre r = ray_setup(ray.org, ray.dir);
     float best_t = ray.tmax, best_u = 0, best_v = 0;
     uint32_t best_id = PG_NO_HIT;
@@ -144,6 +146,7 @@ void closest32(const pgo_scene &S, const pg_ray &ray, pg_hit &hit) {
     int node = 0;
     for (;;) {
         const Node &n = nodes[node];
+        ++n_nodes;
         const float e[2] = {box_enter(r, n.lo0, n.hi0, ray.tmin, best_t), box_enter(r, n.lo1, n.hi1, ray.tmin, best_t)};
         int cand[2], nn = 0;
         float ce[2];
@@ -153,6 +156,7 @@ void closest32(const pgo_scene &S, const pg_ray &ray, pg_hit &hit) {
                 for (int k = 0; k < n.count[c]; ++k) {
                     const float *tv = S.tri_verts + 12 * (size_t)(n.child[c] + k);
                     const uint32_t id = fbits(tv[3]);
+                    ++n_tris;
                     const float lim = best_id == PG_NO_HIT ? best_t : bitsf(fbits(best_t) + 1u);
                     float t, u, v;
                     if (tri_intersect(r, tv, tv + 4, tv + 8, ray.tmin, lim, t, u, v) &&
@@ -187,6 +191,10 @@ void closest32(const pgo_scene &S, const pg_ray &ray, pg_hit &hit) {
     hit.u = best_u;
     hit.v = best_v;
     hit.prim = best_id;
+    if (cnt) {
+        cnt[0] = n_nodes;
+        cnt[1] = n_tris;
+    }
 }
 
 bool any32(const pgo_scene &S, const pg_ray &ray) {
@@ -691,6 +699,16 @@ float pgo_rnd(uint32_t seed, uint32_t pixel, uint32_t sample, uint32_t dim) { re
 
 void pgo_trace_closest(const pgo_scene *s, const pg_ray *rays, uint32_t n, pg_hit *hits, int n_threads) {
     parallel_for(n, n_threads, [&](uint32_t i) { closest32(*s, rays[i], hits[i]); });
+}
+
+void pgo_trace_closest_counted(const pgo_scene *s, const pg_ray *rays, uint32_t n, pg_hit *hits, uint32_t *nodes,
+                               uint32_t *tris, int n_threads) {
+    parallel_for(n, n_threads, [&](uint32_t i) {
+        uint32_t c[2];
+        closest32(*s, rays[i], hits[i], c);
+        nodes[i] = c[0];
+        tris[i] = c[1];
+    });
 }
 
 void pgo_trace_any(const pgo_scene *s, const pg_ray *rays, uint32_t n, uint32_t *occ, int n_threads) {

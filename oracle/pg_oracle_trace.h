@@ -44,6 +44,9 @@ typedef struct pgo_guide {
 } pgo_guide;
 
 void pgo_trace_closest(const pgo_scene *s, const pg_ray *rays, uint32_t n, pg_hit *hits, int n_threads);
+/* pgo_trace_closest that also reports, per ray, BVH nodes fetched and triangles tested. */
+void pgo_trace_closest_counted(const pgo_scene *s, const pg_ray *rays, uint32_t n, pg_hit *hits, uint32_t *nodes,
+                               uint32_t *tris, int n_threads);
 void pgo_trace_any(const pgo_scene *s, const pg_ray *rays, uint32_t n, uint32_t *occluded, int n_threads);
 
 /* Renders rows [row_begin, row_end) of the image with params->spp samples per

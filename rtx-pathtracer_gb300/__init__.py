@@ -68,6 +68,7 @@ SIGNATURES = {
     "pg_scene_set_camera": (_I, [_P, C.POINTER(abi.Camera)]),
     "pg_trace_closest": (_I, [_P, _P, _U32, _P, _P]),
     "pg_trace_any": (_I, [_P, _P, _U32, _P, _P]),
+    "pg_trace_closest_counted": (_I, [_P, _P, _U32, _P, _P, _P, _P]),
     "pg_render": (_I, [_P, C.POINTER(abi.RenderParams), _P, _P, _P, C.POINTER(abi.RenderStats), _P]),
 }
 
@@ -310,6 +311,10 @@ class Scene:
 
     def trace_closest(self, rays_dev, n, hits_dev, stream=None):
         self._check(self.lib.pg_trace_closest(self.h, _dptr(rays_dev), n, _dptr(hits_dev), _stream_handle(stream)))
+
+    def trace_closest_counted(self, rays_dev, n, hits_dev, nodes_dev, tris_dev, stream=None):
+        self._check(self.lib.pg_trace_closest_counted(self.h, _dptr(rays_dev), n, _dptr(hits_dev), _dptr(nodes_dev),
+                                                      _dptr(tris_dev), _stream_handle(stream)))
 
     def trace_any(self, rays_dev, n, occ_dev, stream=None):
         self._check(self.lib.pg_trace_any(self.h, _dptr(rays_dev), n, _dptr(occ_dev), _stream_handle(stream)))

@@ -109,14 +109,22 @@ class SceneInfo(C.Structure):
 class RenderParams(C.Structure):
     _fields_ = [("spp", C.c_uint32), ("max_depth", C.c_uint32), ("seed", C.c_uint32), ("use_nee", C.c_uint32),
                 ("use_mis", C.c_uint32), ("use_guiding", C.c_uint32), ("guiding_prob", C.c_float),
-                ("record_samples", C.c_uint32), ("reserved", C.c_uint32 * 4)]
+                ("record_samples", C.c_uint32), ("flags", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+
+
+PG_RENDER_COUNT_WORK = 1
+PG_RENDER_TIME_STAGES = 2
+STAGES = ("camera", "extend", "shade", "shadow", "advance", "commit")
 
 
 class RenderStats(C.Structure):
     _fields_ = [("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("samples_recorded", C.c_uint64),
-                ("paths", C.c_uint64)]
+                ("paths", C.c_uint64), ("extension_node_visits", C.c_uint64),
+                ("extension_triangle_tests", C.c_uint64), ("shadow_node_visits", C.c_uint64),
+                ("shadow_triangle_tests", C.c_uint64), ("stage_ms", C.c_float * 6),
+                ("stage_launches", C.c_uint32 * 6)]
 
 
 def render_params(spp=1, max_depth=8, seed=1, use_nee=1, use_mis=1, use_guiding=0, guiding_prob=0.5,
-                  record_samples=0) -> RenderParams:
-    return RenderParams(spp, max_depth, seed, use_nee, use_mis, use_guiding, guiding_prob, record_samples)
+                  record_samples=0, flags=0) -> RenderParams:
+    return RenderParams(spp, max_depth, seed, use_nee, use_mis, use_guiding, guiding_prob, record_samples, flags)

@@ -44,6 +44,7 @@ constexpr float kPi = 3.14159265358979323846f;
 constexpr float kTMin = 0.001f;    // tMin of raytrace.rgen:51
 constexpr float kTMax = 1.0e6f;    // tMax of raytrace.rgen:52
 constexpr int kMaxRecords = 16;    // MAX_DIRECTIONAL_DATA_PER_PIXEL (shaders/limits.glsl:7)
+constexpr int kNumStats = 8;       // device render statistics (see DevRender::stats)
 
 struct DevLight {
     int32_t type;      // 0: triangle mesh, 1: sphere
@@ -260,7 +261,7 @@ struct DevRender {
     const uint32_t *light_tris;  // original triangle ids of mesh lights
     const float *light_cdf;      // per light, cumulative area fraction
     const int32_t *tri_light;    // light index of each original triangle, -1 if none
-    unsigned long long *stats;   // [0] extension rays, [1] shadow rays
+    unsigned long long *stats;   // [0] extension rays, [1] shadow rays, [2..5] traversal work (counting renders)
     pg_camera cam;
     float cam_fwd[3], cam_right[3], cam_up[3], tan_half;
     pg_render_params rp;
@@ -362,6 +363,8 @@ __global__ void k_camera(DevRender R) {
 // Queue lengths live on the device (counters[0]: current queue, [1]: next
 // queue being appended, [2]: shadow queue); kernels are launched over all
 // pixels and threads past the length return, so a render needs no host sync.
+// kCount: also add the traversal work to stats[2] (nodes) and stats[3] (triangles).
+template <bool kCount>
 __global__ void k_extend(DevRender R) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= R.counters[0]) return;
@@ -369,7 +372,14 @@ __global__ void k_extend(DevRender R) {
     const float o[3] = {R.ro[3 * p], R.ro[3 * p + 1], R.ro[3 * p + 2]};
     const float d[3] = {R.rd[3 * p], R.rd[3 * p + 1], R.rd[3 * p + 2]};
     pg_hit h;
-    trace_closest(R.S, o, d, kTMin, kTMax, h);
+    if constexpr (kCount) {
+        WorkCount c;
+        trace_closest(R.S, o, d, kTMin, kTMax, h, c);
+        atomicAdd(&R.stats[2], (unsigned long long)c.nodes);
+        atomicAdd(&R.stats[3], (unsigned long long)c.tris);
+    } else {
+        trace_closest(R.S, o, d, kTMin, kTMax, h);
+    }
     R.hits[p] = h;
 }
 
@@ -617,12 +627,23 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
     warp_append(&R.counters[1], R.q_next, p, cont);
 }
 
+// kCount: also add the traversal work to stats[4] (nodes) and stats[5] (triangles).
+template <bool kCount>
 __global__ void k_shadow(DevRender R) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= R.counters[2]) return;
     const float o[3] = {R.sh_o[3 * i], R.sh_o[3 * i + 1], R.sh_o[3 * i + 2]};
     const float d[3] = {R.sh_d[3 * i], R.sh_d[3 * i + 1], R.sh_d[3 * i + 2]};
-    if (trace_any(R.S, o, d, kTMin, R.sh_tmax[i])) return;
+    bool occluded;
+    if constexpr (kCount) {
+        WorkCount c;
+        occluded = trace_any(R.S, o, d, kTMin, R.sh_tmax[i], c);
+        atomicAdd(&R.stats[4], (unsigned long long)c.nodes);
+        atomicAdd(&R.stats[5], (unsigned long long)c.tris);
+    } else {
+        occluded = trace_any(R.S, o, d, kTMin, R.sh_tmax[i]);
+    }
+    if (occluded) return;
     const uint32_t p = R.sh_pix[i];
     atomicAdd(&R.image[3 * p], R.sh_c[3 * i]);
     atomicAdd(&R.image[3 * p + 1], R.sh_c[3 * i + 1]);
@@ -680,6 +701,19 @@ __global__ void k_trace_closest(DevScene S, const pg_ray *rays, uint32_t n, pg_h
     pg_hit h;
     trace_closest(S, r.org, r.dir, r.tmin, r.tmax, h);
     hits[i] = h;
+}
+
+__global__ void k_trace_closest_counted(DevScene S, const pg_ray *rays, uint32_t n, pg_hit *hits, uint32_t *nodes,
+                                        uint32_t *tris) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const pg_ray r = rays[i];
+    pg_hit h;
+    WorkCount c;
+    trace_closest(S, r.org, r.dir, r.tmin, r.tmax, h, c);
+    hits[i] = h;
+    nodes[i] = c.nodes;
+    tris[i] = c.tris;
 }
 
 __global__ void k_trace_any(DevScene S, const pg_ray *rays, uint32_t n, uint32_t *occ) {
@@ -840,11 +874,61 @@ int ensure_uploaded(pg_scene *sc) {
     if (!st) st = upload(&sc->d_light_cdf, sc->h_light_cdf);
     if (!st) st = upload(&sc->d_tri_light, sc->h_tri_light);
     if (!st && cudaMalloc(&sc->d_counters, sizeof(uint32_t) * 16) != cudaSuccess) st = PG_ERR_CUDA;
-    if (!st && cudaMalloc(&sc->d_stats, sizeof(unsigned long long) * 4) != cudaSuccess) st = PG_ERR_CUDA;
+    if (!st && cudaMalloc(&sc->d_stats, sizeof(unsigned long long) * kNumStats) != cudaSuccess) st = PG_ERR_CUDA;
     if (st) return scene_error(st, "scene upload failed (CUDA)");
     sc->uploaded = true;
     return PG_OK;
 }
+
+// Per-stage CUDA-event timing of a render (PG_RENDER_TIME_STAGES): an event
+// pair around every launch, read back whenever the pool fills.
+struct StageTimer {
+    static constexpr uint32_t kPairs = 256;
+    bool on = false;
+    cudaStream_t s = nullptr;
+    std::vector<cudaEvent_t> ev;
+    int stage[kPairs] = {};
+    uint32_t used = 0;
+    float ms[PG_STAGE_COUNT] = {};
+    uint32_t launches[PG_STAGE_COUNT] = {};
+    bool failed = false;
+
+    bool init(bool enable, cudaStream_t st) {
+        on = enable;
+        s = st;
+        if (!on) return true;
+        ev.assign(2 * kPairs, nullptr);
+        for (auto &e : ev)
+            if (cudaEventCreate(&e) != cudaSuccess) return false;
+        return true;
+    }
+    void begin(int stg) {
+        if (!on) return;
+        if (used == kPairs) flush();
+        stage[used] = stg;
+        if (cudaEventRecord(ev[2 * used], s) != cudaSuccess) failed = true;
+    }
+    void end() {
+        if (!on) return;
+        if (cudaEventRecord(ev[2 * used + 1], s) != cudaSuccess) failed = true;
+        ++used;
+    }
+    void flush() {
+        if (!on || used == 0) return;
+        if (cudaEventSynchronize(ev[2 * used - 1]) != cudaSuccess) failed = true;
+        for (uint32_t i = 0; i < used; ++i) {
+            float t = 0.0f;
+            if (cudaEventElapsedTime(&t, ev[2 * i], ev[2 * i + 1]) != cudaSuccess) failed = true;
+            ms[stage[i]] += t;
+            launches[stage[i]] += 1;
+        }
+        used = 0;
+    }
+    ~StageTimer() {
+        for (auto e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+};
 
 DevScene dev_scene(const pg_scene *sc) {
     DevScene S;
@@ -964,6 +1048,16 @@ int pg_trace_closest(pg_scene *sc, const pg_ray *rays, uint32_t n, pg_hit *hits,
     return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ERR_CUDA;
 }
 
+int pg_trace_closest_counted(pg_scene *sc, const pg_ray *rays, uint32_t n, pg_hit *hits, uint32_t *node_visits,
+                             uint32_t *triangle_tests, void *stream) {
+    if (!sc || (n && (!rays || !hits || !node_visits || !triangle_tests))) return PG_ERR_ARG;
+    if (n == 0) return PG_OK;
+    if (int st = ensure_uploaded(sc)) return st;
+    k_trace_closest_counted<<<(n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(dev_scene(sc), rays, n, hits,
+                                                                               node_visits, triangle_tests);
+    return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ERR_CUDA;
+}
+
 int pg_trace_any(pg_scene *sc, const pg_ray *rays, uint32_t n, uint32_t *occluded, void *stream) {
     if (!sc || (!rays && n) || (!occluded && n)) return PG_ERR_ARG;
     if (n == 0) return PG_OK;
@@ -1072,36 +1166,70 @@ int pg_render(pg_scene *sc, const pg_render_params *rp, pg_ctx *guide, float *im
         k_reset_records<<<(slots + 255) / 256, 256, 0, s>>>(records, slots, R.rec_start, P);
     }
     R.stats = sc->d_stats;
-    if (cudaMemsetAsync(sc->d_stats, 0, sizeof(unsigned long long) * 4, s) != cudaSuccess)
+    if (cudaMemsetAsync(sc->d_stats, 0, sizeof(unsigned long long) * kNumStats, s) != cudaSuccess)
         return scene_error(PG_ERR_CUDA, "stats reset");
+    const bool count = (rp->flags & PG_RENDER_COUNT_WORK) != 0;
+    StageTimer tm;
+    if (!tm.init((rp->flags & PG_RENDER_TIME_STAGES) != 0, s)) return scene_error(PG_ERR_CUDA, "stage timer events");
     const uint32_t T = 128;
     const uint32_t G = (P + T - 1) / T;
     for (uint32_t smp = 0; smp < rp->spp; ++smp) {
         R.sample = smp;
         DevRender Rb = R;
+        tm.begin(PG_STAGE_CAMERA);
         k_camera<<<G, T, 0, s>>>(Rb);
+        tm.end();
         for (uint32_t b = 0; b < rp->max_depth; ++b) {
-            k_extend<<<G, T, 0, s>>>(Rb);
+            tm.begin(PG_STAGE_EXTEND);
+            if (count)
+                k_extend<true><<<G, T, 0, s>>>(Rb);
+            else
+                k_extend<false><<<G, T, 0, s>>>(Rb);
+            tm.end();
             const int last = (b + 1 == rp->max_depth) ? 1 : 0;
+            tm.begin(PG_STAGE_SHADE);
             k_shade<<<G, T, 0, s>>>(Rb, (int)b, last);
-            k_shadow<<<G, T, 0, s>>>(Rb);
+            tm.end();
+            tm.begin(PG_STAGE_SHADOW);
+            if (count)
+                k_shadow<true><<<G, T, 0, s>>>(Rb);
+            else
+                k_shadow<false><<<G, T, 0, s>>>(Rb);
+            tm.end();
+            tm.begin(PG_STAGE_ADVANCE);
             k_advance<<<1, 1, 0, s>>>(Rb);
+            tm.end();
             std::swap(Rb.q_cur, Rb.q_next);
         }
-        if (R.recording) k_commit<<<G, T, 0, s>>>(R, P);
+        if (R.recording) {
+            tm.begin(PG_STAGE_COMMIT);
+            k_commit<<<G, T, 0, s>>>(R, P);
+            tm.end();
+        }
     }
     if (cudaGetLastError() != cudaSuccess) return scene_error(PG_ERR_CUDA, "render launch failed");
+    tm.flush();
+    if (tm.failed) return scene_error(PG_ERR_CUDA, "stage timing failed");
     if (stats) {
         uint32_t c[16];
-        unsigned long long st2[4];
+        unsigned long long st2[kNumStats];
         if (cudaMemcpyAsync(c, sc->d_counters, sizeof c, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             cudaMemcpyAsync(st2, sc->d_stats, sizeof st2, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             cudaStreamSynchronize(s) != cudaSuccess)
             return scene_error(PG_ERR_CUDA, "render stats");
+        memset(stats, 0, sizeof *stats);
         stats->extension_rays = st2[0];
         stats->shadow_rays = st2[1];
         stats->samples_recorded = c[4];
         stats->paths = (uint64_t)P * rp->spp;
+        stats->extension_node_visits = st2[2];
+        stats->extension_triangle_tests = st2[3];
+        stats->shadow_node_visits = st2[4];
+        stats->shadow_triangle_tests = st2[5];
+        for (int i = 0; i < PG_STAGE_COUNT; ++i) {
+            stats->stage_ms[i] = tm.ms[i];
+            stats->stage_launches[i] = tm.launches[i];
+        }
     }
     return PG_OK;
 }

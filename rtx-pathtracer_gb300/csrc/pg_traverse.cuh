@@ -150,9 +150,22 @@ __device__ __forceinline__ bool sphere_intersect(const RayPre &r, const pg_spher
 
 constexpr int kStackSize = 64;
 
+// Work counters of one traversal: NoCount compiles to nothing; WorkCount
+// tallies the BVH nodes fetched and the triangles tested.
+struct NoCount {
+    __device__ __forceinline__ void node() {}
+    __device__ __forceinline__ void tri() {}
+};
+struct WorkCount {
+    uint32_t nodes = 0, tris = 0;
+    __device__ __forceinline__ void node() { ++nodes; }
+    __device__ __forceinline__ void tri() { ++tris; }
+};
+
 // Closest hit.  Returns false if nothing is hit in (tmin, tmax).
+template <class Ctr = NoCount>
 __device__ __forceinline__ bool trace_closest(const DevScene &S, const float o[3], const float d[3], float tmin,
-                                              float tmax, pg_hit &hit) {
+                                              float tmax, pg_hit &hit, Ctr &&ctr = Ctr()) {
     const RayPre r = ray_setup(o, d);
     float best_t = tmax;
     uint32_t best_id = PG_NO_HIT;
@@ -169,6 +182,7 @@ __device__ __forceinline__ bool trace_closest(const DevScene &S, const float o[3
     int node = 0;
     for (;;) {
         const DevBvhNode n = S.nodes[node];
+        ctr.node();
         const float e0 = box_enter(r, n.a.x, n.a.y, n.a.z, n.a.w, n.b.x, n.b.y, tmin, best_t);
         const float e1 = box_enter(r, n.b.z, n.b.w, n.c.x, n.c.y, n.c.z, n.c.w, tmin, best_t);
         int nn = 0;
@@ -184,6 +198,7 @@ __device__ __forceinline__ bool trace_closest(const DevScene &S, const float o[3
                 for (int k = 0; k < count; ++k) {
                     const uint32_t ti = (uint32_t)(child + k);
                     const float4 v0 = S.tris[3 * ti], v1 = S.tris[3 * ti + 1], v2 = S.tris[3 * ti + 2];
+                    ctr.tri();
                     float t, u, v;
                     const uint32_t id = __float_as_uint(v0.w);
                     // one ulp above the best t, so an equal t is seen and the lower id wins
@@ -223,8 +238,9 @@ __device__ __forceinline__ bool trace_closest(const DevScene &S, const float o[3
 }
 
 // Any hit in (tmin, tmax).
+template <class Ctr = NoCount>
 __device__ __forceinline__ bool trace_any(const DevScene &S, const float o[3], const float d[3], float tmin,
-                                          float tmax) {
+                                          float tmax, Ctr &&ctr = Ctr()) {
     const RayPre r = ray_setup(o, d);
     for (uint32_t i = 0; i < S.n_spheres; ++i) {
         float t;
@@ -235,6 +251,7 @@ __device__ __forceinline__ bool trace_any(const DevScene &S, const float o[3], c
     int node = 0;
     for (;;) {
         const DevBvhNode n = S.nodes[node];
+        ctr.node();
         const float e0 = box_enter(r, n.a.x, n.a.y, n.a.z, n.a.w, n.b.x, n.b.y, tmin, tmax);
         const float e1 = box_enter(r, n.b.z, n.b.w, n.c.x, n.c.y, n.c.z, n.c.w, tmin, tmax);
         int cand[2];
@@ -248,6 +265,7 @@ __device__ __forceinline__ bool trace_any(const DevScene &S, const float o[3], c
                 for (int k = 0; k < count; ++k) {
                     const uint32_t ti = (uint32_t)(child + k);
                     float t, u, v;
+                    ctr.tri();
                     if (tri_intersect(r, S.tris[3 * ti], S.tris[3 * ti + 1], S.tris[3 * ti + 2], tmin, tmax, t, u, v))
                         return true;
                 }

@@ -6,6 +6,7 @@ import re
 from pathlib import Path
 
 import numpy as np
+import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
 
@@ -60,3 +61,45 @@ def test_struct_layouts(abi):
                                       ("weight", "<f4"), ("pdf", "<f4"), ("distance", "<f4"),
                                       ("flags", "<u4")]))
     assert rec.itemsize == 40
+
+
+def _c_layout(pairs):
+    """sizeof / offsetof of header structs, compiled from include/pathguide.h with gcc."""
+    import shutil
+    import subprocess
+    import tempfile
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "pathguide.h"', "int main(void) {"]
+    for struct, fields in pairs:
+        lines.append(f'printf("{struct} %zu\\n", sizeof({struct}));')
+        for f in fields:
+            lines.append(f'printf("{struct}.{f} %zu\\n", offsetof({struct}, {f}));')
+    lines.append("return 0; }")
+    with tempfile.TemporaryDirectory() as d:
+        src, exe = Path(d) / "layout.c", Path(d) / "layout"
+        src.write_text("\n".join(lines))
+        subprocess.run([cc, "-std=c11", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+        out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    return {k: int(v) for k, v in (ln.split() for ln in out.splitlines())}
+
+
+def test_ctypes_mirrors_match_the_header(abi):
+    structs = [("pg_fit_config", abi.FitConfig), ("pg_fit_tuning", abi.FitTuning), ("pg_camera", abi.Camera),
+               ("pg_cornell_params", abi.CornellParams), ("pg_plates_params", abi.PlatesParams),
+               ("pg_scene_info", abi.SceneInfo), ("pg_render_params", abi.RenderParams),
+               ("pg_render_stats", abi.RenderStats)]
+    dtypes = [("pg_region_state", abi.STATE_DTYPE), ("pg_vmm_theta", abi.VMM_THETA_DTYPE),
+              ("pg_vmf_theta", abi.VMF_THETA_DTYPE), ("pg_material", abi.MATERIAL_DTYPE),
+              ("pg_sphere", abi.SPHERE_DTYPE), ("pg_ray", abi.RAY_DTYPE), ("pg_hit", abi.HIT_DTYPE)]
+    pairs = [(n, [f[0] for f in t._fields_]) for n, t in structs] + [(n, list(dt.names)) for n, dt in dtypes]
+    got = _c_layout(pairs)
+    for n, t in structs:
+        assert got[n] == ctypes.sizeof(t), n
+        for f in t._fields_:
+            assert got[f"{n}.{f[0]}"] == getattr(t, f[0]).offset, f"{n}.{f[0]}"
+    for n, dt in dtypes:
+        assert got[n] == dt.itemsize, n
+        for f in dt.names:
+            assert got[f"{n}.{f}"] == dt.fields[f][1], f"{n}.{f}"

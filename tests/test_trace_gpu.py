@@ -78,7 +78,7 @@ def test_closest_hit_bit_exact(name, cuda, pkg, abi, tracer):
     torch.cuda.synchronize()
     got = host(d_hits, abi.HIT_DTYPE)
     want = tracer.closest(exp, rays)
-    assert (want["prim"] != 0xFFFFFFFF).mean() > 0.3
+    assert (want["prim"] != 0xFFFFFFFF).mean() > 0.15  # the plates scene is open: most random rays escape
     same = got.view(np.uint32).reshape(-1, 4) == want.view(np.uint32).reshape(-1, 4)
     bad = np.where(~same.all(axis=1))[0]
     assert bad.size == 0, f"{bad.size} hits differ; first {bad[:5]}: gpu {got[bad[:3]]} cpu {want[bad[:3]]}"
@@ -98,7 +98,7 @@ def test_any_hit_matches(name, cuda, pkg, abi, tracer):
     torch.cuda.synchronize()
     got = d_occ.cpu().numpy().view(np.uint32)
     want = tracer.any(exp, rays)
-    assert 0.05 < want.mean() < 0.95
+    assert 0.02 < want.mean() < 0.95
     assert np.array_equal(got, want)
     closest = tracer.closest(exp, rays)
     assert np.array_equal(got.astype(bool), closest["prim"] != 0xFFFFFFFF)
@@ -234,3 +234,44 @@ def test_guided_render_same_seed_and_unbiased(cuda, pkg, abi, tracer):
                       guide=ctx)
     u, _ = render_gpu(torch, sc, abi.render_params(spp=spp, max_depth=8, seed=6))
     assert abs(g.mean() - u.mean()) / u.mean() < 0.02
+
+
+@pytest.mark.parametrize("name", sorted(SCENES))
+def test_counted_traversal_matches_cpu_twin(name, cuda, pkg, abi, tracer):
+    """Per-ray BVH node fetches and triangle tests equal the CPU twin's: the
+    work behind the traversal roofline is the algorithm's, counted exactly."""
+    torch = cuda
+    sc = SCENES[name](pkg)
+    exp = sc.export()
+    rays = make_rays(abi, np.random.default_rng(9), exp, 50000)
+    d_rays = dev(torch, rays)
+    d_hits = torch.zeros(rays.shape[0] * 16, dtype=torch.uint8, device="cuda")
+    d_nodes = torch.zeros(rays.shape[0], dtype=torch.int32, device="cuda")
+    d_tris = torch.zeros(rays.shape[0], dtype=torch.int32, device="cuda")
+    sc.trace_closest_counted(d_rays, rays.shape[0], d_hits, d_nodes, d_tris)
+    torch.cuda.synchronize()
+    hits, nodes, tris = tracer.closest_counted(exp, rays)
+    assert np.array_equal(host(d_hits, abi.HIT_DTYPE).view(np.uint32), hits.view(np.uint32))
+    assert np.array_equal(d_nodes.cpu().numpy().view(np.uint32), nodes)
+    assert np.array_equal(d_tris.cpu().numpy().view(np.uint32), tris)
+    assert nodes.mean() > 1 and tris.mean() > 0
+
+
+def test_render_instrumentation(cuda, pkg, abi):
+    """Counting and stage timing leave the image unchanged and report
+    consistent totals."""
+    sc = pkg.Scene.cornell(64, 48, ico_level=4)
+    spp, depth = 3, 6
+    plain, st0 = render_gpu(cuda, sc, abi.render_params(spp=spp, max_depth=depth, seed=2))
+    flags = abi.PG_RENDER_COUNT_WORK | abi.PG_RENDER_TIME_STAGES
+    inst, st = render_gpu(cuda, sc, abi.render_params(spp=spp, max_depth=depth, seed=2, flags=flags))
+    assert np.array_equal(plain, inst)
+    assert st.extension_rays == st0.extension_rays and st.shadow_rays == st0.shadow_rays
+    assert st0.extension_node_visits == 0 and st0.stage_launches[1] == 0
+    assert st.extension_node_visits >= st.extension_rays and st.extension_triangle_tests > 0
+    assert st.shadow_node_visits >= st.shadow_rays
+    launches = dict(zip(abi.STAGES, st.stage_launches))
+    assert launches == {"camera": spp, "extend": spp * depth, "shade": spp * depth, "shadow": spp * depth,
+                        "advance": spp * depth, "commit": 0}
+    ms = dict(zip(abi.STAGES, st.stage_ms))
+    assert all(ms[k] > 0 for k in ("camera", "extend", "shade", "shadow"))
