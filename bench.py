@@ -231,7 +231,7 @@ def bench_tracer(pkg, abi, torch, stream, steps: int, warmup: int, cpu: bool):
     with torch.cuda.stream(stream):
         ev0.record(stream)
         for _ in range(steps):
-            sc.render(params, img, stream=stream)
+            sc.render(params, img, stream=stream, stats=False)
         ev1.record(stream)
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1) / max(steps, 1)
@@ -240,7 +240,7 @@ def bench_tracer(pkg, abi, torch, stream, steps: int, warmup: int, cpu: bool):
     t0 = time.perf_counter()
     with torch.cuda.stream(stream):
         for _ in range(e2e_steps):
-            sc.render(params, img, stream=stream)
+            sc.render(params, img, stream=stream, stats=False)
             img_h.copy_(img, non_blocking=True)
             stream.synchronize()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
@@ -284,6 +284,72 @@ def bench_tracer(pkg, abi, torch, stream, steps: int, warmup: int, cpu: bool):
     return out
 
 
+GUIDED_WORKLOAD = ("guided PT, multi-light glossy scene: 4 GGX plates (roughness 0.005, 0.02, 0.07, 0.2) facing 4 "
+                   "sphere lights (radii 0.03, 0.1, 0.3, 1.0, radiance 0.8/r^2), seeded displaced plane of 707x707 "
+                   "quads (999,698 triangles); 1920x1080, depth 10; 6 training passes of 1-32 spp with recording "
+                   "and a guiding update each, then a 64-spp guided render, all passes accumulated; 4096 regions "
+                   "(12 splits), 8-component parallax-aware mixtures")
+
+
+def bench_guided(pkg, abi, torch, stream, ref_spp: int = 4096):
+    """Equal-time relMSE of guided and plain NEE+MIS path tracing against a
+    high-spp plain render (relMSE = mean (x - r)^2 / (r^2 + 1e-2))."""
+    import __graft_entry__ as entry
+    G = entry.load_submodule("guiding")
+    sc = pkg.Scene.plates(1920, 1080, occluder_grid=707, seed=4)
+    info = sc.info()
+    W, H = info.camera.width, info.camera.height
+    P = W * H
+
+    def plain(spp, seed):
+        img = torch.zeros(P * 3, dtype=torch.float32, device="cuda")
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            done, k = 0, 0
+            while done < spp:
+                n = min(64, spp - done)
+                sc.render(abi.render_params(spp=n, max_depth=10, seed=seed + k), img, stream=stream, stats=False)
+                done, k = done + n, k + 1
+            e1.record(stream)
+        torch.cuda.synchronize()
+        return img.cpu().numpy().reshape(H, W, 3).astype(np.float64) / spp, e0.elapsed_time(e1)
+
+    plain(4, 1)  # warm-up: scene upload and buffers
+    ref, ref_ms = plain(ref_spp, 1_000_000)
+    p64, p64_ms = plain(64, 5000)
+    pg = G.PathGuiding(12, sc.get_scene_size())
+    col = G.SampleCollector(pg.get_region_count(), W, H)
+    img = torch.zeros(P * 3, dtype=torch.float32, device="cuda")
+    G.guided_sequence(sc, pg, col, img, final_spp=4, max_depth=10, seed=3, stream=stream)  # warm-up
+    pg.close()
+    pg = G.PathGuiding(12, sc.get_scene_size())
+    tm = G.guided_sequence(sc, pg, col, img, final_spp=64, max_depth=10, seed=7, stream=stream)
+    guided = img.cpu().numpy().reshape(H, W, 3).astype(np.float64) / tm["spp"]
+    # the final guided render alone (equal samples per pixel with plain 64 spp)
+    g64 = torch.zeros(P * 3, dtype=torch.float32, device="cuda")
+    with torch.cuda.stream(stream):
+        sc.render(abi.render_params(spp=64, max_depth=10, seed=7, use_guiding=1), g64, guide=pg.ctx, stream=stream,
+                  stats=False)
+    torch.cuda.synchronize()
+    g64 = g64.cpu().numpy().reshape(H, W, 3).astype(np.float64) / 64
+    eq_spp = max(1, int(64 * tm["total_ms"] / p64_ms))
+    peq, peq_ms = plain(eq_spp, 9000)
+    out = {"metric": "equal-time relMSE, guided vs plain NEE+MIS PT", "unit": "relMSE", "higher_is_better": False,
+           "config": {"workload": GUIDED_WORKLOAD, "triangles": info.n_triangles,
+                      "reference": f"plain NEE+MIS, {ref_spp} spp ({ref_ms / 1e3:.1f} s)", "relmse_eps": 1e-2},
+           "guided": {"relmse": G.relmse(guided, ref), "ms": tm["total_ms"], "train_ms": tm["train_ms"],
+                      "final_render_ms": tm["render_ms"], "spp": tm["spp"]},
+           "plain_equal_time": {"relmse": G.relmse(peq, ref), "ms": peq_ms, "spp": eq_spp},
+           "equal_spp_64": {"guided_relmse": G.relmse(g64, ref), "plain_relmse": G.relmse(p64, ref),
+                            "plain_ms": p64_ms}}
+    out["value"] = out["guided"]["relmse"] / out["plain_equal_time"]["relmse"]
+    out["value_meaning"] = "guided relMSE / plain relMSE at equal time (< 1: guiding wins)"
+    pg.close()
+    sc.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -302,8 +368,8 @@ def main():
     ap.add_argument("--median", type=float, default=0.0, help="override the median region size")
     ap.add_argument("--sigma", type=float, default=-1.0, help="override the region-size sigma")
     ap.add_argument("--sweep", action="store_true", help="time the tuning grid and print one line per point")
-    ap.add_argument("--workload", default="all", choices=["all", "em", "tracer"],
-                    help="all: the EM line with the tracer block; em / tracer: one of them alone")
+    ap.add_argument("--workload", default="all", choices=["all", "em", "tracer", "guided"],
+                    help="all: the EM line with the tracer and guided blocks; em / tracer / guided: one alone")
     ap.add_argument("--ref-seconds", type=float, default=None,
                     help="CPU seconds per reference step (default: ~100 s over the whole run)")
     args = ap.parse_args()
@@ -324,12 +390,15 @@ def main():
     torch.cuda.set_device(local)
     pkg = entry.load_package()
     abi = pkg.abi
-    if args.workload == "tracer":
+    if args.workload in ("tracer", "guided"):
         stream = torch.cuda.Stream()
         sampler = ClockSampler(local)
         with sampler:
-            line = bench_tracer(pkg, abi, torch, stream, args.steps, args.warmup,
-                                cpu=rank == 0 and not args.no_cpu_baseline)
+            if args.workload == "tracer":
+                line = bench_tracer(pkg, abi, torch, stream, args.steps, args.warmup,
+                                    cpu=rank == 0 and not args.no_cpu_baseline)
+            else:
+                line = bench_guided(pkg, abi, torch, stream)
         line.update(n_gpus=world, scaling="weak", vs_baseline=None, data="synthetic (procedural scene)",
                     clocks=sampler.summary())
         if rank == 0:
@@ -456,6 +525,11 @@ def main():
                               cpu=rank == 0 and not args.no_cpu_baseline)
         tr["clocks"] = tsampler.summary()
         line["tracer"] = tr
+        gsampler = ClockSampler(local)
+        with gsampler:
+            gd = bench_guided(pkg, abi, torch, stream)
+        gd["clocks"] = gsampler.summary()
+        line["guided"] = gd
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

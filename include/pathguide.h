@@ -243,7 +243,8 @@ int pg_sort_samples(pg_ctx *ctx, const pg_directional_data *records, uint64_t n_
 
 /* PathGuiding::preFit (src/PathGuiding.cpp:370-411): sets each region's
  * parallax mean to its box centre, re-aims its lobes at the new mean after the
- * first fit (incrementaldistance.h:109-131), and writes for each bucketed
+ * first fit (incrementaldistance.h:109-131) - both only for regions with
+ * records in this pass, as PathGuiding::update skips empty ones - and writes for each bucketed
  * record the float4 {direction, weight} seen from the mean and the distance
  * (+inf for misses).  Without parallax the directions pass through. */
 int pg_prefit_parallax(pg_ctx *ctx, const pg_directional_data *sorted, const uint32_t *offsets,
@@ -251,7 +252,8 @@ int pg_prefit_parallax(pg_ctx *ctx, const pg_directional_data *sorted, const uin
 
 /* Harmonic-mean lobe distances over one pass of samples (the statistic of
  * external/guiding/incrementaldistance.h:57-107, PathGuiding::postFit,
- * src/PathGuiding.cpp:445-448). */
+ * src/PathGuiding.cpp:445-448).  Regions without samples are left unchanged,
+ * as PathGuiding::update runs postFit only for non-empty regions. */
 int pg_update_distances(pg_ctx *ctx, const float *dirw, const float *dist, const uint32_t *offsets,
                         uint32_t n_regions, void *stream);
 

@@ -307,8 +307,12 @@ static void fit_region32(const pg_fit_config *cfg, int mode, const float *dirw, 
     const uint32_t nk = (K + 3) / 4;
     for (uint32_t c = K; c < 4 * nk; ++c) reset_lane(s, (int)c);
     stats32 old;
+    memset(&old, 0, sizeof old);
     const int update = (mode == PG_FIT_UPDATE);
-    if (update) stats_from_mixture32(cfg, s, &old);
+    /* A region without prior samples starts from its current mixture alone:
+     * lightpmm's removeAvgCosinePrior divides by the prior sample count
+     * (VMMFactory.h:428-433), which would make its statistics NaN for good. */
+    if (update && s->total_num_samples > 0) stats_from_mixture32(cfg, s, &old);
     const uint32_t N = e - b;
     const uint32_t max_itr = (N > 2 * K) ? cfg->max_itr : 0;
     float sum_w = 0.0f, ll = 0.0f, last_ll = 0.0f, abs_inv_last = 0.0f;
@@ -453,7 +457,7 @@ static void fit_region64(const pg_fit_config *cfg, int mode, const float *dirw, 
     stats64 old;
     memset(&old, 0, sizeof old);
     double total = (double)s->total_num_samples;
-    if (update) {
+    if (update && s->total_num_samples > 0) {  /* no prior samples: no prior statistics */
         const double inv_wpn = (double)cfg->v_prior * K + 1.0;
         const double wptn = cfg->v_prior / inv_wpn;
         const double rptw = (double)cfg->r_prior * cfg->r_prior_weight;
@@ -641,6 +645,8 @@ void pgo_prefit_parallax(uint32_t n_regions, const pg_directional_data *sorted,
 void pgo_update_distances(uint32_t n_regions, const float *dirw, const float *dist,
                           const uint32_t *offsets, pg_region_state *states) {
     for (uint32_t r = 0; r < n_regions; ++r) {
+        /* postFit runs only for regions with samples (PathGuiding.cpp:281-288) */
+        if (offsets[r + 1] == offsets[r]) continue;
         pg_region_state *s = &states[r];
         const uint32_t K = s->k;
         double bw[16] = {0}, bwd[16] = {0};

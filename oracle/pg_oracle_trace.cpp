@@ -466,6 +466,22 @@ Eval bsdf(const pg_material &m, D3 n, D3 wi, D3 wo) {
     return r;
 }
 
+bool is_delta(const pg_material &m) { return m.type == PG_MAT_DIELECTRIC || m.type == PG_MAT_SPECULAR; }
+bool almost_delta(const pg_material &m) { return m.type == PG_MAT_GGX && m.roughness <= 0.3f; }
+// guiding follows the recording rule: not on discrete or almost-discrete lobes
+bool guided_material(const pg_material &m) { return !is_delta(m) && !almost_delta(m); }
+
+D3 sample_bsdf(const pg_material &m, D3 d, D3 n, double u1, double u2) {
+    if (m.type == PG_MAT_DIFFUSE) {
+        const double sr = sqrt(u1), ph = 2.0 * PI * u2;
+        return to_world(d3(sr * cos(ph), sr * sin(ph), sqrt(std::max(0.0, 1.0 - u1))), n);
+    }
+    const double a2 = std::max((double)m.roughness * m.roughness, 1e-12);
+    const double t2 = a2 * u1 / std::max(1.0 - u1, 1e-12);
+    const double cm = 1.0 / sqrt(1.0 + t2), sm = sqrt(std::max(0.0, 1.0 - cm * cm)), ph = 2.0 * PI * u2;
+    return reflect(d, to_world(d3(sm * cos(ph), sm * sin(ph), cm), n));
+}
+
 uint32_t region_of(const pgo_guide &g, D3 p) {
     float lo[3] = {g.root[0], g.root[1], g.root[2]}, hi[3] = {g.root[3], g.root[4], g.root[5]};
     const float pp[3] = {(float)p.x, (float)p.y, (float)p.z};
@@ -520,8 +536,6 @@ D3 vmm_sample(const pg_vmm_theta &v, D3 x, int par, double ul, double u1, double
     const double z = 1.0 - 2.0 * u1, r = sqrt(std::max(0.0, 1.0 - z * z)), ph = 2.0 * PI * u2;
     return d3(r * cos(ph), r * sin(ph), z);
 }
-
-bool is_delta(const pg_material &m) { return m.type == PG_MAT_DIELECTRIC || m.type == PG_MAT_SPECULAR; }
 
 D3 render_pixel(const Scene64 &sc, const pg_render_params &rp, const pgo_guide *g, uint32_t pix, uint32_t smp) {
     const pgo_scene &S = *sc.S;
@@ -616,10 +630,12 @@ D3 render_pixel(const Scene64 &sc, const pg_render_params &rp, const pgo_guide *
                 const Eval me = bsdf(m, n, wi, wl);
                 if (mx(me.f) > 0.0) {
                     double pb = me.pdf;
-                    if (rp.use_guiding && g) {
+                    if (rp.use_guiding && g && guided_material(m)) {
                         const uint32_t reg = region_of(*g, x);
-                        if (reg != PG_INVALID_REGION)
-                            pb = (1.0 - rp.guiding_prob) * pb + rp.guiding_prob * vmm_pdf(g->vmm[reg], wl, x, par);
+                        if (reg != PG_INVALID_REGION) {
+                            const double pg = vmm_pdf(g->vmm[reg], wl, x, par);
+                            if (!std::isnan(pg)) pb = (1.0 - rp.guiding_prob) * pb + rp.guiding_prob * pg;
+                        }
                     }
                     const double w = rp.use_mis ? pl * pl / (pl * pl + pb * pb) : 1.0;
                     if (intersect64(S, x, wl, 0.001, dist * (1.0 - 0.0001), true).prim == PG_NO_HIT)
@@ -651,30 +667,36 @@ D3 render_pixel(const Scene64 &sc, const pg_render_params &rp, const pgo_guide *
             tc = fv(m.albedo);
             delta = true;
         } else {
+            const bool gm = rp.use_guiding && g && guided_material(m);
             bool use_guide = false, terminate = false;
             uint32_t reg = PG_INVALID_REGION;
-            if (rp.use_guiding && g) {
+            if (gm) {
                 reg = region_of(*g, x);
                 if (reg == PG_INVALID_REGION) terminate = true;
                 use_guide = uch < rp.guiding_prob;
             }
             if (!terminate) {
-                if (use_guide) {
+                if (use_guide)
                     wo = vmm_sample(g->vmm[reg], x, par, rnd(rp.seed, pix, smp, dimb(b, 7)), u1, u2);
-                } else if (m.type == PG_MAT_DIFFUSE) {
-                    const double sr = sqrt(u1), ph = 2.0 * PI * u2;
-                    wo = to_world(d3(sr * cos(ph), sr * sin(ph), sqrt(std::max(0.0, 1.0 - u1))), n);
-                } else {
-                    const double a2 = std::max((double)m.roughness * m.roughness, 1e-12);
-                    const double t2 = a2 * u1 / std::max(1.0 - u1, 1e-12);
-                    const double cm = 1.0 / sqrt(1.0 + t2), sm = sqrt(std::max(0.0, 1.0 - cm * cm)), ph = 2.0 * PI * u2;
-                    wo = reflect(d, to_world(d3(sm * cos(ph), sm * sin(ph), cm), n));
-                }
-                const Eval me = bsdf(m, n, wi, wo);
+                else
+                    wo = sample_bsdf(m, d, n, u1, u2);
+                Eval me = bsdf(m, n, wi, wo);
                 pdf = me.pdf;
-                if (rp.use_guiding && g && dot(wo, n) > 0.0 && me.pdf > 0.0) {
-                    const double pg = vmm_pdf(g->vmm[reg], wo, x, par);
-                    if (!std::isnan(pg)) pdf = (1.0 - rp.guiding_prob) * me.pdf + rp.guiding_prob * pg;
+                if (gm) {
+                    if (dot(wo, n) < 0.0 || me.pdf <= 0.0) {
+                        pdf = 0.0;
+                    } else {
+                        const double pg = vmm_pdf(g->vmm[reg], wo, x, par);
+                        if (std::isnan(pg)) {
+                            if (use_guide) {
+                                wo = sample_bsdf(m, d, n, u1, u2);
+                                me = bsdf(m, n, wi, wo);
+                            }
+                            pdf = me.pdf;
+                        } else {
+                            pdf = (1.0 - rp.guiding_prob) * me.pdf + rp.guiding_prob * pg;
+                        }
+                    }
                 }
                 if (dot(wo, n) > 0.0 && pdf > 0.0 && me.pdf > 0.0)
                     tc = me.f * (1.0 / pdf);

@@ -320,10 +320,16 @@ class Scene:
         self._check(self.lib.pg_trace_any(self.h, _dptr(rays_dev), n, _dptr(occ_dev), _stream_handle(stream)))
 
     def render(self, params: abi.RenderParams, image_dev, guide: "FitContext | None" = None, records_dev=None,
-               stream=None) -> abi.RenderStats:
-        """Adds params.spp samples per pixel of radiance into image_dev (float32, H*W*3)."""
-        st = abi.RenderStats()
+               stream=None, stats: bool = True) -> "abi.RenderStats | None":
+        """Adds params.spp samples per pixel of radiance into image_dev (float32, H*W*3).
+        With stats, waits for the render and returns its counters; without,
+        returns at once (stream-ordered)."""
+        st = abi.RenderStats() if stats else None
         self._check(self.lib.pg_render(self.h, C.byref(params), guide.h if guide is not None else None,
                                        _dptr(image_dev), _dptr(records_dev) if records_dev is not None else None,
-                                       C.byref(st), _stream_handle(stream)))
+                                       C.byref(st) if st is not None else None, _stream_handle(stream)))
         return st
+
+    def get_scene_size(self):
+        """SceneLoader::getSceneSize (src/SceneLoader.h:118): the scene box (min xyz, max xyz)."""
+        return list(self.info().aabb)

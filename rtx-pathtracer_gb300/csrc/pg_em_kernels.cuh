@@ -168,9 +168,12 @@ __device__ void load_model(const EmArgs &a, EmShared<KMAX, NW> &S, pg_region_sta
         S.rr[lane] = r;
         S.nrm[lane] = n;
         S.em2k[lane] = e;
-        // computeSufficentStatsFromMixture (VMMFactory.h:543-555) for updateFit
+        // computeSufficentStatsFromMixture (VMMFactory.h:543-555) for updateFit.
+        // A region without prior samples starts from its current mixture alone:
+        // removeAvgCosinePrior divides by the prior sample count
+        // (VMMFactory.h:428-433), which would make its statistics NaN for good.
         float ow = 0.0f, osx = 0.0f, osy = 0.0f, osz = 0.0f;
-        if (a.mode == PG_FIT_UPDATE && lane < (int)K) {
+        if (a.mode == PG_FIT_UPDATE && lane < (int)K && st->total_num_samples > 0) {
             const float inv_wpn = cfg.v_prior * (float)K + 1.0f;
             const float wpn = 1.0f / inv_wpn;
             const float wptn = cfg.v_prior * wpn;

@@ -247,8 +247,8 @@ __global__ void prefit_parallax_kernel(const pg_directional_data *rec, const uin
 // src/PathGuiding.cpp:380-383) and, after the first fit, re-aim the lobes with a
 // finite distance at the new mean (IncrementalDistance::reposition,
 // external/guiding/incrementaldistance.h:109-131).
-__global__ void parallax_means_kernel(pg_region_state *states, const float *aabbs, uint32_t n_regions,
-                                      int reposition, float *means_out) {
+__global__ void parallax_means_kernel(pg_region_state *states, const float *aabbs, const uint32_t *offsets,
+                                      uint32_t n_regions, int reposition, float *means_out) {
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n_regions) return;
     pg_region_state *s = states + r;
@@ -256,9 +256,14 @@ __global__ void parallax_means_kernel(pg_region_state *states, const float *aabb
     float m[3];
     for (int i = 0; i < 3; ++i) {
         m[i] = __fadd_rn(b[i], __fmul_rn(0.5f, __fsub_rn(b[3 + i], b[i])));
+        means_out[3 * (size_t)r + i] = m[i];
+    }
+    // regions without samples in this pass are left alone (PathGuiding::update
+    // calls updateRegion only for non-empty ranges, src/PathGuiding.cpp:281-288)
+    if (offsets && offsets[r + 1] == offsets[r]) return;
+    for (int i = 0; i < 3; ++i) {
         s->last_parallax_mean[i] = s->parallax_mean[i];
         s->parallax_mean[i] = m[i];
-        means_out[3 * (size_t)r + i] = m[i];
     }
     if (!reposition) return;
     const float d0 = __fsub_rn(s->last_parallax_mean[0], m[0]);
@@ -291,6 +296,10 @@ __global__ void __launch_bounds__(NT) distance_kernel(pg_region_state *states, c
     __shared__ float red[NW][32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (uint32_t r = blockIdx.x; r < n_regions; r += gridDim.x) {
+        // regions without samples are not updated (postFit runs only for
+        // non-empty regions, src/PathGuiding.cpp:281-288): an empty batch
+        // would turn the initial infinite distance into 0/0
+        if (offsets[r + 1] == offsets[r]) continue;
         pg_region_state *s = states + r;
         const uint32_t K = min(s->k, 16u);
         if (tid < 16) {
@@ -683,7 +692,7 @@ int pg_prefit_parallax(pg_ctx *ctx, const pg_directional_data *sorted, const uin
         return set_error(ctx, PG_ERR_STATE, "pg_set_regions must run before the parallax pre-pass");
     cudaStream_t s = (cudaStream_t)stream;
     if (ctx->cfg.use_parallax) {
-        parallax_means_kernel<<<(n_regions + 127) / 128, 128, 0, s>>>(ctx->d_states, g.aabbs, n_regions,
+        parallax_means_kernel<<<(n_regions + 127) / 128, 128, 0, s>>>(ctx->d_states, g.aabbs, offsets, n_regions,
                                                                        g.fitted ? 1 : 0, g.means);
     }
     if (n_valid)
@@ -742,7 +751,8 @@ int pg_update(pg_ctx *ctx, const pg_directional_data *records, uint64_t n_record
     // 2. parallax pre-pass (PathGuiding::preFit), gathering through the sort order
     const int par = ctx->cfg.use_parallax ? 1 : 0;
     if (par)
-        parallax_means_kernel<<<(R + 127) / 128, 128, 0, s>>>(ctx->d_states, g.aabbs, R, g.fitted ? 1 : 0, g.means);
+        parallax_means_kernel<<<(R + 127) / 128, 128, 0, s>>>(ctx->d_states, g.aabbs, g.offsets, R, g.fitted ? 1 : 0,
+                                                              g.means);
     if (n_records)
         prefit_parallax_kernel<<<std::min<uint64_t>((n_records + 255) / 256, 16384u), 256, 0, s>>>(
             records, order, (uint32_t)n_records, g.offsets + R, R, g.means, par, g.dirw, g.dist);

@@ -161,6 +161,26 @@ __device__ __forceinline__ bool is_delta(const pg_material &m) {
 __device__ __forceinline__ bool almost_delta(const pg_material &m) {
     return m.type == PG_MAT_GGX && m.roughness <= 0.3f;
 }
+// Vertices whose continuation mixes in the guide.  The reference guides every
+// non-discrete material (raytrace.rgen:926) but records only the ones that
+// are not almost discrete; here guiding follows the recording rule, so a
+// near-specular lobe is never sampled from a mixture learned at other
+// surfaces of its region.
+__device__ __forceinline__ bool guided_material(const pg_material &m) { return !is_delta(m) && !almost_delta(m); }
+
+// Lambert (cosine) or GGX (normal distribution, then reflection) sample.
+__device__ __forceinline__ V sample_bsdf(const pg_material &m, V d, V n, float u1, float u2) {
+    if (m.type == PG_MAT_DIFFUSE) {
+        const float sr = sqrtf(u1), ph = 2.0f * kPi * u2;
+        return to_world(mk(sr * cosf(ph), sr * sinf(ph), sqrtf(fmaxf(0.0f, 1.0f - u1))), n);
+    }
+    const float a2 = fmaxf(m.roughness * m.roughness, 1e-12f);
+    const float t2 = a2 * u1 / fmaxf(1.0f - u1, 1e-12f);
+    const float cm = rsqrtf(1.0f + t2), sm = sqrtf(fmaxf(0.0f, 1.0f - cm * cm));
+    const float ph = 2.0f * kPi * u2;
+    const V mh = to_world(mk(sm * cosf(ph), sm * sinf(ph), cm), n);
+    return reflect3(d, mh);
+}
 
 // ---------------------------------------------------------------------------
 // Guiding: region lookup and the vMF mixture (shaders/guiding.glsl:32-96)
@@ -500,12 +520,13 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
                     const float pl = dist2 / (cl * L.area) / (float)R.n_lights;
                     const MatEval me = bsdf_eval(m, n, wi, wl);
                     if (maxc(me.f) > 0.0f) {
+                        // pdf of the continuation sampler for this direction (MIS)
                         float pb = me.pdf;
-                        if (R.guiding) {
+                        if (R.guiding && guided_material(m)) {
                             const uint32_t reg = region_of(R.guide, x);
                             if (reg != PG_INVALID_REGION) {
                                 const float pg = vmm_pdf(R.guide.vmm[reg], wl, x, R.guide.use_parallax);
-                                pb = (1.0f - R.rp.guiding_prob) * pb + R.rp.guiding_prob * pg;
+                                if (!isnan(pg)) pb = (1.0f - R.rp.guiding_prob) * pb + R.rp.guiding_prob * pg;
                             }
                         }
                         const float w = R.rp.use_mis ? pl * pl / (pl * pl + pb * pb) : 1.0f;
@@ -550,10 +571,11 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
                 tc = mk(m.albedo[0], m.albedo[1], m.albedo[2]);
                 delta = true;
             } else {
+                const bool gm = R.guiding && guided_material(m);
                 bool use_guide = false;
                 uint32_t reg = PG_INVALID_REGION;
                 bool terminate = false;
-                if (R.guiding) {
+                if (gm) {
                     reg = region_of(R.guide, x);
                     if (reg == PG_INVALID_REGION) terminate = true;  // no region: the path ends
                     use_guide = uch < R.rp.guiding_prob;
@@ -562,22 +584,27 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
                     if (use_guide) {
                         const float ua = rnd(R.rp.seed, p, R.sample, dimb(b, 7));
                         wo = vmm_sample(R.guide.vmm[reg], x, R.guide.use_parallax, ua, u1, u2);
-                    } else if (m.type == PG_MAT_DIFFUSE) {
-                        const float sr = sqrtf(u1), ph = 2.0f * kPi * u2;
-                        wo = to_world(mk(sr * cosf(ph), sr * sinf(ph), sqrtf(fmaxf(0.0f, 1.0f - u1))), n);
-                    } else {  // GGX: sample the normal distribution, reflect
-                        const float a2 = fmaxf(m.roughness * m.roughness, 1e-12f);
-                        const float t2 = a2 * u1 / fmaxf(1.0f - u1, 1e-12f);
-                        const float cm = rsqrtf(1.0f + t2), sm = sqrtf(fmaxf(0.0f, 1.0f - cm * cm));
-                        const float ph = 2.0f * kPi * u2;
-                        const V mh = to_world(mk(sm * cosf(ph), sm * sinf(ph), cm), n);
-                        wo = reflect3(d, mh);
+                    } else {
+                        wo = sample_bsdf(m, d, n, u1, u2);
                     }
-                    const MatEval me = bsdf_eval(m, n, wi, wo);
+                    MatEval me = bsdf_eval(m, n, wi, wo);
                     pdf = me.pdf;
-                    if (R.guiding && dot3(wo, n) > 0.0f && me.pdf > 0.0f) {
-                        const float pg = vmm_pdf(R.guide.vmm[reg], wo, x, R.guide.use_parallax);
-                        if (!isnan(pg)) pdf = (1.0f - R.rp.guiding_prob) * me.pdf + R.rp.guiding_prob * pg;
+                    if (gm) {
+                        if (dot3(wo, n) < 0.0f || me.pdf <= 0.0f) {
+                            pdf = 0.0f;
+                        } else {
+                            const float pg = vmm_pdf(R.guide.vmm[reg], wo, x, R.guide.use_parallax);
+                            if (isnan(pg)) {
+                                // unusable mixture: a plain BSDF sample (raytrace.rgen:951-953)
+                                if (use_guide) {
+                                    wo = sample_bsdf(m, d, n, u1, u2);
+                                    me = bsdf_eval(m, n, wi, wo);
+                                }
+                                pdf = me.pdf;
+                            } else {
+                                pdf = (1.0f - R.rp.guiding_prob) * me.pdf + R.rp.guiding_prob * pg;
+                            }
+                        }
                     }
                     if (dot3(wo, n) > 0.0f && pdf > 0.0f && me.pdf > 0.0f) tc = mul(me.f, 1.0f / pdf);
                     else pdf = 0.0f;

@@ -1,0 +1,121 @@
+"""Host-side mirror of the reference's guiding loop over the C ABI.
+
+- SampleCollector (src/SampleCollector.h:36-39, src/SampleCollector.cpp:29-131):
+  the tracer's record buffer, width * height * 16 DirectionalData slots on the
+  device, and getSortedData as a host copy bucketed by region.
+- PathGuiding (src/PathGuiding.h:132-136): regions from `splitCount` midpoint
+  splits of the scene box, update(SampleCollector) fitting every region's
+  vMF mixture on the device, getRegionCount().
+- guided_sequence: the headless form of RayTracingApp's frame loop
+  (src/RayTracingApp.cpp:125-157): training passes that render with sample
+  recording and call PathGuiding::update, then a guided render.
+
+Device buffers are torch tensors (allocation and streams only); all work is in
+the library.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import FitContext, Scene, abi
+
+RECORD_BYTES = 40
+RECORDS_PER_PIXEL = 16  # MAX_DIRECTIONAL_DATA_PER_PIXEL (shaders/limits.glsl:7)
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class SampleCollector:
+    """SampleCollector(regionCount, imageSize): one record slot per pixel and
+    path vertex, written by pg_render with record_samples."""
+
+    def __init__(self, region_count: int, width: int, height: int):
+        torch = _torch()
+        self.region_count = region_count
+        self.width, self.height = width, height
+        self.n_slots = width * height * RECORDS_PER_PIXEL
+        self.buffer = torch.empty(self.n_slots * RECORD_BYTES, dtype=torch.uint8, device="cuda")
+
+    def get_sorted_data(self, guiding: "PathGuiding", stream=None):
+        """getSortedData (src/SampleCollector.cpp:76-131): records grouped by
+        region (stable), with regionCount + 1 offsets; INVALID records are
+        dropped.  Returns (records as a structured array, offsets)."""
+        torch = _torch()
+        R = self.region_count
+        out = torch.empty(self.n_slots * RECORD_BYTES, dtype=torch.uint8, device="cuda")
+        offs = torch.empty(R + 1, dtype=torch.int32, device="cuda")
+        guiding.ctx.sort_samples(self.buffer, self.n_slots, R, out, offs, stream=stream)
+        torch.cuda.synchronize()
+        offsets = offs.cpu().numpy().view(np.uint32).copy()
+        n = int(offsets[-1])
+        from .workloads import RECORD_DTYPE
+        rec = np.frombuffer(out[: n * RECORD_BYTES].cpu().numpy().tobytes(), dtype=RECORD_DTYPE).copy()
+        return rec, offsets
+
+
+class PathGuiding:
+    """PathGuiding(splitCount, sceneAabb, useParallaxCompensation)."""
+
+    def __init__(self, split_count: int, scene_aabb, use_parallax: bool = True, cfg: "abi.FitConfig | None" = None,
+                 stream=None):
+        cfg = cfg if cfg is not None else abi.default_fit_config()
+        cfg.use_parallax = 1 if use_parallax else 0
+        self.split_count = split_count
+        self.ctx = FitContext(cfg, max_regions=1 << split_count)
+        self.ctx.set_regions(split_count, np.asarray(scene_aabb, dtype=np.float32), stream=stream)
+
+    def get_region_count(self) -> int:
+        return self.ctx.region_count()
+
+    def update(self, collector: SampleCollector, stream=None) -> bool:
+        """One guiding pass over the collector's records (bucket, parallax
+        pre-pass, fit or stepwise update, distances, VMM_Theta).  Returns
+        whether the tracer must rebind its region buffers; regions are never
+        re-split here, so always False."""
+        self.ctx.update(collector.buffer, collector.n_slots, stream=stream)
+        return False
+
+    def close(self):
+        self.ctx.close()
+
+
+def relmse(img: np.ndarray, ref: np.ndarray, eps: float = 1e-2) -> float:
+    """Relative MSE, mean over pixels and channels of (x - r)^2 / (r^2 + eps)."""
+    img = np.asarray(img, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    return float(np.mean((img - ref) ** 2 / (ref * ref + eps)))
+
+
+def guided_sequence(scene: Scene, guiding: PathGuiding, collector: SampleCollector, image, train_spp=(1, 2, 4, 8, 16, 32),
+                    final_spp: int = 64, max_depth: int = 10, seed: int = 1, guiding_prob: float = 0.5,
+                    accumulate_training: bool = True, stream=None) -> dict:
+    """Training passes (render with recording, then PathGuiding::update; the
+    first pass is unguided), then a guided render of final_spp samples.  The
+    image (cleared first) receives radiance sums: of every pass when
+    accumulate_training (the reference keeps accumulating frames while it
+    trains, src/RayTracingApp.cpp:125-157), else of the final render only.
+    Returns CUDA-event times in ms and the number of samples per pixel summed."""
+    torch = _torch()
+    s = stream or torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    scratch = image if accumulate_training else torch.empty_like(image)
+    with torch.cuda.stream(s):
+        image.zero_()
+        ev[0].record(s)
+        for i, spp in enumerate(train_spp):
+            p = abi.render_params(spp=spp, max_depth=max_depth, seed=seed + 1000 * (i + 1),
+                                  use_guiding=1 if i > 0 else 0, guiding_prob=guiding_prob, record_samples=1)
+            scene.render(p, scratch, guide=guiding.ctx, records_dev=collector.buffer, stream=s, stats=False)
+            guiding.update(collector, stream=s)
+        ev[1].record(s)
+        p = abi.render_params(spp=final_spp, max_depth=max_depth, seed=seed, use_guiding=1,
+                              guiding_prob=guiding_prob)
+        scene.render(p, image, guide=guiding.ctx, stream=s, stats=False)
+        ev[2].record(s)
+    torch.cuda.synchronize()
+    total = final_spp + (sum(train_spp) if accumulate_training else 0)
+    return {"train_ms": ev[0].elapsed_time(ev[1]), "render_ms": ev[1].elapsed_time(ev[2]),
+            "total_ms": ev[0].elapsed_time(ev[2]), "spp": total}

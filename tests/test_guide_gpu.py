@@ -97,7 +97,9 @@ def test_prefit_parallax_matches_oracle(cuda, pkg, abi, oracle, workloads):
     np.testing.assert_array_equal(d_dirw.cpu().numpy(), want_dirw)
     np.testing.assert_array_equal(d_dist.cpu().numpy(), want_dist)
     st = ctx.states(R)
-    np.testing.assert_array_equal(st["parallax_mean"], means)
+    busy = np.diff(off.astype(np.int64)) > 0
+    np.testing.assert_array_equal(st["parallax_mean"][busy], means[busy])
+    np.testing.assert_array_equal(st["parallax_mean"][~busy], 0.0)  # empty regions keep their state
     ctx.close()
 
 
@@ -155,10 +157,11 @@ def oracle_update(oracle, abi, cfg, rec, boxes, states, first):
     srt, off = oracle.sort_samples(rec, R)
     means = boxes[:, :3] + np.float32(0.5) * (boxes[:, 3:] - boxes[:, :3])
     st = states.copy()
-    st["last_parallax_mean"] = st["parallax_mean"]
-    st["parallax_mean"] = means
+    busy = np.diff(off.astype(np.int64)) > 0  # empty regions are not updated (PathGuiding.cpp:281-288)
+    st["last_parallax_mean"][busy] = st["parallax_mean"][busy]
+    st["parallax_mean"][busy] = means[busy]
     if not first:
-        for r in range(R):
+        for r in np.where(busy)[0]:
             st[r] = oracle.reposition(st[r], st["last_parallax_mean"][r] - means[r])
     dirw, dist = oracle.prefit_parallax(srt, off, means)
     st, _ = oracle.fit(cfg, dirw, off, states=st, mode=abi.PG_FIT_CONTINUE if first else abi.PG_FIT_UPDATE)
@@ -202,3 +205,46 @@ def test_update_requires_regions(cuda, pkg, abi):
         ctx.update(torch.zeros(40, dtype=torch.uint8, device="cuda"), 1)
     assert e.value.status == abi.PG_ERR_STATE
     ctx.close()
+
+
+def test_region_first_seen_in_a_later_pass(cuda, pkg, abi, oracle, workloads):
+    """A region empty in the first pass and filled in a later one is fitted
+    from its initial mixture (no prior statistics), never NaN; regions that
+    stay empty keep their state untouched."""
+    torch = cuda
+    scene = np.array([-1.0, -1.0, -1.0, 1.0, 1.0, 1.0], dtype=np.float32)
+    cfg = abi.default_fit_config(num_initial_components=8)
+    ctx = pkg.FitContext(cfg, max_regions=8)
+    ctx.set_regions(3, scene)
+    R = ctx.region_count()
+    rec, _ = records_in_regions(workloads, oracle, 3, scene, seed=5, median=900, invalid=0.0)
+    rec["flags"][rec["flags"] >= R] = 0
+    first = rec[rec["flags"] < 4]           # pass 0: regions 0-3 only
+    ctx.update(dev(torch, first), first.shape[0])
+    ctx.sync()
+    s0 = ctx.states(R)
+    assert (s0["total_num_samples"][4:] == 0).all()
+    ctx.update(dev(torch, rec[rec["flags"] != 7]), int((rec["flags"] != 7).sum()))  # pass 1: all but region 7
+    ctx.sync()                              # raises PG_ERR_NUMERIC on a non-finite parameter
+    s1 = ctx.states(R)
+    K = 8
+    for f in ("weight", "mu_x", "mu_y", "mu_z", "kappa"):
+        assert np.isfinite(s1[f][:, :K]).all(), f
+    assert (s1["total_num_samples"][4:7] > 0).all()
+    for f in s0.dtype.names:                 # region 7 untouched
+        np.testing.assert_array_equal(s1[f][7], s0[f][7])
+    # the later-first region matches a fresh fit (continue mode) of its samples
+    want, _ = oracle.fit(cfg, *_dirw_offsets(oracle, rec[(rec["flags"] >= 4) & (rec["flags"] < 7)], 3, s0, R),
+                         mode=abi.PG_FIT_UPDATE)
+    assert_params_close(s1[4:7], want[4:7], K, GPU_TOL, want["iters_last"][4:7] > 0)
+    ctx.close()
+
+
+def _dirw_offsets(oracle, rec, split_count, states, R):
+    """Oracle inputs of one update pass: bucketed float4 samples seen from the
+    region centres (the first pass of these regions: no reposition)."""
+    srt, off = oracle.sort_samples(rec, R)
+    boxes = oracle.region_aabbs(split_count, np.array([-1.0, -1.0, -1.0, 1.0, 1.0, 1.0], dtype=np.float32))
+    means = boxes[:, :3] + np.float32(0.5) * (boxes[:, 3:] - boxes[:, :3])
+    dirw, _ = oracle.prefit_parallax(srt, off, means)
+    return dirw, off, states

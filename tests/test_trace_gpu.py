@@ -275,3 +275,32 @@ def test_render_instrumentation(cuda, pkg, abi):
                         "advance": spp * depth, "commit": 0}
     ms = dict(zip(abi.STAGES, st.stage_ms))
     assert all(ms[k] > 0 for k in ("camera", "extend", "shade", "shadow"))
+
+
+def test_guided_sequence_accumulates_and_is_unbiased(cuda, pkg, abi):
+    """The headless training loop (SampleCollector, PathGuiding::update per
+    pass, guided render) sums every pass into the image; its mean matches a
+    plain render's and no pixel is non-finite."""
+    import __graft_entry__ as entry
+    G = entry.load_submodule("guiding")
+    torch = cuda
+    sc = pkg.Scene.plates(96, 54, occluder_grid=48, seed=2)
+    W, H = 96, 54
+    pg = G.PathGuiding(8, sc.get_scene_size())
+    col = G.SampleCollector(pg.get_region_count(), W, H)
+    img = torch.zeros(W * H * 3, dtype=torch.float32, device="cuda")
+    tm = G.guided_sequence(sc, pg, col, img, train_spp=(1, 2, 4, 8, 16, 32), final_spp=512, max_depth=10, seed=3)
+    assert tm["spp"] == 63 + 512 and tm["total_ms"] > tm["train_ms"] > 0
+    g = img.cpu().numpy().reshape(H, W, 3) / tm["spp"]
+    assert np.isfinite(g).all()
+    plain, _ = render_gpu(torch, sc, abi.render_params(spp=1024, max_depth=10, seed=77))
+    plain /= 1024
+    assert abs(g.mean() - plain.mean()) / plain.mean() < 0.03
+    st = pg.ctx.states(pg.get_region_count())
+    assert (st["total_num_samples"] > 0).any()
+    for f in ("weight", "mu_x", "kappa"):
+        assert np.isfinite(st[f][:, :8]).all(), f
+    rec, offsets = col.get_sorted_data(pg)
+    assert offsets.shape == (pg.get_region_count() + 1,) and offsets[-1] == rec.shape[0]
+    assert (np.diff(rec["flags"].astype(np.int64)) >= 0).all()
+    pg.close()
