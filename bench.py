@@ -291,12 +291,22 @@ GUIDED_WORKLOAD = ("guided PT, multi-light glossy scene: 4 GGX plates (roughness
                    "(12 splits), 8-component parallax-aware mixtures")
 
 
-def bench_guided(pkg, abi, torch, stream, ref_spp: int = 4096):
+GUIDED_CORNELL_WORKLOAD = ("guided PT on the Cornell box of the tracer workload (1280x720, depth 10): the same 6 "
+                           "training passes of 1-32 spp and 64-spp guided render, all accumulated; 4096 regions "
+                           "(12 splits), 8-component parallax-aware mixtures")
+
+
+def bench_guided(pkg, abi, torch, stream, ref_spp: int = 4096, scene: str = "plates"):
     """Equal-time relMSE of guided and plain NEE+MIS path tracing against a
     high-spp plain render (relMSE = mean (x - r)^2 / (r^2 + 1e-2))."""
     import __graft_entry__ as entry
     G = entry.load_submodule("guiding")
-    sc = pkg.Scene.plates(1920, 1080, occluder_grid=707, seed=4)
+    if scene == "plates":
+        sc = pkg.Scene.plates(1920, 1080, occluder_grid=707, seed=4)
+        workload = GUIDED_WORKLOAD
+    else:
+        sc = pkg.Scene.cornell(1280, 720, ico_level=5)
+        workload = GUIDED_CORNELL_WORKLOAD
     info = sc.info()
     W, H = info.camera.width, info.camera.height
     P = W * H
@@ -336,7 +346,7 @@ def bench_guided(pkg, abi, torch, stream, ref_spp: int = 4096):
     eq_spp = max(1, int(64 * tm["total_ms"] / p64_ms))
     peq, peq_ms = plain(eq_spp, 9000)
     out = {"metric": "equal-time relMSE, guided vs plain NEE+MIS PT", "unit": "relMSE", "higher_is_better": False,
-           "config": {"workload": GUIDED_WORKLOAD, "triangles": info.n_triangles,
+           "config": {"workload": workload, "triangles": info.n_triangles,
                       "reference": f"plain NEE+MIS, {ref_spp} spp ({ref_ms / 1e3:.1f} s)", "relmse_eps": 1e-2},
            "guided": {"relmse": G.relmse(guided, ref), "ms": tm["total_ms"], "train_ms": tm["train_ms"],
                       "final_render_ms": tm["render_ms"], "spp": tm["spp"]},
@@ -399,6 +409,7 @@ def main():
                                     cpu=rank == 0 and not args.no_cpu_baseline)
             else:
                 line = bench_guided(pkg, abi, torch, stream)
+                line["cornell"] = bench_guided(pkg, abi, torch, stream, scene="cornell")
         line.update(n_gpus=world, scaling="weak", vs_baseline=None, data="synthetic (procedural scene)",
                     clocks=sampler.summary())
         if rank == 0:
@@ -528,6 +539,7 @@ def main():
         gsampler = ClockSampler(local)
         with gsampler:
             gd = bench_guided(pkg, abi, torch, stream)
+            gd["cornell"] = bench_guided(pkg, abi, torch, stream, scene="cornell")
         gd["clocks"] = gsampler.summary()
         line["guided"] = gd
     if rank == 0:

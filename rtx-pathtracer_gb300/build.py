@@ -1,8 +1,10 @@
-"""In-tree build of libpathguide.so (CUDA kernels + C ABI + C++ host facades).
+"""In-tree build of libpathguide.so (CUDA kernels + C ABI + C++ host code)
+and of the C++ programs in app/.
 
 Every CUDA translation unit is compiled for sm_103a only, in parallel, then
-linked into one shared library next to this file.  The C++ host facades
-(host/*.cpp) are compiled with g++ and linked into the same library.
+linked into one shared library next to this file.  The host scene code
+(host/*.cpp) is compiled with g++ and linked into the same library; app/*.cpp
+(drivers over include/pathguiding.hpp) become executables next to it.
 """
 from __future__ import annotations
 
@@ -17,6 +19,7 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent
 CSRC = HERE / "csrc"
 HOST = HERE / "host"
+APP = HERE / "app"
 BUILD = HERE / "_build"
 LIB = HERE / "libpathguide.so"
 
@@ -64,6 +67,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
                     sys.stderr.write(" ".join(cmd) + "\n" + out)
                 if rc != 0:
                     raise RuntimeError(f"compile failed: {cmd[-3]}")
+    relinked = False
     if force or jobs or not LIB.exists():
         cmd = [NVCC] + ARCH + ["-shared", "-o", str(LIB)] + [str(o) for o in objs] + \
             ["-lcudart", "-lstdc++"]
@@ -71,7 +75,29 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         if rc != 0:
             sys.stderr.write(" ".join(cmd) + "\n" + out)
             raise RuntimeError("link of libpathguide.so failed")
+        relinked = True
+    build_apps(force or relinked, newest_header)
     return LIB
+
+
+def build_apps(force: bool, newest_header: float) -> list[Path]:
+    """C++ programs over the facades (app/*.cpp), linked against the library
+    with an $ORIGIN run path so they run from the package directory."""
+    bins = []
+    for src in sorted(APP.glob("*.cpp")) if APP.exists() else []:
+        exe = HERE / src.stem
+        bins.append(exe)
+        hpp = ROOT / "include" / "pathguiding.hpp"
+        deps = max(src.stat().st_mtime, newest_header, hpp.stat().st_mtime if hpp.exists() else 0.0)
+        if not force and exe.exists() and exe.stat().st_mtime >= deps:
+            continue
+        cmd = [NVCC, "-O2", "-std=c++17", f"-I{ROOT / 'include'}", str(src), "-o", str(exe), f"-L{HERE}",
+               "-lpathguide", "-Xlinker", "-rpath", "-Xlinker", "$ORIGIN"]
+        cmd, rc, out = _compile(cmd)
+        if rc != 0:
+            sys.stderr.write(" ".join(cmd) + "\n" + out)
+            raise RuntimeError(f"build of {src.name} failed")
+    return bins
 
 
 if __name__ == "__main__":
