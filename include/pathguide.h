@@ -457,6 +457,59 @@ int pg_render(pg_scene *scene, const pg_render_params *params, pg_ctx *guide, fl
 int pg_fit_regions_noalloc(const pg_fit_config *cfg, pg_region_state *states, const float *dirw,
                            const uint32_t *offsets, uint32_t n_regions, int mode, void *stream);
 
+/* ------------------------------------------------------------------ */
+/* Learned guiding surrogate                                           */
+/* ------------------------------------------------------------------ */
+
+/* No counterpart in the reference (it fits one mixture per region,
+ * src/PathGuiding.cpp:350-368).  A small MLP maps a position to a
+ * 16-component vMF mixture: Fourier features of the position in the scene box
+ * (16 octaves per axis, 112 inputs), three hidden layers of 64 ReLU units,
+ * 80 outputs (per component: weight logit, mean direction, log kappa).  BF16
+ * weights and activations on the tensor cores, FP32 accumulation, FP32 master
+ * weights and Adam.  Trained on the tracer's guiding records by maximising
+ * their weighted log-likelihood; the per-region EM fit stays the fallback and
+ * the judge of its KL error.  Parameters are one float vector of
+ * PG_MLP_PARAMS values: W1 (64 x 112), b1, W2 (64 x 64), b2, W3 (64 x 64), b3,
+ * W4 (80 x 64), b4, matrices row-major with one row per output unit. */
+#define PG_MLP_PARAMS 20752u
+#define PG_MLP_COMPONENTS 16u
+
+typedef struct pg_mlp pg_mlp;
+
+typedef struct pg_mlp_config {
+    uint32_t batch;       /* samples per Adam step (e.g. 65536) */
+    float lr;             /* 1e-3 */
+    float beta1, beta2, eps;
+    uint32_t seed;        /* initial weights */
+    float scene_aabb[6];  /* positions are encoded relative to this box */
+} pg_mlp_config;
+
+void pg_mlp_default_config(pg_mlp_config *out);
+int pg_mlp_create(const pg_mlp_config *cfg, pg_mlp **out);
+int pg_mlp_destroy(pg_mlp *mlp);
+/* Host copies of the FP32 master parameters (PG_MLP_PARAMS floats); setting
+ * them also resets Adam's moments and step count. */
+int pg_mlp_get_params(pg_mlp *mlp, float *host_out);
+int pg_mlp_set_params(pg_mlp *mlp, const float *host_in);
+/* Weighted NLL of n records (device) under the current network, and its
+ * gradient (device, PG_MLP_PARAMS floats; may be NULL) - no update.  Records
+ * flagged PG_INVALID_REGION carry no weight.  *loss_out is written after a
+ * stream synchronisation. */
+int pg_mlp_loss_grad(pg_mlp *mlp, const pg_directional_data *records, uint32_t n, float *grad_out, float *loss_out,
+                     void *stream);
+/* One training pass: the records in batches of cfg.batch, one Adam step per
+ * batch.  loss_out (host, may be NULL) receives the mean batch loss, read
+ * after a stream synchronisation. */
+int pg_mlp_train(pg_mlp *mlp, const pg_directional_data *records, uint64_t n, float *loss_out, void *stream);
+/* Mixture parameters at n positions (device, 3 floats each): per position 16
+ * components of {weight, mu x, mu y, mu z, kappa} (80 floats, device). */
+int pg_mlp_infer(pg_mlp *mlp, const float *positions, uint32_t n, float *mixtures_out, void *stream);
+/* Evaluates the network at the centres of the regions of a guiding context
+ * (after pg_set_regions) and installs the mixtures as the context's packed
+ * guide, so pg_render guides with the network (no parallax re-aiming). */
+int pg_mlp_write_guide(pg_mlp *mlp, pg_ctx *guide, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -49,6 +49,15 @@ SIGNATURES = {
     "pg_sync_status": (_I, [_P, _P]),
     "pg_last_launch_count": (_I, [_P, C.POINTER(_U32)]),
     "pg_fit_regions_noalloc": (_I, [C.POINTER(abi.FitConfig), _P, _P, _P, _U32, _I, _P]),
+    "pg_mlp_default_config": (None, [C.POINTER(abi.MlpConfig)]),
+    "pg_mlp_create": (_I, [C.POINTER(abi.MlpConfig), C.POINTER(_P)]),
+    "pg_mlp_destroy": (_I, [_P]),
+    "pg_mlp_get_params": (_I, [_P, _P]),
+    "pg_mlp_set_params": (_I, [_P, _P]),
+    "pg_mlp_loss_grad": (_I, [_P, _P, _U32, _P, C.POINTER(C.c_float), _P]),
+    "pg_mlp_train": (_I, [_P, _P, _U64, C.POINTER(C.c_float), _P]),
+    "pg_mlp_infer": (_I, [_P, _P, _U32, _P, _P]),
+    "pg_mlp_write_guide": (_I, [_P, _P, _P]),
     "pg_set_regions": (_I, [_P, _U32, _P, _P]),
     "pg_region_count": (_I, [_P, C.POINTER(_U32)]),
     "pg_get_region_aabbs": (_I, [_P, _P, _U32]),
@@ -222,6 +231,70 @@ class FitContext:
         n = C.c_uint32()
         self._check(self.lib.pg_last_launch_count(self.h, C.byref(n)))
         return int(n.value)
+
+
+class Surrogate:
+    """The learned guiding surrogate (pg_mlp_*): position -> 16-component vMF
+    mixture, trained on guiding records with BF16 tensor-core kernels."""
+
+    def __init__(self, scene_aabb, batch: int = 65536, lr: float = 1e-3, seed: int = 1):
+        self.lib = library()
+        cfg = abi.MlpConfig()
+        self.lib.pg_mlp_default_config(C.byref(cfg))
+        cfg.batch, cfg.lr, cfg.seed = batch, lr, seed
+        for i, v in enumerate(scene_aabb):
+            cfg.scene_aabb[i] = float(v)
+        self.cfg = cfg
+        h = C.c_void_p()
+        st = self.lib.pg_mlp_create(C.byref(cfg), C.byref(h))
+        if st != abi.PG_OK:
+            raise PathGuideError(st, self.lib.pg_last_error(None).decode())
+        self.h = h
+
+    def _check(self, st):
+        if st != abi.PG_OK:
+            raise PathGuideError(st, self.lib.pg_last_error(None).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pg_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(abi.MLP_PARAMS, dtype=np.float32)
+        self._check(self.lib.pg_mlp_get_params(self.h, out.ctypes.data))
+        return out
+
+    def set_params(self, theta):
+        a = np.ascontiguousarray(theta, dtype=np.float32)
+        assert a.size == abi.MLP_PARAMS
+        self._check(self.lib.pg_mlp_set_params(self.h, a.ctypes.data))
+
+    def loss_grad(self, records_dev, n: int, grad_dev=None, stream=None) -> float:
+        loss = C.c_float()
+        self._check(self.lib.pg_mlp_loss_grad(self.h, _dptr(records_dev), n,
+                                              _dptr(grad_dev) if grad_dev is not None else None, C.byref(loss),
+                                              _stream_handle(stream)))
+        return float(loss.value)
+
+    def train(self, records_dev, n: int, stream=None, want_loss: bool = True):
+        loss = C.c_float()
+        self._check(self.lib.pg_mlp_train(self.h, _dptr(records_dev), n, C.byref(loss) if want_loss else None,
+                                          _stream_handle(stream)))
+        return float(loss.value) if want_loss else None
+
+    def infer(self, positions_dev, n: int, mixtures_dev, stream=None):
+        self._check(self.lib.pg_mlp_infer(self.h, _dptr(positions_dev), n, _dptr(mixtures_dev),
+                                          _stream_handle(stream)))
+
+    def write_guide(self, ctx: FitContext, stream=None):
+        self._check(self.lib.pg_mlp_write_guide(self.h, ctx.h, _stream_handle(stream)))
 
 
 NOALLOC_MAX_REGIONS = 65536

@@ -101,6 +101,15 @@ class PlatesParams(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("occluder_grid", C.c_uint32), ("seed", C.c_uint32)]
 
 
+class MlpConfig(C.Structure):
+    _fields_ = [("batch", C.c_uint32), ("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float),
+                ("eps", C.c_float), ("seed", C.c_uint32), ("scene_aabb", C.c_float * 6)]
+
+
+MLP_PARAMS = 20752
+MLP_COMPONENTS = 16
+
+
 class SceneInfo(C.Structure):
     _fields_ = [("n_triangles", C.c_uint32), ("n_spheres", C.c_uint32), ("n_materials", C.c_uint32),
                 ("n_nodes", C.c_uint32), ("n_lights", C.c_uint32), ("aabb", C.c_float * 6), ("camera", Camera)]

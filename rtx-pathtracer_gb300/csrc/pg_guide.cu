@@ -587,6 +587,17 @@ static int sort_records(pg_ctx *ctx, const pg_directional_data *rec, uint64_t n,
 }
 
 namespace pg {
+int guide_target(pg_ctx *ctx, GuideTarget *out) {
+    GuideScratch &g = guide(ctx);
+    if (!g.aabbs || !g.vmm || g.n_regions == 0) return set_error(ctx, PG_ERR_STATE, "pg_set_regions must run first");
+    out->aabbs = g.aabbs;
+    out->n_regions = g.n_regions;
+    out->vmm = g.vmm;
+    return PG_OK;
+}
+
+void guide_mark_written(pg_ctx *ctx) { guide(ctx).vmm_fresh = true; }
+
 int guide_view(pg_ctx *ctx, GuideView *out, cudaStream_t s) {
     GuideScratch &g = guide(ctx);
     if (!g.aabbs || !g.vmm) return set_error(ctx, PG_ERR_STATE, "pg_set_regions must run before guided rendering");

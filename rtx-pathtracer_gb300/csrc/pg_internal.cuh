@@ -55,6 +55,16 @@ struct GuideView {
     int use_parallax;
 };
 int guide_view(pg_ctx *ctx, GuideView *out, cudaStream_t s);
+// The packed-guide buffer and region boxes of a context, for guides computed
+// elsewhere (the learned surrogate); guide_mark_written keeps what was written
+// until the next pg_update or pg_set_regions.
+struct GuideTarget {
+    const float *aabbs;
+    uint32_t n_regions;
+    pg_vmm_theta *vmm;
+};
+int guide_target(pg_ctx *ctx, GuideTarget *out);
+void guide_mark_written(pg_ctx *ctx);
 
 constexpr float kLog2e = 1.4426950408889634f;
 constexpr float kLn2 = 0.6931471805599453f;

@@ -1,0 +1,897 @@
+// pg_mlp.cu - the learned guiding surrogate: a position -> vMF-mixture MLP
+// trained on the tracer's guiding records, BF16 on the tensor cores with FP32
+// accumulation (mma.sync m16n8k16), FP32 master weights and Adam.
+//
+// Model (restated in FP64 by oracle/mlp_oracle.py):
+//   x = (p - lo) / (hi - lo); 112 inputs: sin/cos(2^k pi x_d) pairs for
+//   k < 16 and the three axes (columns 2i, 2i+1 with d = i % 3, k = i / 3),
+//   x at columns 96..98, zeros after; h1..h3 = relu(W h + b) with 64 units;
+//   80 outputs = 16 components x {logit, m_x, m_y, m_z, log kappa};
+//   q(d) = sum_j softmax(logit)_j vMF(d; m_j / |m_j|, exp(clamp(s_j)))
+//   loss = sum_i w_i (-log q(d_i)) / sum_i w_i.
+//
+// One training step over a batch of B records:
+//   k_fwd_bwd   one warp per 16 records: encoding, four layers, loss and its
+//               output gradient, back through the layers; activations and
+//               gradients go to a BF16 scratch (B x 1152 bytes, L2-resident
+//               for B = 65536)
+//   k_wgrad     weight gradients dW = D^T X as tensor-core GEMMs over the
+//               batch (split over row blocks, one layer per grid row), bias
+//               gradients by column sums; per-block partials
+//   k_sum_scalars, k_reduce_adam
+//               partials -> gradient / sum(w) -> Adam -> FP32 masters and the
+//               BF16 weight copy the next step reads.
+#include <cuda_bf16.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <vector>
+
+#include "pg_internal.cuh"
+
+namespace pg {
+namespace mlp {
+
+constexpr int NIN = 112, NH = 64, NOUT = 80, NC = 16;
+constexpr int SIN = NIN + 8, SH = NH + 8;  // padded shared-memory row strides (bf16 elements)
+constexpr float S_MIN = -4.0f, S_MAX = 9.0f;
+constexpr int OW1 = 0, OB1 = OW1 + NH * NIN, OW2 = OB1 + NH, OB2 = OW2 + NH * NH, OW3 = OB2 + NH,
+              OB3 = OW3 + NH * NH, OW4 = OB3 + NH, OB4 = OW4 + NOUT * NH, NPARAM = OB4 + NOUT;
+static_assert(NPARAM == PG_MLP_PARAMS, "parameter count");
+// bf16 weight copy: W1, W2, W3, W4 back to back (unpadded)
+constexpr int WB1 = 0, WB2 = WB1 + NH * NIN, WB3 = WB2 + NH * NH, WB4 = WB3 + NH * NH, NWB = WB4 + NOUT * NH;
+// scratch row layout (bf16 elements per record)
+constexpr int RA0 = 0, RH1 = RA0 + NIN, RH2 = RH1 + NH, RH3 = RH2 + NH, RDO = RH3 + NH, RD3 = RDO + NOUT,
+              RD2 = RD3 + NH, RD1 = RD2 + NH, RROW = RD1 + NH;  // 576 bf16 = 1152 bytes
+constexpr int kWarps = 4, kRowsPerCta = 16 * kWarps;
+constexpr float kPi = 3.14159265358979323846f;
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+__device__ __forceinline__ uint32_t pack2(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t *>(&v);
+}
+__device__ __forceinline__ uint32_t cat16(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+struct Shared {
+    __nv_bfloat16 w1[NH * SIN];
+    __nv_bfloat16 w2[NH * SH];
+    __nv_bfloat16 w3[NH * SH];
+    __nv_bfloat16 w4[NOUT * SH];
+    float b[NH * 3 + NOUT];
+    float o[kWarps][16][NOUT];
+};
+
+// acc = bias + A W^T for one layer (A: 16 x 16*KC in fragments, W: rows of K).
+template <int KC, int NT>
+__device__ __forceinline__ void layer_fwd(float (&acc)[NT][4], const uint32_t (&a)[KC][4], const __nv_bfloat16 *w,
+                                          int stride, const float *bias, int g, int t) {
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+        const float b0 = bias[8 * nt + 2 * t], b1 = bias[8 * nt + 2 * t + 1];
+        acc[nt][0] = b0;
+        acc[nt][1] = b1;
+        acc[nt][2] = b0;
+        acc[nt][3] = b1;
+    }
+#pragma unroll
+    for (int kc = 0; kc < KC; ++kc)
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) {
+            const __nv_bfloat16 *row = w + (8 * nt + g) * stride + 16 * kc + 2 * t;
+            mma_bf16(acc[nt], a[kc], *reinterpret_cast<const uint32_t *>(row),
+                     *reinterpret_cast<const uint32_t *>(row + 8));
+        }
+}
+
+// acc = A W for the backward pass (A: 16 x 16*KC gradients over the layer's
+// outputs, W: KC*16 rows of 8*NT inputs).
+template <int KC, int NT>
+__device__ __forceinline__ void layer_bwd(float (&acc)[NT][4], const uint32_t (&a)[KC][4], const __nv_bfloat16 *w,
+                                          int stride, int g, int t) {
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+#pragma unroll
+    for (int kc = 0; kc < KC; ++kc)
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) {
+            const int o0 = 16 * kc + 2 * t, i = 8 * nt + g;
+            const uint32_t b0 = cat16(w[o0 * stride + i], w[(o0 + 1) * stride + i]);
+            const uint32_t b1 = cat16(w[(o0 + 8) * stride + i], w[(o0 + 9) * stride + i]);
+            mma_bf16(acc[nt], a[kc], b0, b1);
+        }
+}
+
+// relu (or the relu mask for gradients), then the C fragments as the next
+// MMA's A fragments.
+__device__ __forceinline__ void relu_mask(float (&acc)[8][4], uint32_t &mask) {
+    mask = 0;
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const bool pos = acc[nt][i] > 0.0f;
+            if (!pos) acc[nt][i] = 0.0f;
+            mask |= (pos ? 1u : 0u) << (4 * nt + i);
+        }
+}
+__device__ __forceinline__ void apply_mask(float (&acc)[8][4], uint32_t mask) {
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            if (!((mask >> (4 * nt + i)) & 1u)) acc[nt][i] = 0.0f;
+}
+__device__ __forceinline__ void to_afrag(const float (&acc)[8][4], uint32_t (&a)[4][4]) {
+#pragma unroll
+    for (int kc = 0; kc < 4; ++kc) {
+        a[kc][0] = pack2(acc[2 * kc][0], acc[2 * kc][1]);
+        a[kc][1] = pack2(acc[2 * kc][2], acc[2 * kc][3]);
+        a[kc][2] = pack2(acc[2 * kc + 1][0], acc[2 * kc + 1][1]);
+        a[kc][3] = pack2(acc[2 * kc + 1][2], acc[2 * kc + 1][3]);
+    }
+}
+// A fragments of a 16 x 16*KC tile to rows of the scratch (row stride RROW).
+template <int KC>
+__device__ __forceinline__ void store_afrag(const uint32_t (&a)[KC][4], __nv_bfloat16 *rows, int col0, int g, int t) {
+#pragma unroll
+    for (int kc = 0; kc < KC; ++kc) {
+        const int c = col0 + 16 * kc + 2 * t;
+        *reinterpret_cast<uint32_t *>(rows + (size_t)g * RROW + c) = a[kc][0];
+        *reinterpret_cast<uint32_t *>(rows + (size_t)(g + 8) * RROW + c) = a[kc][1];
+        *reinterpret_cast<uint32_t *>(rows + (size_t)g * RROW + c + 8) = a[kc][2];
+        *reinterpret_cast<uint32_t *>(rows + (size_t)(g + 8) * RROW + c + 8) = a[kc][3];
+    }
+}
+
+// Fourier features of the columns (c, c+1) of one row.
+__device__ __forceinline__ uint32_t enc_pair(const float x[3], int c) {
+    if (c < 96) {
+        const int i = c >> 1, d = i % 3, k = i / 3;
+        float s, co;
+        sincospif(ldexpf(x[d], k), &s, &co);
+        return pack2(s, co);
+    }
+    if (c == 96) return pack2(x[0], x[1]);
+    if (c == 98) return pack2(x[2], 0.0f);
+    return 0u;
+}
+
+struct FwdArgs {
+    const pg_directional_data *rec;  // training records (or NULL for inference)
+    const float *pos;                // inference positions (3 floats each)
+    uint32_t n;
+    float lo[3], inv_ext[3];
+    const __nv_bfloat16 *wb;         // bf16 weights
+    const float *theta;              // fp32 masters (biases are read from here)
+    __nv_bfloat16 *scratch;          // B x RROW (training)
+    float *partials;                 // per-warp {sum w (-log q), sum w} (training)
+    float *mix_out;                  // n x 80 mixture parameters (inference)
+};
+
+// kTrain: loss, gradients and scratch; otherwise mixture parameters.
+template <bool kTrain>
+__global__ void __launch_bounds__(32 * kWarps) k_fwd_bwd(FwdArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Shared &S = *reinterpret_cast<Shared *>(smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+    // weights to shared memory (padded rows)
+    for (int i = tid; i < NH * NIN / 2; i += blockDim.x) {
+        const int r = (2 * i) / NIN, c = (2 * i) % NIN;
+        *reinterpret_cast<uint32_t *>(&S.w1[r * SIN + c]) = reinterpret_cast<const uint32_t *>(A.wb + WB1)[i];
+    }
+    for (int i = tid; i < NH * NH / 2; i += blockDim.x) {
+        const int r = (2 * i) / NH, c = (2 * i) % NH;
+        *reinterpret_cast<uint32_t *>(&S.w2[r * SH + c]) = reinterpret_cast<const uint32_t *>(A.wb + WB2)[i];
+        *reinterpret_cast<uint32_t *>(&S.w3[r * SH + c]) = reinterpret_cast<const uint32_t *>(A.wb + WB3)[i];
+    }
+    for (int i = tid; i < NOUT * NH / 2; i += blockDim.x) {
+        const int r = (2 * i) / NH, c = (2 * i) % NH;
+        *reinterpret_cast<uint32_t *>(&S.w4[r * SH + c]) = reinterpret_cast<const uint32_t *>(A.wb + WB4)[i];
+    }
+    for (int i = tid; i < NH; i += blockDim.x) {
+        S.b[i] = A.theta[OB1 + i];
+        S.b[NH + i] = A.theta[OB2 + i];
+        S.b[2 * NH + i] = A.theta[OB3 + i];
+    }
+    for (int i = tid; i < NOUT; i += blockDim.x) S.b[3 * NH + i] = A.theta[OB4 + i];
+    __syncthreads();
+
+    const uint32_t row0 = blockIdx.x * kRowsPerCta + warp * 16;
+    // positions of this lane's two rows (g, g + 8); rows past n sit at the box corner with no weight
+    float x[2][3];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const uint32_t r = row0 + g + 8 * h;
+        float p[3] = {A.lo[0], A.lo[1], A.lo[2]};
+        if (r < A.n) {
+            if (kTrain) {
+                p[0] = A.rec[r].position[0];
+                p[1] = A.rec[r].position[1];
+                p[2] = A.rec[r].position[2];
+            } else {
+                p[0] = A.pos[3 * (size_t)r];
+                p[1] = A.pos[3 * (size_t)r + 1];
+                p[2] = A.pos[3 * (size_t)r + 2];
+            }
+        }
+        for (int d = 0; d < 3; ++d) x[h][d] = (p[d] - A.lo[d]) * A.inv_ext[d];
+    }
+    // layer 1 inputs: the encoding as A fragments
+    uint32_t a0[7][4];
+#pragma unroll
+    for (int kc = 0; kc < 7; ++kc) {
+        const int c = 16 * kc + 2 * t;
+        a0[kc][0] = enc_pair(x[0], c);
+        a0[kc][1] = enc_pair(x[1], c);
+        a0[kc][2] = enc_pair(x[0], c + 8);
+        a0[kc][3] = enc_pair(x[1], c + 8);
+    }
+    __nv_bfloat16 *rows = kTrain ? A.scratch + (size_t)row0 * RROW : nullptr;
+    if (kTrain) store_afrag<7>(a0, rows, RA0, g, t);
+
+    float acc[8][4];
+    uint32_t m1, m2, m3;
+    uint32_t h[4][4];
+    layer_fwd<7, 8>(acc, a0, S.w1, SIN, S.b, g, t);
+    relu_mask(acc, m1);
+    to_afrag(acc, h);
+    if (kTrain) store_afrag<4>(h, rows, RH1, g, t);
+    layer_fwd<4, 8>(acc, h, S.w2, SH, S.b + NH, g, t);
+    relu_mask(acc, m2);
+    to_afrag(acc, h);
+    if (kTrain) store_afrag<4>(h, rows, RH2, g, t);
+    layer_fwd<4, 8>(acc, h, S.w3, SH, S.b + 2 * NH, g, t);
+    relu_mask(acc, m3);
+    to_afrag(acc, h);
+    if (kTrain) store_afrag<4>(h, rows, RH3, g, t);
+    {
+        float out[10][4];
+        layer_fwd<4, 10>(out, h, S.w4, SH, S.b + 3 * NH, g, t);
+#pragma unroll
+        for (int nt = 0; nt < 10; ++nt) {
+            S.o[warp][g][8 * nt + 2 * t] = out[nt][0];
+            S.o[warp][g][8 * nt + 2 * t + 1] = out[nt][1];
+            S.o[warp][g + 8][8 * nt + 2 * t] = out[nt][2];
+            S.o[warp][g + 8][8 * nt + 2 * t + 1] = out[nt][3];
+        }
+    }
+    __syncwarp();
+
+    // ---- mixture, loss and output gradient: two lanes per row, 8 components each
+    {
+        const int s = lane >> 1, half = lane & 1;
+        const uint32_t r = row0 + s;
+        float* o = S.o[warp][s];
+        float d[3] = {0.0f, 0.0f, 1.0f}, w = 0.0f;
+        if (kTrain && r < A.n) {
+            const pg_directional_data &rc = A.rec[r];
+            d[0] = rc.direction[0];
+            d[1] = rc.direction[1];
+            d[2] = rc.direction[2];
+            w = rc.flags == PG_INVALID_REGION ? 0.0f : rc.weight;
+            if (!(w > 0.0f) || !isfinite(w)) w = 0.0f;
+        }
+        // softmax normaliser of the logits
+        float lmax = -INFINITY;
+        for (int j = 8 * half; j < 8 * half + 8; ++j) lmax = fmaxf(lmax, o[5 * j]);
+        lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, 1));
+        float lsum = 0.0f;
+        for (int j = 8 * half; j < 8 * half + 8; ++j) lsum += expf(o[5 * j] - lmax);
+        lsum += __shfl_xor_sync(0xffffffffu, lsum, 1);
+        const float lse = lmax + logf(lsum);
+        float lp[8], kap[8], cs[8], mn[8], mu[8][3], sraw[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int j = 8 * half + q;
+            const float mx = o[5 * j + 1], my = o[5 * j + 2], mz = o[5 * j + 3];
+            mn[q] = sqrtf(mx * mx + my * my + mz * mz);
+            const float inv = mn[q] > 0.0f ? 1.0f / mn[q] : 0.0f;
+            mu[q][0] = mx * inv;
+            mu[q][1] = my * inv;
+            mu[q][2] = mz * inv;
+            sraw[q] = o[5 * j + 4];
+            kap[q] = expf(fminf(fmaxf(sraw[q], S_MIN), S_MAX));
+            cs[q] = mu[q][0] * d[0] + mu[q][1] * d[1] + mu[q][2] * d[2];
+            const float lognorm = logf(kap[q]) - logf(2.0f * kPi) - logf(-expm1f(-2.0f * kap[q]));
+            lp[q] = (o[5 * j] - lse) + lognorm + kap[q] * (cs[q] - 1.0f);
+        }
+        if (!kTrain) {
+            if (r < A.n) {
+                float *mo = A.mix_out + (size_t)r * NOUT;
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const int j = 8 * half + q;
+                    mo[5 * j] = expf(o[5 * j] - lse);
+                    mo[5 * j + 1] = mu[q][0];
+                    mo[5 * j + 2] = mu[q][1];
+                    mo[5 * j + 3] = mu[q][2];
+                    mo[5 * j + 4] = kap[q];
+                }
+            }
+        } else {
+            float qmax = -INFINITY;
+            for (int q = 0; q < 8; ++q) qmax = fmaxf(qmax, lp[q]);
+            qmax = fmaxf(qmax, __shfl_xor_sync(0xffffffffu, qmax, 1));
+            float qs = 0.0f;
+            for (int q = 0; q < 8; ++q) qs += expf(lp[q] - qmax);
+            qs += __shfl_xor_sync(0xffffffffu, qs, 1);
+            const float logq = qmax + logf(qs);
+            __syncwarp();
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int j = 8 * half + q;
+                const float rr = expf(lp[q] - logq);  // responsibility
+                const float pi = expf(o[5 * j] - lse);
+                const float k = kap[q];
+                const float f = mn[q] > 0.0f ? -w * rr * k / mn[q] : 0.0f;
+                o[5 * j] = w * (pi - rr);
+                o[5 * j + 1] = f * (d[0] - cs[q] * mu[q][0]);
+                o[5 * j + 2] = f * (d[1] - cs[q] * mu[q][1]);
+                o[5 * j + 3] = f * (d[2] - cs[q] * mu[q][2]);
+                const bool inside = sraw[q] > S_MIN && sraw[q] < S_MAX;
+                const float e = expf(-2.0f * k);
+                const float tt = 2.0f * k * e / -expm1f(-2.0f * k);
+                o[5 * j + 4] = inside ? -w * rr * (1.0f - tt + k * (cs[q] - 1.0f)) : 0.0f;
+            }
+            // loss partials: one lane per row
+            float lw = half == 0 ? w * -logq : 0.0f, ww = half == 0 ? w : 0.0f;
+            if (w == 0.0f) lw = 0.0f;
+            for (int off = 16; off > 0; off >>= 1) {
+                lw += __shfl_xor_sync(0xffffffffu, lw, off);
+                ww += __shfl_xor_sync(0xffffffffu, ww, off);
+            }
+            if (lane == 0) {  // one slot per warp: the sums are deterministic
+                A.partials[2 * (blockIdx.x * kWarps + warp)] = lw;
+                A.partials[2 * (blockIdx.x * kWarps + warp) + 1] = ww;
+            }
+        }
+    }
+    if (!kTrain) return;
+    __syncwarp();
+
+    // ---- backward through the layers
+    uint32_t dof[5][4];
+#pragma unroll
+    for (int kc = 0; kc < 5; ++kc) {
+        const int c = 16 * kc + 2 * t;
+        dof[kc][0] = pack2(S.o[warp][g][c], S.o[warp][g][c + 1]);
+        dof[kc][1] = pack2(S.o[warp][g + 8][c], S.o[warp][g + 8][c + 1]);
+        dof[kc][2] = pack2(S.o[warp][g][c + 8], S.o[warp][g][c + 9]);
+        dof[kc][3] = pack2(S.o[warp][g + 8][c + 8], S.o[warp][g + 8][c + 9]);
+    }
+    store_afrag<5>(dof, rows, RDO, g, t);
+    layer_bwd<5, 8>(acc, dof, S.w4, SH, g, t);
+    apply_mask(acc, m3);
+    to_afrag(acc, h);
+    store_afrag<4>(h, rows, RD3, g, t);
+    layer_bwd<4, 8>(acc, h, S.w3, SH, g, t);
+    apply_mask(acc, m2);
+    to_afrag(acc, h);
+    store_afrag<4>(h, rows, RD2, g, t);
+    layer_bwd<4, 8>(acc, h, S.w2, SH, g, t);
+    apply_mask(acc, m1);
+    to_afrag(acc, h);
+    store_afrag<4>(h, rows, RD1, g, t);
+}
+
+// Weight gradients of one layer (blockIdx.y) over a block of rows:
+// dW[o][i] = sum_r D[r][o] X[r][i] on the tensor cores (M = outputs,
+// N = inputs, K = rows), db[o] = sum_r D[r][o].  Partials per row block.
+struct WgradArgs {
+    const __nv_bfloat16 *scratch;
+    uint32_t rows;        // padded batch rows (multiple of 16)
+    uint32_t rows_per_block;
+    float *partials;      // gridDim.x x NPARAM
+};
+
+template <int O, int I>
+__device__ __forceinline__ void wgrad_layer(const WgradArgs &A, int dcol, int xcol, int wofs, int bofs) {
+    constexpr int MT = O / 16, NT = I / 8;
+    constexpr int MT_PER_WARP = (MT + kWarps - 1) / kWarps;
+    __shared__ __align__(16) __nv_bfloat16 sd[16][NOUT + 8];
+    __shared__ __align__(16) __nv_bfloat16 sx[16][NIN + 8];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+    float acc[MT_PER_WARP][NT][4];
+#pragma unroll
+    for (int m = 0; m < MT_PER_WARP; ++m)
+#pragma unroll
+        for (int n = 0; n < NT; ++n) acc[m][n][0] = acc[m][n][1] = acc[m][n][2] = acc[m][n][3] = 0.0f;
+    float bacc = 0.0f;
+    const uint32_t r0 = blockIdx.x * A.rows_per_block;
+    const uint32_t r1 = min(A.rows, r0 + A.rows_per_block);
+    for (uint32_t rb = r0; rb < r1; rb += 16) {
+        __syncthreads();
+        for (int i = tid; i < 16 * O / 2; i += blockDim.x) {
+            const int r = (2 * i) / O, c = (2 * i) % O;
+            *reinterpret_cast<uint32_t *>(&sd[r][c]) =
+                *reinterpret_cast<const uint32_t *>(A.scratch + (size_t)(rb + r) * RROW + dcol + c);
+        }
+        for (int i = tid; i < 16 * I / 2; i += blockDim.x) {
+            const int r = (2 * i) / I, c = (2 * i) % I;
+            *reinterpret_cast<uint32_t *>(&sx[r][c]) =
+                *reinterpret_cast<const uint32_t *>(A.scratch + (size_t)(rb + r) * RROW + xcol + c);
+        }
+        __syncthreads();
+        if (tid < O)
+            for (int r = 0; r < 16; ++r) bacc += __bfloat162float(sd[r][tid]);
+#pragma unroll
+        for (int m = 0; m < MT_PER_WARP; ++m) {
+            const int mt = warp + kWarps * m;
+            if (mt >= MT) break;
+            // A = D^T: rows o, columns r
+            uint32_t a[4];
+            const int o = 16 * mt + g;
+            a[0] = cat16(sd[2 * t][o], sd[2 * t + 1][o]);
+            a[1] = cat16(sd[2 * t][o + 8], sd[2 * t + 1][o + 8]);
+            a[2] = cat16(sd[2 * t + 8][o], sd[2 * t + 9][o]);
+            a[3] = cat16(sd[2 * t + 8][o + 8], sd[2 * t + 9][o + 8]);
+#pragma unroll
+            for (int n = 0; n < NT; ++n) {
+                const int i = 8 * n + g;
+                const uint32_t b0 = cat16(sx[2 * t][i], sx[2 * t + 1][i]);
+                const uint32_t b1 = cat16(sx[2 * t + 8][i], sx[2 * t + 9][i]);
+                mma_bf16(acc[m][n], a, b0, b1);
+            }
+        }
+    }
+    float *out = A.partials + (size_t)blockIdx.x * NPARAM;
+#pragma unroll
+    for (int m = 0; m < MT_PER_WARP; ++m) {
+        const int mt = warp + kWarps * m;
+        if (mt >= MT) break;
+#pragma unroll
+        for (int n = 0; n < NT; ++n) {
+            const int o = 16 * mt + g, i = 8 * n + 2 * t;
+            out[wofs + o * I + i] = acc[m][n][0];
+            out[wofs + o * I + i + 1] = acc[m][n][1];
+            out[wofs + (o + 8) * I + i] = acc[m][n][2];
+            out[wofs + (o + 8) * I + i + 1] = acc[m][n][3];
+        }
+    }
+    if (tid < O) out[bofs + tid] = bacc;
+}
+
+__global__ void __launch_bounds__(32 * kWarps) k_wgrad(WgradArgs A) {
+    switch (blockIdx.y) {
+        case 0: wgrad_layer<NH, NIN>(A, RD1, RA0, OW1, OB1); break;
+        case 1: wgrad_layer<NH, NH>(A, RD2, RH1, OW2, OB2); break;
+        case 2: wgrad_layer<NH, NH>(A, RD3, RH2, OW3, OB3); break;
+        default: wgrad_layer<NOUT, NH>(A, RDO, RH3, OW4, OB4); break;
+    }
+}
+
+// sums of the forward kernel's per-CTA {loss, weight} partials (one block)
+__global__ void k_sum_scalars(const float *partials, uint32_t n, double *out) {
+    __shared__ double sl[256], sw[256];
+    double l = 0.0, w = 0.0;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        l += partials[2 * i];
+        w += partials[2 * i + 1];
+    }
+    sl[threadIdx.x] = l;
+    sw[threadIdx.x] = w;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) {
+            sl[threadIdx.x] += sl[threadIdx.x + s];
+            sw[threadIdx.x] += sw[threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = sl[0];
+        out[1] = sw[0];
+    }
+}
+
+struct AdamArgs {
+    const float *partials;
+    uint32_t n_blocks;
+    const double *scalars;   // {sum w (-log q), sum w}
+    float *theta, *m, *v;
+    __nv_bfloat16 *wb;
+    float *grad_out;         // gradient only (no update) when not null
+    float lr, b1, b2, eps, c1, c2;  // c1 = 1 - b1^t, c2 = 1 - b2^t
+};
+
+__device__ __forceinline__ int wb_index(int p) {
+    if (p < OB1) return WB1 + (p - OW1);
+    if (p >= OW2 && p < OB2) return WB2 + (p - OW2);
+    if (p >= OW3 && p < OB3) return WB3 + (p - OW3);
+    if (p >= OW4 && p < OB4) return WB4 + (p - OW4);
+    return -1;
+}
+
+__global__ void k_reduce_adam(AdamArgs A) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= NPARAM) return;
+    float s = 0.0f, c = 0.0f;
+    for (uint32_t b = 0; b < A.n_blocks; ++b) neumaier_add(s, c, A.partials[(size_t)b * NPARAM + p]);
+    const double W = A.scalars[1];
+    const float gr = W > 0.0 ? (float)((double)(s + c) / W) : 0.0f;
+    if (A.grad_out) {
+        A.grad_out[p] = gr;
+        return;
+    }
+    const float m = A.b1 * A.m[p] + (1.0f - A.b1) * gr;
+    const float v = A.b2 * A.v[p] + (1.0f - A.b2) * gr * gr;
+    A.m[p] = m;
+    A.v[p] = v;
+    const float th = A.theta[p] - A.lr * (m / A.c1) / (sqrtf(v / A.c2) + A.eps);
+    A.theta[p] = th;
+    const int wi = wb_index(p);
+    if (wi >= 0) A.wb[wi] = __float2bfloat16_rn(th);
+}
+
+__global__ void k_theta_to_wb(const float *theta, __nv_bfloat16 *wb) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= NPARAM) return;
+    const int wi = wb_index(p);
+    if (wi >= 0) wb[wi] = __float2bfloat16_rn(theta[p]);
+}
+
+// centres of the guide's region boxes
+__global__ void k_region_centres(const float *aabbs, uint32_t n, float *pos) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    for (int i = 0; i < 3; ++i) pos[3 * r + i] = aabbs[6 * r + i] + 0.5f * (aabbs[6 * r + 3 + i] - aabbs[6 * r + i]);
+}
+
+// mixtures -> VMM_Theta (setK of guiding.glsl:23-30: norm and e^{-2k} from k)
+__global__ void k_pack_guide(const float *mix, const float *pos, uint32_t n, pg_vmm_theta *out) {
+    const uint32_t r = blockIdx.x;
+    const int j = threadIdx.x;
+    if (r >= n || j >= NC) return;
+    const float *m = mix + (size_t)r * NOUT + 5 * j;
+    pg_vmm_theta *v = out + r;
+    pg_vmf_theta th;
+    th.mu[0] = m[1];
+    th.mu[1] = m[2];
+    th.mu[2] = m[3];
+    float k = m[4];
+    k = k < kVmfMinKappa ? 0.0f : k;
+    th.k = k;
+    const double kd = (double)k;
+    th.norm = k > 0.0f ? (float)(kd / (2.0 * 3.14159265358979323846 * (1.0 - exp(-2.0 * kd)))) : 0.0f;
+    th.e_min2k = (float)exp(-2.0 * kd);
+    th.distance = -1.0f;
+    th.target[0] = th.target[1] = th.target[2] = 0.0f;
+    v->thetas[j] = th;
+    v->pi[j] = m[0];
+    if (j == 0) {
+        v->mean_position[0] = pos[3 * r];
+        v->mean_position[1] = pos[3 * r + 1];
+        v->mean_position[2] = pos[3 * r + 2];
+        v->used_distributions = NC;
+    }
+}
+
+}  // namespace mlp
+}  // namespace pg
+
+using namespace pg;
+using namespace pg::mlp;
+
+struct pg_mlp {
+    pg_mlp_config cfg{};
+    int sm_count = 0;
+    float *theta = nullptr, *m = nullptr, *v = nullptr;
+    __nv_bfloat16 *wb = nullptr;
+    __nv_bfloat16 *scratch = nullptr;
+    float *fwd_partials = nullptr;   // 2 per forward CTA
+    float *wg_partials = nullptr;    // per row block
+    double *scalars = nullptr;       // per batch: {loss sum, weight sum}
+    float *pos = nullptr;            // guide positions
+    float *mix = nullptr;            // guide mixtures
+    uint32_t cap_guide = 0;
+    uint32_t cap_rows = 0;           // padded batch rows
+    uint32_t cap_batches = 0;
+    uint32_t wg_blocks = 0;
+    uint32_t wg_used = 0;            // row blocks of the last weight-gradient launch
+    uint32_t step = 0;
+    size_t smem = 0;
+};
+
+namespace {
+
+int mlp_error(int st, const char *msg) { return set_error(nullptr, st, msg); }
+
+FwdArgs fwd_args(const pg_mlp *M) {
+    FwdArgs A{};
+    for (int i = 0; i < 3; ++i) {
+        A.lo[i] = M->cfg.scene_aabb[i];
+        const float ext = M->cfg.scene_aabb[3 + i] - M->cfg.scene_aabb[i];
+        A.inv_ext[i] = ext > 0.0f ? 1.0f / ext : 0.0f;
+    }
+    A.wb = M->wb;
+    A.theta = M->theta;
+    return A;
+}
+
+// forward + backward + weight gradients of one batch; leaves the partials and
+// the batch's scalars in scalars[2 * slot]
+int batch_gradients(pg_mlp *M, const pg_directional_data *rec, uint32_t n, uint32_t slot, cudaStream_t s) {
+    const uint32_t ctas = (n + kRowsPerCta - 1) / kRowsPerCta;
+    const uint32_t rows = ctas * kRowsPerCta;
+    FwdArgs A = fwd_args(M);
+    A.rec = rec;
+    A.n = n;
+    A.scratch = M->scratch;
+    A.partials = M->fwd_partials;
+    k_fwd_bwd<true><<<ctas, 32 * kWarps, M->smem, s>>>(A);
+    WgradArgs W{};
+    W.scratch = M->scratch;
+    W.rows = rows;
+    const uint32_t blocks = std::min<uint32_t>(M->wg_blocks, (rows + 15) / 16);
+    W.rows_per_block = ((rows / 16 + blocks - 1) / blocks) * 16;
+    const uint32_t used = (rows + W.rows_per_block - 1) / W.rows_per_block;
+    W.partials = M->wg_partials;
+    k_wgrad<<<dim3(used, 4), 32 * kWarps, 0, s>>>(W);
+    k_sum_scalars<<<1, 256, 0, s>>>(M->fwd_partials, ctas * kWarps, M->scalars + 2 * slot);
+    if (cudaGetLastError() != cudaSuccess) return mlp_error(PG_ERR_CUDA, "surrogate gradient launch");
+    M->wg_used = used;
+    return PG_OK;
+}
+
+int reduce_step(pg_mlp *M, uint32_t slot, float *grad_out, cudaStream_t s) {
+    AdamArgs A{};
+    A.partials = M->wg_partials;
+    A.n_blocks = M->wg_used;
+    A.scalars = M->scalars + 2 * slot;
+    A.theta = M->theta;
+    A.m = M->m;
+    A.v = M->v;
+    A.wb = M->wb;
+    A.grad_out = grad_out;
+    if (!grad_out) {
+        M->step += 1;
+        A.lr = M->cfg.lr;
+        A.b1 = M->cfg.beta1;
+        A.b2 = M->cfg.beta2;
+        A.eps = M->cfg.eps;
+        A.c1 = (float)(1.0 - pow((double)M->cfg.beta1, (double)M->step));
+        A.c2 = (float)(1.0 - pow((double)M->cfg.beta2, (double)M->step));
+    }
+    k_reduce_adam<<<(NPARAM + 255) / 256, 256, 0, s>>>(A);
+    return cudaGetLastError() == cudaSuccess ? PG_OK : mlp_error(PG_ERR_CUDA, "surrogate update launch");
+}
+
+// grows the batch scratch to `rows` padded rows and `batches` scalar slots
+int ensure_capacity(pg_mlp *M, uint32_t rows, uint32_t batches) {
+    if (rows > M->cap_rows) {
+        cudaFree(M->scratch);
+        cudaFree(M->fwd_partials);
+        M->scratch = nullptr;
+        M->fwd_partials = nullptr;
+        if (cudaMalloc(&M->scratch, sizeof(__nv_bfloat16) * (size_t)rows * RROW) != cudaSuccess ||
+            cudaMalloc(&M->fwd_partials, sizeof(float) * 2 * (rows / 16)) != cudaSuccess) {
+            M->cap_rows = 0;
+            return mlp_error(PG_ERR_NOMEM, "surrogate batch scratch: out of device memory");
+        }
+        M->cap_rows = rows;
+    }
+    if (batches > M->cap_batches) {
+        cudaFree(M->scalars);
+        M->scalars = nullptr;
+        if (cudaMalloc(&M->scalars, sizeof(double) * 2 * batches) != cudaSuccess) {
+            M->cap_batches = 0;
+            return mlp_error(PG_ERR_NOMEM, "surrogate scalars: out of device memory");
+        }
+        M->cap_batches = batches;
+    }
+    return PG_OK;
+}
+
+uint32_t padded_rows(uint64_t n) { return (uint32_t)(((n + kRowsPerCta - 1) / kRowsPerCta) * kRowsPerCta); }
+
+}  // namespace
+
+extern "C" {
+
+void pg_mlp_default_config(pg_mlp_config *out) {
+    if (!out) return;
+    memset(out, 0, sizeof *out);
+    out->batch = 65536;
+    out->lr = 1e-3f;
+    out->beta1 = 0.9f;
+    out->beta2 = 0.999f;
+    out->eps = 1e-8f;
+    out->seed = 1;
+    for (int i = 0; i < 3; ++i) {
+        out->scene_aabb[i] = 0.0f;
+        out->scene_aabb[3 + i] = 1.0f;
+    }
+}
+
+int pg_mlp_create(const pg_mlp_config *cfg, pg_mlp **out) {
+    if (!cfg || !out) return PG_ERR_ARG;
+    if (cfg->batch == 0 || cfg->batch > (1u << 22)) return mlp_error(PG_ERR_ARG, "batch must be in [1, 2^22]");
+    for (int i = 0; i < 3; ++i)
+        if (!(cfg->scene_aabb[3 + i] > cfg->scene_aabb[i])) return mlp_error(PG_ERR_ARG, "empty scene box");
+    pg_mlp *M = new pg_mlp();
+    M->cfg = *cfg;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&M->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    M->wg_blocks = std::max(1, M->sm_count);
+    M->smem = sizeof(Shared);
+    bool ok = cudaMalloc(&M->theta, sizeof(float) * NPARAM) == cudaSuccess &&
+              cudaMalloc(&M->m, sizeof(float) * NPARAM) == cudaSuccess &&
+              cudaMalloc(&M->v, sizeof(float) * NPARAM) == cudaSuccess &&
+              cudaMalloc(&M->wb, sizeof(__nv_bfloat16) * NWB) == cudaSuccess &&
+              cudaMalloc(&M->wg_partials, sizeof(float) * (size_t)M->wg_blocks * NPARAM) == cudaSuccess;
+    ok = ok && cudaFuncSetAttribute(k_fwd_bwd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)M->smem) ==
+                   cudaSuccess &&
+         cudaFuncSetAttribute(k_fwd_bwd<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)M->smem) ==
+             cudaSuccess;
+    if (!ok) {
+        pg_mlp_destroy(M);
+        return mlp_error(PG_ERR_CUDA, "surrogate allocation failed");
+    }
+    // initial weights: the same construction as the oracle's init_params
+    // (He-uniform hidden layers from a seeded generator, small output layer,
+    // log-kappa biases log 5, spherical-Fibonacci mean directions)
+    std::vector<float> th(NPARAM, 0.0f);
+    uint64_t st = 0x9E3779B97F4A7C15ull ^ ((uint64_t)cfg->seed * 0xBF58476D1CE4E5B9ull);
+    auto uni = [&]() {  // splitmix64 -> [0, 1)
+        uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+    };
+    auto fill = [&](int ofs, int rows, int cols, int fan_in, double scale) {
+        const double lim = sqrt(6.0 / fan_in) * scale;
+        for (int r = 0; r < rows; ++r)
+            for (int c = 0; c < cols; ++c) th[ofs + r * cols + c] = (float)((2.0 * uni() - 1.0) * lim);
+    };
+    fill(OW1, NH, NIN, 99, 1.0);
+    for (int r = 0; r < NH; ++r)
+        for (int c = 99; c < NIN; ++c) th[OW1 + r * NIN + c] = 0.0f;
+    fill(OW2, NH, NH, NH, 1.0);
+    fill(OW3, NH, NH, NH, 1.0);
+    fill(OW4, NOUT, NH, NH, 0.1);
+    for (int j = 0; j < NC; ++j) {
+        const double jj = j + 0.5, z = 1.0 - 2.0 * jj / NC, phi = 3.14159265358979323846 * (3.0 - sqrt(5.0)) * jj;
+        const double rr = sqrt(1.0 - z * z);
+        th[OB4 + 5 * j + 1] = (float)(rr * cos(phi));
+        th[OB4 + 5 * j + 2] = (float)(rr * sin(phi));
+        th[OB4 + 5 * j + 3] = (float)z;
+        th[OB4 + 5 * j + 4] = (float)log(5.0);
+    }
+    *out = M;
+    const int rc = pg_mlp_set_params(M, th.data());
+    if (rc) {
+        pg_mlp_destroy(M);
+        *out = nullptr;
+    }
+    return rc;
+}
+
+int pg_mlp_destroy(pg_mlp *M) {
+    if (!M) return PG_OK;
+    cudaFree(M->theta);
+    cudaFree(M->m);
+    cudaFree(M->v);
+    cudaFree(M->wb);
+    cudaFree(M->scratch);
+    cudaFree(M->fwd_partials);
+    cudaFree(M->wg_partials);
+    cudaFree(M->scalars);
+    cudaFree(M->pos);
+    cudaFree(M->mix);
+    delete M;
+    return PG_OK;
+}
+
+int pg_mlp_get_params(pg_mlp *M, float *host_out) {
+    if (!M || !host_out) return PG_ERR_ARG;
+    return cudaMemcpy(host_out, M->theta, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost) == cudaSuccess
+               ? PG_OK
+               : mlp_error(PG_ERR_CUDA, "parameter download");
+}
+
+int pg_mlp_set_params(pg_mlp *M, const float *host_in) {
+    if (!M || !host_in) return PG_ERR_ARG;
+    if (cudaMemcpy(M->theta, host_in, sizeof(float) * NPARAM, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(M->m, 0, sizeof(float) * NPARAM) != cudaSuccess ||
+        cudaMemset(M->v, 0, sizeof(float) * NPARAM) != cudaSuccess)
+        return mlp_error(PG_ERR_CUDA, "parameter upload");
+    k_theta_to_wb<<<(NPARAM + 255) / 256, 256>>>(M->theta, M->wb);
+    if (cudaDeviceSynchronize() != cudaSuccess) return mlp_error(PG_ERR_CUDA, "weight conversion");
+    M->step = 0;
+    return PG_OK;
+}
+
+int pg_mlp_loss_grad(pg_mlp *M, const pg_directional_data *records, uint32_t n, float *grad_out, float *loss_out,
+                     void *stream) {
+    if (!M || (!records && n)) return PG_ERR_ARG;
+    if (n == 0 || n > M->cfg.batch) return mlp_error(PG_ERR_ARG, "n must be in [1, batch]");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (int st = ensure_capacity(M, padded_rows(n), 1)) return st;
+    if (int st = batch_gradients(M, records, n, 0, s)) return st;
+    if (grad_out)
+        if (int st = reduce_step(M, 0, grad_out, s)) return st;
+    if (loss_out) {
+        double sc[2];
+        if (cudaMemcpyAsync(sc, M->scalars, sizeof sc, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return mlp_error(PG_ERR_CUDA, "loss download");
+        *loss_out = sc[1] > 0.0 ? (float)(sc[0] / sc[1]) : 0.0f;
+    }
+    return PG_OK;
+}
+
+int pg_mlp_train(pg_mlp *M, const pg_directional_data *records, uint64_t n, float *loss_out, void *stream) {
+    if (!M || (!records && n)) return PG_ERR_ARG;
+    if (n == 0) return PG_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint64_t B = M->cfg.batch;
+    const uint32_t batches = (uint32_t)((n + B - 1) / B);
+    if (int st = ensure_capacity(M, padded_rows(std::min<uint64_t>(n, B)), batches)) return st;
+    for (uint32_t b = 0; b < batches; ++b) {
+        const uint64_t first = (uint64_t)b * B;
+        const uint32_t cnt = (uint32_t)std::min<uint64_t>(B, n - first);
+        if (int st = batch_gradients(M, records + first, cnt, b, s)) return st;
+        if (int st = reduce_step(M, b, nullptr, s)) return st;
+    }
+    if (loss_out) {
+        std::vector<double> sc(2 * (size_t)batches);
+        if (cudaMemcpyAsync(sc.data(), M->scalars, sizeof(double) * sc.size(), cudaMemcpyDeviceToHost, s) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return mlp_error(PG_ERR_CUDA, "loss download");
+        double acc = 0.0;
+        for (uint32_t b = 0; b < batches; ++b) acc += sc[2 * b + 1] > 0.0 ? sc[2 * b] / sc[2 * b + 1] : 0.0;
+        *loss_out = (float)(acc / batches);
+    }
+    return PG_OK;
+}
+
+int pg_mlp_infer(pg_mlp *M, const float *positions, uint32_t n, float *mixtures_out, void *stream) {
+    if (!M || (n && (!positions || !mixtures_out))) return PG_ERR_ARG;
+    if (n == 0) return PG_OK;
+    FwdArgs A = fwd_args(M);
+    A.pos = positions;
+    A.n = n;
+    A.mix_out = mixtures_out;
+    k_fwd_bwd<false><<<(n + kRowsPerCta - 1) / kRowsPerCta, 32 * kWarps, M->smem, (cudaStream_t)stream>>>(A);
+    return cudaGetLastError() == cudaSuccess ? PG_OK : mlp_error(PG_ERR_CUDA, "surrogate inference launch");
+}
+
+int pg_mlp_write_guide(pg_mlp *M, pg_ctx *guide, void *stream) {
+    if (!M || !guide) return PG_ERR_ARG;
+    GuideTarget T{};
+    if (int st = guide_target(guide, &T)) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (T.n_regions > M->cap_guide) {
+        cudaFree(M->pos);
+        cudaFree(M->mix);
+        M->pos = M->mix = nullptr;
+        if (cudaMalloc(&M->pos, sizeof(float) * 3 * (size_t)T.n_regions) != cudaSuccess ||
+            cudaMalloc(&M->mix, sizeof(float) * NOUT * (size_t)T.n_regions) != cudaSuccess) {
+            M->cap_guide = 0;
+            return mlp_error(PG_ERR_NOMEM, "guide scratch: out of device memory");
+        }
+        M->cap_guide = T.n_regions;
+    }
+    k_region_centres<<<(T.n_regions + 255) / 256, 256, 0, s>>>(T.aabbs, T.n_regions, M->pos);
+    if (int st = pg_mlp_infer(M, M->pos, T.n_regions, M->mix, stream)) return st;
+    k_pack_guide<<<T.n_regions, NC, 0, s>>>(M->mix, M->pos, T.n_regions, T.vmm);
+    if (cudaGetLastError() != cudaSuccess) return mlp_error(PG_ERR_CUDA, "guide pack launch");
+    guide_mark_written(guide);
+    return PG_OK;
+}
+
+}  // extern "C"
