@@ -509,6 +509,22 @@ int pg_mlp_infer(pg_mlp *mlp, const float *positions, uint32_t n, float *mixture
  * (after pg_set_regions) and installs the mixtures as the context's packed
  * guide, so pg_render guides with the network (no parallax re-aiming). */
 int pg_mlp_write_guide(pg_mlp *mlp, pg_ctx *guide, void *stream);
+/* The network beside the per-region fit, the fit staying the fallback and
+ * the judge: for each region of `guide`, the weighted NLL (the KL divergence
+ * up to a constant) of the given records (device; flags = region id, as the
+ * tracer writes them) under the context's own mixture and under the
+ * network's mixture at the region centre are compared; regions with at least
+ * min_records records where the network's is lower take the network's
+ * mixture.  *switched_out (host, may be NULL) receives the number of regions
+ * switched, after a stream synchronisation. */
+int pg_mlp_judge_guide(pg_mlp *mlp, pg_ctx *guide, const pg_directional_data *records, uint64_t n,
+                       uint32_t min_records, uint32_t *switched_out, void *stream);
+/* Weighted NLL, sum w (-log q(d)) / sum w, of records (device; flags = region
+ * id) under a context's current guide - the fitted mixtures or what
+ * pg_mlp_write_guide / pg_mlp_judge_guide installed - with parallax re-aiming
+ * when the context uses it.  *nll_out is written after a stream
+ * synchronisation. */
+int pg_guide_nll(pg_ctx *guide, const pg_directional_data *records, uint64_t n, double *nll_out, void *stream);
 
 #ifdef __cplusplus
 }

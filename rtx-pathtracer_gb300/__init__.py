@@ -58,6 +58,8 @@ SIGNATURES = {
     "pg_mlp_train": (_I, [_P, _P, _U64, C.POINTER(C.c_float), _P]),
     "pg_mlp_infer": (_I, [_P, _P, _U32, _P, _P]),
     "pg_mlp_write_guide": (_I, [_P, _P, _P]),
+    "pg_mlp_judge_guide": (_I, [_P, _P, _P, _U64, _U32, C.POINTER(_U32), _P]),
+    "pg_guide_nll": (_I, [_P, _P, _U64, C.POINTER(C.c_double), _P]),
     "pg_set_regions": (_I, [_P, _U32, _P, _P]),
     "pg_region_count": (_I, [_P, C.POINTER(_U32)]),
     "pg_get_region_aabbs": (_I, [_P, _P, _U32]),
@@ -227,6 +229,12 @@ class FitContext:
         self._check(self.lib.pg_update(self.h, _dptr(records), n_records,
                                        _dptr(vmm_out) if vmm_out is not None else None, _stream_handle(stream)))
 
+    def guide_nll(self, records_dev, n: int, stream=None) -> float:
+        """Weighted NLL of records under the context's current guide (the KL judge)."""
+        v = C.c_double()
+        self._check(self.lib.pg_guide_nll(self.h, _dptr(records_dev), n, C.byref(v), _stream_handle(stream)))
+        return float(v.value)
+
     def last_launch_count(self) -> int:
         n = C.c_uint32()
         self._check(self.lib.pg_last_launch_count(self.h, C.byref(n)))
@@ -295,6 +303,14 @@ class Surrogate:
 
     def write_guide(self, ctx: FitContext, stream=None):
         self._check(self.lib.pg_mlp_write_guide(self.h, ctx.h, _stream_handle(stream)))
+
+    def judge_guide(self, ctx: FitContext, records_dev, n: int, min_records: int = 32, stream=None) -> int:
+        """Per region, keeps the context's fitted mixture or takes the
+        network's, whichever has the lower weighted NLL on the records."""
+        k = C.c_uint32()
+        self._check(self.lib.pg_mlp_judge_guide(self.h, ctx.h, _dptr(records_dev), n, min_records, C.byref(k),
+                                                _stream_handle(stream)))
+        return int(k.value)
 
 
 NOALLOC_MAX_REGIONS = 65536

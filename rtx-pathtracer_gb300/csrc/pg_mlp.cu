@@ -577,6 +577,80 @@ __global__ void k_pack_guide(const float *mix, const float *pos, uint32_t n, pg_
     }
 }
 
+// Mixture pdf of a packed VMM_Theta (guiding.glsl:32-60), parallax re-aiming
+// toward each lobe's target when its distance is positive.
+__device__ float vmm_theta_pdf(const pg_vmm_theta &v, const float d[3], const float x[3], int par) {
+    float res = 0.0f;
+    const int K = min(v.used_distributions, 16);
+    for (int i = 0; i < K; ++i) {
+        const pg_vmf_theta &t = v.thetas[i];
+        float f;
+        if (t.k == 0.0f) {
+            f = 1.0f / (4.0f * kPi);
+        } else {
+            float mu[3] = {t.mu[0], t.mu[1], t.mu[2]};
+            if (par && t.distance > 0.0f) {
+                for (int c = 0; c < 3; ++c) mu[c] = t.target[c] - x[c];
+                const float l = rsqrtf(mu[0] * mu[0] + mu[1] * mu[1] + mu[2] * mu[2]);
+                for (int c = 0; c < 3; ++c) mu[c] *= l;
+            }
+            f = t.norm * expf(t.k * (mu[0] * d[0] + mu[1] * d[1] + mu[2] * d[2] - 1.0f));
+        }
+        res += v.pi[i] * f;
+    }
+    return res;
+}
+
+// per-region sums of w (-log q) under the context's and the network's mixtures
+__global__ void k_judge_accumulate(const pg_directional_data *rec, uint64_t n, const pg_vmm_theta *fit,
+                                   const pg_vmm_theta *net, uint32_t n_regions, int par, float *sums) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const pg_directional_data &r = rec[i];
+        if (r.flags >= n_regions) continue;
+        const float w = r.weight;
+        if (!(w > 0.0f) || !isfinite(w)) continue;
+        const float qf = fmaxf(vmm_theta_pdf(fit[r.flags], r.direction, r.position, par), 1e-30f);
+        const float qn = fmaxf(vmm_theta_pdf(net[r.flags], r.direction, r.position, 0), 1e-30f);
+        float *s = sums + 4 * (size_t)r.flags;
+        atomicAdd(s, isfinite(qf) ? -w * logf(qf) : INFINITY);
+        atomicAdd(s + 1, -w * logf(qn));
+        atomicAdd(s + 2, w);
+        atomicAdd(s + 3, 1.0f);
+    }
+}
+
+__global__ void k_judge_select(const float *sums, const pg_vmm_theta *net, uint32_t n_regions, float min_records,
+                               pg_vmm_theta *fit, uint32_t *switched) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_regions) return;
+    const float *s = sums + 4 * (size_t)r;
+    const bool better = s[1] < s[0] || (!isfinite(s[0]) && isfinite(s[1]));
+    if (s[3] < min_records || !better) return;
+    fit[r] = net[r];
+    atomicAdd(switched, 1u);
+}
+
+// sum w (-log q) and sum w of records under a packed guide (double accumulators)
+__global__ void k_guide_nll(const pg_directional_data *rec, uint64_t n, const pg_vmm_theta *vmm, uint32_t n_regions,
+                            int par, double *out) {
+    double l = 0.0, w = 0.0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const pg_directional_data &r = rec[i];
+        if (r.flags >= n_regions || !(r.weight > 0.0f) || !isfinite(r.weight)) continue;
+        const float q = fmaxf(vmm_theta_pdf(vmm[r.flags], r.direction, r.position, par), 1e-30f);
+        l += -(double)r.weight * log((double)q);
+        w += r.weight;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        l += __shfl_xor_sync(0xffffffffu, l, o);
+        w += __shfl_xor_sync(0xffffffffu, w, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out, l);
+        atomicAdd(out + 1, w);
+    }
+}
+
 }  // namespace mlp
 }  // namespace pg
 
@@ -594,6 +668,9 @@ struct pg_mlp {
     double *scalars = nullptr;       // per batch: {loss sum, weight sum}
     float *pos = nullptr;            // guide positions
     float *mix = nullptr;            // guide mixtures
+    pg_vmm_theta *net_vmm = nullptr; // the network's packed mixtures at region centres
+    float *judge = nullptr;          // per-region judge sums (4 floats)
+    uint32_t *judge_count = nullptr;
     uint32_t cap_guide = 0;
     uint32_t cap_rows = 0;           // padded batch rows
     uint32_t cap_batches = 0;
@@ -791,6 +868,9 @@ int pg_mlp_destroy(pg_mlp *M) {
     cudaFree(M->scalars);
     cudaFree(M->pos);
     cudaFree(M->mix);
+    cudaFree(M->net_vmm);
+    cudaFree(M->judge);
+    cudaFree(M->judge_count);
     delete M;
     return PG_OK;
 }
@@ -870,27 +950,103 @@ int pg_mlp_infer(pg_mlp *M, const float *positions, uint32_t n, float *mixtures_
     return cudaGetLastError() == cudaSuccess ? PG_OK : mlp_error(PG_ERR_CUDA, "surrogate inference launch");
 }
 
-int pg_mlp_write_guide(pg_mlp *M, pg_ctx *guide, void *stream) {
-    if (!M || !guide) return PG_ERR_ARG;
-    GuideTarget T{};
-    if (int st = guide_target(guide, &T)) return st;
-    cudaStream_t s = (cudaStream_t)stream;
+}  // extern "C"
+
+namespace {
+// the network's mixtures at the centres of the context's regions, packed into
+// the context's guide (to_ctx) or into the surrogate's own buffer
+int net_guide(pg_mlp *M, const GuideTarget &T, bool to_ctx, cudaStream_t s) {
     if (T.n_regions > M->cap_guide) {
         cudaFree(M->pos);
         cudaFree(M->mix);
-        M->pos = M->mix = nullptr;
+        cudaFree(M->net_vmm);
+        cudaFree(M->judge);
+        M->pos = M->mix = M->judge = nullptr;
+        M->net_vmm = nullptr;
         if (cudaMalloc(&M->pos, sizeof(float) * 3 * (size_t)T.n_regions) != cudaSuccess ||
-            cudaMalloc(&M->mix, sizeof(float) * NOUT * (size_t)T.n_regions) != cudaSuccess) {
+            cudaMalloc(&M->mix, sizeof(float) * NOUT * (size_t)T.n_regions) != cudaSuccess ||
+            cudaMalloc(&M->net_vmm, sizeof(pg_vmm_theta) * (size_t)T.n_regions) != cudaSuccess ||
+            cudaMalloc(&M->judge, sizeof(float) * 4 * (size_t)T.n_regions) != cudaSuccess) {
             M->cap_guide = 0;
             return mlp_error(PG_ERR_NOMEM, "guide scratch: out of device memory");
         }
         M->cap_guide = T.n_regions;
     }
     k_region_centres<<<(T.n_regions + 255) / 256, 256, 0, s>>>(T.aabbs, T.n_regions, M->pos);
-    if (int st = pg_mlp_infer(M, M->pos, T.n_regions, M->mix, stream)) return st;
-    k_pack_guide<<<T.n_regions, NC, 0, s>>>(M->mix, M->pos, T.n_regions, T.vmm);
-    if (cudaGetLastError() != cudaSuccess) return mlp_error(PG_ERR_CUDA, "guide pack launch");
+    if (int st = pg_mlp_infer(M, M->pos, T.n_regions, M->mix, s)) return st;
+    k_pack_guide<<<T.n_regions, NC, 0, s>>>(M->mix, M->pos, T.n_regions, to_ctx ? T.vmm : M->net_vmm);
+    return cudaGetLastError() == cudaSuccess ? PG_OK : mlp_error(PG_ERR_CUDA, "guide pack launch");
+}
+}  // namespace
+
+extern "C" {
+
+int pg_mlp_write_guide(pg_mlp *M, pg_ctx *guide, void *stream) {
+    if (!M || !guide) return PG_ERR_ARG;
+    GuideTarget T{};
+    if (int st = guide_target(guide, &T)) return st;
+    if (int st = net_guide(M, T, true, (cudaStream_t)stream)) return st;
     guide_mark_written(guide);
+    return PG_OK;
+}
+
+int pg_mlp_judge_guide(pg_mlp *M, pg_ctx *guide, const pg_directional_data *records, uint64_t n,
+                       uint32_t min_records, uint32_t *switched_out, void *stream) {
+    if (!M || !guide || (!records && n)) return PG_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    GuideView V{};
+    if (int st = guide_view(guide, &V, s)) return st;  // brings the fit's packed mixtures up to date
+    GuideTarget T{};
+    if (int st = guide_target(guide, &T)) return st;
+    if (int st = net_guide(M, T, false, s)) return st;
+    if (!M->judge_count && cudaMalloc(&M->judge_count, sizeof(uint32_t)) != cudaSuccess)
+        return mlp_error(PG_ERR_NOMEM, "judge counter");
+    if (cudaMemsetAsync(M->judge, 0, sizeof(float) * 4 * (size_t)T.n_regions, s) != cudaSuccess ||
+        cudaMemsetAsync(M->judge_count, 0, sizeof(uint32_t), s) != cudaSuccess)
+        return mlp_error(PG_ERR_CUDA, "judge reset");
+    if (n) {
+        const uint32_t blocks = (uint32_t)std::min<uint64_t>((n + 255) / 256, (uint64_t)M->sm_count * 8);
+        k_judge_accumulate<<<blocks, 256, 0, s>>>(records, n, T.vmm, M->net_vmm, T.n_regions, V.use_parallax,
+                                                  M->judge);
+    }
+    k_judge_select<<<(T.n_regions + 255) / 256, 256, 0, s>>>(M->judge, M->net_vmm, T.n_regions,
+                                                              (float)std::max(1u, min_records), T.vmm,
+                                                              M->judge_count);
+    if (cudaGetLastError() != cudaSuccess) return mlp_error(PG_ERR_CUDA, "judge launch");
+    guide_mark_written(guide);
+    if (switched_out) {
+        if (cudaMemcpyAsync(switched_out, M->judge_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, s) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return mlp_error(PG_ERR_CUDA, "judge count download");
+    }
+    return PG_OK;
+}
+
+int pg_guide_nll(pg_ctx *guide, const pg_directional_data *records, uint64_t n, double *nll_out, void *stream) {
+    if (!guide || !nll_out || (!records && n)) return PG_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    GuideView V{};
+    if (int st = guide_view(guide, &V, s)) return st;
+    double *acc = nullptr;
+    if (cudaMalloc(&acc, 2 * sizeof(double)) != cudaSuccess) return mlp_error(PG_ERR_NOMEM, "nll accumulators");
+    double h[2] = {0.0, 0.0};
+    int st = PG_OK;
+    if (cudaMemsetAsync(acc, 0, 2 * sizeof(double), s) != cudaSuccess) st = PG_ERR_CUDA;
+    if (!st && n) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const uint32_t blocks = (uint32_t)std::min<uint64_t>((n + 255) / 256, (uint64_t)std::max(sms, 1) * 8);
+        k_guide_nll<<<blocks, 256, 0, s>>>(records, n, V.vmm, V.n_regions, V.use_parallax, acc);
+        if (cudaGetLastError() != cudaSuccess) st = PG_ERR_CUDA;
+    }
+    if (!st && (cudaMemcpyAsync(h, acc, sizeof h, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                cudaStreamSynchronize(s) != cudaSuccess))
+        st = PG_ERR_CUDA;
+    cudaFree(acc);
+    if (st) return mlp_error(st, "guide NLL");
+    *nll_out = h[1] > 0.0 ? h[0] / h[1] : 0.0;
     return PG_OK;
 }
 

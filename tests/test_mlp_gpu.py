@@ -150,3 +150,92 @@ def test_training_reduces_loss(cuda, pkg, abi, workloads):
     # the held-out NLL falls well below the initial one (a kappa-50 vMF has NLL ~ -1.07)
     assert np.isfinite(l1) and l1 < l0 - 1.5 and l1 < 0.0, (l0, l1)
     net.close()
+
+
+def collect(torch, pkg, abi, G, sc, pg, col, spp_list, seed0, guided_after_first=True):
+    """Training passes with recording; returns the valid records of all passes
+    (host, bucketed by region per pass)."""
+    info = sc.info()
+    P = info.camera.width * info.camera.height
+    img = torch.zeros(P * 3, dtype=torch.float32, device="cuda")
+    out = []
+    for i, spp in enumerate(spp_list):
+        p = abi.render_params(spp=spp, max_depth=10, seed=seed0 + 1000 * i,
+                              use_guiding=1 if (guided_after_first and i > 0) else 0, record_samples=1)
+        sc.render(p, img, guide=pg.ctx, records_dev=col.buffer)
+        rec, _ = col.get_sorted_data(pg)
+        out.append(rec)
+        pg.update(col)
+    torch.cuda.synchronize()
+    return np.concatenate(out)
+
+
+def test_surrogate_beside_the_fit_lowers_held_out_nll(cuda, pkg, abi):
+    """What the network adds to the per-region fit: trained on the same sparse
+    records (two short passes), it is judged per region against the fit on a
+    second set of records; the regions where it wins take its mixture, and the
+    weighted NLL (KL up to a constant) of a third, held-out set falls.  The
+    combined guide still renders the same expectation."""
+    import __graft_entry__ as entry
+    G = entry.load_submodule("guiding")
+    torch = cuda
+    W, H = 160, 90
+    sc = pkg.Scene.cornell(W, H, ico_level=4)
+    box = np.array(sc.get_scene_size(), dtype=np.float32)
+    pg = G.PathGuiding(12, box)
+    col = G.SampleCollector(pg.get_region_count(), W, H)
+    train = collect(torch, pkg, abi, G, sc, pg, col, (1, 2), seed0=11)
+    net = pkg.Surrogate(box, batch=1 << 13, lr=1e-3)
+    d_train = dev(torch, train)
+    for _ in range(8):
+        net.train(d_train, train.shape[0])
+    P = W * H
+    img = torch.zeros(P * 3, dtype=torch.float32, device="cuda")
+
+    def records_pass(seed):
+        sc.render(abi.render_params(spp=4, max_depth=10, seed=seed, record_samples=1), img, guide=pg.ctx,
+                  records_dev=col.buffer)
+        rec, _ = col.get_sorted_data(pg)
+        return rec
+
+    judge = records_pass(501)
+    held = records_pass(777)
+    d_held = dev(torch, held)
+    nll_fit = pg.ctx.guide_nll(d_held, held.shape[0])
+    switched = net.judge_guide(pg.ctx, dev(torch, judge), judge.shape[0], min_records=32)
+    nll_comb = pg.ctx.guide_nll(d_held, held.shape[0])
+    assert switched > 0
+    assert nll_comb < nll_fit - 0.01, (nll_fit, nll_comb, switched)
+    # unbiased with the combined guide
+    g = torch.zeros(P * 3, dtype=torch.float32, device="cuda")
+    sc.render(abi.render_params(spp=512, max_depth=10, seed=3, use_guiding=1), g, guide=pg.ctx)
+    p = torch.zeros(P * 3, dtype=torch.float32, device="cuda")
+    sc.render(abi.render_params(spp=512, max_depth=10, seed=4), p)
+    torch.cuda.synchronize()
+    gm, pm = g.mean().item(), p.mean().item()
+    assert abs(gm - pm) / pm < 0.02
+    net.close()
+    pg.close()
+
+
+def test_network_guide_renders_unbiased(cuda, pkg, abi):
+    """pg_mlp_write_guide: the network alone as the guide of a fine region
+    grid (no fit) keeps the image's expectation."""
+    torch = cuda
+    W, H = 96, 54
+    sc = pkg.Scene.cornell(W, H, ico_level=3)
+    box = np.array(sc.get_scene_size(), dtype=np.float32)
+    net = pkg.Surrogate(box)
+    ctx = pkg.FitContext(abi.default_fit_config(), max_regions=1 << 14)
+    ctx.set_regions(14, box)
+    net.write_guide(ctx)
+    P = W * H
+    g = torch.zeros(P * 3, dtype=torch.float32, device="cuda")
+    sc.render(abi.render_params(spp=1024, max_depth=10, seed=3, use_guiding=1), g, guide=ctx)
+    p = torch.zeros(P * 3, dtype=torch.float32, device="cuda")
+    sc.render(abi.render_params(spp=1024, max_depth=10, seed=4), p)
+    torch.cuda.synchronize()
+    assert np.isfinite(g.cpu().numpy()).all()
+    assert abs(g.mean().item() - p.mean().item()) / p.mean().item() < 0.02
+    net.close()
+    ctx.close()
