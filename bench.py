@@ -345,6 +345,21 @@ def bench_guided(pkg, abi, torch, stream, ref_spp: int = 4096, scene: str = "pla
     g64 = g64.cpu().numpy().reshape(H, W, 3).astype(np.float64) / 64
     eq_spp = max(1, int(64 * tm["total_ms"] / p64_ms))
     peq, peq_ms = plain(eq_spp, 9000)
+    sur = None
+    if scene != "plates":
+        # the same sequence with the surrogate trained online beside the fit and judged per region
+        net = pkg.Surrogate(sc.get_scene_size(), batch=65536)
+        pg2 = G.PathGuiding(12, sc.get_scene_size())
+        tms = G.guided_sequence(sc, pg2, col, img, final_spp=64, max_depth=10, seed=7, stream=stream, surrogate=net)
+        simg = img.cpu().numpy().reshape(H, W, 3).astype(np.float64) / tms["spp"]
+        eq2 = max(1, int(64 * tms["total_ms"] / p64_ms))
+        peq2, peq2_ms = plain(eq2, 9100)
+        sur = {"relmse": G.relmse(simg, ref), "ms": tms["total_ms"], "train_ms": tms["train_ms"], "spp": tms["spp"],
+               "regions_switched": tms.get("regions_switched"),
+               "plain_equal_time": {"relmse": G.relmse(peq2, ref), "ms": peq2_ms, "spp": eq2}}
+        sur["value"] = sur["relmse"] / sur["plain_equal_time"]["relmse"]
+        pg2.close()
+        net.close()
     out = {"metric": "equal-time relMSE, guided vs plain NEE+MIS PT", "unit": "relMSE", "higher_is_better": False,
            "config": {"workload": workload, "triangles": info.n_triangles,
                       "reference": f"plain NEE+MIS, {ref_spp} spp ({ref_ms / 1e3:.1f} s)", "relmse_eps": 1e-2},
@@ -355,8 +370,74 @@ def bench_guided(pkg, abi, torch, stream, ref_spp: int = 4096, scene: str = "pla
                             "plain_ms": p64_ms}}
     out["value"] = out["guided"]["relmse"] / out["plain_equal_time"]["relmse"]
     out["value_meaning"] = "guided relMSE / plain relMSE at equal time (< 1: guiding wins)"
+    if sur is not None:
+        out["surrogate_beside_fit"] = sur
     pg.close()
     sc.close()
+    return out
+
+
+SURROGATE_WORKLOAD = ("learned guiding surrogate: MLP 112 Fourier inputs (16 octaves x 3 axes) -> 3 x 64 ReLU -> 80 "
+                      "(16 vMF components), BF16 weights/activations, FP32 accumulation and Adam (lr 1e-3, batch "
+                      "65536); one training pass over 2^22 records (seeded positions in a box, directions from "
+                      "kappa-50 vMF lobes around 4 point lights, lognormal(0,1) weights)")
+# multiply-adds per record: forward 112*64 + 64*64 + 64*64 + 64*80, backward data 80*64 + 64*64 + 64*64,
+# weight gradients as forward
+SURROGATE_TRAIN_FLOP = 2 * (20480 + 13312 + 20480)
+SURROGATE_INFER_FLOP = 2 * 20480
+
+
+def measured_bf16_sustained():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["bf16_tflops_sustained"]), "measured"
+        except Exception:
+            pass
+    return 1700.0, "fallback"
+
+
+def bench_surrogate(pkg, abi, torch, stream, passes: int = 3):
+    """Training and inference throughput of the surrogate on 2^22 records."""
+    import __graft_entry__ as entry
+    wl = entry.load_submodule("workloads")
+    box = (-2.0, -1.0, -1.5, 2.0, 3.0, 1.5)
+    n = 1 << 22
+    rec = wl.surrogate_records(n=n, box=box)
+    d_rec = torch.from_numpy(rec.view(np.uint8).reshape(-1).copy()).cuda()
+    net = pkg.Surrogate(box, batch=65536, lr=1e-3)
+    losses = [net.train(d_rec, n, stream=stream)]  # warm-up pass
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        ev0.record(stream)
+        for _ in range(passes):
+            net.train(d_rec, n, stream=stream, want_loss=False)
+        ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / passes
+    losses.append(net.train(d_rec, n, stream=stream))
+    pos = torch.from_numpy(np.ascontiguousarray(rec["position"], dtype=np.float32)).cuda()
+    mix = torch.empty(n * 80, dtype=torch.float32, device="cuda")
+    net.infer(pos, n, mix, stream=stream)
+    with torch.cuda.stream(stream):
+        ev0.record(stream)
+        for _ in range(passes):
+            net.infer(pos, n, mix, stream=stream)
+        ev1.record(stream)
+    torch.cuda.synchronize()
+    infer_ms = ev0.elapsed_time(ev1) / passes
+    peak, src = measured_bf16_sustained()
+    achieved = SURROGATE_TRAIN_FLOP * n / (ms * 1e-3) / 1e12
+    out = {"metric": "surrogate training records/s", "value": n / (ms * 1e-3) / 1e6, "unit": "Mrecords/s",
+           "higher_is_better": True, "dtype": "bf16 (fp32 accumulate)", "config": {"workload": SURROGATE_WORKLOAD},
+           "ms_per_pass": ms, "batches_per_pass": n // 65536, "loss_first_pass": losses[0],
+           "loss_after": losses[-1],
+           "inference": {"value": n / (infer_ms * 1e-3) / 1e6, "unit": "Mpositions/s", "ms": infer_ms},
+           "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                        "frac": achieved / peak, "peak_source": f"{src} bf16 sustained",
+                        "flop_per_record": SURROGATE_TRAIN_FLOP}}
+    net.close()
     return out
 
 
@@ -378,8 +459,8 @@ def main():
     ap.add_argument("--median", type=float, default=0.0, help="override the median region size")
     ap.add_argument("--sigma", type=float, default=-1.0, help="override the region-size sigma")
     ap.add_argument("--sweep", action="store_true", help="time the tuning grid and print one line per point")
-    ap.add_argument("--workload", default="all", choices=["all", "em", "tracer", "guided"],
-                    help="all: the EM line with the tracer and guided blocks; em / tracer / guided: one alone")
+    ap.add_argument("--workload", default="all", choices=["all", "em", "tracer", "guided", "surrogate"],
+                    help="all: the EM line with the tracer, guided and surrogate blocks; or one of them alone")
     ap.add_argument("--ref-seconds", type=float, default=None,
                     help="CPU seconds per reference step (default: ~100 s over the whole run)")
     args = ap.parse_args()
@@ -400,13 +481,15 @@ def main():
     torch.cuda.set_device(local)
     pkg = entry.load_package()
     abi = pkg.abi
-    if args.workload in ("tracer", "guided"):
+    if args.workload in ("tracer", "guided", "surrogate"):
         stream = torch.cuda.Stream()
         sampler = ClockSampler(local)
         with sampler:
             if args.workload == "tracer":
                 line = bench_tracer(pkg, abi, torch, stream, args.steps, args.warmup,
                                     cpu=rank == 0 and not args.no_cpu_baseline)
+            elif args.workload == "surrogate":
+                line = bench_surrogate(pkg, abi, torch, stream)
             else:
                 line = bench_guided(pkg, abi, torch, stream)
                 line["cornell"] = bench_guided(pkg, abi, torch, stream, scene="cornell")
@@ -542,6 +625,11 @@ def main():
             gd["cornell"] = bench_guided(pkg, abi, torch, stream, scene="cornell")
         gd["clocks"] = gsampler.summary()
         line["guided"] = gd
+        ssampler = ClockSampler(local)
+        with ssampler:
+            sg = bench_surrogate(pkg, abi, torch, stream)
+        sg["clocks"] = ssampler.summary()
+        line["surrogate"] = sg
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -91,17 +91,27 @@ def relmse(img: np.ndarray, ref: np.ndarray, eps: float = 1e-2) -> float:
 
 def guided_sequence(scene: Scene, guiding: PathGuiding, collector: SampleCollector, image, train_spp=(1, 2, 4, 8, 16, 32),
                     final_spp: int = 64, max_depth: int = 10, seed: int = 1, guiding_prob: float = 0.5,
-                    accumulate_training: bool = True, stream=None) -> dict:
+                    accumulate_training: bool = True, surrogate=None, judge_min_records: int = 32,
+                    stream=None) -> dict:
     """Training passes (render with recording, then PathGuiding::update; the
     first pass is unguided), then a guided render of final_spp samples.  The
     image (cleared first) receives radiance sums: of every pass when
     accumulate_training (the reference keeps accumulating frames while it
     trains, src/RayTracingApp.cpp:125-157), else of the final render only.
-    Returns CUDA-event times in ms and the number of samples per pixel summed."""
+    With a surrogate (a Surrogate), every pass's valid records also train the
+    network online (one epoch each), and before the final render the network
+    is judged against the fit region by region on the last pass's records
+    (pg_mlp_judge_guide).  Returns CUDA-event times in ms and the number of
+    samples per pixel summed."""
     torch = _torch()
     s = stream or torch.cuda.current_stream()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     scratch = image if accumulate_training else torch.empty_like(image)
+    R = guiding.get_region_count()
+    if surrogate is not None:
+        srt = torch.empty(collector.n_slots * RECORD_BYTES, dtype=torch.uint8, device="cuda")
+        offs = torch.empty(R + 1, dtype=torch.int32, device="cuda")
+    switched = None
     with torch.cuda.stream(s):
         image.zero_()
         ev[0].record(s)
@@ -110,6 +120,12 @@ def guided_sequence(scene: Scene, guiding: PathGuiding, collector: SampleCollect
                                   use_guiding=1 if i > 0 else 0, guiding_prob=guiding_prob, record_samples=1)
             scene.render(p, scratch, guide=guiding.ctx, records_dev=collector.buffer, stream=s, stats=False)
             guiding.update(collector, stream=s)
+            if surrogate is not None:
+                guiding.ctx.sort_samples(collector.buffer, collector.n_slots, R, srt, offs, stream=s)
+                n_valid = int(offs[R].item())
+                surrogate.train(srt, n_valid, stream=s, want_loss=False)
+        if surrogate is not None:
+            switched = surrogate.judge_guide(guiding.ctx, srt, n_valid, min_records=judge_min_records, stream=s)
         ev[1].record(s)
         p = abi.render_params(spp=final_spp, max_depth=max_depth, seed=seed, use_guiding=1,
                               guiding_prob=guiding_prob)
@@ -117,5 +133,8 @@ def guided_sequence(scene: Scene, guiding: PathGuiding, collector: SampleCollect
         ev[2].record(s)
     torch.cuda.synchronize()
     total = final_spp + (sum(train_spp) if accumulate_training else 0)
-    return {"train_ms": ev[0].elapsed_time(ev[1]), "render_ms": ev[1].elapsed_time(ev[2]),
-            "total_ms": ev[0].elapsed_time(ev[2]), "spp": total}
+    out = {"train_ms": ev[0].elapsed_time(ev[1]), "render_ms": ev[1].elapsed_time(ev[2]),
+           "total_ms": ev[0].elapsed_time(ev[2]), "spp": total}
+    if switched is not None:
+        out["regions_switched"] = switched
+    return out

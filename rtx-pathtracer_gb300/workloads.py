@@ -134,3 +134,27 @@ def fit_batched(seed: int = 3, n_regions: int = 4096, median: float = 2048.0, si
     counts = region_counts_lognormal(rng, n_regions, median, sigma, lo, hi)
     return mixture_samples(rng, counts, 1, 6, 2.0, 2000.0, 1.5, region_boxes=region_boxes,
                            dist_range=(0.1, 100.0), miss_frac=0.1)
+
+
+def surrogate_records(seed: int = 5, n: int = 1 << 22, box=(-2.0, -1.0, -1.5, 2.0, 3.0, 1.5), lights=4,
+                      kappa: float = 50.0) -> np.ndarray:
+    """Training records for the learned surrogate: positions uniform in the
+    box, each direction drawn from a vMF (kappa) around the direction to one
+    of `lights` seeded point lights (picked per record), weights
+    lognormal(0, 1).  Returns a RECORD_DTYPE array (flags 0)."""
+    rng = np.random.default_rng(seed)
+    box = np.asarray(box, dtype=np.float64)
+    lo, hi = box[:3], box[3:]
+    pos = lo + (hi - lo) * rng.random((n, 3))
+    lp = lo + (hi - lo) * rng.random((lights, 3))
+    pick = rng.integers(0, lights, n)
+    mu = lp[pick] - pos
+    mu /= np.maximum(np.linalg.norm(mu, axis=1, keepdims=True), 1e-12)
+    d = sample_vmf(rng, mu, np.full(n, kappa))
+    rec = np.zeros(n, dtype=RECORD_DTYPE)
+    rec["position"] = pos
+    rec["direction"] = d
+    rec["weight"] = rng.lognormal(0.0, 1.0, n)
+    rec["pdf"] = 1.0
+    rec["distance"] = np.linalg.norm(lp[pick] - pos, axis=1)
+    return rec
