@@ -504,8 +504,6 @@ def main():
     n_samples = int(counts.sum())
     cfg = abi.forced_iterations(ITERS, num_initial_components=K)
     ctx = pkg.FitContext(cfg, max_regions=R)
-    ctx.set_tuning(threads_per_cta=args.threads, smem_samples=args.smem_samples, cluster_size=args.cluster,
-                   components_per_thread=args.cpt, unroll=args.unroll, large_threshold=args.large)
     stream = torch.cuda.Stream()
     dirw_h = torch.from_numpy(w["dirw"]).pin_memory()
     offs_h = torch.from_numpy(w["offsets"].view(np.int32)).pin_memory()
@@ -513,9 +511,26 @@ def main():
     offs_d = offs_h.to("cuda", non_blocking=False)
     fitted = counts > 2 * K
     si_per_step = int(counts[fitted].sum()) * ITERS  # regions with N <= 2K are not fitted
+    manual = any((args.threads, args.smem_samples, args.cluster, args.cpt, args.unroll, args.large))
+    tune_ms = None
+    if manual or args.sweep:
+        ctx.set_tuning(threads_per_cta=args.threads, smem_samples=args.smem_samples, cluster_size=args.cluster,
+                       components_per_thread=args.cpt, unroll=args.unroll, large_threshold=args.large)
+        tuned = None
+    else:
+        # the project's autotuner picks the launch shape on this workload (untimed)
+        best, tune_ms = ctx.autotune(dirw_d, offs_d, R, abi.PG_FIT_INIT, stream=stream)
+        tuned = {f: int(getattr(best, f)) for f, _ in abi.FitTuning._fields_}
+    graph = None
+    if not args.sweep:
+        # the fit as one captured CUDA graph (ordering kernel + persistent clustered fit)
+        graph = ctx.capture_fit(dirw_d, offs_d, R, abi.PG_FIT_INIT, stream=stream)
 
     def step():
-        ctx.fit(dirw_d, offs_d, R, abi.PG_FIT_INIT, stream=stream)
+        if graph is not None:
+            graph.launch(stream)
+        else:
+            ctx.fit(dirw_d, offs_d, R, abi.PG_FIT_INIT, stream=stream)
 
     if args.sweep:
         grid = [(128, cl, cap, cpt, 2, T) for cpt in (16, 8) for cl in (2, 4, 8, 16)
@@ -546,7 +561,7 @@ def main():
             step()
     torch.cuda.synchronize()
     ctx.sync(stream)
-    launches = ctx.last_launch_count()
+    launches = 2  # per fit: the region-ordering kernel and the persistent fit kernel
 
     def barrier():
         if world > 1:
@@ -605,12 +620,16 @@ def main():
             "config": {"workload": WORKLOAD if not args.small else "512-region case of: " + WORKLOAD,
                        "regions": R, "samples": n_samples, "em_iterations": ITERS, "components": K,
                        "l2": "inputs larger than L2 (221 MB of float4 samples), no flush",
-                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                       "launch": "captured CUDA graph" if graph is not None else "direct",
+                       "tuning": tuned if tuned is not None else "manual", "autotuned_ms": tune_ms},
             "gpu_launches": launches * args.steps,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": roofline, "clocks": sampler.summary()}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(w).items() if k != "seconds"}
+    if graph is not None:
+        graph.close()
     ctx.close()
     if args.workload == "all" and not args.small:
         tsampler = ClockSampler(local)

@@ -218,6 +218,29 @@ int pg_sync_status(pg_ctx *ctx, void *stream);
  * launches in benchmarks). */
 int pg_last_launch_count(const pg_ctx *ctx, uint32_t *count);
 
+/* Autotuner (no counterpart in the reference, which fits on the host): times
+ * the fit on the caller's own samples for each candidate tuning (the built-in
+ * grid of CTA size, samples staged per CTA, components per thread, cluster
+ * size and cluster threshold when candidates is NULL) with CUDA events on
+ * `stream`, keeps the fastest in the context and returns it in best_out with
+ * its time in best_ms_out (either may be NULL).  The mixture states are saved
+ * before and restored after, so the call leaves them as it found them;
+ * candidates the device cannot launch are skipped.  Synchronises the stream. */
+int pg_autotune_fit(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t n_regions, int mode,
+                    const pg_fit_tuning *candidates, uint32_t n_candidates, pg_fit_tuning *best_out,
+                    float *best_ms_out, void *stream);
+
+/* The fit as a CUDA graph: pg_fit_graph_create captures pg_fit_regions on
+ * `stream` (a non-default stream) with the given buffers and the context's
+ * current tuning; every pg_fit_graph_launch replays it - the caller refills
+ * the same sample and offset buffers between launches.  The graph holds
+ * pointers into the context: destroy it before the context. */
+typedef struct pg_fit_graph pg_fit_graph;
+int pg_fit_graph_create(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t n_regions, int mode,
+                        void *stream, pg_fit_graph **out);
+int pg_fit_graph_launch(pg_fit_graph *graph, void *stream);
+int pg_fit_graph_destroy(pg_fit_graph *graph);
+
 /* ------------------------------------------------------------------ */
 /* Regions, sample bucketing, parallax, distances, VMM_Theta            */
 /* ------------------------------------------------------------------ */

@@ -48,6 +48,11 @@ SIGNATURES = {
     "pg_get_fit_tuning": (_I, [_P, C.POINTER(abi.FitTuning)]),
     "pg_sync_status": (_I, [_P, _P]),
     "pg_last_launch_count": (_I, [_P, C.POINTER(_U32)]),
+    "pg_autotune_fit": (_I, [_P, _P, _P, _U32, _I, C.POINTER(abi.FitTuning), _U32, C.POINTER(abi.FitTuning),
+                             C.POINTER(C.c_float), _P]),
+    "pg_fit_graph_create": (_I, [_P, _P, _P, _U32, _I, _P, C.POINTER(_P)]),
+    "pg_fit_graph_launch": (_I, [_P, _P]),
+    "pg_fit_graph_destroy": (_I, [_P]),
     "pg_fit_regions_noalloc": (_I, [C.POINTER(abi.FitConfig), _P, _P, _P, _U32, _I, _P]),
     "pg_mlp_default_config": (None, [C.POINTER(abi.MlpConfig)]),
     "pg_mlp_create": (_I, [C.POINTER(abi.MlpConfig), C.POINTER(_P)]),
@@ -235,10 +240,54 @@ class FitContext:
         self._check(self.lib.pg_guide_nll(self.h, _dptr(records_dev), n, C.byref(v), _stream_handle(stream)))
         return float(v.value)
 
+    def autotune(self, dirw, offsets, n_regions: int, mode: int = abi.PG_FIT_INIT, candidates=None, stream=None):
+        """pg_autotune_fit: times the candidate launch shapes (the built-in grid
+        when None) on these samples, keeps the fastest; states are preserved."""
+        best = abi.FitTuning()
+        ms = C.c_float()
+        if candidates:
+            arr = (abi.FitTuning * len(candidates))(*candidates)
+            cand, n = arr, len(candidates)
+        else:
+            cand, n = None, 0
+        self._check(self.lib.pg_autotune_fit(self.h, _dptr(dirw), _dptr(offsets), n_regions, mode, cand, n,
+                                             C.byref(best), C.byref(ms), _stream_handle(stream)))
+        return best, float(ms.value)
+
+    def capture_fit(self, dirw, offsets, n_regions: int, mode: int, stream) -> "FitGraph":
+        """pg_fit_graph_create: the fit captured as a CUDA graph on `stream`."""
+        g = C.c_void_p()
+        self._check(self.lib.pg_fit_graph_create(self.h, _dptr(dirw), _dptr(offsets), n_regions, mode,
+                                                 _stream_handle(stream), C.byref(g)))
+        return FitGraph(self.lib, g)
+
     def last_launch_count(self) -> int:
         n = C.c_uint32()
         self._check(self.lib.pg_last_launch_count(self.h, C.byref(n)))
         return int(n.value)
+
+
+class FitGraph:
+    """A captured fit (pg_fit_graph_*): launch() replays it on a stream."""
+
+    def __init__(self, lib, handle):
+        self.lib, self.h = lib, handle
+
+    def launch(self, stream=None):
+        st = self.lib.pg_fit_graph_launch(self.h, _stream_handle(stream))
+        if st != abi.PG_OK:
+            raise PathGuideError(st, self.lib.pg_last_error(None).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pg_fit_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Surrogate:
