@@ -296,7 +296,8 @@ struct DevRender {
     uint8_t *found;              // radiance reached the camera on this path
     pg_hit *hits;
     uint32_t *q_cur, *q_next;
-    uint32_t *counters;          // [0] next queue, [1] shadow queue, [2] ext rays, [3] shadow rays, [4] records
+    uint32_t *counters;          // [0] current queue, [1] next queue, [2] shadow queue, [4] records,
+                                 // [6] / [7] extension / shadow fetch positions
     // shadow queue
     float *sh_o, *sh_d, *sh_tmax, *sh_c, *sh_l;  // origin, dir, tmax, contribution (thr * L), radiance L
     uint32_t *sh_pix, *sh_nrec;
@@ -372,6 +373,8 @@ __global__ void k_camera(DevRender R) {
         R.counters[0] = W * H;
         R.counters[1] = 0;
         R.counters[2] = 0;
+        R.counters[6] = 0;  // extension and shadow fetch positions
+        R.counters[7] = 0;
     }
     if (R.recording) {
         R.rec_count[pix] = R.rec_start[pix];
@@ -383,24 +386,60 @@ __global__ void k_camera(DevRender R) {
 // Queue lengths live on the device (counters[0]: current queue, [1]: next
 // queue being appended, [2]: shadow queue); kernels are launched over all
 // pixels and threads past the length return, so a render needs no host sync.
+// Persistent closest-hit stage: warps stay resident and every lane whose ray
+// is finished takes the next queue entry (warp-aggregated fetch from
+// counters[6]), so a warp's lanes stay busy instead of waiting for its
+// slowest ray.  One BVH node per lane per loop trip (trav_step).
 // kCount: also add the traversal work to stats[2] (nodes) and stats[3] (triangles).
 template <bool kCount>
-__global__ void k_extend(DevRender R) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= R.counters[0]) return;
-    const uint32_t p = R.q_cur[i];
-    const float o[3] = {R.ro[3 * p], R.ro[3 * p + 1], R.ro[3 * p + 2]};
-    const float d[3] = {R.rd[3 * p], R.rd[3 * p + 1], R.rd[3 * p + 2]};
-    pg_hit h;
-    if constexpr (kCount) {
-        WorkCount c;
-        trace_closest(R.S, o, d, kTMin, kTMax, h, c);
-        atomicAdd(&R.stats[2], (unsigned long long)c.nodes);
-        atomicAdd(&R.stats[3], (unsigned long long)c.tris);
-    } else {
-        trace_closest(R.S, o, d, kTMin, kTMax, h);
+__global__ void __launch_bounds__(128) k_extend(DevRender R) {
+    const uint32_t n = R.counters[0];
+    const int lane = threadIdx.x & 31;
+    TravState st;
+    int stack[kStackSize];
+    WorkCount wc;
+    NoCount nc;
+    uint32_t p = 0;
+    bool have = false, exhausted = false;
+    for (;;) {
+        if (!exhausted) {
+            const unsigned need = __ballot_sync(0xffffffffu, !have);
+            if (need) {
+                const int leader = __ffs(need) - 1;
+                uint32_t base = 0;
+                if (lane == leader) base = atomicAdd(&R.counters[6], (uint32_t)__popc(need));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (!have) {
+                    const uint32_t idx = base + (uint32_t)__popc(need & ((1u << lane) - 1u));
+                    if (idx < n) {
+                        p = R.q_cur[idx];
+                        const float o[3] = {R.ro[3 * p], R.ro[3 * p + 1], R.ro[3 * p + 2]};
+                        const float d[3] = {R.rd[3 * p], R.rd[3 * p + 1], R.rd[3 * p + 2]};
+                        trav_begin<false>(R.S, st, o, d, kTMin, kTMax);
+                        have = true;
+                    }
+                }
+                if (base + (uint32_t)__popc(need) >= n) exhausted = true;  // warp-uniform
+            }
+        }
+        if (!__any_sync(0xffffffffu, have)) break;
+        if (have) {
+            const bool done = kCount ? trav_step<false>(R.S, st, stack, wc) : trav_step<false>(R.S, st, stack, nc);
+            if (done) {
+                pg_hit h;
+                h.t = st.tmax;
+                h.u = st.best_u;
+                h.v = st.best_v;
+                h.prim = st.best_id;
+                R.hits[p] = h;
+                have = false;
+            }
+        }
     }
-    R.hits[p] = h;
+    if (kCount) {
+        atomicAdd(&R.stats[2], (unsigned long long)wc.nodes);
+        atomicAdd(&R.stats[3], (unsigned long long)wc.tris);
+    }
 }
 
 __global__ void k_shade(DevRender R, int bounce, int last) {
@@ -654,29 +693,64 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
     warp_append(&R.counters[1], R.q_next, p, cont);
 }
 
-// kCount: also add the traversal work to stats[4] (nodes) and stats[5] (triangles).
-template <bool kCount>
-__global__ void k_shadow(DevRender R) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= R.counters[2]) return;
-    const float o[3] = {R.sh_o[3 * i], R.sh_o[3 * i + 1], R.sh_o[3 * i + 2]};
-    const float d[3] = {R.sh_d[3 * i], R.sh_d[3 * i + 1], R.sh_d[3 * i + 2]};
-    bool occluded;
-    if constexpr (kCount) {
-        WorkCount c;
-        occluded = trace_any(R.S, o, d, kTMin, R.sh_tmax[i], c);
-        atomicAdd(&R.stats[4], (unsigned long long)c.nodes);
-        atomicAdd(&R.stats[5], (unsigned long long)c.tris);
-    } else {
-        occluded = trace_any(R.S, o, d, kTMin, R.sh_tmax[i]);
-    }
-    if (occluded) return;
+// Unoccluded shadow ray i: its NEE contribution into the image and the
+// path's guiding records.
+__device__ __forceinline__ void shadow_finish(const DevRender &R, uint32_t i) {
     const uint32_t p = R.sh_pix[i];
     atomicAdd(&R.image[3 * p], R.sh_c[3 * i]);
     atomicAdd(&R.image[3 * p + 1], R.sh_c[3 * i + 1]);
     atomicAdd(&R.image[3 * p + 2], R.sh_c[3 * i + 2]);
     R.found[p] = 1;
     if (R.recording) update_records(R, p, R.sh_nrec[i], ld3(R.sh_l, i));
+}
+
+// Persistent any-hit stage over the shadow queue (fetch from counters[7]),
+// scheduled like k_extend.
+// kCount: also add the traversal work to stats[4] (nodes) and stats[5] (triangles).
+template <bool kCount>
+__global__ void __launch_bounds__(128) k_shadow(DevRender R) {
+    const uint32_t n = R.counters[2];
+    const int lane = threadIdx.x & 31;
+    TravState st;
+    int stack[kStackSize];
+    WorkCount wc;
+    NoCount nc;
+    uint32_t i = 0;
+    bool have = false, exhausted = false;
+    for (;;) {
+        if (!exhausted) {
+            const unsigned need = __ballot_sync(0xffffffffu, !have);
+            if (need) {
+                const int leader = __ffs(need) - 1;
+                uint32_t base = 0;
+                if (lane == leader) base = atomicAdd(&R.counters[7], (uint32_t)__popc(need));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (!have) {
+                    const uint32_t idx = base + (uint32_t)__popc(need & ((1u << lane) - 1u));
+                    if (idx < n) {
+                        i = idx;
+                        const float o[3] = {R.sh_o[3 * i], R.sh_o[3 * i + 1], R.sh_o[3 * i + 2]};
+                        const float d[3] = {R.sh_d[3 * i], R.sh_d[3 * i + 1], R.sh_d[3 * i + 2]};
+                        // a sphere in the way decides the query at once
+                        have = !trav_begin<true>(R.S, st, o, d, kTMin, R.sh_tmax[i]);
+                    }
+                }
+                if (base + (uint32_t)__popc(need) >= n) exhausted = true;  // warp-uniform
+            }
+        }
+        if (!__any_sync(0xffffffffu, have)) break;
+        if (have) {
+            const bool done = kCount ? trav_step<true>(R.S, st, stack, wc) : trav_step<true>(R.S, st, stack, nc);
+            if (done) {
+                if (st.best_id == PG_NO_HIT) shadow_finish(R, i);
+                have = false;
+            }
+        }
+    }
+    if (kCount) {
+        atomicAdd(&R.stats[4], (unsigned long long)wc.nodes);
+        atomicAdd(&R.stats[5], (unsigned long long)wc.tris);
+    }
 }
 
 // commitSamples (raytrace.rgen:980-990) and slot reuse when the path found no light
@@ -713,6 +787,8 @@ __global__ void k_advance(DevRender R) {
     R.counters[0] = R.counters[1];
     R.counters[1] = 0;
     R.counters[2] = 0;
+    R.counters[6] = 0;
+    R.counters[7] = 0;
 }
 
 __global__ void k_reset_records(pg_directional_data *rec, uint32_t n_slots, uint32_t *rec_start, uint32_t n_pix) {
@@ -780,6 +856,7 @@ struct pg_scene {
     float aabb[6] = {0, 0, 0, 0, 0, 0};
     // render scratch
     uint32_t cap_pix = 0;
+    uint32_t persist_blocks = 0;  // resident CTAs of the persistent traversal stages (all SMs)
     std::vector<void *> bufs;
     DevRender R{};
     uint32_t *d_counters = nullptr;
@@ -1200,6 +1277,16 @@ int pg_render(pg_scene *sc, const pg_render_params *rp, pg_ctx *guide, float *im
     if (!tm.init((rp->flags & PG_RENDER_TIME_STAGES) != 0, s)) return scene_error(PG_ERR_CUDA, "stage timer events");
     const uint32_t T = 128;
     const uint32_t G = (P + T - 1) / T;
+    if (sc->persist_blocks == 0) {
+        int dev = 0, sms = 0, b_ext = 0, b_sh = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b_ext, k_extend<false>, (int)T, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b_sh, k_shadow<false>, (int)T, 0);
+        sc->persist_blocks = (uint32_t)std::max(1, sms) * (uint32_t)std::max(1, std::min(b_ext, b_sh));
+    }
+    // persistent traversal grid: every SM full, never more CTAs than the full queue needs
+    const uint32_t GP = std::min(G, sc->persist_blocks);
     for (uint32_t smp = 0; smp < rp->spp; ++smp) {
         R.sample = smp;
         DevRender Rb = R;
@@ -1209,9 +1296,9 @@ int pg_render(pg_scene *sc, const pg_render_params *rp, pg_ctx *guide, float *im
         for (uint32_t b = 0; b < rp->max_depth; ++b) {
             tm.begin(PG_STAGE_EXTEND);
             if (count)
-                k_extend<true><<<G, T, 0, s>>>(Rb);
+                k_extend<true><<<GP, T, 0, s>>>(Rb);
             else
-                k_extend<false><<<G, T, 0, s>>>(Rb);
+                k_extend<false><<<GP, T, 0, s>>>(Rb);
             tm.end();
             const int last = (b + 1 == rp->max_depth) ? 1 : 0;
             tm.begin(PG_STAGE_SHADE);
@@ -1219,9 +1306,9 @@ int pg_render(pg_scene *sc, const pg_render_params *rp, pg_ctx *guide, float *im
             tm.end();
             tm.begin(PG_STAGE_SHADOW);
             if (count)
-                k_shadow<true><<<G, T, 0, s>>>(Rb);
+                k_shadow<true><<<GP, T, 0, s>>>(Rb);
             else
-                k_shadow<false><<<G, T, 0, s>>>(Rb);
+                k_shadow<false><<<GP, T, 0, s>>>(Rb);
             tm.end();
             tm.begin(PG_STAGE_ADVANCE);
             k_advance<<<1, 1, 0, s>>>(Rb);

@@ -162,130 +162,135 @@ struct WorkCount {
     __device__ __forceinline__ void tri() { ++tris; }
 };
 
+// Traversal state of one ray, advanced one BVH node per step, so a warp
+// whose lanes finish at different times can hand finished lanes new rays
+// (the persistent extension and shadow kernels).  The order of visits per
+// ray does not depend on how the steps are scheduled.
+struct TravState {
+    RayPre r;
+    float tmin, tmax;  // tmax: best t so far for closest-hit queries
+    float best_u, best_v;
+    uint32_t best_id;
+    int node, sp;
+};
+
+// Spheres first (closest: they set the initial best; any: a hit ends the
+// query), then the BVH from the root.  Returns true when the query is
+// already decided (any-hit occluded by a sphere).
+template <bool kAny>
+__device__ __forceinline__ bool trav_begin(const DevScene &S, TravState &st, const float o[3], const float d[3],
+                                           float tmin, float tmax) {
+    st.r = ray_setup(o, d);
+    st.tmin = tmin;
+    st.tmax = tmax;
+    st.best_u = st.best_v = 0.0f;
+    st.best_id = PG_NO_HIT;
+    st.node = 0;
+    st.sp = 0;
+    for (uint32_t i = 0; i < S.n_spheres; ++i) {
+        float t;
+        if (sphere_intersect(st.r, S.spheres[i], tmin, st.tmax, t)) {
+            if (kAny) {
+                st.best_id = PG_SPHERE_BIT | i;
+                return true;
+            }
+            st.tmax = t;
+            st.best_id = PG_SPHERE_BIT | i;
+        }
+    }
+    return false;
+}
+
+// One node of a closest-hit (kAny false) or any-hit (kAny true) traversal:
+// both child boxes, leaves tested at once, inner children visited near first
+// (closest) or first-child first (any).  Returns true when the traversal is
+// over; for any-hit, st.best_id != PG_NO_HIT then means occluded.
+template <bool kAny, class Ctr>
+__device__ __forceinline__ bool trav_step(const DevScene &S, TravState &st, int *stack, Ctr &ctr) {
+    const DevBvhNode n = S.nodes[st.node];
+    ctr.node();
+    const float e0 = box_enter(st.r, n.a.x, n.a.y, n.a.z, n.a.w, n.b.x, n.b.y, st.tmin, st.tmax);
+    const float e1 = box_enter(st.r, n.b.z, n.b.w, n.c.x, n.c.y, n.c.z, n.c.w, st.tmin, st.tmax);
+    int nn = 0;
+    int cand[2] = {-1, -1};
+    float ce[2] = {INFINITY, INFINITY};
+    for (int c = 0; c < 2; ++c) {
+        const float e = c == 0 ? e0 : e1;
+        if (e == INFINITY) continue;
+        const int child = c == 0 ? n.d.x : n.d.y;
+        const int count = c == 0 ? n.d.z : n.d.w;
+        if (count > 0) {
+            for (int k = 0; k < count; ++k) {
+                const uint32_t ti = (uint32_t)(child + k);
+                const float4 v0 = S.tris[3 * ti], v1 = S.tris[3 * ti + 1], v2 = S.tris[3 * ti + 2];
+                ctr.tri();
+                float t, u, v;
+                if (kAny) {
+                    if (tri_intersect(st.r, v0, v1, v2, st.tmin, st.tmax, t, u, v)) {
+                        st.best_id = __float_as_uint(v0.w);
+                        return true;
+                    }
+                } else {
+                    const uint32_t id = __float_as_uint(v0.w);
+                    // one ulp above the best t, so an equal t is seen and the lower id wins
+                    const float lim =
+                        st.best_id == PG_NO_HIT ? st.tmax : __uint_as_float(__float_as_uint(st.tmax) + 1u);
+                    if (tri_intersect(st.r, v0, v1, v2, st.tmin, lim, t, u, v) &&
+                        (t < st.tmax || (t == st.tmax && id < st.best_id))) {
+                        st.tmax = t;
+                        st.best_id = id;
+                        st.best_u = u;
+                        st.best_v = v;
+                    }
+                }
+            }
+        } else if (child >= 0) {
+            cand[nn] = child;
+            ce[nn] = e;
+            ++nn;
+        }
+    }
+    if (nn == 2) {
+        const int first = kAny ? 0 : (ce[1] < ce[0] ? 1 : 0);
+        if (st.sp < kStackSize) stack[st.sp++] = cand[1 - first];
+        st.node = cand[first];
+        return false;
+    }
+    if (nn == 1) {
+        st.node = cand[0];
+        return false;
+    }
+    if (st.sp == 0) return true;
+    st.node = stack[--st.sp];
+    return false;
+}
+
 // Closest hit.  Returns false if nothing is hit in (tmin, tmax).
 template <class Ctr = NoCount>
 __device__ __forceinline__ bool trace_closest(const DevScene &S, const float o[3], const float d[3], float tmin,
                                               float tmax, pg_hit &hit, Ctr &&ctr = Ctr()) {
-    const RayPre r = ray_setup(o, d);
-    float best_t = tmax;
-    uint32_t best_id = PG_NO_HIT;
-    float best_u = 0.0f, best_v = 0.0f;
-    for (uint32_t i = 0; i < S.n_spheres; ++i) {
-        float t;
-        if (sphere_intersect(r, S.spheres[i], tmin, best_t, t)) {
-            best_t = t;
-            best_id = PG_SPHERE_BIT | i;
-        }
-    }
+    TravState st;
     int stack[kStackSize];
-    int sp = 0;
-    int node = 0;
-    for (;;) {
-        const DevBvhNode n = S.nodes[node];
-        ctr.node();
-        const float e0 = box_enter(r, n.a.x, n.a.y, n.a.z, n.a.w, n.b.x, n.b.y, tmin, best_t);
-        const float e1 = box_enter(r, n.b.z, n.b.w, n.c.x, n.c.y, n.c.z, n.c.w, tmin, best_t);
-        int nn = 0;
-        // leaves are tested immediately; inner children are visited near first
-        int cand[2] = {-1, -1};
-        float ce[2] = {INFINITY, INFINITY};
-        for (int c = 0; c < 2; ++c) {
-            const float e = c == 0 ? e0 : e1;
-            if (e == INFINITY) continue;
-            const int child = c == 0 ? n.d.x : n.d.y;
-            const int count = c == 0 ? n.d.z : n.d.w;
-            if (count > 0) {
-                for (int k = 0; k < count; ++k) {
-                    const uint32_t ti = (uint32_t)(child + k);
-                    const float4 v0 = S.tris[3 * ti], v1 = S.tris[3 * ti + 1], v2 = S.tris[3 * ti + 2];
-                    ctr.tri();
-                    float t, u, v;
-                    const uint32_t id = __float_as_uint(v0.w);
-                    // one ulp above the best t, so an equal t is seen and the lower id wins
-                    const float lim = best_id == PG_NO_HIT ? best_t : __uint_as_float(__float_as_uint(best_t) + 1u);
-                    if (tri_intersect(r, v0, v1, v2, tmin, lim, t, u, v) &&
-                        (t < best_t || (t == best_t && id < best_id))) {
-                        best_t = t;
-                        best_id = id;
-                        best_u = u;
-                        best_v = v;
-                    }
-                }
-            } else if (child >= 0) {
-                cand[nn] = child;
-                ce[nn] = e;
-                ++nn;
-            }
-        }
-        if (nn == 2) {
-            const int near_i = ce[1] < ce[0] ? 1 : 0;
-            if (sp < kStackSize) stack[sp++] = cand[1 - near_i];
-            node = cand[near_i];
-            continue;
-        }
-        if (nn == 1) {
-            node = cand[0];
-            continue;
-        }
-        if (sp == 0) break;
-        node = stack[--sp];
+    trav_begin<false>(S, st, o, d, tmin, tmax);
+    while (!trav_step<false>(S, st, stack, ctr)) {
     }
-    hit.t = best_t;
-    hit.u = best_u;
-    hit.v = best_v;
-    hit.prim = best_id;
-    return best_id != PG_NO_HIT;
+    hit.t = st.tmax;
+    hit.u = st.best_u;
+    hit.v = st.best_v;
+    hit.prim = st.best_id;
+    return st.best_id != PG_NO_HIT;
 }
 
 // Any hit in (tmin, tmax).
 template <class Ctr = NoCount>
 __device__ __forceinline__ bool trace_any(const DevScene &S, const float o[3], const float d[3], float tmin,
                                           float tmax, Ctr &&ctr = Ctr()) {
-    const RayPre r = ray_setup(o, d);
-    for (uint32_t i = 0; i < S.n_spheres; ++i) {
-        float t;
-        if (sphere_intersect(r, S.spheres[i], tmin, tmax, t)) return true;
-    }
+    TravState st;
     int stack[kStackSize];
-    int sp = 0;
-    int node = 0;
-    for (;;) {
-        const DevBvhNode n = S.nodes[node];
-        ctr.node();
-        const float e0 = box_enter(r, n.a.x, n.a.y, n.a.z, n.a.w, n.b.x, n.b.y, tmin, tmax);
-        const float e1 = box_enter(r, n.b.z, n.b.w, n.c.x, n.c.y, n.c.z, n.c.w, tmin, tmax);
-        int cand[2];
-        int nn = 0;
-        for (int c = 0; c < 2; ++c) {
-            const float e = c == 0 ? e0 : e1;
-            if (e == INFINITY) continue;
-            const int child = c == 0 ? n.d.x : n.d.y;
-            const int count = c == 0 ? n.d.z : n.d.w;
-            if (count > 0) {
-                for (int k = 0; k < count; ++k) {
-                    const uint32_t ti = (uint32_t)(child + k);
-                    float t, u, v;
-                    ctr.tri();
-                    if (tri_intersect(r, S.tris[3 * ti], S.tris[3 * ti + 1], S.tris[3 * ti + 2], tmin, tmax, t, u, v))
-                        return true;
-                }
-            } else if (child >= 0) {
-                cand[nn++] = child;
-            }
-        }
-        if (nn == 2) {
-            if (sp < kStackSize) stack[sp++] = cand[1];
-            node = cand[0];
-            continue;
-        }
-        if (nn == 1) {
-            node = cand[0];
-            continue;
-        }
-        if (sp == 0) break;
-        node = stack[--sp];
+    if (trav_begin<true>(S, st, o, d, tmin, tmax)) return true;
+    while (!trav_step<true>(S, st, stack, ctr)) {
     }
-    return false;
+    return st.best_id != PG_NO_HIT;
 }
 
 }  // namespace pg
