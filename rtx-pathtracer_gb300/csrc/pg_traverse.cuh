@@ -207,7 +207,12 @@ __device__ __forceinline__ bool trav_begin(const DevScene &S, TravState &st, con
 // over; for any-hit, st.best_id != PG_NO_HIT then means occluded.
 template <bool kAny, class Ctr>
 __device__ __forceinline__ bool trav_step(const DevScene &S, TravState &st, int *stack, Ctr &ctr) {
-    const DevBvhNode n = S.nodes[st.node];
+    // read-only path: the scene never changes during a launch
+    DevBvhNode n;
+    n.a = __ldg(&S.nodes[st.node].a);
+    n.b = __ldg(&S.nodes[st.node].b);
+    n.c = __ldg(&S.nodes[st.node].c);
+    n.d = __ldg(&S.nodes[st.node].d);
     ctr.node();
     const float e0 = box_enter(st.r, n.a.x, n.a.y, n.a.z, n.a.w, n.b.x, n.b.y, st.tmin, st.tmax);
     const float e1 = box_enter(st.r, n.b.z, n.b.w, n.c.x, n.c.y, n.c.z, n.c.w, st.tmin, st.tmax);
@@ -222,7 +227,8 @@ __device__ __forceinline__ bool trav_step(const DevScene &S, TravState &st, int 
         if (count > 0) {
             for (int k = 0; k < count; ++k) {
                 const uint32_t ti = (uint32_t)(child + k);
-                const float4 v0 = S.tris[3 * ti], v1 = S.tris[3 * ti + 1], v2 = S.tris[3 * ti + 2];
+                const float4 v0 = __ldg(&S.tris[3 * ti]), v1 = __ldg(&S.tris[3 * ti + 1]),
+                             v2 = __ldg(&S.tris[3 * ti + 2]);
                 ctr.tri();
                 float t, u, v;
                 if (kAny) {

@@ -671,7 +671,9 @@ uint32_t bsdf_material(SceneData &s, const XNode &b) {
     }
     const std::string type = bb->attr.count("type") ? bb->attr.at("type") : "diffuse";
     if (type == "dielectric" || type == "thindielectric")
-        return add_material(s, PG_MAT_DIELECTRIC, v3(1, 1, 1), v3(0, 0, 0), 0, read_float(*bb, "intIOR", 1.5f));
+        // refractionIndex = intIOR / extIOR (src/SceneLoader.cpp:590)
+        return add_material(s, PG_MAT_DIELECTRIC, v3(1, 1, 1), v3(0, 0, 0), 0,
+                            read_float(*bb, "intIOR", 1.5f) / read_float(*bb, "extIOR", 1.0f));
     if (type == "conductor")
         return add_material(s, PG_MAT_SPECULAR, read_rgb(*bb, "specularReflectance", v3(1, 1, 1)), v3(0, 0, 0), 0, 1);
     if (type == "roughconductor" || type == "roughplastic")
@@ -712,7 +714,9 @@ bool load_mitsuba(SceneData &s, const std::string &path, uint32_t width, uint32_
     if (const XNode *sensor = scene->child("sensor")) {
         s.camera.vfov_deg = read_float(*sensor, "fov", 45.0f);
         if (const XNode *tw = sensor->child("transform")) {
-            if (const XNode *la = tw->child("lookat")) {
+            // both spellings, as src/SceneLoader.cpp:620-622 accepts
+            const XNode *la = tw->child("lookAt") ? tw->child("lookAt") : tw->child("lookat");
+            if (la) {
                 float o[3], t[3], u[3];
                 if (la->attr.count("origin") && parse_floats(la->attr.at("origin"), o, 3) && la->attr.count("target") &&
                     parse_floats(la->attr.at("target"), t, 3)) {

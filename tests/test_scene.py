@@ -170,7 +170,7 @@ MITSUBA = """<?xml version="1.0" encoding="utf-8"?>
   <sensor type="perspective">
     <float name="fov" value="40"/>
     <transform name="toWorld">
-      <lookat origin="0, 1, 6" target="0, 1, 0" up="0, 1, 0"/>
+      <lookAt origin="0, 1, 6" target="0, 1, 0" up="0, 1, 0"/>
     </transform>
   </sensor>
   <bsdf type="twosided" id="white">
@@ -188,7 +188,7 @@ MITSUBA = """<?xml version="1.0" encoding="utf-8"?>
   <shape type="sphere">
     <point name="center" x="1" y="2" z="0"/>
     <float name="radius" value="0.25"/>
-    <bsdf type="dielectric"><float name="intIOR" value="1.33"/></bsdf>
+    <bsdf type="dielectric"><float name="intIOR" value="1.596"/><float name="extIOR" value="1.2"/></bsdf>
   </shape>
   <shape type="rectangle">
     <transform name="toWorld"><translate x="0" y="3" z="0"/></transform>
@@ -221,7 +221,7 @@ def test_mitsuba_loader(pkg, abi, tmp_path):
     by_type = {int(t): m for t, m in zip(mats["type"], mats)}
     assert np.allclose(by_type[abi.PG_MAT_DIFFUSE]["albedo"], [0.7, 0.6, 0.5])
     assert abs(by_type[abi.PG_MAT_GGX]["roughness"] - 0.2) < 1e-7
-    assert abs(by_type[abi.PG_MAT_DIELECTRIC]["ior"] - 1.33) < 1e-6
+    assert abs(by_type[abi.PG_MAT_DIELECTRIC]["ior"] - 1.596 / 1.2) < 1e-6  # intIOR / extIOR
     assert np.allclose(by_type[abi.PG_MAT_LIGHT]["emission"], [10, 9, 8])
     assert np.allclose(exp["spheres"]["center"][0], [1, 2, 0]) and abs(exp["spheres"]["radius"][0] - 0.25) < 1e-7
     # the unit cube scaled by 0.5 and lifted by 0.5 spans [-0.5, 0.5] x [0, 1] x [-0.5, 0.5]
