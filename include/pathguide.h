@@ -421,7 +421,7 @@ int pg_scene_create_cornell(const pg_cornell_params *p, pg_scene **out);
 int pg_scene_create_plates(const pg_plates_params *p, pg_scene **out);
 int pg_scene_destroy(pg_scene *scene);
 int pg_scene_get_info(const pg_scene *scene, pg_scene_info *out);
-/* Host copies of the built scene: BVH nodes (64 B each), triangles in BVH
+/* Host copies of the built scene: BVH nodes (128 B each, four-wide), triangles in BVH
  * order (12 floats each), their original ids, per-triangle materials, the
  * materials and the spheres.  Any pointer may be NULL. */
 int pg_scene_export(const pg_scene *scene, void *nodes, float *tri_verts, uint32_t *tri_order,
@@ -433,7 +433,7 @@ int pg_scene_export_mesh(const pg_scene *scene, float *positions, uint32_t *indi
  * and the image size. */
 int pg_scene_set_camera(pg_scene *scene, const pg_camera *cam);
 
-/* Closest hit / any hit of n rays (device arrays).  Traversal: two-wide BVH,
+/* Closest hit / any hit of n rays (device arrays).  Traversal: four-wide BVH,
  * near child first, watertight FP32 ray-triangle test (Woop, Benthin and
  * Wald 2013); ties in t go to the lower triangle id. */
 int pg_trace_closest(pg_scene *scene, const pg_ray *rays, uint32_t n, pg_hit *hits, void *stream);

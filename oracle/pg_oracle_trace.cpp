@@ -13,12 +13,15 @@
 
 namespace {
 
+// four-wide node: child boxes slot-major per coordinate (the library's BvhNode)
 struct Node {
-    float lo0[3], hi0[3], lo1[3], hi1[3];
-    int32_t child[2];
-    int32_t count[2];
+    float lo[3][4];
+    float hi[3][4];
+    int32_t child[4];
+    int32_t count[4];
 };
-static_assert(sizeof(Node) == 64, "node layout");
+static_assert(sizeof(Node) == 128, "node layout");
+constexpr int kStack = 128;  // the device's stack depth; a full stack drops the push there too
 
 // ---------------------------------------------------------------------------
 // FP32 twin of the device traversal (pg_traverse.cuh), same operation order
@@ -127,6 +130,71 @@ float bitsf(uint32_t u) {
     return f;
 }
 
+// One node step of the device traversal (trav_step in pg_traverse.cuh), same
+// order: four box tests against the best t at the start of the step, leaves
+// in slot order, inner children nearest first (closest: stable by entry
+// distance; any: slot order).  Returns true when the traversal is over.
+template <bool kAny>
+bool node_step(const pgo_scene &S, const RayPre &r, float tmin, float &best_t, uint32_t &best_id, float &best_u,
+               float &best_v, int &node, int *stack, int &sp, uint32_t &n_nodes, uint32_t &n_tris) {
+    const Node &n = ((const Node *)S.nodes)[node];
+    ++n_nodes;
+    float e[4];
+    for (int j = 0; j < 4; ++j) {
+        const float lo[3] = {n.lo[0][j], n.lo[1][j], n.lo[2][j]}, hi[3] = {n.hi[0][j], n.hi[1][j], n.hi[2][j]};
+        e[j] = box_enter(r, lo, hi, tmin, best_t);
+    }
+    for (int j = 0; j < 4; ++j) {
+        if (e[j] == INFINITY || n.count[j] <= 0) continue;
+        for (int k = 0; k < n.count[j]; ++k) {
+            const float *tv = S.tri_verts + 12 * (size_t)(n.child[j] + k);
+            ++n_tris;
+            float t, u, v;
+            if (kAny) {
+                if (tri_intersect(r, tv, tv + 4, tv + 8, tmin, best_t, t, u, v)) {
+                    best_id = fbits(tv[3]);
+                    return true;
+                }
+            } else {
+                const uint32_t id = fbits(tv[3]);
+                const float lim = best_id == PG_NO_HIT ? best_t : bitsf(fbits(best_t) + 1u);
+                if (tri_intersect(r, tv, tv + 4, tv + 8, tmin, lim, t, u, v) &&
+                    (t < best_t || (t == best_t && id < best_id))) {
+                    best_t = t;
+                    best_id = id;
+                    best_u = u;
+                    best_v = v;
+                }
+            }
+        }
+    }
+    int cand[4];
+    float ce[4];
+    int nn = 0;
+    for (int j = 0; j < 4; ++j) {
+        if (e[j] == INFINITY || n.count[j] > 0 || n.child[j] < 0) continue;
+        int pos = nn;
+        if (!kAny)
+            while (pos > 0 && ce[pos - 1] > e[j]) {
+                ce[pos] = ce[pos - 1];
+                cand[pos] = cand[pos - 1];
+                --pos;
+            }
+        ce[pos] = e[j];
+        cand[pos] = n.child[j];
+        ++nn;
+    }
+    if (nn > 0) {
+        for (int q = nn - 1; q >= 1; --q)
+            if (sp < kStack) stack[sp++] = cand[q];
+        node = cand[0];
+        return false;
+    }
+    if (sp == 0) return true;
+    node = stack[--sp];
+    return false;
+}
+
 // cnt (optional): [0] BVH nodes fetched, [1] triangles tested
 void closest32(const pgo_scene &S, const pg_ray &ray, pg_hit &hit, uint32_t *cnt = nullptr) {
     uint32_t n_nodes = 0, n_tris = 0;
@@ -140,52 +208,9 @@ void closest32(const pgo_scene &S, const pg_ray &ray, pg_hit &hit, uint32_t *cnt
             best_id = PG_SPHERE_BIT | i;
         }
     }
-    const Node *nodes = (const Node *)S.nodes;
-    std::vector<int> stack;
-    stack.reserve(64);
-    int node = 0;
-    for (;;) {
-        const Node &n = nodes[node];
-        ++n_nodes;
-        const float e[2] = {box_enter(r, n.lo0, n.hi0, ray.tmin, best_t), box_enter(r, n.lo1, n.hi1, ray.tmin, best_t)};
-        int cand[2], nn = 0;
-        float ce[2];
-        for (int c = 0; c < 2; ++c) {
-            if (e[c] == INFINITY) continue;
-            if (n.count[c] > 0) {
-                for (int k = 0; k < n.count[c]; ++k) {
-                    const float *tv = S.tri_verts + 12 * (size_t)(n.child[c] + k);
-                    const uint32_t id = fbits(tv[3]);
-                    ++n_tris;
-                    const float lim = best_id == PG_NO_HIT ? best_t : bitsf(fbits(best_t) + 1u);
-                    float t, u, v;
-                    if (tri_intersect(r, tv, tv + 4, tv + 8, ray.tmin, lim, t, u, v) &&
-                        (t < best_t || (t == best_t && id < best_id))) {
-                        best_t = t;
-                        best_id = id;
-                        best_u = u;
-                        best_v = v;
-                    }
-                }
-            } else if (n.child[c] >= 0) {
-                cand[nn] = n.child[c];
-                ce[nn] = e[c];
-                ++nn;
-            }
-        }
-        if (nn == 2) {
-            const int near_i = ce[1] < ce[0] ? 1 : 0;
-            stack.push_back(cand[1 - near_i]);
-            node = cand[near_i];
-            continue;
-        }
-        if (nn == 1) {
-            node = cand[0];
-            continue;
-        }
-        if (stack.empty()) break;
-        node = stack.back();
-        stack.pop_back();
+    int stack[kStack];
+    int sp = 0, node = 0;
+    while (!node_step<false>(S, r, ray.tmin, best_t, best_id, best_u, best_v, node, stack, sp, n_nodes, n_tris)) {
     }
     hit.t = best_t;
     hit.u = best_u;
@@ -203,39 +228,13 @@ bool any32(const pgo_scene &S, const pg_ray &ray) {
         float t;
         if (sphere_intersect(r, S.spheres[i], ray.tmin, ray.tmax, t)) return true;
     }
-    const Node *nodes = (const Node *)S.nodes;
-    std::vector<int> stack;
-    int node = 0;
-    for (;;) {
-        const Node &n = nodes[node];
-        const float e[2] = {box_enter(r, n.lo0, n.hi0, ray.tmin, ray.tmax), box_enter(r, n.lo1, n.hi1, ray.tmin, ray.tmax)};
-        int cand[2], nn = 0;
-        for (int c = 0; c < 2; ++c) {
-            if (e[c] == INFINITY) continue;
-            if (n.count[c] > 0) {
-                for (int k = 0; k < n.count[c]; ++k) {
-                    const float *tv = S.tri_verts + 12 * (size_t)(n.child[c] + k);
-                    float t, u, v;
-                    if (tri_intersect(r, tv, tv + 4, tv + 8, ray.tmin, ray.tmax, t, u, v)) return true;
-                }
-            } else if (n.child[c] >= 0) {
-                cand[nn++] = n.child[c];
-            }
-        }
-        if (nn == 2) {
-            stack.push_back(cand[1]);
-            node = cand[0];
-            continue;
-        }
-        if (nn == 1) {
-            node = cand[0];
-            continue;
-        }
-        if (stack.empty()) break;
-        node = stack.back();
-        stack.pop_back();
+    float best_t = ray.tmax, best_u = 0, best_v = 0;
+    uint32_t best_id = PG_NO_HIT, n_nodes = 0, n_tris = 0;
+    int stack[kStack];
+    int sp = 0, node = 0;
+    while (!node_step<true>(S, r, ray.tmin, best_t, best_id, best_u, best_v, node, stack, sp, n_nodes, n_tris)) {
     }
-    return false;
+    return best_id != PG_NO_HIT;
 }
 
 template <typename F>
@@ -389,8 +388,9 @@ Hit64 intersect64(const pgo_scene &S, D3 o, D3 d, double tmin, double tmax, bool
     stack[sp++] = 0;
     while (sp) {
         const Node &n = nodes[stack[--sp]];
-        for (int c = 0; c < 2; ++c) {
-            const float *lo = c == 0 ? n.lo0 : n.lo1, *hi = c == 0 ? n.hi0 : n.hi1;
+        for (int c = 0; c < 4; ++c) {
+            if (n.count[c] <= 0 && n.child[c] < 0) continue;  // empty slot
+            const float lo[3] = {n.lo[0][c], n.lo[1][c], n.lo[2][c]}, hi[3] = {n.hi[0][c], n.hi[1][c], n.hi[2][c]};
             if (!box64(o, inv, lo, hi, tmin, h.t)) continue;
             if (n.count[c] > 0) {
                 for (int k = 0; k < n.count[c]; ++k) {

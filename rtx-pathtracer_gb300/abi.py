@@ -81,10 +81,9 @@ MATERIAL_DTYPE = np.dtype([("type", "<i4"), ("albedo", "<f4", (3,)), ("emission"
 SPHERE_DTYPE = np.dtype([("center", "<f4", (3,)), ("radius", "<f4"), ("material", "<u4"), ("reserved", "<u4", (3,))])
 RAY_DTYPE = np.dtype([("org", "<f4", (3,)), ("tmin", "<f4"), ("dir", "<f4", (3,)), ("tmax", "<f4")])
 HIT_DTYPE = np.dtype([("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("prim", "<u4")])
-NODE_DTYPE = np.dtype([("lo0", "<f4", (3,)), ("hi0", "<f4", (3,)), ("lo1", "<f4", (3,)), ("hi1", "<f4", (3,)),
-                       ("child", "<i4", (2,)), ("count", "<i4", (2,))])
+NODE_DTYPE = np.dtype([("lo", "<f4", (3, 4)), ("hi", "<f4", (3, 4)), ("child", "<i4", (4,)), ("count", "<i4", (4,))])
 assert MATERIAL_DTYPE.itemsize == 48 and SPHERE_DTYPE.itemsize == 32 and RAY_DTYPE.itemsize == 32
-assert HIT_DTYPE.itemsize == 16 and NODE_DTYPE.itemsize == 64
+assert HIT_DTYPE.itemsize == 16 and NODE_DTYPE.itemsize == 128
 
 
 class Camera(C.Structure):

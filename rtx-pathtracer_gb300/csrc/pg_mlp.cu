@@ -18,9 +18,10 @@
 //   k_wgrad     weight gradients dW = D^T X as tensor-core GEMMs over the
 //               batch (split over row blocks, one layer per grid row), bias
 //               gradients by column sums; per-block partials
-//   k_sum_scalars, k_reduce_adam
+//   k_reduce_adam
 //               partials -> gradient / sum(w) -> Adam -> FP32 masters and the
-//               BF16 weight copy the next step reads.
+//               BF16 weight copy the next step reads (the loss and weight sums
+//               are formed by the first weight-gradient block).
 #include <cuda_bf16.h>
 #include <math.h>
 #include <string.h>
@@ -181,7 +182,7 @@ struct FwdArgs {
 
 // kTrain: loss, gradients and scratch; otherwise mixture parameters.
 template <bool kTrain>
-__global__ void __launch_bounds__(32 * kWarps) k_fwd_bwd(FwdArgs A) {
+__global__ void __launch_bounds__(32 * kWarps, 3) k_fwd_bwd(FwdArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Shared &S = *reinterpret_cast<Shared *>(smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
@@ -393,7 +394,34 @@ struct WgradArgs {
     uint32_t rows;        // padded batch rows (multiple of 16)
     uint32_t rows_per_block;
     float *partials;      // gridDim.x x NPARAM
+    const float *fwd_partials;  // per-warp {sum w (-log q), sum w} of the forward kernel
+    uint32_t n_fwd_partials;
+    double *scalars;      // their sums (written by block (0, 0))
 };
+
+// Block-wide sums of the forward kernel's per-warp partials (one block).
+__device__ void sum_fwd_partials(const WgradArgs &A) {
+    __shared__ double sl[32 * kWarps], sw[32 * kWarps];
+    double l = 0.0, w = 0.0;
+    for (uint32_t i = threadIdx.x; i < A.n_fwd_partials; i += blockDim.x) {
+        l += A.fwd_partials[2 * i];
+        w += A.fwd_partials[2 * i + 1];
+    }
+    sl[threadIdx.x] = l;
+    sw[threadIdx.x] = w;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if ((int)threadIdx.x < st) {
+            sl[threadIdx.x] += sl[threadIdx.x + st];
+            sw[threadIdx.x] += sw[threadIdx.x + st];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        A.scalars[0] = sl[0];
+        A.scalars[1] = sw[0];
+    }
+}
 
 template <int O, int I>
 __device__ __forceinline__ void wgrad_layer(const WgradArgs &A, int dcol, int xcol, int wofs, int bofs) {
@@ -463,35 +491,12 @@ __device__ __forceinline__ void wgrad_layer(const WgradArgs &A, int dcol, int xc
 }
 
 __global__ void __launch_bounds__(32 * kWarps) k_wgrad(WgradArgs A) {
+    if (blockIdx.x == 0 && blockIdx.y == 0) sum_fwd_partials(A);
     switch (blockIdx.y) {
         case 0: wgrad_layer<NH, NIN>(A, RD1, RA0, OW1, OB1); break;
         case 1: wgrad_layer<NH, NH>(A, RD2, RH1, OW2, OB2); break;
         case 2: wgrad_layer<NH, NH>(A, RD3, RH2, OW3, OB3); break;
         default: wgrad_layer<NOUT, NH>(A, RDO, RH3, OW4, OB4); break;
-    }
-}
-
-// sums of the forward kernel's per-CTA {loss, weight} partials (one block)
-__global__ void k_sum_scalars(const float *partials, uint32_t n, double *out) {
-    __shared__ double sl[256], sw[256];
-    double l = 0.0, w = 0.0;
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-        l += partials[2 * i];
-        w += partials[2 * i + 1];
-    }
-    sl[threadIdx.x] = l;
-    sw[threadIdx.x] = w;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if ((int)threadIdx.x < s) {
-            sl[threadIdx.x] += sl[threadIdx.x + s];
-            sw[threadIdx.x] += sw[threadIdx.x + s];
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        out[0] = sl[0];
-        out[1] = sw[0];
     }
 }
 
@@ -714,8 +719,10 @@ int batch_gradients(pg_mlp *M, const pg_directional_data *rec, uint32_t n, uint3
     W.rows_per_block = ((rows / 16 + blocks - 1) / blocks) * 16;
     const uint32_t used = (rows + W.rows_per_block - 1) / W.rows_per_block;
     W.partials = M->wg_partials;
+    W.fwd_partials = M->fwd_partials;
+    W.n_fwd_partials = ctas * kWarps;
+    W.scalars = M->scalars + 2 * slot;
     k_wgrad<<<dim3(used, 4), 32 * kWarps, 0, s>>>(W);
-    k_sum_scalars<<<1, 256, 0, s>>>(M->fwd_partials, ctas * kWarps, M->scalars + 2 * slot);
     if (cudaGetLastError() != cudaSuccess) return mlp_error(PG_ERR_CUDA, "surrogate gradient launch");
     M->wg_used = used;
     return PG_OK;

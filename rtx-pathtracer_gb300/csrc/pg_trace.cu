@@ -956,14 +956,9 @@ void build_host(pg_scene *sc) {
 int ensure_uploaded(pg_scene *sc) {
     if (sc->uploaded) return PG_OK;
     const SceneData &s = sc->host;
+    static_assert(sizeof(DevBvhNode) == sizeof(BvhNode), "host and device nodes share one layout");
     std::vector<DevBvhNode> dn(s.nodes.size());
-    for (size_t i = 0; i < s.nodes.size(); ++i) {
-        const BvhNode &n = s.nodes[i];
-        dn[i].a = make_float4(n.lo0[0], n.lo0[1], n.lo0[2], n.hi0[0]);
-        dn[i].b = make_float4(n.hi0[1], n.hi0[2], n.lo1[0], n.lo1[1]);
-        dn[i].c = make_float4(n.lo1[2], n.hi1[0], n.hi1[1], n.hi1[2]);
-        dn[i].d = make_int4(n.child[0], n.child[1], n.count[0], n.count[1]);
-    }
+    memcpy(dn.data(), s.nodes.data(), sizeof(BvhNode) * s.nodes.size());
     std::vector<float4> tv(s.tri_verts.size() / 4);
     memcpy(tv.data(), s.tri_verts.data(), sizeof(float) * s.tri_verts.size());
     int st = upload(&sc->d_nodes, dn);

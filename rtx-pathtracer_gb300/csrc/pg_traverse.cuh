@@ -1,6 +1,6 @@
 // pg_traverse.cuh - BVH traversal and ray-primitive tests on the device.
 //
-// Closest hit and any hit over the two-wide BVH of host/pg_scene.cpp.  The
+// Closest hit and any hit over the four-wide BVH of host/pg_scene.cpp.  The
 // triangle test is the watertight algorithm of Woop, Benthin and Wald (JCGT
 // 2013).  Every product, sum and quotient of the triangle and box tests is an
 // explicit round-to-nearest operation (__fmul_rn, __fadd_rn, __fdiv_rn, ...),
@@ -16,12 +16,14 @@
 
 namespace pg {
 
+// Four-wide node (the host BvhNode): child boxes slot-major per coordinate.
 struct DevBvhNode {
-    float4 a;  // lo0.xyz, hi0.x
-    float4 b;  // hi0.yz, lo1.xy
-    float4 c;  // lo1.z, hi1.xyz
-    int4 d;    // child0, child1, count0, count1
+    float4 lox, loy, loz;
+    float4 hix, hiy, hiz;
+    int4 child;
+    int4 count;
 };
+static_assert(sizeof(DevBvhNode) == 128, "node layout");
 
 struct DevScene {
     const DevBvhNode *nodes;
@@ -148,7 +150,10 @@ __device__ __forceinline__ bool sphere_intersect(const RayPre &r, const pg_spher
     return false;
 }
 
-constexpr int kStackSize = 64;
+// Deep enough for any tree the builder makes (depth <= 60 binary levels, at
+// most three pushes per four-wide level); a full stack drops the push, which
+// the CPU twin does identically.
+constexpr int kStackSize = 128;
 
 // Work counters of one traversal: NoCount compiles to nothing; WorkCount
 // tallies the BVH nodes fetched and the triangles tested.
@@ -201,68 +206,76 @@ __device__ __forceinline__ bool trav_begin(const DevScene &S, TravState &st, con
     return false;
 }
 
+__device__ __forceinline__ float f4(const float4 &v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w)); }
+__device__ __forceinline__ int i4(const int4 &v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w)); }
+
 // One node of a closest-hit (kAny false) or any-hit (kAny true) traversal:
-// both child boxes, leaves tested at once, inner children visited near first
-// (closest) or first-child first (any).  Returns true when the traversal is
-// over; for any-hit, st.best_id != PG_NO_HIT then means occluded.
+// the four child boxes against the best t at the start of the step, leaf
+// children tested in slot order, inner children visited nearest first
+// (closest: entry distance, ties by slot; any: slot order), the others pushed
+// so the next nearest is on top.  Returns true when the traversal is over; for
+// any-hit, st.best_id != PG_NO_HIT then means occluded.
 template <bool kAny, class Ctr>
 __device__ __forceinline__ bool trav_step(const DevScene &S, TravState &st, int *stack, Ctr &ctr) {
     // read-only path: the scene never changes during a launch
-    DevBvhNode n;
-    n.a = __ldg(&S.nodes[st.node].a);
-    n.b = __ldg(&S.nodes[st.node].b);
-    n.c = __ldg(&S.nodes[st.node].c);
-    n.d = __ldg(&S.nodes[st.node].d);
+    const DevBvhNode *np = S.nodes + st.node;
+    const float4 lox = __ldg(&np->lox), loy = __ldg(&np->loy), loz = __ldg(&np->loz);
+    const float4 hix = __ldg(&np->hix), hiy = __ldg(&np->hiy), hiz = __ldg(&np->hiz);
+    const int4 child = __ldg(&np->child), count = __ldg(&np->count);
     ctr.node();
-    const float e0 = box_enter(st.r, n.a.x, n.a.y, n.a.z, n.a.w, n.b.x, n.b.y, st.tmin, st.tmax);
-    const float e1 = box_enter(st.r, n.b.z, n.b.w, n.c.x, n.c.y, n.c.z, n.c.w, st.tmin, st.tmax);
-    int nn = 0;
-    int cand[2] = {-1, -1};
-    float ce[2] = {INFINITY, INFINITY};
-    for (int c = 0; c < 2; ++c) {
-        const float e = c == 0 ? e0 : e1;
-        if (e == INFINITY) continue;
-        const int child = c == 0 ? n.d.x : n.d.y;
-        const int count = c == 0 ? n.d.z : n.d.w;
-        if (count > 0) {
-            for (int k = 0; k < count; ++k) {
-                const uint32_t ti = (uint32_t)(child + k);
-                const float4 v0 = __ldg(&S.tris[3 * ti]), v1 = __ldg(&S.tris[3 * ti + 1]),
-                             v2 = __ldg(&S.tris[3 * ti + 2]);
-                ctr.tri();
-                float t, u, v;
-                if (kAny) {
-                    if (tri_intersect(st.r, v0, v1, v2, st.tmin, st.tmax, t, u, v)) {
-                        st.best_id = __float_as_uint(v0.w);
-                        return true;
-                    }
-                } else {
-                    const uint32_t id = __float_as_uint(v0.w);
-                    // one ulp above the best t, so an equal t is seen and the lower id wins
-                    const float lim =
-                        st.best_id == PG_NO_HIT ? st.tmax : __uint_as_float(__float_as_uint(st.tmax) + 1u);
-                    if (tri_intersect(st.r, v0, v1, v2, st.tmin, lim, t, u, v) &&
-                        (t < st.tmax || (t == st.tmax && id < st.best_id))) {
-                        st.tmax = t;
-                        st.best_id = id;
-                        st.best_u = u;
-                        st.best_v = v;
-                    }
+    float e[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        e[j] = box_enter(st.r, f4(lox, j), f4(loy, j), f4(loz, j), f4(hix, j), f4(hiy, j), f4(hiz, j), st.tmin,
+                         st.tmax);
+    for (int j = 0; j < 4; ++j) {
+        const int cnt = i4(count, j);
+        if (e[j] == INFINITY || cnt <= 0) continue;
+        const int first = i4(child, j);
+        for (int k = 0; k < cnt; ++k) {
+            const uint32_t ti = (uint32_t)(first + k);
+            const float4 v0 = __ldg(&S.tris[3 * ti]), v1 = __ldg(&S.tris[3 * ti + 1]), v2 = __ldg(&S.tris[3 * ti + 2]);
+            ctr.tri();
+            float t, u, v;
+            if (kAny) {
+                if (tri_intersect(st.r, v0, v1, v2, st.tmin, st.tmax, t, u, v)) {
+                    st.best_id = __float_as_uint(v0.w);
+                    return true;
+                }
+            } else {
+                const uint32_t id = __float_as_uint(v0.w);
+                // one ulp above the best t, so an equal t is seen and the lower id wins
+                const float lim = st.best_id == PG_NO_HIT ? st.tmax : __uint_as_float(__float_as_uint(st.tmax) + 1u);
+                if (tri_intersect(st.r, v0, v1, v2, st.tmin, lim, t, u, v) &&
+                    (t < st.tmax || (t == st.tmax && id < st.best_id))) {
+                    st.tmax = t;
+                    st.best_id = id;
+                    st.best_u = u;
+                    st.best_v = v;
                 }
             }
-        } else if (child >= 0) {
-            cand[nn] = child;
-            ce[nn] = e;
-            ++nn;
         }
     }
-    if (nn == 2) {
-        const int first = kAny ? 0 : (ce[1] < ce[0] ? 1 : 0);
-        if (st.sp < kStackSize) stack[st.sp++] = cand[1 - first];
-        st.node = cand[first];
-        return false;
+    // inner children, sorted (insertion, stable) by entry distance for closest hits
+    int cand[4];
+    float ce[4];
+    int nn = 0;
+    for (int j = 0; j < 4; ++j) {
+        if (e[j] == INFINITY || i4(count, j) > 0 || i4(child, j) < 0) continue;
+        int pos = nn;
+        if (!kAny)
+            while (pos > 0 && ce[pos - 1] > e[j]) {
+                ce[pos] = ce[pos - 1];
+                cand[pos] = cand[pos - 1];
+                --pos;
+            }
+        ce[pos] = e[j];
+        cand[pos] = i4(child, j);
+        ++nn;
     }
-    if (nn == 1) {
+    if (nn > 0) {
+        for (int q = nn - 1; q >= 1; --q)
+            if (st.sp < kStackSize) stack[st.sp++] = cand[q];
         st.node = cand[0];
         return false;
     }

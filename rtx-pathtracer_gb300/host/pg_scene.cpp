@@ -261,6 +261,14 @@ struct Box {
     }
 };
 
+// Binary node of the SAH build, before the collapse into four-wide nodes.
+struct BinNode {
+    float lo0[3], hi0[3];
+    float lo1[3], hi1[3];
+    int32_t child[2];
+    int32_t count[2];
+};
+
 struct Builder {
     SceneData &s;
     int max_leaf;
@@ -274,6 +282,8 @@ struct Builder {
         int32_t count;
         Box box;
     };
+
+    std::vector<BinNode> bin;  // the binary tree, pre-order
 
     Ref build(uint32_t begin, uint32_t end, int depth) {
         Box bounds, cb;
@@ -338,11 +348,11 @@ struct Builder {
             mid = (uint32_t)(it - prims.begin());
             if (mid == begin || mid == end) mid = begin + n / 2;
         }
-        const int32_t node = (int32_t)s.nodes.size();
-        s.nodes.push_back(BvhNode{});
+        const int32_t node = (int32_t)bin.size();
+        bin.push_back(BinNode{});
         const Ref l = build(begin, mid, depth + 1);
         const Ref r = build(mid, end, depth + 1);
-        BvhNode &nd = s.nodes[node];
+        BinNode &nd = bin[node];
         for (int i = 0; i < 3; ++i) {
             nd.lo0[i] = l.box.lo[i];
             nd.hi0[i] = l.box.hi[i];
@@ -359,9 +369,83 @@ struct Builder {
 
 }  // namespace
 
+// One child reference of a binary node (empty when child < 0 and count == 0).
+struct ChildRef {
+    int32_t child, count;
+    float lo[3], hi[3];
+};
+
+static float box_area(const float lo[3], const float hi[3]) {
+    const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+    if (!(dx >= 0 && dy >= 0 && dz >= 0)) return 0.0f;
+    return 2.0f * (dx * dy + dy * dz + dz * dx);
+}
+
+static void bin_children(const BinNode &n, std::vector<ChildRef> &out) {
+    for (int c = 0; c < 2; ++c) {
+        if (n.child[c] < 0 && n.count[c] == 0) continue;
+        ChildRef r;
+        r.child = n.child[c];
+        r.count = n.count[c];
+        for (int i = 0; i < 3; ++i) {
+            r.lo[i] = c == 0 ? n.lo0[i] : n.lo1[i];
+            r.hi[i] = c == 0 ? n.hi0[i] : n.hi1[i];
+        }
+        out.push_back(r);
+    }
+}
+
+// Four-wide node for binary node b, appended in pre-order; returns its index.
+static int32_t collapse(const std::vector<BinNode> &bin, int32_t b, std::vector<BvhNode> &out) {
+    std::vector<ChildRef> ch;
+    bin_children(bin[b], ch);
+    while (ch.size() < 4) {
+        int best = -1;
+        float best_a = -1.0f;
+        for (size_t i = 0; i < ch.size(); ++i)
+            if (ch[i].count == 0 && ch[i].child >= 0) {
+                const float a = box_area(ch[i].lo, ch[i].hi);
+                if (a > best_a) {
+                    best_a = a;
+                    best = (int)i;
+                }
+            }
+        if (best < 0) break;
+        std::vector<ChildRef> kids;
+        bin_children(bin[ch[best].child], kids);
+        if (ch.size() - 1 + kids.size() > 4) break;
+        ch.erase(ch.begin() + best);
+        ch.insert(ch.begin() + best, kids.begin(), kids.end());
+    }
+    const int32_t me = (int32_t)out.size();
+    out.push_back(BvhNode{});
+    int32_t child_idx[4] = {-1, -1, -1, -1};
+    for (size_t i = 0; i < ch.size(); ++i)
+        child_idx[i] = ch[i].count > 0 ? ch[i].child : collapse(bin, ch[i].child, out);
+    BvhNode &n = out[me];
+    for (int slot = 0; slot < 4; ++slot) {
+        if (slot < (int)ch.size()) {
+            for (int a = 0; a < 3; ++a) {
+                n.lo[a][slot] = ch[slot].lo[a];
+                n.hi[a][slot] = ch[slot].hi[a];
+            }
+            n.child[slot] = child_idx[slot];
+            n.count[slot] = ch[slot].count;
+        } else {
+            for (int a = 0; a < 3; ++a) {
+                n.lo[a][slot] = INFINITY;
+                n.hi[a][slot] = -INFINITY;
+            }
+            n.child[slot] = -1;
+            n.count[slot] = 0;
+        }
+    }
+    return me;
+}
+
 void build_bvh(SceneData &s, int max_leaf) {
     const uint32_t T = (uint32_t)(s.idx.size() / 3);
-    Builder b{s, max_leaf, {}, {}, {}};
+    Builder b{s, max_leaf, {}, {}, {}, {}};
     b.tri_box.resize(T);
     b.cen.resize(3 * (size_t)T);
     b.prims.resize(T);
@@ -373,33 +457,30 @@ void build_bvh(SceneData &s, int max_leaf) {
         b.prims[t] = t;
     }
     s.nodes.clear();
-    s.nodes.reserve(T ? 2 * (size_t)T / std::max(1, max_leaf) + 1 : 1);
+    // binary nodes are numbered in pre-order, so an interior root is node 0;
+    // a leaf root becomes a node with one leaf child
+    BinNode root{};
+    for (int i = 0; i < 3; ++i) {
+        root.lo0[i] = root.lo1[i] = INFINITY;
+        root.hi0[i] = root.hi1[i] = -INFINITY;
+    }
+    root.child[0] = root.child[1] = -1;
     if (T == 0) {
-        BvhNode root{};
-        for (int i = 0; i < 3; ++i) {
-            root.lo0[i] = root.lo1[i] = INFINITY;
-            root.hi0[i] = root.hi1[i] = -INFINITY;
-        }
-        root.child[0] = root.child[1] = -1;
-        s.nodes.push_back(root);
+        b.bin.push_back(root);
     } else {
-        // nodes are numbered in pre-order, so an interior root is node 0
         const Builder::Ref top = b.build(0, T, 0);
         if (top.leaf) {
-            BvhNode root{};
             for (int i = 0; i < 3; ++i) {
                 root.lo0[i] = top.box.lo[i];
                 root.hi0[i] = top.box.hi[i];
-                root.lo1[i] = INFINITY;
-                root.hi1[i] = -INFINITY;
             }
             root.child[0] = top.index;
             root.count[0] = top.count;
-            root.child[1] = -1;
-            root.count[1] = 0;
-            s.nodes.push_back(root);
+            b.bin.push_back(root);
         }
     }
+    s.nodes.reserve(b.bin.size() / 2 + 1);
+    collapse(b.bin, 0, s.nodes);
     s.tri_order = b.prims;
     s.tri_verts.assign(12 * (size_t)T, 0.0f);
     for (uint32_t i = 0; i < T; ++i) {

@@ -16,16 +16,18 @@
 
 namespace pg {
 
-// Node of the two-wide BVH: both children's boxes live in the parent, so one
-// 64-byte fetch tests two boxes.  child[i] >= 0: inner node index; count[i] > 0:
-// leaf with triangles [child[i], child[i] + count[i]) of the reordered list.
+// Node of the four-wide BVH: the boxes of all four children live in the
+// parent, slot-major per coordinate (lo[axis][slot]), so one 128-byte fetch
+// tests four boxes.  Slot i: count[i] > 0 is a leaf with triangles
+// [child[i], child[i] + count[i]) of the reordered list; count[i] == 0 and
+// child[i] >= 0 an inner node; child[i] < 0 an empty slot (box +inf..-inf).
 struct BvhNode {
-    float lo0[3], hi0[3];
-    float lo1[3], hi1[3];
-    int32_t child[2];
-    int32_t count[2];
+    float lo[3][4];
+    float hi[3][4];
+    int32_t child[4];
+    int32_t count[4];
 };
-static_assert(sizeof(BvhNode) == 64, "BvhNode is 64 bytes");
+static_assert(sizeof(BvhNode) == 128, "BvhNode is 128 bytes");
 
 struct SceneData {
     std::vector<float> pos;        // 3 per vertex
@@ -43,7 +45,10 @@ struct SceneData {
 };
 
 // Binned SAH build (32 bins on centroid extents, leaves of at most max_leaf
-// triangles).  Deterministic: same input, same tree.
+// triangles) of a binary tree, collapsed into four-wide nodes (each node
+// takes its binary children and repeatedly opens the inner child with the
+// largest surface area until it holds four).  Deterministic: same input, same
+// tree.
 void build_bvh(SceneData &s, int max_leaf = 4);
 
 // Procedural scenes of the benchmark workloads.

@@ -19,34 +19,25 @@ def tracer(oracle):
     return TraceOracle()
 
 
-def leaf_triangles(nodes):
-    """Triangle ranges [first, first + count) of every leaf reference."""
-    out = []
-    for n in nodes:
-        for c in range(2):
-            if n["count"][c] > 0:
-                out.append((int(n["child"][c]), int(n["count"][c])))
-    return out
-
-
 def check_bvh(exp):
+    """Structure of the four-wide BVH: every triangle in exactly one leaf, leaf
+    boxes bound their triangles, child boxes nest, every node has one parent."""
     nodes, tv, order = exp["nodes"], exp["tri_verts"], exp["tri_order"]
     T = tv.shape[0]
     assert sorted(order.tolist()) == list(range(T)), "tri_order is a permutation"
-    # tri_verts row i holds triangle order[i]: v0, e1, e2 in some packing; its
-    # original id sits in the bits of float [3]
+    # tri_verts row i holds triangle order[i]; its original id sits in the bits of float [3]
     assert np.array_equal(tv[:, 3].view(np.uint32), order)
     pos, idx = exp["pos"], exp["idx"]
     covered = np.zeros(T, dtype=np.int32)
     seen_nodes = np.zeros(len(nodes), dtype=np.int32)
     stack = [0] if len(nodes) else []
-    seen_nodes[0] = 1 if len(nodes) else 0
+    if len(nodes):
+        seen_nodes[0] = 1
     while stack:
         i = stack.pop()
         n = nodes[i]
-        for c in range(2):
-            lo = n["lo0"] if c == 0 else n["lo1"]
-            hi = n["hi0"] if c == 0 else n["hi1"]
+        for c in range(4):
+            lo, hi = n["lo"][:, c], n["hi"][:, c]
             cnt, ch = int(n["count"][c]), int(n["child"][c])
             if cnt > 0:
                 assert cnt <= 4, "leaf size"
@@ -54,17 +45,22 @@ def check_bvh(exp):
                 covered[ch:ch + cnt] += 1
                 v = pos[idx[order[ch:ch + cnt]]].reshape(-1, 3)
                 assert (v >= lo - 1e-6).all() and (v <= hi + 1e-6).all(), "leaf box bounds its triangles"
-            elif cnt == 0 and ch >= 0:
+            elif ch >= 0:
                 assert 0 < ch < len(nodes)
                 assert seen_nodes[ch] == 0, "each node has one parent"
                 seen_nodes[ch] = 1
                 kid = nodes[ch]
-                for lo2, hi2 in ((kid["lo0"], kid["hi0"]), (kid["lo1"], kid["hi1"])):
-                    if (lo2 <= hi2).all():
-                        assert (lo2 >= lo).all() and (hi2 <= hi).all(), "child boxes nest"
+                for c2 in range(4):
+                    if kid["count"][c2] > 0 or kid["child"][c2] >= 0:
+                        assert (kid["lo"][:, c2] >= lo).all() and (kid["hi"][:, c2] <= hi).all(), "boxes nest"
                 stack.append(ch)
+            else:
+                assert not (lo <= hi).any(), "empty slots have empty boxes"
     assert (covered == 1).all(), "every triangle in exactly one leaf"
     assert seen_nodes.all(), "no orphan nodes"
+    # four-wide: most nodes use all four slots
+    if len(nodes) > 8:
+        assert np.mean((nodes["child"] >= 0).sum(axis=1) == 4) > 0.5
 
 
 def brute_closest(exp, rays):
