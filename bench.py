@@ -441,6 +441,48 @@ def bench_surrogate(pkg, abi, torch, stream, passes: int = 3):
     return out
 
 
+CONFIG1_WORKLOAD = ("plain CPU-runnable guiding fit: 64 regions x 16384 samples, 4-lobe vMF truth kappa 5-500, "
+                    "weights lognormal(0,1), K=8, 20 EM iterations")
+
+
+def bench_config1(pkg, abi, torch, stream, steps: int, cpu: bool):
+    """The reference's CPU-runnable fit configuration on the GPU, with the
+    bit-exact lightpmm port on the host cores beside it."""
+    import __graft_entry__ as entry
+    wl = entry.load_submodule("workloads")
+    w = wl.fit_plain()
+    R = len(w["offsets"]) - 1
+    cfg = abi.forced_iterations(ITERS, num_initial_components=8)
+    ctx = pkg.FitContext(cfg, max_regions=R)
+    d = torch.from_numpy(np.ascontiguousarray(w["dirw"], dtype=np.float32)).cuda()
+    o = torch.from_numpy(w["offsets"].view(np.int32)).cuda()
+    best, _ = ctx.autotune(d, o, R, abi.PG_FIT_INIT, stream=stream)  # 64 regions: wide clusters fill the GPU
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            ctx.fit(d, o, R, abi.PG_FIT_INIT, stream=stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            ctx.fit(d, o, R, abi.PG_FIT_INIT, stream=stream)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    si = int(np.diff(w["offsets"].astype(np.int64)).sum()) * ITERS
+    out = {"metric": METRIC, "value": si / (ms * 1e-3) / 1e6, "unit": UNIT, "ms_per_step": ms,
+           "config": {"workload": CONFIG1_WORKLOAD, "l2": "1 M samples (16 MB) stay in L2 and shared memory",
+                      "tuning": {f: int(getattr(best, f)) for f, _ in abi.FitTuning._fields_}}}
+    if cpu:
+        from oracle.oracle import Oracle
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        Oracle().fit(cfg, w["dirw"], w["offsets"], f64=False, threads=threads)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": si / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": "the whole configuration (64 regions, 20 iterations)"}
+    ctx.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -632,6 +674,8 @@ def main():
         graph.close()
     ctx.close()
     if args.workload == "all" and not args.small:
+        line["cpu_runnable_config"] = bench_config1(pkg, abi, torch, stream, args.steps,
+                                                    cpu=rank == 0 and not args.no_cpu_baseline)
         tsampler = ClockSampler(local)
         with tsampler:
             tr = bench_tracer(pkg, abi, torch, stream, args.steps, args.warmup,

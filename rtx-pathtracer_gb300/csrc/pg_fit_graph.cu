@@ -21,7 +21,7 @@ namespace {
 std::vector<pg_fit_tuning> default_grid() {
     std::vector<pg_fit_tuning> g;
     for (uint32_t cpt : {16u, 8u})
-        for (uint32_t cl : {1u, 2u, 4u})
+        for (uint32_t cl : {1u, 2u, 4u, 8u, 16u})
             for (uint32_t cap : {3072u, 6144u})
                 for (uint32_t large : {8192u, 12288u, 24576u}) {
                     if (cl == 1 && large != 12288u) continue;  // no cluster: the threshold is unused

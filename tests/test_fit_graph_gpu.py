@@ -34,7 +34,7 @@ def test_autotune_keeps_states_and_picks_a_grid_point(cuda, pkg, abi, workloads,
     s = torch.cuda.Stream()
     best, ms = ctx.autotune(d, o, R, abi.PG_FIT_UPDATE, stream=s)
     assert ms > 0 and best.threads_per_cta == 128 and best.components_per_thread in (8, 16)
-    assert best.cluster_size in (1, 2, 4) and best.smem_samples in (3072, 6144)
+    assert best.cluster_size in (1, 2, 4, 8, 16) and best.smem_samples in (3072, 6144)
     after = ctx.states(R)
     assert before.tobytes() == after.tobytes()
     # the tuned shape fits as well as any other
