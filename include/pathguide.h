@@ -218,6 +218,50 @@ int pg_sync_status(pg_ctx *ctx, void *stream);
  * launches in benchmarks). */
 int pg_last_launch_count(const pg_ctx *ctx, uint32_t *count);
 
+/* ------------------------------------------------------------------ */
+/* Split and merge of mixture components                               */
+/* ------------------------------------------------------------------ */
+
+/* PathGuiding::postFit with splitAndMerge (src/PathGuiding.cpp:413-451):
+ * components whose Pearson chi-square divergence is large are split along
+ * the principal axis of their 2-D covariance (PCA split, :494-561) and
+ * refitted by a masked EM; pairs whose merged component would barely change
+ * the mixture are merged (:635-781).  The statistics it keeps per region and
+ * component (incrementalpearsonchisquared.h, incrementalcovariance2d.h): */
+typedef struct pg_region_extra {
+    float chi2_div[16];        /* divergencePlusOneTimesIntegralSqr */
+    float chi2_n[16];          /* numSamples                        */
+    float cov[16][3];          /* variance x, variance y, covariance (component frame) */
+    float cov_w[16];           /* sumWeights                        */
+    float samples_since_merge; /* samplesSinceLastMerge             */
+    uint32_t reserved[3];
+} pg_region_extra;
+
+/* The reference's knobs (src/PathGuiding.h:124-129). */
+typedef struct pg_split_merge_config {
+    uint32_t enabled;                            /* splitAndMerge                 */
+    uint32_t min_samples_for_merging;            /* 8192                          */
+    uint32_t min_samples_for_splitting;          /* 4096                          */
+    uint32_t min_samples_for_post_split_fitting; /* 4096                          */
+    float split_min_divergence;                  /* 0.5                           */
+    float merge_max_divergence;                  /* 0.025                         */
+} pg_split_merge_config;
+
+/* The reference's defaults, enabled. */
+void pg_default_split_merge_config(pg_split_merge_config *out);
+/* Sets the context's split/merge configuration (contexts start with it
+ * disabled); pg_update then runs it after each fit, before the distances. */
+int pg_set_split_merge(pg_ctx *ctx, const pg_split_merge_config *cfg);
+/* The post-fit split/merge of regions [0, n_regions) on one pass of samples:
+ * dirw as for pg_fit_regions, pdf = the records' sampling pdf per sample
+ * (device, grouped like dirw).  Regions without samples are untouched.
+ * Mixture components may change in number (1..16). */
+int pg_split_merge(pg_ctx *ctx, const float *dirw, const float *pdf, const uint32_t *offsets, uint32_t n_regions,
+                   void *stream);
+/* Host copies of the per-region split/merge statistics. */
+int pg_get_region_extra(pg_ctx *ctx, pg_region_extra *host_out, uint32_t count);
+int pg_set_region_extra(pg_ctx *ctx, const pg_region_extra *host_in, uint32_t count);
+
 /* Autotuner (no counterpart in the reference, which fits on the host): times
  * the fit on the caller's own samples for each candidate tuning (the built-in
  * grid of CTA size, samples staged per CTA, components per thread, cluster

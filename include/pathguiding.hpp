@@ -210,8 +210,10 @@ private:
 class PathGuiding {
 public:
     PathGuiding() = default;
+    // splitAndMerge: the post-fit split and merge of mixture components
+    // (src/PathGuiding.h:124, on by default there too).
     PathGuiding(uint32_t splitCount, const Aabb &sceneAabb, bool useParallaxCompensation,
-                cudaStream_t stream = nullptr, uint32_t numInitialComponents = 8)
+                cudaStream_t stream = nullptr, uint32_t numInitialComponents = 8, bool splitAndMerge = true)
         : stream_(stream) {
         pg_fit_config cfg;
         pg_default_fit_config(&cfg);
@@ -222,6 +224,11 @@ public:
         float box[6];
         sceneAabb.to_array(box);
         check(pg_set_regions(ctx_, splitCount, box, stream_), ctx_);
+        if (splitAndMerge) {
+            pg_split_merge_config sm;
+            pg_default_split_merge_config(&sm);
+            check(pg_set_split_merge(ctx_, &sm), ctx_);
+        }
     }
     PathGuiding(PathGuiding &&o) noexcept { *this = std::move(o); }
     PathGuiding &operator=(PathGuiding &&o) noexcept {
@@ -234,8 +241,9 @@ public:
     ~PathGuiding() { cleanup(); }
 
     // update (src/PathGuiding.cpp:276-312): bucket the collector's records by
-    // region, parallax pre-pass, fit (first pass) or stepwise update, lobe
-    // distances and VMM_Theta packing, all on the device and stream-ordered.
+    // region, parallax pre-pass, fit (first pass) or stepwise update, split
+    // and merge, lobe distances and VMM_Theta packing, all on the device and
+    // stream-ordered.
     // Returns whether the tracer must rebind its buffers (regions are never
     // split here: false).
     bool update(SampleCollector &sampleCollector) {

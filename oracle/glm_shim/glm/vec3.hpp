@@ -26,6 +26,9 @@ struct vec3 {
     vec3 &operator*=(float s) { x *= s; y *= s; z *= s; return *this; }
     vec3 &operator/=(float s) { x /= s; y /= s; z /= s; return *this; }
     bool operator==(const vec3 &o) const { return x == o.x && y == o.y && z == o.z; }
+    // GLM's member length() is the number of components, not the Euclidean
+    // norm (glm::length is); code that calls it gets 3, as with the real library
+    static constexpr int length() { return 3; }
 };
 inline vec3 operator*(float s, const vec3 &v) { return v * s; }
 

@@ -153,6 +153,8 @@ class ReferenceFit:
         L.lpmm_ref_update_distances.argtypes = [_U32, _P, _P, _P, _P]
         L.lpmm_ref_reposition.argtypes = [_P, _P]
         L.lpmm_ref_fastexp.argtypes = [_P, _P, _U32]
+        L.lpmm_ref_postfit.argtypes = [C.POINTER(abi.FitConfig), C.POINTER(abi.SplitMergeConfig), _U32, _P, _P, _P,
+                                       _P, _P]
         L.lpmm_ref_state_size.restype = _U32
         assert L.lpmm_ref_state_size() == abi.STATE_DTYPE.itemsize
 
@@ -170,6 +172,26 @@ class ReferenceFit:
         self.lib.lpmm_ref_fit(C.byref(cfg), mode, R, abi.ptr(dirw), abi.ptr(offsets), abi.ptr(st),
                               abi.ptr(ll))
         return st, ll
+
+    def postfit(self, cfg, sm, dirw, pdf, dist, offsets, states, extras):
+        """PathGuiding::postFit with split/merge per region (regions without
+        samples are skipped, as PathGuiding::update skips them)."""
+        st, ex = states.copy(), extras.copy()
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint32)
+        dirw, pdf = _f32(dirw), _f32(pdf)
+        dist = _f32(dist) if dist is not None else None
+        for r in range(offsets.shape[0] - 1):
+            b, e = int(offsets[r]), int(offsets[r + 1])
+            if e == b:
+                continue
+            one_st, one_ex = st[r:r + 1].copy(), ex[r:r + 1].copy()
+            d = np.ascontiguousarray(dirw[b:e])
+            p = np.ascontiguousarray(pdf[b:e])
+            t = np.ascontiguousarray(dist[b:e]) if dist is not None else None
+            self.lib.lpmm_ref_postfit(C.byref(cfg), C.byref(sm), e - b, abi.ptr(d), abi.ptr(p),
+                                      abi.ptr(t) if t is not None else None, abi.ptr(one_st), abi.ptr(one_ex))
+            st[r], ex[r] = one_st[0], one_ex[0]
+        return st, ex
 
     def update_distances(self, dirw, dist, offsets, states):
         st = states.copy()

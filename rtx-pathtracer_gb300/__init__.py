@@ -54,6 +54,11 @@ SIGNATURES = {
     "pg_fit_graph_launch": (_I, [_P, _P]),
     "pg_fit_graph_destroy": (_I, [_P]),
     "pg_fit_regions_noalloc": (_I, [C.POINTER(abi.FitConfig), _P, _P, _P, _U32, _I, _P]),
+    "pg_default_split_merge_config": (None, [C.POINTER(abi.SplitMergeConfig)]),
+    "pg_set_split_merge": (_I, [_P, C.POINTER(abi.SplitMergeConfig)]),
+    "pg_split_merge": (_I, [_P, _P, _P, _P, _U32, _P]),
+    "pg_get_region_extra": (_I, [_P, _P, _U32]),
+    "pg_set_region_extra": (_I, [_P, _P, _U32]),
     "pg_mlp_default_config": (None, [C.POINTER(abi.MlpConfig)]),
     "pg_mlp_create": (_I, [C.POINTER(abi.MlpConfig), C.POINTER(_P)]),
     "pg_mlp_destroy": (_I, [_P]),
@@ -265,6 +270,28 @@ class FitContext:
         n = C.c_uint32()
         self._check(self.lib.pg_last_launch_count(self.h, C.byref(n)))
         return int(n.value)
+
+    # ---- split and merge (PathGuiding::postFit with splitAndMerge) ----
+    def set_split_merge(self, cfg: abi.SplitMergeConfig | None = None):
+        """Turns the post-fit split/merge on with `cfg` (the reference's
+        defaults when None); a config with enabled=0 turns it off."""
+        c = cfg if cfg is not None else abi.default_split_merge_config()
+        self._check(self.lib.pg_set_split_merge(self.h, C.byref(c)))
+
+    def split_merge(self, dirw, pdf, offsets, n_regions: int, stream=None):
+        """One post-fit split/merge pass of regions [0, n_regions) on the
+        samples of the last fit and their sampling pdfs."""
+        self._check(self.lib.pg_split_merge(self.h, _dptr(dirw), _dptr(pdf), _dptr(offsets), n_regions,
+                                            _stream_handle(stream)))
+
+    def extras(self, n: int) -> np.ndarray:
+        out = np.zeros(n, dtype=abi.EXTRA_DTYPE)
+        self._check(self.lib.pg_get_region_extra(self.h, out.ctypes.data, n))
+        return out
+
+    def set_extras(self, extras: np.ndarray):
+        e = np.ascontiguousarray(extras, dtype=abi.EXTRA_DTYPE)
+        self._check(self.lib.pg_set_region_extra(self.h, e.ctypes.data, e.shape[0]))
 
 
 class FitGraph:

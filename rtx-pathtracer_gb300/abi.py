@@ -100,6 +100,25 @@ class PlatesParams(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("occluder_grid", C.c_uint32), ("seed", C.c_uint32)]
 
 
+EXTRA_DTYPE = np.dtype([("chi2_div", "<f4", (16,)), ("chi2_n", "<f4", (16,)), ("cov", "<f4", (16, 3)),
+                        ("cov_w", "<f4", (16,)), ("samples_since_merge", "<f4"), ("reserved", "<u4", (3,))])
+assert EXTRA_DTYPE.itemsize == 400
+
+
+class SplitMergeConfig(C.Structure):
+    _fields_ = [("enabled", C.c_uint32), ("min_samples_for_merging", C.c_uint32),
+                ("min_samples_for_splitting", C.c_uint32), ("min_samples_for_post_split_fitting", C.c_uint32),
+                ("split_min_divergence", C.c_float), ("merge_max_divergence", C.c_float)]
+
+
+def default_split_merge_config(**kw) -> SplitMergeConfig:
+    """The reference's knobs (src/PathGuiding.h:124-129), enabled."""
+    c = SplitMergeConfig(1, 8192, 4096, 4096, 0.5, 0.025)
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
 class MlpConfig(C.Structure):
     _fields_ = [("batch", C.c_uint32), ("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float),
                 ("eps", C.c_float), ("seed", C.c_uint32), ("scene_aabb", C.c_float * 6)]

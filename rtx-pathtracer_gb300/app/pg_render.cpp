@@ -15,7 +15,7 @@
 // Options: --spp N (final guided samples, default 64), --train LIST (training
 // samples per frame, default 1,2,4,8,16,32), --depth N (10), --seed N (1),
 // --prob P (guiding probability 0.5), --no-guiding (plain NEE + MIS with the
-// same total samples), --no-parallax, --out FILE.
+// same total samples), --no-parallax, --no-split-merge, --out FILE.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -56,7 +56,8 @@ bool write_pfm(const std::string &path, const std::vector<float> &rgb, uint32_t 
 
 int usage() {
     fprintf(stderr, "Required parameters: WIDTH HEIGHT IC_SIZE GUIDING_SPLITS SCENE [--spp N] [--train LIST] "
-                    "[--depth N] [--seed N] [--prob P] [--no-guiding] [--no-parallax] [--out FILE]\n");
+                    "[--depth N] [--seed N] [--prob P] [--no-guiding] [--no-parallax] [--no-split-merge] "
+                    "[--out FILE]\n");
     return EXIT_FAILURE;
 }
 
@@ -69,7 +70,7 @@ int main(int argc, char **argv) {
     const std::string scene_arg = argv[5];
     uint32_t spp = 64, depth = 10, seed = 1;
     float prob = 0.5f;
-    bool guiding = true, parallax = true;
+    bool guiding = true, parallax = true, split_merge = true;
     std::vector<uint32_t> train = {1, 2, 4, 8, 16, 32};
     std::string out;
     for (int i = 6; i < argc; ++i) {
@@ -82,6 +83,7 @@ int main(int argc, char **argv) {
         else if (a == "--prob") prob = strtof(next(), nullptr);
         else if (a == "--no-guiding") guiding = false;
         else if (a == "--no-parallax") parallax = false;
+        else if (a == "--no-split-merge") split_merge = false;
         else if (a == "--out") out = next();
         else return usage();
     }
@@ -105,7 +107,7 @@ int main(int argc, char **argv) {
         uint64_t sorted_records = 0, regions_with_samples = 0;
         cudaEventRecord(e0, stream);
         if (guiding) {
-            pg::PathGuiding pg(splits, scene.getSceneSize(), parallax, stream);
+            pg::PathGuiding pg(splits, scene.getSceneSize(), parallax, stream, 8, split_merge);
             pg::SampleCollector collector(pg.getRegionCount(), W, H, stream);
             for (size_t f = 0; f < train.size(); ++f) {
                 tracer.render(pg::render_params(train[f], depth, seed + 1000u * (uint32_t)(f + 1), f > 0, true, prob),

@@ -28,6 +28,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               f"-I{ROOT / 'include'}", f"-I{CSRC}"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", f"-I{ROOT / 'include'}", f"-I{HOST}"]
+# Per-file extras.  The split/merge control arithmetic follows the reference's
+# SSE2 build, which rounds every product and sum: no FMA contraction there.
+FILE_FLAGS = {"pg_splitmerge.cu": ["-fmad=false"]}
 
 
 def _sources():
@@ -56,7 +59,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         if not stale:
             continue
         if src.suffix == ".cu":
-            cmd = [NVCC] + ARCH + NVCC_FLAGS + ["-c", str(src), "-o", str(obj)]
+            cmd = [NVCC] + ARCH + NVCC_FLAGS + FILE_FLAGS.get(src.name, []) + ["-c", str(src), "-o", str(obj)]
         else:
             cmd = ["g++"] + CXX_FLAGS + ["-c", str(src), "-o", str(obj)]
         jobs.append(cmd)

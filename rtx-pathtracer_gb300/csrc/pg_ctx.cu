@@ -126,6 +126,7 @@ int pg_ctx_create(const pg_fit_config *cfg, uint32_t max_regions, uint64_t max_s
 int pg_ctx_destroy(pg_ctx *ctx) {
     if (!ctx) return PG_OK;
     guide_release(ctx);
+    extras_release(ctx);
     cudaFree(ctx->d_states);
     cudaFree(ctx->d_order);
     cudaFree(ctx->d_counters);

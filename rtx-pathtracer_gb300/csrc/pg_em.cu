@@ -64,8 +64,11 @@ int pg_init_regions(pg_ctx *ctx, uint32_t n_regions, void *stream) {
     if (n_regions == 0) return PG_OK;
     // All-zero offsets: every region is empty, so only initialisation runs and
     // no sample is read (the sample pointer is never dereferenced).
-    return pg_fit_regions(ctx, reinterpret_cast<const float *>(ctx->d_init), ctx->d_zero_offsets, n_regions,
-                          PG_FIT_INIT, stream);
+    int st = pg_fit_regions(ctx, reinterpret_cast<const float *>(ctx->d_init), ctx->d_zero_offsets, n_regions,
+                            PG_FIT_INIT, stream);
+    // fresh mixtures start with fresh split/merge statistics (PMM_ExtraData{})
+    if (!st && ctx->d_extras) st = extras_reset(ctx, 0, n_regions, (cudaStream_t)stream);
+    return st;
 }
 
 int pg_fit_regions(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t n_regions, int mode,

@@ -208,14 +208,16 @@ __global__ void gather_records(const pg_directional_data *rec, const uint32_t *o
 // The sample count is n_valid, or *n_valid_dev when given (the sort's valid
 // count, which only the device knows); records with an out-of-range region id
 // are written with zero weight.
+// pdf (may be null): the records' sampling pdf, for the split/merge statistics.
 __global__ void prefit_parallax_kernel(const pg_directional_data *rec, const uint32_t *order, uint32_t n_valid,
                                        const uint32_t *n_valid_dev, uint32_t n_regions, const float *means,
-                                       int use_parallax, float4 *dirw, float *dist) {
+                                       int use_parallax, float4 *dirw, float *dist, float *pdf) {
     const uint32_t n = n_valid_dev ? *n_valid_dev : n_valid;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const pg_directional_data d = rec[order ? order[i] : i];
         float dx = d.direction[0], dy = d.direction[1], dz = d.direction[2];
         float t = d.distance;
+        if (pdf) pdf[i] = d.pdf;
         if (d.flags >= n_regions) {
             dirw[i] = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
             dist[i] = INFINITY;
@@ -474,6 +476,7 @@ struct GuideScratch {
     uint64_t cap_tiles = 0;
     float4 *dirw = nullptr;
     float *dist = nullptr;
+    float *pdf = nullptr;
     uint32_t *offsets = nullptr;
     uint32_t *order = nullptr;
     float *means = nullptr;
@@ -495,6 +498,7 @@ static GuideScratch &guide(pg_ctx *ctx) {
 void guide_release(pg_ctx *ctx) {
     if (!ctx || !ctx->guide) return;
     GuideScratch &g = *static_cast<GuideScratch *>(ctx->guide);
+    cudaFree(g.pdf);
     for (int i = 0; i < 2; ++i) {
         cudaFree(g.keys[i]);
         cudaFree(g.vals[i]);
@@ -709,7 +713,7 @@ int pg_prefit_parallax(pg_ctx *ctx, const pg_directional_data *sorted, const uin
     if (n_valid)
         prefit_parallax_kernel<<<std::min<uint64_t>((n_valid + 255) / 256, 16384u), 256, 0, s>>>(
             sorted, nullptr, (uint32_t)n_valid, nullptr, n_regions, g.means, ctx->cfg.use_parallax ? 1 : 0,
-            reinterpret_cast<float4 *>(dirw_out), dist_out);
+            reinterpret_cast<float4 *>(dirw_out), dist_out, nullptr);
     return check_cuda(ctx, cudaGetLastError(), "prefit launch");
 }
 
@@ -743,11 +747,14 @@ int pg_update(pg_ctx *ctx, const pg_directional_data *records, uint64_t n_record
     if (n_records > g.cap_samples || !g.dirw) {
         cudaFree(g.dirw);
         cudaFree(g.dist);
+        cudaFree(g.pdf);
         g.dirw = nullptr;
         g.dist = nullptr;
+        g.pdf = nullptr;
         const uint64_t cap = std::max<uint64_t>(n_records, 1);
         int st = check_cuda(ctx, cudaMalloc(&g.dirw, sizeof(float4) * cap), "fit samples");
         if (!st) st = check_cuda(ctx, cudaMalloc(&g.dist, sizeof(float) * cap), "fit distances");
+        if (!st) st = check_cuda(ctx, cudaMalloc(&g.pdf, sizeof(float) * cap), "sample pdfs");
         if (st) return st;
         g.cap_samples = cap;
     }
@@ -766,7 +773,7 @@ int pg_update(pg_ctx *ctx, const pg_directional_data *records, uint64_t n_record
                                                               g.means);
     if (n_records)
         prefit_parallax_kernel<<<std::min<uint64_t>((n_records + 255) / 256, 16384u), 256, 0, s>>>(
-            records, order, (uint32_t)n_records, g.offsets + R, R, g.means, par, g.dirw, g.dist);
+            records, order, (uint32_t)n_records, g.offsets + R, R, g.means, par, g.dirw, g.dist, g.pdf);
     st = check_cuda(ctx, cudaGetLastError(), "prefit launch");
     if (st) return st;
     // Records past the valid count (invalid slots) are never read by the fit:
@@ -775,6 +782,11 @@ int pg_update(pg_ctx *ctx, const pg_directional_data *records, uint64_t n_record
     st = pg_fit_regions(ctx, reinterpret_cast<const float *>(g.dirw), g.offsets, R,
                         g.fitted ? PG_FIT_UPDATE : PG_FIT_CONTINUE, stream);
     if (st) return st;
+    // 3b. split and merge of components (PathGuiding::postFit, before the distances)
+    if (ctx->sm.enabled) {
+        st = pg_split_merge(ctx, reinterpret_cast<const float *>(g.dirw), g.pdf, g.offsets, R, stream);
+        if (st) return st;
+    }
     // 4. parallax distances (PathGuiding::postFit)
     if (par) {
         st = pg_update_distances(ctx, reinterpret_cast<const float *>(g.dirw), g.dist, g.offsets, R, stream);

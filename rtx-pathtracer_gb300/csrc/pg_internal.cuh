@@ -12,6 +12,7 @@
 static_assert(sizeof(pg_region_state) == 704, "pg_region_state layout");
 static_assert(sizeof(pg_directional_data) == 40, "DirectionalData layout");
 static_assert(sizeof(pg_vmm_theta) == 720, "VMM_Theta layout");
+static_assert(sizeof(pg_region_extra) == 400, "pg_region_extra layout");
 
 // Device-side error word bits (ORed by kernels, read back by the host).
 #define PG_DEV_ERR_TIMEOUT 1u   // a bounded wait ran out
@@ -34,6 +35,8 @@ struct pg_ctx {
     float init_kappa = -1.0f;
     uint32_t last_launches = 0;
     void *guide = nullptr;           // sort / parallax / distance scratch (pg_guide.cu)
+    pg_region_extra *d_extras = nullptr;  // split/merge statistics per region (pg_splitmerge.cu)
+    pg_split_merge_config sm{};      // disabled unless pg_set_split_merge
     std::string last_error;
 };
 
@@ -43,6 +46,11 @@ int set_error(pg_ctx *ctx, int status, const std::string &msg);
 int check_cuda(pg_ctx *ctx, cudaError_t e, const char *what);
 int upload_init_table(pg_ctx *ctx, cudaStream_t s);
 void guide_release(pg_ctx *ctx);
+// split/merge statistics: allocated (zeroed) on first use, zeroed again when
+// regions are initialised
+int extras_ensure(pg_ctx *ctx, cudaStream_t s);
+void extras_release(pg_ctx *ctx);
+int extras_reset(pg_ctx *ctx, uint32_t first, uint32_t n, cudaStream_t s);
 
 // What the renderer needs from a guiding context: the padded root box and
 // split count of the region tree (point -> region by descent) and the packed

@@ -1,0 +1,866 @@
+// pg_splitmerge.cu - split and merge of mixture components after a region's
+// fit (PathGuiding::postFit with splitAndMerge, src/PathGuiding.cpp:413-451).
+//
+// One CTA per region with samples in the pass.  Thread 0 runs the control
+// logic of the reference - the Pearson chi-square merge metric of every pair
+// (:709-760), greedy disjoint merges (:635-707, 762-781), split candidates by
+// weighted divergence (:563-633), PCA splits along the principal axis of the
+// component's 2-D covariance (:494-561) - on the mixture held in shared
+// memory; all threads run the passes over the region's samples: the
+// divergence statistic (incrementalpearsonchisquared.h:54-94), the
+// covariance statistic (incrementalcovariance2d.h:54-106) and the masked EM
+// refit of split components (VMMFactory.h:226-297, 458-485), with per-thread
+// sums reduced in a fixed order.
+//
+// The statistics, the VMF products and divisions (VMFKernel.h:315-400), the
+// component merge (:478-530) and the weight priors (ParametricMixtureModel.h:
+// 339-370) follow the reference's formulas in FP32.  Its sorts are restated
+// exactly: candidates are separated with the two-ended partition of
+// libstdc++'s std::partition (whose order decides which components are split
+// or merged first), then sorted by value.  The one substitution: the
+// reference takes the PCA axis from an Eigen solver; here the principal
+// eigenvector of the symmetric 2x2 covariance is computed in closed form.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+
+#include "pg_internal.cuh"
+
+namespace pg {
+namespace sm {
+
+// The control logic runs on thread 0 and is also host-callable.
+#define SM_HD __host__ __device__
+
+constexpr int NT = 128, NW = NT / 32, KM = 16;
+constexpr float kPiF = 3.14159265358979323846f;
+
+struct Mix {
+    float w[KM], mx[KM], my[KM], mz[KM], k[KM], r[KM], nrm[KM], em2k[KM];
+    uint32_t K;
+    float sample_weight, num_samples;
+    unsigned long long total;
+};
+
+struct Stats {
+    float div[KM], dn[KM];   // chi-square: divergencePlusOneTimesIntegralSqr, numSamples
+    float cov[KM][3], cw[KM];
+    float dist[KM], dw[KM];  // IncrementalDistance
+    float since;
+};
+
+struct Shared {
+    Mix m;
+    Stats s;
+    float red[NW][4 * KM + 2];
+    float acc[4 * KM + 2];
+    uint32_t mask;           // components refitted by the masked EM
+    int fit_iters;
+    int stop;
+    float ll_last, ll_abs_inv;
+    float sum_w;             // weight of the valid samples (masked EM, first iteration)
+};
+
+struct Args {
+    pg_region_state *states;
+    pg_region_extra *extras;
+    const float4 *dirw;
+    const float *pdf;
+    const uint32_t *offsets;
+    uint32_t n_regions;
+    pg_fit_config cfg;
+    pg_split_merge_config sm;
+};
+
+SM_HD __forceinline__ uint32_t active_lanes(uint32_t K) { return (K + 3u) & ~3u; }
+
+// kappaToMeanCosine / meanCosineToKappa (VMFKernel.h:46-66), one component
+SM_HD __forceinline__ float k2r(float k) {
+    if (k > 5.0f) return 1.0f - 1.0f / k;
+    return k > 0.0f ? 1.0f / tanhf(k) - 1.0f / k : 0.0f;
+}
+SM_HD __forceinline__ float r2k(float r) { return (r * 3.0f - r * r * r) / (1.0f - r * r); }
+
+// calNormalization (VMFKernel.h:620-628)
+SM_HD __forceinline__ void normalise(Mix &m, int c) {
+    m.em2k[c] = expf(-2.0f * m.k[c]);
+    m.nrm[c] = m.k[c] > 0.0f ? m.k[c] / (2.0f * kPiF * (1.0f - m.em2k[c])) : 1.0f / (4.0f * kPiF);
+}
+SM_HD __forceinline__ void reset_comp(Mix &m, int c) {
+    m.w[c] = 0.0f;
+    m.k[c] = 0.0f;
+    m.r[c] = 0.0f;
+    m.mx[c] = m.my[c] = 0.0f;
+    m.mz[c] = 1.0f;
+    m.nrm[c] = 1.0f / (4.0f * kPiF);
+    m.em2k[c] = 1.0f;
+}
+// setK / cutoff: components from K on are reset
+SM_HD __forceinline__ void set_k(Mix &m, uint32_t K) {
+    m.K = K;
+    for (int c = (int)K; c < KM; ++c) reset_comp(m, c);
+}
+// setKappaAndR (VMFKernel.h:212-227)
+SM_HD __forceinline__ void set_kappa_r(Mix &m, int c, float k, float r) {
+    const bool small = k < 1e-3f;
+    m.k[c] = small ? 0.0f : k;
+    m.r[c] = small ? 0.0f : r;
+    normalise(m, c);
+}
+
+// ParametricMixtureModel::removeWeightPrior / applyWeightPrior
+SM_HD void remove_prior(Mix &m, float v) {
+    const float inv = v * (float)m.K + 1.0f, wpn = 1.0f / inv, wptn = v * wpn;
+    for (uint32_t c = 0; c < active_lanes(m.K); ++c) m.w[c] = (m.w[c] - wptn) * inv;
+    for (uint32_t c = m.K; c < active_lanes(m.K); ++c) m.w[c] = 0.0f;
+}
+SM_HD void apply_prior(Mix &m, float v) {
+    const float inv = v * (float)m.K + 1.0f, wpn = 1.0f / inv, wptn = v * wpn;
+    for (uint32_t c = 0; c < active_lanes(m.K); ++c) m.w[c] = m.w[c] * wpn + wptn;
+    for (uint32_t c = m.K; c < active_lanes(m.K); ++c) m.w[c] = 0.0f;
+}
+
+// lightpmm's exp of its 4-wide arithmetic (pmm-vcl.h:158-184): Mineiro's
+// fastpow2 (fastapprox) of x log2(e), clipped at -126, with SSE2 truncation
+// and round-to-nearest conversion.  Within 2e-5 of exp for x <= 0, but the
+// offset of the fractional part is +1 for either sign, so for x > 0 it is off
+// by up to 90%.  The vMF divisions of the merge metric take it at positive
+// arguments, which moves the metric by more than its threshold: the
+// reference's merges follow this function, so it is restated exactly (this
+// file is compiled without FMA contraction, as the SSE2 build rounds every
+// product and sum).
+SM_HD __forceinline__ float lpmm_fastexp(float x) {
+    const float p = 1.442695040f * x;
+    const float clipp = (-126.0f > p) ? -126.0f : p;
+    const float w = (clipp >= -2147483648.0f && clipp < 2147483648.0f) ? truncf(clipp) : clipp;
+    const float z = (clipp - w) + 1.0f;
+    const float t = ((clipp + 121.2740575f) + (27.7280233f / (4.84252568f - z))) - (1.49012907f * z);
+    const float v = 8388608.0f * t;
+    int32_t bits = INT32_MIN;  // cvtps2dq's answer out of range and for NaN
+#ifdef __CUDA_ARCH__
+    if (v >= -2147483648.0f && v < 2147483648.0f) bits = __float2int_rn(v);
+    return __int_as_float(bits);
+#else
+    if (v >= -2147483648.0f && v < 2147483648.0f) bits = (int32_t)nearbyintf(v);
+    float out;
+    memcpy(&out, &bits, sizeof out);
+    return out;
+#endif
+}
+
+// A single vMF lobe as the merge metric manipulates it.
+struct Lobe {
+    float w, mx, my, mz, k, r, nrm, em2k;
+};
+SM_HD __forceinline__ Lobe lobe(const Mix &m, int c) {
+    return Lobe{m.w[c], m.mx[c], m.my[c], m.mz[c], m.k[c], m.r[c], m.nrm[c], m.em2k[c]};
+}
+
+// VMFKernel::product (VMFKernel.h:315-355): a becomes a*b, returns its integral
+SM_HD float product(Lobe &a, const Lobe &b) {
+    float nx = a.mx * a.k + b.mx * b.k, ny = a.my * a.k + b.my * b.k, nz = a.mz * a.k + b.mz * b.k;
+    float nk = sqrtf(nx * nx + ny * ny + nz * nz);
+    const bool small = nk < 1e-3f;
+    nk = small ? 0.0f : nk;
+    if (small) {
+        nx = a.mx, ny = a.my, nz = a.mz;
+    } else {
+        nx /= nk, ny /= nk, nz /= nk;
+    }
+    const float ci = a.nrm, cj = b.nrm;
+    const float e2 = lpmm_fastexp(-2.0f * nk);
+    const float cij = small ? 1.0f / (4.0f * kPiF) : (1.0f / (2.0f * kPiF)) * nk / (1.0f - e2);
+    const float ti = nx * a.mx + ny * a.my + nz * a.mz, tj = nx * b.mx + ny * b.my + nz * b.mz;
+    const float t = a.k * (ti - 1.0f) + b.k * (tj - 1.0f);
+    const float s = lpmm_fastexp(t) * a.w * b.w * (ci * cj) / cij;
+    a = Lobe{s, nx, ny, nz, nk, k2r(nk), cij, e2};
+    return s;
+}
+
+// VMFKernel::division (VMFKernel.h:362-400): a becomes a/b, returns its integral
+SM_HD float division(Lobe &a, const Lobe &b) {
+    float nx = a.mx * a.k - b.mx * b.k, ny = a.my * a.k - b.my * b.k, nz = a.mz * a.k - b.mz * b.k;
+    float nk = sqrtf(nx * nx + ny * ny + nz * nz);
+    const bool small = nk < 1e-3f;
+    nk = small ? 0.0f : nk;
+    if (small) {
+        nx = a.mx, ny = a.my, nz = a.mz;
+    } else {
+        nx /= nk, ny /= nk, nz /= nk;
+    }
+    const float ci = a.nrm, cj = b.nrm;
+    const float e2 = lpmm_fastexp(-2.0f * nk);
+    const float cij = small ? 1.0f / (4.0f * kPiF) : (1.0f / (2.0f * kPiF)) * nk / (1.0f - e2);
+    const float mi = nx * a.mx + ny * a.my + nz * a.mz, mj = nx * b.mx + ny * b.my + nz * b.mz;
+    const float t = a.k * (mi - 1.0f) - b.k * (mj - 1.0f);
+    const float s = lpmm_fastexp(t) * a.w * ci / (b.w * cj * cij);
+    a = Lobe{s, nx, ny, nz, nk, k2r(nk), cij, e2};
+    return s;
+}
+
+// VMFKernel::mergeComponent (VMFKernel.h:478-530), the merged lobe of a and b
+SM_HD Lobe merge_lobes(const Lobe &a, const Lobe &b) {
+    const float w = a.w + b.w;
+    float mx = (a.w * a.r * a.mx + b.w * b.r * b.mx) / w;
+    float my = (a.w * a.r * a.my + b.w * b.r * b.my) / w;
+    float mz = (a.w * a.r * a.mz + b.w * b.r * b.mz) / w;
+    float r = mx * mx + my * my + mz * mz;
+    float k = 0.0f, nrm = 1.0f / (4.0f * kPiF), em2k = 1.0f;
+    if (r > 0.0f) {
+        r = sqrtf(r);
+        k = r2k(r);
+        k = k < 1e-3f ? 0.0f : k;
+        em2k = expf(-2.0f * k);
+        nrm = k / (2.0f * kPiF * (1.0f - em2k));  // 0/0 when the merged lobe is flat, as in the reference
+        mx /= r, my /= r, mz /= r;
+    } else {
+        mx = a.mx, my = a.my, mz = a.mz;
+    }
+    return Lobe{w, mx, my, mz, k, r, nrm, em2k};
+}
+
+// computePearsonChiSquaredMergeMetric for one pair (src/PathGuiding.cpp:709-760)
+SM_HD float merge_metric(const Mix &m, int i, int j) {
+    const Lobe ci = lobe(m, i), cj = lobe(m, j);
+    Lobe si = ci, sj = cj, pij = ci;
+    product(si, ci);
+    product(sj, cj);
+    product(pij, cj);
+    const Lobe merged = merge_lobes(ci, cj);
+    const float q1 = division(si, merged), q2 = division(pij, merged), q3 = division(sj, merged);
+    return q1 + 2.0f * q2 + q3 - merged.w;
+}
+
+// lightpmm::coordinateAxis / Frame (pmm-glm.h:107-133)
+SM_HD void coordinate_axis(const float z[3], float x[3], float y[3]) {
+    if (fabsf(z[0]) > fabsf(z[1])) {
+        const float inv = 1.0f / sqrtf(z[0] * z[0] + z[2] * z[2]);
+        y[0] = z[2] * inv, y[1] = 0.0f, y[2] = -z[0] * inv;
+    } else {
+        const float inv = 1.0f / sqrtf(z[1] * z[1] + z[2] * z[2]);
+        y[0] = 0.0f, y[1] = z[2] * inv, y[2] = -z[1] * inv;
+    }
+    x[0] = y[1] * z[2] - y[2] * z[1];
+    x[1] = y[2] * z[0] - y[0] * z[2];
+    x[2] = y[0] * z[1] - y[1] * z[0];
+}
+
+// Statistic merges (incrementaldistance.h:165-204, incrementalpearsonchisquared.h:176-204,
+// incrementalcovariance2d.h:200-247) for components a < b with `last` the last component.
+SM_HD void merge_stats(const Mix &m, Stats &s, int a, int b, int last) {
+    const float wa = m.w[a], wb = m.w[b], mw = wa + wb;
+    // parallax distance: harmonic means
+    {
+        const float msw = mw / (wa / s.dw[a] + wb / s.dw[b]);
+        const float md = mw / (wa / s.dist[a] + wb / s.dist[b]);
+        s.dist[a] = md;
+        s.dw[a] = msw;
+    }
+    const float inv = 1.0f / mw;
+    // chi-square
+    if (!isinf(inv)) {
+        const float sa = wa * inv, sb = wb * inv;
+        const float d = sa * s.div[a] + sb * s.div[b];
+        const float n = sa * s.dn[a] + sb * s.dn[b];
+        s.div[a] = d;
+        s.dn[a] = n;
+    } else {
+        s.div[a] = 0.0f;
+        s.dn[a] = 0.0f;
+    }
+    // covariance; the merged mean is scaled by 1/3, what GLM's vec3::length() returns
+    if (!isinf(inv)) {
+        float mu[3] = {wa * m.mx[a] + wb * m.mx[b], wa * m.my[a] + wb * m.my[b], wa * m.mz[a] + wb * m.mz[b]};
+        const float sc = 1.0f / 3.0f;
+        for (int i = 0; i < 3; ++i) mu[i] *= sc;
+        float fx[3], fy[3];
+        coordinate_axis(mu, fx, fy);
+        const float ax = m.mx[a] * fx[0] + m.my[a] * fx[1] + m.mz[a] * fx[2];
+        const float ay = m.mx[a] * fy[0] + m.my[a] * fy[1] + m.mz[a] * fy[2];
+        const float bx = m.mx[b] * fx[0] + m.my[b] * fx[1] + m.mz[b] * fx[2];
+        const float by = m.mx[b] * fy[0] + m.my[b] * fy[1] + m.mz[b] * fy[2];
+        const float msw = s.cw[a] + s.cw[b];
+        const float f = wa * wb / mw;
+        const float dx = ax - bx, dy = ay - by;
+        const float dv[3] = {dx * dx, dy * dy, dx * dy};
+        for (int i = 0; i < 3; ++i) s.cov[a][i] = (wa * s.cov[a][i] + wb * s.cov[b][i] + f * dv[i]) * inv;
+        s.cw[a] = msw;
+    } else {
+        s.cov[a][0] = s.cov[a][1] = s.cov[a][2] = 0.0f;
+        s.cw[a] = 0.0f;
+    }
+    if (b != last) {
+        s.dist[b] = s.dist[last];
+        s.dw[b] = s.dw[last];
+        s.div[b] = s.div[last];
+        s.dn[b] = s.dn[last];
+        for (int i = 0; i < 3; ++i) s.cov[b][i] = s.cov[last][i];
+        s.cw[b] = s.cw[last];
+    }
+}
+
+// ParametricMixtureModel::mergeComponents: a takes the merge, b is reset and
+// swapped with the last component, K decreases.
+SM_HD void merge_components(Mix &m, Stats &s, int a, int b) {
+    const int last = (int)m.K - 1;
+    merge_stats(m, s, a, b, last);
+    const Lobe mg = merge_lobes(lobe(m, a), lobe(m, b));
+    m.w[a] = mg.w, m.k[a] = mg.k, m.r[a] = mg.r;
+    m.mx[a] = mg.mx, m.my[a] = mg.my, m.mz[a] = mg.mz;
+    m.nrm[a] = mg.nrm, m.em2k[a] = mg.em2k;
+    reset_comp(m, b);
+    m.K -= 1;
+    if (b != (int)m.K) {  // swapComponents(b, K)
+        const Lobe t = lobe(m, b);
+        m.w[b] = m.w[m.K], m.k[b] = m.k[m.K], m.r[b] = m.r[m.K];
+        m.mx[b] = m.mx[m.K], m.my[b] = m.my[m.K], m.mz[b] = m.mz[m.K];
+        m.nrm[b] = m.nrm[m.K], m.em2k[b] = m.em2k[m.K];
+        m.w[m.K] = t.w, m.k[m.K] = t.k, m.r[m.K] = t.r;
+        m.mx[m.K] = t.mx, m.my[m.K] = t.my, m.mz[m.K] = t.mz;
+        m.nrm[m.K] = t.nrm, m.em2k[m.K] = t.em2k;
+    }
+}
+
+// libstdc++ std::partition (two-ended), over keys with their payload
+template <class Pred>
+SM_HD int hoare_partition(float *key, int *pa, int *pb, int n, Pred pred) {
+    int first = 0, last = n;
+    while (true) {
+        while (true) {
+            if (first == last) return first;
+            if (pred(key[first])) ++first;
+            else break;
+        }
+        --last;
+        while (true) {
+            if (first == last) return first;
+            if (!pred(key[last])) --last;
+            else break;
+        }
+        float tk = key[first];
+        key[first] = key[last];
+        key[last] = tk;
+        int t = pa[first];
+        pa[first] = pa[last];
+        pa[last] = t;
+        if (pb) {
+            t = pb[first];
+            pb[first] = pb[last];
+            pb[last] = t;
+        }
+        ++first;
+    }
+}
+
+// mergeAll (src/PathGuiding.cpp:635-707), thread 0
+SM_HD void merge_all(Mix &m, Stats &s, const pg_split_merge_config &cfg) {
+    float key[KM * (KM - 1) / 2];
+    int ca[KM * (KM - 1) / 2], cb[KM * (KM - 1) / 2];
+    for (int round = 0; round < KM; ++round) {
+        const int n = (int)m.K;
+        if (n <= 1) return;
+        int idx = 0;
+        for (int a = 0; a < n; ++a)
+            for (int b = a + 1; b < n; ++b, ++idx) {
+                key[idx] = merge_metric(m, a, b);
+                ca[idx] = a;
+                cb[idx] = b;
+            }
+        const float thr = cfg.merge_max_divergence;
+        const int end = hoare_partition(key, ca, cb, idx, [thr](float v) { return v <= thr; });
+        // sort by metric ascending (insertion; the reference's std::sort on distinct values)
+        for (int i = 1; i < end; ++i) {
+            const float k = key[i];
+            const int a = ca[i], b = cb[i];
+            int j = i - 1;
+            while (j >= 0 && key[j] > k) {
+                key[j + 1] = key[j], ca[j + 1] = ca[j], cb[j + 1] = cb[j];
+                --j;
+            }
+            key[j + 1] = k, ca[j + 1] = a, cb[j + 1] = b;
+        }
+        uint32_t used = 0;
+        int ma[KM], mb[KM], nm = 0;
+        for (int i = 0; i < end; ++i) {
+            const int a = min(ca[i], cb[i]), b = max(ca[i], cb[i]);
+            if ((used >> a) & 1u || (used >> b) & 1u) continue;
+            ma[nm] = a, mb[nm] = b, ++nm;
+            used |= (1u << a) | (1u << b);
+        }
+        if (nm == 0) return;
+        // by second index, descending, so later merges keep their indices
+        for (int i = 1; i < nm; ++i) {
+            const int a = ma[i], b = mb[i];
+            int j = i - 1;
+            while (j >= 0 && mb[j] < b) {
+                ma[j + 1] = ma[j], mb[j + 1] = mb[j];
+                --j;
+            }
+            ma[j + 1] = a, mb[j + 1] = b;
+        }
+        for (int i = 0; i < nm; ++i) merge_components(m, s, ma[i], mb[i]);
+    }
+}
+
+// Principal axis of the symmetric 2x2 covariance [[a, b], [b, c]]
+SM_HD void principal_axis(float a, float b, float c, float &lambda, float &vx, float &vy) {
+    const float h = 0.5f * (a - c);
+    const float d = sqrtf(h * h + b * b);
+    lambda = 0.5f * (a + c) + d;
+    if (b == 0.0f) {
+        vx = a >= c ? 1.0f : 0.0f;
+        vy = a >= c ? 0.0f : 1.0f;
+        return;
+    }
+    if (a >= c) {
+        vx = lambda - c;
+        vy = b;
+    } else {
+        vx = b;
+        vy = lambda - a;
+    }
+    const float inv = 1.0f / sqrtf(vx * vx + vy * vy);
+    vx *= inv;
+    vy *= inv;
+}
+
+// splitComponentUsingPCA (src/PathGuiding.cpp:494-561), thread 0
+SM_HD void split_component(Mix &m, Stats &s, int c, float max_kappa) {
+    if (m.K == KM) return;
+    const int dst = (int)m.K;
+    const float z3[3] = {m.mx[c], m.my[c], m.mz[c]};
+    float fx[3], fy[3];
+    coordinate_axis(z3, fx, fy);
+    const bool has = s.cw[c] > 0.0f;
+    const float va = has ? s.cov[c][0] : 0.0f, vb = has ? s.cov[c][2] : 0.0f, vc = has ? s.cov[c][1] : 0.0f;
+    float lambda, px, py;
+    principal_axis(va, vb, vc, lambda, px, py);
+    const float off = fminf(1.0f, 0.5f * sqrtf(lambda));
+    px *= off;
+    py *= off;
+    const float z = sqrtf(1.0f - off * off);
+    float a[3], b[3];
+    for (int i = 0; i < 3; ++i) {
+        a[i] = px * fx[i] + py * fy[i] + z * z3[i];
+        b[i] = -px * fx[i] + -py * fy[i] + z * z3[i];
+    }
+    set_k(m, m.K + 1);
+    const float src_r = m.r[c], src_w = m.w[c];
+    const float split_w = src_w * 0.5f;
+    const float max_r = k2r(max_kappa);
+    const float split_r = z > 0.0f ? fminf(max_r, src_r / z) : max_r;
+    const float split_k = r2k(split_r);
+    set_kappa_r(m, c, split_k, split_r);
+    m.mx[c] = a[0], m.my[c] = a[1], m.mz[c] = a[2];
+    m.w[c] = split_w;
+    set_kappa_r(m, dst, split_k, split_r);
+    m.mx[dst] = b[0], m.my[dst] = b[1], m.mz[dst] = b[2];
+    m.w[dst] = split_w;
+    // statistics (incrementaldistance.h:206-216, chi-square and covariance reset)
+    s.dist[dst] = s.dist[c];
+    const float hw = 0.5f * s.dw[c];
+    s.dw[c] = hw;
+    s.dw[dst] = hw;
+    s.div[c] = s.div[dst] = 0.0f;
+    s.dn[c] = s.dn[dst] = 0.0f;
+    for (int i = 0; i < 3; ++i) s.cov[c][i] = s.cov[dst][i] = 0.0f;
+    s.cw[c] = s.cw[dst] = 0.0f;
+}
+
+// vMF pdf of component c (VMFKernel::pdf: cos clamped at 1)
+__device__ __forceinline__ float comp_pdf(const Mix &m, int c, float dx, float dy, float dz) {
+    const float cs = m.mx[c] * dx + m.my[c] * dy + m.mz[c] * dz;
+    return m.nrm[c] * expf(m.k[c] * fminf(cs - 1.0f, 0.0f));
+}
+
+// Block reduction of per-thread values v[0..n) into S.acc[0..n), fixed order.
+__device__ void block_sum(Shared &S, float *v, int n) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = 0; i < n; ++i) {
+        float x = v[i];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) S.red[warp][i] = x;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        float x = 0.0f;
+        for (int w = 0; w < NW; ++w) x += S.red[w][i];
+        S.acc[i] = x;
+    }
+    __syncthreads();
+}
+
+// Pass kinds over the region's samples
+enum { PASS_CHI2 = 0, PASS_COV = 1, PASS_EM = 2 };
+
+// One pass: per component sums into S.acc (chi2: [c]; cov: [4c..4c+3] =
+// weight, xx, yy, xy; em: [4c..4c+3] = sum gamma w d.xyz, [64 + c]... see below).
+template <int KIND>
+__device__ void sample_pass(Shared &S, const Args &A, uint32_t b, uint32_t e, float s_frame[KM][3],
+                            float t_frame[KM][3]) {
+    const Mix &m = S.m;
+    const int L = (int)active_lanes(m.K);
+    float v[4 * KM + 2];
+    for (int i = 0; i < 4 * KM + 2; ++i) v[i] = 0.0f;
+    for (uint32_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+        const float4 d = A.dirw[i];
+        float p[KM];
+        float mix = 0.0f;
+        for (int c = 0; c < L; ++c) {
+            p[c] = comp_pdf(m, c, d.x, d.y, d.z);
+            mix += m.w[c] * p[c];
+        }
+        if (!(mix > kPmmEps)) continue;
+        if (KIND == PASS_CHI2) {
+            const float f = d.w * d.w * A.pdf[i] / (mix * mix);
+            for (int c = 0; c < L; ++c) v[c] += p[c] * f;
+        } else if (KIND == PASS_COV) {
+            const float inv = 1.0f / mix;
+            for (int c = 0; c < L; ++c) {
+                const float wt = d.w * (m.w[c] * p[c] * inv);
+                const float lx = s_frame[c][0] * d.x + s_frame[c][1] * d.y + s_frame[c][2] * d.z;
+                const float ly = t_frame[c][0] * d.x + t_frame[c][1] * d.y + t_frame[c][2] * d.z;
+                v[4 * c] += wt;
+                v[4 * c + 1] += lx * lx * wt;
+                v[4 * c + 2] += ly * ly * wt;
+                v[4 * c + 3] += lx * ly * wt;
+            }
+        } else {
+            const float inv = 1.0f / mix;
+            for (int c = 0; c < L; ++c) {
+                const float g = m.w[c] * p[c] * inv * d.w;
+                v[4 * c] += g * d.x;
+                v[4 * c + 1] += g * d.y;
+                v[4 * c + 2] += g * d.z;
+                v[4 * c + 3] += g;
+            }
+            v[4 * KM] += d.w;
+            v[4 * KM + 1] += d.w * logf(mix);
+        }
+    }
+    block_sum(S, v, KIND == PASS_CHI2 ? KM : 4 * KM + 2);
+}
+
+// incrementalcovariance2d.h:67-77: the tangent frame of each component's mean
+__device__ void cov_frames(const Mix &m, float s_frame[KM][3], float t_frame[KM][3]) {
+    for (int c = 0; c < KM; ++c) {
+        const float nx = m.mx[c], ny = m.my[c], nz = m.mz[c];
+        const bool xg = nx * nx > ny * ny;
+        const float inv = 1.0f / sqrtf((xg ? nx * nx : ny * ny) + nz * nz);
+        float t[3];
+        if (xg) {
+            t[0] = nz * inv, t[1] = 0.0f, t[2] = -nx * inv;
+        } else {
+            t[0] = 0.0f, t[1] = nz * inv, t[2] = -ny * inv;
+        }
+        t_frame[c][0] = t[0], t_frame[c][1] = t[1], t_frame[c][2] = t[2];
+        s_frame[c][0] = t[1] * nz - t[2] * ny;
+        s_frame[c][1] = t[2] * nx - t[0] * nz;
+        s_frame[c][2] = t[0] * ny - t[1] * nx;
+    }
+}
+
+// updateDivergence(Masked) and updateStatistics(Masked) over the region's samples
+__device__ void update_stats(Shared &S, const Args &A, uint32_t b, uint32_t e, uint32_t mask) {
+    __shared__ float sf[KM][3], tf[KM][3];
+    const int L = (int)active_lanes(S.m.K);
+    const float n = (float)(e - b);
+    sample_pass<PASS_CHI2>(S, A, b, e, sf, tf);
+    if (threadIdx.x == 0)
+        for (int c = 0; c < L; ++c) {
+            if (!((mask >> c) & 1u)) continue;
+            const float nn = S.s.dn[c] + n;
+            S.s.div[c] = (S.s.div[c] * S.s.dn[c] + S.acc[c]) / nn;
+            S.s.dn[c] = nn;
+        }
+    __syncthreads();
+    if (threadIdx.x == 0) cov_frames(S.m, sf, tf);
+    __syncthreads();
+    sample_pass<PASS_COV>(S, A, b, e, sf, tf);
+    if (threadIdx.x == 0)
+        for (int c = 0; c < L; ++c) {
+            if (!((mask >> c) & 1u)) continue;
+            const float nw = S.s.cw[c] + S.acc[4 * c];
+            for (int i = 0; i < 3; ++i)
+                S.s.cov[c][i] = nw > 0.0f ? (S.s.cov[c][i] * S.s.cw[c] + S.acc[4 * c + 1 + i]) / nw : 0.0f;
+            S.s.cw[c] = nw;
+        }
+    __syncthreads();
+}
+
+// VMMFactory::maskedFit with maskedParameterUpdate (VMMFactory.h:226-297, 458-485)
+__device__ void masked_fit(Shared &S, const Args &A, uint32_t b, uint32_t e) {
+    const pg_fit_config &cfg = A.cfg;
+    Mix &m = S.m;
+    const uint32_t K = m.K;
+    const float inv_wpn = cfg.v_prior * (float)K + 1.0f, wpn = 1.0f / inv_wpn, wptn = cfg.v_prior * wpn;
+    float old_active = 0.0f;
+    if (threadIdx.x == 0) {
+        set_k(m, K);  // resetInactiveComponents
+        for (int c = 0; c < (int)active_lanes(K); ++c)
+            if ((S.mask >> c) & 1u) old_active += m.w[c] > wptn ? (m.w[c] - wptn) * inv_wpn : 0.0f;
+        S.fit_iters = (e - b) > 2u * K ? (int)cfg.max_itr : 0;
+        S.ll_last = 0.0f;
+        S.ll_abs_inv = 0.0f;
+    }
+    __syncthreads();
+    const int iters = S.fit_iters;
+    const float max_r = k2r(cfg.max_kappa);
+    for (int it = 0; it < iters; ++it) {
+        sample_pass<PASS_EM>(S, A, b, e, nullptr, nullptr);
+        if (threadIdx.x == 0) {
+            if (it == 0) S.sum_w = S.acc[4 * KM];
+            const float sum_w = S.sum_w;
+            float active = 0.0f;
+            for (int c = 0; c < (int)active_lanes(K); ++c)
+                if ((S.mask >> c) & 1u) active += S.acc[4 * c + 3];
+            const float norm = old_active * (sum_w / active);
+            for (int c = 0; c < (int)active_lanes(K); ++c) {
+                if (!((S.mask >> c) & 1u)) continue;
+                float sx = S.acc[4 * c] * norm, sy = S.acc[4 * c + 1] * norm, sz = S.acc[4 * c + 2] * norm;
+                const float sw = S.acc[4 * c + 3] * norm;
+                const float mw = (sw / sum_w) * wpn + wptn;
+                const float rl = sqrtf(sx * sx + sy * sy + sz * sz);
+                if (rl > 0.0f) {
+                    m.mx[c] = sx / rl;
+                    m.my[c] = sy / rl;
+                    m.mz[c] = sz / rl;
+                }
+                const float avg = rl / sw;
+                const float nsc = (float)m.total * mw;
+                float ap = (avg * nsc + cfg.r_prior * cfg.r_prior_weight) / (nsc + cfg.r_prior_weight);
+                ap = fminf(ap, max_r);
+                m.w[c] = mw;
+                set_kappa_r(m, c, r2k(ap), ap);
+            }
+            set_k(m, K);
+            // relative log-likelihood stop (VMMFactory.h:284-295)
+            int stop = 0;
+            const float ll = S.acc[4 * KM + 1];
+            if ((uint32_t)it >= cfg.min_itr) {
+                if ((uint32_t)it > cfg.min_itr) {
+                    const float rel = (ll - S.ll_last) * S.ll_abs_inv;
+                    if (rel < cfg.rel_ll_threshold) stop = 1;
+                }
+                if (!stop) {
+                    S.ll_last = ll;
+                    S.ll_abs_inv = 1.0f / fabsf(ll);
+                }
+            }
+            S.stop = stop;
+        }
+        __syncthreads();
+        if (S.stop) break;
+    }
+}
+
+__global__ void __launch_bounds__(NT) k_split_merge(Args A) {
+    __shared__ Shared S;
+    const uint32_t r = blockIdx.x;
+    if (r >= A.n_regions) return;
+    const uint32_t b = A.offsets[r], e = A.offsets[r + 1];
+    if (e == b) return;  // PathGuiding::update skips empty regions
+    pg_region_state *st = A.states + r;
+    pg_region_extra *ex = A.extras + r;
+    if (threadIdx.x == 0) {
+        Mix &m = S.m;
+        m.K = min(st->k, (uint32_t)KM);
+        for (int c = 0; c < KM; ++c) {
+            m.w[c] = st->weight[c];
+            m.mx[c] = st->mu_x[c];
+            m.my[c] = st->mu_y[c];
+            m.mz[c] = st->mu_z[c];
+            m.k[c] = st->kappa[c];
+            m.r[c] = st->r[c];
+            m.nrm[c] = st->norm[c];
+            m.em2k[c] = st->e_min2k[c];
+            S.s.div[c] = ex->chi2_div[c];
+            S.s.dn[c] = ex->chi2_n[c];
+            for (int i = 0; i < 3; ++i) S.s.cov[c][i] = ex->cov[c][i];
+            S.s.cw[c] = ex->cov_w[c];
+            S.s.dist[c] = st->distance[c];
+            S.s.dw[c] = st->dist_sum_w[c];
+        }
+        m.sample_weight = st->sample_weight;
+        m.num_samples = st->num_samples;
+        m.total = st->total_num_samples;
+        S.s.since = ex->samples_since_merge + (float)(e - b);
+        if (S.s.since > (float)A.sm.min_samples_for_merging) {
+            remove_prior(m, A.cfg.v_prior);
+            merge_all(m, S.s, A.sm);
+            apply_prior(m, A.cfg.v_prior);
+            S.s.since = 0.0f;
+        }
+    }
+    __syncthreads();
+    update_stats(S, A, b, e, 0xFFFFu);
+    const bool first = (unsigned long long)(e - b) == S.m.total;
+    const bool fit = first || (e - b) > A.sm.min_samples_for_post_split_fitting;
+    if (threadIdx.x == 0) remove_prior(S.m, A.cfg.v_prior);
+    __syncthreads();
+    if (S.m.K < (uint32_t)KM) {
+        for (int round = 0; round < KM; ++round) {
+            __shared__ int n_split;
+            if (threadIdx.x == 0) {
+                Mix &m = S.m;
+                // split candidates by weighted divergence (computeDivergence,
+                // incrementalpearsonchisquared.h:141-153)
+                const float ia = (m.num_samples * m.num_samples) / (m.sample_weight * m.sample_weight);
+                float key[KM];
+                int cand[KM];
+                for (int c = 0; c < (int)m.K; ++c) {
+                    const float div = S.s.div[c] * ia - 1.0f;
+                    const bool enough = S.s.dn[c] > (float)A.sm.min_samples_for_splitting;
+                    key[c] = fabsf((first || enough) ? div * m.w[c] : 0.0f);
+                    cand[c] = c;
+                }
+                const float thr = A.sm.split_min_divergence;
+                const int nc = hoare_partition(key, cand, (int *)nullptr, (int)m.K,
+                                               [thr](float v) { return v >= thr; });
+                const int ns = min(nc, KM - (int)m.K);
+                if (ns > 0 && nc > ns) {  // std::partial_sort: the ns largest, descending
+                    for (int i = 1; i < nc; ++i) {
+                        const float k = key[i];
+                        const int c = cand[i];
+                        int j = i - 1;
+                        while (j >= 0 && key[j] < k) {
+                            key[j + 1] = key[j], cand[j + 1] = cand[j];
+                            --j;
+                        }
+                        key[j + 1] = k, cand[j + 1] = c;
+                    }
+                }
+                uint32_t mask = 0;
+                for (int i = 0; i < ns; ++i) {
+                    mask |= 1u << cand[i];
+                    mask |= 1u << m.K;
+                    split_component(m, S.s, cand[i], A.cfg.max_kappa);
+                }
+                S.mask = mask;
+                n_split = ns;
+                if (ns > 0 && fit) apply_prior(m, A.cfg.v_prior);
+            }
+            __syncthreads();
+            if (n_split == 0) break;
+            if (fit) {
+                masked_fit(S, A, b, e);
+                update_stats(S, A, b, e, S.mask);
+                if (threadIdx.x == 0) remove_prior(S.m, A.cfg.v_prior);
+                __syncthreads();
+            }
+        }
+    }
+    if (threadIdx.x == 0) {
+        Mix &m = S.m;
+        apply_prior(m, A.cfg.v_prior);
+        st->k = m.K;
+        for (int c = 0; c < KM; ++c) {
+            st->weight[c] = m.w[c];
+            st->mu_x[c] = m.mx[c];
+            st->mu_y[c] = m.my[c];
+            st->mu_z[c] = m.mz[c];
+            st->kappa[c] = m.k[c];
+            st->r[c] = m.r[c];
+            st->norm[c] = m.nrm[c];
+            st->e_min2k[c] = m.em2k[c];
+            st->distance[c] = S.s.dist[c];
+            st->dist_sum_w[c] = S.s.dw[c];
+            ex->chi2_div[c] = S.s.div[c];
+            ex->chi2_n[c] = S.s.dn[c];
+            for (int i = 0; i < 3; ++i) ex->cov[c][i] = S.s.cov[c][i];
+            ex->cov_w[c] = S.s.cw[c];
+        }
+        ex->samples_since_merge = S.s.since;
+    }
+}
+
+}  // namespace sm
+}  // namespace pg
+
+namespace pg {
+
+int extras_ensure(pg_ctx *ctx, cudaStream_t s) {
+    if (ctx->d_extras) return PG_OK;
+    int st = check_cuda(ctx, cudaMalloc(&ctx->d_extras, sizeof(pg_region_extra) * (size_t)ctx->max_regions),
+                        "split/merge statistics");
+    if (!st) st = extras_reset(ctx, 0, ctx->max_regions, s);
+    return st;
+}
+
+void extras_release(pg_ctx *ctx) {
+    if (ctx && ctx->d_extras) cudaFree(ctx->d_extras);
+    if (ctx) ctx->d_extras = nullptr;
+}
+
+int extras_reset(pg_ctx *ctx, uint32_t first, uint32_t n, cudaStream_t s) {
+    if (!ctx->d_extras || n == 0) return PG_OK;
+    return check_cuda(ctx, cudaMemsetAsync(ctx->d_extras + first, 0, sizeof(pg_region_extra) * (size_t)n, s),
+                      "split/merge statistics reset");
+}
+
+}  // namespace pg
+
+using namespace pg;
+
+extern "C" {
+
+void pg_default_split_merge_config(pg_split_merge_config *out) {
+    if (!out) return;
+    out->enabled = 1;
+    out->min_samples_for_merging = 8192;
+    out->min_samples_for_splitting = 4096;
+    out->min_samples_for_post_split_fitting = 4096;
+    out->split_min_divergence = 0.5f;
+    out->merge_max_divergence = 0.025f;
+}
+
+int pg_set_split_merge(pg_ctx *ctx, const pg_split_merge_config *cfg) {
+    if (!ctx || !cfg) return PG_ERR_ARG;
+    if (cfg->enabled) {
+        if (int st = extras_ensure(ctx, nullptr)) return st;
+        if (cudaDeviceSynchronize() != cudaSuccess) return set_error(ctx, PG_ERR_CUDA, "split/merge setup");
+    }
+    ctx->sm = *cfg;
+    return PG_OK;
+}
+
+int pg_split_merge(pg_ctx *ctx, const float *dirw, const float *pdf, const uint32_t *offsets, uint32_t n_regions,
+                   void *stream) {
+    if (!ctx || !dirw || !pdf || !offsets) return PG_ERR_ARG;
+    if (n_regions > ctx->max_regions) return set_error(ctx, PG_ERR_ARG, "n_regions exceeds context capacity");
+    if (n_regions == 0) return PG_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (int st = extras_ensure(ctx, s)) return st;
+    sm::Args A;
+    A.states = ctx->d_states;
+    A.extras = ctx->d_extras;
+    A.dirw = reinterpret_cast<const float4 *>(dirw);
+    A.pdf = pdf;
+    A.offsets = offsets;
+    A.n_regions = n_regions;
+    A.cfg = ctx->cfg;
+    A.sm = ctx->sm;
+    if (!A.sm.min_samples_for_merging && !A.sm.split_min_divergence) pg_default_split_merge_config(&A.sm);
+    A.sm.enabled = 1;
+    sm::k_split_merge<<<n_regions, sm::NT, 0, s>>>(A);
+    return check_cuda(ctx, cudaGetLastError(), "split/merge launch");
+}
+
+int pg_get_region_extra(pg_ctx *ctx, pg_region_extra *host_out, uint32_t count) {
+    if (!ctx || (!host_out && count)) return PG_ERR_ARG;
+    if (count > ctx->max_regions) return set_error(ctx, PG_ERR_ARG, "count exceeds context capacity");
+    if (int st = extras_ensure(ctx, nullptr)) return st;
+    return check_cuda(ctx, cudaMemcpy(host_out, ctx->d_extras, sizeof(pg_region_extra) * count, cudaMemcpyDeviceToHost),
+                      "split/merge statistics download");
+}
+
+int pg_set_region_extra(pg_ctx *ctx, const pg_region_extra *host_in, uint32_t count) {
+    if (!ctx || (!host_in && count)) return PG_ERR_ARG;
+    if (count > ctx->max_regions) return set_error(ctx, PG_ERR_ARG, "count exceeds context capacity");
+    if (int st = extras_ensure(ctx, nullptr)) return st;
+    return check_cuda(ctx, cudaMemcpy(ctx->d_extras, host_in, sizeof(pg_region_extra) * count, cudaMemcpyHostToDevice),
+                      "split/merge statistics upload");
+}
+
+}  // extern "C"

@@ -57,22 +57,28 @@ class SampleCollector:
 
 
 class PathGuiding:
-    """PathGuiding(splitCount, sceneAabb, useParallaxCompensation)."""
+    """PathGuiding(splitCount, sceneAabb, useParallaxCompensation); split and
+    merge of mixture components after each fit is on by default, as the
+    reference's splitAndMerge (src/PathGuiding.h:124)."""
 
     def __init__(self, split_count: int, scene_aabb, use_parallax: bool = True, cfg: "abi.FitConfig | None" = None,
-                 stream=None):
+                 stream=None, split_and_merge: "bool | abi.SplitMergeConfig" = True):
         cfg = cfg if cfg is not None else abi.default_fit_config()
         cfg.use_parallax = 1 if use_parallax else 0
         self.split_count = split_count
         self.ctx = FitContext(cfg, max_regions=1 << split_count)
         self.ctx.set_regions(split_count, np.asarray(scene_aabb, dtype=np.float32), stream=stream)
+        if isinstance(split_and_merge, abi.SplitMergeConfig):
+            self.ctx.set_split_merge(split_and_merge)
+        elif split_and_merge:
+            self.ctx.set_split_merge()
 
     def get_region_count(self) -> int:
         return self.ctx.region_count()
 
     def update(self, collector: SampleCollector, stream=None) -> bool:
         """One guiding pass over the collector's records (bucket, parallax
-        pre-pass, fit or stepwise update, distances, VMM_Theta).  Returns
+        pre-pass, fit or stepwise update, split and merge, distances, VMM_Theta).  Returns
         whether the tracer must rebind its region buffers; regions are never
         re-split here, so always False."""
         self.ctx.update(collector.buffer, collector.n_slots, stream=stream)

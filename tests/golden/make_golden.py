@@ -80,8 +80,106 @@ def main():
     # lightpmm's exp approximation on a grid
     x = np.concatenate([np.linspace(-130.0, 0.0, 4001), -np.logspace(-6, 1, 200)]).astype(np.float32)
     save("fastexp", x=x, y=ref.fastexp(x))
+    make_splitmerge(ref)
+    make_update_splitmerge(ref)
     print("golden fixtures written to", HERE)
 
 
+# Split/merge sequences: region sample counts per pass, the split/merge knobs
+# and the number of passes.  "default" uses the reference's knobs
+# (src/PathGuiding.h:124-129); "eager" lowers the sample thresholds so small
+# regions merge, split and refit within a few passes.
+SPLITMERGE = {
+    "default": (np.array([0, 40, 700, 2800, 4500, 8500, 1500], dtype=np.int64), {}, 3),
+    "eager": (np.array([0, 30, 300, 800, 1500, 2500, 600], dtype=np.int64),
+              {"min_samples_for_merging": 2048, "min_samples_for_splitting": 1024,
+               "min_samples_for_post_split_fitting": 1024}, 4),
+}
+
+
+def make_splitmerge(ref):
+    """PathGuiding::update over several passes (fit, then postFit with split
+    and merge) on samples of fixed per-region mixtures; stores every pass's
+    samples, the fitted states that enter postFit and what postFit returns."""
+    for name, (counts, knobs, passes) in SPLITMERGE.items():
+        rng = np.random.default_rng(4242 if name == "default" else 5151)
+        w = wl.mixture_samples(rng, counts * passes, 1, 6, 2.0, 2000.0, 1.0)
+        R = counts.shape[0]
+        cfg = abi.default_fit_config(num_initial_components=8)
+        sm = abi.default_split_merge_config(**knobs)
+        st = ref.init_states(cfg, R)
+        ex = np.zeros(R, dtype=abi.EXTRA_DTYPE)
+        big = w["offsets"].astype(np.int64)
+        out = {"cfg": np.array(list(cfg_dict(cfg).values()), dtype=np.float64),
+               "sm": np.array(list(cfg_dict(sm).values()), dtype=np.float64), "passes": np.array(passes)}
+        for p in range(passes):
+            idx = np.concatenate([np.arange(big[r] + p * counts[r], big[r] + (p + 1) * counts[r]) for r in range(R)])
+            dirw = np.ascontiguousarray(w["dirw"][idx])
+            offsets = np.concatenate([[0], np.cumsum(counts)]).astype(np.uint32)
+            pdf = (rng.uniform(0.5, 2.0, dirw.shape[0]) / (4.0 * np.pi)).astype(np.float32)
+            st, _ = ref.fit(cfg, dirw, offsets, states=st, mode=abi.PG_FIT_CONTINUE if p == 0 else abi.PG_FIT_UPDATE)
+            fitted, ex_in = st.copy(), ex.copy()
+            st, ex = ref.postfit(cfg, sm, dirw, pdf, None, offsets, st, ex)
+            out.update({f"dirw{p}": dirw, f"pdf{p}": pdf, f"offsets{p}": offsets, f"fitted{p}": fitted,
+                        f"extras_in{p}": ex_in, f"states{p}": st.copy(), f"extras{p}": ex.copy()})
+            print(name, "pass", p, "K", st["k"].tolist(), "since", ex["samples_since_merge"].tolist())
+        save(f"splitmerge_{name}", **out)
+
+
+def make_update_splitmerge(ref):
+    """Whole PathGuiding::update passes with splitAndMerge on: the tracer's
+    records in, per pass the reference's states and split/merge statistics
+    out.  Bucketing, region centres, reposition and the parallax pre-pass are
+    the oracle's (pinned against the reference by the other fixtures); fit and
+    postFit (merge, statistics, split, distances) are the reference's."""
+    build_oracle.build_oracle()
+    from oracle.oracle import Oracle  # noqa: E402
+    orc = Oracle()
+    split_count, passes = 3, 3
+    scene = np.array([-1.0, -1.0, -1.0, 1.0, 1.0, 1.0], dtype=np.float32)
+    boxes = orc.region_aabbs(split_count, scene)
+    R = boxes.shape[0]
+    means = boxes[:, :3] + np.float32(0.5) * (boxes[:, 3:] - boxes[:, :3])
+    rng = np.random.default_rng(8080)
+    counts = wl.region_counts_lognormal(rng, R, 700, 1.0, 0, 6000)
+    counts[2] = 0  # a region that never has samples
+    w = wl.mixture_samples(rng, counts * passes, 1, 5, 3.0, 600.0, 1.0, region_boxes=boxes,
+                           dist_range=(0.05, 30.0), miss_frac=0.1)
+    cfg = abi.default_fit_config(num_initial_components=8)
+    sm = abi.default_split_merge_config(min_samples_for_merging=1536, min_samples_for_splitting=768,
+                                        min_samples_for_post_split_fitting=768)
+    st = ref.init_states(cfg, R)
+    st["distance"][:] = np.inf
+    ex = np.zeros(R, dtype=abi.EXTRA_DTYPE)
+    big = w["offsets"].astype(np.int64)
+    out = {"cfg": np.array(list(cfg_dict(cfg).values()), dtype=np.float64),
+           "sm": np.array(list(cfg_dict(sm).values()), dtype=np.float64), "passes": np.array(passes),
+           "split_count": np.array(split_count), "scene": scene}
+    for p in range(passes):
+        idx = np.concatenate([np.arange(big[r] + p * counts[r], big[r] + (p + 1) * counts[r]) for r in range(R)])
+        rec = w["records"][idx].copy()
+        rec["pdf"] = (rng.uniform(0.5, 2.0, rec.shape[0]) / (4.0 * np.pi)).astype(np.float32)
+        rec = rec[rng.permutation(rec.shape[0])]
+        rec["flags"][rng.random(rec.shape[0]) < 0.1] = 0xFFFFFFFF  # invalid slots
+        srt, off = orc.sort_samples(rec, R)
+        busy = np.diff(off.astype(np.int64)) > 0
+        st["last_parallax_mean"][busy] = st["parallax_mean"][busy]
+        st["parallax_mean"][busy] = means[busy]
+        if p > 0:
+            for r in np.nonzero(busy)[0]:
+                st[r] = ref.reposition(st[r], st["last_parallax_mean"][r] - means[r])
+        dirw, dist = orc.prefit_parallax(srt, off, means)
+        st, _ = ref.fit(cfg, dirw, off, states=st, mode=abi.PG_FIT_CONTINUE if p == 0 else abi.PG_FIT_UPDATE)
+        st, ex = ref.postfit(cfg, sm, dirw, srt["pdf"], dist, off, st, ex)
+        out.update({f"records{p}": rec, f"states{p}": st.copy(), f"extras{p}": ex.copy()})
+        print("update pass", p, "K", st["k"].tolist())
+    save("splitmerge_update", **out)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["splitmerge"]:
+        build_oracle.build_reference(force=False)
+        make_splitmerge(ReferenceFit())
+        make_update_splitmerge(ReferenceFit())
+    else:
+        main()

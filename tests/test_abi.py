@@ -89,10 +89,12 @@ def test_ctypes_mirrors_match_the_header(abi):
     structs = [("pg_fit_config", abi.FitConfig), ("pg_fit_tuning", abi.FitTuning), ("pg_camera", abi.Camera),
                ("pg_cornell_params", abi.CornellParams), ("pg_plates_params", abi.PlatesParams),
                ("pg_scene_info", abi.SceneInfo), ("pg_render_params", abi.RenderParams),
-               ("pg_render_stats", abi.RenderStats), ("pg_mlp_config", abi.MlpConfig)]
+               ("pg_render_stats", abi.RenderStats), ("pg_mlp_config", abi.MlpConfig),
+               ("pg_split_merge_config", abi.SplitMergeConfig)]
     dtypes = [("pg_region_state", abi.STATE_DTYPE), ("pg_vmm_theta", abi.VMM_THETA_DTYPE),
               ("pg_vmf_theta", abi.VMF_THETA_DTYPE), ("pg_material", abi.MATERIAL_DTYPE),
-              ("pg_sphere", abi.SPHERE_DTYPE), ("pg_ray", abi.RAY_DTYPE), ("pg_hit", abi.HIT_DTYPE)]
+              ("pg_sphere", abi.SPHERE_DTYPE), ("pg_ray", abi.RAY_DTYPE), ("pg_hit", abi.HIT_DTYPE),
+              ("pg_region_extra", abi.EXTRA_DTYPE)]
     pairs = [(n, [f[0] for f in t._fields_]) for n, t in structs] + [(n, list(dt.names)) for n, dt in dtypes]
     got = _c_layout(pairs)
     for n, t in structs:

@@ -31,7 +31,8 @@ def cfg_from(abi, c):
 def mu_angle(a, b):
     ma = np.stack([a["mu_x"], a["mu_y"], a["mu_z"]], -1).astype(np.float64)
     mb = np.stack([b["mu_x"], b["mu_y"], b["mu_z"]], -1).astype(np.float64)
-    c = (ma * mb).sum(-1) / np.linalg.norm(ma, axis=-1) / np.linalg.norm(mb, axis=-1)
+    with np.errstate(invalid="ignore", divide="ignore"):  # unused components may hold zero vectors
+        c = (ma * mb).sum(-1) / np.linalg.norm(ma, axis=-1) / np.linalg.norm(mb, axis=-1)
     return np.arccos(np.clip(c, -1.0, 1.0))
 
 

@@ -1,0 +1,170 @@
+"""GPU parity of the post-fit split and merge (pg_split_merge) through the C
+ABI, against the reference's PathGuiding::postFit (src/PathGuiding.cpp:413-451)
+as the fixtures tests/golden/splitmerge_*.npz hold it.
+
+Every pass starts from the reference's fitted states and statistics, so each
+pass is compared on its own: the component count K, samplesSinceLastMerge and
+the chi-square sample counts must match exactly; the merges and splits are
+FP32 formulas of the same operands (SM_TOL), while refitted components carry
+the masked EM's differences - FP32 sums in another order, lightpmm's fastexp
+against expf - bounded like the fit itself (REF_TOL).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from test_guide_gpu import dev, records_in_regions
+from test_oracle import REF_TOL, assert_params_close, cfg_from
+from test_splitmerge import SETS, sm_from
+
+pytestmark = pytest.mark.gpu
+
+# statistics: chi-square divergence and covariance are sums over the region's
+# samples in FP32 (relative), with an absolute floor for near-empty components
+SM_TOL = {"div_rtol": 2e-3, "cov_rtol": 5e-3, "cov_atol": 1e-6, "w_rtol": 1e-3}
+
+
+def tensors(torch, g, p):
+    d = torch.from_numpy(np.ascontiguousarray(g[f"dirw{p}"], dtype=np.float32)).cuda()
+    pdf = torch.from_numpy(np.ascontiguousarray(g[f"pdf{p}"], dtype=np.float32)).cuda()
+    o = torch.from_numpy(g[f"offsets{p}"].astype(np.uint32).view(np.int32)).cuda()
+    return d, pdf, o
+
+
+def split_merge_pass(torch, pkg, g, p):
+    abi = pkg.abi
+    R = len(g[f"offsets{p}"]) - 1
+    ctx = pkg.FitContext(cfg_from(abi, g["cfg"]), max_regions=R)
+    ctx.set_split_merge(sm_from(abi, g["sm"]))
+    ctx.set_states(g[f"fitted{p}"])
+    ctx.set_extras(g[f"extras_in{p}"])
+    d, pdf, o = tensors(torch, g, p)
+    ctx.split_merge(d, pdf, o, R)
+    ctx.sync()
+    out = ctx.states(R), ctx.extras(R)
+    ctx.close()
+    return out
+
+
+def assert_extras_close(got, want, K, busy):
+    for r in np.nonzero(busy)[0]:
+        k = int(K[r])
+        np.testing.assert_array_equal(got["chi2_n"][r, :k], want["chi2_n"][r, :k])
+        np.testing.assert_allclose(got["chi2_div"][r, :k], want["chi2_div"][r, :k], rtol=SM_TOL["div_rtol"])
+        np.testing.assert_allclose(got["cov_w"][r, :k], want["cov_w"][r, :k], rtol=SM_TOL["w_rtol"],
+                                   atol=SM_TOL["cov_atol"])
+        np.testing.assert_allclose(got["cov"][r, :k], want["cov"][r, :k], rtol=SM_TOL["cov_rtol"],
+                                   atol=SM_TOL["cov_atol"])
+
+
+@pytest.mark.parametrize("name", SETS)
+def test_split_merge_matches_reference_per_pass(name, cuda, pkg, golden):
+    g = golden(name)
+    for p in range(int(g["passes"])):
+        st, ex = split_merge_pass(cuda, pkg, g, p)
+        want, want_ex = g[f"states{p}"], g[f"extras{p}"]
+        np.testing.assert_array_equal(st["k"], want["k"], err_msg=f"pass {p}")
+        np.testing.assert_array_equal(ex["samples_since_merge"], want_ex["samples_since_merge"])
+        busy = np.diff(g[f"offsets{p}"].astype(np.int64)) > 0
+        for r in np.nonzero(busy)[0]:
+            assert_params_close(st[r:r + 1], want[r:r + 1], int(want["k"][r]), REF_TOL, np.array([True]))
+        assert_extras_close(ex, want_ex, want["k"], busy)
+        # regions without samples are untouched
+        assert st[~busy].tobytes() == g[f"fitted{p}"][~busy].tobytes()
+
+
+@pytest.mark.parametrize("name", SETS)
+def test_fit_then_split_merge_sequence(name, cuda, pkg, golden):
+    """The reference's update sequence (fit, then postFit) run entirely on the
+    GPU from the initial mixtures: the GPU's own fit feeds its split/merge."""
+    torch = cuda
+    abi = pkg.abi
+    g = golden(name)
+    cfg = cfg_from(abi, g["cfg"])
+    R = len(g["offsets0"]) - 1
+    ctx = pkg.FitContext(cfg, max_regions=R)
+    ctx.set_split_merge(sm_from(abi, g["sm"]))
+    ctx.init_regions(R)
+    for p in range(int(g["passes"])):
+        d, pdf, o = tensors(torch, g, p)
+        ctx.fit(d, o, R, abi.PG_FIT_CONTINUE if p == 0 else abi.PG_FIT_UPDATE)
+        ctx.split_merge(d, pdf, o, R)
+        ctx.sync()
+        st = ctx.states(R)
+        want = g[f"states{p}"]
+        np.testing.assert_array_equal(st["k"], want["k"], err_msg=f"pass {p}")
+        busy = np.diff(g[f"offsets{p}"].astype(np.int64)) > 0
+        for r in np.nonzero(busy)[0]:
+            assert_params_close(st[r:r + 1], want[r:r + 1], int(want["k"][r]),
+                                {k: 4 * v for k, v in REF_TOL.items()}, np.array([True]))
+    ctx.close()
+
+
+def test_split_merge_is_deterministic(cuda, pkg, golden):
+    g = golden("splitmerge_eager")
+    a = split_merge_pass(cuda, pkg, g, 3)
+    b = split_merge_pass(cuda, pkg, g, 3)
+    assert a[0].tobytes() == b[0].tobytes() and a[1].tobytes() == b[1].tobytes()
+
+
+def test_split_merge_disabled_update_is_unchanged(cuda, pkg, abi, oracle, workloads):
+    """pg_update with split/merge configured but disabled equals the plain pass."""
+    torch = cuda
+    scene = np.array([-1.0, -1.0, -1.0, 1.0, 1.0, 1.0], dtype=np.float32)
+    cfg = abi.default_fit_config(num_initial_components=8)
+    outs = []
+    for sm in (None, abi.default_split_merge_config(enabled=0)):
+        ctx = pkg.FitContext(cfg, max_regions=64)
+        if sm is not None:
+            ctx.set_split_merge(sm)
+        ctx.set_regions(4, scene)
+        R = ctx.region_count()
+        for p in range(2):
+            rec, _ = records_in_regions(workloads, oracle, 4, scene, seed=300 + p, median=1500)
+            ctx.update(dev(torch, rec), rec.shape[0])
+        ctx.sync()
+        outs.append(ctx.states(R))
+        ctx.close()
+    assert outs[0].tobytes() == outs[1].tobytes()
+
+
+def test_update_with_split_merge_matches_reference(cuda, pkg, golden):
+    """PathGuiding::update with splitAndMerge on, records in: bucketing,
+    parallax pre-pass, fit, merge, statistics, split with masked refits and
+    distances against the reference's passes; the VMM_Theta the tracer reads
+    is packed from the changed mixtures."""
+    torch = cuda
+    abi = pkg.abi
+    g = golden("splitmerge_update")
+    ctx = pkg.FitContext(cfg_from(abi, g["cfg"]), max_regions=64)
+    ctx.set_split_merge(sm_from(abi, g["sm"]))
+    ctx.set_regions(int(g["split_count"]), g["scene"])
+    R = ctx.region_count()
+    tol = {k: 4 * v for k, v in REF_TOL.items()}  # the GPU's own fit feeds the split/merge
+    moved = 0
+    for p in range(int(g["passes"])):
+        rec = g[f"records{p}"]
+        vmm = torch.zeros(R * 720, dtype=torch.uint8, device="cuda")
+        ctx.update(dev(torch, rec), rec.shape[0], vmm)
+        ctx.sync()
+        st, ex = ctx.states(R), ctx.extras(R)
+        want, want_ex = g[f"states{p}"], g[f"extras{p}"]
+        np.testing.assert_array_equal(st["k"], want["k"], err_msg=f"pass {p}")
+        np.testing.assert_array_equal(ex["samples_since_merge"], want_ex["samples_since_merge"])
+        moved += int(np.sum(want["k"] != 8))
+        busy = want["total_num_samples"] > 0
+        for r in np.nonzero(busy)[0]:
+            k = int(want["k"][r])
+            assert_params_close(st[r:r + 1], want[r:r + 1], k, tol, np.array([True]))
+            fin = np.isfinite(want["distance"][r, :k])
+            np.testing.assert_array_equal(np.isfinite(st["distance"][r, :k]), fin)
+            np.testing.assert_allclose(st["distance"][r, :k][fin], want["distance"][r, :k][fin], rtol=1e-2)
+        v = np.frombuffer(vmm.cpu().numpy().tobytes(), dtype=abi.VMM_THETA_DTYPE)
+        np.testing.assert_array_equal(v["used_distributions"], st["k"].astype(np.int32))
+        for r in range(R):
+            k = int(st["k"][r])
+            np.testing.assert_array_equal(v["pi"][r, :k], st["weight"][r, :k])
+            assert np.all(v["pi"][r, k:] == 0.0)
+    assert moved > 0
+    ctx.close()
