@@ -483,6 +483,64 @@ def bench_config1(pkg, abi, torch, stream, steps: int, cpu: bool):
     return out
 
 
+def bench_split_merge(pkg, abi, torch, stream, w, steps: int, warmup: int, cluster_threshold: int = 0,
+                      cluster_size: int = 0):
+    """PathGuiding::postFit with splitAndMerge (pg_split_merge) on the fit
+    workload's regions, after a first fit with the reference's default fit
+    configuration (K=8, up to 100 iterations): a first pass, so every region
+    may split and its split components are refitted by the masked EM.  Each
+    step restores the fitted states and statistics (untimed) and times the
+    split/merge launch with CUDA events on its stream."""
+    R = len(w["offsets"]) - 1
+    counts = np.diff(w["offsets"].astype(np.int64))
+    n = int(counts.sum())
+    ctx = pkg.FitContext(abi.default_fit_config(num_initial_components=8), max_regions=R)
+    ctx.set_split_merge(abi.default_split_merge_config(cluster_threshold=cluster_threshold,
+                                                       cluster_size=cluster_size))
+    d = torch.from_numpy(np.ascontiguousarray(w["dirw"], dtype=np.float32)).cuda()
+    o = torch.from_numpy(w["offsets"].view(np.int32)).cuda()
+    rng = np.random.default_rng(7)
+    pdf = torch.from_numpy((rng.uniform(0.5, 2.0, n) / (4.0 * np.pi)).astype(np.float32)).cuda()
+    ctx.fit(d, o, R, abi.PG_FIT_INIT, stream=stream)
+    ctx.sync(stream)
+    st0, ex0 = ctx.states(R), ctx.extras(R)
+    times = []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for i in range(warmup + steps):
+        ctx.set_states(st0, stream=stream)
+        ctx.set_extras(ex0)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        ctx.split_merge(d, pdf, o, R, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if i >= warmup:
+            times.append(e0.elapsed_time(e1))
+    ctx.sync(stream)
+    st, ex = ctx.states(R), ctx.extras(R)
+    ms = float(np.mean(times))
+    passes = ex["stat_passes"].astype(np.int64) + ex["em_iterations"].astype(np.int64)
+    sample_passes = int((counts * passes).sum())
+    # per sample: a statistics pass reads dirw + pdf (chi-square) and dirw (covariance), an EM iteration dirw
+    alg = float((counts * (36 * ex["stat_passes"].astype(np.int64) + 16 * ex["em_iterations"])).sum()) + \
+        R * 2.0 * (abi.STATE_DTYPE.itemsize + abi.EXTRA_DTYPE.itemsize)
+    hbm, src = measured_peaks()
+    K = st["k"].astype(np.int64)
+    out = {"metric": "split/merge sample passes per second", "unit": "Msample-pass/s",
+           "value": sample_passes / (ms * 1e-3) / 1e6, "ms_per_step": ms, "steps": steps,
+           "config": {"workload": "first-pass split/merge of the fit workload's 4096 regions (13.8 M samples, "
+                                  "pdf uniform 0.5-2 / 4 pi) after a default-configuration fit (K=8)",
+                      "split_merge": "reference defaults (merge 8192, split 4096, refit 4096, 0.5, 0.025)"},
+           "regions_split": int((K > 8).sum()), "k_mean_after": float(K.mean()),
+           "stat_passes": int(ex["stat_passes"].sum()), "em_iterations": int(ex["em_iterations"].sum()),
+           "gpu_launches": steps,
+           "roofline": {"bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+                        "frac": alg / (ms * 1e-3) / 1e9 / hbm, "traffic": None, "peak_source": src,
+                        "algorithmic_bytes_per_launch": alg}}
+    ctx.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -501,8 +559,12 @@ def main():
     ap.add_argument("--median", type=float, default=0.0, help="override the median region size")
     ap.add_argument("--sigma", type=float, default=-1.0, help="override the region-size sigma")
     ap.add_argument("--sweep", action="store_true", help="time the tuning grid and print one line per point")
-    ap.add_argument("--workload", default="all", choices=["all", "em", "tracer", "guided", "surrogate"],
+    ap.add_argument("--workload", default="all",
+                    choices=["all", "em", "tracer", "guided", "surrogate", "splitmerge"],
                     help="all: the EM line with the tracer, guided and surrogate blocks; or one of them alone")
+    ap.add_argument("--sm-cluster-threshold", type=int, default=0,
+                    help="split/merge: regions above this many samples use a cluster (0: library default)")
+    ap.add_argument("--sm-cluster-size", type=int, default=0, help="split/merge: CTAs per cluster (0: default)")
     ap.add_argument("--ref-seconds", type=float, default=None,
                     help="CPU seconds per reference step (default: ~100 s over the whole run)")
     args = ap.parse_args()
@@ -541,6 +603,17 @@ def main():
             print(json.dumps(line), flush=True)
         return
     w = make_workload(args.small, args)
+    if args.workload == "splitmerge":
+        stream = torch.cuda.Stream()
+        sampler = ClockSampler(local)
+        with sampler:
+            line = bench_split_merge(pkg, abi, torch, stream, w, args.steps, args.warmup,
+                                     args.sm_cluster_threshold, args.sm_cluster_size)
+        line.update(n_gpus=world, scaling="weak", vs_baseline=None, data="synthetic (seeded vMF mixtures)",
+                    clocks=sampler.summary())
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        return
     R = len(w["offsets"]) - 1
     counts = np.diff(w["offsets"].astype(np.int64))
     n_samples = int(counts.sum())
@@ -693,6 +766,11 @@ def main():
             sg = bench_surrogate(pkg, abi, torch, stream)
         sg["clocks"] = ssampler.summary()
         line["surrogate"] = sg
+        msampler = ClockSampler(local)
+        with msampler:
+            sm = bench_split_merge(pkg, abi, torch, stream, w, min(args.steps, 5), 2)
+        sm["clocks"] = msampler.summary()
+        line["split_merge"] = sm
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

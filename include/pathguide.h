@@ -234,7 +234,12 @@ typedef struct pg_region_extra {
     float cov[16][3];          /* variance x, variance y, covariance (component frame) */
     float cov_w[16];           /* sumWeights                        */
     float samples_since_merge; /* samplesSinceLastMerge             */
-    uint32_t reserved[3];
+    /* work of the last pg_split_merge on the region (not in the reference):
+     * passes of the divergence + covariance statistics over its samples and
+     * masked EM iterations */
+    uint32_t stat_passes;
+    uint32_t em_iterations;
+    uint32_t reserved;
 } pg_region_extra;
 
 /* The reference's knobs (src/PathGuiding.h:124-129). */
@@ -245,6 +250,12 @@ typedef struct pg_split_merge_config {
     uint32_t min_samples_for_post_split_fitting; /* 4096                          */
     float split_min_divergence;                  /* 0.5                           */
     float merge_max_divergence;                  /* 0.025                         */
+    /* GPU work split (not in the reference): regions above cluster_threshold
+     * samples are processed by a cluster of cluster_size CTAs, the others by
+     * one CTA each, both at once.  0 selects the defaults (8192 samples, 8 CTAs);
+     * cluster_threshold 0xFFFFFFFF keeps every region on one CTA. */
+    uint32_t cluster_threshold;
+    uint32_t cluster_size;
 } pg_split_merge_config;
 
 /* The reference's defaults, enabled. */

@@ -290,7 +290,11 @@ class FitContext:
         return out
 
     def set_extras(self, extras: np.ndarray):
-        e = np.ascontiguousarray(extras, dtype=abi.EXTRA_DTYPE)
+        e = np.ascontiguousarray(extras)
+        if e.dtype != abi.EXTRA_DTYPE:
+            if e.dtype.itemsize != abi.EXTRA_DTYPE.itemsize:
+                raise ValueError("extras must be pg_region_extra records (400 bytes each)")
+            e = e.view(abi.EXTRA_DTYPE)
         self._check(self.lib.pg_set_region_extra(self.h, e.ctypes.data, e.shape[0]))
 
 

@@ -101,19 +101,21 @@ class PlatesParams(C.Structure):
 
 
 EXTRA_DTYPE = np.dtype([("chi2_div", "<f4", (16,)), ("chi2_n", "<f4", (16,)), ("cov", "<f4", (16, 3)),
-                        ("cov_w", "<f4", (16,)), ("samples_since_merge", "<f4"), ("reserved", "<u4", (3,))])
+                        ("cov_w", "<f4", (16,)), ("samples_since_merge", "<f4"), ("stat_passes", "<u4"),
+                        ("em_iterations", "<u4"), ("reserved", "<u4")])
 assert EXTRA_DTYPE.itemsize == 400
 
 
 class SplitMergeConfig(C.Structure):
     _fields_ = [("enabled", C.c_uint32), ("min_samples_for_merging", C.c_uint32),
                 ("min_samples_for_splitting", C.c_uint32), ("min_samples_for_post_split_fitting", C.c_uint32),
-                ("split_min_divergence", C.c_float), ("merge_max_divergence", C.c_float)]
+                ("split_min_divergence", C.c_float), ("merge_max_divergence", C.c_float),
+                ("cluster_threshold", C.c_uint32), ("cluster_size", C.c_uint32)]
 
 
 def default_split_merge_config(**kw) -> SplitMergeConfig:
     """The reference's knobs (src/PathGuiding.h:124-129), enabled."""
-    c = SplitMergeConfig(1, 8192, 4096, 4096, 0.5, 0.025)
+    c = SplitMergeConfig(1, 8192, 4096, 4096, 0.5, 0.025, 0, 0)
     for k, v in kw.items():
         setattr(c, k, v)
     return c

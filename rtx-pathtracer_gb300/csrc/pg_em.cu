@@ -52,6 +52,14 @@ __global__ void __launch_bounds__(NT) em_eval_kernel(EmArgs a) {
     }
 }
 
+// Region ids into ctx->d_order, largest sample count first; the number of
+// regions in size buckets at or above `large_threshold` into *n_large_out.
+int order_regions(pg_ctx *ctx, const uint32_t *offsets, uint32_t n_regions, uint32_t large_threshold,
+                  uint32_t *n_large_out, cudaStream_t s) {
+    order_regions_kernel<128><<<1, 1024, 0, s>>>(offsets, n_regions, ctx->d_order, large_threshold, n_large_out);
+    return check_cuda(ctx, cudaGetLastError(), "order_regions launch");
+}
+
 }  // namespace pg
 
 using namespace pg;

@@ -36,6 +36,8 @@ struct pg_ctx {
     uint32_t last_launches = 0;
     void *guide = nullptr;           // sort / parallax / distance scratch (pg_guide.cu)
     pg_region_extra *d_extras = nullptr;  // split/merge statistics per region (pg_splitmerge.cu)
+    cudaStream_t sm_aux = nullptr;        // split/merge: the clustered launch runs beside the per-CTA one
+    cudaEvent_t sm_fork = nullptr, sm_join = nullptr;
     pg_split_merge_config sm{};      // disabled unless pg_set_split_merge
     std::string last_error;
 };
@@ -45,6 +47,10 @@ namespace pg {
 int set_error(pg_ctx *ctx, int status, const std::string &msg);
 int check_cuda(pg_ctx *ctx, cudaError_t e, const char *what);
 int upload_init_table(pg_ctx *ctx, cudaStream_t s);
+// region ids into ctx->d_order, largest sample count first; *n_large_out
+// (device) = regions in size buckets at or above large_threshold
+int order_regions(pg_ctx *ctx, const uint32_t *offsets, uint32_t n_regions, uint32_t large_threshold,
+                  uint32_t *n_large_out, cudaStream_t s);
 void guide_release(pg_ctx *ctx);
 // split/merge statistics: allocated (zeroed) on first use, zeroed again when
 // regions are initialised

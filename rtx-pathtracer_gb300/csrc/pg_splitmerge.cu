@@ -25,7 +25,11 @@
 
 #include <algorithm>
 
+#include <cooperative_groups.h>
+
 #include "pg_internal.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace pg {
 namespace sm {
@@ -50,14 +54,35 @@ struct Stats {
     float since;
 };
 
+// Pair candidates of one merge round (in shared memory on the device).
+struct MergeScratch {
+    float key[KM * (KM - 1) / 2];
+    int ca[KM * (KM - 1) / 2], cb[KM * (KM - 1) / 2];
+};
+
+// The mixture as the sample passes read it (float4 / float2 broadcasts):
+// log2 of weight x pdf of component c at direction d is
+// min(e.xyz . d + e.w, l.x) with e = {kappa log2(e) mu, l.x - kappa log2(e)}
+// and l.x = log2(weight norm) - the vMF pdf with the cosine clamped at 1.
+struct PassMix {
+    float4 e[KM];
+    float2 l[KM];           // log2(weight norm), weight
+    float4 sf[KM], tf[KM];  // covariance frames
+};
+
 struct Shared {
     Mix m;
     Stats s;
+    PassMix pm;
+    MergeScratch ms;
     float red[NW][4 * KM + 2];
-    float acc[4 * KM + 2];
+    float part[4 * KM + 2];  // this CTA's sums of a pass (read by the cluster)
+    float acc[4 * KM + 2];   // the region's sums of a pass
     uint32_t mask;           // components refitted by the masked EM
     int fit_iters;
     int stop;
+    float old_active;        // masked EM: prior-free weight of the refitted components
+    uint32_t stat_passes, em_iters;  // work done, reported in the region's statistics
     float ll_last, ll_abs_inv;
     float sum_w;             // weight of the valid samples (masked EM, first iteration)
 };
@@ -68,6 +93,8 @@ struct Args {
     const float4 *dirw;
     const float *pdf;
     const uint32_t *offsets;
+    const uint32_t *order;   // region ids, largest first (the biggest regions start first)
+    const uint32_t *n_large; // leading regions of `order` split by clusters
     uint32_t n_regions;
     pg_fit_config cfg;
     pg_split_merge_config sm;
@@ -354,9 +381,9 @@ SM_HD int hoare_partition(float *key, int *pa, int *pb, int n, Pred pred) {
 }
 
 // mergeAll (src/PathGuiding.cpp:635-707), thread 0
-SM_HD void merge_all(Mix &m, Stats &s, const pg_split_merge_config &cfg) {
-    float key[KM * (KM - 1) / 2];
-    int ca[KM * (KM - 1) / 2], cb[KM * (KM - 1) / 2];
+SM_HD void merge_all(Mix &m, Stats &s, const pg_split_merge_config &cfg, MergeScratch &ms) {
+    float *key = ms.key;
+    int *ca = ms.ca, *cb = ms.cb;
     for (int round = 0; round < KM; ++round) {
         const int n = (int)m.K;
         if (n <= 1) return;
@@ -468,138 +495,214 @@ SM_HD void split_component(Mix &m, Stats &s, int c, float max_kappa) {
     s.cw[c] = s.cw[dst] = 0.0f;
 }
 
-// vMF pdf of component c (VMFKernel::pdf: cos clamped at 1)
-__device__ __forceinline__ float comp_pdf(const Mix &m, int c, float dx, float dy, float dz) {
-    const float cs = m.mx[c] * dx + m.my[c] * dy + m.mz[c] * dz;
-    return m.nrm[c] * expf(m.k[c] * fminf(cs - 1.0f, 0.0f));
+__device__ __forceinline__ float ex2_approx(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float lg2_approx(float x) {
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
 }
 
-// Block reduction of per-thread values v[0..n) into S.acc[0..n), fixed order.
-__device__ void block_sum(Shared &S, float *v, int n) {
+// weight x vMF pdf (VMFKernel::pdf, cosine clamped at 1) of a component
+__device__ __forceinline__ float weighted_pdf(float4 e, float lw, float4 d) {
+    const float t = __fmaf_rn(e.x, d.x, __fmaf_rn(e.y, d.y, __fmaf_rn(e.z, d.z, e.w)));
+    return ex2_approx(fminf(t, lw));
+}
+__device__ __forceinline__ float dot3(float4 a, float4 d) {
+    return __fmaf_rn(a.z, d.z, __fmaf_rn(a.y, d.y, __fmul_rn(a.x, d.x)));
+}
+
+// incrementalcovariance2d.h:67-77: the tangent frame {s, t} of a component's mean
+__device__ void cov_frame(float nx, float ny, float nz, float4 &sf, float4 &tf) {
+    const bool xg = nx * nx > ny * ny;
+    const float inv = 1.0f / sqrtf((xg ? nx * nx : ny * ny) + nz * nz);
+    float t[3];
+    if (xg) {
+        t[0] = nz * inv, t[1] = 0.0f, t[2] = -nx * inv;
+    } else {
+        t[0] = 0.0f, t[1] = nz * inv, t[2] = -ny * inv;
+    }
+    tf = make_float4(t[0], t[1], t[2], 0.0f);
+    sf = make_float4(t[1] * nz - t[2] * ny, t[2] * nx - t[0] * nz, t[0] * ny - t[1] * nx, 0.0f);
+}
+
+// Copies the mixture into the pass layout (and the covariance frames when
+// asked); every thread calls it after the mixture's last change.
+__device__ void load_pass_mix(Shared &S, bool frames) {
+    __syncthreads();
+    const int c = threadIdx.x;
+    if (c < KM) {
+        const Mix &m = S.m;
+        const float kl = m.k[c] * 1.4426950408889634f;
+        const float lw = log2f(m.w[c] * m.nrm[c]);  // -inf for an empty lane: its pdf term is 0
+        S.pm.e[c] = make_float4(kl * m.mx[c], kl * m.my[c], kl * m.mz[c], lw - kl);
+        S.pm.l[c] = make_float2(lw, m.w[c]);
+        if (frames) cov_frame(m.mx[c], m.my[c], m.mz[c], S.pm.sf[c], S.pm.tf[c]);
+    }
+    __syncthreads();
+}
+
+// The CTAs that share a region: a thread-block cluster (size > 1) or one CTA.
+// Every CTA of a cluster holds the same mixture and statistics and runs the
+// same control code on the same sums, so all reach the same decisions; only
+// rank 0 writes the region back.
+struct Team {
+    uint32_t rank, size;
+};
+
+// Reduction of per-thread values v[0..N) in a fixed order (lanes, warps, then
+// cluster ranks 0..size-1): value i goes to S.acc[i] below `tail`, to
+// S.acc[4 KM + i - tail] from it on, in every CTA of the team.
+template <int N, bool kCluster>
+__device__ void block_sum(Shared &S, const float (&v)[N], int tail) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int i = 0; i < n; ++i) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
         float x = v[i];
+#pragma unroll
         for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
         if (lane == 0) S.red[warp][i] = x;
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int i = threadIdx.x;
+    if (!kCluster) {
+        if (i < N) {
+            float x = 0.0f;
+            for (int w = 0; w < NW; ++w) x += S.red[w][i];
+            S.acc[i < tail ? i : 4 * KM + i - tail] = x;
+        }
+        __syncthreads();
+        return;
+    }
+    if (i < N) {
         float x = 0.0f;
         for (int w = 0; w < NW; ++w) x += S.red[w][i];
-        S.acc[i] = x;
+        S.part[i] = x;
     }
-    __syncthreads();
+    cg::cluster_group cl = cg::this_cluster();
+    cl.sync();  // every rank's partial sums are visible
+    if (i < N) {
+        const uint32_t nr = cl.num_blocks();
+        float x = 0.0f;
+        for (uint32_t r = 0; r < nr; ++r) x += cl.map_shared_rank(S.part, r)[i];
+        S.acc[i < tail ? i : 4 * KM + i - tail] = x;
+    }
+    cl.sync();  // no rank overwrites its partials while another still reads them
 }
 
 // Pass kinds over the region's samples
 enum { PASS_CHI2 = 0, PASS_COV = 1, PASS_EM = 2 };
 
-// One pass: per component sums into S.acc (chi2: [c]; cov: [4c..4c+3] =
-// weight, xx, yy, xy; em: [4c..4c+3] = sum gamma w d.xyz, [64 + c]... see below).
-template <int KIND>
-__device__ void sample_pass(Shared &S, const Args &A, uint32_t b, uint32_t e, float s_frame[KM][3],
-                            float t_frame[KM][3]) {
-    const Mix &m = S.m;
-    const int L = (int)active_lanes(m.K);
-    float v[4 * KM + 2];
-    for (int i = 0; i < 4 * KM + 2; ++i) v[i] = 0.0f;
-    for (uint32_t i = b + threadIdx.x; i < e; i += blockDim.x) {
-        const float4 d = A.dirw[i];
-        float p[KM];
+// One pass over the region's samples with L active component lanes (a
+// compile-time count, so the per-thread sums stay in registers).  Sums land
+// in S.acc: chi-square [c] = sum weight_c pdf_c w^2 pdf / mix^2 (divided by
+// weight_c afterwards); covariance [4c..4c+3] = sum of gamma_c w, and its xx,
+// yy, xy moments in the component's frame; EM [4c..4c+3] = sum of gamma_c w
+// d.xyz and gamma_c w, [4 KM] = sum w, [4 KM + 1] = sum w log2(mix).
+template <int KIND, int L, bool kCluster>
+__device__ void sample_pass_l(Shared &S, const Args &A, Team T, uint32_t b, uint32_t e) {
+    constexpr int NV = KIND == PASS_CHI2 ? L : 4 * L + (KIND == PASS_EM ? 2 : 0);
+    float v[NV];
+#pragma unroll
+    for (int i = 0; i < NV; ++i) v[i] = 0.0f;
+    for (uint32_t i = b + T.rank * NT + threadIdx.x; i < e; i += T.size * NT) {
+        const float4 d = __ldg(A.dirw + i);
+        float p[L];  // weight_c pdf_c
         float mix = 0.0f;
+#pragma unroll
         for (int c = 0; c < L; ++c) {
-            p[c] = comp_pdf(m, c, d.x, d.y, d.z);
-            mix += m.w[c] * p[c];
+            p[c] = weighted_pdf(S.pm.e[c], S.pm.l[c].x, d);
+            mix += p[c];
         }
         if (!(mix > kPmmEps)) continue;
         if (KIND == PASS_CHI2) {
-            const float f = d.w * d.w * A.pdf[i] / (mix * mix);
-            for (int c = 0; c < L; ++c) v[c] += p[c] * f;
+            const float f = d.w * d.w * __ldg(A.pdf + i) / (mix * mix);
+#pragma unroll
+            for (int c = 0; c < L; ++c) v[c] = __fmaf_rn(p[c], f, v[c]);
         } else if (KIND == PASS_COV) {
-            const float inv = 1.0f / mix;
+            const float inv = d.w / mix;
+#pragma unroll
             for (int c = 0; c < L; ++c) {
-                const float wt = d.w * (m.w[c] * p[c] * inv);
-                const float lx = s_frame[c][0] * d.x + s_frame[c][1] * d.y + s_frame[c][2] * d.z;
-                const float ly = t_frame[c][0] * d.x + t_frame[c][1] * d.y + t_frame[c][2] * d.z;
+                const float wt = p[c] * inv;
+                const float lx = dot3(S.pm.sf[c], d), ly = dot3(S.pm.tf[c], d);
                 v[4 * c] += wt;
-                v[4 * c + 1] += lx * lx * wt;
-                v[4 * c + 2] += ly * ly * wt;
-                v[4 * c + 3] += lx * ly * wt;
+                v[4 * c + 1] = __fmaf_rn(lx * lx, wt, v[4 * c + 1]);
+                v[4 * c + 2] = __fmaf_rn(ly * ly, wt, v[4 * c + 2]);
+                v[4 * c + 3] = __fmaf_rn(lx * ly, wt, v[4 * c + 3]);
             }
         } else {
-            const float inv = 1.0f / mix;
+            const float inv = d.w / mix;
+#pragma unroll
             for (int c = 0; c < L; ++c) {
-                const float g = m.w[c] * p[c] * inv * d.w;
-                v[4 * c] += g * d.x;
-                v[4 * c + 1] += g * d.y;
-                v[4 * c + 2] += g * d.z;
+                const float g = p[c] * inv;
+                v[4 * c] = __fmaf_rn(g, d.x, v[4 * c]);
+                v[4 * c + 1] = __fmaf_rn(g, d.y, v[4 * c + 1]);
+                v[4 * c + 2] = __fmaf_rn(g, d.z, v[4 * c + 2]);
                 v[4 * c + 3] += g;
             }
-            v[4 * KM] += d.w;
-            v[4 * KM + 1] += d.w * logf(mix);
+            if (KIND == PASS_EM) {
+                v[NV - 2] += d.w;
+                v[NV - 1] = __fmaf_rn(d.w, lg2_approx(mix), v[NV - 1]);
+            }
         }
     }
-    block_sum(S, v, KIND == PASS_CHI2 ? KM : 4 * KM + 2);
+    block_sum<NV, kCluster>(S, v, KIND == PASS_CHI2 ? NV : 4 * L);
 }
 
-// incrementalcovariance2d.h:67-77: the tangent frame of each component's mean
-__device__ void cov_frames(const Mix &m, float s_frame[KM][3], float t_frame[KM][3]) {
-    for (int c = 0; c < KM; ++c) {
-        const float nx = m.mx[c], ny = m.my[c], nz = m.mz[c];
-        const bool xg = nx * nx > ny * ny;
-        const float inv = 1.0f / sqrtf((xg ? nx * nx : ny * ny) + nz * nz);
-        float t[3];
-        if (xg) {
-            t[0] = nz * inv, t[1] = 0.0f, t[2] = -nx * inv;
-        } else {
-            t[0] = 0.0f, t[1] = nz * inv, t[2] = -ny * inv;
-        }
-        t_frame[c][0] = t[0], t_frame[c][1] = t[1], t_frame[c][2] = t[2];
-        s_frame[c][0] = t[1] * nz - t[2] * ny;
-        s_frame[c][1] = t[2] * nx - t[0] * nz;
-        s_frame[c][2] = t[0] * ny - t[1] * nx;
+template <int KIND, bool kCluster>
+__device__ void sample_pass(Shared &S, const Args &A, Team T, uint32_t b, uint32_t e) {
+    switch (active_lanes(S.m.K)) {
+        case 4: sample_pass_l<KIND, 4, kCluster>(S, A, T, b, e); break;
+        case 8: sample_pass_l<KIND, 8, kCluster>(S, A, T, b, e); break;
+        case 12: sample_pass_l<KIND, 12, kCluster>(S, A, T, b, e); break;
+        default: sample_pass_l<KIND, 16, kCluster>(S, A, T, b, e); break;
     }
 }
 
 // updateDivergence(Masked) and updateStatistics(Masked) over the region's samples
-__device__ void update_stats(Shared &S, const Args &A, uint32_t b, uint32_t e, uint32_t mask) {
-    __shared__ float sf[KM][3], tf[KM][3];
+template <bool kCluster>
+__device__ void update_stats(Shared &S, const Args &A, Team T, uint32_t b, uint32_t e, uint32_t mask) {
     const int L = (int)active_lanes(S.m.K);
     const float n = (float)(e - b);
-    sample_pass<PASS_CHI2>(S, A, b, e, sf, tf);
-    if (threadIdx.x == 0)
-        for (int c = 0; c < L; ++c) {
-            if (!((mask >> c) & 1u)) continue;
-            const float nn = S.s.dn[c] + n;
-            S.s.div[c] = (S.s.div[c] * S.s.dn[c] + S.acc[c]) / nn;
-            S.s.dn[c] = nn;
-        }
+    if (threadIdx.x == 0) ++S.stat_passes;
+    load_pass_mix(S, true);
+    sample_pass<PASS_CHI2, kCluster>(S, A, T, b, e);
+    const int c = threadIdx.x;  // one thread per component
+    if (c < L && ((mask >> c) & 1u)) {
+        const float w = S.pm.l[c].y;
+        const float sum = w > 0.0f ? S.acc[c] / w : 0.0f;
+        const float nn = S.s.dn[c] + n;
+        S.s.div[c] = (S.s.div[c] * S.s.dn[c] + sum) / nn;
+        S.s.dn[c] = nn;
+    }
     __syncthreads();
-    if (threadIdx.x == 0) cov_frames(S.m, sf, tf);
-    __syncthreads();
-    sample_pass<PASS_COV>(S, A, b, e, sf, tf);
-    if (threadIdx.x == 0)
-        for (int c = 0; c < L; ++c) {
-            if (!((mask >> c) & 1u)) continue;
-            const float nw = S.s.cw[c] + S.acc[4 * c];
-            for (int i = 0; i < 3; ++i)
-                S.s.cov[c][i] = nw > 0.0f ? (S.s.cov[c][i] * S.s.cw[c] + S.acc[4 * c + 1 + i]) / nw : 0.0f;
-            S.s.cw[c] = nw;
-        }
+    sample_pass<PASS_COV, kCluster>(S, A, T, b, e);
+    if (c < L && ((mask >> c) & 1u)) {
+        const float nw = S.s.cw[c] + S.acc[4 * c];
+        for (int i = 0; i < 3; ++i)
+            S.s.cov[c][i] = nw > 0.0f ? (S.s.cov[c][i] * S.s.cw[c] + S.acc[4 * c + 1 + i]) / nw : 0.0f;
+        S.s.cw[c] = nw;
+    }
     __syncthreads();
 }
 
 // VMMFactory::maskedFit with maskedParameterUpdate (VMMFactory.h:226-297, 458-485)
-__device__ void masked_fit(Shared &S, const Args &A, uint32_t b, uint32_t e) {
+template <bool kCluster>
+__device__ void masked_fit(Shared &S, const Args &A, Team T, uint32_t b, uint32_t e) {
     const pg_fit_config &cfg = A.cfg;
     Mix &m = S.m;
     const uint32_t K = m.K;
     const float inv_wpn = cfg.v_prior * (float)K + 1.0f, wpn = 1.0f / inv_wpn, wptn = cfg.v_prior * wpn;
-    float old_active = 0.0f;
+    const int L = (int)active_lanes(K);
     if (threadIdx.x == 0) {
         set_k(m, K);  // resetInactiveComponents
-        for (int c = 0; c < (int)active_lanes(K); ++c)
+        float old_active = 0.0f;
+        for (int c = 0; c < L; ++c)
             if ((S.mask >> c) & 1u) old_active += m.w[c] > wptn ? (m.w[c] - wptn) * inv_wpn : 0.0f;
+        S.old_active = old_active;
         S.fit_iters = (e - b) > 2u * K ? (int)cfg.max_itr : 0;
         S.ll_last = 0.0f;
         S.ll_abs_inv = 0.0f;
@@ -608,36 +711,40 @@ __device__ void masked_fit(Shared &S, const Args &A, uint32_t b, uint32_t e) {
     const int iters = S.fit_iters;
     const float max_r = k2r(cfg.max_kappa);
     for (int it = 0; it < iters; ++it) {
-        sample_pass<PASS_EM>(S, A, b, e, nullptr, nullptr);
-        if (threadIdx.x == 0) {
-            if (it == 0) S.sum_w = S.acc[4 * KM];
-            const float sum_w = S.sum_w;
+        load_pass_mix(S, false);
+        sample_pass<PASS_EM, kCluster>(S, A, T, b, e);
+        // M-step: one thread per refitted component
+        const float sum_w = it == 0 ? S.acc[4 * KM] : S.sum_w;
+        const int c = threadIdx.x;
+        if (c < L && ((S.mask >> c) & 1u)) {
             float active = 0.0f;
-            for (int c = 0; c < (int)active_lanes(K); ++c)
-                if ((S.mask >> c) & 1u) active += S.acc[4 * c + 3];
-            const float norm = old_active * (sum_w / active);
-            for (int c = 0; c < (int)active_lanes(K); ++c) {
-                if (!((S.mask >> c) & 1u)) continue;
-                float sx = S.acc[4 * c] * norm, sy = S.acc[4 * c + 1] * norm, sz = S.acc[4 * c + 2] * norm;
-                const float sw = S.acc[4 * c + 3] * norm;
-                const float mw = (sw / sum_w) * wpn + wptn;
-                const float rl = sqrtf(sx * sx + sy * sy + sz * sz);
-                if (rl > 0.0f) {
-                    m.mx[c] = sx / rl;
-                    m.my[c] = sy / rl;
-                    m.mz[c] = sz / rl;
-                }
-                const float avg = rl / sw;
-                const float nsc = (float)m.total * mw;
-                float ap = (avg * nsc + cfg.r_prior * cfg.r_prior_weight) / (nsc + cfg.r_prior_weight);
-                ap = fminf(ap, max_r);
-                m.w[c] = mw;
-                set_kappa_r(m, c, r2k(ap), ap);
+            for (int j = 0; j < L; ++j)
+                if ((S.mask >> j) & 1u) active += S.acc[4 * j + 3];
+            const float norm = S.old_active * (sum_w / active);
+            const float sx = S.acc[4 * c] * norm, sy = S.acc[4 * c + 1] * norm, sz = S.acc[4 * c + 2] * norm;
+            const float sw = S.acc[4 * c + 3] * norm;
+            const float mw = (sw / sum_w) * wpn + wptn;
+            const float rl = sqrtf(sx * sx + sy * sy + sz * sz);
+            if (rl > 0.0f) {
+                m.mx[c] = sx / rl;
+                m.my[c] = sy / rl;
+                m.mz[c] = sz / rl;
             }
+            const float avg = rl / sw;
+            const float nsc = (float)m.total * mw;
+            float ap = (avg * nsc + cfg.r_prior * cfg.r_prior_weight) / (nsc + cfg.r_prior_weight);
+            ap = fminf(ap, max_r);
+            m.w[c] = mw;
+            set_kappa_r(m, c, r2k(ap), ap);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            ++S.em_iters;
+            if (it == 0) S.sum_w = sum_w;
             set_k(m, K);
-            // relative log-likelihood stop (VMMFactory.h:284-295)
+            // relative log-likelihood stop (VMMFactory.h:284-295), natural log
             int stop = 0;
-            const float ll = S.acc[4 * KM + 1];
+            const float ll = S.acc[4 * KM + 1] * 0.6931471805599453f;
             if ((uint32_t)it >= cfg.min_itr) {
                 if ((uint32_t)it > cfg.min_itr) {
                     const float rel = (ll - S.ll_last) * S.ll_abs_inv;
@@ -655,10 +762,9 @@ __device__ void masked_fit(Shared &S, const Args &A, uint32_t b, uint32_t e) {
     }
 }
 
-__global__ void __launch_bounds__(NT) k_split_merge(Args A) {
-    __shared__ Shared S;
-    const uint32_t r = blockIdx.x;
-    if (r >= A.n_regions) return;
+// PathGuiding::postFit with splitAndMerge of region r by a team of CTAs.
+template <bool kCluster>
+__device__ void split_merge_region(Shared &S, const Args &A, Team T, uint32_t r) {
     const uint32_t b = A.offsets[r], e = A.offsets[r + 1];
     if (e == b) return;  // PathGuiding::update skips empty regions
     pg_region_state *st = A.states + r;
@@ -685,16 +791,18 @@ __global__ void __launch_bounds__(NT) k_split_merge(Args A) {
         m.sample_weight = st->sample_weight;
         m.num_samples = st->num_samples;
         m.total = st->total_num_samples;
+        S.stat_passes = 0;
+        S.em_iters = 0;
         S.s.since = ex->samples_since_merge + (float)(e - b);
         if (S.s.since > (float)A.sm.min_samples_for_merging) {
             remove_prior(m, A.cfg.v_prior);
-            merge_all(m, S.s, A.sm);
+            merge_all(m, S.s, A.sm, S.ms);
             apply_prior(m, A.cfg.v_prior);
             S.s.since = 0.0f;
         }
     }
     __syncthreads();
-    update_stats(S, A, b, e, 0xFFFFu);
+    update_stats<kCluster>(S, A, T, b, e, 0xFFFFu);
     const bool first = (unsigned long long)(e - b) == S.m.total;
     const bool fit = first || (e - b) > A.sm.min_samples_for_post_split_fitting;
     if (threadIdx.x == 0) remove_prior(S.m, A.cfg.v_prior);
@@ -744,14 +852,14 @@ __global__ void __launch_bounds__(NT) k_split_merge(Args A) {
             __syncthreads();
             if (n_split == 0) break;
             if (fit) {
-                masked_fit(S, A, b, e);
-                update_stats(S, A, b, e, S.mask);
+                masked_fit<kCluster>(S, A, T, b, e);
+                update_stats<kCluster>(S, A, T, b, e, S.mask);
                 if (threadIdx.x == 0) remove_prior(S.m, A.cfg.v_prior);
                 __syncthreads();
             }
         }
     }
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && T.rank == 0) {
         Mix &m = S.m;
         apply_prior(m, A.cfg.v_prior);
         st->k = m.K;
@@ -772,7 +880,30 @@ __global__ void __launch_bounds__(NT) k_split_merge(Args A) {
             ex->cov_w[c] = S.s.cw[c];
         }
         ex->samples_since_merge = S.s.since;
+        ex->stat_passes = S.stat_passes;
+        ex->em_iterations = S.em_iters;
     }
+    __syncthreads();
+}
+
+// Regions up to the cluster threshold: one CTA each, in the order after the
+// large ones (A.order[n_large..]).
+__global__ void __launch_bounds__(NT, 4) k_split_merge(Args A) {
+    __shared__ Shared S;
+    const uint32_t j = *A.n_large + blockIdx.x;
+    if (j >= A.n_regions) return;
+    split_merge_region<false>(S, A, Team{0, 1}, A.order[j]);
+}
+
+// Regions above the cluster threshold (A.order[0..n_large), largest first):
+// one cluster of CTAs per region, clusters striding over the regions.
+__global__ void __launch_bounds__(NT, 4) k_split_merge_cluster(Args A) {
+    __shared__ Shared S;
+    cg::cluster_group cl = cg::this_cluster();
+    const uint32_t size = cl.num_blocks(), n_clusters = gridDim.x / size;
+    const uint32_t n_large = *A.n_large;
+    for (uint32_t j = blockIdx.x / size; j < n_large; j += n_clusters)
+        split_merge_region<true>(S, A, Team{cl.block_rank(), size}, A.order[j]);
 }
 
 }  // namespace sm
@@ -784,13 +915,22 @@ int extras_ensure(pg_ctx *ctx, cudaStream_t s) {
     if (ctx->d_extras) return PG_OK;
     int st = check_cuda(ctx, cudaMalloc(&ctx->d_extras, sizeof(pg_region_extra) * (size_t)ctx->max_regions),
                         "split/merge statistics");
+    if (!st) st = check_cuda(ctx, cudaStreamCreateWithFlags(&ctx->sm_aux, cudaStreamNonBlocking), "split/merge stream");
+    if (!st) st = check_cuda(ctx, cudaEventCreateWithFlags(&ctx->sm_fork, cudaEventDisableTiming), "split/merge event");
+    if (!st) st = check_cuda(ctx, cudaEventCreateWithFlags(&ctx->sm_join, cudaEventDisableTiming), "split/merge event");
     if (!st) st = extras_reset(ctx, 0, ctx->max_regions, s);
     return st;
 }
 
 void extras_release(pg_ctx *ctx) {
-    if (ctx && ctx->d_extras) cudaFree(ctx->d_extras);
-    if (ctx) ctx->d_extras = nullptr;
+    if (!ctx) return;
+    if (ctx->d_extras) cudaFree(ctx->d_extras);
+    if (ctx->sm_aux) cudaStreamDestroy(ctx->sm_aux);
+    if (ctx->sm_fork) cudaEventDestroy(ctx->sm_fork);
+    if (ctx->sm_join) cudaEventDestroy(ctx->sm_join);
+    ctx->d_extras = nullptr;
+    ctx->sm_aux = nullptr;
+    ctx->sm_fork = ctx->sm_join = nullptr;
 }
 
 int extras_reset(pg_ctx *ctx, uint32_t first, uint32_t n, cudaStream_t s) {
@@ -813,6 +953,8 @@ void pg_default_split_merge_config(pg_split_merge_config *out) {
     out->min_samples_for_post_split_fitting = 4096;
     out->split_min_divergence = 0.5f;
     out->merge_max_divergence = 0.025f;
+    out->cluster_threshold = 0;
+    out->cluster_size = 0;
 }
 
 int pg_set_split_merge(pg_ctx *ctx, const pg_split_merge_config *cfg) {
@@ -838,13 +980,54 @@ int pg_split_merge(pg_ctx *ctx, const float *dirw, const float *pdf, const uint3
     A.dirw = reinterpret_cast<const float4 *>(dirw);
     A.pdf = pdf;
     A.offsets = offsets;
+    A.order = ctx->d_order;
+    A.n_large = ctx->d_counters + 8;
     A.n_regions = n_regions;
     A.cfg = ctx->cfg;
     A.sm = ctx->sm;
     if (!A.sm.min_samples_for_merging && !A.sm.split_min_divergence) pg_default_split_merge_config(&A.sm);
     A.sm.enabled = 1;
+    const uint32_t threshold = A.sm.cluster_threshold ? A.sm.cluster_threshold : 8192u;
+    const uint32_t csize = A.sm.cluster_size ? A.sm.cluster_size : 8u;
+    if (csize > 16) return set_error(ctx, PG_ERR_ARG, "split/merge cluster size above 16");
+    const bool clusters = threshold != 0xFFFFFFFFu && csize > 1;
+    if (int st = order_regions(ctx, offsets, n_regions, clusters ? threshold : 0xFFFFFFFFu,
+                               ctx->d_counters + 8, s))
+        return st;
+    if (clusters) {
+        auto kern = sm::k_split_merge_cluster;
+        if (csize > 8) {
+            if (int st = check_cuda(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1),
+                                    "split/merge cluster attribute"))
+                return st;
+        }
+        cudaLaunchConfig_t lc = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = csize;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        lc.blockDim = dim3(sm::NT, 1, 1);
+        lc.stream = ctx->sm_aux;
+        lc.attrs = attr;
+        lc.numAttrs = 1;
+        lc.gridDim = dim3(csize * (uint32_t)ctx->sm_count, 1, 1);
+        int resident = 0;
+        if (int st = check_cuda(ctx, cudaOccupancyMaxActiveClusters(&resident, kern, &lc), "split/merge occupancy"))
+            return st;
+        if (resident < 1) return set_error(ctx, PG_ERR_CUDA, "split/merge cluster does not fit on the device");
+        lc.gridDim = dim3(csize * std::min<uint32_t>((uint32_t)resident, n_regions), 1, 1);
+        // the large regions' clusters run on a side stream beside the per-CTA regions
+        int st = check_cuda(ctx, cudaEventRecord(ctx->sm_fork, s), "split/merge fork");
+        if (!st) st = check_cuda(ctx, cudaStreamWaitEvent(ctx->sm_aux, ctx->sm_fork, 0), "split/merge fork");
+        if (!st) st = check_cuda(ctx, cudaLaunchKernelEx(&lc, kern, A), "split/merge cluster launch");
+        if (!st) st = check_cuda(ctx, cudaEventRecord(ctx->sm_join, ctx->sm_aux), "split/merge join");
+        if (st) return st;
+    }
     sm::k_split_merge<<<n_regions, sm::NT, 0, s>>>(A);
-    return check_cuda(ctx, cudaGetLastError(), "split/merge launch");
+    int st = check_cuda(ctx, cudaGetLastError(), "split/merge launch");
+    if (!st && clusters) st = check_cuda(ctx, cudaStreamWaitEvent(s, ctx->sm_join, 0), "split/merge join");
+    return st;
 }
 
 int pg_get_region_extra(pg_ctx *ctx, pg_region_extra *host_out, uint32_t count) {

@@ -32,11 +32,14 @@ def tensors(torch, g, p):
     return d, pdf, o
 
 
-def split_merge_pass(torch, pkg, g, p):
+def split_merge_pass(torch, pkg, g, p, **knobs):
     abi = pkg.abi
     R = len(g[f"offsets{p}"]) - 1
     ctx = pkg.FitContext(cfg_from(abi, g["cfg"]), max_regions=R)
-    ctx.set_split_merge(sm_from(abi, g["sm"]))
+    sm = sm_from(abi, g["sm"])
+    for k, v in knobs.items():
+        setattr(sm, k, v)
+    ctx.set_split_merge(sm)
     ctx.set_states(g[f"fitted{p}"])
     ctx.set_extras(g[f"extras_in{p}"])
     d, pdf, o = tensors(torch, g, p)
@@ -58,11 +61,18 @@ def assert_extras_close(got, want, K, busy):
                                    atol=SM_TOL["cov_atol"])
 
 
+# regions above cluster_threshold samples are shared by a cluster of CTAs
+# (default: above 8192, 8 CTAs); 1 sends every region to a cluster
+TEAMS = [{}, {"cluster_threshold": 0xFFFFFFFF}, {"cluster_threshold": 1, "cluster_size": 2},
+         {"cluster_threshold": 1, "cluster_size": 4}, {"cluster_threshold": 1, "cluster_size": 16}]
+
+
+@pytest.mark.parametrize("team", TEAMS)
 @pytest.mark.parametrize("name", SETS)
-def test_split_merge_matches_reference_per_pass(name, cuda, pkg, golden):
+def test_split_merge_matches_reference_per_pass(name, team, cuda, pkg, golden):
     g = golden(name)
     for p in range(int(g["passes"])):
-        st, ex = split_merge_pass(cuda, pkg, g, p)
+        st, ex = split_merge_pass(cuda, pkg, g, p, **team)
         want, want_ex = g[f"states{p}"], g[f"extras{p}"]
         np.testing.assert_array_equal(st["k"], want["k"], err_msg=f"pass {p}")
         np.testing.assert_array_equal(ex["samples_since_merge"], want_ex["samples_since_merge"])
@@ -101,10 +111,11 @@ def test_fit_then_split_merge_sequence(name, cuda, pkg, golden):
     ctx.close()
 
 
-def test_split_merge_is_deterministic(cuda, pkg, golden):
+@pytest.mark.parametrize("team", [{}, {"cluster_threshold": 1, "cluster_size": 8}])
+def test_split_merge_is_deterministic(team, cuda, pkg, golden):
     g = golden("splitmerge_eager")
-    a = split_merge_pass(cuda, pkg, g, 3)
-    b = split_merge_pass(cuda, pkg, g, 3)
+    a = split_merge_pass(cuda, pkg, g, 3, **team)
+    b = split_merge_pass(cuda, pkg, g, 3, **team)
     assert a[0].tobytes() == b[0].tobytes() and a[1].tobytes() == b[1].tobytes()
 
 
