@@ -483,8 +483,39 @@ def bench_config1(pkg, abi, torch, stream, steps: int, cpu: bool):
     return out
 
 
+def split_merge_cpu_baseline(abi, w, pdf, states, extras, seconds: float):
+    """The C port of the reference's postFit (oracle/pg_oracle.c, lightpmm's
+    FP32 arithmetic) on the host cores, over the first regions of the same
+    workload from the same fitted states, sized for about `seconds`."""
+    from oracle.oracle import Oracle
+    o = Oracle()
+    threads = os.cpu_count() or 1
+    offsets = w["offsets"].astype(np.int64)
+    counts = np.diff(offsets)
+    cfg = abi.default_fit_config(num_initial_components=8)
+    sm = abi.default_split_merge_config()
+
+    def run(n):
+        sub = (offsets[:n + 1] - offsets[0]).astype(np.uint32)
+        t0 = time.perf_counter()
+        _, ex = o.postfit(cfg, sm, w["dirw"][:offsets[n]], pdf[:offsets[n]], sub, states[:n], extras[:n],
+                          threads=threads)
+        dt = time.perf_counter() - t0
+        passes = ex["stat_passes"].astype(np.int64) + ex["em_iterations"].astype(np.int64)
+        return int((counts[:n] * passes).sum()), dt
+
+    n = min(256, len(counts))
+    sp, dt = run(n)
+    rate = sp / max(dt, 1e-6)
+    per_region = sp / n
+    n = int(max(n, min(len(counts), rate * seconds / max(per_region, 1.0))))
+    sp, dt = run(n)
+    return {"value": sp / dt / 1e6, "unit": "Msample-pass/s", "cores": threads, "kind": "port",
+            "sample": f"first {n} of {len(counts)} regions ({int(counts[:n].sum())} samples), same fitted states"}
+
+
 def bench_split_merge(pkg, abi, torch, stream, w, steps: int, warmup: int, cluster_threshold: int = 0,
-                      cluster_size: int = 0):
+                      cluster_size: int = 0, cpu_seconds: float = 10.0, sampler=None):
     """PathGuiding::postFit with splitAndMerge (pg_split_merge) on the fit
     workload's regions, after a first fit with the reference's default fit
     configuration (K=8, up to 100 iterations): a first pass, so every region
@@ -506,16 +537,18 @@ def bench_split_merge(pkg, abi, torch, stream, w, steps: int, warmup: int, clust
     st0, ex0 = ctx.states(R), ctx.extras(R)
     times = []
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for i in range(warmup + steps):
-        ctx.set_states(st0, stream=stream)
-        ctx.set_extras(ex0)
-        torch.cuda.synchronize()
-        e0.record(stream)
-        ctx.split_merge(d, pdf, o, R, stream=stream)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        if i >= warmup:
-            times.append(e0.elapsed_time(e1))
+    import contextlib
+    with sampler if sampler is not None else contextlib.nullcontext():
+        for i in range(warmup + steps):
+            ctx.set_states(st0, stream=stream)
+            ctx.set_extras(ex0)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            ctx.split_merge(d, pdf, o, R, stream=stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if i >= warmup:
+                times.append(e0.elapsed_time(e1))
     ctx.sync(stream)
     st, ex = ctx.states(R), ctx.extras(R)
     ms = float(np.mean(times))
@@ -526,12 +559,16 @@ def bench_split_merge(pkg, abi, torch, stream, w, steps: int, warmup: int, clust
         R * 2.0 * (abi.STATE_DTYPE.itemsize + abi.EXTRA_DTYPE.itemsize)
     hbm, src = measured_peaks()
     K = st["k"].astype(np.int64)
+    cpu = None
+    if cpu_seconds > 0:
+        cpu = split_merge_cpu_baseline(abi, w, pdf.cpu().numpy(), st0, ex0, cpu_seconds)
     out = {"metric": "split/merge sample passes per second", "unit": "Msample-pass/s",
            "value": sample_passes / (ms * 1e-3) / 1e6, "ms_per_step": ms, "steps": steps,
-           "config": {"workload": "first-pass split/merge of the fit workload's 4096 regions (13.8 M samples, "
-                                  "pdf uniform 0.5-2 / 4 pi) after a default-configuration fit (K=8)",
+           "config": {"workload": f"first-pass split/merge of the fit workload's {R} regions ({n / 1e6:.1f} M "
+                                  "samples, pdf uniform 0.5-2 / 4 pi) after a default-configuration fit (K=8)",
                       "split_merge": "reference defaults (merge 8192, split 4096, refit 4096, 0.5, 0.025)"},
            "regions_split": int((K > 8).sum()), "k_mean_after": float(K.mean()),
+           "cpu_baseline": cpu,
            "stat_passes": int(ex["stat_passes"].sum()), "em_iterations": int(ex["em_iterations"].sum()),
            "gpu_launches": steps,
            "roofline": {"bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
@@ -606,9 +643,9 @@ def main():
     if args.workload == "splitmerge":
         stream = torch.cuda.Stream()
         sampler = ClockSampler(local)
-        with sampler:
-            line = bench_split_merge(pkg, abi, torch, stream, w, args.steps, args.warmup,
-                                     args.sm_cluster_threshold, args.sm_cluster_size)
+        line = bench_split_merge(pkg, abi, torch, stream, w, args.steps, args.warmup,
+                                 args.sm_cluster_threshold, args.sm_cluster_size,
+                                 cpu_seconds=0.0 if args.no_cpu_baseline or rank else 10.0, sampler=sampler)
         line.update(n_gpus=world, scaling="weak", vs_baseline=None, data="synthetic (seeded vMF mixtures)",
                     clocks=sampler.summary())
         if rank == 0:
@@ -767,8 +804,8 @@ def main():
         sg["clocks"] = ssampler.summary()
         line["surrogate"] = sg
         msampler = ClockSampler(local)
-        with msampler:
-            sm = bench_split_merge(pkg, abi, torch, stream, w, min(args.steps, 5), 2)
+        sm = bench_split_merge(pkg, abi, torch, stream, w, min(args.steps, 5), 2,
+                               cpu_seconds=0.0 if args.no_cpu_baseline or rank else 10.0, sampler=msampler)
         sm["clocks"] = msampler.summary()
         line["split_merge"] = sm
     if rank == 0:

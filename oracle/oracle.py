@@ -55,6 +55,8 @@ class Oracle:
         L.pgo_region_aabbs.argtypes = [_U32, _P, _P]
         L.pgo_sort_samples.argtypes = [_P, C.c_uint64, _U32, _P, _P]
         L.pgo_sort_samples.restype = C.c_uint64
+        L.pgo_postfit_lpmm32.argtypes = [C.POINTER(abi.FitConfig), C.POINTER(abi.SplitMergeConfig), _U32, _P, _P,
+                                         _P, _P, _P, _I]
 
     def init_states(self, cfg, n, exact=True):
         s = np.zeros(n, dtype=abi.STATE_DTYPE)
@@ -103,6 +105,20 @@ class Oracle:
         self.lib.pgo_prefit_parallax(R, abi.ptr(sorted_records), abi.ptr(offsets), abi.ptr(means),
                                      abi.ptr(dirw), abi.ptr(dist))
         return dirw, dist
+
+    def postfit(self, cfg, sm, dirw, pdf, offsets, states, extras, threads=None):
+        """PathGuiding::postFit's split and merge on lightpmm's FP32 arithmetic
+        (no distance update); returns new states and statistics."""
+        st = np.ascontiguousarray(states.copy())
+        ex = np.ascontiguousarray(extras.copy())
+        if ex.dtype != abi.EXTRA_DTYPE:
+            ex = ex.view(abi.EXTRA_DTYPE)
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint32)
+        dirw, pdf = _f32(dirw), _f32(pdf)  # kept alive across the call
+        threads = threads or (os.cpu_count() or 1)
+        self.lib.pgo_postfit_lpmm32(C.byref(cfg), C.byref(sm), offsets.shape[0] - 1, abi.ptr(dirw),
+                                    abi.ptr(pdf), abi.ptr(offsets), abi.ptr(st), abi.ptr(ex), threads)
+        return st, ex
 
     def update_distances(self, dirw, dist, offsets, states):
         st = states.copy()

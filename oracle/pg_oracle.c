@@ -782,3 +782,678 @@ uint64_t pgo_sort_samples(const pg_directional_data *rec, uint64_t n, uint32_t n
     free(cursor);
     return offsets[n_regions];
 }
+
+/* ------------------------------------------------------------------ */
+/* Split and merge after the fit (PathGuiding::postFit)                */
+/* ------------------------------------------------------------------ */
+/*
+ * PathGuiding::postFit with splitAndMerge (src/PathGuiding.cpp:413-451) on
+ * lightpmm's FP32 4-lane arithmetic: component pdfs with fastexp, per-lane
+ * partial sums folded as (l0 + l2) + (l1 + l3), a whole kernel's norms
+ * recomputed whenever one lane's kappa is set.  The statistics follow
+ * external/guiding/incrementalpearsonchisquared.h:53-204,
+ * incrementalcovariance2d.h:53-263 and incrementaldistance.h:165-216; the
+ * merge metric and merges src/PathGuiding.cpp:635-781 with
+ * VMFKernel.h:315-400, 478-530; the splits :494-633 with VMMFactory.h:226-297,
+ * 458-485.  The principal axis of the PCA split is the closed-form eigenvector
+ * of the symmetric 2x2 covariance (the reference calls Eigen there).
+ */
+
+#define SM_KM 16
+
+static float hsum4(const float p[4]) { return (p[0] + p[2]) + (p[1] + p[3]); }
+
+static float lane_pdf(const pg_region_state *s, int c, float dx, float dy, float dz) {
+    const float cs = (s->mu_x[c] * dx + s->mu_y[c] * dy) + s->mu_z[c] * dz;
+    const float tm = cs - 1.0f;
+    const float t = (tm < 0.0f) ? tm : 0.0f;
+    return s->norm[c] * pgo_fastexp(s->kappa[c] * t);
+}
+
+/* kappaToMeanCosine for one scalar (the 4-lane rule with all lanes equal) */
+static float k2r_scalar(float k) {
+    float kk[4] = {k, k, k, k}, r[4];
+    kappa_to_mean_cosine4(kk, r);
+    return r[0];
+}
+
+static float r2k_f(float r) { return (r * 3.0f - ((r * r) * r)) / (1.0f - r * r); }
+
+/* VMFKernel::setKappaAndR(idx, ...) then calNormalization of the whole kernel */
+static void set_kappa_r_lane(pg_region_state *s, int c, float kappa, float r) {
+    const int small = kappa < VMF_MIN_KAPPA;
+    s->kappa[c] = small ? 0.0f : kappa;
+    s->r[c] = small ? 0.0f : r;
+    const int k0 = c & ~3;
+    for (int i = 0; i < 4; ++i) cal_normalization_f32(s, k0 + i);
+}
+
+/* ParametricMixtureModel::removeWeightPrior / applyWeightPrior (:339-370) */
+static void pmm_remove_prior(pg_region_state *s, float v) {
+    const uint32_t K = s->k, nk = (K + 3) / 4;
+    const float inv = v * (float)K + 1.0f, wpn = 1.0f / inv, wptn = v * wpn;
+    for (uint32_t c = 0; c < 4 * nk; ++c) s->weight[c] = (s->weight[c] - wptn) * inv;
+    for (uint32_t c = K; c < 4 * nk; ++c) s->weight[c] = 0.0f;
+}
+static void pmm_apply_prior(pg_region_state *s, float v) {
+    const uint32_t K = s->k, nk = (K + 3) / 4;
+    const float inv = v * (float)K + 1.0f, wpn = 1.0f / inv, wptn = v * wpn;
+    for (uint32_t c = 0; c < 4 * nk; ++c) s->weight[c] = s->weight[c] * wpn + wptn;
+    for (uint32_t c = K; c < 4 * nk; ++c) s->weight[c] = 0.0f;
+}
+
+/* VMFKernel::cutoff of the lanes from K in K's kernel (resetInactiveComponents) */
+static void cutoff_last(pg_region_state *s) {
+    const uint32_t K = s->k;
+    if (K % 4 == 0) return;
+    for (uint32_t c = K; c < (K + 3) / 4 * 4; ++c) reset_lane(s, (int)c);
+}
+
+/* ParametricMixtureModel::setK (:426-440): lanes beyond K in K's kernel are
+ * cut off, the kernels after the next are reset */
+static void set_k(pg_region_state *s, uint32_t K) {
+    s->k = K;
+    const uint32_t full = K / 4, rem = K % 4;
+    if (rem) for (uint32_t c = K; c < 4 * full + 4; ++c) reset_lane(s, (int)c);
+    for (uint32_t k = full + 1; k < 4; ++k)
+        for (int i = 0; i < 4; ++i) reset_lane(s, (int)(4 * k + i));
+}
+
+/* Component pdfs and weight x pdf of one sample over the active kernels */
+static float sample_pdfs(const pg_region_state *s, uint32_t nk, float dx, float dy, float dz, float *pdf,
+                         float *wpdf) {
+    float part[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (uint32_t k = 0; k < nk; ++k)
+        for (int i = 0; i < 4; ++i) {
+            const int c = 4 * (int)k + i;
+            pdf[c] = lane_pdf(s, c, dx, dy, dz);
+            wpdf[c] = s->weight[c] * pdf[c];
+            part[i] = part[i] + wpdf[c];
+        }
+    return hsum4(part);
+}
+
+/* IncrementalPearsonChiSquared::updateDivergence(Masked) */
+static void chi2_update(const pg_region_state *s, pg_region_extra *x, const float *dirw, const float *pdf_s,
+                        uint32_t b, uint32_t e, uint32_t mask) {
+    if (e == b) return;
+    const uint32_t nk = (s->k + 3) / 4;
+    float batch[SM_KM] = {0};
+    for (uint32_t n = b; n < e; ++n) {
+        const float *d = dirw + 4 * (size_t)n;
+        float pdf[SM_KM], wpdf[SM_KM];
+        const float mix = sample_pdfs(s, nk, d[0], d[1], d[2], pdf, wpdf);
+        if (!(mix > PMM_EPS)) continue;
+        const float f = ((d[3] * d[3]) * pdf_s[n]) / (mix * mix);
+        for (uint32_t c = 0; c < 4 * nk; ++c)
+            if ((mask >> c) & 1u) batch[c] = batch[c] + pdf[c] * f;
+    }
+    const float N = (float)(e - b);
+    for (uint32_t c = 0; c < 4 * nk; ++c) {
+        if (!((mask >> c) & 1u)) continue;
+        const float nn = x->chi2_n[c] + N;
+        x->chi2_div[c] = (x->chi2_div[c] * x->chi2_n[c] + batch[c]) / nn;
+        x->chi2_n[c] = nn;
+    }
+}
+
+/* IncrementalCovariance2D::updateStatistics(Masked) */
+static void cov_update(const pg_region_state *s, pg_region_extra *x, const float *dirw, uint32_t b, uint32_t e,
+                       uint32_t mask) {
+    const uint32_t nk = (s->k + 3) / 4;
+    float sv[SM_KM][3], tv[SM_KM][3];
+    for (uint32_t c = 0; c < 4 * nk; ++c) {
+        const float nx = s->mu_x[c], ny = s->mu_y[c], nz = s->mu_z[c];
+        const float sx = nx * nx, sy = ny * ny, sz = nz * nz;
+        const int xg = sx > sy;
+        const float inv = 1.0f / sqrtf((xg ? sx : sy) + sz);
+        const float t0 = xg ? nz * inv : 0.0f, t1 = xg ? 0.0f : nz * inv, t2 = xg ? -nx * inv : -ny * inv;
+        tv[c][0] = t0, tv[c][1] = t1, tv[c][2] = t2;
+        sv[c][0] = (t1 * nz) - (t2 * ny);
+        sv[c][1] = (t2 * nx) - (t0 * nz);
+        sv[c][2] = (t0 * ny) - (t1 * nx);
+    }
+    float bw[SM_KM] = {0}, bv[SM_KM][3] = {{0}};
+    for (uint32_t n = b; n < e; ++n) {
+        const float *d = dirw + 4 * (size_t)n;
+        float pdf[SM_KM], wpdf[SM_KM];
+        const float mix = sample_pdfs(s, nk, d[0], d[1], d[2], pdf, wpdf);
+        const float inv = 1.0f / mix;
+        if (!(mix > PMM_EPS)) continue;
+        for (uint32_t c = 0; c < 4 * nk; ++c) {
+            if (!((mask >> c) & 1u)) continue;
+            const float wt = d[3] * (wpdf[c] * inv);
+            bw[c] = bw[c] + wt;
+            const float lx = (sv[c][0] * d[0] + sv[c][1] * d[1]) + sv[c][2] * d[2];
+            const float ly = (tv[c][0] * d[0] + tv[c][1] * d[1]) + tv[c][2] * d[2];
+            bv[c][0] = bv[c][0] + (lx * lx) * wt;
+            bv[c][1] = bv[c][1] + (ly * ly) * wt;
+            bv[c][2] = bv[c][2] + (lx * ly) * wt;
+        }
+    }
+    for (uint32_t c = 0; c < 4 * nk; ++c) {
+        if (!((mask >> c) & 1u)) continue;
+        const float ns = x->cov_w[c] + bw[c];
+        for (int i = 0; i < 3; ++i) x->cov[c][i] = ns > 0.0f ? (x->cov[c][i] * x->cov_w[c] + bv[c][i]) / ns : 0.0f;
+        x->cov_w[c] = ns;
+    }
+}
+
+/* VMMFactory::maskedFit with maskedParameterUpdate (prior applied on entry) */
+static void masked_fit32(const pg_fit_config *cfg, pg_region_state *s, const float *dirw, uint32_t b, uint32_t e,
+                         uint32_t mask, uint32_t *iters) {
+    const uint32_t K = s->k, nk = (K + 3) / 4;
+    cutoff_last(s);
+    const float inv_wpn = cfg->v_prior * (float)K + 1.0f, wpn = 1.0f / inv_wpn, wptn = cfg->v_prior * wpn;
+    const float rptw = cfg->r_prior * cfg->r_prior_weight;
+    float part[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (uint32_t c = 0; c < 4 * nk; ++c) {
+        const float w = s->weight[c];
+        const float wnp = (w > wptn) ? (w - wptn) * inv_wpn : 0.0f;
+        part[c & 3] = part[c & 3] + (((mask >> c) & 1u) ? wnp : 0.0f);
+    }
+    const float old_active = hsum4(part);
+    float mk[4] = {cfg->max_kappa, cfg->max_kappa, cfg->max_kappa, cfg->max_kappa}, maxr[4];
+    kappa_to_mean_cosine4(mk, maxr);
+    const uint32_t max_itr = (e - b) > 2u * K ? cfg->max_itr : 0;
+    float sum_w = 0.0f, ll = 0.0f, last_ll = 0.0f, abs_inv_last = 0.0f;
+    uint32_t i = 0;
+    for (; i < max_itr; ++i) {
+        stats32 st;
+        estep32(s, dirw, b, e, &st, i == 0 ? &sum_w : NULL, i >= cfg->min_itr ? &ll : NULL);
+        float ap[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        for (uint32_t k = 0; k < nk; ++k) {
+            if (!((mask >> (4 * k)) & 0xFu)) continue;
+            for (int l = 0; l < 4; ++l)
+                ap[l] = ap[l] + (((mask >> (4 * k + l)) & 1u) ? st.w[4 * k + l] : 0.0f);
+        }
+        const float norm = old_active * (sum_w / hsum4(ap));
+        for (uint32_t c = 0; c < 4 * nk; ++c)
+            if ((mask >> c) & 1u) {
+                st.sx[c] = st.sx[c] * norm;
+                st.sy[c] = st.sy[c] * norm;
+                st.sz[c] = st.sz[c] * norm;
+                st.w[c] = st.w[c] * norm;
+            }
+        for (uint32_t k = 0; k < nk; ++k) {
+            if (!((mask >> (4 * k)) & 0xFu)) continue;
+            float kap[4], rr[4];
+            for (int l = 0; l < 4; ++l) {
+                const int c = 4 * (int)k + l;
+                if (!((mask >> c) & 1u)) {
+                    kap[l] = s->kappa[c];
+                    rr[l] = s->r[c];
+                    continue;
+                }
+                const float mw = (st.w[c] / sum_w) * wpn + wptn;
+                const float rl = sqrtf((st.sx[c] * st.sx[c] + st.sy[c] * st.sy[c]) + st.sz[c] * st.sz[c]);
+                if (rl > 0.0f) {
+                    s->mu_x[c] = st.sx[c] / rl;
+                    s->mu_y[c] = st.sy[c] / rl;
+                    s->mu_z[c] = st.sz[c] / rl;
+                }
+                const float avg = rl / st.w[c];
+                const float ns = (float)s->total_num_samples * mw;
+                float rp = (avg * ns + rptw) / (ns + cfg->r_prior_weight);
+                rp = (rp < maxr[l]) ? rp : maxr[l];
+                s->weight[c] = mw;
+                kap[l] = r2k_f(rp);
+                rr[l] = rp;
+            }
+            for (int l = 0; l < 4; ++l) {
+                const int c = 4 * (int)k + l;
+                const int small = kap[l] < VMF_MIN_KAPPA;
+                s->kappa[c] = small ? 0.0f : kap[l];
+                s->r[c] = small ? 0.0f : rr[l];
+            }
+            for (int l = 0; l < 4; ++l) cal_normalization_f32(s, 4 * (int)k + l);
+        }
+        cutoff_last(s);
+        if (i >= cfg->min_itr) {
+            if (i > cfg->min_itr) {
+                const float rel = (ll - last_ll) * abs_inv_last;
+                if (rel < cfg->rel_ll_threshold) {
+                    ++i;
+                    break;
+                }
+            }
+            last_ll = ll;
+            abs_inv_last = 1.0f / fabsf(ll);
+        }
+    }
+    *iters += i;
+}
+
+typedef struct {
+    float w, mx, my, mz, k, nrm;
+} lobe_t;
+
+static lobe_t lobe_of(const pg_region_state *s, int c) {
+    lobe_t l = {s->weight[c], s->mu_x[c], s->mu_y[c], s->mu_z[c], s->kappa[c], s->norm[c]};
+    return l;
+}
+
+/* VMFKernel::product (sign +1) and division (sign -1): a becomes a*b or a/b,
+ * the integral is returned */
+static float vmf_combine(lobe_t *a, const lobe_t *b, int sign) {
+    float nx, ny, nz;
+    if (sign > 0) {
+        nx = a->mx * a->k + b->mx * b->k, ny = a->my * a->k + b->my * b->k, nz = a->mz * a->k + b->mz * b->k;
+    } else {
+        nx = a->mx * a->k - b->mx * b->k, ny = a->my * a->k - b->my * b->k, nz = a->mz * a->k - b->mz * b->k;
+    }
+    float nk = sqrtf((nx * nx + ny * ny) + nz * nz);
+    const int small = nk < VMF_MIN_KAPPA;
+    if (small) {
+        nk = 0.0f;
+        nx = a->mx, ny = a->my, nz = a->mz;
+    } else {
+        nx = nx / nk, ny = ny / nk, nz = nz / nk;
+    }
+    const float ci = a->nrm, cj = b->nrm;
+    const float e2 = pgo_fastexp(-2.0f * nk);
+    const float cij = small ? INV_4PI_F : ((float)(1.0 / (2.0 * 3.14159265358979323846)) * nk) / (1.0f - e2);
+    const float ti = (nx * a->mx + ny * a->my) + nz * a->mz, tj = (nx * b->mx + ny * b->my) + nz * b->mz;
+    float s;
+    if (sign > 0) {
+        const float t = a->k * (ti - 1.0f) + b->k * (tj - 1.0f);
+        s = (((pgo_fastexp(t) * a->w) * b->w) * (ci * cj)) / cij;
+    } else {
+        const float t = a->k * (ti - 1.0f) - b->k * (tj - 1.0f);
+        s = ((pgo_fastexp(t) * a->w) * ci) / ((b->w * cj) * cij);
+    }
+    a->w = s, a->mx = nx, a->my = ny, a->mz = nz, a->k = nk, a->nrm = cij;
+    return s;
+}
+
+/* VMFKernel::mergeComponent (:478-530): the merged lobe of two components,
+ * with its r and exp(-2 kappa) */
+static void merge_lobes(const pg_region_state *s, int a, int b, float out[8]) {
+    const float w0 = s->weight[a], w1 = s->weight[b], r0 = s->r[a], r1 = s->r[b];
+    float kappa = 0.0f, norm = INV_4PI_F, em2k = 1.0f;
+    const float w = w0 + w1;
+    float mx = w0 * r0 * s->mu_x[a] + w1 * r1 * s->mu_x[b];
+    float my = w0 * r0 * s->mu_y[a] + w1 * r1 * s->mu_y[b];
+    float mz = w0 * r0 * s->mu_z[a] + w1 * r1 * s->mu_z[b];
+    mx /= w, my /= w, mz /= w;
+    float r = mx * mx + my * my + mz * mz;
+    if (r > 0.0f) {
+        r = sqrtf(r);
+        kappa = r2k_f(r);
+        kappa = kappa < VMF_MIN_KAPPA ? 0.0f : kappa;
+        em2k = expf(-2.0f * kappa);
+        norm = (float)((double)kappa / (2.0 * 3.14159265358979323846 * (double)(1.0f - em2k)));
+        mx /= r, my /= r, mz /= r;
+    } else {
+        mx = s->mu_x[a], my = s->mu_y[a], mz = s->mu_z[a];
+    }
+    out[0] = w, out[1] = mx, out[2] = my, out[3] = mz, out[4] = kappa, out[5] = r, out[6] = norm, out[7] = em2k;
+}
+
+/* computePearsonChiSquaredMergeMetric for the pair a < b */
+static float merge_metric(const pg_region_state *s, int a, int b) {
+    const lobe_t ci = lobe_of(s, a), cj = lobe_of(s, b);
+    lobe_t si = ci, sj = cj, pij = ci;
+    vmf_combine(&si, &ci, 1);
+    vmf_combine(&sj, &cj, 1);
+    vmf_combine(&pij, &cj, 1);
+    float m[8];
+    merge_lobes(s, a, b, m);
+    const lobe_t mg = {m[0], m[1], m[2], m[3], m[4], m[6]};
+    const float q1 = vmf_combine(&si, &mg, -1), q2 = vmf_combine(&pij, &mg, -1), q3 = vmf_combine(&sj, &mg, -1);
+    return ((q1 + 2.0f * q2) + q3) - mg.w;
+}
+
+/* lightpmm::coordinateAxis (pmm-glm.h:107-117); its unqualified sqrt is the
+ * double one: 1/length in double, rounded to float */
+static void coordinate_axis(const float z[3], float x[3], float y[3]) {
+    if (fabsf(z[0]) > fabsf(z[1])) {
+        const float inv = (float)(1.0 / sqrt((double)(z[0] * z[0] + z[2] * z[2])));
+        y[0] = z[2] * inv, y[1] = 0.0f, y[2] = -z[0] * inv;
+    } else {
+        const float inv = (float)(1.0 / sqrt((double)(z[1] * z[1] + z[2] * z[2])));
+        y[0] = 0.0f, y[1] = z[2] * inv, y[2] = -z[1] * inv;
+    }
+    x[0] = y[1] * z[2] - y[2] * z[1];
+    x[1] = y[2] * z[0] - y[0] * z[2];
+    x[2] = y[0] * z[1] - y[1] * z[0];
+}
+
+/* VMFKernel::swapComponent across kernels */
+static void swap_lanes(pg_region_state *s, int i, int j) {
+    float *f[8] = {s->weight, s->mu_x, s->mu_y, s->mu_z, s->kappa, s->r, s->norm, s->e_min2k};
+    for (int q = 0; q < 8; ++q) {
+        const float t = f[q][i];
+        f[q][i] = f[q][j];
+        f[q][j] = t;
+    }
+}
+
+/* PathGuiding::mergeComponents (:762-781): statistics first, then the
+ * mixture (a takes the merge, b is reset and swapped with the last) */
+static void merge_pair(pg_region_state *s, pg_region_extra *x, int a, int b) {
+    const float wa = s->weight[a], wb = s->weight[b], mw = wa + wb;
+    const int last = (int)s->k - 1;
+    /* incrementaldistance.h:165-204 */
+    {
+        const float msw = mw / (wa / s->dist_sum_w[a] + wb / s->dist_sum_w[b]);
+        const float md = mw / (wa / s->distance[a] + wb / s->distance[b]);
+        s->distance[a] = md;
+        s->dist_sum_w[a] = msw;
+        if (b != last) {
+            s->distance[b] = s->distance[last];
+            s->dist_sum_w[b] = s->dist_sum_w[last];
+        }
+    }
+    const float inv = 1.0f / mw;
+    /* incrementalpearsonchisquared.h:176-204 */
+    if (!isinf(inv)) {
+        const float sa = wa * inv, sb = wb * inv;
+        const float d = sa * x->chi2_div[a] + sb * x->chi2_div[b];
+        const float n = sa * x->chi2_n[a] + sb * x->chi2_n[b];
+        x->chi2_div[a] = d;
+        x->chi2_n[a] = n;
+    } else {
+        x->chi2_div[a] = 0.0f;
+        x->chi2_n[a] = 0.0f;
+    }
+    if (b != last) {
+        x->chi2_div[b] = x->chi2_div[last];
+        x->chi2_n[b] = x->chi2_n[last];
+    }
+    /* incrementalcovariance2d.h:200-247; the merged mean is scaled by 1/3,
+     * what the reference's glm::vec3::length() (the component count) gives */
+    if (!isinf(inv)) {
+        float mu[3] = {wa * s->mu_x[a] + wb * s->mu_x[b], wa * s->mu_y[a] + wb * s->mu_y[b],
+                       wa * s->mu_z[a] + wb * s->mu_z[b]};
+        const float sc = 1.0f / 3.0f;
+        for (int i = 0; i < 3; ++i) mu[i] *= sc;
+        float fx[3], fy[3];
+        coordinate_axis(mu, fx, fy);
+        const float ax = (s->mu_x[a] * fx[0] + s->mu_y[a] * fx[1]) + s->mu_z[a] * fx[2];
+        const float ay = (s->mu_x[a] * fy[0] + s->mu_y[a] * fy[1]) + s->mu_z[a] * fy[2];
+        const float bx = (s->mu_x[b] * fx[0] + s->mu_y[b] * fx[1]) + s->mu_z[b] * fx[2];
+        const float by = (s->mu_x[b] * fy[0] + s->mu_y[b] * fy[1]) + s->mu_z[b] * fy[2];
+        const float msw = x->cov_w[a] + x->cov_w[b];
+        const float f = wa * wb / mw;
+        const float dx = ax - bx, dy = ay - by;
+        const float dv[3] = {dx * dx, dy * dy, dx * dy};
+        for (int i = 0; i < 3; ++i) x->cov[a][i] = ((wa * x->cov[a][i] + wb * x->cov[b][i]) + f * dv[i]) * inv;
+        x->cov_w[a] = msw;
+    } else {
+        x->cov[a][0] = x->cov[a][1] = x->cov[a][2] = 0.0f;
+        x->cov_w[a] = 0.0f;
+    }
+    if (b != last) {
+        for (int i = 0; i < 3; ++i) x->cov[b][i] = x->cov[last][i];
+        x->cov_w[b] = x->cov_w[last];
+    }
+    /* the mixture */
+    float m[8];
+    merge_lobes(s, a, b, m);
+    s->weight[a] = m[0], s->mu_x[a] = m[1], s->mu_y[a] = m[2], s->mu_z[a] = m[3];
+    s->kappa[a] = m[4], s->r[a] = m[5], s->norm[a] = m[6], s->e_min2k[a] = m[7];
+    reset_lane(s, b);
+    s->k -= 1;
+    if (b != (int)s->k) swap_lanes(s, b, (int)s->k);
+}
+
+/* libstdc++'s two-ended std::partition over keys with one or two payloads */
+static int partition_keys(float *key, int *pa, int *pb, int n, float thr, int keep_le) {
+    int first = 0, last = n;
+#define PRED(v) (keep_le ? ((v) <= thr) : ((v) >= thr))
+    for (;;) {
+        for (;;) {
+            if (first == last) return first;
+            if (PRED(key[first])) ++first;
+            else break;
+        }
+        --last;
+        for (;;) {
+            if (first == last) return first;
+            if (!PRED(key[last])) --last;
+            else break;
+        }
+        float tk = key[first];
+        key[first] = key[last];
+        key[last] = tk;
+        int t = pa[first];
+        pa[first] = pa[last];
+        pa[last] = t;
+        if (pb) {
+            t = pb[first];
+            pb[first] = pb[last];
+            pb[last] = t;
+        }
+        ++first;
+    }
+#undef PRED
+}
+
+/* PathGuiding::mergeAll (:635-707), prior removed */
+static void merge_all(pg_region_state *s, pg_region_extra *x, const pg_split_merge_config *sm) {
+    for (;;) {
+        const int n = (int)s->k;
+        if (n <= 1) return;
+        float key[SM_KM * (SM_KM - 1) / 2];
+        int ca[SM_KM * (SM_KM - 1) / 2], cb[SM_KM * (SM_KM - 1) / 2];
+        int idx = 0;
+        for (int a = 0; a < n; ++a)
+            for (int b = a + 1; b < n; ++b, ++idx) {
+                key[idx] = merge_metric(s, a, b);
+                ca[idx] = a;
+                cb[idx] = b;
+            }
+        const int end = partition_keys(key, ca, cb, idx, sm->merge_max_divergence, 1);
+        for (int i = 1; i < end; ++i) { /* ascending by metric */
+            const float k = key[i];
+            const int a = ca[i], b = cb[i];
+            int j = i - 1;
+            while (j >= 0 && key[j] > k) {
+                key[j + 1] = key[j], ca[j + 1] = ca[j], cb[j + 1] = cb[j];
+                --j;
+            }
+            key[j + 1] = k, ca[j + 1] = a, cb[j + 1] = b;
+        }
+        uint32_t used = 0;
+        int ma[SM_KM], mb[SM_KM], nm = 0;
+        for (int i = 0; i < end; ++i) {
+            const int a = ca[i] < cb[i] ? ca[i] : cb[i], b = ca[i] < cb[i] ? cb[i] : ca[i];
+            if (((used >> a) & 1u) || ((used >> b) & 1u)) continue;
+            ma[nm] = a, mb[nm] = b, ++nm;
+            used |= (1u << a) | (1u << b);
+        }
+        if (nm == 0) return;
+        for (int i = 1; i < nm; ++i) { /* by second index, descending */
+            const int a = ma[i], b = mb[i];
+            int j = i - 1;
+            while (j >= 0 && mb[j] < b) {
+                ma[j + 1] = ma[j], mb[j + 1] = mb[j];
+                --j;
+            }
+            ma[j + 1] = a, mb[j + 1] = b;
+        }
+        for (int i = 0; i < nm; ++i) merge_pair(s, x, ma[i], mb[i]);
+    }
+}
+
+/* The larger eigenvalue of the symmetric 2x2 [[a, b], [b, c]] and its unit
+ * eigenvector, in closed form */
+static void principal_axis(float a, float b, float c, float *lambda, float *vx, float *vy) {
+    const float h = 0.5f * (a - c);
+    const float d = sqrtf(h * h + b * b);
+    *lambda = 0.5f * (a + c) + d;
+    if (b == 0.0f) {
+        *vx = a >= c ? 1.0f : 0.0f;
+        *vy = a >= c ? 0.0f : 1.0f;
+        return;
+    }
+    float x, y;
+    if (a >= c) {
+        x = *lambda - c;
+        y = b;
+    } else {
+        x = b;
+        y = *lambda - a;
+    }
+    const float inv = 1.0f / sqrtf(x * x + y * y);
+    *vx = x * inv;
+    *vy = y * inv;
+}
+
+/* splitComponentUsingPCA (:494-561) */
+static void split_component(pg_region_state *s, pg_region_extra *x, int c, float max_kappa) {
+    if (s->k == SM_KM) return;
+    const int dst = (int)s->k;
+    const float z3[3] = {s->mu_x[c], s->mu_y[c], s->mu_z[c]};
+    float fx[3], fy[3];
+    coordinate_axis(z3, fx, fy);
+    const int has = x->cov_w[c] > 0.0f;
+    const float va = has ? x->cov[c][0] : 0.0f, vb = has ? x->cov[c][2] : 0.0f, vc = has ? x->cov[c][1] : 0.0f;
+    float lambda, px, py;
+    principal_axis(va, vb, vc, &lambda, &px, &py);
+    const float hv = 0.5f * sqrtf(lambda);
+    const float off = (hv < 1.0f) ? hv : 1.0f;
+    px *= off;
+    py *= off;
+    const float z = sqrtf(1.0f - off * off);
+    float ma[3], mbv[3];
+    for (int i = 0; i < 3; ++i) {
+        ma[i] = (px * fx[i] + py * fy[i]) + z * z3[i];
+        mbv[i] = (-px * fx[i] + -py * fy[i]) + z * z3[i];
+    }
+    set_k(s, (uint32_t)dst + 1);
+    const float src_r = s->r[c], src_w = s->weight[c];
+    const float split_w = src_w * 0.5f;
+    const float max_r = k2r_scalar(max_kappa);
+    float split_r = max_r;
+    if (z > 0.0f) {
+        const float q = src_r / z;
+        split_r = (q < max_r) ? q : max_r;
+    }
+    const float split_k = r2k_f(split_r);
+    set_kappa_r_lane(s, c, split_k, split_r);
+    s->mu_x[c] = ma[0], s->mu_y[c] = ma[1], s->mu_z[c] = ma[2];
+    s->weight[c] = split_w;
+    set_kappa_r_lane(s, dst, split_k, split_r);
+    s->mu_x[dst] = mbv[0], s->mu_y[dst] = mbv[1], s->mu_z[dst] = mbv[2];
+    s->weight[dst] = split_w;
+    s->distance[dst] = s->distance[c];
+    const float hw = 0.5f * s->dist_sum_w[c];
+    s->dist_sum_w[c] = hw;
+    s->dist_sum_w[dst] = hw;
+    x->chi2_div[c] = x->chi2_div[dst] = 0.0f;
+    x->chi2_n[c] = x->chi2_n[dst] = 0.0f;
+    for (int i = 0; i < 3; ++i) x->cov[c][i] = x->cov[dst][i] = 0.0f;
+    x->cov_w[c] = x->cov_w[dst] = 0.0f;
+}
+
+/* splitAll (:563-633), iterative, prior removed on entry and exit */
+static void split_all(const pg_fit_config *cfg, const pg_split_merge_config *sm, pg_region_state *s,
+                      pg_region_extra *x, const float *dirw, const float *pdf, uint32_t b, uint32_t e, int fit) {
+    if (s->k >= SM_KM) return;
+    const int first = (uint64_t)(e - b) == s->total_num_samples;
+    for (;;) {
+        const int K = (int)s->k;
+        const float ia = (s->num_samples * s->num_samples) / (s->sample_weight * s->sample_weight);
+        float key[SM_KM];
+        int cand[SM_KM];
+        for (int c = 0; c < K; ++c) {
+            const float div = x->chi2_div[c] * ia - 1.0f;
+            const int enough = x->chi2_n[c] > (float)sm->min_samples_for_splitting;
+            key[c] = fabsf((first || enough) ? div * s->weight[c] : 0.0f);
+            cand[c] = c;
+        }
+        const int nc = partition_keys(key, cand, NULL, K, sm->split_min_divergence, 0);
+        const int room = SM_KM - K;
+        const int ns = nc < room ? nc : room;
+        if (ns == 0) break;
+        if (nc > ns)
+            for (int i = 1; i < nc; ++i) { /* the ns largest first, descending */
+                const float k = key[i];
+                const int c = cand[i];
+                int j = i - 1;
+                while (j >= 0 && key[j] < k) {
+                    key[j + 1] = key[j], cand[j + 1] = cand[j];
+                    --j;
+                }
+                key[j + 1] = k, cand[j + 1] = c;
+            }
+        uint32_t mask = 0;
+        for (int i = 0; i < ns; ++i) {
+            mask |= 1u << cand[i];
+            mask |= 1u << s->k;
+            split_component(s, x, cand[i], cfg->max_kappa);
+        }
+        if (fit) {
+            pmm_apply_prior(s, cfg->v_prior);
+            masked_fit32(cfg, s, dirw, b, e, mask, &x->em_iterations);
+            chi2_update(s, x, dirw, pdf, b, e, mask);
+            cov_update(s, x, dirw, b, e, mask);
+            x->stat_passes += 1;
+            pmm_remove_prior(s, cfg->v_prior);
+        }
+    }
+}
+
+static void postfit_region32(const pg_fit_config *cfg, const pg_split_merge_config *sm, const float *dirw,
+                             const float *pdf, uint32_t b, uint32_t e, pg_region_state *s, pg_region_extra *x) {
+    if (e == b) return;
+    x->stat_passes = 0;
+    x->em_iterations = 0;
+    x->samples_since_merge += (float)(e - b);
+    if (x->samples_since_merge > (float)sm->min_samples_for_merging) {
+        pmm_remove_prior(s, cfg->v_prior);
+        merge_all(s, x, sm);
+        pmm_apply_prior(s, cfg->v_prior);
+        x->samples_since_merge = 0.0f;
+    }
+    chi2_update(s, x, dirw, pdf, b, e, 0xFFFFu);
+    cov_update(s, x, dirw, b, e, 0xFFFFu);
+    x->stat_passes += 1;
+    const int first = (uint64_t)(e - b) == s->total_num_samples;
+    const int fit = first || (e - b) > sm->min_samples_for_post_split_fitting;
+    pmm_remove_prior(s, cfg->v_prior);
+    split_all(cfg, sm, s, x, dirw, pdf, b, e, fit);
+    pmm_apply_prior(s, cfg->v_prior);
+}
+
+typedef struct {
+    const pg_fit_config *cfg;
+    const pg_split_merge_config *sm;
+    uint32_t n_regions;
+    const float *dirw, *pdf;
+    const uint32_t *offsets;
+    pg_region_state *states;
+    pg_region_extra *extras;
+    uint32_t next; /* atomic */
+} postfit_job_t;
+
+static void *postfit_worker(void *arg) {
+    postfit_job_t *j = (postfit_job_t *)arg;
+    for (;;) {
+        const uint32_t r = __atomic_fetch_add(&j->next, 1u, __ATOMIC_RELAXED);
+        if (r >= j->n_regions) break;
+        postfit_region32(j->cfg, j->sm, j->dirw, j->pdf, j->offsets[r], j->offsets[r + 1], &j->states[r],
+                         &j->extras[r]);
+    }
+    return NULL;
+}
+
+int pgo_postfit_lpmm32(const pg_fit_config *cfg, const pg_split_merge_config *sm, uint32_t n_regions,
+                       const float *dirw, const float *pdf, const uint32_t *offsets, pg_region_state *states,
+                       pg_region_extra *extras, int n_threads) {
+    postfit_job_t j = {cfg, sm, n_regions, dirw, pdf, offsets, states, extras, 0};
+    if (n_threads <= 1) {
+        postfit_worker(&j);
+        return 0;
+    }
+    if (n_threads > 256) n_threads = 256;
+    pthread_t th[256];
+    int started = 0;
+    for (int t = 0; t < n_threads; ++t)
+        if (pthread_create(&th[t], NULL, postfit_worker, &j) == 0) ++started;
+    if (started == 0) postfit_worker(&j);
+    for (int t = 0; t < started; ++t) pthread_join(th[t], NULL);
+    return 0;
+}

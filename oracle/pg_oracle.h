@@ -50,6 +50,16 @@ int pgo_fit_f64(const pg_fit_config *cfg, int mode, uint32_t n_regions, const fl
 void pgo_eval_ll_f64(uint32_t n_regions, const float *dirw, const uint32_t *offsets,
                      const pg_region_state *states, double *ll_out);
 
+/* PathGuiding::postFit with splitAndMerge (src/PathGuiding.cpp:413-451):
+ * merges, divergence and covariance statistics, PCA splits with masked refits,
+ * on lightpmm's FP32 4-lane arithmetic, for regions [0, n_regions) over
+ * `n_threads` host threads; regions without samples are untouched.  pdf = the
+ * records' sampling pdf, grouped like dirw.  The parallax distances are not
+ * updated here (pgo_update_distances). */
+int pgo_postfit_lpmm32(const pg_fit_config *cfg, const pg_split_merge_config *sm, uint32_t n_regions,
+                       const float *dirw, const float *pdf, const uint32_t *offsets, pg_region_state *states,
+                       pg_region_extra *extras, int n_threads);
+
 /* lightpmm fastexp (pmm-vcl.h:158-184), scalar restatement. */
 float pgo_fastexp(float x);
 

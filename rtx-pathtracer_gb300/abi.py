@@ -69,7 +69,9 @@ def forced_iterations(n: int, **kw) -> FitConfig:
 
 
 def ptr(a: np.ndarray) -> C.c_void_p:
-    return C.c_void_p(a.ctypes.data)
+    """Address of an array's data; the pointer holds a reference to the
+    array, so a temporary (a converted copy) outlives the call it is passed to."""
+    return a.ctypes.data_as(C.c_void_p)
 
 # ---- tracer -------------------------------------------------------------
 PG_MAT_DIFFUSE, PG_MAT_SPECULAR, PG_MAT_DIELECTRIC, PG_MAT_LIGHT, PG_MAT_GGX = 0, 1, 2, 3, 6

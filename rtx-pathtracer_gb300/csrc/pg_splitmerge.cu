@@ -82,6 +82,7 @@ struct Shared {
     int fit_iters;
     int stop;
     float old_active;        // masked EM: prior-free weight of the refitted components
+    int merge, n_merged;     // mergeAll runs / merges of the last round
     uint32_t stat_passes, em_iters;  // work done, reported in the region's statistics
     float ll_last, ll_abs_inv;
     float sum_w;             // weight of the valid samples (masked EM, first iteration)
@@ -259,13 +260,14 @@ SM_HD float merge_metric(const Mix &m, int i, int j) {
     return q1 + 2.0f * q2 + q3 - merged.w;
 }
 
-// lightpmm::coordinateAxis / Frame (pmm-glm.h:107-133)
+// lightpmm::coordinateAxis / Frame (pmm-glm.h:107-133).  Its unqualified
+// sqrt resolves to the double one, so 1/length is taken in double and rounded.
 SM_HD void coordinate_axis(const float z[3], float x[3], float y[3]) {
     if (fabsf(z[0]) > fabsf(z[1])) {
-        const float inv = 1.0f / sqrtf(z[0] * z[0] + z[2] * z[2]);
+        const float inv = (float)(1.0 / sqrt((double)(z[0] * z[0] + z[2] * z[2])));
         y[0] = z[2] * inv, y[1] = 0.0f, y[2] = -z[0] * inv;
     } else {
-        const float inv = 1.0f / sqrtf(z[1] * z[1] + z[2] * z[2]);
+        const float inv = (float)(1.0 / sqrt((double)(z[1] * z[1] + z[2] * z[2])));
         y[0] = 0.0f, y[1] = z[2] * inv, y[2] = -z[1] * inv;
     }
     x[0] = y[1] * z[2] - y[2] * z[1];
@@ -381,52 +383,73 @@ SM_HD int hoare_partition(float *key, int *pa, int *pb, int n, Pred pred) {
 }
 
 // mergeAll (src/PathGuiding.cpp:635-707), thread 0
-SM_HD void merge_all(Mix &m, Stats &s, const pg_split_merge_config &cfg, MergeScratch &ms) {
+// Merge metric of the pairs [first, n (n - 1) / 2) with stride `step`, in the
+// row-major order of (a, b), a < b.
+SM_HD void merge_candidates(const Mix &m, MergeScratch &ms, int first, int step) {
+    const int n = (int)m.K;
+    const int np = n * (n - 1) / 2;
+    for (int idx = first; idx < np; idx += step) {
+        int a = 0, rem = idx;
+        while (rem >= n - 1 - a) {
+            rem -= n - 1 - a;
+            ++a;
+        }
+        const int b = a + 1 + rem;
+        ms.key[idx] = merge_metric(m, a, b);
+        ms.ca[idx] = a;
+        ms.cb[idx] = b;
+    }
+}
+
+// One round of mergeAll (src/PathGuiding.cpp:635-707) on the candidates:
+// pairs below the threshold, cheapest first, disjoint, merged from the highest
+// second index down.  Returns the number of merges.
+SM_HD int merge_round(Mix &m, Stats &s, const pg_split_merge_config &cfg, MergeScratch &ms) {
     float *key = ms.key;
     int *ca = ms.ca, *cb = ms.cb;
+    const int n = (int)m.K;
+    const int np = n * (n - 1) / 2;
+    const float thr = cfg.merge_max_divergence;
+    const int end = hoare_partition(key, ca, cb, np, [thr](float v) { return v <= thr; });
+    // sort by metric ascending (insertion; the reference's std::sort on distinct values)
+    for (int i = 1; i < end; ++i) {
+        const float k = key[i];
+        const int a = ca[i], b = cb[i];
+        int j = i - 1;
+        while (j >= 0 && key[j] > k) {
+            key[j + 1] = key[j], ca[j + 1] = ca[j], cb[j + 1] = cb[j];
+            --j;
+        }
+        key[j + 1] = k, ca[j + 1] = a, cb[j + 1] = b;
+    }
+    uint32_t used = 0;
+    int ma[KM], mb[KM], nm = 0;
+    for (int i = 0; i < end; ++i) {
+        const int a = min(ca[i], cb[i]), b = max(ca[i], cb[i]);
+        if ((used >> a) & 1u || (used >> b) & 1u) continue;
+        ma[nm] = a, mb[nm] = b, ++nm;
+        used |= (1u << a) | (1u << b);
+    }
+    // by second index, descending, so later merges keep their indices
+    for (int i = 1; i < nm; ++i) {
+        const int a = ma[i], b = mb[i];
+        int j = i - 1;
+        while (j >= 0 && mb[j] < b) {
+            ma[j + 1] = ma[j], mb[j + 1] = mb[j];
+            --j;
+        }
+        ma[j + 1] = a, mb[j + 1] = b;
+    }
+    for (int i = 0; i < nm; ++i) merge_components(m, s, ma[i], mb[i]);
+    return nm;
+}
+
+// mergeAll on one thread (host checks)
+SM_HD void merge_all(Mix &m, Stats &s, const pg_split_merge_config &cfg, MergeScratch &ms) {
     for (int round = 0; round < KM; ++round) {
-        const int n = (int)m.K;
-        if (n <= 1) return;
-        int idx = 0;
-        for (int a = 0; a < n; ++a)
-            for (int b = a + 1; b < n; ++b, ++idx) {
-                key[idx] = merge_metric(m, a, b);
-                ca[idx] = a;
-                cb[idx] = b;
-            }
-        const float thr = cfg.merge_max_divergence;
-        const int end = hoare_partition(key, ca, cb, idx, [thr](float v) { return v <= thr; });
-        // sort by metric ascending (insertion; the reference's std::sort on distinct values)
-        for (int i = 1; i < end; ++i) {
-            const float k = key[i];
-            const int a = ca[i], b = cb[i];
-            int j = i - 1;
-            while (j >= 0 && key[j] > k) {
-                key[j + 1] = key[j], ca[j + 1] = ca[j], cb[j + 1] = cb[j];
-                --j;
-            }
-            key[j + 1] = k, ca[j + 1] = a, cb[j + 1] = b;
-        }
-        uint32_t used = 0;
-        int ma[KM], mb[KM], nm = 0;
-        for (int i = 0; i < end; ++i) {
-            const int a = min(ca[i], cb[i]), b = max(ca[i], cb[i]);
-            if ((used >> a) & 1u || (used >> b) & 1u) continue;
-            ma[nm] = a, mb[nm] = b, ++nm;
-            used |= (1u << a) | (1u << b);
-        }
-        if (nm == 0) return;
-        // by second index, descending, so later merges keep their indices
-        for (int i = 1; i < nm; ++i) {
-            const int a = ma[i], b = mb[i];
-            int j = i - 1;
-            while (j >= 0 && mb[j] < b) {
-                ma[j + 1] = ma[j], mb[j + 1] = mb[j];
-                --j;
-            }
-            ma[j + 1] = a, mb[j + 1] = b;
-        }
-        for (int i = 0; i < nm; ++i) merge_components(m, s, ma[i], mb[i]);
+        if (m.K <= 1) return;
+        merge_candidates(m, ms, 0, 1);
+        if (!merge_round(m, s, cfg, ms)) return;
     }
 }
 
@@ -794,14 +817,25 @@ __device__ void split_merge_region(Shared &S, const Args &A, Team T, uint32_t r)
         S.stat_passes = 0;
         S.em_iters = 0;
         S.s.since = ex->samples_since_merge + (float)(e - b);
-        if (S.s.since > (float)A.sm.min_samples_for_merging) {
+        S.merge = S.s.since > (float)A.sm.min_samples_for_merging;
+        if (S.merge) {
             remove_prior(m, A.cfg.v_prior);
-            merge_all(m, S.s, A.sm, S.ms);
-            apply_prior(m, A.cfg.v_prior);
             S.s.since = 0.0f;
         }
     }
     __syncthreads();
+    if (S.merge) {
+        // mergeAll: the pair metrics by all threads, each round's merges by thread 0
+        for (int round = 0; round < KM && S.m.K > 1; ++round) {
+            merge_candidates(S.m, S.ms, threadIdx.x, NT);
+            __syncthreads();
+            if (threadIdx.x == 0) S.n_merged = merge_round(S.m, S.s, A.sm, S.ms);
+            __syncthreads();
+            if (!S.n_merged) break;
+        }
+        if (threadIdx.x == 0) apply_prior(S.m, A.cfg.v_prior);
+        __syncthreads();
+    }
     update_stats<kCluster>(S, A, T, b, e, 0xFFFFu);
     const bool first = (unsigned long long)(e - b) == S.m.total;
     const bool fit = first || (e - b) > A.sm.min_samples_for_post_split_fitting;
