@@ -76,7 +76,7 @@ struct Shared {
     PassMix pm;
     MergeScratch ms;
     float red[NW][4 * KM + 2];
-    float part[4 * KM + 2];  // this CTA's sums of a pass (read by the cluster)
+    float part[2][4 * KM + 2];  // this CTA's sums of a pass, double-buffered (read by the cluster)
     float acc[4 * KM + 2];   // the region's sums of a pass
     uint32_t mask;           // components refitted by the masked EM
     int fit_iters;
@@ -574,13 +574,14 @@ __device__ void load_pass_mix(Shared &S, bool frames) {
 // rank 0 writes the region back.
 struct Team {
     uint32_t rank, size;
+    uint32_t phase;  // passes reduced so far: selects the partial-sum buffer
 };
 
 // Reduction of per-thread values v[0..N) in a fixed order (lanes, warps, then
 // cluster ranks 0..size-1): value i goes to S.acc[i] below `tail`, to
 // S.acc[4 KM + i - tail] from it on, in every CTA of the team.
 template <int N, bool kCluster>
-__device__ void block_sum(Shared &S, const float (&v)[N], int tail) {
+__device__ void block_sum(Shared &S, Team &T, const float (&v)[N], int tail) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int i = 0; i < N; ++i) {
@@ -600,20 +601,25 @@ __device__ void block_sum(Shared &S, const float (&v)[N], int tail) {
         __syncthreads();
         return;
     }
+    // Partials of consecutive passes alternate between two buffers: a rank
+    // writes a buffer again two passes later, after the next cluster barrier,
+    // which every rank reaches only once it has read this pass's partials.
+    float *part = S.part[T.phase & 1u];
+    ++T.phase;
     if (i < N) {
         float x = 0.0f;
         for (int w = 0; w < NW; ++w) x += S.red[w][i];
-        S.part[i] = x;
+        part[i] = x;
     }
     cg::cluster_group cl = cg::this_cluster();
     cl.sync();  // every rank's partial sums are visible
     if (i < N) {
         const uint32_t nr = cl.num_blocks();
         float x = 0.0f;
-        for (uint32_t r = 0; r < nr; ++r) x += cl.map_shared_rank(S.part, r)[i];
+        for (uint32_t r = 0; r < nr; ++r) x += cl.map_shared_rank(part, r)[i];
         S.acc[i < tail ? i : 4 * KM + i - tail] = x;
     }
-    cl.sync();  // no rank overwrites its partials while another still reads them
+    __syncthreads();
 }
 
 // Pass kinds over the region's samples
@@ -626,7 +632,7 @@ enum { PASS_CHI2 = 0, PASS_COV = 1, PASS_EM = 2 };
 // yy, xy moments in the component's frame; EM [4c..4c+3] = sum of gamma_c w
 // d.xyz and gamma_c w, [4 KM] = sum w, [4 KM + 1] = sum w log2(mix).
 template <int KIND, int L, bool kCluster>
-__device__ void sample_pass_l(Shared &S, const Args &A, Team T, uint32_t b, uint32_t e) {
+__device__ void sample_pass_l(Shared &S, const Args &A, Team &T, uint32_t b, uint32_t e) {
     constexpr int NV = KIND == PASS_CHI2 ? L : 4 * L + (KIND == PASS_EM ? 2 : 0);
     float v[NV];
 #pragma unroll
@@ -672,11 +678,11 @@ __device__ void sample_pass_l(Shared &S, const Args &A, Team T, uint32_t b, uint
             }
         }
     }
-    block_sum<NV, kCluster>(S, v, KIND == PASS_CHI2 ? NV : 4 * L);
+    block_sum<NV, kCluster>(S, T, v, KIND == PASS_CHI2 ? NV : 4 * L);
 }
 
 template <int KIND, bool kCluster>
-__device__ void sample_pass(Shared &S, const Args &A, Team T, uint32_t b, uint32_t e) {
+__device__ void sample_pass(Shared &S, const Args &A, Team &T, uint32_t b, uint32_t e) {
     switch (active_lanes(S.m.K)) {
         case 4: sample_pass_l<KIND, 4, kCluster>(S, A, T, b, e); break;
         case 8: sample_pass_l<KIND, 8, kCluster>(S, A, T, b, e); break;
@@ -687,7 +693,7 @@ __device__ void sample_pass(Shared &S, const Args &A, Team T, uint32_t b, uint32
 
 // updateDivergence(Masked) and updateStatistics(Masked) over the region's samples
 template <bool kCluster>
-__device__ void update_stats(Shared &S, const Args &A, Team T, uint32_t b, uint32_t e, uint32_t mask) {
+__device__ void update_stats(Shared &S, const Args &A, Team &T, uint32_t b, uint32_t e, uint32_t mask) {
     const int L = (int)active_lanes(S.m.K);
     const float n = (float)(e - b);
     if (threadIdx.x == 0) ++S.stat_passes;
@@ -714,7 +720,7 @@ __device__ void update_stats(Shared &S, const Args &A, Team T, uint32_t b, uint3
 
 // VMMFactory::maskedFit with maskedParameterUpdate (VMMFactory.h:226-297, 458-485)
 template <bool kCluster>
-__device__ void masked_fit(Shared &S, const Args &A, Team T, uint32_t b, uint32_t e) {
+__device__ void masked_fit(Shared &S, const Args &A, Team &T, uint32_t b, uint32_t e) {
     const pg_fit_config &cfg = A.cfg;
     Mix &m = S.m;
     const uint32_t K = m.K;
@@ -787,7 +793,7 @@ __device__ void masked_fit(Shared &S, const Args &A, Team T, uint32_t b, uint32_
 
 // PathGuiding::postFit with splitAndMerge of region r by a team of CTAs.
 template <bool kCluster>
-__device__ void split_merge_region(Shared &S, const Args &A, Team T, uint32_t r) {
+__device__ void split_merge_region(Shared &S, const Args &A, Team &T, uint32_t r) {
     const uint32_t b = A.offsets[r], e = A.offsets[r + 1];
     if (e == b) return;  // PathGuiding::update skips empty regions
     pg_region_state *st = A.states + r;
@@ -917,7 +923,10 @@ __device__ void split_merge_region(Shared &S, const Args &A, Team T, uint32_t r)
         ex->stat_passes = S.stat_passes;
         ex->em_iterations = S.em_iters;
     }
-    __syncthreads();
+    // no rank leaves (or starts the next region) while another may still read
+    // its last partial sums
+    if (kCluster) cg::this_cluster().sync();
+    else __syncthreads();
 }
 
 // Regions up to the cluster threshold: one CTA each, in the order after the
@@ -926,7 +935,8 @@ __global__ void __launch_bounds__(NT, 4) k_split_merge(Args A) {
     __shared__ Shared S;
     const uint32_t j = *A.n_large + blockIdx.x;
     if (j >= A.n_regions) return;
-    split_merge_region<false>(S, A, Team{0, 1}, A.order[j]);
+    Team T{0, 1, 0};
+    split_merge_region<false>(S, A, T, A.order[j]);
 }
 
 // Regions above the cluster threshold (A.order[0..n_large), largest first):
@@ -936,8 +946,8 @@ __global__ void __launch_bounds__(NT, 4) k_split_merge_cluster(Args A) {
     cg::cluster_group cl = cg::this_cluster();
     const uint32_t size = cl.num_blocks(), n_clusters = gridDim.x / size;
     const uint32_t n_large = *A.n_large;
-    for (uint32_t j = blockIdx.x / size; j < n_large; j += n_clusters)
-        split_merge_region<true>(S, A, Team{cl.block_rank(), size}, A.order[j]);
+    Team T{cl.block_rank(), size, 0};
+    for (uint32_t j = blockIdx.x / size; j < n_large; j += n_clusters) split_merge_region<true>(S, A, T, A.order[j]);
 }
 
 }  // namespace sm
