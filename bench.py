@@ -559,6 +559,13 @@ def bench_split_merge(pkg, abi, torch, stream, w, steps: int, warmup: int, clust
         R * 2.0 * (abi.STATE_DTYPE.itemsize + abi.EXTRA_DTYPE.itemsize)
     hbm, src = measured_peaks()
     K = st["k"].astype(np.int64)
+    traffic = None
+    tp = ROOT / "profiles" / "split_merge_traffic.json"
+    if tp.exists() and R == 4096:
+        try:
+            traffic = json.loads(tp.read_text()).get("bytes_per_launch")
+        except Exception:
+            traffic = None
     cpu = None
     if cpu_seconds > 0:
         cpu = split_merge_cpu_baseline(abi, w, pdf.cpu().numpy(), st0, ex0, cpu_seconds)
@@ -572,7 +579,7 @@ def bench_split_merge(pkg, abi, torch, stream, w, steps: int, warmup: int, clust
            "stat_passes": int(ex["stat_passes"].sum()), "em_iterations": int(ex["em_iterations"].sum()),
            "gpu_launches": steps,
            "roofline": {"bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
-                        "frac": alg / (ms * 1e-3) / 1e9 / hbm, "traffic": None, "peak_source": src,
+                        "frac": alg / (ms * 1e-3) / 1e9 / hbm, "traffic": traffic, "peak_source": src,
                         "algorithmic_bytes_per_launch": alg}}
     ctx.close()
     return out
