@@ -311,6 +311,33 @@ int pg_region_count(const pg_ctx *ctx, uint32_t *out);
 int pg_get_region_aabbs(pg_ctx *ctx, float *host_out, uint32_t count);
 int pg_region_aabbs_device(pg_ctx *ctx, const float **dev_out);
 
+/* Adaptive region splitting (PathGuiding::update's split check and
+ * splitRegion, src/PathGuiding.cpp:290-348; the reference's knobs
+ * splitRegions = false and samplesForRegionSplit = 10000, src/PathGuiding.h:121-122). */
+typedef struct pg_region_split_config {
+    uint32_t enabled;
+    float samples_for_region_split; /* a region splits when its mixture's sample count exceeds this */
+} pg_region_split_config;
+/* The reference's threshold, enabled (the reference leaves it off by default). */
+void pg_default_region_split_config(pg_region_split_config *out);
+/* Sets the context's region splitting (off until set); pg_update then runs
+ * pg_split_regions after each fit, before VMM_Theta packing. */
+int pg_set_region_split(pg_ctx *ctx, const pg_region_split_config *cfg);
+/* The split check over the current regions, in region order: a region whose
+ * mixture has seen more than samples_for_region_split samples (m_numSamples)
+ * is halved along the largest axis of its box (Aabb::splitAabb); it keeps the
+ * lower half and the upper half becomes region n, n+1, ... in that order; both
+ * start from its mixture and split/merge statistics with the sample count and
+ * sample weight decayed by 0.25.  Regions that would exceed the context's
+ * capacity are not created.  Synchronises the stream; *n_regions_out = the new
+ * region count (a split happened if it grew). */
+int pg_split_regions(pg_ctx *ctx, uint32_t *n_regions_out, void *stream);
+/* The region tree the renderer descends: 2 n_regions - 1 nodes; a node >= 0
+ * is an inner node whose children are nodes v and v + 1 (lower half first,
+ * the midpoint split of the node's box along its largest axis), a node < 0 is
+ * the leaf of region -v - 1.  Node 0 is the padded scene box. */
+int pg_get_region_tree(pg_ctx *ctx, int32_t *host_nodes, uint32_t capacity, uint32_t *n_nodes_out);
+
 /* SampleCollector::getSortedData (src/SampleCollector.cpp:76-131) on the
  * device: buckets n_records records by region id (flags), stably (equal ids
  * keep their order); INVALID or out-of-range ids are dropped.  offsets_out

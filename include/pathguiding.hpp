@@ -161,6 +161,18 @@ public:
     pg_directional_data *deviceRecords() const { return records_; }
     uint64_t slotCount() const { return slots_; }
     uint32_t regionCount() const { return region_count_; }
+    // After PathGuiding::update split regions (it returned true): bucket by the
+    // new count from then on (the reference recreates its collector then).
+    void setRegionCount(uint32_t regionCount) {
+        if (regionCount == region_count_) return;
+        pg_fit_config cfg;
+        pg_default_fit_config(&cfg);
+        pg_ctx *sorter = nullptr;
+        check(pg_ctx_create(&cfg, regionCount, 0, &sorter));
+        if (sorter_) pg_ctx_destroy(sorter_);
+        sorter_ = sorter;
+        region_count_ = regionCount;
+    }
 
     // getSortedData (src/SampleCollector.cpp:76-131): a host copy of the
     // valid records grouped by region (stable), and regionCount + 1 offsets.
@@ -211,16 +223,19 @@ class PathGuiding {
 public:
     PathGuiding() = default;
     // splitAndMerge: the post-fit split and merge of mixture components
-    // (src/PathGuiding.h:124, on by default there too).
+    // (src/PathGuiding.h:124, on by default there too).  maxRegions: room for
+    // regions created by setSplitRegions (default: no more than splitCount gives).
     PathGuiding(uint32_t splitCount, const Aabb &sceneAabb, bool useParallaxCompensation,
-                cudaStream_t stream = nullptr, uint32_t numInitialComponents = 8, bool splitAndMerge = true)
+                cudaStream_t stream = nullptr, uint32_t numInitialComponents = 8, bool splitAndMerge = true,
+                uint32_t maxRegions = 0)
         : stream_(stream) {
         pg_fit_config cfg;
         pg_default_fit_config(&cfg);
         cfg.use_parallax = useParallaxCompensation ? 1u : 0u;
         cfg.num_initial_components = numInitialComponents;
         if (splitCount > 24) throw Error(PG_ERR_ARG, "splitCount must be <= 24");
-        check(pg_ctx_create(&cfg, 1u << splitCount, 0, &ctx_));
+        const uint32_t cap = maxRegions > (1u << splitCount) ? maxRegions : (1u << splitCount);
+        check(pg_ctx_create(&cfg, cap, 0, &ctx_));
         float box[6];
         sceneAabb.to_array(box);
         check(pg_set_regions(ctx_, splitCount, box, stream_), ctx_);
@@ -240,15 +255,22 @@ public:
     PathGuiding &operator=(const PathGuiding &) = delete;
     ~PathGuiding() { cleanup(); }
 
+    // splitRegions / samplesForRegionSplit (src/PathGuiding.h:121-122; off by
+    // default there and here).
+    void setSplitRegions(bool splitRegions, float samplesForRegionSplit = 10000.0f) {
+        pg_region_split_config rs{splitRegions ? 1u : 0u, samplesForRegionSplit};
+        check(pg_set_region_split(ctx_, &rs), ctx_);
+    }
     // update (src/PathGuiding.cpp:276-312): bucket the collector's records by
     // region, parallax pre-pass, fit (first pass) or stepwise update, split
-    // and merge, lobe distances and VMM_Theta packing, all on the device and
-    // stream-ordered.
-    // Returns whether the tracer must rebind its buffers (regions are never
-    // split here: false).
+    // and merge, lobe distances, the region split check and VMM_Theta packing,
+    // all on the device and stream-ordered (a region split check synchronises).
+    // Returns whether regions were split (the reference's signal to rebind
+    // the tracer's buffers; the collector then needs setRegionCount).
     bool update(SampleCollector &sampleCollector) {
+        const uint32_t before = getRegionCount();
         check(pg_update(ctx_, sampleCollector.deviceRecords(), sampleCollector.slotCount(), nullptr, stream_), ctx_);
-        return false;
+        return getRegionCount() != before;
     }
     uint32_t getRegionCount() const {
         uint32_t n = 0;

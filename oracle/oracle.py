@@ -55,6 +55,10 @@ class Oracle:
         L.pgo_region_aabbs.argtypes = [_U32, _P, _P]
         L.pgo_sort_samples.argtypes = [_P, C.c_uint64, _U32, _P, _P]
         L.pgo_sort_samples.restype = C.c_uint64
+        L.pgo_split_regions.argtypes = [_U32, _U32, C.c_float, _P, _P, _P, _P, _P, _P]
+        L.pgo_split_regions.restype = _U32
+        L.pgo_region_of.argtypes = [_P, _P, _P]
+        L.pgo_region_of.restype = _U32
         L.pgo_postfit_lpmm32.argtypes = [C.POINTER(abi.FitConfig), C.POINTER(abi.SplitMergeConfig), _U32, _P, _P,
                                          _P, _P, _P, _I]
 
@@ -119,6 +123,46 @@ class Oracle:
         self.lib.pgo_postfit_lpmm32(C.byref(cfg), C.byref(sm), offsets.shape[0] - 1, abi.ptr(dirw),
                                     abi.ptr(pdf), abi.ptr(offsets), abi.ptr(st), abi.ptr(ex), threads)
         return st, ex
+
+    def split_regions(self, cap, thr, states, extras, aabbs, nodes, leaf_of, n_nodes):
+        """PathGuiding::update's region split check over all current regions;
+        arrays are grown to `cap` regions and returned with the new counts."""
+        n = states.shape[0]
+        st = np.zeros(cap, dtype=states.dtype)
+        st[:n] = states
+        ex = None
+        if extras is not None:
+            ex = np.zeros(cap, dtype=abi.EXTRA_DTYPE)
+            ex[:n] = extras.view(abi.EXTRA_DTYPE) if extras.dtype != abi.EXTRA_DTYPE else extras
+        bx = np.zeros((cap, 6), dtype=np.float32)
+        bx[:n] = aabbs
+        nd = np.zeros(2 * cap, dtype=np.int32)
+        nd[:n_nodes] = nodes[:n_nodes]
+        lf = np.zeros(cap, dtype=np.uint32)
+        lf[:n] = leaf_of[:n]
+        nn = C.c_uint32(n_nodes)
+        count = self.lib.pgo_split_regions(n, cap, float(thr), abi.ptr(st), abi.ptr(ex) if ex is not None else None,
+                                           abi.ptr(bx), abi.ptr(nd), abi.ptr(lf), C.byref(nn))
+        return (st[:count], ex[:count] if ex is not None else None, bx[:count], nd[:nn.value], lf[:count],
+                int(nn.value))
+
+    def complete_tree(self, split_count):
+        """The region tree of pg_set_regions (breadth first) and each region's leaf."""
+        n = 1 << split_count
+        nodes = np.zeros(2 * n - 1, dtype=np.int32)
+        nodes[:n - 1] = 2 * np.arange(n - 1) + 1
+        nodes[n - 1:] = -np.arange(n, dtype=np.int32) - 1
+        return nodes, (n - 1 + np.arange(n)).astype(np.uint32)
+
+    def region_of(self, root, nodes, points):
+        root = _f32(root)
+        nodes = np.ascontiguousarray(nodes, dtype=np.int32)
+        pts = _f32(points).reshape(-1, 3)
+        out = np.zeros(pts.shape[0], dtype=np.uint32)
+        for i in range(pts.shape[0]):
+            p = np.ascontiguousarray(pts[i])
+            out[i] = self.lib.pgo_region_of(abi.ptr(root), abi.ptr(nodes), abi.ptr(p))
+        return out
 
     def update_distances(self, dirw, dist, offsets, states):
         st = states.copy()
@@ -235,7 +279,8 @@ class PgoScene(C.Structure):
 
 
 class PgoGuide(C.Structure):
-    _fields_ = [("root", C.c_float * 6), ("split_count", _U32), ("vmm", _P), ("use_parallax", C.c_int32)]
+    _fields_ = [("root", C.c_float * 6), ("split_count", _U32), ("nodes", _P), ("vmm", _P),
+                ("use_parallax", C.c_int32)]
 
 
 class TraceOracle:
@@ -301,8 +346,11 @@ class TraceOracle:
         if guide is not None:
             vmm = np.ascontiguousarray(guide["vmm"])
             keep["_vmm"] = vmm
+            nodes = guide.get("nodes")
+            nodes = np.ascontiguousarray(nodes, dtype=np.int32) if nodes is not None else None
             g = PgoGuide((C.c_float * 6)(*[float(x) for x in guide["root"]]), guide["split_count"],
-                         vmm.ctypes.data, int(guide.get("use_parallax", 1)))
+                         nodes.ctypes.data if nodes is not None else None, vmm.ctypes.data,
+                         int(guide.get("use_parallax", 1)))
         self.lib.pgo_render_f64(C.byref(s), C.byref(params), C.byref(g) if g is not None else None, img.ctypes.data,
                                 r0, r1, threads or (os.cpu_count() or 1))
         return img

@@ -1457,3 +1457,72 @@ int pgo_postfit_lpmm32(const pg_fit_config *cfg, const pg_split_merge_config *sm
     for (int t = 0; t < started; ++t) pthread_join(th[t], NULL);
     return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* Region splitting (PathGuiding::update's split check, splitRegion)   */
+/* ------------------------------------------------------------------ */
+
+/* src/PathGuiding.cpp:290-348 with Aabb::splitAabb (src/Shapes.h:32-46):
+ * regions [0, n) in order; one whose m_numSamples exceeds `thr` keeps the
+ * lower half of its box, the upper half becomes the next new region, both
+ * with the mixture (and statistics) whose sample count and weight were
+ * multiplied by 0.25.  The tree: node v >= 0 has children v, v + 1; a node
+ * < 0 is the leaf of region -v - 1; leaf_of maps regions to their leaves.
+ * Stops creating regions at `cap`.  Returns the new region count. */
+uint32_t pgo_split_regions(uint32_t n, uint32_t cap, float thr, pg_region_state *states, pg_region_extra *extras,
+                           float *aabbs, int32_t *nodes, uint32_t *leaf_of, uint32_t *n_nodes) {
+    uint32_t count = n;
+    for (uint32_t r = 0; r < n; ++r) {
+        if (!(states[r].num_samples > thr) || count >= cap) continue;
+        const uint32_t nr = count++;
+        pg_region_state *st = &states[r];
+        st->num_samples = st->num_samples * 0.25f;
+        st->sample_weight = st->sample_weight * 0.25f;
+        states[nr] = *st;
+        if (extras) extras[nr] = extras[r];
+        float *b = aabbs + 6 * (size_t)r, *c = aabbs + 6 * (size_t)nr;
+        float size[3];
+        for (int i = 0; i < 3; ++i) size[i] = b[3 + i] - b[i];
+        const int ax = size[0] > size[1] ? (size[0] > size[2] ? 0 : 2) : (size[1] > size[2] ? 1 : 2);
+        for (int i = 0; i < 6; ++i) c[i] = b[i];
+        b[3 + ax] -= 0.5f * size[ax];
+        c[ax] += 0.5f * size[ax];
+        const uint32_t a = *n_nodes;
+        *n_nodes += 2;
+        nodes[leaf_of[r]] = (int32_t)a;
+        nodes[a] = -(int32_t)r - 1;
+        nodes[a + 1] = -(int32_t)nr - 1;
+        leaf_of[r] = a;
+        leaf_of[nr] = a + 1;
+    }
+    return count;
+}
+
+/* Point -> region by descending the tree from the padded scene box (the
+ * region boxes' midpoint rule); PG_INVALID_REGION outside it or in a rounding
+ * gap between halves. */
+uint32_t pgo_region_of(const float root[6], const int32_t *nodes, const float p[3]) {
+    float lo[3] = {root[0], root[1], root[2]}, hi[3] = {root[3], root[4], root[5]};
+    for (int i = 0; i < 3; ++i)
+        if (!(p[i] >= lo[i] && p[i] <= hi[i])) return PG_INVALID_REGION;
+    int32_t node = 0;
+    for (int depth = 0; depth < 64; ++depth) {
+        const int32_t v = nodes[node];
+        if (v < 0) return (uint32_t)(-(v + 1));
+        float size[3];
+        for (int i = 0; i < 3; ++i) size[i] = hi[i] - lo[i];
+        const int ax = size[0] > size[1] ? (size[0] > size[2] ? 0 : 2) : (size[1] > size[2] ? 1 : 2);
+        const float lhi = hi[ax] - 0.5f * size[ax];
+        const float rlo = lo[ax] + 0.5f * size[ax];
+        if (p[ax] <= lhi) {
+            hi[ax] = lhi;
+            node = v;
+        } else if (p[ax] >= rlo) {
+            lo[ax] = rlo;
+            node = v + 1;
+        } else {
+            return PG_INVALID_REGION;
+        }
+    }
+    return PG_INVALID_REGION;
+}

@@ -60,6 +60,16 @@ int pgo_postfit_lpmm32(const pg_fit_config *cfg, const pg_split_merge_config *sm
                        const float *dirw, const float *pdf, const uint32_t *offsets, pg_region_state *states,
                        pg_region_extra *extras, int n_threads);
 
+/* PathGuiding::update's region split check and splitRegion
+ * (src/PathGuiding.cpp:290-348, Aabb::splitAabb src/Shapes.h:32-46) over
+ * regions [0, n); returns the new region count (at most cap).  nodes /
+ * leaf_of / n_nodes: the region tree (node v >= 0: children v, v + 1; v < 0:
+ * leaf of region -v - 1). */
+uint32_t pgo_split_regions(uint32_t n, uint32_t cap, float thr, pg_region_state *states, pg_region_extra *extras,
+                           float *aabbs, int32_t *nodes, uint32_t *leaf_of, uint32_t *n_nodes);
+/* Point -> region by descent of that tree from the padded scene box. */
+uint32_t pgo_region_of(const float root[6], const int32_t *nodes, const float p[3]);
+
 /* lightpmm fastexp (pmm-vcl.h:158-184), scalar restatement. */
 float pgo_fastexp(float x);
 

@@ -2,6 +2,7 @@
 // Compiled with -ffp-contract=off: every FP32 operation of the traversal twin
 // rounds exactly where the device code's explicit _rn intrinsics round.
 #include "pg_oracle_trace.h"
+#include "pg_oracle.h"
 
 #include <math.h>
 #include <pthread.h>
@@ -485,6 +486,7 @@ D3 sample_bsdf(const pg_material &m, D3 d, D3 n, double u1, double u2) {
 uint32_t region_of(const pgo_guide &g, D3 p) {
     float lo[3] = {g.root[0], g.root[1], g.root[2]}, hi[3] = {g.root[3], g.root[4], g.root[5]};
     const float pp[3] = {(float)p.x, (float)p.y, (float)p.z};
+    if (g.nodes) return pgo_region_of(g.root, g.nodes, pp);
     for (int i = 0; i < 3; ++i)
         if (!(pp[i] >= lo[i] && pp[i] <= hi[i])) return PG_INVALID_REGION;
     uint32_t id = 0;

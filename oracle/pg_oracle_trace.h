@@ -39,6 +39,7 @@ typedef struct pgo_scene {
 typedef struct pgo_guide {
     float root[6];
     uint32_t split_count;
+    const int32_t *nodes; /* the region tree after region splits, or NULL (complete tree) */
     const pg_vmm_theta *vmm;
     int32_t use_parallax;
 } pgo_guide;

@@ -59,6 +59,10 @@ SIGNATURES = {
     "pg_split_merge": (_I, [_P, _P, _P, _P, _U32, _P]),
     "pg_get_region_extra": (_I, [_P, _P, _U32]),
     "pg_set_region_extra": (_I, [_P, _P, _U32]),
+    "pg_default_region_split_config": (None, [C.POINTER(abi.RegionSplitConfig)]),
+    "pg_set_region_split": (_I, [_P, C.POINTER(abi.RegionSplitConfig)]),
+    "pg_split_regions": (_I, [_P, C.POINTER(_U32), _P]),
+    "pg_get_region_tree": (_I, [_P, _P, _U32, C.POINTER(_U32)]),
     "pg_mlp_default_config": (None, [C.POINTER(abi.MlpConfig)]),
     "pg_mlp_create": (_I, [C.POINTER(abi.MlpConfig), C.POINTER(_P)]),
     "pg_mlp_destroy": (_I, [_P]),
@@ -287,6 +291,27 @@ class FitContext:
     def extras(self, n: int) -> np.ndarray:
         out = np.zeros(n, dtype=abi.EXTRA_DTYPE)
         self._check(self.lib.pg_get_region_extra(self.h, out.ctypes.data, n))
+        return out
+
+    # ---- region splitting (PathGuiding::update's split check) ----
+    def set_region_split(self, cfg: abi.RegionSplitConfig | None = None):
+        """Turns region splitting on with `cfg` (the reference's threshold when
+        None); pg_update then splits regions after each fit."""
+        c = cfg if cfg is not None else abi.default_region_split_config()
+        self._check(self.lib.pg_set_region_split(self.h, C.byref(c)))
+
+    def split_regions(self, stream=None) -> int:
+        """One split check over the current regions; returns the region count."""
+        n = C.c_uint32()
+        self._check(self.lib.pg_split_regions(self.h, C.byref(n), _stream_handle(stream)))
+        return int(n.value)
+
+    def region_tree(self) -> np.ndarray:
+        """The region tree (node v >= 0: children v, v + 1; v < 0: leaf of region -v - 1)."""
+        n = C.c_uint32()
+        self._check(self.lib.pg_get_region_tree(self.h, None, 0, C.byref(n)))
+        out = np.zeros(n.value, dtype=np.int32)
+        self._check(self.lib.pg_get_region_tree(self.h, out.ctypes.data, n.value, C.byref(n)))
         return out
 
     def set_extras(self, extras: np.ndarray):

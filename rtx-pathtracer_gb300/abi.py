@@ -115,6 +115,18 @@ class SplitMergeConfig(C.Structure):
                 ("cluster_threshold", C.c_uint32), ("cluster_size", C.c_uint32)]
 
 
+class RegionSplitConfig(C.Structure):
+    _fields_ = [("enabled", C.c_uint32), ("samples_for_region_split", C.c_float)]
+
+
+def default_region_split_config(**kw) -> RegionSplitConfig:
+    """The reference's threshold (src/PathGuiding.h:122), enabled."""
+    c = RegionSplitConfig(1, 10000.0)
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
 def default_split_merge_config(**kw) -> SplitMergeConfig:
     """The reference's knobs (src/PathGuiding.h:124-129), enabled."""
     c = SplitMergeConfig(1, 8192, 4096, 4096, 0.5, 0.025, 0, 0)

@@ -57,7 +57,7 @@ bool write_pfm(const std::string &path, const std::vector<float> &rgb, uint32_t 
 int usage() {
     fprintf(stderr, "Required parameters: WIDTH HEIGHT IC_SIZE GUIDING_SPLITS SCENE [--spp N] [--train LIST] "
                     "[--depth N] [--seed N] [--prob P] [--no-guiding] [--no-parallax] [--no-split-merge] "
-                    "[--out FILE]\n");
+                    "[--split-regions SAMPLES] [--out FILE]\n");
     return EXIT_FAILURE;
 }
 
@@ -71,6 +71,7 @@ int main(int argc, char **argv) {
     uint32_t spp = 64, depth = 10, seed = 1;
     float prob = 0.5f;
     bool guiding = true, parallax = true, split_merge = true;
+    float split_regions = 0.0f;  // samplesForRegionSplit; 0: regions are not split (the reference's default)
     std::vector<uint32_t> train = {1, 2, 4, 8, 16, 32};
     std::string out;
     for (int i = 6; i < argc; ++i) {
@@ -84,6 +85,7 @@ int main(int argc, char **argv) {
         else if (a == "--no-guiding") guiding = false;
         else if (a == "--no-parallax") parallax = false;
         else if (a == "--no-split-merge") split_merge = false;
+        else if (a == "--split-regions") split_regions = strtof(next(), nullptr);
         else if (a == "--out") out = next();
         else return usage();
     }
@@ -105,16 +107,22 @@ int main(int argc, char **argv) {
         cudaEventCreate(&e2);
         uint32_t total = 0;
         uint64_t sorted_records = 0, regions_with_samples = 0;
+        uint32_t regions = 0;
         cudaEventRecord(e0, stream);
         if (guiding) {
-            pg::PathGuiding pg(splits, scene.getSceneSize(), parallax, stream, 8, split_merge);
+            // room for 4x the initial regions when regions may split
+            pg::PathGuiding pg(splits, scene.getSceneSize(), parallax, stream, 8, split_merge,
+                               split_regions > 0.0f ? 4u << splits : 0u);
+            if (split_regions > 0.0f) pg.setSplitRegions(true, split_regions);
             pg::SampleCollector collector(pg.getRegionCount(), W, H, stream);
             for (size_t f = 0; f < train.size(); ++f) {
                 tracer.render(pg::render_params(train[f], depth, seed + 1000u * (uint32_t)(f + 1), f > 0, true, prob),
                               image, &pg, &collector);
-                pg.update(collector);
+                // RayTracingApp rebuilds its buffers when update reports split regions
+                if (pg.update(collector)) collector.setRegionCount(pg.getRegionCount());
                 total += train[f];
             }
+            regions = pg.getRegionCount();
             cudaEventRecord(e1, stream);
             tracer.render(pg::render_params(spp, depth, seed, true, false, prob), image, &pg);
             total += spp;
@@ -151,9 +159,9 @@ int main(int argc, char **argv) {
         }
         printf("{\"scene\": \"%s\", \"width\": %u, \"height\": %u, \"guiding\": %s, \"spp\": %u, "
                "\"train_ms\": %.3f, \"render_ms\": %.3f, \"mean\": %.9g, \"sorted_records\": %llu, "
-               "\"regions_with_samples\": %llu}\n",
+               "\"regions_with_samples\": %llu, \"regions\": %u}\n",
                scene_arg.c_str(), W, H, guiding ? "true" : "false", total, train_ms, render_ms, mean,
-               (unsigned long long)sorted_records, (unsigned long long)regions_with_samples);
+               (unsigned long long)sorted_records, (unsigned long long)regions_with_samples, regions);
         cudaFree(image);
         cudaStreamDestroy(stream);
     } catch (const pg::Error &e) {

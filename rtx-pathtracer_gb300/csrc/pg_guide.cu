@@ -423,6 +423,67 @@ __global__ void pack_vmm_theta_kernel(const pg_region_state *states, uint32_t n_
     }
 }
 
+// PathGuiding::update's split check and splitRegion (src/PathGuiding.cpp:290-348)
+// over regions [0, R), one CTA: regions above the threshold are ranked in
+// region order by a block scan, the k-th becomes region R + k and takes nodes
+// n_nodes + 2k, n_nodes + 2k + 1.  out = {new region count, new node count}.
+__global__ void __launch_bounds__(1024) split_regions_kernel(pg_region_state *states, pg_region_extra *extras,
+                                                             float *aabbs, int32_t *nodes, uint32_t *leaf_of,
+                                                             uint32_t R, uint32_t n_nodes, uint32_t cap, float thr,
+                                                             uint32_t *out) {
+    __shared__ uint32_t warp_tot[32];
+    __shared__ uint32_t base;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    if (tid == 0) base = 0;
+    __syncthreads();
+    for (uint32_t c0 = 0; c0 < R; c0 += 1024u) {
+        const uint32_t r = c0 + tid;
+        const bool flag = r < R && states[r].num_samples > thr;
+        const uint32_t bal = __ballot_sync(0xffffffffu, flag);
+        if (lane == 0) warp_tot[warp] = __popc(bal);
+        __syncthreads();
+        uint32_t before = 0, total = 0;
+        for (uint32_t w = 0; w < 32u; ++w) {
+            const uint32_t t = warp_tot[w];
+            before += w < warp ? t : 0u;
+            total += t;
+        }
+        const uint32_t rank = base + before + __popc(bal & ((1u << lane) - 1u));
+        if (flag && R + rank < cap) {
+            const uint32_t nr = R + rank, a = n_nodes + 2u * rank;
+            pg_region_state &st = states[r];
+            st.num_samples = __fmul_rn(st.num_samples, 0.25f);  // decayTerm
+            st.sample_weight = __fmul_rn(st.sample_weight, 0.25f);
+            states[nr] = st;
+            if (extras) extras[nr] = extras[r];
+            // Aabb::splitAabb (src/Shapes.h:32-46): the lower half stays, the upper half is new
+            float *b = aabbs + 6 * (size_t)r, *c = aabbs + 6 * (size_t)nr;
+            float size[3];
+            for (int i = 0; i < 3; ++i) size[i] = __fsub_rn(b[3 + i], b[i]);
+            const int ax = size[0] > size[1] ? (size[0] > size[2] ? 0 : 2) : (size[1] > size[2] ? 1 : 2);
+            for (int i = 0; i < 6; ++i) c[i] = b[i];
+            const float half = __fmul_rn(0.5f, size[ax]);
+            b[3 + ax] = __fsub_rn(b[3 + ax], half);
+            c[ax] = __fadd_rn(c[ax], half);
+            const uint32_t leaf = leaf_of[r];
+            nodes[leaf] = (int32_t)a;
+            nodes[a] = -(int32_t)r - 1;
+            nodes[a + 1] = -(int32_t)nr - 1;
+            leaf_of[r] = a;
+            leaf_of[nr] = a + 1;
+        }
+        __syncthreads();
+        if (tid == 0) base += total;
+        __syncthreads();
+    }
+    if (tid == 0) {
+        const uint32_t room = cap > R ? cap - R : 0u;
+        const uint32_t n = base < room ? base : room;
+        out[0] = R + n;
+        out[1] = n_nodes + 2u * n;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Host helpers
 // ---------------------------------------------------------------------------
@@ -488,6 +549,13 @@ struct GuideScratch {
     pg_vmm_theta *vmm = nullptr;   // packed mixtures for the renderer
     bool vmm_fresh = false;
     float root[6] = {0, 0, 0, 0, 0, 0};
+    // region tree (2 n - 1 nodes; see pg_get_region_tree) and each region's leaf
+    int32_t *nodes = nullptr;
+    uint32_t *leaf_of = nullptr;
+    uint32_t n_nodes = 0;
+    bool tree_split = false;       // a region was split: the renderer descends the node array
+    uint32_t *split_out = nullptr; // device: new region and node counts
+    pg_region_split_config rs{};
 };
 
 static GuideScratch &guide(pg_ctx *ctx) {
@@ -512,6 +580,9 @@ void guide_release(pg_ctx *ctx) {
     cudaFree(g.means);
     cudaFree(g.aabbs);
     cudaFree(g.vmm);
+    cudaFree(g.nodes);
+    cudaFree(g.leaf_of);
+    cudaFree(g.split_out);
     delete static_cast<GuideScratch *>(ctx->guide);
     ctx->guide = nullptr;
 }
@@ -612,6 +683,7 @@ int guide_view(pg_ctx *ctx, GuideView *out, cudaStream_t s) {
     }
     for (int i = 0; i < 6; ++i) out->root[i] = g.root[i];
     out->split_count = g.split_count;
+    out->nodes = g.tree_split ? g.nodes : nullptr;
     out->n_regions = g.n_regions;
     out->vmm = g.vmm;
     out->use_parallax = ctx->cfg.use_parallax ? 1 : 0;
@@ -630,15 +702,28 @@ int pg_set_regions(pg_ctx *ctx, uint32_t split_count, const float scene_aabb[6],
     std::vector<float> boxes;
     region_boxes(split_count, scene_aabb, boxes);
     cudaStream_t s = (cudaStream_t)stream;
-    if (g.n_regions < n || !g.aabbs) {
-        cudaFree(g.aabbs);
-        cudaFree(g.means);
-        g.aabbs = g.means = nullptr;
-        int st = check_cuda(ctx, cudaMalloc(&g.aabbs, sizeof(float) * 6 * n), "region boxes");
-        if (!st) st = check_cuda(ctx, cudaMalloc(&g.means, sizeof(float) * 3 * n), "region means");
+    // boxes, means, packed mixtures and the tree for the context's capacity:
+    // regions may be split later (pg_split_regions)
+    const uint32_t cap = ctx->max_regions;
+    if (!g.aabbs) {
+        int st = check_cuda(ctx, cudaMalloc(&g.aabbs, sizeof(float) * 6 * cap), "region boxes");
+        if (!st) st = check_cuda(ctx, cudaMalloc(&g.means, sizeof(float) * 3 * cap), "region means");
+        if (!st) st = check_cuda(ctx, cudaMalloc(&g.nodes, sizeof(int32_t) * (2 * (size_t)cap)), "region tree");
+        if (!st) st = check_cuda(ctx, cudaMalloc(&g.leaf_of, sizeof(uint32_t) * cap), "region leaves");
+        if (!st) st = check_cuda(ctx, cudaMalloc(&g.split_out, sizeof(uint32_t) * 2), "split counts");
         if (st) return st;
     }
+    // the complete tree in breadth-first order: inner node k has children 2k+1, 2k+2
+    std::vector<int32_t> nodes(2 * (size_t)n - 1);
+    std::vector<uint32_t> leaf_of(n);
+    for (uint32_t k = 0; k + 1 < n; ++k) nodes[k] = (int32_t)(2 * k + 1);
+    for (uint32_t r = 0; r < n; ++r) {
+        nodes[n - 1 + r] = -(int32_t)r - 1;
+        leaf_of[r] = n - 1 + r;
+    }
     g.n_regions = n;
+    g.n_nodes = 2 * n - 1;
+    g.tree_split = false;
     g.split_count = split_count;
     g.fitted = false;
     g.vmm_fresh = false;
@@ -648,14 +733,18 @@ int pg_set_regions(pg_ctx *ctx, uint32_t split_count, const float scene_aabb[6],
         g.root[i] = cen - 0.50001f * ext;
         g.root[3 + i] = cen + 0.50001f * ext;
     }
-    cudaFree(g.vmm);
-    g.vmm = nullptr;
-    {
-        int st0 = check_cuda(ctx, cudaMalloc(&g.vmm, sizeof(pg_vmm_theta) * n), "packed mixtures");
+    if (!g.vmm) {
+        int st0 = check_cuda(ctx, cudaMalloc(&g.vmm, sizeof(pg_vmm_theta) * cap), "packed mixtures");
         if (st0) return st0;
     }
     int st = check_cuda(ctx, cudaMemcpyAsync(g.aabbs, boxes.data(), sizeof(float) * 6 * n, cudaMemcpyHostToDevice, s),
                         "region boxes upload");
+    if (!st)
+        st = check_cuda(ctx, cudaMemcpyAsync(g.nodes, nodes.data(), sizeof(int32_t) * nodes.size(),
+                                             cudaMemcpyHostToDevice, s), "region tree upload");
+    if (!st)
+        st = check_cuda(ctx, cudaMemcpyAsync(g.leaf_of, leaf_of.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s),
+                        "region leaves upload");
     if (!st) st = check_cuda(ctx, cudaStreamSynchronize(s), "region boxes sync");
     if (st) return st;
     return pg_init_regions(ctx, n, stream);
@@ -793,13 +882,66 @@ int pg_update(pg_ctx *ctx, const pg_directional_data *records, uint64_t n_record
         if (st) return st;
     }
     g.fitted = true;
-    // 5. VMM_Theta for the tracer (the context's copy, and the caller's if asked)
-    st = pg_pack_vmm_theta(ctx, R, g.vmm, stream);
+    // 5. the split check of PathGuiding::update (src/PathGuiding.cpp:290-300)
+    uint32_t R_out = R;
+    if (g.rs.enabled) {
+        st = pg_split_regions(ctx, &R_out, stream);
+        if (st) return st;
+    }
+    // 6. VMM_Theta for the tracer (the context's copy, and the caller's if asked)
+    st = pg_pack_vmm_theta(ctx, R_out, g.vmm, stream);
     if (st) return st;
     g.vmm_fresh = true;
-    if (vmm_out) st = check_cuda(ctx, cudaMemcpyAsync(vmm_out, g.vmm, sizeof(pg_vmm_theta) * R,
+    if (vmm_out) st = check_cuda(ctx, cudaMemcpyAsync(vmm_out, g.vmm, sizeof(pg_vmm_theta) * R_out,
                                                       cudaMemcpyDeviceToDevice, s), "VMM_Theta copy");
     return st;
+}
+
+void pg_default_region_split_config(pg_region_split_config *out) {
+    if (!out) return;
+    out->enabled = 1;
+    out->samples_for_region_split = 10000.0f;
+}
+
+int pg_set_region_split(pg_ctx *ctx, const pg_region_split_config *cfg) {
+    if (!ctx || !cfg) return PG_ERR_ARG;
+    guide(ctx).rs = *cfg;
+    return PG_OK;
+}
+
+int pg_split_regions(pg_ctx *ctx, uint32_t *n_regions_out, void *stream) {
+    if (!ctx) return PG_ERR_ARG;
+    GuideScratch &g = guide(ctx);
+    if (!g.aabbs || g.n_regions == 0) return set_error(ctx, PG_ERR_STATE, "pg_set_regions must run first");
+    cudaStream_t s = (cudaStream_t)stream;
+    const float thr = g.rs.samples_for_region_split > 0.0f ? g.rs.samples_for_region_split : 10000.0f;
+    split_regions_kernel<<<1, 1024, 0, s>>>(ctx->d_states, ctx->d_extras, g.aabbs, g.nodes, g.leaf_of, g.n_regions,
+                                            g.n_nodes, ctx->max_regions, thr, g.split_out);
+    int st = check_cuda(ctx, cudaGetLastError(), "region split launch");
+    uint32_t h[2] = {0, 0};
+    if (!st)
+        st = check_cuda(ctx, cudaMemcpyAsync(h, g.split_out, sizeof h, cudaMemcpyDeviceToHost, s), "split counts");
+    if (!st) st = check_cuda(ctx, cudaStreamSynchronize(s), "region split sync");
+    if (st) return st;
+    if (h[0] != g.n_regions) {
+        g.n_regions = h[0];
+        g.n_nodes = h[1];
+        g.tree_split = true;
+        g.vmm_fresh = false;
+    }
+    if (n_regions_out) *n_regions_out = g.n_regions;
+    return PG_OK;
+}
+
+int pg_get_region_tree(pg_ctx *ctx, int32_t *host_nodes, uint32_t capacity, uint32_t *n_nodes_out) {
+    if (!ctx || (!host_nodes && capacity)) return PG_ERR_ARG;
+    GuideScratch &g = guide(ctx);
+    if (!g.nodes || g.n_regions == 0) return set_error(ctx, PG_ERR_STATE, "pg_set_regions must run first");
+    if (n_nodes_out) *n_nodes_out = g.n_nodes;
+    if (!host_nodes) return PG_OK;
+    if (capacity < g.n_nodes) return set_error(ctx, PG_ERR_ARG, "capacity below the node count");
+    return check_cuda(ctx, cudaMemcpy(host_nodes, g.nodes, sizeof(int32_t) * g.n_nodes, cudaMemcpyDeviceToHost),
+                      "region tree download");
 }
 
 }  // extern "C"

@@ -64,6 +64,7 @@ int extras_reset(pg_ctx *ctx, uint32_t first, uint32_t n, cudaStream_t s);
 struct GuideView {
     float root[6];
     uint32_t split_count;
+    const int32_t *nodes;  // the region tree once a region was split (else null: complete tree)
     uint32_t n_regions;
     const pg_vmm_theta *vmm;
     int use_parallax;

@@ -188,13 +188,36 @@ __device__ __forceinline__ V sample_bsdf(const pg_material &m, V d, V n, float u
 struct DevGuide {
     float root[6];
     uint32_t split_count;
+    const int32_t *nodes;  // the region tree after region splits (null: the complete tree)
     const pg_vmm_theta *vmm;
     int use_parallax;
 };
 
 // Point -> region by descending the midpoint split tree with the same float
 // arithmetic that built it; points outside the root box (or in a rounding gap)
-// have no region (getGuidingRegion returns -1, raytrace.rgen:904-921).
+// have no region (getGuidingRegion returns -1, raytrace.rgen:904-921).  The
+// levels of pg_set_regions' complete tree are descended by arithmetic alone;
+// once regions were split, the descent continues from that level's leaf
+// through the node array (inner node v: children v, v + 1), so a region that
+// was never split costs one load.
+__device__ __forceinline__ bool descend_level(float lo[3], float hi[3], const float pp[3], int &side) {
+    float size[3];
+    for (int i = 0; i < 3; ++i) size[i] = __fsub_rn(hi[i], lo[i]);
+    const int ax = size[0] > size[1] ? (size[0] > size[2] ? 0 : 2) : (size[1] > size[2] ? 1 : 2);
+    const float lhi = __fsub_rn(hi[ax], __fmul_rn(0.5f, size[ax]));
+    const float rlo = __fadd_rn(lo[ax], __fmul_rn(0.5f, size[ax]));
+    if (pp[ax] <= lhi) {
+        hi[ax] = lhi;
+        side = 0;
+    } else if (pp[ax] >= rlo) {
+        lo[ax] = rlo;
+        side = 1;
+    } else {
+        return false;
+    }
+    return true;
+}
+
 __device__ __forceinline__ uint32_t region_of(const DevGuide &g, V p) {
     float lo[3] = {g.root[0], g.root[1], g.root[2]}, hi[3] = {g.root[3], g.root[4], g.root[5]};
     const float pp[3] = {p.x, p.y, p.z};
@@ -202,22 +225,20 @@ __device__ __forceinline__ uint32_t region_of(const DevGuide &g, V p) {
         if (!(pp[i] >= lo[i] && pp[i] <= hi[i])) return PG_INVALID_REGION;
     uint32_t id = 0;
     for (uint32_t l = 0; l < g.split_count; ++l) {
-        float size[3];
-        for (int i = 0; i < 3; ++i) size[i] = __fsub_rn(hi[i], lo[i]);
-        const int ax = size[0] > size[1] ? (size[0] > size[2] ? 0 : 2) : (size[1] > size[2] ? 1 : 2);
-        const float lhi = __fsub_rn(hi[ax], __fmul_rn(0.5f, size[ax]));
-        const float rlo = __fadd_rn(lo[ax], __fmul_rn(0.5f, size[ax]));
-        if (pp[ax] <= lhi) {
-            hi[ax] = lhi;
-            id = 2u * id;
-        } else if (pp[ax] >= rlo) {
-            lo[ax] = rlo;
-            id = 2u * id + 1u;
-        } else {
-            return PG_INVALID_REGION;
-        }
+        int side;
+        if (!descend_level(lo, hi, pp, side)) return PG_INVALID_REGION;
+        id = 2u * id + (uint32_t)side;
     }
-    return id;
+    if (!g.nodes) return id;
+    int32_t node = (int32_t)((1u << g.split_count) - 1u + id);
+    for (int depth = 0; depth < 64; ++depth) {
+        const int32_t v = __ldg(g.nodes + node);
+        if (v < 0) return (uint32_t)(-(v + 1));
+        int side;
+        if (!descend_level(lo, hi, pp, side)) return PG_INVALID_REGION;
+        node = v + side;
+    }
+    return PG_INVALID_REGION;
 }
 
 __device__ __forceinline__ V lobe_mu(const pg_vmf_theta &t, V x, int par) {
@@ -1255,6 +1276,7 @@ int pg_render(pg_scene *sc, const pg_render_params *rp, pg_ctx *guide, float *im
         if (st) return scene_error(st, pg_last_error(guide));
         for (int i = 0; i < 6; ++i) R.guide.root[i] = gv.root[i];
         R.guide.split_count = gv.split_count;
+        R.guide.nodes = gv.nodes;
         R.guide.vmm = gv.vmm;
         R.guide.use_parallax = gv.use_parallax;
     }

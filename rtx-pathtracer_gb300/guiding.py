@@ -44,7 +44,7 @@ class SampleCollector:
         region (stable), with regionCount + 1 offsets; INVALID records are
         dropped.  Returns (records as a structured array, offsets)."""
         torch = _torch()
-        R = self.region_count
+        R = guiding.get_region_count()  # regions may have been split since construction
         out = torch.empty(self.n_slots * RECORD_BYTES, dtype=torch.uint8, device="cuda")
         offs = torch.empty(R + 1, dtype=torch.int32, device="cuda")
         guiding.ctx.sort_samples(self.buffer, self.n_slots, R, out, offs, stream=stream)
@@ -62,16 +62,19 @@ class PathGuiding:
     reference's splitAndMerge (src/PathGuiding.h:124)."""
 
     def __init__(self, split_count: int, scene_aabb, use_parallax: bool = True, cfg: "abi.FitConfig | None" = None,
-                 stream=None, split_and_merge: "bool | abi.SplitMergeConfig" = True):
+                 stream=None, split_and_merge: "bool | abi.SplitMergeConfig" = True, split_regions: bool = False,
+                 samples_for_region_split: float = 10000.0, max_regions: int | None = None):
         cfg = cfg if cfg is not None else abi.default_fit_config()
         cfg.use_parallax = 1 if use_parallax else 0
         self.split_count = split_count
-        self.ctx = FitContext(cfg, max_regions=1 << split_count)
+        self.ctx = FitContext(cfg, max_regions=max(max_regions or 0, 1 << split_count))
         self.ctx.set_regions(split_count, np.asarray(scene_aabb, dtype=np.float32), stream=stream)
         if isinstance(split_and_merge, abi.SplitMergeConfig):
             self.ctx.set_split_merge(split_and_merge)
         elif split_and_merge:
             self.ctx.set_split_merge()
+        if split_regions:  # splitRegions / samplesForRegionSplit (src/PathGuiding.h:121-122), off by default
+            self.ctx.set_region_split(abi.default_region_split_config(samples_for_region_split=samples_for_region_split))
 
     def get_region_count(self) -> int:
         return self.ctx.region_count()
@@ -79,10 +82,11 @@ class PathGuiding:
     def update(self, collector: SampleCollector, stream=None) -> bool:
         """One guiding pass over the collector's records (bucket, parallax
         pre-pass, fit or stepwise update, split and merge, distances, VMM_Theta).  Returns
-        whether the tracer must rebind its region buffers; regions are never
-        re-split here, so always False."""
+        whether a region was split (the reference's signal to rebind the
+        tracer's region buffers; here the tracer picks the new tree up itself)."""
+        before = self.ctx.region_count()
         self.ctx.update(collector.buffer, collector.n_slots, stream=stream)
-        return False
+        return self.ctx.region_count() != before
 
     def close(self):
         self.ctx.close()

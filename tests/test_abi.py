@@ -90,7 +90,7 @@ def test_ctypes_mirrors_match_the_header(abi):
                ("pg_cornell_params", abi.CornellParams), ("pg_plates_params", abi.PlatesParams),
                ("pg_scene_info", abi.SceneInfo), ("pg_render_params", abi.RenderParams),
                ("pg_render_stats", abi.RenderStats), ("pg_mlp_config", abi.MlpConfig),
-               ("pg_split_merge_config", abi.SplitMergeConfig)]
+               ("pg_split_merge_config", abi.SplitMergeConfig), ("pg_region_split_config", abi.RegionSplitConfig)]
     dtypes = [("pg_region_state", abi.STATE_DTYPE), ("pg_vmm_theta", abi.VMM_THETA_DTYPE),
               ("pg_vmf_theta", abi.VMF_THETA_DTYPE), ("pg_material", abi.MATERIAL_DTYPE),
               ("pg_sphere", abi.SPHERE_DTYPE), ("pg_ray", abi.RAY_DTYPE), ("pg_hit", abi.HIT_DTYPE),

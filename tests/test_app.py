@@ -49,11 +49,13 @@ def test_usage_and_scene_errors(exe, tmp_path):
 def test_guided_and_plain_renders(exe, tmp_path, cuda, pkg, abi):
     W, H = 96, 54
     out = {}
-    for mode in ("guided", "plain"):
+    for mode in ("guided", "plain", "split"):
         pfm = tmp_path / f"{mode}.pfm"
         args = [str(exe), str(W), str(H), "0", "8", "cornell", "--spp", "256", "--out", str(pfm)]
         if mode == "plain":
             args.append("--no-guiding")
+        if mode == "split":  # region splitting at a threshold the training passes reach
+            args += ["--split-regions", "400"]
         r = subprocess.run(args, capture_output=True, text=True, timeout=300)
         assert r.returncode == 0, r.stderr
         info = json.loads(r.stdout.strip().splitlines()[-1])
@@ -63,10 +65,11 @@ def test_guided_and_plain_renders(exe, tmp_path, cuda, pkg, abi):
         assert abs(img.mean() - info["mean"]) < 1e-6 * max(1.0, info["mean"])
         out[mode] = (img, info)
     assert out["guided"][1]["sorted_records"] > 0 and out["guided"][1]["regions_with_samples"] > 0
+    assert out["guided"][1]["regions"] == 256 and out["split"][1]["regions"] > 256
     torch = cuda
     sc = pkg.Scene.cornell(W, H)
     img = torch.zeros(W * H * 3, dtype=torch.float32, device="cuda")
     sc.render(abi.render_params(spp=1024, max_depth=10, seed=99), img)
     ref = img.cpu().numpy().reshape(H, W, 3) / 1024
-    for mode in ("guided", "plain"):
+    for mode in ("guided", "plain", "split"):
         assert abs(out[mode][0].mean() - ref.mean()) / ref.mean() < 0.03, mode
