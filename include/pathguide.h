@@ -381,15 +381,30 @@ int pg_update(pg_ctx *ctx, const pg_directional_data *records, uint64_t n_record
  * shaders/raytrace.rgen:21-27.  PG_MAT_GGX is a GGX microfacet conductor; it
  * takes the place of the reference's Beckmann MAT_ROUGH_CONDUCTOR
  * (raytrace.rgen:222-236). */
-enum { PG_MAT_DIFFUSE = 0, PG_MAT_SPECULAR = 1, PG_MAT_DIELECTRIC = 2, PG_MAT_LIGHT = 3, PG_MAT_GGX = 6 };
+/* Material types: the reference's EMatType (src/SceneLoader.h:31-39) - diffuse,
+ * specular, dielectric, light, Phong, conductor - plus GGX (the project's
+ * glossy lobe) and the reference's Beckmann rough conductor. */
+enum {
+    PG_MAT_DIFFUSE = 0,
+    PG_MAT_SPECULAR = 1,
+    PG_MAT_DIELECTRIC = 2,
+    PG_MAT_LIGHT = 3,
+    PG_MAT_PHONG = 4,
+    PG_MAT_CONDUCTOR = 5,
+    PG_MAT_GGX = 6,
+    PG_MAT_BECKMANN = 7
+};
 
 typedef struct pg_material {
     int32_t type;
-    float albedo[3];    /* diffuse reflectance; specular / GGX tint (Fresnel F0) */
+    float albedo[3];    /* diffuse reflectance (diffuse, Phong); specular / GGX tint (Fresnel F0) */
     float emission[3];  /* radiance of a light (lightColor) */
-    float roughness;    /* GGX alpha */
-    float ior;          /* dielectric index of refraction */
-    int32_t reserved[3];
+    float roughness;    /* GGX and Beckmann alpha */
+    float ior;          /* dielectric index of refraction (intIOR / extIOR) */
+    float specular[3];  /* Phong specular reflectance */
+    float exponent;     /* Phong exponent (specularHighlight) */
+    float eta, k;       /* conductor and Beckmann conductor: Fresnel eta and k (one spectrum value) */
+    int32_t reserved;
 } pg_material;
 
 typedef struct pg_sphere {

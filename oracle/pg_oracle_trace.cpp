@@ -436,6 +436,31 @@ double fresnel(double eta, double ci) {
     return 0.5 * (rs * rs + rp * rp);
 }
 
+// Fresnel of a conductor (raytrace.rgen:163-176), one spectrum value of eta and k
+double fresnel_conductor(double ci, double eta, double k) {
+    ci = fabs(ci);
+    const double ek = eta * eta + k * k, c2 = ci * ci;
+    const double rs2 = (ek * c2 - 2.0 * eta * ci + 1.0) / (ek * c2 + 2.0 * eta * ci + 1.0);
+    const double rp2 = (ek - 2.0 * eta * ci + c2) / (ek + 2.0 * eta * ci + c2);
+    return 0.5 * (rs2 + rp2);
+}
+
+// the reference's Beckmann D and G1 as written (raytrace.rgen:178-231): the
+// tangent of the cosine dot(v, n), and 2.577 a in the denominator
+double beckmann_D(double alpha, double c) {
+    if (c <= 0.0) return 0.0;
+    const double c2 = c * c, t2 = std::max(1.0 - c2, 0.0) / c2, a2 = alpha * alpha;
+    return exp(-t2 / a2) / (PI * a2 * c2 * c2);
+}
+double beckmann_G1(double alpha, D3 n, D3 m, D3 v) {
+    const double tv = dot(v, n);
+    const double c = dot(v, m) / tv;
+    if (c <= 0.0) return 0.0;
+    const double a = 1.0 / (alpha * tan(tv));
+    if (a >= 1.6) return 1.0;
+    return (3.535 * a + 2.181 * a * a) / (1.0 + 2.276 * a + 2.577 * a);
+}
+
 struct Eval {
     D3 f;
     double pdf;
@@ -463,19 +488,59 @@ Eval bsdf(const pg_material &m, D3 n, D3 wi, D3 wo) {
                         m.albedo[2] + (1 - m.albedo[2]) * w);
         r.f = F * (D * G / (4.0 * ci));
         r.pdf = D * ch / (4.0 * fabs(hi));
+    } else if (m.type == PG_MAT_BECKMANN) {
+        const D3 h = unit(wi + wo);
+        const double D = beckmann_D(m.roughness, dot(n, h));
+        double G = beckmann_G1(m.roughness, n, h, wi) * beckmann_G1(m.roughness, n, h, wo);
+        G = G < 0.0 ? 0.0 : G;
+        const double v = fresnel_conductor(dot(wi, h), m.eta, m.k) * G * D / (4.0 * ci);
+        r.f = std::isnan(v) ? d3(0, 0, 0) : d3(v, v, v);
+        const double pm = D * fabs(dot(h, n)), oh = dot(wo, h);
+        r.pdf = (pm <= 0.0 || oh <= 0.0) ? 0.0 : pm / (4.0 * fabs(oh));
+    } else if (m.type == PG_MAT_PHONG) {
+        const D3 kd = fv(m.albedo), ks = fv(m.specular);
+        D3 res = kd * (1.0 / PI);
+        const double rw = dot(reflect(wo * -1.0, n), wi);
+        if (rw > 0.0) res = res + ks * ((m.exponent + 2.0) / (2.0 * PI) * pow(rw, (double)m.exponent));
+        r.f = res * co;
+        const double ld = sqrt(dot(kd, kd)), ls = sqrt(dot(ks, ks)), sum = ld + ls;
+        if (sum > 0.0) {
+            const double rr = dot(reflect(wi * -1.0, n), wo);
+            const double pdf = rr > 0.0 ? (m.exponent + 1.0) * pow(rr, (double)m.exponent) / (2.0 * PI) * (ls / sum) : 0.0;
+            r.pdf = pdf + co / PI * (ld / sum);
+        }
     }
     return r;
 }
 
-bool is_delta(const pg_material &m) { return m.type == PG_MAT_DIELECTRIC || m.type == PG_MAT_SPECULAR; }
-bool almost_delta(const pg_material &m) { return m.type == PG_MAT_GGX && m.roughness <= 0.3f; }
+bool is_delta(const pg_material &m) {
+    return m.type == PG_MAT_DIELECTRIC || m.type == PG_MAT_SPECULAR || m.type == PG_MAT_CONDUCTOR;
+}
+bool almost_delta(const pg_material &m) {
+    return ((m.type == PG_MAT_GGX || m.type == PG_MAT_BECKMANN) && m.roughness <= 0.3f) ||
+           (m.type == PG_MAT_PHONG && m.exponent >= 250.0f);
+}
 // guiding follows the recording rule: not on discrete or almost-discrete lobes
 bool guided_material(const pg_material &m) { return !is_delta(m) && !almost_delta(m); }
 
-D3 sample_bsdf(const pg_material &m, D3 d, D3 n, double u1, double u2) {
-    if (m.type == PG_MAT_DIFFUSE) {
+D3 sample_bsdf(const pg_material &m, D3 d, D3 n, double ul, double u1, double u2) {
+    if (m.type == PG_MAT_PHONG) {
+        const D3 kd = fv(m.albedo), ks = fv(m.specular);
+        const double ld = sqrt(dot(kd, kd)), ls = sqrt(dot(ks, ks));
+        if (ul * (ld + ls) > ld) {
+            const double ct = pow(u1, 1.0 / (m.exponent + 1.0)), st = sqrt(std::max(0.0, 1.0 - ct * ct));
+            const double ph = 2.0 * PI * u2;
+            return to_world(d3(st * cos(ph), st * sin(ph), ct), reflect(d, n));
+        }
+    }
+    if (m.type == PG_MAT_DIFFUSE || m.type == PG_MAT_PHONG) {
         const double sr = sqrt(u1), ph = 2.0 * PI * u2;
         return to_world(d3(sr * cos(ph), sr * sin(ph), sqrt(std::max(0.0, 1.0 - u1))), n);
+    }
+    if (m.type == PG_MAT_BECKMANN) {
+        const double th = atan(sqrt(-(double)m.roughness * m.roughness * log(1.0 - u1))), ph = 2.0 * PI * u2;
+        const D3 mh = to_world(d3(sin(th) * cos(ph), sin(th) * sin(ph), cos(th)), n);
+        return reflect(d, mh);
     }
     const double a2 = std::max((double)m.roughness * m.roughness, 1e-12);
     const double t2 = a2 * u1 / std::max(1.0 - u1, 1e-12);
@@ -668,6 +733,12 @@ D3 render_pixel(const Scene64 &sc, const pg_render_params &rp, const pgo_guide *
             pdf = 1.0;
             tc = fv(m.albedo);
             delta = true;
+        } else if (m.type == PG_MAT_CONDUCTOR) {
+            wo = reflect(d, n);
+            pdf = 1.0;
+            const double F = fresnel_conductor(dot(wi, n), m.eta, m.k);
+            tc = d3(F, F, F);
+            delta = true;
         } else {
             const bool gm = rp.use_guiding && g && guided_material(m);
             bool use_guide = false, terminate = false;
@@ -681,7 +752,7 @@ D3 render_pixel(const Scene64 &sc, const pg_render_params &rp, const pgo_guide *
                 if (use_guide)
                     wo = vmm_sample(g->vmm[reg], x, par, rnd(rp.seed, pix, smp, dimb(b, 7)), u1, u2);
                 else
-                    wo = sample_bsdf(m, d, n, u1, u2);
+                    wo = sample_bsdf(m, d, n, ul, u1, u2);
                 Eval me = bsdf(m, n, wi, wo);
                 pdf = me.pdf;
                 if (gm) {
@@ -691,7 +762,7 @@ D3 render_pixel(const Scene64 &sc, const pg_render_params &rp, const pgo_guide *
                         const double pg = vmm_pdf(g->vmm[reg], wo, x, par);
                         if (std::isnan(pg)) {
                             if (use_guide) {
-                                wo = sample_bsdf(m, d, n, u1, u2);
+                                wo = sample_bsdf(m, d, n, ul, u1, u2);
                                 me = bsdf(m, n, wi, wo);
                             }
                             pdf = me.pdf;

@@ -75,16 +75,18 @@ def ptr(a: np.ndarray) -> C.c_void_p:
 
 # ---- tracer -------------------------------------------------------------
 PG_MAT_DIFFUSE, PG_MAT_SPECULAR, PG_MAT_DIELECTRIC, PG_MAT_LIGHT, PG_MAT_GGX = 0, 1, 2, 3, 6
+PG_MAT_PHONG, PG_MAT_CONDUCTOR, PG_MAT_BECKMANN = 4, 5, 7
 NO_HIT = 0xFFFFFFFF
 SPHERE_BIT = 0x80000000
 
 MATERIAL_DTYPE = np.dtype([("type", "<i4"), ("albedo", "<f4", (3,)), ("emission", "<f4", (3,)),
-                           ("roughness", "<f4"), ("ior", "<f4"), ("reserved", "<i4", (3,))])
+                           ("roughness", "<f4"), ("ior", "<f4"), ("specular", "<f4", (3,)), ("exponent", "<f4"),
+                           ("eta", "<f4"), ("k", "<f4"), ("reserved", "<i4")])
 SPHERE_DTYPE = np.dtype([("center", "<f4", (3,)), ("radius", "<f4"), ("material", "<u4"), ("reserved", "<u4", (3,))])
 RAY_DTYPE = np.dtype([("org", "<f4", (3,)), ("tmin", "<f4"), ("dir", "<f4", (3,)), ("tmax", "<f4")])
 HIT_DTYPE = np.dtype([("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("prim", "<u4")])
 NODE_DTYPE = np.dtype([("lo", "<f4", (3, 4)), ("hi", "<f4", (3, 4)), ("child", "<i4", (4,)), ("count", "<i4", (4,))])
-assert MATERIAL_DTYPE.itemsize == 48 and SPHERE_DTYPE.itemsize == 32 and RAY_DTYPE.itemsize == 32
+assert MATERIAL_DTYPE.itemsize == 64 and SPHERE_DTYPE.itemsize == 32 and RAY_DTYPE.itemsize == 32
 assert HIT_DTYPE.itemsize == 16 and NODE_DTYPE.itemsize == 128
 
 

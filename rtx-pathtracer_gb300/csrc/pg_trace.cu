@@ -126,6 +126,33 @@ __device__ __forceinline__ float ggx_G1(float a2, float cos_v) {
     return 2.0f * c / (c + sqrtf(a2 + (1.0f - a2) * c * c));
 }
 
+// Fresnel of a conductor (raytrace.rgen:163-176), one spectrum value of eta and k.
+__device__ __forceinline__ float fresnel_conductor(float ci, float eta, float k) {
+    ci = fabsf(ci);
+    const float ek = eta * eta + k * k, c2 = ci * ci;
+    const float rs2 = (ek * c2 - 2.0f * eta * ci + 1.0f) / (ek * c2 + 2.0f * eta * ci + 1.0f);
+    const float rp2 = (ek - 2.0f * eta * ci + c2) / (ek + 2.0f * eta * ci + c2);
+    return 0.5f * (rs2 + rp2);
+}
+
+// The reference's Beckmann rough conductor (raytrace.rgen:178-231, 269-297):
+// D with tan^2 = (1 - cos^2) / cos^2, and its G1 approximation as written
+// there (the tangent taken of the cosine dot(v, n), and 2.577 a where the
+// published rational fit has 2.577 a^2).
+__device__ __forceinline__ float beckmann_D(float alpha, float c) {
+    if (c <= 0.0f) return 0.0f;
+    const float c2 = c * c, t2 = fmaxf(1.0f - c2, 0.0f) / c2, a2 = alpha * alpha;
+    return expf(-t2 / a2) / (kPi * a2 * c2 * c2);
+}
+__device__ __forceinline__ float beckmann_G1(float alpha, V n, V m, V v) {
+    const float tv = dot3(v, n);
+    const float c = dot3(v, m) / tv;
+    if (c <= 0.0f) return 0.0f;
+    const float a = 1.0f / (alpha * tanf(tv));
+    if (a >= 1.6f) return 1.0f;
+    return (3.535f * a + 2.181f * a * a) / (1.0f + 2.276f * a + 2.577f * a);
+}
+
 struct MatEval {
     V f;        // BSDF * cos(theta_o)
     float pdf;  // solid-angle pdf of sampling wo
@@ -150,16 +177,40 @@ __device__ __forceinline__ MatEval bsdf_eval(const pg_material &m, V n, V wi, V 
                        m.albedo[2] + (1.0f - m.albedo[2]) * w);
         r.f = mul(F, D * G / (4.0f * ci));
         r.pdf = D * ch / (4.0f * fabsf(hi));
+    } else if (m.type == PG_MAT_BECKMANN) {
+        // roughConductor and pdfBSDF (raytrace.rgen:269-297)
+        const V h = nrm(add(wi, wo));
+        const float D = beckmann_D(m.roughness, dot3(n, h));
+        float G = beckmann_G1(m.roughness, n, h, wi) * beckmann_G1(m.roughness, n, h, wo);
+        G = G < 0.0f ? 0.0f : G;
+        const float v = fresnel_conductor(dot3(wi, h), m.eta, m.k) * G * D / (4.0f * ci);
+        r.f = isnan(v) ? mk(0, 0, 0) : mk(v, v, v);
+        const float pm = D * fabsf(dot3(h, n)), oh = dot3(wo, h);
+        r.pdf = (pm <= 0.0f || oh <= 0.0f) ? 0.0f : pm / (4.0f * fabsf(oh));
+    } else if (m.type == PG_MAT_PHONG) {
+        // phong and pdfBSDF (raytrace.rgen:242-267, 306-333)
+        const V kd = mk(m.albedo[0], m.albedo[1], m.albedo[2]), ks = mk(m.specular[0], m.specular[1], m.specular[2]);
+        V res = mul(kd, 1.0f / kPi);
+        const float rw = dot3(reflect3(mul(wo, -1.0f), n), wi);
+        if (rw > 0.0f) res = add(res, mul(ks, (m.exponent + 2.0f) / (2.0f * kPi) * powf(rw, m.exponent)));
+        r.f = mul(res, co);
+        const float ld = sqrtf(dot3(kd, kd)), ls = sqrtf(dot3(ks, ks)), sum = ld + ls;
+        if (sum > 0.0f) {
+            const float rr = dot3(reflect3(mul(wi, -1.0f), n), wo);
+            const float pdf = rr > 0.0f ? (m.exponent + 1.0f) * powf(rr, m.exponent) / (2.0f * kPi) * (ls / sum) : 0.0f;
+            r.pdf = pdf + co / kPi * (ld / sum);
+        }
     }
     return r;
 }
 
-__device__ __forceinline__ bool is_delta(const pg_material &m) {
-    return m.type == PG_MAT_DIELECTRIC || m.type == PG_MAT_SPECULAR;  // hasDiscreteDirection
+__device__ __forceinline__ bool is_delta(const pg_material &m) {  // hasDiscreteDirection (raytrace.rgen:733-741)
+    return m.type == PG_MAT_DIELECTRIC || m.type == PG_MAT_SPECULAR || m.type == PG_MAT_CONDUCTOR;
 }
 // isMatAlmostDiscrete (raytrace.rgen:962-964): glossy lobes that are not recorded
 __device__ __forceinline__ bool almost_delta(const pg_material &m) {
-    return m.type == PG_MAT_GGX && m.roughness <= 0.3f;
+    return ((m.type == PG_MAT_GGX || m.type == PG_MAT_BECKMANN) && m.roughness <= 0.3f) ||
+           (m.type == PG_MAT_PHONG && m.exponent >= 250.0f);
 }
 // Vertices whose continuation mixes in the guide.  The reference guides every
 // non-discrete material (raytrace.rgen:926) but records only the ones that
@@ -168,11 +219,27 @@ __device__ __forceinline__ bool almost_delta(const pg_material &m) {
 // surfaces of its region.
 __device__ __forceinline__ bool guided_material(const pg_material &m) { return !is_delta(m) && !almost_delta(m); }
 
-// Lambert (cosine) or GGX (normal distribution, then reflection) sample.
-__device__ __forceinline__ V sample_bsdf(const pg_material &m, V d, V n, float u1, float u2) {
-    if (m.type == PG_MAT_DIFFUSE) {
+// Lambert (cosine), Phong (a lobe chosen by ul, sampleBSDF raytrace.rgen:
+// 491-517), Beckmann (randomBeckmannNormal, random.glsl:127-136) or GGX
+// (normal distribution, then reflection) sample.
+__device__ __forceinline__ V sample_bsdf(const pg_material &m, V d, V n, float ul, float u1, float u2) {
+    if (m.type == PG_MAT_PHONG) {
+        const V kd = mk(m.albedo[0], m.albedo[1], m.albedo[2]), ks = mk(m.specular[0], m.specular[1], m.specular[2]);
+        const float ld = sqrtf(dot3(kd, kd)), ls = sqrtf(dot3(ks, ks));
+        if (ul * (ld + ls) > ld) {  // cosine power around the mirror direction
+            const float ct = powf(u1, 1.0f / (m.exponent + 1.0f)), st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+            const float ph = 2.0f * kPi * u2;
+            return to_world(mk(st * cosf(ph), st * sinf(ph), ct), reflect3(d, n));
+        }
+    }
+    if (m.type == PG_MAT_DIFFUSE || m.type == PG_MAT_PHONG) {
         const float sr = sqrtf(u1), ph = 2.0f * kPi * u2;
         return to_world(mk(sr * cosf(ph), sr * sinf(ph), sqrtf(fmaxf(0.0f, 1.0f - u1))), n);
+    }
+    if (m.type == PG_MAT_BECKMANN) {
+        const float th = atanf(sqrtf(-m.roughness * m.roughness * logf(1.0f - u1))), ph = 2.0f * kPi * u2;
+        const V mh = to_world(mk(sinf(th) * cosf(ph), sinf(th) * sinf(ph), cosf(th)), n);
+        return reflect3(d, mh);
     }
     const float a2 = fmaxf(m.roughness * m.roughness, 1e-12f);
     const float t2 = a2 * u1 / fmaxf(1.0f - u1, 1e-12f);
@@ -630,6 +697,13 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
                 pdf = 1.0f;
                 tc = mk(m.albedo[0], m.albedo[1], m.albedo[2]);
                 delta = true;
+            } else if (m.type == PG_MAT_CONDUCTOR) {
+                // evalBsdf MAT_CONDUCTOR (raytrace.rgen:588-592)
+                wo = reflect3(d, n);
+                pdf = 1.0f;
+                const float F = fresnel_conductor(dot3(wi, n), m.eta, m.k);
+                tc = mk(F, F, F);
+                delta = true;
             } else {
                 const bool gm = R.guiding && guided_material(m);
                 bool use_guide = false;
@@ -645,7 +719,7 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
                         const float ua = rnd(R.rp.seed, p, R.sample, dimb(b, 7));
                         wo = vmm_sample(R.guide.vmm[reg], x, R.guide.use_parallax, ua, u1, u2);
                     } else {
-                        wo = sample_bsdf(m, d, n, u1, u2);
+                        wo = sample_bsdf(m, d, n, ul, u1, u2);
                     }
                     MatEval me = bsdf_eval(m, n, wi, wo);
                     pdf = me.pdf;
@@ -657,7 +731,7 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
                             if (isnan(pg)) {
                                 // unusable mixture: a plain BSDF sample (raytrace.rgen:951-953)
                                 if (use_guide) {
-                                    wo = sample_bsdf(m, d, n, u1, u2);
+                                    wo = sample_bsdf(m, d, n, ul, u1, u2);
                                     me = bsdf_eval(m, n, wi, wo);
                                 }
                                 pdf = me.pdf;

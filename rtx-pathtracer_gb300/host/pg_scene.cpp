@@ -742,8 +742,9 @@ std::string read_string(const XNode &n, const std::string &name) {
     return "";
 }
 
-// parseXmlBSDF (src/SceneLoader.cpp:558-611): diffuse, dielectric, conductor,
-// roughconductor (as GGX here), phong/plastic as diffuse.
+// parseXmlBSDF (src/SceneLoader.cpp:558-611): diffuse, phong, dielectric,
+// conductor (a mirror when its material is "none"), roughconductor (Beckmann);
+// roughplastic as GGX, anything else diffuse.
 uint32_t bsdf_material(SceneData &s, const XNode &b) {
     const XNode *bb = &b;
     if (b.attr.count("type") && b.attr.at("type") == "twosided" && !b.kids.empty()) {
@@ -755,9 +756,30 @@ uint32_t bsdf_material(SceneData &s, const XNode &b) {
         // refractionIndex = intIOR / extIOR (src/SceneLoader.cpp:590)
         return add_material(s, PG_MAT_DIELECTRIC, v3(1, 1, 1), v3(0, 0, 0), 0,
                             read_float(*bb, "intIOR", 1.5f) / read_float(*bb, "extIOR", 1.0f));
-    if (type == "conductor")
-        return add_material(s, PG_MAT_SPECULAR, read_rgb(*bb, "specularReflectance", v3(1, 1, 1)), v3(0, 0, 0), 0, 1);
-    if (type == "roughconductor" || type == "roughplastic")
+    if (type == "phong") {
+        const uint32_t id = add_material(s, PG_MAT_PHONG, read_rgb(*bb, "diffuseReflectance", v3(0.5f, 0.5f, 0.5f)),
+                                         v3(0, 0, 0), 0, 1);
+        const V3 sp = read_rgb(*bb, "specularReflectance", v3(0.2f, 0.2f, 0.2f));
+        pg_material &m = s.mats[id];
+        m.specular[0] = sp.x, m.specular[1] = sp.y, m.specular[2] = sp.z;
+        m.exponent = read_float(*bb, "exponent", 30.0f);
+        return id;
+    }
+    if (type == "conductor") {
+        if (read_string(*bb, "material") == "none")
+            return add_material(s, PG_MAT_SPECULAR, v3(1, 1, 1), v3(0, 0, 0), 0, 1);
+        const uint32_t id = add_material(s, PG_MAT_CONDUCTOR, v3(1, 1, 1), v3(0, 0, 0), 0, 1);
+        s.mats[id].eta = read_rgb(*bb, "eta", v3(0.2f, 0.2f, 0.2f)).x;
+        s.mats[id].k = read_rgb(*bb, "k", v3(3.9f, 3.9f, 3.9f)).x;
+        return id;
+    }
+    if (type == "roughconductor") {
+        const uint32_t id = add_material(s, PG_MAT_BECKMANN, v3(1, 1, 1), v3(0, 0, 0), read_float(*bb, "alpha", 0.1f), 1);
+        s.mats[id].eta = read_rgb(*bb, "eta", v3(0.2f, 0.2f, 0.2f)).x;
+        s.mats[id].k = read_rgb(*bb, "k", v3(3.9f, 3.9f, 3.9f)).x;
+        return id;
+    }
+    if (type == "roughplastic")
         return add_material(s, PG_MAT_GGX, read_rgb(*bb, "specularReflectance", v3(1, 1, 1)), v3(0, 0, 0),
                             read_float(*bb, "alpha", 0.1f), 1);
     return add_material(s, PG_MAT_DIFFUSE, read_rgb(*bb, "reflectance", v3(0.5f, 0.5f, 0.5f)), v3(0, 0, 0), 0, 1);

@@ -172,7 +172,14 @@ MITSUBA = """<?xml version="1.0" encoding="utf-8"?>
   <bsdf type="twosided" id="white">
     <bsdf type="diffuse"><rgb name="reflectance" value="0.7, 0.6, 0.5"/></bsdf>
   </bsdf>
-  <bsdf type="roughconductor" id="metal"><float name="alpha" value="0.2"/></bsdf>
+  <bsdf type="roughconductor" id="metal">
+    <string name="distribution" value="beckmann"/><float name="alpha" value="0.2"/>
+    <spectrum name="eta" value="0.370"/><spectrum name="k" value="2.820"/>
+  </bsdf>
+  <bsdf type="phong" id="plastic">
+    <rgb name="diffuseReflectance" value="0.3, 0.4, 0.5"/><rgb name="specularReflectance" value="0.2, 0.2, 0.2"/>
+    <float name="exponent" value="40"/>
+  </bsdf>
   <shape type="obj">
     <string name="filename" value="quad.obj"/>
     <ref id="white"/>
@@ -185,6 +192,20 @@ MITSUBA = """<?xml version="1.0" encoding="utf-8"?>
     <point name="center" x="1" y="2" z="0"/>
     <float name="radius" value="0.25"/>
     <bsdf type="dielectric"><float name="intIOR" value="1.596"/><float name="extIOR" value="1.2"/></bsdf>
+  </shape>
+  <shape type="sphere">
+    <point name="center" x="-1.2" y="0.6" z="0.5"/>
+    <float name="radius" value="0.5"/>
+    <bsdf type="conductor"><spectrum name="eta" value="0.2"/><spectrum name="k" value="3.9"/></bsdf>
+  </shape>
+  <shape type="sphere">
+    <point name="center" x="1.3" y="0.4" z="0.8"/>
+    <float name="radius" value="0.4"/>
+    <bsdf type="conductor"><string name="material" value="none"/></bsdf>
+  </shape>
+  <shape type="rectangle">
+    <transform name="toWorld"><rotate x="1" angle="90"/><translate x="0" y="1" z="-2"/></transform>
+    <ref id="plastic"/>
   </shape>
   <shape type="rectangle">
     <transform name="toWorld"><translate x="0" y="3" z="0"/></transform>
@@ -208,7 +229,7 @@ def test_mitsuba_loader(pkg, abi, tmp_path):
     (tmp_path / "scene.xml").write_text(MITSUBA)
     sc = pkg.Scene.load(tmp_path / "scene.xml", 40, 30)
     i = sc.info()
-    assert i.n_triangles == 2 + 12 + 2 and i.n_spheres == 1 and i.n_lights == 1
+    assert i.n_triangles == 2 + 12 + 2 + 2 and i.n_spheres == 3 and i.n_lights == 1
     cam = i.camera
     assert (cam.width, cam.height) == (40, 30) and abs(cam.vfov_deg - 40) < 1e-6
     assert list(cam.origin) == [0, 1, 6] and list(cam.target) == [0, 1, 0]
@@ -216,12 +237,19 @@ def test_mitsuba_loader(pkg, abi, tmp_path):
     mats = exp["mats"]
     by_type = {int(t): m for t, m in zip(mats["type"], mats)}
     assert np.allclose(by_type[abi.PG_MAT_DIFFUSE]["albedo"], [0.7, 0.6, 0.5])
-    assert abs(by_type[abi.PG_MAT_GGX]["roughness"] - 0.2) < 1e-7
+    metal = by_type[abi.PG_MAT_BECKMANN]  # roughconductor: the reference's Beckmann conductor
+    assert abs(metal["roughness"] - 0.2) < 1e-7 and abs(metal["eta"] - 0.37) < 1e-7 and abs(metal["k"] - 2.82) < 1e-6
+    phong = by_type[abi.PG_MAT_PHONG]
+    assert np.allclose(phong["albedo"], [0.3, 0.4, 0.5]) and np.allclose(phong["specular"], 0.2)
+    assert phong["exponent"] == 40
+    cond = by_type[abi.PG_MAT_CONDUCTOR]
+    assert abs(cond["eta"] - 0.2) < 1e-7 and abs(cond["k"] - 3.9) < 1e-6
+    assert abi.PG_MAT_SPECULAR in by_type  # conductor with material "none": a mirror
     assert abs(by_type[abi.PG_MAT_DIELECTRIC]["ior"] - 1.596 / 1.2) < 1e-6  # intIOR / extIOR
     assert np.allclose(by_type[abi.PG_MAT_LIGHT]["emission"], [10, 9, 8])
     assert np.allclose(exp["spheres"]["center"][0], [1, 2, 0]) and abs(exp["spheres"]["radius"][0] - 0.25) < 1e-7
     # the unit cube scaled by 0.5 and lifted by 0.5 spans [-0.5, 0.5] x [0, 1] x [-0.5, 0.5]
-    cube = exp["pos"][exp["idx"][exp["tri_mat"] == int(np.where(mats["type"] == abi.PG_MAT_GGX)[0][0])]].reshape(-1, 3)
+    cube = exp["pos"][exp["idx"][exp["tri_mat"] == int(np.where(mats["type"] == abi.PG_MAT_BECKMANN)[0][0])]].reshape(-1, 3)
     assert np.allclose(cube.min(0), [-0.5, 0.0, -0.5]) and np.allclose(cube.max(0), [0.5, 1.0, 0.5])
     check_bvh(exp)
 
