@@ -529,6 +529,24 @@ int pg_scene_export_mesh(const pg_scene *scene, float *positions, uint32_t *indi
 /* Replaces the camera (SceneLoader origin/target/upDir/vfov, src/SceneLoader.h:147-150)
  * and the image size. */
 int pg_scene_set_camera(pg_scene *scene, const pg_camera *cam);
+/* Environment map (SceneLoader::parseEnvMap, src/SceneLoader.cpp:370-401;
+ * shaders/raytrace.rmiss): a lat-long RGB image, width x height texels, row 0
+ * looking up (+y), column u = atan2(x, -z) / 2 pi; sampled bilinearly with
+ * wrap-around.  It lights misses and is one more light for next-event
+ * estimation (a uniform direction in the hemisphere, raytrace.rgen:406-421).
+ * width = height = 0 removes it.  A Mitsuba file's envmap emitter sets it. */
+int pg_scene_set_envmap(pg_scene *scene, const float *rgb, uint32_t width, uint32_t height);
+/* Its size, and a copy when rgb_out is not NULL (3 * width * height floats). */
+int pg_scene_get_envmap(const pg_scene *scene, float *rgb_out, uint32_t *width, uint32_t *height);
+
+/* OpenEXR images (writeEXR / readEXR, src/CommonOps.cpp:12-65): scanline
+ * files with HALF, FLOAT or UINT channels, uncompressed, ZIPS or ZIP
+ * compressed (the project inflates ZIP itself); RGB floats row-major from the
+ * top row (a Y-only image fills all three).  With rgb_out NULL only the size
+ * is returned; capacity counts floats.  The writer stores FLOAT R, G, B
+ * without compression. */
+int pg_exr_read(const char *path, float *rgb_out, uint64_t capacity, uint32_t *width, uint32_t *height);
+int pg_exr_write(const char *path, const float *rgb, uint32_t width, uint32_t height);
 
 /* Closest hit / any hit of n rays (device arrays).  Traversal: four-wide BVH,
  * near child first, watertight FP32 ray-triangle test (Woop, Benthin and

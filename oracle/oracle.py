@@ -275,7 +275,8 @@ class ReferenceFit:
 class PgoScene(C.Structure):
     _fields_ = [("nodes", _P), ("n_nodes", _U32), ("tri_verts", _P), ("n_tris", _U32), ("pos", _P),
                 ("n_vertices", _U32), ("idx", _P), ("tri_mat", _P), ("mats", _P), ("n_mats", _U32),
-                ("spheres", _P), ("n_spheres", _U32), ("camera", abi.Camera)]
+                ("spheres", _P), ("n_spheres", _U32), ("camera", abi.Camera), ("env", _P), ("env_w", _U32),
+                ("env_h", _U32)]
 
 
 class PgoGuide(C.Structure):
@@ -301,11 +302,14 @@ class TraceOracle:
     @staticmethod
     def scene(exp: dict, camera: "abi.Camera | None" = None) -> tuple:
         keep = {k: np.ascontiguousarray(v) for k, v in exp.items() if isinstance(v, np.ndarray)}
+        env = keep.get("env")
         s = PgoScene(keep["nodes"].ctypes.data, keep["nodes"].shape[0], keep["tri_verts"].ctypes.data,
                      keep["tri_verts"].shape[0], keep["pos"].ctypes.data, keep["pos"].shape[0],
                      keep["idx"].ctypes.data, keep["tri_mat"].ctypes.data, keep["mats"].ctypes.data,
                      keep["mats"].shape[0], keep["spheres"].ctypes.data, keep["spheres"].shape[0],
-                     camera if camera is not None else exp["info"].camera)
+                     camera if camera is not None else exp["info"].camera,
+                     env.ctypes.data if env is not None else None, env.shape[1] if env is not None else 0,
+                     env.shape[0] if env is not None else 0)
         return s, keep
 
     def closest(self, exp, rays, threads=None):

@@ -604,6 +604,20 @@ D3 vmm_sample(const pg_vmm_theta &v, D3 x, int par, double ul, double u1, double
     return d3(r * cos(ph), r * sin(ph), z);
 }
 
+// the lat-long environment along d (raytrace.rmiss), bilinear with wrap-around
+D3 env_radiance(const pgo_scene &S, D3 d) {
+    const double u = atan2(d.x, -d.z) / (2.0 * PI), v = acos(std::min(std::max(d.y, -1.0), 1.0)) / PI;
+    const double sx = u * S.env_w - 0.5, sy = v * S.env_h - 0.5;
+    const double fx0 = floor(sx), fy0 = floor(sy), fx = sx - fx0, fy = sy - fy0;
+    const long W = S.env_w, H = S.env_h;
+    long x0 = (long)fx0 % W, y0 = (long)fy0 % H;
+    x0 += x0 < 0 ? W : 0;
+    y0 += y0 < 0 ? H : 0;
+    const long x1 = x0 + 1 == W ? 0 : x0 + 1, y1 = y0 + 1 == H ? 0 : y0 + 1;
+    auto tx = [&](long x, long y) { return fv(S.env + 3 * (size_t)(y * W + x)); };
+    return (tx(x0, y0) * (1.0 - fx) + tx(x1, y0) * fx) * (1.0 - fy) + (tx(x0, y1) * (1.0 - fx) + tx(x1, y1) * fx) * fy;
+}
+
 D3 render_pixel(const Scene64 &sc, const pg_render_params &rp, const pgo_guide *g, uint32_t pix, uint32_t smp) {
     const pgo_scene &S = *sc.S;
     const pg_camera &cam = S.camera;
@@ -622,7 +636,17 @@ D3 render_pixel(const Scene64 &sc, const pg_render_params &rp, const pgo_guide *
     for (int b = 0; b < (int)rp.max_depth; ++b) {
         const bool last = b + 1 == (int)rp.max_depth;
         const Hit64 h = intersect64(S, o, d, 0.001, 1e6, false);
-        if (h.prim == PG_NO_HIT) break;
+        if (h.prim == PG_NO_HIT) {
+            if (S.env && S.env_w) {
+                double w = 1.0;
+                if (rp.use_nee && prev_pdf > 0.0) {
+                    const double pl = 1.0 / (2.0 * PI) / nL;
+                    w = rp.use_mis ? prev_pdf * prev_pdf / (prev_pdf * prev_pdf + pl * pl) : 0.0;
+                }
+                L = L + hm(thr, env_radiance(S, d) * w);
+            }
+            break;
+        }
         const D3 x = o + d * h.t;
         D3 ng;
         uint32_t mat_id;
@@ -670,6 +694,25 @@ D3 render_pixel(const Scene64 &sc, const pg_render_params &rp, const pgo_guide *
             const Light &Li = sc.lights[l];
             const double u1 = rnd(rp.seed, pix, smp, dimb(b, 1)), u2 = rnd(rp.seed, pix, smp, dimb(b, 2));
             D3 lp, ln;
+            if (Li.type == 2) {
+                const double ct = u1, st = sqrt(std::max(0.0, 1.0 - ct * ct)), ph = 2.0 * PI * u2;
+                const D3 wl = to_world(d3(st * cos(ph), st * sin(ph), ct), n);
+                const double pl = 1.0 / (2.0 * PI) / nL;
+                const Eval me = bsdf(m, n, wi, wl);
+                if (mx(me.f) > 0.0) {
+                    double pb = me.pdf;
+                    if (rp.use_guiding && g && guided_material(m)) {
+                        const uint32_t reg = region_of(*g, x);
+                        if (reg != PG_INVALID_REGION) {
+                            const double pg = vmm_pdf(g->vmm[reg], wl, x, par);
+                            if (!std::isnan(pg)) pb = (1.0 - rp.guiding_prob) * pb + rp.guiding_prob * pg;
+                        }
+                    }
+                    const double w = rp.use_mis ? pl * pl / (pl * pl + pb * pb) : 1.0;
+                    if (intersect64(S, x, wl, 0.001, 1e30, true).prim == PG_NO_HIT)
+                        L = L + hm(thr, hm(me.f, env_radiance(S, wl)) * (w / pl));
+                }
+            } else {
             if (Li.type == 1) {
                 const pg_sphere &sp = S.spheres[Li.sphere];
                 const double z = 1.0 - 2.0 * u1, rr = sqrt(std::max(0.0, 1.0 - z * z)), ph = 2.0 * PI * u2;
@@ -708,6 +751,7 @@ D3 render_pixel(const Scene64 &sc, const pg_render_params &rp, const pgo_guide *
                     if (intersect64(S, x, wl, 0.001, dist * (1.0 - 0.0001), true).prim == PG_NO_HIT)
                         L = L + hm(thr, hm(me.f, Li.emission) * (w / pl));
                 }
+            }
             }
         }
         D3 wo = d3(0, 0, 1), tc = d3(0, 0, 0);
@@ -845,6 +889,14 @@ void pgo_render_f64(const pgo_scene *s, const pg_render_params *rp, const pgo_gu
         L.sphere = i;
         L.area = 4.0 * PI * (double)s->spheres[i].radius * s->spheres[i].radius;
         L.emission = fv(m.emission);
+        sc.lights.push_back(L);
+    }
+    if (s->env && s->env_w && s->env_h) {  // the environment is the last light
+        Light L;
+        L.type = 2;
+        L.sphere = 0;
+        L.area = 0.0;
+        L.emission = d3(0, 0, 0);
         sc.lights.push_back(L);
     }
     const uint32_t W = s->camera.width;

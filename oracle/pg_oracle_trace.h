@@ -34,6 +34,8 @@ typedef struct pgo_scene {
     const pg_sphere *spheres;
     uint32_t n_spheres;
     pg_camera camera;
+    const float *env;           /* environment map, RGB per texel, or NULL */
+    uint32_t env_w, env_h;
 } pgo_scene;
 
 typedef struct pgo_guide {

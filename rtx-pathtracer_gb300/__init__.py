@@ -87,6 +87,10 @@ SIGNATURES = {
     "pg_scene_create_cornell": (_I, [C.POINTER(abi.CornellParams), C.POINTER(_P)]),
     "pg_scene_create_plates": (_I, [C.POINTER(abi.PlatesParams), C.POINTER(_P)]),
     "pg_scene_destroy": (_I, [_P]),
+    "pg_scene_set_envmap": (_I, [_P, _P, _U32, _U32]),
+    "pg_scene_get_envmap": (_I, [_P, _P, C.POINTER(_U32), C.POINTER(_U32)]),
+    "pg_exr_read": (_I, [C.c_char_p, _P, _U64, C.POINTER(_U32), C.POINTER(_U32)]),
+    "pg_exr_write": (_I, [C.c_char_p, _P, _U32, _U32]),
     "pg_scene_get_info": (_I, [_P, C.POINTER(abi.SceneInfo)]),
     "pg_scene_export": (_I, [_P, _P, _P, _P, _P, _P, _P]),
     "pg_scene_export_mesh": (_I, [_P, _P, _P, C.POINTER(_U32)]),
@@ -431,6 +435,29 @@ def fit_regions_noalloc(cfg: abi.FitConfig, states_dev, dirw, offsets, n_regions
                                             n_regions, mode, _stream_handle(stream))
 
 
+def read_exr(path) -> np.ndarray:
+    """An OpenEXR image as (height, width, 3) float32 (pg_exr_read)."""
+    lib = library()
+    w, h = C.c_uint32(), C.c_uint32()
+    st = lib.pg_exr_read(str(path).encode(), None, 0, C.byref(w), C.byref(h))
+    if st != abi.PG_OK:
+        raise PathGuideError(st, lib.pg_last_error(None).decode())
+    out = np.zeros((h.value, w.value, 3), dtype=np.float32)
+    st = lib.pg_exr_read(str(path).encode(), out.ctypes.data, out.size, C.byref(w), C.byref(h))
+    if st != abi.PG_OK:
+        raise PathGuideError(st, lib.pg_last_error(None).decode())
+    return out
+
+
+def write_exr(path, rgb) -> None:
+    """Writes (height, width, 3) floats as an uncompressed FLOAT OpenEXR file (pg_exr_write)."""
+    lib = library()
+    a = np.ascontiguousarray(rgb, dtype=np.float32)
+    st = lib.pg_exr_write(str(path).encode(), a.ctypes.data, a.shape[1], a.shape[0])
+    if st != abi.PG_OK:
+        raise PathGuideError(st, lib.pg_last_error(None).decode())
+
+
 class Scene:
     """A pg_scene: geometry, materials, lights and camera with its BVH (SceneLoader)."""
 
@@ -500,8 +527,32 @@ class Scene:
         pos = np.zeros((nv.value, 3), dtype=np.float32)
         idx = np.zeros((i.n_triangles, 3), dtype=np.uint32)
         self._check(self.lib.pg_scene_export_mesh(self.h, pos.ctypes.data, idx.ctypes.data, C.byref(nv)))
-        return {"nodes": nodes, "tri_verts": tv, "tri_order": order, "tri_mat": tmat, "mats": mats,
-                "spheres": sph, "pos": pos, "idx": idx, "info": i}
+        out = {"nodes": nodes, "tri_verts": tv, "tri_order": order, "tri_mat": tmat, "mats": mats,
+               "spheres": sph, "pos": pos, "idx": idx, "info": i}
+        env = self.envmap()
+        if env is not None:
+            out["env"] = env
+        return out
+
+    def set_envmap(self, rgb):
+        """The environment map: a lat-long RGB image (height, width, 3), row 0
+        looking up; None removes it (pg_scene_set_envmap)."""
+        if rgb is None:
+            self._check(self.lib.pg_scene_set_envmap(self.h, None, 0, 0))
+            return
+        a = np.ascontiguousarray(rgb, dtype=np.float32)
+        if a.ndim != 3 or a.shape[2] != 3:
+            raise ValueError("environment map must be (height, width, 3)")
+        self._check(self.lib.pg_scene_set_envmap(self.h, a.ctypes.data, a.shape[1], a.shape[0]))
+
+    def envmap(self):
+        w, h = C.c_uint32(), C.c_uint32()
+        self._check(self.lib.pg_scene_get_envmap(self.h, None, C.byref(w), C.byref(h)))
+        if w.value == 0:
+            return None
+        out = np.zeros((h.value, w.value, 3), dtype=np.float32)
+        self._check(self.lib.pg_scene_get_envmap(self.h, out.ctypes.data, C.byref(w), C.byref(h)))
+        return out
 
     def trace_closest(self, rays_dev, n, hits_dev, stream=None):
         self._check(self.lib.pg_trace_closest(self.h, _dptr(rays_dev), n, _dptr(hits_dev), _stream_handle(stream)))

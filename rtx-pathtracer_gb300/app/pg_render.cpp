@@ -153,7 +153,14 @@ int main(int argc, char **argv) {
             mean += v;
         }
         mean /= (double)n;
-        if (!out.empty() && !write_pfm(out, rgb, W, H)) {
+        const bool exr = out.size() > 4 && out.compare(out.size() - 4, 4, ".exr") == 0;
+        if (!out.empty() && exr) {
+            // writeEXR (src/CommonOps.cpp:12-38): rows from the top
+            if (pg_exr_write(out.c_str(), rgb.data(), W, H) != PG_OK) {
+                fprintf(stderr, "cannot write %s\n", out.c_str());
+                return EXIT_FAILURE;
+            }
+        } else if (!out.empty() && !write_pfm(out, rgb, W, H)) {
             fprintf(stderr, "cannot write %s\n", out.c_str());
             return EXIT_FAILURE;
         }

@@ -34,6 +34,7 @@
 #include <string>
 #include <vector>
 
+#include "../host/pg_exr.h"
 #include "../host/pg_scene.h"
 #include "pg_internal.cuh"
 #include "pg_traverse.cuh"
@@ -47,7 +48,7 @@ constexpr int kMaxRecords = 16;    // MAX_DIRECTIONAL_DATA_PER_PIXEL (shaders/li
 constexpr int kNumStats = 8;       // device render statistics (see DevRender::stats)
 
 struct DevLight {
-    int32_t type;      // 0: triangle mesh, 1: sphere
+    int32_t type;      // 0: triangle mesh, 1: sphere, 2: environment map
     uint32_t first;    // into light_tris / light_cdf
     uint32_t count;
     uint32_t sphere;
@@ -369,6 +370,8 @@ struct DevRender {
     const uint32_t *light_tris;  // original triangle ids of mesh lights
     const float *light_cdf;      // per light, cumulative area fraction
     const int32_t *tri_light;    // light index of each original triangle, -1 if none
+    const float *env;            // environment map, RGB per texel (null: black)
+    uint32_t env_w, env_h;
     unsigned long long *stats;   // [0] extension rays, [1] shadow rays, [2..5] traversal work (counting renders)
     pg_camera cam;
     float cam_fwd[3], cam_right[3], cam_up[3], tan_half;
@@ -427,6 +430,24 @@ __device__ __forceinline__ void update_records(const DevRender &R, uint32_t pix,
         R.rec_lsum[3 * s + 2] += L.z;
         L = hmul(L, ld3(R.rec_tc, s));
     }
+}
+
+// Environment radiance along a direction (raytrace.rmiss): the lat-long map
+// at u = atan2(x, -z) / 2 pi, v = acos(y) / pi, bilinear with wrap-around in
+// both axes as the reference's linear, repeating sampler.
+__device__ __forceinline__ V env_radiance(const DevRender &R, V d) {
+    const float kInv2Pi = 0.15915494309189535f;
+    const float u = atan2f(d.x, -d.z) * kInv2Pi, v = acosf(fminf(fmaxf(d.y, -1.0f), 1.0f)) * (1.0f / kPi);
+    const float sx = u * (float)R.env_w - 0.5f, sy = v * (float)R.env_h - 0.5f;
+    const float fx0 = floorf(sx), fy0 = floorf(sy), fx = sx - fx0, fy = sy - fy0;
+    const int W = (int)R.env_w, H = (int)R.env_h;
+    int x0 = (int)fx0 % W, y0 = (int)fy0 % H;
+    x0 += x0 < 0 ? W : 0;
+    y0 += y0 < 0 ? H : 0;
+    const int x1 = x0 + 1 == W ? 0 : x0 + 1, y1 = y0 + 1 == H ? 0 : y0 + 1;
+    const V a = ld3(R.env, (uint32_t)(y0 * W + x0)), b = ld3(R.env, (uint32_t)(y0 * W + x1));
+    const V c = ld3(R.env, (uint32_t)(y1 * W + x0)), e = ld3(R.env, (uint32_t)(y1 * W + x1));
+    return add(mul(add(mul(a, 1.0f - fx), mul(b, fx)), 1.0f - fy), mul(add(mul(c, 1.0f - fx), mul(e, fx)), fy));
 }
 
 // Solid-angle pdf of NEE picking the emitter point hit at distance t with
@@ -540,10 +561,29 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
     bool cont = false;
     const bool rec_on = R.recording != 0;
     if (h.prim == PG_NO_HIT) {
-        // miss: black environment; a pending record saw infinity (distance 0)
+        // miss: a pending record saw infinity (distance 0)
         if (rec_on && R.rec_pending[p] >= 0) {
             R.rec[p * kMaxRecords + (uint32_t)R.rec_pending[p]].distance = 0.0f;
             R.rec_pending[p] = -1;
+        }
+        if (R.env) {
+            // the environment (raytrace.rgen:1025-1037), MIS-weighted against its NEE:
+            // a uniform direction in the hemisphere of the previous vertex
+            float w = 1.0f;
+            const float pp = R.prev_pdf[p];
+            if (R.rp.use_nee && pp > 0.0f) {
+                const float pl = 0.15915494309189535f / (float)R.n_lights;
+                w = R.rp.use_mis ? pp * pp / (pp * pp + pl * pl) : 0.0f;
+            }
+            const V Le = mul(env_radiance(R, d), w);
+            if (maxc(Le) > 0.0f) {
+                const V c = hmul(thr, Le);
+                atomicAdd(&R.image[3 * p], c.x);
+                atomicAdd(&R.image[3 * p + 1], c.y);
+                atomicAdd(&R.image[3 * p + 2], c.z);
+                R.found[p] = 1;
+                if (rec_on) update_records(R, p, R.rec_count[p], Le);
+            }
         }
     } else {
         const V o = ld3(R.ro, p);
@@ -613,41 +653,13 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
                 const DevLight &L = R.lights[l];
                 const float u1 = rnd(R.rp.seed, p, R.sample, dimb(b, 1)), u2 = rnd(R.rp.seed, p, R.sample, dimb(b, 2));
                 V lp, ln;
-                if (L.type == 1) {
-                    const pg_sphere &sp = R.S.spheres[L.sphere];
-                    const float z = 1.0f - 2.0f * u1, rr = sqrtf(fmaxf(0.0f, 1.0f - z * z)), ph = 2.0f * kPi * u2;
-                    ln = mk(rr * cosf(ph), rr * sinf(ph), z);
-                    lp = add(mk(sp.center[0], sp.center[1], sp.center[2]), mul(ln, sp.radius));
-                } else {
-                    // triangle by area, then a uniform point (raytrace.rgen:445-456)
-                    uint32_t lo = 0, hi = L.count - 1;
-                    const float uc = u1;
-                    while (lo < hi) {
-                        const uint32_t mid = (lo + hi) / 2;
-                        if (R.light_cdf[L.first + mid] < uc)
-                            lo = mid + 1;
-                        else
-                            hi = mid;
-                    }
-                    const float c0 = lo == 0 ? 0.0f : R.light_cdf[L.first + lo - 1];
-                    const float c1 = R.light_cdf[L.first + lo];
-                    const float ur = c1 > c0 ? fminf((uc - c0) / (c1 - c0), 0.99999994f) : 0.5f;
-                    const uint32_t t = R.light_tris[L.first + lo];
-                    const V a = ld3(R.pos, R.idx[3 * t]), bb = ld3(R.pos, R.idx[3 * t + 1]), c = ld3(R.pos, R.idx[3 * t + 2]);
-                    const float sx = sqrtf(ur);
-                    lp = add(add(mul(a, 1.0f - sx), mul(bb, sx * (1.0f - u2))), mul(c, u2 * sx));
-                    ln = nrm(cross3(sub(bb, a), sub(c, a)));
-                }
-                V tl = sub(lp, x);
-                const float dist2 = dot3(tl, tl), dist = sqrtf(dist2);
-                const V wl = mul(tl, 1.0f / dist);
-                float cl = -dot3(wl, ln);
-                if (L.type == 0) cl = fabsf(cl);  // two-sided mesh lights (raytrace.rgen:463-466)
-                if (cl > 0.0f && dot3(n, wl) > 0.0f) {
-                    const float pl = dist2 / (cl * L.area) / (float)R.n_lights;
+                if (L.type == 2) {
+                    // environment: a uniform direction in the hemisphere (raytrace.rgen:406-421)
+                    const float ct = u1, st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct)), ph = 2.0f * kPi * u2;
+                    const V wl = to_world(mk(st * cosf(ph), st * sinf(ph), ct), n);
+                    const float pl = 0.15915494309189535f / (float)R.n_lights;
                     const MatEval me = bsdf_eval(m, n, wi, wl);
                     if (maxc(me.f) > 0.0f) {
-                        // pdf of the continuation sampler for this direction (MIS)
                         float pb = me.pdf;
                         if (R.guiding && guided_material(m)) {
                             const uint32_t reg = region_of(R.guide, x);
@@ -657,15 +669,71 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
                             }
                         }
                         const float w = R.rp.use_mis ? pl * pl / (pl * pl + pb * pb) : 1.0f;
-                        const V Lnee = mul(hmul(me.f, mk(L.emission[0], L.emission[1], L.emission[2])), w / pl);
+                        const V Lnee = mul(hmul(me.f, env_radiance(R, wl)), w / pl);
                         const uint32_t s = atomicAdd(&R.counters[2], 1u);
                         st3(R.sh_o, s, x);
                         st3(R.sh_d, s, wl);
-                        R.sh_tmax[s] = dist * (1.0f - 0.0001f);
+                        R.sh_tmax[s] = 1e30f;
                         st3(R.sh_c, s, hmul(thr, Lnee));
                         st3(R.sh_l, s, Lnee);
                         R.sh_pix[s] = p;
                         R.sh_nrec[s] = rec_on ? R.rec_count[p] : 0u;
+                    }
+                } else {
+                    if (L.type == 1) {
+                        const pg_sphere &sp = R.S.spheres[L.sphere];
+                        const float z = 1.0f - 2.0f * u1, rr = sqrtf(fmaxf(0.0f, 1.0f - z * z)), ph = 2.0f * kPi * u2;
+                        ln = mk(rr * cosf(ph), rr * sinf(ph), z);
+                        lp = add(mk(sp.center[0], sp.center[1], sp.center[2]), mul(ln, sp.radius));
+                    } else {
+                        // triangle by area, then a uniform point (raytrace.rgen:445-456)
+                        uint32_t lo = 0, hi = L.count - 1;
+                        const float uc = u1;
+                        while (lo < hi) {
+                            const uint32_t mid = (lo + hi) / 2;
+                            if (R.light_cdf[L.first + mid] < uc)
+                                lo = mid + 1;
+                            else
+                                hi = mid;
+                        }
+                        const float c0 = lo == 0 ? 0.0f : R.light_cdf[L.first + lo - 1];
+                        const float c1 = R.light_cdf[L.first + lo];
+                        const float ur = c1 > c0 ? fminf((uc - c0) / (c1 - c0), 0.99999994f) : 0.5f;
+                        const uint32_t t = R.light_tris[L.first + lo];
+                        const V a = ld3(R.pos, R.idx[3 * t]), bb = ld3(R.pos, R.idx[3 * t + 1]), c = ld3(R.pos, R.idx[3 * t + 2]);
+                        const float sx = sqrtf(ur);
+                        lp = add(add(mul(a, 1.0f - sx), mul(bb, sx * (1.0f - u2))), mul(c, u2 * sx));
+                        ln = nrm(cross3(sub(bb, a), sub(c, a)));
+                    }
+                    V tl = sub(lp, x);
+                    const float dist2 = dot3(tl, tl), dist = sqrtf(dist2);
+                    const V wl = mul(tl, 1.0f / dist);
+                    float cl = -dot3(wl, ln);
+                    if (L.type == 0) cl = fabsf(cl);  // two-sided mesh lights (raytrace.rgen:463-466)
+                    if (cl > 0.0f && dot3(n, wl) > 0.0f) {
+                        const float pl = dist2 / (cl * L.area) / (float)R.n_lights;
+                        const MatEval me = bsdf_eval(m, n, wi, wl);
+                        if (maxc(me.f) > 0.0f) {
+                            // pdf of the continuation sampler for this direction (MIS)
+                            float pb = me.pdf;
+                            if (R.guiding && guided_material(m)) {
+                                const uint32_t reg = region_of(R.guide, x);
+                                if (reg != PG_INVALID_REGION) {
+                                    const float pg = vmm_pdf(R.guide.vmm[reg], wl, x, R.guide.use_parallax);
+                                    if (!isnan(pg)) pb = (1.0f - R.rp.guiding_prob) * pb + R.rp.guiding_prob * pg;
+                                }
+                            }
+                            const float w = R.rp.use_mis ? pl * pl / (pl * pl + pb * pb) : 1.0f;
+                            const V Lnee = mul(hmul(me.f, mk(L.emission[0], L.emission[1], L.emission[2])), w / pl);
+                            const uint32_t s = atomicAdd(&R.counters[2], 1u);
+                            st3(R.sh_o, s, x);
+                            st3(R.sh_d, s, wl);
+                            R.sh_tmax[s] = dist * (1.0f - 0.0001f);
+                            st3(R.sh_c, s, hmul(thr, Lnee));
+                            st3(R.sh_l, s, Lnee);
+                            R.sh_pix[s] = p;
+                            R.sh_nrec[s] = rec_on ? R.rec_count[p] : 0u;
+                        }
                     }
                 }
             }
@@ -941,6 +1009,7 @@ struct pg_scene {
     uint32_t *d_light_tris = nullptr;
     float *d_light_cdf = nullptr;
     int32_t *d_tri_light = nullptr;
+    float *d_env = nullptr;
     unsigned long long *d_stats = nullptr;
     uint32_t n_lights = 0;
     bool uploaded = false;
@@ -1043,6 +1112,11 @@ void build_host(pg_scene *sc) {
         for (int k = 0; k < 3; ++k) L.emission[k] = m.emission[k];
         lights.push_back(L);
     }
+    if (!s.env.empty()) {  // the environment is the last light (SceneLoader::parseEnvMap)
+        DevLight L{};
+        L.type = 2;
+        lights.push_back(L);
+    }
     sc->n_lights = (uint32_t)lights.size();
 }
 
@@ -1067,6 +1141,7 @@ int ensure_uploaded(pg_scene *sc) {
     if (!st) st = upload(&sc->d_light_tris, sc->h_light_tris);
     if (!st) st = upload(&sc->d_light_cdf, sc->h_light_cdf);
     if (!st) st = upload(&sc->d_tri_light, sc->h_tri_light);
+    if (!st) st = upload(&sc->d_env, s.env);
     if (!st && cudaMalloc(&sc->d_counters, sizeof(uint32_t) * 16) != cudaSuccess) st = PG_ERR_CUDA;
     if (!st && cudaMalloc(&sc->d_stats, sizeof(unsigned long long) * kNumStats) != cudaSuccess) st = PG_ERR_CUDA;
     if (st) return scene_error(st, "scene upload failed (CUDA)");
@@ -1174,6 +1249,61 @@ int pg_scene_load(const char *path, uint32_t width, uint32_t height, pg_scene **
     return create_common(sc, out);
 }
 
+int pg_scene_set_envmap(pg_scene *sc, const float *rgb, uint32_t width, uint32_t height) {
+    if (!sc || (!rgb && (width || height)) || (width == 0) != (height == 0)) return PG_ERR_ARG;
+    SceneData &s = sc->host;
+    s.env.assign(rgb, rgb + 3 * (size_t)width * height);
+    s.env_w = width;
+    s.env_h = height;
+    // the light table gains (or loses) the environment; device copies follow
+    auto &L = sc->h_lights;
+    if (!L.empty() && L.back().type == 2) L.pop_back();
+    if (width) {
+        DevLight e{};
+        e.type = 2;
+        L.push_back(e);
+    }
+    sc->n_lights = (uint32_t)L.size();
+    if (sc->uploaded) {
+        cudaFree(sc->d_env);
+        cudaFree(sc->d_lights);
+        sc->d_env = nullptr;
+        sc->d_lights = nullptr;
+        int st = upload(&sc->d_env, s.env);
+        if (!st) st = upload(&sc->d_lights, L);
+        if (st) return scene_error(st, "environment upload failed (CUDA)");
+    }
+    return PG_OK;
+}
+
+int pg_scene_get_envmap(const pg_scene *sc, float *rgb_out, uint32_t *width, uint32_t *height) {
+    if (!sc) return PG_ERR_ARG;
+    if (width) *width = sc->host.env_w;
+    if (height) *height = sc->host.env_h;
+    if (rgb_out && !sc->host.env.empty()) memcpy(rgb_out, sc->host.env.data(), sizeof(float) * sc->host.env.size());
+    return PG_OK;
+}
+
+int pg_exr_read(const char *path, float *rgb_out, uint64_t capacity, uint32_t *width, uint32_t *height) {
+    if (!path || !width || !height) return PG_ERR_ARG;
+    ExrImage img;
+    std::string err;
+    if (!read_exr(path, img, err)) return scene_error(err.rfind("cannot open", 0) == 0 ? PG_ERR_IO : PG_ERR_PARSE, err);
+    *width = img.width;
+    *height = img.height;
+    if (!rgb_out) return PG_OK;
+    if (capacity < img.rgb.size()) return scene_error(PG_ERR_ARG, "EXR image larger than the buffer");
+    memcpy(rgb_out, img.rgb.data(), sizeof(float) * img.rgb.size());
+    return PG_OK;
+}
+
+int pg_exr_write(const char *path, const float *rgb, uint32_t width, uint32_t height) {
+    if (!path || !rgb || !width || !height) return PG_ERR_ARG;
+    std::string err;
+    if (!write_exr(path, rgb, width, height, err)) return scene_error(PG_ERR_IO, err);
+    return PG_OK;
+}
+
 int pg_scene_destroy(pg_scene *sc) {
     if (!sc) return PG_OK;
     cudaFree(sc->d_nodes);
@@ -1187,6 +1317,7 @@ int pg_scene_destroy(pg_scene *sc) {
     cudaFree(sc->d_light_tris);
     cudaFree(sc->d_light_cdf);
     cudaFree(sc->d_tri_light);
+    cudaFree(sc->d_env);
     cudaFree(sc->d_stats);
     cudaFree(sc->d_counters);
     for (void *b : sc->bufs) cudaFree(b);
@@ -1320,6 +1451,9 @@ int pg_render(pg_scene *sc, const pg_render_params *rp, pg_ctx *guide, float *im
     R.light_tris = sc->d_light_tris;
     R.light_cdf = sc->d_light_cdf;
     R.tri_light = sc->d_tri_light;
+    R.env = sc->d_env;
+    R.env_w = sc->host.env_w;
+    R.env_h = sc->host.env_h;
     R.cam = cam;
     {
         float f[3] = {cam.target[0] - cam.origin[0], cam.target[1] - cam.origin[1], cam.target[2] - cam.origin[2]};

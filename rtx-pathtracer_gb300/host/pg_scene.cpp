@@ -1,6 +1,7 @@
 // pg_scene.cpp - procedural scenes, OBJ / Mitsuba-XML subset loading and the
 // binned-SAH BVH builder (host side of the tracer).
 #include "pg_scene.h"
+#include "pg_exr.h"
 
 #include <math.h>
 #include <stdio.h>
@@ -832,6 +833,25 @@ bool load_mitsuba(SceneData &s, const std::string &path, uint32_t width, uint32_
     }
     for (auto &k : scene->kids)
         if (k.name == "bsdf" && k.attr.count("id")) named[k.attr.at("id")] = bsdf_material(s, k);
+    // SceneLoader::parseEnvMap (src/SceneLoader.cpp:370-401): an envmap emitter's EXR image
+    for (auto &k : scene->kids) {
+        if (k.name != "emitter" || !k.attr.count("type") || k.attr.at("type") != "envmap") continue;
+        const std::string file = read_string(k, "filename");
+        if (file.empty()) {
+            s.error = "envmap emitter without a filename";
+            return false;
+        }
+        ExrImage img;
+        std::string err;
+        if (!read_exr(file[0] == '/' ? file : dir + file, img, err)) {
+            s.error = err.rfind("cannot open", 0) == 0 ? err : "envmap: " + err;
+            return false;
+        }
+        s.env_w = img.width;
+        s.env_h = img.height;
+        s.env.swap(img.rgb);
+        break;
+    }
     for (auto &sh : scene->kids) {
         if (sh.name != "shape") continue;
         const std::string type = sh.attr.count("type") ? sh.attr.at("type") : "";

@@ -37,6 +37,9 @@ struct SceneData {
     std::vector<pg_material> mats;
     std::vector<pg_sphere> spheres;
     pg_camera camera{};
+    // environment map (the reference's envmap emitter): lat-long RGB, row 0 = up
+    uint32_t env_w = 0, env_h = 0;
+    std::vector<float> env;
     // built
     std::vector<BvhNode> nodes;
     std::vector<float> tri_verts;  // 12 floats per triangle in BVH order: v0.xyz id, v1.xyz 0, v2.xyz 0

@@ -73,3 +73,9 @@ def test_guided_and_plain_renders(exe, tmp_path, cuda, pkg, abi):
     ref = img.cpu().numpy().reshape(H, W, 3) / 1024
     for mode in ("guided", "plain", "split"):
         assert abs(out[mode][0].mean() - ref.mean()) / ref.mean() < 0.03, mode
+    # the same plain render written as OpenEXR (writeEXR) holds the same pixels
+    exr = tmp_path / "plain.exr"
+    r = subprocess.run([str(exe), str(W), str(H), "0", "8", "cornell", "--spp", "256", "--no-guiding", "--out",
+                        str(exr)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    np.testing.assert_array_equal(pkg.read_exr(exr), out["plain"][0])

@@ -71,3 +71,35 @@ def test_materials_guided_same_seed(scene, cuda, pkg, abi, tracer):
     want = tracer.render(sc.export(), params, guide=guide)
     assert_same_seed_parity(got, want, "materials guided")
     ctx.close()
+
+
+@pytest.mark.parametrize("nee,mis", [(1, 1), (0, 0), (1, 0)])
+def test_envmap_same_seed(nee, mis, scene, cuda, abi, tracer):
+    """The environment map lights misses and is sampled by NEE (a uniform
+    direction in the hemisphere), MIS-weighted like the other lights."""
+    from test_exr import sky
+    sc = scene(48, 36)
+    sc.set_envmap(sky())
+    params = abi.render_params(spp=4, max_depth=8, seed=23, use_nee=nee, use_mis=mis)
+    got, _ = render_gpu(cuda, sc, params)
+    want = tracer.render(sc.export(), params)
+    assert_same_seed_parity(got, want, f"envmap nee={nee} mis={mis}")
+
+
+def test_envmap_estimators_converge(scene, cuda, abi, tracer):
+    from test_exr import sky
+    sc = scene(32, 24)
+    sc.set_envmap(sky())
+    spp = 2048
+    imgs = {}
+    for name, nee, mis in (("bsdf", 0, 0), ("nee", 1, 0), ("mis", 1, 1)):
+        imgs[name], _ = render_gpu(cuda, sc, abi.render_params(spp=spp, max_depth=8, seed=41, use_nee=nee,
+                                                               use_mis=mis))
+        imgs[name] /= spp
+    ref = tracer.render(sc.export(), abi.render_params(spp=512, max_depth=8, seed=97)) / 512
+    m = ref.mean()
+    blk = lambda x: x.reshape(3, 8, 4, 8, 3).mean(axis=(1, 3))
+    for name, img in imgs.items():
+        assert abs(img.mean() - m) / m < 0.03, f"{name}: mean {img.mean()} vs f64 {m}"
+        rel = np.abs(blk(img) - blk(ref)) / (blk(ref) + 0.05 * m)
+        assert rel.max() < 0.15, f"{name}: block rel err {rel.max():.3f}"
