@@ -756,23 +756,22 @@ def main():
         ms = float(t.item())
     value = si_per_step * world / (ms * 1e-3) / 1e6
 
-    # e2e through the public API: H2D of the step's inputs, fit, D2H of the states
+    # e2e through the public API: the fit from pinned HOST samples (pg_fit_regions_host:
+    # the H2D copy of the step's samples and offsets, then the fit), then the D2H read
+    # of the fitted states
     h2d = dirw_h.numel() * 4 + offs_h.numel() * 4
     d2h = R * abi.STATE_DTYPE.itemsize
+    offs_np = offs_h  # pinned: the offsets copy is asynchronous too
     with torch.cuda.stream(stream):
         for _ in range(max(1, args.warmup)):
-            dirw_d.copy_(dirw_h, non_blocking=True)
-            offs_d.copy_(offs_h, non_blocking=True)
-            ctx.fit(dirw_d, offs_d, R, abi.PG_FIT_INIT, stream=stream)
+            ctx.fit_host(dirw_h, offs_np, R, abi.PG_FIT_INIT, stream=stream)
             ctx.states(R, stream=stream)
     torch.cuda.synchronize()
     e2e_steps = max(1, min(args.steps, 5))
     t0 = time.perf_counter()
     with torch.cuda.stream(stream):
         for _ in range(e2e_steps):
-            dirw_d.copy_(dirw_h, non_blocking=True)
-            offs_d.copy_(offs_h, non_blocking=True)
-            ctx.fit(dirw_d, offs_d, R, abi.PG_FIT_INIT, stream=stream)
+            ctx.fit_host(dirw_h, offs_np, R, abi.PG_FIT_INIT, stream=stream)
             ctx.states(R, stream=stream)  # D2H of the fitted states + stream sync
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
     e2e_value = si_per_step * world / (e2e_ms * 1e-3) / 1e6

@@ -188,6 +188,19 @@ int pg_region_states_device(pg_ctx *ctx, pg_region_state **dev_out);
 int pg_fit_regions(pg_ctx *ctx, const float *dirw, const uint32_t *offsets,
                    uint32_t n_regions, int mode, void *stream);
 
+/* VMMFactory::fit / updateFit over regions whose samples are in HOST memory
+ * (the reference fits the host copy of the records, src/PathGuiding.cpp:
+ * 276-312): dirw_host holds float4 {direction, weight} per sample grouped by
+ * region, offsets_host n_regions + 1 sample offsets.  The samples go to a
+ * context-owned device buffer on a copy stream that starts behind the work
+ * already queued on `stream`, then the fit runs on `stream` (page-locked host
+ * memory copies asynchronously; pageable memory works through staging).
+ * Same results as pg_fit_regions on the same samples; the states stay on the
+ * device (pg_get_region_states).  Both buffers must stay valid until the
+ * stream reaches the fit. */
+int pg_fit_regions_host(pg_ctx *ctx, const float *dirw_host, const uint32_t *offsets_host, uint32_t n_regions,
+                        int mode, void *stream);
+
 /* Weighted log-likelihood sum_n w_n log p(d_n) of each region's samples under
  * the current mixtures (the quantity of VMMFactory.h:531-532), written as
  * double to ll_out (device, n_regions entries). */

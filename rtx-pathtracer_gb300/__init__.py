@@ -54,6 +54,7 @@ SIGNATURES = {
     "pg_fit_graph_launch": (_I, [_P, _P]),
     "pg_fit_graph_destroy": (_I, [_P]),
     "pg_fit_regions_noalloc": (_I, [C.POINTER(abi.FitConfig), _P, _P, _P, _U32, _I, _P]),
+    "pg_fit_regions_host": (_I, [_P, _P, _P, _U32, _I, _P]),
     "pg_default_split_merge_config": (None, [C.POINTER(abi.SplitMergeConfig)]),
     "pg_set_split_merge": (_I, [_P, C.POINTER(abi.SplitMergeConfig)]),
     "pg_split_merge": (_I, [_P, _P, _P, _P, _U32, _P]),
@@ -187,6 +188,17 @@ class FitContext:
         """Fits regions [0, n_regions).  dirw: device float4 per sample; offsets: device uint32 (n+1)."""
         self._check(self.lib.pg_fit_regions(self.h, _dptr(dirw), _dptr(offsets), n_regions, mode,
                                             _stream_handle(stream)))
+
+    def fit_host(self, dirw, offsets, n_regions: int, mode: int = abi.PG_FIT_INIT, stream=None):
+        """pg_fit_regions_host: the fit from HOST samples (a pinned torch tensor
+        or a numpy array), copied on the context's copy stream.  The arrays
+        must stay alive until the stream has run the fit."""
+        def hptr(x):
+            if isinstance(x, np.ndarray):
+                return x.ctypes.data
+            return _dptr(x)
+        self._check(self.lib.pg_fit_regions_host(self.h, hptr(dirw), hptr(offsets), n_regions, mode,
+                                                 _stream_handle(stream)))
 
     def eval_loglik(self, dirw, offsets, n_regions: int, ll_out, stream=None):
         self._check(self.lib.pg_eval_loglik(self.h, _dptr(dirw), _dptr(offsets), n_regions, _dptr(ll_out),

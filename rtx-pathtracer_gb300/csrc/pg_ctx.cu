@@ -127,6 +127,11 @@ int pg_ctx_destroy(pg_ctx *ctx) {
     if (!ctx) return PG_OK;
     guide_release(ctx);
     extras_release(ctx);
+    cudaFree(ctx->h2d_dirw);
+    cudaFree(ctx->h2d_offsets);
+    if (ctx->h2d_stream) cudaStreamDestroy(ctx->h2d_stream);
+    for (cudaEvent_t e : ctx->h2d_events)
+        if (e) cudaEventDestroy(e);
     cudaFree(ctx->d_states);
     cudaFree(ctx->d_order);
     cudaFree(ctx->d_counters);

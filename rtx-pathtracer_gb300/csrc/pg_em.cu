@@ -1,5 +1,7 @@
 // pg_em.cu - host side of the batched EM fit (C ABI entry points), the
 // largest-first region ordering and the log-likelihood evaluation kernel.
+#include <algorithm>
+
 #include "pg_em_kernels.cuh"
 
 namespace pg {
@@ -79,17 +81,16 @@ int pg_init_regions(pg_ctx *ctx, uint32_t n_regions, void *stream) {
     return st;
 }
 
-int pg_fit_regions(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t n_regions, int mode,
-                   void *stream) {
-    if (!ctx) return PG_ERR_ARG;
-    if (!dirw || !offsets) return set_error(ctx, PG_ERR_ARG, "null sample or offset pointer");
-    if ((reinterpret_cast<uintptr_t>(dirw) & 15u) != 0) return set_error(ctx, PG_ERR_ARG, "dirw must be 16-byte aligned");
-    if (n_regions > ctx->max_regions) return set_error(ctx, PG_ERR_ARG, "n_regions exceeds context capacity");
-    if (mode != PG_FIT_INIT && mode != PG_FIT_CONTINUE && mode != PG_FIT_UPDATE)
-        return set_error(ctx, PG_ERR_ARG, "unknown fit mode");
+}  // extern "C"
+
+namespace pg {
+
+// The fit of regions [first, first + n_regions): offsets points at region
+// first's entry, the states written are first's onwards.
+int fit_range(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t first, uint32_t n_regions, int mode,
+              cudaStream_t s) {
     ctx->last_launches = 0;
     if (n_regions == 0) return PG_OK;
-    cudaStream_t s = (cudaStream_t)stream;
     int st = upload_init_table(ctx, s);
     if (st) return st;
     st = check_cuda(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(uint32_t) * 4, s), "queue reset");
@@ -106,7 +107,7 @@ int pg_fit_regions(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint
     st = check_cuda(ctx, cudaGetLastError(), "order_regions launch");
     if (st) return st;
     EmArgs args;
-    args.states = ctx->d_states;
+    args.states = ctx->d_states + first;
     args.dirw = reinterpret_cast<const float4 *>(dirw);
     args.offsets = offsets;
     args.order = ctx->d_order;
@@ -128,6 +129,71 @@ int pg_fit_regions(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint
     if (st) return st;
     ctx->last_launches = 2;
     return PG_OK;
+}
+
+}  // namespace pg
+
+extern "C" {
+
+int pg_fit_regions(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t n_regions, int mode,
+                   void *stream) {
+    if (!ctx) return PG_ERR_ARG;
+    if (!dirw || !offsets) return set_error(ctx, PG_ERR_ARG, "null sample or offset pointer");
+    if ((reinterpret_cast<uintptr_t>(dirw) & 15u) != 0) return set_error(ctx, PG_ERR_ARG, "dirw must be 16-byte aligned");
+    if (n_regions > ctx->max_regions) return set_error(ctx, PG_ERR_ARG, "n_regions exceeds context capacity");
+    if (mode != PG_FIT_INIT && mode != PG_FIT_CONTINUE && mode != PG_FIT_UPDATE)
+        return set_error(ctx, PG_ERR_ARG, "unknown fit mode");
+    return fit_range(ctx, dirw, offsets, 0, n_regions, mode, (cudaStream_t)stream);
+}
+
+int pg_fit_regions_host(pg_ctx *ctx, const float *dirw_host, const uint32_t *offsets_host, uint32_t n_regions,
+                        int mode, void *stream) {
+    if (!ctx) return PG_ERR_ARG;
+    if (!dirw_host || !offsets_host) return set_error(ctx, PG_ERR_ARG, "null sample or offset pointer");
+    if (n_regions > ctx->max_regions) return set_error(ctx, PG_ERR_ARG, "n_regions exceeds context capacity");
+    if (mode != PG_FIT_INIT && mode != PG_FIT_CONTINUE && mode != PG_FIT_UPDATE)
+        return set_error(ctx, PG_ERR_ARG, "unknown fit mode");
+    ctx->last_launches = 0;
+    if (n_regions == 0) return PG_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint64_t total = offsets_host[n_regions];
+    // device copies of the samples and offsets, and the copy stream
+    if (total > ctx->h2d_cap) {
+        cudaFree(ctx->h2d_dirw);
+        ctx->h2d_dirw = nullptr;
+        ctx->h2d_cap = 0;
+        if (int st = check_cuda(ctx, cudaMalloc(&ctx->h2d_dirw, sizeof(float4) * (total ? total : 1)), "host-fit samples"))
+            return st;
+        ctx->h2d_cap = total;
+    }
+    if (!ctx->h2d_offsets) {
+        if (int st = check_cuda(ctx, cudaMalloc(&ctx->h2d_offsets, sizeof(uint32_t) * ((size_t)ctx->max_regions + 1)),
+                                "host-fit offsets"))
+            return st;
+        int st = check_cuda(ctx, cudaStreamCreateWithFlags(&ctx->h2d_stream, cudaStreamNonBlocking), "copy stream");
+        for (int i = 0; !st && i < 2; ++i)
+            st = check_cuda(ctx, cudaEventCreateWithFlags(&ctx->h2d_events[i], cudaEventDisableTiming), "copy events");
+        if (st) return st;
+    }
+    int st = check_cuda(ctx, cudaMemcpyAsync(ctx->h2d_offsets, offsets_host, sizeof(uint32_t) * (n_regions + 1),
+                                             cudaMemcpyHostToDevice, s), "offsets upload");
+    // the copy stream starts after everything queued on the caller's stream
+    // (an earlier fit may still read the sample buffer)
+    if (!st) st = check_cuda(ctx, cudaEventRecord(ctx->h2d_events[1], s), "copy fork");
+    if (!st) st = check_cuda(ctx, cudaStreamWaitEvent(ctx->h2d_stream, ctx->h2d_events[1], 0), "copy fork");
+    if (st) return st;
+    // One copy, then one fit.  Fitting chunks of regions while later chunks
+    // copy was measured slower: every chunk's largest region adds its own
+    // tail, which costs more than the copy (about 200 GB/s from page-locked
+    // memory) that it hides.
+    if (total) {
+        st = check_cuda(ctx, cudaMemcpyAsync(ctx->h2d_dirw, dirw_host, sizeof(float4) * total, cudaMemcpyHostToDevice,
+                                             ctx->h2d_stream), "samples upload");
+        if (!st) st = check_cuda(ctx, cudaEventRecord(ctx->h2d_events[0], ctx->h2d_stream), "copy event");
+        if (!st) st = check_cuda(ctx, cudaStreamWaitEvent(s, ctx->h2d_events[0], 0), "copy join");
+        if (st) return st;
+    }
+    return fit_range(ctx, reinterpret_cast<const float *>(ctx->h2d_dirw), ctx->h2d_offsets, 0, n_regions, mode, s);
 }
 
 int pg_eval_loglik(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t n_regions, double *ll_out,

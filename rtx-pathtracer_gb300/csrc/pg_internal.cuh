@@ -35,6 +35,12 @@ struct pg_ctx {
     float init_kappa = -1.0f;
     uint32_t last_launches = 0;
     void *guide = nullptr;           // sort / parallax / distance scratch (pg_guide.cu)
+    // pg_fit_regions_host: device copies of host samples, filled on a copy stream
+    float4 *h2d_dirw = nullptr;
+    uint64_t h2d_cap = 0;
+    uint32_t *h2d_offsets = nullptr;
+    cudaStream_t h2d_stream = nullptr;
+    cudaEvent_t h2d_events[2] = {nullptr, nullptr};  // copy done, caller's stream fork
     pg_region_extra *d_extras = nullptr;  // split/merge statistics per region (pg_splitmerge.cu)
     cudaStream_t sm_aux = nullptr;        // split/merge: the clustered launch runs beside the per-CTA one
     cudaEvent_t sm_fork = nullptr, sm_join = nullptr;
@@ -49,6 +55,8 @@ int check_cuda(pg_ctx *ctx, cudaError_t e, const char *what);
 int upload_init_table(pg_ctx *ctx, cudaStream_t s);
 // region ids into ctx->d_order, largest sample count first; *n_large_out
 // (device) = regions in size buckets at or above large_threshold
+int fit_range(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t first, uint32_t n_regions, int mode,
+              cudaStream_t s);
 int order_regions(pg_ctx *ctx, const uint32_t *offsets, uint32_t n_regions, uint32_t large_threshold,
                   uint32_t *n_large_out, cudaStream_t s);
 void guide_release(pg_ctx *ctx);

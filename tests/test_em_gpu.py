@@ -181,3 +181,38 @@ def test_argument_errors(cuda, pkg, abi):
     with pytest.raises(pkg.PathGuideError):
         ctx.fit(d, o, 2, mode=7)
     ctx.close()
+
+
+@pytest.mark.parametrize("mode", ["init", "update"])
+def test_fit_from_host_memory_equals_device_fit(mode, cuda, pkg, abi, workloads):
+    """pg_fit_regions_host (the fit from host memory) gives the same states,
+    bit for bit, as pg_fit_regions on device copies of the samples."""
+    torch = cuda
+    w = workloads.fit_batched(seed=12, n_regions=300, median=3000, sigma=1.0, lo=64, hi=40000)
+    R = len(w["offsets"]) - 1
+    cfg = abi.default_fit_config(num_initial_components=8)
+    m = abi.PG_FIT_INIT if mode == "init" else abi.PG_FIT_UPDATE
+    start = None
+    if mode == "update":
+        start, _ = run_fit(cuda, pkg, cfg, w["dirw"], w["offsets"])
+    a_ctx = pkg.FitContext(cfg, max_regions=R)
+    b_ctx = pkg.FitContext(cfg, max_regions=R)
+    if start is not None:
+        a_ctx.set_states(start)
+        b_ctx.set_states(start)
+    d = torch.from_numpy(np.ascontiguousarray(w["dirw"], dtype=np.float32)).cuda()
+    o = torch.from_numpy(w["offsets"].astype(np.uint32).view(np.int32)).cuda()
+    a_ctx.fit(d, o, R, m)
+    dirw_h = torch.from_numpy(np.ascontiguousarray(w["dirw"], dtype=np.float32)).pin_memory()
+    offs_h = torch.from_numpy(w["offsets"].astype(np.uint32).view(np.int32)).pin_memory()
+    b_ctx.fit_host(dirw_h, offs_h, R, m)
+    a_ctx.sync()
+    b_ctx.sync()
+    assert a_ctx.states(R).tobytes() == b_ctx.states(R).tobytes()
+    # pageable numpy buffers work too
+    c_ctx = pkg.FitContext(cfg, max_regions=R)
+    if start is not None:
+        c_ctx.set_states(start)
+    c_ctx.fit_host(np.ascontiguousarray(w["dirw"], dtype=np.float32), w["offsets"].astype(np.uint32), R, m)
+    c_ctx.sync()
+    assert a_ctx.states(R).tobytes() == c_ctx.states(R).tobytes()
