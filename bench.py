@@ -611,6 +611,10 @@ def main():
     ap.add_argument("--cpt", type=int, default=0, help="components per thread (8 or 16)")
     ap.add_argument("--unroll", type=int, default=0)
     ap.add_argument("--large", type=int, default=0, help="samples above which a cluster shares a region")
+    ap.add_argument("--ctas-per-sm", type=int, default=0,
+                    help="resident CTAs per SM (3, 4: register-capped builds; 0: as many as fit)")
+    ap.add_argument("--stages", type=int, default=0,
+                    help="ring stages for slices streamed from L2 (0: library default)")
     ap.add_argument("--regions", type=int, default=0, help="override the region count (experiments)")
     ap.add_argument("--median", type=float, default=0.0, help="override the median region size")
     ap.add_argument("--sigma", type=float, default=-1.0, help="override the region-size sigma")
@@ -682,11 +686,13 @@ def main():
     offs_d = offs_h.to("cuda", non_blocking=False)
     fitted = counts > 2 * K
     si_per_step = int(counts[fitted].sum()) * ITERS  # regions with N <= 2K are not fitted
-    manual = any((args.threads, args.smem_samples, args.cluster, args.cpt, args.unroll, args.large))
+    manual = any((args.threads, args.smem_samples, args.cluster, args.cpt, args.unroll, args.large, args.stages,
+                  args.ctas_per_sm))
     tune_ms = None
     if manual or args.sweep:
         ctx.set_tuning(threads_per_cta=args.threads, smem_samples=args.smem_samples, cluster_size=args.cluster,
-                       components_per_thread=args.cpt, unroll=args.unroll, large_threshold=args.large)
+                       components_per_thread=args.cpt, unroll=args.unroll, large_threshold=args.large,
+                       stream_stages=args.stages, ctas_per_sm=args.ctas_per_sm)
         tuned = None
     else:
         # the project's autotuner picks the launch shape on this workload (untimed)
@@ -704,13 +710,18 @@ def main():
             ctx.fit(dirw_d, offs_d, R, abi.PG_FIT_INIT, stream=stream)
 
     if args.sweep:
-        grid = [(128, cl, cap, cpt, 2, T) for cpt in (16, 8) for cl in (2, 4, 8, 16)
-                for cap in (3072, 6144) for T in (0, 2048, 12288)]
-        for nt, cl, cap, cpt, u, T in grid:
-            point = {"threads": nt, "cluster": cl, "smem_samples": cap, "cpt": cpt, "unroll": u, "large": T}
+        # (ctas_per_sm, components per thread, unroll, staged samples): 0 = as many
+        # CTAs as fit; 3 and 4 select the register-capped builds
+        shapes = [(0, 16, 2, 6144), (3, 16, 2, 4096), (3, 16, 2, 3072), (4, 16, 1, 3072), (4, 16, 2, 3072),
+                  (4, 16, 1, 2048), (4, 16, 2, 2048), (4, 8, 4, 3072)]
+        grid = [(128, cl, cap, cpt, u, T, ns, cps) for cps, cpt, u, cap in shapes for cl in (2, 4)
+                for T in (12288, 24576) for ns in (2, 4)]
+        for nt, cl, cap, cpt, u, T, ns, cps in grid:
+            point = {"threads": nt, "cluster": cl, "smem_samples": cap, "cpt": cpt, "unroll": u, "large": T,
+                     "stages": ns, "ctas_per_sm": cps}
             try:
                 ctx.set_tuning(threads_per_cta=nt, smem_samples=cap, cluster_size=cl, components_per_thread=cpt,
-                               unroll=u, large_threshold=T)
+                               unroll=u, large_threshold=T, stream_stages=ns, ctas_per_sm=cps)
                 with torch.cuda.stream(stream):
                     step()
                 torch.cuda.synchronize()

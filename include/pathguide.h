@@ -211,12 +211,22 @@ int pg_eval_loglik(pg_ctx *ctx, const float *dirw, const uint32_t *offsets,
 typedef struct pg_fit_tuning {
     uint32_t threads_per_cta;       /* 128 or 256                               */
     uint32_t smem_samples;          /* samples kept in shared memory per CTA    */
-    uint32_t ctas_per_sm;           /* cap on resident CTAs per SM (0: maximum) */
+    uint32_t ctas_per_sm;           /* cap on resident CTAs per SM (0: maximum);
+                                       with 128 threads, 3 (16 components per
+                                       thread, unroll 2) and 4 (8 components per
+                                       thread) also cap the registers per thread
+                                       so that as many CTAs fit                 */
     uint32_t cluster_size;          /* CTAs sharing one large region: 1..16     */
     uint32_t components_per_thread; /* 8 or 16: K=16 mixtures use 2 or 1 threads per sample */
-    uint32_t unroll;                /* samples per loop trip: 1 or 2            */
+    uint32_t unroll;                /* samples per loop trip: 1, 2 or 4 (4: 128
+                                       threads per CTA)                         */
     uint32_t large_threshold;       /* regions with more samples are shared by a
                                        cluster (0: smem_samples)                */
+    uint32_t stream_stages;         /* slices larger than smem_samples stream
+                                       from L2 through a ring of this many
+                                       TMA-filled shared-memory stages (0: 2; at
+                                       most 8; fewer when a stage would hold
+                                       less than one E-step loop trip)          */
 } pg_fit_tuning;
 int pg_set_fit_tuning(pg_ctx *ctx, const pg_fit_tuning *t);
 int pg_get_fit_tuning(const pg_ctx *ctx, pg_fit_tuning *t);

@@ -176,9 +176,9 @@ class FitContext:
         self.cfg = cfg
 
     def set_tuning(self, threads_per_cta=0, smem_samples=0, ctas_per_sm=0, cluster_size=0,
-                   components_per_thread=0, unroll=0, large_threshold=0):
+                   components_per_thread=0, unroll=0, large_threshold=0, stream_stages=0):
         t = abi.FitTuning(threads_per_cta, smem_samples, ctas_per_sm, cluster_size, components_per_thread, unroll,
-                          large_threshold)
+                          large_threshold, stream_stages)
         self._check(self.lib.pg_set_fit_tuning(self.h, C.byref(t)))
 
     def init_regions(self, n_regions: int, stream=None):

@@ -47,7 +47,7 @@ class FitTuning(C.Structure):
     _fields_ = [("threads_per_cta", C.c_uint32), ("smem_samples", C.c_uint32),
                 ("ctas_per_sm", C.c_uint32), ("cluster_size", C.c_uint32),
                 ("components_per_thread", C.c_uint32), ("unroll", C.c_uint32),
-                ("large_threshold", C.c_uint32)]
+                ("large_threshold", C.c_uint32), ("stream_stages", C.c_uint32)]
 
 
 def default_fit_config(**kw) -> FitConfig:

@@ -215,7 +215,10 @@ int pg_set_fit_tuning(pg_ctx *ctx, const pg_fit_tuning *t) {
     if (t->cluster_size > 16) return set_error(ctx, PG_ERR_ARG, "cluster_size must be <= 16");
     if (t->components_per_thread && t->components_per_thread != 8 && t->components_per_thread != 16)
         return set_error(ctx, PG_ERR_ARG, "components_per_thread must be 8 or 16");
-    if (t->unroll > 2) return set_error(ctx, PG_ERR_ARG, "unroll must be 1 or 2");
+    if (t->unroll > 2 && t->unroll != 4) return set_error(ctx, PG_ERR_ARG, "unroll must be 1, 2 or 4");
+    if (t->unroll == 4 && t->threads_per_cta && t->threads_per_cta != 128)
+        return set_error(ctx, PG_ERR_ARG, "unroll 4 needs 128 threads per CTA");
+    if (t->stream_stages > 8) return set_error(ctx, PG_ERR_ARG, "stream_stages must be <= 8");
     ctx->tuning = *t;
     return PG_OK;
 }

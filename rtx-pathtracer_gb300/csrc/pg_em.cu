@@ -97,12 +97,13 @@ int fit_range(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t 
     if (st) return st;
     const pg_fit_tuning &t = ctx->tuning;
     // Defaults: the best point of the tuning sweep on the 4096-region K=16
-    // workload (pairs of CTAs share regions above 12288 samples, 6144 samples
-    // staged per CTA, one thread per sample, two samples per loop trip).
+    // workload (pairs of CTAs share regions above 24576 samples, 4096 samples
+    // staged per CTA in a two-stage ring when streamed, one thread per sample,
+    // two samples per loop trip, three CTAs per SM).
     const uint32_t cluster = t.cluster_size ? t.cluster_size : 2u;
-    const uint32_t cap = t.smem_samples ? t.smem_samples : 6144u;
+    const uint32_t cap = t.smem_samples ? t.smem_samples : 4096u;
     const uint32_t large_threshold =
-        cluster > 1 ? (t.large_threshold ? t.large_threshold : 12288u) : 0xFFFFFFFFu;
+        cluster > 1 ? (t.large_threshold ? t.large_threshold : 24576u) : 0xFFFFFFFFu;
     order_regions_kernel<128><<<1, 1024, 0, s>>>(offsets, n_regions, ctx->d_order, large_threshold, ctx->d_counters + 3);
     st = check_cuda(ctx, cudaGetLastError(), "order_regions launch");
     if (st) return st;
@@ -121,6 +122,7 @@ int fit_range(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t 
     args.mode = mode;
     args.ll_out = nullptr;
     args.smem_cap = cap;
+    args.stages = t.stream_stages ? t.stream_stages : 2u;
     const uint32_t K = ctx->cfg.num_initial_components;
     // The component count of an existing state is read from the state; size
     // for the widest case unless the mixtures are initialised here.

@@ -9,6 +9,7 @@ int launch_fit_k8(pg_ctx *ctx, const EmArgs &args, cudaStream_t s, const pg_fit_
     const uint32_t cps = t.ctas_per_sm;
     if (nt == 256) return u == 2 ? launch_fit<8, 256, 8, 2>(ctx, args, s, cps, cluster)
                                  : launch_fit<8, 256, 8, 1>(ctx, args, s, cps, cluster);
+    if (u == 4) return launch_fit<8, 128, 8, 4>(ctx, args, s, cps, cluster);
     return u == 2 ? launch_fit<8, 128, 8, 2>(ctx, args, s, cps, cluster)
                   : launch_fit<8, 128, 8, 1>(ctx, args, s, cps, cluster);
 }

@@ -7,8 +7,10 @@
 // the GPU without a host round trip.  Per region, a CTA:
 //   1. stages the region's float4 {direction.xyz, weight} samples into shared
 //      memory with 1-D TMA bulk copies (cp.async.bulk, mbarrier completion) and
-//      keeps them resident across all EM iterations (regions larger than the
-//      staging capacity stream through L2 with 128-bit loads each iteration);
+//      keeps them resident across all EM iterations; a slice larger than the
+//      staging capacity streams from L2 every iteration through a ring of
+//      TMA-filled stages, whose copies run ahead across iteration boundaries
+//      (the next iteration's first chunks load during the M-step);
 //   2. E-step: every thread evaluates all K components for its samples with
 //      packed FP32x2 FMAs - the exponent of pi_k * vMF_k(d) is folded into one
 //      affine form kappa_k log2(e) mu_k.d + log2(pi_k norm_k) - kappa_k log2(e),
@@ -58,11 +60,21 @@ struct EmArgs {
     double *ll_out;     // eval mode only
     uint32_t *large_counter;     // cluster work queue (largest regions)
     const uint32_t *n_large;     // number of regions fitted by a whole cluster
+    uint32_t stages;             // ring stages for streamed slices (>= 1)
+    uint32_t stage_n;            // samples per ring stage: a multiple of the E-step trip width
+};
+
+constexpr uint32_t kMaxStages = 8;
+
+// E-step constants of components 2j and 2j+1, laid out for two 128-bit and one
+// 64-bit broadcast load: {ax, ay}, {az, c0}, {cm}.
+struct __align__(16) ConstPair {
+    float ax[2], ay[2], az[2], c0[2], cm[2], pad[2];
 };
 
 template <int KMAX, int NW>
 struct EmShared {
-    float cax[KMAX], cay[KMAX], caz[KMAX], cc0[KMAX], ccm[KMAX];  // E-step constants
+    ConstPair cp[KMAX / 2];  // E-step constants
     float w[16], mx[16], my[16], mz[16], kap[16], rr[16], nrm[16], em2k[16];
     float osx[16], osy[16], osz[16], ow[16];  // statistics recovered from the prior mixture (updateFit)
     float red[NW][4 * KMAX];
@@ -74,6 +86,7 @@ struct EmShared {
     unsigned long long total;
     uint32_t K, max_itr, item, stop, nonfinite;
     unsigned long long bar;
+    unsigned long long ring_bar[kMaxStages];  // one per ring stage of a streamed slice
 };
 
 // E-step constants of component c from the model held in shared memory.
@@ -83,11 +96,13 @@ __device__ __forceinline__ void make_consts(EmShared<KMAX, NW> &S, int c, uint32
     const float kl = S.kap[c] * kLog2e;
     const float pn = S.w[c] * S.nrm[c];
     const float lw = (c < (int)K && pn > 0.0f) ? lg2_approx(pn) : -INFINITY;
-    S.cax[c] = kl * S.mx[c];
-    S.cay[c] = kl * S.my[c];
-    S.caz[c] = kl * S.mz[c];
-    S.cc0[c] = lw - kl;
-    S.ccm[c] = lw;
+    ConstPair &q = S.cp[c >> 1];
+    const int i = c & 1;
+    q.ax[i] = kl * S.mx[c];
+    q.ay[i] = kl * S.my[c];
+    q.az[i] = kl * S.mz[c];
+    q.c0[i] = lw - kl;
+    q.cm[i] = lw;
 }
 
 __device__ __forceinline__ void reset_component(float &w, float &mx, float &my, float &mz, float &k, float &r,
@@ -280,11 +295,12 @@ __device__ __forceinline__ void estep_sample(float4 s, bool count_totals, const 
     }
 }
 
-// E-step over n samples of src: thread pairs (TPS = 2) or single threads share
-// a sample; U samples per loop trip for instruction-level parallelism.  The trip
+// E-step over n samples of src (shared memory): thread pairs (TPS = 2) or single
+// threads share a sample; U samples per loop trip for instruction-level
+// parallelism.  The trip
 // count is the same for every thread of the CTA, so the pair shuffle is always
 // executed by full warps; samples past n enter with zero weight.
-template <int CPT, int TPS, int U, bool kShared>
+template <int CPT, int TPS, int U>
 __device__ __forceinline__ void estep(const float4 *__restrict__ src, uint32_t n, int tid, int nt,
                                       const float2 (&AX)[CPT / 2], const float2 (&AY)[CPT / 2],
                                       const float2 (&AZ)[CPT / 2], const float2 (&C0)[CPT / 2],
@@ -299,13 +315,95 @@ __device__ __forceinline__ void estep(const float4 *__restrict__ src, uint32_t n
         for (int u = 0; u < U; ++u) {
             const uint32_t idx = i0 + g + (uint32_t)u * stride;
             if (idx < n)
-                sm[u] = kShared ? src[idx] : __ldg(src + idx);
+                sm[u] = src[idx];
             else
                 sm[u] = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
         }
 #pragma unroll
         for (int u = 0; u < U; ++u)
             estep_sample<CPT, TPS>(sm[u], lead, AX, AY, AZ, C0, CM, SX, SY, SZ, SW, ll, sw);
+    }
+}
+
+// Shared-memory loads kept in place: the loop-invariant constants are re-read
+// every trip instead of being hoisted into registers.
+__device__ __forceinline__ float4 lds_f4(const float *p) {
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"(smem_u32(p)));
+    return v;
+}
+__device__ __forceinline__ float2 lds_f2(const float *p) {
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(smem_u32(p)));
+    return v;
+}
+
+// The E-step with the constants read from shared memory (broadcast loads, once
+// per pair of components per loop trip of U samples) instead of held in
+// registers: the same arithmetic in the same order, about 80 fewer registers
+// per thread, so more CTAs fit on an SM.
+template <int CPT, int TPS, int U>
+__device__ __forceinline__ void estep_sc(const float4 *__restrict__ src, uint32_t n, int tid, int nt,
+                                         const ConstPair *__restrict__ cpb, float2 (&SX)[CPT / 2],
+                                         float2 (&SY)[CPT / 2], float2 (&SZ)[CPT / 2], float2 (&SW)[CPT / 2],
+                                         float &ll, float &sw) {
+    const uint32_t g = (uint32_t)tid / TPS;
+    const uint32_t stride = (uint32_t)nt / TPS;
+    const bool lead = (tid % TPS) == 0;
+    for (uint32_t i0 = 0; i0 < n; i0 += stride * U) {
+        float4 sm[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint32_t idx = i0 + g + (uint32_t)u * stride;
+            sm[u] = idx < n ? src[idx] : make_float4(0.0f, 0.0f, 1.0f, 0.0f);
+        }
+        float v[U][CPT];
+        float2 p2[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) p2[u] = make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int j = 0; j < CPT / 2; ++j) {
+            const float4 qa = lds_f4(cpb[j].ax);  // ax0 ax1 ay0 ay1
+            const float4 qb = lds_f4(cpb[j].az);  // az0 az1 c00 c01
+            const float2 qm = lds_f2(cpb[j].cm);
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                float2 t = __ffma2_rn(make_float2(qb.x, qb.y), make_float2(sm[u].z, sm[u].z),
+                                      make_float2(qb.z, qb.w));
+                t = __ffma2_rn(make_float2(qa.z, qa.w), make_float2(sm[u].y, sm[u].y), t);
+                t = __ffma2_rn(make_float2(qa.x, qa.y), make_float2(sm[u].x, sm[u].x), t);
+                v[u][2 * j] = ex2_approx(fminf(t.x, qm.x));
+                v[u][2 * j + 1] = ex2_approx(fminf(t.y, qm.y));
+                p2[u] = __fadd2_rn(p2[u], make_float2(v[u][2 * j], v[u][2 * j + 1]));
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const float4 s = sm[u];
+            float p = p2[u].x + p2[u].y;
+            if (TPS == 2) p += __shfl_xor_sync(0xffffffffu, p, 1);
+            const bool valid = p > kPmmEps;
+            const float wt = s.w;
+            const float sc = valid ? wt * rcp_approx(p) : 0.0f;
+            if (lead) {
+                ll = valid ? fmaf(wt, lg2_approx(p), ll) : ll;
+                sw = valid ? sw + wt : sw;
+            }
+            const float2 sx = make_float2(sc * s.x, sc * s.x);
+            const float2 sy = make_float2(sc * s.y, sc * s.y);
+            const float2 sz = make_float2(sc * s.z, sc * s.z);
+            const float2 s2 = make_float2(sc, sc);
+#pragma unroll
+            for (int j = 0; j < CPT / 2; ++j) {
+                const float2 vv = make_float2(v[u][2 * j], v[u][2 * j + 1]);
+                SX[j] = __ffma2_rn(vv, sx, SX[j]);
+                SY[j] = __ffma2_rn(vv, sy, SY[j]);
+                SZ[j] = __ffma2_rn(vv, sz, SZ[j]);
+                SW[j] = __ffma2_rn(vv, s2, SW[j]);
+            }
+        }
     }
 }
 
@@ -522,13 +620,10 @@ __device__ void store_model(const EmArgs &a, EmShared<KMAX, NW> &S, pg_region_st
 template <int KMAX, int NW>
 __device__ __forceinline__ void pull_consts(cg::cluster_group &cluster, EmShared<KMAX, NW> &S, int lane) {
     EmShared<KMAX, NW> *R0 = cluster.map_shared_rank(&S, 0);
-    if (lane < KMAX) {
-        S.cax[lane] = R0->cax[lane];
-        S.cay[lane] = R0->cay[lane];
-        S.caz[lane] = R0->caz[lane];
-        S.cc0[lane] = R0->cc0[lane];
-        S.ccm[lane] = R0->ccm[lane];
-    }
+    constexpr int kWords = (int)sizeof(S.cp) / 4;
+    const float *src = reinterpret_cast<const float *>(R0->cp);
+    float *dst = reinterpret_cast<float *>(S.cp);
+    for (int i = lane; i < kWords; i += 32) dst[i] = src[i];
     if (lane == 0) {
         S.K = R0->K;
         S.max_itr = R0->max_itr;
@@ -538,9 +633,27 @@ __device__ __forceinline__ void pull_consts(cg::cluster_group &cluster, EmShared
 
 // One region (or, in a cluster, this CTA's slice of one region): stage the
 // samples, iterate E-step / reduction / M-step, store the mixture.
-template <int KMAX, int NT, bool kCluster, int CPT, int U>
+// Issues ring use q of a streamed slice [sb, sb + n_local): chunk q mod nch of
+// stage_n samples into stage (g0 + q) mod stages, completing on that stage's
+// mbarrier.  One thread; the stage's previous readers have passed a CTA barrier.
+template <int KMAX, int NW>
+__device__ __forceinline__ void ring_issue(const EmArgs &a, EmShared<KMAX, NW> &S, float4 *s_samp, uint32_t sb,
+                                           uint32_t n_local, uint32_t nch, uint32_t g0, uint32_t q) {
+    const uint32_t stage_n = a.stage_n;
+    const uint32_t c = q % nch;
+    const uint32_t stg = (g0 + q) % a.stages;
+    const uint32_t n0 = c * stage_n;
+    const uint32_t bytes = min(stage_n, n_local - n0) * 16u;
+    uint64_t *rb = reinterpret_cast<uint64_t *>(&S.ring_bar[stg]);
+    mbar_arrive_expect_tx(rb, bytes);
+    const char *src = reinterpret_cast<const char *>(a.dirw + sb + n0);
+    char *dst = reinterpret_cast<char *>(s_samp + (size_t)stg * stage_n);
+    for (uint32_t off = 0; off < bytes; off += 32768u) tma_bulk_g2s(dst + off, src + off, min(32768u, bytes - off), rb);
+}
+
+template <int KMAX, int NT, bool kCluster, int CPT, int U, bool SC>
 __device__ void process_region(const EmArgs &a, EmShared<KMAX, NT / 32> &S, float4 *s_samp, uint64_t *bar,
-                               uint32_t &phase, uint32_t item, cg::cluster_group &cluster) {
+                               uint32_t &phase, uint32_t &ring_pos, uint32_t item, cg::cluster_group &cluster) {
     constexpr int NW = NT / 32;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t crank = kCluster ? cluster.block_rank() : 0u;
@@ -583,29 +696,74 @@ __device__ void process_region(const EmArgs &a, EmShared<KMAX, NT / 32> &S, floa
     uint32_t it = 0;
     constexpr int TPS = KMAX / CPT;  // threads per sample
     const int h = tid % TPS;         // this thread's component block
+    // A slice larger than the staging capacity streams through a ring of
+    // a.stages stages of stage_n samples.  stage_n is a multiple of the E-step's
+    // trip width (NT / TPS threads x U samples), so every thread meets the same
+    // samples in the same order as in one pass over the slice.  Ring use q
+    // (chunk q mod nch of iteration q / nch) lives in stage (ring_pos + q) mod
+    // stages and completes phase ((ring_pos + q) / stages) & 1 of that stage's
+    // mbarrier; ring_pos carries over from region to region so the phases stay
+    // in step.  A resident slice is one "chunk" that stays in place.
+    const uint32_t stages = a.stages, stage_n = a.stage_n;
+    const bool ring = !resident && max_itr > 0;  // then n_local > smem_cap >= stage_n > 0
+    const uint32_t nch = ring ? (n_local + stage_n - 1) / stage_n : 1u;
+    const unsigned long long uses = ring ? (unsigned long long)nch * max_itr : 0ull;
+    uint32_t consumed = 0;  // ring uses completed
+    if (ring && tid == 0) {
+        fence_proxy_async_smem();
+        const uint32_t first = (uint32_t)min(uses, (unsigned long long)stages);
+        for (uint32_t q = 0; q < first; ++q) ring_issue(a, S, s_samp, sb, n_local, nch, ring_pos, q);
+    }
     for (; it < max_itr; ++it) {
         float2 AX[CPT / 2], AY[CPT / 2], AZ[CPT / 2], C0[CPT / 2];
         float CM[CPT];
+        const ConstPair *cpb = S.cp + h * (CPT / 2);  // this thread's component block
+        if constexpr (!SC) {
 #pragma unroll
-        for (int j = 0; j < CPT / 2; ++j) {
-            const int c = h * CPT + 2 * j;
-            AX[j] = make_float2(S.cax[c], S.cax[c + 1]);
-            AY[j] = make_float2(S.cay[c], S.cay[c + 1]);
-            AZ[j] = make_float2(S.caz[c], S.caz[c + 1]);
-            C0[j] = make_float2(S.cc0[c], S.cc0[c + 1]);
-            CM[2 * j] = S.ccm[c];
-            CM[2 * j + 1] = S.ccm[c + 1];
+            for (int j = 0; j < CPT / 2; ++j) {
+                const ConstPair &q = cpb[j];
+                AX[j] = make_float2(q.ax[0], q.ax[1]);
+                AY[j] = make_float2(q.ay[0], q.ay[1]);
+                AZ[j] = make_float2(q.az[0], q.az[1]);
+                C0[j] = make_float2(q.c0[0], q.c0[1]);
+                CM[2 * j] = q.cm[0];
+                CM[2 * j + 1] = q.cm[1];
+            }
         }
         float2 SX[CPT / 2], SY[CPT / 2], SZ[CPT / 2], SW[CPT / 2];
 #pragma unroll
         for (int j = 0; j < CPT / 2; ++j) SX[j] = SY[j] = SZ[j] = SW[j] = make_float2(0.0f, 0.0f);
         float ll = 0.0f, sw = 0.0f;
-        if (ok) {
-            if (resident)
-                estep<CPT, TPS, U, true>(s_samp, n_local, tid, NT, AX, AY, AZ, C0, CM, SX, SY, SZ, SW, ll, sw);
-            else
-                estep<CPT, TPS, U, false>(a.dirw + sb, n_local, tid, NT, AX, AY, AZ, C0, CM, SX, SY, SZ, SW, ll,
-                                          sw);
+        for (uint32_t c = 0; c < nch && ok; ++c) {
+            const float4 *src = s_samp;
+            uint32_t n = n_local;
+            bool got = true;
+            if (ring) {
+                const uint32_t g = ring_pos + consumed;
+                const uint32_t stg = g % stages;
+                got = mbar_wait_bounded(reinterpret_cast<uint64_t *>(&S.ring_bar[stg]), (g / stages) & 1u,
+                                        a.error_word);
+                src = s_samp + (size_t)stg * stage_n;
+                n = min(stage_n, n_local - c * stage_n);
+            }
+            if (got) {
+                if constexpr (SC)
+                    estep_sc<CPT, TPS, U>(src, n, tid, NT, cpb, SX, SY, SZ, SW, ll, sw);
+                else
+                    estep<CPT, TPS, U>(src, n, tid, NT, AX, AY, AZ, C0, CM, SX, SY, SZ, SW, ll, sw);
+            }
+            if (ring) {
+                // Every thread is done with the stage: refill it with use consumed + stages.
+                if (__syncthreads_or(!got)) {  // a copy timed out: stop streaming (reported)
+                    ok = false;
+                    break;
+                }
+                if ((unsigned long long)consumed + stages < uses && tid == 0) {
+                    fence_proxy_async_smem();
+                    ring_issue(a, S, s_samp, sb, n_local, nch, ring_pos, consumed + stages);
+                }
+                ++consumed;
+            }
         }
         float f[4 * CPT];
 #pragma unroll
@@ -686,12 +844,26 @@ __device__ void process_region(const EmArgs &a, EmShared<KMAX, NT / 32> &S, floa
         }
         if (S.stop) break;
     }
+    if (ring) {
+        // An early stop leaves copies in flight: let them land before the
+        // shared memory is reused, so every issued use completes its phase.
+        const uint32_t issued = (uint32_t)min(uses, (unsigned long long)consumed + stages);
+        if (tid == 0)
+            for (uint32_t q = consumed; q < issued; ++q) {
+                const uint32_t g = ring_pos + q;
+                mbar_wait_bounded(reinterpret_cast<uint64_t *>(&S.ring_bar[g % stages]), (g / stages) & 1u,
+                                  a.error_word);
+            }
+        ring_pos += issued;
+    }
     if (owner && warp == 0) store_model(a, S, st, lane, it);
     __syncthreads();
 }
 
-template <int KMAX, int NT, bool kCluster, int CPT, int U>
-__global__ void __launch_bounds__(NT) em_fit_kernel(EmArgs a) {
+// MINB: CTAs per SM the register allocation is sized for (0: no limit); SC:
+// E-step constants read from shared memory rather than held in registers.
+template <int KMAX, int NT, bool kCluster, int CPT, int U, int MINB = 0, bool SC = false>
+__global__ void __launch_bounds__(NT, MINB) em_fit_kernel(EmArgs a) {
     constexpr int NW = NT / 32;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float4 *s_samp = reinterpret_cast<float4 *>(smem_raw);
@@ -701,10 +873,11 @@ __global__ void __launch_bounds__(NT) em_fit_kernel(EmArgs a) {
     cg::cluster_group cluster = cg::this_cluster();
     if (tid == 0) {
         mbar_init(bar, 1);
+        for (uint32_t i = 0; i < kMaxStages; ++i) mbar_init(reinterpret_cast<uint64_t *>(&S.ring_bar[i]), 1);
         fence_mbar_init();
     }
     __syncthreads();
-    uint32_t phase = 0;
+    uint32_t phase = 0, ring_pos = 0;
     const uint32_t n_large = kCluster ? *a.n_large : 0u;
     if constexpr (kCluster) {
         // Phase 1: the largest regions, each shared by all CTAs of a cluster.
@@ -714,7 +887,7 @@ __global__ void __launch_bounds__(NT) em_fit_kernel(EmArgs a) {
             const uint32_t item = *cluster.map_shared_rank(&S.item, 0);
             cluster.sync();
             if (item >= n_large) break;
-            process_region<KMAX, NT, true, CPT, U>(a, S, s_samp, bar, phase, item, cluster);
+            process_region<KMAX, NT, true, CPT, U, SC>(a, S, s_samp, bar, phase, ring_pos, item, cluster);
         }
     }
     // Phase 2: the remaining regions, one CTA each, largest first.
@@ -724,7 +897,7 @@ __global__ void __launch_bounds__(NT) em_fit_kernel(EmArgs a) {
         const uint32_t item = S.item;
         __syncthreads();
         if (item >= a.n_regions) break;
-        process_region<KMAX, NT, false, CPT, U>(a, S, s_samp, bar, phase, item, cluster);
+        process_region<KMAX, NT, false, CPT, U, SC>(a, S, s_samp, bar, phase, ring_pos, item, cluster);
     }
 }
 
@@ -734,8 +907,21 @@ inline size_t fit_smem_bytes(uint32_t cap) {
     return (size_t)cap * 16 + sizeof(EmShared<KMAX, NT / 32>);
 }
 
-template <int KMAX, int NT, int CPT, int U>
-static int launch_fit(pg_ctx *ctx, const EmArgs &args, cudaStream_t s, uint32_t ctas_per_sm, uint32_t cluster) {
+// Ring shape for a launch whose E-step trip covers `grain` samples: at least
+// one trip per stage (the staging capacity grows to one trip if smaller, and
+// the stage count shrinks until a stage holds a trip), stages a whole number
+// of trips.
+inline void ring_shape(EmArgs &a, uint32_t grain) {
+    a.smem_cap = std::max(a.smem_cap, grain);
+    a.stages = std::min(std::max(a.stages, 1u), kMaxStages);
+    while (a.stages > 1 && a.smem_cap / a.stages < grain) --a.stages;
+    a.stage_n = (a.smem_cap / a.stages) / grain * grain;
+}
+
+template <int KMAX, int NT, int CPT, int U, int MINB = 0, bool SC = false>
+static int launch_fit(pg_ctx *ctx, const EmArgs &args_in, cudaStream_t s, uint32_t ctas_per_sm, uint32_t cluster) {
+    EmArgs args = args_in;
+    ring_shape(args, (uint32_t)(NT / (KMAX / CPT)) * U);
     const size_t smem = fit_smem_bytes<KMAX, NT>(args.smem_cap);
     cudaLaunchConfig_t lc = {};
     cudaLaunchAttribute attr[1];
@@ -744,7 +930,7 @@ static int launch_fit(pg_ctx *ctx, const EmArgs &args, cudaStream_t s, uint32_t 
     lc.stream = s;
     int st;
     if (cluster > 1) {
-        auto kern = em_fit_kernel<KMAX, NT, true, CPT, U>;
+        auto kern = em_fit_kernel<KMAX, NT, true, CPT, U, MINB, SC>;
         st = check_cuda(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                         "em_fit smem attribute");
         if (st) return st;
@@ -770,7 +956,7 @@ static int launch_fit(pg_ctx *ctx, const EmArgs &args, cudaStream_t s, uint32_t 
         lc.gridDim = dim3(grid, 1, 1);
         st = check_cuda(ctx, cudaLaunchKernelEx(&lc, kern, args), "em_fit launch");
     } else {
-        auto kern = em_fit_kernel<KMAX, NT, false, CPT, U>;
+        auto kern = em_fit_kernel<KMAX, NT, false, CPT, U, MINB, SC>;
         st = check_cuda(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                         "em_fit smem attribute");
         if (st) return st;

@@ -19,21 +19,28 @@ struct pg_fit_graph {
 namespace {
 
 std::vector<pg_fit_tuning> default_grid() {
+    // (CTAs per SM, components per thread, samples per trip, staged samples):
+    // 3 and 4 CTAs per SM are the register-capped builds, 0 the unrestricted one.
+    struct Shape {
+        uint32_t cps, cpt, unroll, cap;
+    };
+    const Shape shapes[] = {{3, 16, 2, 4096}, {3, 16, 2, 3072}, {4, 16, 2, 3072}, {0, 16, 2, 6144}, {4, 8, 4, 3072}};
     std::vector<pg_fit_tuning> g;
-    for (uint32_t cpt : {16u, 8u})
-        for (uint32_t cl : {1u, 2u, 4u, 8u, 16u})
-            for (uint32_t cap : {3072u, 6144u})
-                for (uint32_t large : {8192u, 12288u, 24576u}) {
-                    if (cl == 1 && large != 12288u) continue;  // no cluster: the threshold is unused
-                    pg_fit_tuning t{};
-                    t.threads_per_cta = 128;
-                    t.smem_samples = cap;
-                    t.cluster_size = cl;
-                    t.components_per_thread = cpt;
-                    t.unroll = 2;
-                    t.large_threshold = large;
-                    g.push_back(t);
-                }
+    for (const Shape &sh : shapes)
+        for (uint32_t cl : {1u, 2u, 4u})
+            for (uint32_t large : {12288u, 24576u}) {
+                if (cl == 1 && large != 12288u) continue;  // no cluster: the threshold is unused
+                pg_fit_tuning t{};
+                t.threads_per_cta = 128;
+                t.ctas_per_sm = sh.cps;
+                t.components_per_thread = sh.cpt;
+                t.unroll = sh.unroll;
+                t.smem_samples = sh.cap;
+                t.cluster_size = cl;
+                t.large_threshold = large;
+                t.stream_stages = 2;
+                g.push_back(t);
+            }
     return g;
 }
 

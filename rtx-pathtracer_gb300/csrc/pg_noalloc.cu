@@ -77,14 +77,19 @@ void initial_table(uint32_t K, float kap, float *t) {
     }
 }
 
-template <int KMAX>
+// K <= 16: the register-capped build at three CTAs per SM (E-step constants in
+// shared memory); K <= 8: the unrestricted build.
+template <int KMAX, int MINB, bool SC>
 int launch_noalloc(const pg::EmArgs &args, cudaStream_t s, uint32_t cluster, uint32_t smem_cap, int sm_count) {
     using namespace pg;
     constexpr int NT = 128;
     constexpr int CPT = KMAX;
     constexpr int U = 2;
-    auto kern = em_fit_kernel<KMAX, NT, true, CPT, U>;
-    const size_t smem = fit_smem_bytes<KMAX, NT>(smem_cap);
+    auto kern = em_fit_kernel<KMAX, NT, true, CPT, U, MINB, SC>;
+    pg::EmArgs a = args;
+    a.smem_cap = smem_cap;
+    ring_shape(a, (uint32_t)NT * U);
+    const size_t smem = fit_smem_bytes<KMAX, NT>(a.smem_cap);
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return PG_ERR_CUDA;
     cudaLaunchConfig_t lc = {};
@@ -102,7 +107,7 @@ int launch_noalloc(const pg::EmArgs &args, cudaStream_t s, uint32_t cluster, uin
     int nclusters = 0;
     if (cudaOccupancyMaxActiveClusters(&nclusters, kern, &lc) != cudaSuccess || nclusters < 1) return PG_ERR_CUDA;
     lc.gridDim = dim3((uint32_t)nclusters * cluster, 1, 1);
-    return cudaLaunchKernelEx(&lc, kern, args) == cudaSuccess ? PG_OK : PG_ERR_CUDA;
+    return cudaLaunchKernelEx(&lc, kern, a) == cudaSuccess ? PG_OK : PG_ERR_CUDA;
 }
 
 }  // namespace
@@ -133,7 +138,7 @@ extern "C" int pg_fit_regions_noalloc(const pg_fit_config *cfg, pg_region_state 
         return PG_ERR_CUDA;
     // Work queues and the error word start at zero; the order is rewritten below.
     if (cudaMemsetAsync(scr->counters, 0, sizeof(scr->counters), s) != cudaSuccess) return PG_ERR_CUDA;
-    const uint32_t cluster = 2u, cap = 6144u, large_threshold = 12288u;
+    const uint32_t cluster = 2u, cap = 4096u, large_threshold = 24576u;
     order_regions_kernel<128><<<1, 1024, 0, s>>>(offsets, n_regions, scr->order, large_threshold, scr->counters + 3);
     if (cudaGetLastError() != cudaSuccess) return PG_ERR_CUDA;
     EmArgs args;
@@ -151,6 +156,8 @@ extern "C" int pg_fit_regions_noalloc(const pg_fit_config *cfg, pg_region_state 
     args.mode = mode;
     args.smem_cap = cap;
     args.ll_out = nullptr;
+    args.stages = 2u;
     const bool wide = (mode == PG_FIT_INIT) ? (cfg->num_initial_components > 8) : true;
-    return wide ? launch_noalloc<16>(args, s, cluster, cap, sms) : launch_noalloc<8>(args, s, cluster, cap, sms);
+    return wide ? launch_noalloc<16, 3, true>(args, s, cluster, cap, sms)
+                : launch_noalloc<8, 0, false>(args, s, cluster, cap, sms);
 }

@@ -88,7 +88,13 @@ def test_fit_within_stated_tolerance_of_reference(name, cuda, pkg, golden, abi):
 @pytest.mark.parametrize("tuning", [{}, {"components_per_thread": 16}, {"unroll": 2}, {"threads_per_cta": 256},
                                     {"threads_per_cta": 256, "components_per_thread": 16, "unroll": 2},
                                     {"smem_samples": 256}, {"cluster_size": 1}, {"cluster_size": 2},
-                                    {"cluster_size": 16}, {"cluster_size": 4, "smem_samples": 512}])
+                                    {"cluster_size": 16}, {"cluster_size": 4, "smem_samples": 512},
+                                    {"unroll": 4}, {"stream_stages": 1}, {"stream_stages": 3, "smem_samples": 2048},
+                                    {"unroll": 4, "stream_stages": 8, "smem_samples": 4096},
+                                    {"ctas_per_sm": 3, "smem_samples": 3072, "stream_stages": 2},
+                                    {"ctas_per_sm": 4, "unroll": 1, "smem_samples": 2048},
+                                    {"ctas_per_sm": 4, "components_per_thread": 8, "unroll": 4,
+                                     "smem_samples": 2048}])
 def test_uneven_batch_and_launch_shapes(K, tuning, cuda, pkg, oracle, abi, workloads):
     """Uneven regions (64..20000 samples): resident and streamed staging, regions
     shared by a cluster of 2..16 CTAs and regions fitted by one CTA."""
@@ -98,6 +104,39 @@ def test_uneven_batch_and_launch_shapes(K, tuning, cuda, pkg, oracle, abi, workl
     want, _ = oracle.fit(cfg, w["dirw"], w["offsets"], f64=True)
     assert_params_close(st, want, K, GPU_TOL, want["iters_last"] > 0)
     ll_close(ll, oracle.eval_ll(w["dirw"], w["offsets"], st), w["dirw"], w["offsets"], GPU_TOL)
+
+
+@pytest.mark.parametrize("K,unroll", [(8, 2), (16, 2), (16, 4)])
+def test_streamed_ring_equals_resident_slices(K, unroll, cuda, pkg, abi, workloads):
+    """Slices larger than the staging capacity stream from L2 through a ring of
+    TMA-filled stages.  Each stage holds a whole number of E-step trips, so every
+    thread meets the same samples in the same order as when the whole slice is
+    resident: the fitted states are bit-identical for any stage count.  The
+    convergence test is on, so regions stop at different iterations with ring
+    copies still in flight (drained before the next region)."""
+    w = workloads.fit_batched(seed=5, n_regions=40, median=3000, sigma=1.0, lo=64, hi=20000)
+    cfg = abi.default_fit_config(num_initial_components=K)
+    base = {"cluster_size": 2, "large_threshold": 4096, "unroll": unroll}
+    want, _ = run_fit(cuda, pkg, cfg, w["dirw"], w["offsets"], tuning={**base, "smem_samples": 12288})
+    iters = want["iters_last"]
+    assert len(np.unique(iters[iters > 0])) > 1  # regions stop at different iterations
+    for ns in (1, 2, 3, 4, 8):
+        got, _ = run_fit(cuda, pkg, cfg, w["dirw"], w["offsets"],
+                         tuning={**base, "smem_samples": 2048, "stream_stages": ns})
+        assert got.tobytes() == want.tobytes(), f"{ns} stages"
+
+
+def test_shared_constants_equal_register_constants(cuda, pkg, abi, workloads):
+    """The register-capped builds read the E-step constants from shared memory;
+    the arithmetic and its order are those of the register build, so the fitted
+    states are bit-identical."""
+    w = workloads.fit_batched(seed=6, n_regions=30, median=2500, sigma=1.0, lo=64, hi=20000)
+    cfg = abi.default_fit_config(num_initial_components=16)
+    base = {"cluster_size": 2, "smem_samples": 3072, "stream_stages": 2}
+    want, _ = run_fit(cuda, pkg, cfg, w["dirw"], w["offsets"], tuning={**base, "unroll": 2})
+    for extra in ({"ctas_per_sm": 3, "unroll": 2}, {"ctas_per_sm": 4, "unroll": 2}):
+        got, _ = run_fit(cuda, pkg, cfg, w["dirw"], w["offsets"], tuning={**base, **extra})
+        assert got.tobytes() == want.tobytes(), extra
 
 
 def test_fit_is_deterministic(cuda, pkg, abi, workloads):
