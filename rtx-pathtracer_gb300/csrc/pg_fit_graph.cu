@@ -20,11 +20,11 @@ namespace {
 
 std::vector<pg_fit_tuning> default_grid() {
     // (CTAs per SM, components per thread, samples per trip, staged samples):
-    // 3 and 4 CTAs per SM are the register-capped builds, 0 the unrestricted one.
+    // 3 and 4 CTAs per SM are the register-capped builds, 2 the unrestricted one.
     struct Shape {
         uint32_t cps, cpt, unroll, cap;
     };
-    const Shape shapes[] = {{3, 16, 2, 4096}, {3, 16, 2, 3072}, {4, 16, 2, 3072}, {0, 16, 2, 6144}, {4, 8, 4, 3072}};
+    const Shape shapes[] = {{3, 16, 2, 4096}, {3, 16, 2, 3072}, {4, 16, 2, 3072}, {2, 16, 2, 6144}, {4, 8, 4, 3072}};
     std::vector<pg_fit_tuning> g;
     for (const Shape &sh : shapes)
         for (uint32_t cl : {1u, 2u, 4u})
