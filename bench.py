@@ -418,17 +418,26 @@ def bench_surrogate(pkg, abi, torch, stream, passes: int = 3):
     n = 1 << 22
     rec = wl.surrogate_records(n=n, box=box)
     d_rec = torch.from_numpy(rec.view(np.uint8).reshape(-1).copy()).cuda()
-    net = pkg.Surrogate(box, batch=65536, lr=1e-3)
-    losses = [net.train(d_rec, n, stream=stream)]  # warm-up pass
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with torch.cuda.stream(stream):
-        ev0.record(stream)
-        for _ in range(passes):
-            net.train(d_rec, n, stream=stream, want_loss=False)
-        ev1.record(stream)
-    torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1) / passes
-    losses.append(net.train(d_rec, n, stream=stream))
+
+    def time_training(path):
+        net = pkg.Surrogate(box, batch=65536, lr=1e-3)
+        net.set_path(path)
+        losses = [net.train(d_rec, n, stream=stream)]  # warm-up pass
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            for _ in range(passes):
+                net.train(d_rec, n, stream=stream, want_loss=False)
+            ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1) / passes
+        losses.append(net.train(d_rec, n, stream=stream))
+        return net, ms, losses
+
+    # the warp-level mma.sync kernels, for comparison
+    warp_net, warp_ms, warp_losses = time_training(abi.PG_MLP_PATH_WARP_MMA)
+    warp_net.close()
+    net, ms, losses = time_training(abi.PG_MLP_PATH_TCGEN05)
     pos = torch.from_numpy(np.ascontiguousarray(rec["position"], dtype=np.float32)).cuda()
     mix = torch.empty(n * 80, dtype=torch.float32, device="cuda")
     net.infer(pos, n, mix, stream=stream)
@@ -444,7 +453,9 @@ def bench_surrogate(pkg, abi, torch, stream, passes: int = 3):
     out = {"metric": "surrogate training records/s", "value": n / (ms * 1e-3) / 1e6, "unit": "Mrecords/s",
            "higher_is_better": True, "dtype": "bf16 (fp32 accumulate)", "config": {"workload": SURROGATE_WORKLOAD},
            "ms_per_pass": ms, "batches_per_pass": n // 65536, "loss_first_pass": losses[0],
-           "loss_after": losses[-1],
+           "loss_after": losses[-1], "kernel": "fused tcgen05 training step (k_train_tc)",
+           "warp_mma_path": {"ms_per_pass": warp_ms, "value": n / (warp_ms * 1e-3) / 1e6,
+                             "loss_first_pass": warp_losses[0], "loss_after": warp_losses[-1]},
            "inference": {"value": n / (infer_ms * 1e-3) / 1e6, "unit": "Mpositions/s", "ms": infer_ms},
            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                         "frac": achieved / peak, "peak_source": f"{src} bf16 sustained",

@@ -663,6 +663,15 @@ int pg_mlp_loss_grad(pg_mlp *mlp, const pg_directional_data *records, uint32_t n
  * batch.  loss_out (host, may be NULL) receives the mean batch loss, read
  * after a stream synchronisation. */
 int pg_mlp_train(pg_mlp *mlp, const pg_directional_data *records, uint64_t n, float *loss_out, void *stream);
+/* Implementation of the training step: PG_MLP_PATH_TCGEN05 (default) runs one
+ * persistent kernel per batch on the tcgen05 tensor cores (forward, loss,
+ * backward and weight gradients of 128-record tiles, gradient sums kept in
+ * tensor memory); PG_MLP_PATH_WARP_MMA runs warp-level mma.sync kernels with
+ * a DRAM scratch between the forward/backward and weight-gradient passes.
+ * Both compute the same quantities in the same precision. */
+#define PG_MLP_PATH_TCGEN05 0
+#define PG_MLP_PATH_WARP_MMA 1
+int pg_mlp_set_path(pg_mlp *mlp, int path);
 /* Mixture parameters at n positions (device, 3 floats each): per position 16
  * components of {weight, mu x, mu y, mu z, kappa} (80 floats, device). */
 int pg_mlp_infer(pg_mlp *mlp, const float *positions, uint32_t n, float *mixtures_out, void *stream);

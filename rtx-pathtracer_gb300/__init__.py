@@ -72,6 +72,7 @@ SIGNATURES = {
     "pg_mlp_loss_grad": (_I, [_P, _P, _U32, _P, C.POINTER(C.c_float), _P]),
     "pg_mlp_train": (_I, [_P, _P, _U64, C.POINTER(C.c_float), _P]),
     "pg_mlp_infer": (_I, [_P, _P, _U32, _P, _P]),
+    "pg_mlp_set_path": (_I, [_P, C.c_int]),
     "pg_mlp_write_guide": (_I, [_P, _P, _P]),
     "pg_mlp_judge_guide": (_I, [_P, _P, _P, _U64, _U32, C.POINTER(_U32), _P]),
     "pg_guide_nll": (_I, [_P, _P, _U64, C.POINTER(C.c_double), _P]),
@@ -399,6 +400,11 @@ class Surrogate:
         out = np.zeros(abi.MLP_PARAMS, dtype=np.float32)
         self._check(self.lib.pg_mlp_get_params(self.h, out.ctypes.data))
         return out
+
+    def set_path(self, path: int):
+        """Training-step implementation: abi.PG_MLP_PATH_TCGEN05 (default) or
+        abi.PG_MLP_PATH_WARP_MMA."""
+        self._check(self.lib.pg_mlp_set_path(self.h, int(path)))
 
     def set_params(self, theta):
         a = np.ascontiguousarray(theta, dtype=np.float32)

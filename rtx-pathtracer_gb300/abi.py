@@ -173,3 +173,7 @@ class RenderStats(C.Structure):
 def render_params(spp=1, max_depth=8, seed=1, use_nee=1, use_mis=1, use_guiding=0, guiding_prob=0.5,
                   record_samples=0, flags=0) -> RenderParams:
     return RenderParams(spp, max_depth, seed, use_nee, use_mis, use_guiding, guiding_prob, record_samples, flags)
+
+# surrogate training-step implementations (pg_mlp_set_path)
+PG_MLP_PATH_TCGEN05 = 0
+PG_MLP_PATH_WARP_MMA = 1

@@ -506,9 +506,22 @@ struct AdamArgs {
     const double *scalars;   // {sum w (-log q), sum w}
     float *theta, *m, *v;
     __nv_bfloat16 *wb;
+    __nv_bfloat16 *img;      // the tensor-core kernel's weight image
     float *grad_out;         // gradient only (no update) when not null
     float lr, b1, b2, eps, c1, c2;  // c1 = 1 - b1^t, c2 = 1 - b2^t
 };
+
+// Index of weight p in the tensor-core kernel's BF16 image (rows = outputs,
+// 8 x 8 core matrices; GEMM depth 128 for layer 1 and 80 for the others), or -1.
+__host__ __device__ inline int tc_img_index(int p) {
+    auto el = [](int r, int c, int kc) { return (((r >> 3) * kc + (c >> 3)) << 6) + ((r & 7) << 3) + (c & 7); };
+    constexpr int i2 = NH * 128, i3 = i2 + NH * 80, i4 = i3 + NH * 80;
+    if (p >= OW1 && p < OB1) return el((p - OW1) / NIN, (p - OW1) % NIN, 16);
+    if (p >= OW2 && p < OB2) return i2 + el((p - OW2) / NH, (p - OW2) % NH, 10);
+    if (p >= OW3 && p < OB3) return i3 + el((p - OW3) / NH, (p - OW3) % NH, 10);
+    if (p >= OW4 && p < OB4) return i4 + el((p - OW4) / NH, (p - OW4) % NH, 10);
+    return -1;
+}
 
 __device__ __forceinline__ int wb_index(int p) {
     if (p < OB1) return WB1 + (p - OW1);
@@ -537,6 +550,8 @@ __global__ void k_reduce_adam(AdamArgs A) {
     A.theta[p] = th;
     const int wi = wb_index(p);
     if (wi >= 0) A.wb[wi] = __float2bfloat16_rn(th);
+    const int ii = tc_img_index(p);
+    if (ii >= 0) A.img[ii] = __float2bfloat16_rn(th);
 }
 
 __global__ void k_theta_to_wb(const float *theta, __nv_bfloat16 *wb) {
@@ -545,6 +560,510 @@ __global__ void k_theta_to_wb(const float *theta, __nv_bfloat16 *wb) {
     const int wi = wb_index(p);
     if (wi >= 0) wb[wi] = __float2bfloat16_rn(theta[p]);
 }
+
+// ---- the training step on the 5th-generation tensor cores (tcgen05) --------
+//
+// k_train_tc: one persistent CTA per SM (TPR threads per record of a
+// 128-record tile) runs a whole batch: encoding, the four layers forward, the
+// loss and its output gradient, the three layers backward, and the weight
+// gradients of its tiles accumulated in tensor memory across tiles - no
+// scratch round trip through DRAM.  Every GEMM is a tcgen05.mma (BF16 operands
+// from shared memory, FP32 accumulators in tensor memory) issued by one
+// thread and completed through an mbarrier; the epilogues read tensor memory
+// with tcgen05.ld (thread t of warp w <-> lane 32 w + t).
+//
+//   forward  l: D[128 rec x out]  = X_l (K-major) . W_l^T (K-major), then +b_l
+//               (FP32), ReLU, BF16 -> X_{l+1}
+//   backward l: D[128 rec x 64]   = dY_l (K-major) . W_l (MN-major)
+//   weights  l: G_l[128 x out]   += X_l^T (MN-major) . dY_l (MN-major): rows
+//               are the layer's inputs, a column of ones after them (its row
+//               of G_l is the bias gradient) and zeros up to the GEMM depth.
+//
+// Operand tiles are stored as 8 x 8 core matrices (8 rows of 16 bytes):
+// element (r, c) of a tile with KC column chunks at element
+// ((r / 8) KC + c / 8) 64 + (r % 8) 8 + c % 8.  One buffer serves as a
+// K-major operand (rows = M or N) and as an MN-major one (rows = K), with the
+// descriptor's strides swapped: LBO is the byte stride between 8-wide units
+// along K, SBO the stride between 8-wide units along M or N.
+namespace tc {
+constexpr int TILE = 128;                 // records per tile (the MMA's M)
+constexpr int K1 = 128, KH = 80;          // GEMM depths: inputs, ones column, zeros
+constexpr int KC1 = K1 / 8, KCH = KH / 8; // column chunks
+// BF16 weight image (rows = outputs; input columns; the ones column's weight is
+// zero - the FP32 bias is added in the epilogue)
+constexpr int IW1 = 0, IW2 = IW1 + NH * K1, IW3 = IW2 + NH * KH, IW4 = IW3 + NH * KH, NIMG = IW4 + NOUT * KH;
+// shared memory (bytes)
+constexpr int SM_W = 0, SM_X1 = SM_W + NIMG * 2, SM_X2 = SM_X1 + TILE * K1 * 2, SM_X3 = SM_X2 + TILE * KH * 2,
+              SM_X4 = SM_X3 + TILE * KH * 2, SM_DY = SM_X4 + TILE * KH * 2, SM_SLACK = SM_DY + TILE * KH * 2,
+              SM_BIAS = SM_SLACK + 2048, SM_O = SM_BIAS + (3 * NH + NOUT) * 4, SM_XCH = SM_O + NOUT * TILE * 4,
+              SM_TOTAL = SM_XCH + 2 * 4 * TILE * 4;
+// The weight GEMMs of layers 2-4 use M = 128 over 81 meaningful rows: rows 81..127
+// read past the end of X_l (at most 767 bytes) into the next buffer or the slack.
+static_assert(SM_X1 % 128 == 0 && SM_TOTAL <= 227 * 1024, "shared memory layout");
+// tensor-memory columns: layer accumulator, then the four weight-gradient blocks
+constexpr uint32_t TM_ACT = 0, TM_G1 = 128, TM_G2 = 192, TM_G3 = 256, TM_G4 = 320, TM_COLS = 512;
+constexpr int kTpr = 4;  // threads per record
+
+__host__ __device__ constexpr int elem(int r, int c, int kc) {
+    return (((r >> 3) * kc + (c >> 3)) << 6) + ((r & 7) << 3) + (c & 7);
+}
+
+static_assert(IW2 == NH * 128 && IW3 == IW2 + NH * 80 && IW4 == IW3 + NH * 80 && KC1 == 16 && KCH == 10,
+              "tc_img_index uses this image layout");
+
+// Shared-memory matrix descriptor: start, leading (K) and stride (M/N) byte
+// offsets, descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, the
+// operands' major-ness, N >> 3 and M >> 4.
+__host__ __device__ constexpr uint32_t idesc(int M, int N, int a_mn, int b_mn) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)a_mn << 15) | ((uint32_t)b_mn << 16) |
+           ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+        "l"(a), "l"(b), "r"(id), "r"(accumulate));
+}
+// One operand walk: start address, LBO, SBO, bytes to advance per K-step of 16.
+struct Opnd {
+    uint32_t addr, lbo, sbo, step;
+};
+// D (+)= A B over `steps` K-steps (one thread).
+__device__ __forceinline__ void gemm(uint32_t d, Opnd a, Opnd b, int steps, uint32_t id, bool accumulate) {
+    for (int k = 0; k < steps; ++k)
+        mma(d, sdesc(a.addr + k * a.step, a.lbo, a.sbo), sdesc(b.addr + k * b.step, b.lbo, b.sbo), id,
+            (accumulate || k > 0) ? 1u : 0u);
+}
+__device__ __forceinline__ void commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// 16 consecutive FP32 columns of this thread's tensor-memory lane
+__device__ __forceinline__ void tld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+__device__ __forceinline__ void tld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+struct TrainArgs {
+    const pg_directional_data *rec;
+    uint32_t n;
+    float lo[3], inv_ext[3];
+    const __nv_bfloat16 *wimg;  // NIMG
+    const float *theta;         // FP32 masters (biases)
+    float *partials;            // gridDim.x x NPARAM weight / bias gradient sums
+    float *loss_partials;       // gridDim.x x {sum w (-log q), sum w}
+    uint32_t *err;              // PG_DEV_ERR_TIMEOUT if a wait ran out
+};
+
+// Waits for the MMAs committed to `bar` (phase `phase`), bounded.
+__device__ __forceinline__ void mma_wait(uint64_t *bar, uint32_t &phase, uint32_t *err) {
+    mbar_wait_bounded(bar, phase, err);
+    phase ^= 1u;
+    fence_after();
+}
+
+// Generic-proxy stores of the operands -> visible to the tensor cores; all
+// threads' tensor-memory loads done; then thread 0 issues.
+__device__ __forceinline__ void operands_ready() {
+    fence_proxy_async_smem();
+    fence_before();
+    __syncthreads();
+}
+
+// Hidden-layer epilogue for this thread's share of a record's 64 columns
+// (NCOL from column c0): + bias, ReLU (mask bits kept), BF16 into the next
+// layer's X; the last share also writes [1, 0...] and a zero chunk.
+template <int NCOL>
+__device__ __forceinline__ void hidden_epilogue(uint32_t tacc, int c0, const float *bias, __nv_bfloat16 *xn, int row,
+                                                bool last, uint32_t &mask) {
+    float v[NCOL / 16][16];
+#pragma unroll
+    for (int q = 0; q < NCOL / 16; ++q) tld16(tacc + c0 + 16 * q, v[q]);
+    tld_wait();
+    mask = 0u;
+#pragma unroll
+    for (int ch = 0; ch < NCOL / 8; ++ch) {
+        uint32_t pk[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int c = 8 * ch + 2 * e;
+            float a = v[c >> 4][c & 15] + bias[c0 + c], b = v[(c + 1) >> 4][(c + 1) & 15] + bias[c0 + c + 1];
+            const bool pa = a > 0.0f, pb = b > 0.0f;
+            a = pa ? a : 0.0f;
+            b = pb ? b : 0.0f;
+            mask |= ((pa ? 1u : 0u) << c) | ((pb ? 1u : 0u) << (c + 1));
+            pk[e] = pack2(a, b);
+        }
+        *reinterpret_cast<uint4 *>(xn + elem(row, c0 + 8 * ch, KCH)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    }
+    if (last) {
+        *reinterpret_cast<uint4 *>(xn + elem(row, 64, KCH)) = make_uint4(pack2(1.0f, 0.0f), 0u, 0u, 0u);
+        *reinterpret_cast<uint4 *>(xn + elem(row, 72, KCH)) = make_uint4(0u, 0u, 0u, 0u);
+    }
+}
+
+// Backward epilogue for the same share: dH, ReLU mask, BF16 into dY.
+template <int NCOL>
+__device__ __forceinline__ void backward_epilogue(uint32_t tacc, int c0, uint32_t mask, __nv_bfloat16 *dy, int row) {
+    float v[NCOL / 16][16];
+#pragma unroll
+    for (int q = 0; q < NCOL / 16; ++q) tld16(tacc + c0 + 16 * q, v[q]);
+    tld_wait();
+#pragma unroll
+    for (int ch = 0; ch < NCOL / 8; ++ch) {
+        uint32_t pk[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int c = 8 * ch + 2 * e;
+            const float a = ((mask >> c) & 1u) ? v[c >> 4][c & 15] : 0.0f;
+            const float b = ((mask >> (c + 1)) & 1u) ? v[(c + 1) >> 4][(c + 1) & 15] : 0.0f;
+            pk[e] = pack2(a, b);
+        }
+        *reinterpret_cast<uint4 *>(dy + elem(row, c0 + 8 * ch, KCH)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    }
+}
+
+// TPR threads per record: warps w, w + 4, ... share tensor-memory lanes
+// 32 (w % 4) .. + 31, i.e. the same 32 records; share h = warp / 4 takes 64 / TPR
+// of a layer's columns, 16 / TPR of the mixture components and every TPR-th
+// encoding chunk.  The output layer goes through shared memory (sO, one
+// column-major row of 80 floats per record) so the component split does not
+// follow the tensor-memory column blocks.
+template <int TPR>
+__global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
+    constexpr int NT = TILE * TPR, HC = 64 / TPR, NCMP = NC / TPR;
+    extern __shared__ __align__(1024) unsigned char sm[];
+    __shared__ uint32_t s_tmem;
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ float s_red[2 * NT / 32];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int rec = tid & (TILE - 1), h = tid / TILE;  // record within the tile, share
+    __nv_bfloat16 *sX1 = reinterpret_cast<__nv_bfloat16 *>(sm + SM_X1);
+    __nv_bfloat16 *sX2 = reinterpret_cast<__nv_bfloat16 *>(sm + SM_X2);
+    __nv_bfloat16 *sX3 = reinterpret_cast<__nv_bfloat16 *>(sm + SM_X3);
+    __nv_bfloat16 *sX4 = reinterpret_cast<__nv_bfloat16 *>(sm + SM_X4);
+    __nv_bfloat16 *sDY = reinterpret_cast<__nv_bfloat16 *>(sm + SM_DY);
+    float *sB = reinterpret_cast<float *>(sm + SM_BIAS);
+    float *sO = reinterpret_cast<float *>(sm + SM_O);      // [NOUT][TILE]
+    float *sXm = reinterpret_cast<float *>(sm + SM_XCH);   // [TPR][TILE] partial maxima
+    float *sXs = sXm + TPR * TILE;                          // [TPR][TILE] partial sums
+    {
+        const uint4 *src = reinterpret_cast<const uint4 *>(A.wimg);
+        uint4 *dst = reinterpret_cast<uint4 *>(sm + SM_W);
+        for (int i = tid; i < NIMG * 2 / 16; i += NT) dst[i] = src[i];
+        uint4 *slack = reinterpret_cast<uint4 *>(sm + SM_SLACK);
+        for (int i = tid; i < 2048 / 16; i += NT) slack[i] = make_uint4(0u, 0u, 0u, 0u);
+        for (int i = tid; i < NH; i += NT) {
+            sB[i] = A.theta[OB1 + i];
+            sB[NH + i] = A.theta[OB2 + i];
+            sB[2 * NH + i] = A.theta[OB3 + i];
+        }
+        for (int i = tid; i < NOUT; i += NT) sB[3 * NH + i] = A.theta[OB4 + i];
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s_tmem)),
+                     "r"(TM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        mbar_init(&s_bar, 1);
+        fence_mbar_init();
+    }
+    operands_ready();
+    fence_after();
+    const uint32_t tm = s_tmem;
+    const uint32_t tl = tm + ((uint32_t)((warp & 3) * 32) << 16);  // this warp's lanes
+    const uint32_t aW = smem_u32(sm + SM_W), aX1 = smem_u32(sX1), aX2 = smem_u32(sX2), aX3 = smem_u32(sX3),
+                   aX4 = smem_u32(sX4), aDY = smem_u32(sDY);
+    // operand walks (bytes): K-major tiles advance 2 chunks (256 B) per K-step of 16,
+    // MN-major ones 2 row groups
+    const Opnd fX1{aX1, 128, KC1 * 128, 256}, fX2{aX2, 128, KCH * 128, 256}, fX3{aX3, 128, KCH * 128, 256},
+        fX4{aX4, 128, KCH * 128, 256};
+    const Opnd fW1{aW + IW1 * 2, 128, KC1 * 128, 256}, fW2{aW + IW2 * 2, 128, KCH * 128, 256},
+        fW3{aW + IW3 * 2, 128, KCH * 128, 256}, fW4{aW + IW4 * 2, 128, KCH * 128, 256};
+    const Opnd bDY{aDY, 128, KCH * 128, 256};
+    const Opnd bW2{aW + IW2 * 2, KCH * 128, 128, 2 * KCH * 128}, bW3{aW + IW3 * 2, KCH * 128, 128, 2 * KCH * 128},
+        bW4{aW + IW4 * 2, KCH * 128, 128, 2 * KCH * 128};
+    const Opnd gX1{aX1, KC1 * 128, 128, 2 * KC1 * 128}, gX2{aX2, KCH * 128, 128, 2 * KCH * 128},
+        gX3{aX3, KCH * 128, 128, 2 * KCH * 128}, gX4{aX4, KCH * 128, 128, 2 * KCH * 128};
+    const Opnd gDY{aDY, KCH * 128, 128, 2 * KCH * 128};
+    uint32_t phase = 0;
+    float lsum = 0.0f, wsum = 0.0f;
+    bool first = true;
+    const uint32_t tiles = (A.n + TILE - 1) / TILE;
+    const int hc0 = h * HC;  // this share's hidden columns
+    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const uint32_t r = tile * TILE + (uint32_t)rec;
+        float x[3] = {0.0f, 0.0f, 0.0f}, d[3] = {0.0f, 0.0f, 1.0f}, w = 0.0f;
+        if (r < A.n) {
+            const pg_directional_data &rc = A.rec[r];
+            for (int k = 0; k < 3; ++k) {
+                x[k] = (rc.position[k] - A.lo[k]) * A.inv_ext[k];
+                d[k] = rc.direction[k];
+            }
+            w = rc.flags == PG_INVALID_REGION ? 0.0f : rc.weight;
+            if (!(w > 0.0f) || !isfinite(w)) w = 0.0f;
+        }
+        // encoding -> X1: 112 features, the ones column, zeros to 128 (chunks h, h + TPR, ...)
+        for (int ch = h; ch < KC1; ch += TPR) {
+            const int c = 8 * ch;
+            uint4 v;
+            if (ch < 14)
+                v = make_uint4(enc_pair(x, c), enc_pair(x, c + 2), enc_pair(x, c + 4), enc_pair(x, c + 6));
+            else
+                v = make_uint4(ch == 14 ? pack2(1.0f, 0.0f) : 0u, 0u, 0u, 0u);
+            *reinterpret_cast<uint4 *>(sX1 + elem(rec, c, KC1)) = v;
+        }
+        uint32_t m1, m2, m3;
+        // ---- forward
+        operands_ready();
+        if (tid == 0) {
+            fence_after();
+            gemm(tm + TM_ACT, fX1, fW1, K1 / 16, idesc(128, NH, 0, 0), false);
+            commit(&s_bar);
+        }
+        mma_wait(&s_bar, phase, A.err);
+        hidden_epilogue<HC>(tl + TM_ACT, hc0, sB, sX2, rec, h == TPR - 1, m1);
+        operands_ready();
+        if (tid == 0) {
+            fence_after();
+            gemm(tm + TM_ACT, fX2, fW2, KH / 16, idesc(128, NH, 0, 0), false);
+            commit(&s_bar);
+        }
+        mma_wait(&s_bar, phase, A.err);
+        hidden_epilogue<HC>(tl + TM_ACT, hc0, sB + NH, sX3, rec, h == TPR - 1, m2);
+        operands_ready();
+        if (tid == 0) {
+            fence_after();
+            gemm(tm + TM_ACT, fX3, fW3, KH / 16, idesc(128, NH, 0, 0), false);
+            commit(&s_bar);
+        }
+        mma_wait(&s_bar, phase, A.err);
+        hidden_epilogue<HC>(tl + TM_ACT, hc0, sB + 2 * NH, sX4, rec, h == TPR - 1, m3);
+        operands_ready();
+        if (tid == 0) {
+            fence_after();
+            gemm(tm + TM_ACT, fX4, fW4, KH / 16, idesc(128, NOUT, 0, 0), false);
+            commit(&s_bar);
+        }
+        mma_wait(&s_bar, phase, A.err);
+        // ---- mixture, loss and output gradient: outputs + bias -> sO (column blocks h, h + TPR, ...)
+        for (int q = h; q < NOUT / 16; q += TPR) {
+            float v[16];
+            tld16(tl + TM_ACT + 16 * q, v);
+            tld_wait();
+#pragma unroll
+            for (int j = 0; j < 16; ++j) sO[(16 * q + j) * TILE + rec] = v[j] + sB[3 * NH + 16 * q + j];
+        }
+        __syncthreads();
+        const int j0 = h * NCMP;  // this share's components
+        float ml = -INFINITY;
+#pragma unroll
+        for (int q = 0; q < NCMP; ++q) ml = fmaxf(ml, sO[(5 * (j0 + q)) * TILE + rec]);
+        float sl = 0.0f;
+#pragma unroll
+        for (int q = 0; q < NCMP; ++q) sl += expf(sO[(5 * (j0 + q)) * TILE + rec] - ml);
+        sXm[h * TILE + rec] = ml;
+        sXs[h * TILE + rec] = sl;
+        __syncthreads();
+        float lmax = -INFINITY;
+#pragma unroll
+        for (int g = 0; g < TPR; ++g) lmax = fmaxf(lmax, sXm[g * TILE + rec]);
+        float lsm = 0.0f;
+#pragma unroll
+        for (int g = 0; g < TPR; ++g) lsm += sXs[g * TILE + rec] * expf(sXm[g * TILE + rec] - lmax);
+        const float lse = lmax + logf(lsm);
+        float lp[NCMP];
+#pragma unroll
+        for (int q = 0; q < NCMP; ++q) {
+            const int j = j0 + q;
+            const float mx = sO[(5 * j + 1) * TILE + rec], my = sO[(5 * j + 2) * TILE + rec],
+                        mz = sO[(5 * j + 3) * TILE + rec];
+            const float mn = sqrtf(mx * mx + my * my + mz * mz);
+            const float inv = mn > 0.0f ? 1.0f / mn : 0.0f;
+            const float k = expf(fminf(fmaxf(sO[(5 * j + 4) * TILE + rec], S_MIN), S_MAX));
+            const float cs = mx * inv * d[0] + my * inv * d[1] + mz * inv * d[2];
+            const float lognorm = logf(k) - logf(2.0f * kPi) - logf(-expm1f(-2.0f * k));
+            lp[q] = (sO[(5 * j) * TILE + rec] - lse) + lognorm + k * (cs - 1.0f);
+        }
+        float mq = -INFINITY;
+#pragma unroll
+        for (int q = 0; q < NCMP; ++q) mq = fmaxf(mq, lp[q]);
+        float sq = 0.0f;
+#pragma unroll
+        for (int q = 0; q < NCMP; ++q) sq += expf(lp[q] - mq);
+        __syncthreads();  // everyone has read the logit maxima
+        sXm[h * TILE + rec] = mq;
+        sXs[h * TILE + rec] = sq;
+        __syncthreads();
+        float qmax = -INFINITY;
+#pragma unroll
+        for (int g = 0; g < TPR; ++g) qmax = fmaxf(qmax, sXm[g * TILE + rec]);
+        float qs = 0.0f;
+#pragma unroll
+        for (int g = 0; g < TPR; ++g) qs += sXs[g * TILE + rec] * expf(sXm[g * TILE + rec] - qmax);
+        const float logq = qmax + logf(qs);
+        if (h == 0 && w > 0.0f) {
+            lsum += w * -logq;
+            wsum += w;
+        }
+#pragma unroll
+        for (int q = 0; q < NCMP; ++q) {
+            const int j = j0 + q;
+            float *o = sO + (5 * j) * TILE + rec;
+            const float mx = o[TILE], my = o[2 * TILE], mz = o[3 * TILE], sraw = o[4 * TILE];
+            const float mn = sqrtf(mx * mx + my * my + mz * mz);
+            const float inv = mn > 0.0f ? 1.0f / mn : 0.0f;
+            const float mu0 = mx * inv, mu1 = my * inv, mu2 = mz * inv;
+            const float k = expf(fminf(fmaxf(sraw, S_MIN), S_MAX));
+            const float cs = mu0 * d[0] + mu1 * d[1] + mu2 * d[2];
+            const float rr = expf(lp[q] - logq);  // responsibility
+            const float pi = expf(o[0] - lse);
+            const float f = mn > 0.0f ? -w * rr * k / mn : 0.0f;
+            o[0] = w * (pi - rr);
+            o[TILE] = f * (d[0] - cs * mu0);
+            o[2 * TILE] = f * (d[1] - cs * mu1);
+            o[3 * TILE] = f * (d[2] - cs * mu2);
+            const bool inside = sraw > S_MIN && sraw < S_MAX;
+            const float e = expf(-2.0f * k);
+            const float tt = 2.0f * k * e / -expm1f(-2.0f * k);
+            o[4 * TILE] = inside ? -w * rr * (1.0f - tt + k * (cs - 1.0f)) : 0.0f;
+        }
+        __syncthreads();
+        for (int ch = h; ch < NOUT / 8; ch += TPR) {
+            const float *o = sO + (8 * ch) * TILE + rec;
+            *reinterpret_cast<uint4 *>(sDY + elem(rec, 8 * ch, KCH)) =
+                make_uint4(pack2(o[0], o[TILE]), pack2(o[2 * TILE], o[3 * TILE]), pack2(o[4 * TILE], o[5 * TILE]),
+                           pack2(o[6 * TILE], o[7 * TILE]));
+        }
+        // ---- backward: weight gradients of layer l and dH_{l-1} from one commit
+        operands_ready();
+        if (tid == 0) {
+            fence_after();
+            gemm(tm + TM_G4, gX4, gDY, TILE / 16, idesc(128, NOUT, 1, 1), !first);
+            gemm(tm + TM_ACT, bDY, bW4, NOUT / 16, idesc(128, NH, 0, 1), false);
+            commit(&s_bar);
+        }
+        mma_wait(&s_bar, phase, A.err);
+        backward_epilogue<HC>(tl + TM_ACT, hc0, m3, sDY, rec);
+        operands_ready();
+        if (tid == 0) {
+            fence_after();
+            gemm(tm + TM_G3, gX3, gDY, TILE / 16, idesc(128, NH, 1, 1), !first);
+            gemm(tm + TM_ACT, bDY, bW3, NH / 16, idesc(128, NH, 0, 1), false);
+            commit(&s_bar);
+        }
+        mma_wait(&s_bar, phase, A.err);
+        backward_epilogue<HC>(tl + TM_ACT, hc0, m2, sDY, rec);
+        operands_ready();
+        if (tid == 0) {
+            fence_after();
+            gemm(tm + TM_G2, gX2, gDY, TILE / 16, idesc(128, NH, 1, 1), !first);
+            gemm(tm + TM_ACT, bDY, bW2, NH / 16, idesc(128, NH, 0, 1), false);
+            commit(&s_bar);
+        }
+        mma_wait(&s_bar, phase, A.err);
+        backward_epilogue<HC>(tl + TM_ACT, hc0, m1, sDY, rec);
+        operands_ready();
+        if (tid == 0) {
+            fence_after();
+            gemm(tm + TM_G1, gX1, gDY, TILE / 16, idesc(128, NH, 1, 1), !first);
+            commit(&s_bar);
+        }
+        mma_wait(&s_bar, phase, A.err);
+        first = false;
+    }
+    // ---- this CTA's gradient sums: lane = input row (bias row = the ones column);
+    // column blocks h, h + TPR, ...
+    float *out = A.partials + (size_t)blockIdx.x * NPARAM;
+    const int i = rec;
+    auto dump = [&](uint32_t tcol, int nout, int nin, int ow, int ob) {
+        for (int c = 16 * h; c < nout; c += 16 * TPR) {
+            float v[16];
+            tld16(tl + tcol + c, v);
+            tld_wait();
+            if (first) {  // no tile: zero sums
+#pragma unroll
+                for (int j = 0; j < 16; ++j) v[j] = 0.0f;
+            }
+            if (i < nin) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) out[ow + (c + j) * nin + i] = v[j];
+            } else if (i == nin) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) out[ob + c + j] = v[j];
+            }
+        }
+    };
+    dump(TM_G1, NH, NIN, OW1, OB1);
+    dump(TM_G2, NH, NH, OW2, OB2);
+    dump(TM_G3, NH, NH, OW3, OB3);
+    dump(TM_G4, NOUT, NH, OW4, OB4);
+    for (int off = 16; off > 0; off >>= 1) {
+        lsum += __shfl_xor_sync(0xffffffffu, lsum, off);
+        wsum += __shfl_xor_sync(0xffffffffu, wsum, off);
+    }
+    if (lane == 0) {
+        s_red[2 * warp] = lsum;
+        s_red[2 * warp + 1] = wsum;
+    }
+    fence_before();
+    __syncthreads();
+    if (tid == 0) {  // only share 0 (warps 0-3) carries loss sums
+        A.loss_partials[2 * blockIdx.x] = (s_red[0] + s_red[2]) + (s_red[4] + s_red[6]);
+        A.loss_partials[2 * blockIdx.x + 1] = (s_red[1] + s_red[3]) + (s_red[5] + s_red[7]);
+    }
+    if (warp == 0) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(TM_COLS));
+    }
+}
+
+// Sums of the per-CTA loss partials (one block, deterministic order).
+__global__ void k_tc_scalars(const float *lp, uint32_t n, double *scalars) {
+    __shared__ double sl[256], sw[256];
+    double l = 0.0, w = 0.0;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        l += lp[2 * i];
+        w += lp[2 * i + 1];
+    }
+    sl[threadIdx.x] = l;
+    sw[threadIdx.x] = w;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if ((int)threadIdx.x < st) {
+            sl[threadIdx.x] += sl[threadIdx.x + st];
+            sw[threadIdx.x] += sw[threadIdx.x + st];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        scalars[0] = sl[0];
+        scalars[1] = sw[0];
+    }
+}
+
+__global__ void k_theta_to_img(const float *theta, __nv_bfloat16 *img) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= NPARAM) return;
+    const int ii = tc_img_index(p);
+    if (ii >= 0) img[ii] = __float2bfloat16_rn(theta[p]);
+}
+}  // namespace tc
 
 // centres of the guide's region boxes
 __global__ void k_region_centres(const float *aabbs, uint32_t n, float *pos) {
@@ -683,6 +1202,9 @@ struct pg_mlp {
     uint32_t wg_used = 0;            // row blocks of the last weight-gradient launch
     uint32_t step = 0;
     size_t smem = 0;
+    __nv_bfloat16 *img = nullptr;    // tensor-core kernel's weight image
+    uint32_t *err = nullptr;         // device error word of the tensor-core kernel
+    int path = PG_MLP_PATH_TCGEN05;
 };
 
 namespace {
@@ -704,6 +1226,28 @@ FwdArgs fwd_args(const pg_mlp *M) {
 // forward + backward + weight gradients of one batch; leaves the partials and
 // the batch's scalars in scalars[2 * slot]
 int batch_gradients(pg_mlp *M, const pg_directional_data *rec, uint32_t n, uint32_t slot, cudaStream_t s) {
+    if (M->path == PG_MLP_PATH_TCGEN05) {
+        const uint32_t tiles = (n + tc::TILE - 1) / tc::TILE;
+        const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)M->sm_count);
+        tc::TrainArgs T{};
+        FwdArgs F = fwd_args(M);
+        T.rec = rec;
+        T.n = n;
+        for (int i = 0; i < 3; ++i) {
+            T.lo[i] = F.lo[i];
+            T.inv_ext[i] = F.inv_ext[i];
+        }
+        T.wimg = M->img;
+        T.theta = M->theta;
+        T.partials = M->wg_partials;
+        T.loss_partials = M->fwd_partials;
+        T.err = M->err;
+        tc::k_train_tc<tc::kTpr><<<grid, tc::TILE * tc::kTpr, tc::SM_TOTAL, s>>>(T);
+        tc::k_tc_scalars<<<1, 256, 0, s>>>(M->fwd_partials, grid, M->scalars + 2 * slot);
+        if (cudaGetLastError() != cudaSuccess) return mlp_error(PG_ERR_CUDA, "surrogate gradient launch");
+        M->wg_used = grid;
+        return PG_OK;
+    }
     const uint32_t ctas = (n + kRowsPerCta - 1) / kRowsPerCta;
     const uint32_t rows = ctas * kRowsPerCta;
     FwdArgs A = fwd_args(M);
@@ -737,6 +1281,7 @@ int reduce_step(pg_mlp *M, uint32_t slot, float *grad_out, cudaStream_t s) {
     A.m = M->m;
     A.v = M->v;
     A.wb = M->wb;
+    A.img = M->img;
     A.grad_out = grad_out;
     if (!grad_out) {
         M->step += 1;
@@ -773,6 +1318,19 @@ int ensure_capacity(pg_mlp *M, uint32_t rows, uint32_t batches) {
             return mlp_error(PG_ERR_NOMEM, "surrogate scalars: out of device memory");
         }
         M->cap_batches = batches;
+    }
+    return PG_OK;
+}
+
+// After a stream synchronisation: a bounded wait of the tensor-core kernel
+// that ran out is reported (and the word cleared).
+int check_device_error(pg_mlp *M) {
+    uint32_t e = 0;
+    if (cudaMemcpy(&e, M->err, sizeof e, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return mlp_error(PG_ERR_CUDA, "surrogate error word");
+    if (e) {
+        cudaMemset(M->err, 0, sizeof(uint32_t));
+        return mlp_error(PG_ERR_TIMEOUT, "surrogate training: a tensor-core wait timed out");
     }
     return PG_OK;
 }
@@ -814,11 +1372,17 @@ int pg_mlp_create(const pg_mlp_config *cfg, pg_mlp **out) {
               cudaMalloc(&M->m, sizeof(float) * NPARAM) == cudaSuccess &&
               cudaMalloc(&M->v, sizeof(float) * NPARAM) == cudaSuccess &&
               cudaMalloc(&M->wb, sizeof(__nv_bfloat16) * NWB) == cudaSuccess &&
-              cudaMalloc(&M->wg_partials, sizeof(float) * (size_t)M->wg_blocks * NPARAM) == cudaSuccess;
+              cudaMalloc(&M->wg_partials, sizeof(float) * (size_t)M->wg_blocks * NPARAM) == cudaSuccess &&
+              cudaMalloc(&M->img, sizeof(__nv_bfloat16) * tc::NIMG) == cudaSuccess &&
+              cudaMemset(M->img, 0, sizeof(__nv_bfloat16) * tc::NIMG) == cudaSuccess &&
+              cudaMalloc(&M->err, sizeof(uint32_t)) == cudaSuccess &&
+              cudaMemset(M->err, 0, sizeof(uint32_t)) == cudaSuccess;
     ok = ok && cudaFuncSetAttribute(k_fwd_bwd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)M->smem) ==
                    cudaSuccess &&
          cudaFuncSetAttribute(k_fwd_bwd<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)M->smem) ==
-             cudaSuccess;
+             cudaSuccess &&
+         cudaFuncSetAttribute(tc::k_train_tc<tc::kTpr>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              tc::SM_TOTAL) == cudaSuccess;
     if (!ok) {
         pg_mlp_destroy(M);
         return mlp_error(PG_ERR_CUDA, "surrogate allocation failed");
@@ -878,6 +1442,8 @@ int pg_mlp_destroy(pg_mlp *M) {
     cudaFree(M->net_vmm);
     cudaFree(M->judge);
     cudaFree(M->judge_count);
+    cudaFree(M->img);
+    cudaFree(M->err);
     delete M;
     return PG_OK;
 }
@@ -896,6 +1462,7 @@ int pg_mlp_set_params(pg_mlp *M, const float *host_in) {
         cudaMemset(M->v, 0, sizeof(float) * NPARAM) != cudaSuccess)
         return mlp_error(PG_ERR_CUDA, "parameter upload");
     k_theta_to_wb<<<(NPARAM + 255) / 256, 256>>>(M->theta, M->wb);
+    tc::k_theta_to_img<<<(NPARAM + 255) / 256, 256>>>(M->theta, M->img);
     if (cudaDeviceSynchronize() != cudaSuccess) return mlp_error(PG_ERR_CUDA, "weight conversion");
     M->step = 0;
     return PG_OK;
@@ -915,6 +1482,7 @@ int pg_mlp_loss_grad(pg_mlp *M, const pg_directional_data *records, uint32_t n, 
         if (cudaMemcpyAsync(sc, M->scalars, sizeof sc, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             cudaStreamSynchronize(s) != cudaSuccess)
             return mlp_error(PG_ERR_CUDA, "loss download");
+        if (int st = check_device_error(M)) return st;
         *loss_out = sc[1] > 0.0 ? (float)(sc[0] / sc[1]) : 0.0f;
     }
     return PG_OK;
@@ -939,10 +1507,17 @@ int pg_mlp_train(pg_mlp *M, const pg_directional_data *records, uint64_t n, floa
                 cudaSuccess ||
             cudaStreamSynchronize(s) != cudaSuccess)
             return mlp_error(PG_ERR_CUDA, "loss download");
+        if (int st = check_device_error(M)) return st;
         double acc = 0.0;
         for (uint32_t b = 0; b < batches; ++b) acc += sc[2 * b + 1] > 0.0 ? sc[2 * b] / sc[2 * b + 1] : 0.0;
         *loss_out = (float)(acc / batches);
     }
+    return PG_OK;
+}
+
+int pg_mlp_set_path(pg_mlp *M, int path) {
+    if (!M || (path != PG_MLP_PATH_TCGEN05 && path != PG_MLP_PATH_WARP_MMA)) return PG_ERR_ARG;
+    M->path = path;
     return PG_OK;
 }
 

@@ -94,6 +94,34 @@ def test_loss_and_gradient_match_oracle(n, cuda, pkg, abi, workloads):
     net.close()
 
 
+@pytest.mark.parametrize("n", [1, 200, 3001])
+def test_tensor_core_step_equals_warp_mma_step(n, cuda, pkg, abi, workloads):
+    """The fused tcgen05 step and the warp-level mma.sync kernels compute the same
+    loss and gradient: BF16 operands rounded at the same points, FP32 sums in a
+    different order."""
+    torch = cuda
+    rng = np.random.default_rng(100 + n)
+    net = pkg.Surrogate(BOX, batch=4096)
+    theta = net.params()
+    theta = theta + (0.03 * rng.normal(size=theta.shape)).astype(np.float32) * (theta != 0)
+    net.set_params(theta)
+    rec = records(workloads, rng, n)
+    rec["flags"][0] = 0
+    d = dev(torch, rec)
+    out = {}
+    for path in (abi.PG_MLP_PATH_TCGEN05, abi.PG_MLP_PATH_WARP_MMA):
+        net.set_path(path)
+        grad = torch.zeros(abi.MLP_PARAMS, dtype=torch.float32, device="cuda")
+        loss = net.loss_grad(d, n, grad)
+        out[path] = (loss, grad.cpu().numpy().astype(np.float64))
+    (la, ga), (lb, gb) = out[abi.PG_MLP_PATH_TCGEN05], out[abi.PG_MLP_PATH_WARP_MMA]
+    assert abs(la - lb) <= 1e-5 * max(1.0, abs(lb)), (la, lb)
+    errs = block_errors(ga, gb)
+    for name in ("W1", "W2", "W3", "W4", "b1", "b2", "b3", "b4"):
+        assert errs[name] < 1e-2, errs
+    net.close()
+
+
 def test_inference_matches_oracle(cuda, pkg, abi):
     torch = cuda
     rng = np.random.default_rng(5)
