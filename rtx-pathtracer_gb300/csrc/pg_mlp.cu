@@ -531,11 +531,30 @@ __device__ __forceinline__ int wb_index(int p) {
     return -1;
 }
 
-__global__ void k_reduce_adam(AdamArgs A) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= NPARAM) return;
+// 32 parameters per block of kAdamGroups warps: warp g sums the partials of
+// blocks g, g + kAdamGroups, ... (coalesced rows, loads from all warps in
+// flight), the groups' compensated sums are merged in a fixed order.
+constexpr int kAdamGroups = 8;
+__global__ void __launch_bounds__(32 * kAdamGroups) k_reduce_adam(AdamArgs A) {
+    __shared__ float ps[kAdamGroups][32], pc[kAdamGroups][32];
+    const int lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
+    const int p = blockIdx.x * 32 + lane;
+    {
+        float s = 0.0f, c = 0.0f;
+        if (p < NPARAM)
+            for (uint32_t b = grp; b < A.n_blocks; b += kAdamGroups)
+                neumaier_add(s, c, A.partials[(size_t)b * NPARAM + p]);
+        ps[grp][lane] = s;
+        pc[grp][lane] = c;
+    }
+    __syncthreads();
+    if (grp != 0 || p >= NPARAM) return;
     float s = 0.0f, c = 0.0f;
-    for (uint32_t b = 0; b < A.n_blocks; ++b) neumaier_add(s, c, A.partials[(size_t)b * NPARAM + p]);
+#pragma unroll
+    for (int g = 0; g < kAdamGroups; ++g) {
+        neumaier_add(s, c, ps[g][lane]);
+        c += pc[g][lane];
+    }
     const double W = A.scalars[1];
     const float gr = W > 0.0 ? (float)((double)(s + c) / W) : 0.0f;
     if (A.grad_out) {
@@ -684,6 +703,24 @@ __device__ __forceinline__ void operands_ready() {
     __syncthreads();
 }
 
+// Fourier features of columns (c, c + 1) as enc_pair, with the argument
+// reduced exactly (2^k x minus the nearest even integer, |r| <= 1) and the fast
+// sine / cosine of pi r (absolute error ~2^-21, far below the BF16 rounding
+// of the features).
+__device__ __forceinline__ uint32_t enc_pair_fast(const float x[3], int c) {
+    if (c < 96) {
+        const int i = c >> 1, d = i % 3, k = i / 3;
+        const float y = ldexpf(x[d], k);
+        const float r = y - 2.0f * rintf(0.5f * y);
+        float sn, cs;
+        __sincosf(kPi * r, &sn, &cs);
+        return pack2(sn, cs);
+    }
+    if (c == 96) return pack2(x[0], x[1]);
+    if (c == 98) return pack2(x[2], 0.0f);
+    return 0u;
+}
+
 // Hidden-layer epilogue for this thread's share of a record's 64 columns
 // (NCOL from column c0): + bias, ReLU (mask bits kept), BF16 into the next
 // layer's X; the last share also writes [1, 0...] and a zero chunk.
@@ -823,7 +860,8 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
             const int c = 8 * ch;
             uint4 v;
             if (ch < 14)
-                v = make_uint4(enc_pair(x, c), enc_pair(x, c + 2), enc_pair(x, c + 4), enc_pair(x, c + 6));
+                v = make_uint4(enc_pair_fast(x, c), enc_pair_fast(x, c + 2), enc_pair_fast(x, c + 4),
+                               enc_pair_fast(x, c + 6));
             else
                 v = make_uint4(ch == 14 ? pack2(1.0f, 0.0f) : 0u, 0u, 0u, 0u);
             *reinterpret_cast<uint4 *>(sX1 + elem(rec, c, KC1)) = v;
@@ -871,12 +909,15 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
         }
         __syncthreads();
         const int j0 = h * NCMP;  // this share's components
+        // Fast exponentials and logarithms (relative error ~1e-6): the loss and
+        // gradient are sums over many records of terms that are rounded to
+        // BF16 on the way back.
         float ml = -INFINITY;
 #pragma unroll
         for (int q = 0; q < NCMP; ++q) ml = fmaxf(ml, sO[(5 * (j0 + q)) * TILE + rec]);
         float sl = 0.0f;
 #pragma unroll
-        for (int q = 0; q < NCMP; ++q) sl += expf(sO[(5 * (j0 + q)) * TILE + rec] - ml);
+        for (int q = 0; q < NCMP; ++q) sl += __expf(sO[(5 * (j0 + q)) * TILE + rec] - ml);
         sXm[h * TILE + rec] = ml;
         sXs[h * TILE + rec] = sl;
         __syncthreads();
@@ -885,9 +926,9 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
         for (int g = 0; g < TPR; ++g) lmax = fmaxf(lmax, sXm[g * TILE + rec]);
         float lsm = 0.0f;
 #pragma unroll
-        for (int g = 0; g < TPR; ++g) lsm += sXs[g * TILE + rec] * expf(sXm[g * TILE + rec] - lmax);
-        const float lse = lmax + logf(lsm);
-        float lp[NCMP];
+        for (int g = 0; g < TPR; ++g) lsm += sXs[g * TILE + rec] * __expf(sXm[g * TILE + rec] - lmax);
+        const float lse = lmax + __logf(lsm);
+        float lp[NCMP], kq[NCMP], csq[NCMP], mu[NCMP][3], fin[NCMP];
 #pragma unroll
         for (int q = 0; q < NCMP; ++q) {
             const int j = j0 + q;
@@ -895,17 +936,24 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
                         mz = sO[(5 * j + 3) * TILE + rec];
             const float mn = sqrtf(mx * mx + my * my + mz * mz);
             const float inv = mn > 0.0f ? 1.0f / mn : 0.0f;
-            const float k = expf(fminf(fmaxf(sO[(5 * j + 4) * TILE + rec], S_MIN), S_MAX));
-            const float cs = mx * inv * d[0] + my * inv * d[1] + mz * inv * d[2];
-            const float lognorm = logf(k) - logf(2.0f * kPi) - logf(-expm1f(-2.0f * k));
+            const float k = __expf(fminf(fmaxf(sO[(5 * j + 4) * TILE + rec], S_MIN), S_MAX));
+            mu[q][0] = mx * inv;
+            mu[q][1] = my * inv;
+            mu[q][2] = mz * inv;
+            const float cs = mu[q][0] * d[0] + mu[q][1] * d[1] + mu[q][2] * d[2];
+            const float om = -expm1f(-2.0f * k);  // 1 - e^{-2k}
+            const float lognorm = __logf(k) - __logf(2.0f * kPi) - __logf(om);
             lp[q] = (sO[(5 * j) * TILE + rec] - lse) + lognorm + k * (cs - 1.0f);
+            kq[q] = k;
+            csq[q] = cs;
+            fin[q] = inv * k;  // kappa / |m|
         }
         float mq = -INFINITY;
 #pragma unroll
         for (int q = 0; q < NCMP; ++q) mq = fmaxf(mq, lp[q]);
         float sq = 0.0f;
 #pragma unroll
-        for (int q = 0; q < NCMP; ++q) sq += expf(lp[q] - mq);
+        for (int q = 0; q < NCMP; ++q) sq += __expf(lp[q] - mq);
         __syncthreads();  // everyone has read the logit maxima
         sXm[h * TILE + rec] = mq;
         sXs[h * TILE + rec] = sq;
@@ -915,8 +963,8 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
         for (int g = 0; g < TPR; ++g) qmax = fmaxf(qmax, sXm[g * TILE + rec]);
         float qs = 0.0f;
 #pragma unroll
-        for (int g = 0; g < TPR; ++g) qs += sXs[g * TILE + rec] * expf(sXm[g * TILE + rec] - qmax);
-        const float logq = qmax + logf(qs);
+        for (int g = 0; g < TPR; ++g) qs += sXs[g * TILE + rec] * __expf(sXm[g * TILE + rec] - qmax);
+        const float logq = qmax + __logf(qs);
         if (h == 0 && w > 0.0f) {
             lsum += w * -logq;
             wsum += w;
@@ -925,21 +973,17 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
         for (int q = 0; q < NCMP; ++q) {
             const int j = j0 + q;
             float *o = sO + (5 * j) * TILE + rec;
-            const float mx = o[TILE], my = o[2 * TILE], mz = o[3 * TILE], sraw = o[4 * TILE];
-            const float mn = sqrtf(mx * mx + my * my + mz * mz);
-            const float inv = mn > 0.0f ? 1.0f / mn : 0.0f;
-            const float mu0 = mx * inv, mu1 = my * inv, mu2 = mz * inv;
-            const float k = expf(fminf(fmaxf(sraw, S_MIN), S_MAX));
-            const float cs = mu0 * d[0] + mu1 * d[1] + mu2 * d[2];
-            const float rr = expf(lp[q] - logq);  // responsibility
-            const float pi = expf(o[0] - lse);
-            const float f = mn > 0.0f ? -w * rr * k / mn : 0.0f;
+            const float sraw = o[4 * TILE];
+            const float k = kq[q], cs = csq[q];
+            const float rr = __expf(lp[q] - logq);  // responsibility
+            const float pi = __expf(o[0] - lse);
+            const float f = -w * rr * fin[q];
             o[0] = w * (pi - rr);
-            o[TILE] = f * (d[0] - cs * mu0);
-            o[2 * TILE] = f * (d[1] - cs * mu1);
-            o[3 * TILE] = f * (d[2] - cs * mu2);
+            o[TILE] = f * (d[0] - cs * mu[q][0]);
+            o[2 * TILE] = f * (d[1] - cs * mu[q][1]);
+            o[3 * TILE] = f * (d[2] - cs * mu[q][2]);
             const bool inside = sraw > S_MIN && sraw < S_MAX;
-            const float e = expf(-2.0f * k);
+            const float e = __expf(-2.0f * k);
             const float tt = 2.0f * k * e / -expm1f(-2.0f * k);
             o[4 * TILE] = inside ? -w * rr * (1.0f - tt + k * (cs - 1.0f)) : 0.0f;
         }
@@ -1292,7 +1336,7 @@ int reduce_step(pg_mlp *M, uint32_t slot, float *grad_out, cudaStream_t s) {
         A.c1 = (float)(1.0 - pow((double)M->cfg.beta1, (double)M->step));
         A.c2 = (float)(1.0 - pow((double)M->cfg.beta2, (double)M->step));
     }
-    k_reduce_adam<<<(NPARAM + 255) / 256, 256, 0, s>>>(A);
+    k_reduce_adam<<<(NPARAM + 31) / 32, 32 * kAdamGroups, 0, s>>>(A);
     return cudaGetLastError() == cudaSuccess ? PG_OK : mlp_error(PG_ERR_CUDA, "surrogate update launch");
 }
 
