@@ -427,7 +427,8 @@ typedef struct pg_material {
     float specular[3];  /* Phong specular reflectance */
     float exponent;     /* Phong exponent (specularHighlight) */
     float eta, k;       /* conductor and Beckmann conductor: Fresnel eta and k (one spectrum value) */
-    int32_t reserved;
+    int32_t texture;    /* 0: none; t: scene texture t - 1, which scales a diffuse albedo
+                           (textureIdDiffuse) and alpha-tests every hit (raytrace.rahit) */
 } pg_material;
 
 typedef struct pg_sphere {
@@ -549,6 +550,17 @@ int pg_scene_export(const pg_scene *scene, void *nodes, float *tri_verts, uint32
 /* Host copies of the vertex positions (3 floats each, n_vertices of them) and
  * triangle indices (3 per triangle, original order). */
 int pg_scene_export_mesh(const pg_scene *scene, float *positions, uint32_t *indices, uint32_t *n_vertices);
+/* Material textures (Mitsuba bitmap textures, PNG; SceneLoader::addTexture,
+ * src/SceneLoader.cpp:184-233): the count and total texel count, then host
+ * copies of the texture coordinates (6 floats per triangle, original order),
+ * per texture {first texel, width, height, 0} and the RGBA8 texels (rows from
+ * the top).  Any output pointer may be NULL. */
+int pg_scene_texture_sizes(const pg_scene *scene, uint32_t *n_textures, uint64_t *n_texels);
+int pg_scene_export_textures(const pg_scene *scene, float *tri_uv, uint32_t *tex_info, uint8_t *texels);
+/* Decodes a PNG file (8-bit grey, grey + alpha, RGB, RGBA or palette,
+ * non-interlaced) to RGBA8: *width and *height are set; rgba_out (NULL: a size
+ * query) receives width * height * 4 bytes, PG_ERR_ARG if capacity is smaller. */
+int pg_png_read(const char *path, uint8_t *rgba_out, uint64_t capacity, uint32_t *width, uint32_t *height);
 /* Replaces the camera (SceneLoader origin/target/upDir/vfov, src/SceneLoader.h:147-150)
  * and the image size. */
 int pg_scene_set_camera(pg_scene *scene, const pg_camera *cam);

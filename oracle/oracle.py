@@ -276,7 +276,8 @@ class PgoScene(C.Structure):
     _fields_ = [("nodes", _P), ("n_nodes", _U32), ("tri_verts", _P), ("n_tris", _U32), ("pos", _P),
                 ("n_vertices", _U32), ("idx", _P), ("tri_mat", _P), ("mats", _P), ("n_mats", _U32),
                 ("spheres", _P), ("n_spheres", _U32), ("camera", abi.Camera), ("env", _P), ("env_w", _U32),
-                ("env_h", _U32)]
+                ("env_h", _U32), ("tri_uv", _P), ("tex_info", _P), ("tex_data", _P), ("n_tex", _U32),
+                ("alpha_salt", _U32)]
 
 
 class PgoGuide(C.Structure):
@@ -310,6 +311,12 @@ class TraceOracle:
                      camera if camera is not None else exp["info"].camera,
                      env.ctypes.data if env is not None else None, env.shape[1] if env is not None else 0,
                      env.shape[0] if env is not None else 0)
+        if "tri_uv" in keep and keep["tri_uv"].size:
+            s.tri_uv = keep["tri_uv"].ctypes.data
+        if "tex_info" in keep and keep["tex_info"].shape[0]:
+            s.tex_info = keep["tex_info"].ctypes.data
+            s.tex_data = keep["tex_data"].ctypes.data
+            s.n_tex = keep["tex_info"].shape[0]
         return s, keep
 
     def closest(self, exp, rays, threads=None):

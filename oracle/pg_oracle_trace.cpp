@@ -131,6 +131,58 @@ float bitsf(uint32_t u) {
     return f;
 }
 
+// Alpha test of a textured hit (raytrace.rahit:21-46, device alpha_keep in
+// pg_traverse.cuh): same operations in the same order, each rounded to FP32
+// (the file is compiled without FMA contraction).
+uint32_t tea16(uint32_t v0, uint32_t v1) {
+    uint32_t s0 = 0;
+    for (int n = 0; n < 16; ++n) {
+        s0 += 0x9e3779b9u;
+        v0 += ((v1 << 4) + 0xa341316cu) ^ (v1 + s0) ^ ((v1 >> 5) + 0xc8013ea4u);
+        v1 += ((v0 << 4) + 0xad90777du) ^ (v0 + s0) ^ ((v0 >> 5) + 0x7e95761eu);
+    }
+    return v0;
+}
+
+float tex_alpha(const pgo_scene &S, uint32_t tex, float u, float v) {
+    const uint32_t *ti = S.tex_info + 4 * (size_t)tex;
+    const int w = (int)ti[1], h = (int)ti[2];
+    u = u - floorf(u);
+    v = v - floorf(v);
+    const float x = u * (float)w - 0.5f, y = v * (float)h - 0.5f;
+    const float x0 = floorf(x), y0 = floorf(y);
+    const float fx = x - x0, fy = y - y0;
+    int ix0 = (int)x0, iy0 = (int)y0;
+    int ix1 = ix0 + 1, iy1 = iy0 + 1;
+    ix0 = ix0 < 0 ? ix0 + w : ix0;
+    iy0 = iy0 < 0 ? iy0 + h : iy0;
+    ix1 = ix1 >= w ? ix1 - w : ix1;
+    iy1 = iy1 >= h ? iy1 - h : iy1;
+    const uint8_t *d = S.tex_data + 4 * (size_t)ti[0];
+    const float k = 1.0f / 255.0f;
+    const float a00 = (float)d[4 * (iy0 * w + ix0) + 3] * k, a10 = (float)d[4 * (iy0 * w + ix1) + 3] * k;
+    const float a01 = (float)d[4 * (iy1 * w + ix0) + 3] * k, a11 = (float)d[4 * (iy1 * w + ix1) + 3] * k;
+    const float gx = 1.0f - fx, gy = 1.0f - fy;
+    const float top = a00 * gx + a10 * fx;
+    const float bot = a01 * gx + a11 * fx;
+    return top * gy + bot * fy;
+}
+
+bool alpha_keep(const pgo_scene &S, float org_x, uint32_t id, uint32_t tex, float bu, float bv, float t) {
+    const float *uv = S.tri_uv + 6 * (size_t)id;
+    const float w0 = (1.0f - bu) - bv;
+    const float tu = (uv[0] * w0 + uv[2] * bu) + uv[4] * bv;
+    const float tv = (uv[1] * w0 + uv[3] * bu) + uv[5] * bv;
+    const float a = tex_alpha(S, tex - 1u, tu, tv);
+    const float sx = fminf(fmaxf(tu * 100000000.0f + org_x * t, -4.0e18f), 4.0e18f);
+    uint32_t seed = tea16((uint32_t)(long long)sx, S.alpha_salt);
+    seed = 1664525u * seed + 1013904223u;
+    const float r = (float)(seed & 0x00FFFFFFu) * (1.0f / 16777216.0f);
+    return !(r > a);
+}
+
+uint32_t tri_tex(const float *tv) { return fbits(tv[7]); }
+
 // One node step of the device traversal (trav_step in pg_traverse.cuh), same
 // order: four box tests against the best t at the start of the step, leaves
 // in slot order, inner children nearest first (closest: stable by entry
@@ -151,8 +203,10 @@ bool node_step(const pgo_scene &S, const RayPre &r, float tmin, float &best_t, u
             const float *tv = S.tri_verts + 12 * (size_t)(n.child[j] + k);
             ++n_tris;
             float t, u, v;
+            const uint32_t tex = tri_tex(tv);
             if (kAny) {
-                if (tri_intersect(r, tv, tv + 4, tv + 8, tmin, best_t, t, u, v)) {
+                if (tri_intersect(r, tv, tv + 4, tv + 8, tmin, best_t, t, u, v) &&
+                    (tex == 0u || alpha_keep(S, r.org[0], fbits(tv[3]), tex, u, v, t))) {
                     best_id = fbits(tv[3]);
                     return true;
                 }
@@ -160,7 +214,8 @@ bool node_step(const pgo_scene &S, const RayPre &r, float tmin, float &best_t, u
                 const uint32_t id = fbits(tv[3]);
                 const float lim = best_id == PG_NO_HIT ? best_t : bitsf(fbits(best_t) + 1u);
                 if (tri_intersect(r, tv, tv + 4, tv + 8, tmin, lim, t, u, v) &&
-                    (t < best_t || (t == best_t && id < best_id))) {
+                    (t < best_t || (t == best_t && id < best_id)) &&
+                    (tex == 0u || alpha_keep(S, r.org[0], id, tex, u, v, t))) {
                     best_t = t;
                     best_id = id;
                     best_u = u;
@@ -311,6 +366,7 @@ struct Light {
 struct Hit64 {
     double t;
     uint32_t prim;
+    double u = 0.0, v = 0.0;  // barycentrics of the triangle's second and third corners
 };
 
 struct Scene64 {
@@ -320,7 +376,7 @@ struct Scene64 {
 };
 
 // double-precision closest hit (Moller-Trumbore over the same BVH)
-bool tri64(D3 o, D3 d, D3 a, D3 b, D3 c, double tmin, double tmax, double &t) {
+bool tri64(D3 o, D3 d, D3 a, D3 b, D3 c, double tmin, double tmax, double &t, double &bu, double &bv) {
     const D3 e1 = b - a, e2 = c - a;
     const D3 p = cross(d, e2);
     const double det = dot(e1, p);
@@ -335,6 +391,8 @@ bool tri64(D3 o, D3 d, D3 a, D3 b, D3 c, double tmin, double tmax, double &t) {
     const double tt = dot(e2, q) * inv;
     if (!(tt > tmin && tt < tmax)) return false;
     t = tt;
+    bu = u;
+    bv = v;
     return true;
 }
 
@@ -372,6 +430,36 @@ bool sphere64(D3 o, D3 d, const pg_sphere &s, double tmin, double tmax, double &
     return false;
 }
 
+// sRGB byte to linear, and the bilinear linear-RGB texture colour at a hit
+// (repeat addressing, texel centres at half-integers), in double.
+double srgb64(uint8_t b) {
+    const double c = b / 255.0;
+    return c <= 0.04045 ? c / 12.92 : pow((c + 0.055) / 1.055, 2.4);
+}
+D3 tex_rgb64(const pgo_scene &S, uint32_t prim, uint32_t tex, double bu, double bv) {
+    const float *uv = S.tri_uv + 6 * (size_t)prim;
+    const double w0 = 1.0 - bu - bv;
+    double u = uv[0] * w0 + uv[2] * bu + uv[4] * bv, v = uv[1] * w0 + uv[3] * bu + uv[5] * bv;
+    const uint32_t *ti = S.tex_info + 4 * (size_t)tex;
+    const int w = (int)ti[1], h = (int)ti[2];
+    u -= floor(u);
+    v -= floor(v);
+    const double x = u * w - 0.5, y = v * h - 0.5, x0 = floor(x), y0 = floor(y), fx = x - x0, fy = y - y0;
+    int ix0 = (int)x0, iy0 = (int)y0, ix1 = ix0 + 1, iy1 = iy0 + 1;
+    ix0 = ix0 < 0 ? ix0 + w : ix0;
+    iy0 = iy0 < 0 ? iy0 + h : iy0;
+    ix1 = ix1 >= w ? ix1 - w : ix1;
+    iy1 = iy1 >= h ? iy1 - h : iy1;
+    const uint8_t *d = S.tex_data + 4 * (size_t)ti[0];
+    double c[3];
+    for (int k = 0; k < 3; ++k) {
+        const double top = srgb64(d[4 * (iy0 * w + ix0) + k]) * (1 - fx) + srgb64(d[4 * (iy0 * w + ix1) + k]) * fx;
+        const double bot = srgb64(d[4 * (iy1 * w + ix0) + k]) * (1 - fx) + srgb64(d[4 * (iy1 * w + ix1) + k]) * fx;
+        c[k] = top * (1 - fy) + bot * fy;
+    }
+    return d3(c[0], c[1], c[2]);
+}
+
 Hit64 intersect64(const pgo_scene &S, D3 o, D3 d, double tmin, double tmax, bool any) {
     Hit64 h{tmax, PG_NO_HIT};
     for (uint32_t i = 0; i < S.n_spheres; ++i) {
@@ -396,10 +484,14 @@ Hit64 intersect64(const pgo_scene &S, D3 o, D3 d, double tmin, double tmax, bool
             if (n.count[c] > 0) {
                 for (int k = 0; k < n.count[c]; ++k) {
                     const float *tv = S.tri_verts + 12 * (size_t)(n.child[c] + k);
-                    double t;
-                    if (tri64(o, d, fv(tv), fv(tv + 4), fv(tv + 8), tmin, h.t, t)) {
+                    double t, bu, bv;
+                    if (tri64(o, d, fv(tv), fv(tv + 4), fv(tv + 8), tmin, h.t, t, bu, bv) &&
+                        (tri_tex(tv) == 0u ||
+                         alpha_keep(S, (float)o.x, fbits(tv[3]), tri_tex(tv), (float)bu, (float)bv, (float)t))) {
                         h.t = t;
                         h.prim = fbits(tv[3]);
+                        h.u = bu;
+                        h.v = bv;
                         if (any) return h;
                     }
                 }
@@ -661,7 +753,14 @@ D3 render_pixel(const Scene64 &sc, const pg_render_params &rp, const pgo_guide *
             ng = unit(cross(v1 - v0, v2 - v0));
             mat_id = S.tri_mat[t];
         }
-        const pg_material &m = S.mats[mat_id];
+        pg_material m = S.mats[mat_id];
+        if (m.texture > 0 && !(h.prim & PG_SPHERE_BIT) && (m.type == PG_MAT_DIFFUSE || m.type == PG_MAT_PHONG)) {
+            // diffuse reflectance times the texture (raytrace.rgen:233-249)
+            const D3 tc = tex_rgb64(S, h.prim, (uint32_t)m.texture - 1u, h.u, h.v);
+            m.albedo[0] = (float)(m.albedo[0] * tc.x);
+            m.albedo[1] = (float)(m.albedo[1] * tc.y);
+            m.albedo[2] = (float)(m.albedo[2] * tc.z);
+        }
         const bool front = dot(d, ng) < 0.0;
         const D3 n = front ? ng : ng * -1.0;
         const D3 wi = d * -1.0;
@@ -857,7 +956,9 @@ void pgo_trace_any(const pgo_scene *s, const pg_ray *rays, uint32_t n, uint32_t 
 void pgo_render_f64(const pgo_scene *s, const pg_render_params *rp, const pgo_guide *guide, double *image,
                     uint32_t row_begin, uint32_t row_end, int n_threads) {
     Scene64 sc;
-    sc.S = s;
+    pgo_scene sa = *s;  // the frame's alpha-test salt, as the device renderer derives it
+    sa.alpha_salt = fmix32(rp->seed ^ 0x5bd1e995u);
+    sc.S = &sa;
     sc.tri_light.assign(s->n_tris, -1);
     // lights: one per emissive material over triangles (area-weighted), one per emissive sphere
     for (uint32_t m = 0; m < s->n_mats; ++m) {

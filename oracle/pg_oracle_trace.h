@@ -36,6 +36,11 @@ typedef struct pgo_scene {
     pg_camera camera;
     const float *env;           /* environment map, RGB per texel, or NULL */
     uint32_t env_w, env_h;
+    const float *tri_uv;        /* 6 per original triangle, or NULL */
+    const uint32_t *tex_info;   /* per texture: first texel, width, height, 0 */
+    const uint8_t *tex_data;    /* RGBA8 texels */
+    uint32_t n_tex;
+    uint32_t alpha_salt;        /* the alpha test's per-frame salt (traversal queries) */
 } pgo_scene;
 
 typedef struct pgo_guide {

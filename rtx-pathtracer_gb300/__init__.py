@@ -96,6 +96,9 @@ SIGNATURES = {
     "pg_scene_get_info": (_I, [_P, C.POINTER(abi.SceneInfo)]),
     "pg_scene_export": (_I, [_P, _P, _P, _P, _P, _P, _P]),
     "pg_scene_export_mesh": (_I, [_P, _P, _P, C.POINTER(_U32)]),
+    "pg_scene_texture_sizes": (_I, [_P, C.POINTER(_U32), C.POINTER(_U64)]),
+    "pg_scene_export_textures": (_I, [_P, _P, _P, _P]),
+    "pg_png_read": (_I, [C.c_char_p, _P, _U64, C.POINTER(_U32), C.POINTER(_U32)]),
     "pg_scene_set_camera": (_I, [_P, C.POINTER(abi.Camera)]),
     "pg_trace_closest": (_I, [_P, _P, _U32, _P, _P]),
     "pg_trace_any": (_I, [_P, _P, _U32, _P, _P]),
@@ -453,6 +456,20 @@ def fit_regions_noalloc(cfg: abi.FitConfig, states_dev, dirw, offsets, n_regions
                                             n_regions, mode, _stream_handle(stream))
 
 
+def read_png(path) -> np.ndarray:
+    """A PNG image as (height, width, 4) uint8 RGBA (pg_png_read)."""
+    lib = library()
+    w, h = C.c_uint32(), C.c_uint32()
+    st = lib.pg_png_read(str(path).encode(), None, 0, C.byref(w), C.byref(h))
+    if st != abi.PG_OK:
+        raise PathGuideError(st, lib.pg_last_error(None).decode())
+    out = np.zeros((h.value, w.value, 4), dtype=np.uint8)
+    st = lib.pg_png_read(str(path).encode(), out.ctypes.data, out.size, C.byref(w), C.byref(h))
+    if st != abi.PG_OK:
+        raise PathGuideError(st, lib.pg_last_error(None).decode())
+    return out
+
+
 def read_exr(path) -> np.ndarray:
     """An OpenEXR image as (height, width, 3) float32 (pg_exr_read)."""
     lib = library()
@@ -547,6 +564,13 @@ class Scene:
         self._check(self.lib.pg_scene_export_mesh(self.h, pos.ctypes.data, idx.ctypes.data, C.byref(nv)))
         out = {"nodes": nodes, "tri_verts": tv, "tri_order": order, "tri_mat": tmat, "mats": mats,
                "spheres": sph, "pos": pos, "idx": idx, "info": i}
+        nt, ntx = C.c_uint32(), C.c_uint64()
+        self._check(self.lib.pg_scene_texture_sizes(self.h, C.byref(nt), C.byref(ntx)))
+        out["tri_uv"] = np.zeros((i.n_triangles, 6), dtype=np.float32)
+        out["tex_info"] = np.zeros((nt.value, 4), dtype=np.uint32)
+        out["tex_data"] = np.zeros((ntx.value, 4), dtype=np.uint8)
+        self._check(self.lib.pg_scene_export_textures(self.h, out["tri_uv"].ctypes.data, out["tex_info"].ctypes.data,
+                                                      out["tex_data"].ctypes.data))
         env = self.envmap()
         if env is not None:
             out["env"] = env

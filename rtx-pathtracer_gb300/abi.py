@@ -81,7 +81,7 @@ SPHERE_BIT = 0x80000000
 
 MATERIAL_DTYPE = np.dtype([("type", "<i4"), ("albedo", "<f4", (3,)), ("emission", "<f4", (3,)),
                            ("roughness", "<f4"), ("ior", "<f4"), ("specular", "<f4", (3,)), ("exponent", "<f4"),
-                           ("eta", "<f4"), ("k", "<f4"), ("reserved", "<i4")])
+                           ("eta", "<f4"), ("k", "<f4"), ("texture", "<i4")])
 SPHERE_DTYPE = np.dtype([("center", "<f4", (3,)), ("radius", "<f4"), ("material", "<u4"), ("reserved", "<u4", (3,))])
 RAY_DTYPE = np.dtype([("org", "<f4", (3,)), ("tmin", "<f4"), ("dir", "<f4", (3,)), ("tmax", "<f4")])
 HIT_DTYPE = np.dtype([("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("prim", "<u4")])

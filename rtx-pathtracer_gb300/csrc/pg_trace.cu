@@ -35,6 +35,7 @@
 #include <vector>
 
 #include "../host/pg_exr.h"
+#include "../host/pg_png.h"
 #include "../host/pg_scene.h"
 #include "pg_internal.cuh"
 #include "pg_traverse.cuh"
@@ -359,6 +360,44 @@ __device__ V vmm_sample(const pg_vmm_theta &v, V x, int par, float u_lobe, float
 // ---------------------------------------------------------------------------
 // Device scene and render state
 // ---------------------------------------------------------------------------
+// Per-frame salt of the alpha test (the reference's push-constant random number).
+__host__ __device__ inline uint32_t alpha_salt(uint32_t seed) { return fmix32(seed ^ 0x5bd1e995u); }
+
+// sRGB-encoded byte to linear (the sRGB texture format's decode before filtering).
+__device__ __forceinline__ float srgb_to_linear(uint8_t b) {
+    const float c = (float)b * (1.0f / 255.0f);
+    return c <= 0.04045f ? c * (1.0f / 12.92f) : powf((c + 0.055f) * (1.0f / 1.055f), 2.4f);
+}
+
+// Bilinear linear-RGB colour of texture `tex` at the texture coordinate of the
+// hit (barycentrics bu, bv) on original triangle `prim` (repeat addressing).
+__device__ __forceinline__ void tex_rgb(const DevScene &S, uint32_t prim, uint32_t tex, float bu, float bv,
+                                        float out[3]) {
+    const float *uv = S.tri_uv + 6 * (size_t)prim;
+    const float w0 = 1.0f - bu - bv;
+    float u = uv[0] * w0 + uv[2] * bu + uv[4] * bv, v = uv[1] * w0 + uv[3] * bu + uv[5] * bv;
+    const uint4 ti = S.tex_info[tex];
+    const int w = (int)ti.y, h = (int)ti.z;
+    u -= floorf(u);
+    v -= floorf(v);
+    const float x = u * (float)w - 0.5f, y = v * (float)h - 0.5f;
+    const float x0 = floorf(x), y0 = floorf(y), fx = x - x0, fy = y - y0;
+    int ix0 = (int)x0, iy0 = (int)y0, ix1 = ix0 + 1, iy1 = iy0 + 1;
+    ix0 = ix0 < 0 ? ix0 + w : ix0;
+    iy0 = iy0 < 0 ? iy0 + h : iy0;
+    ix1 = ix1 >= w ? ix1 - w : ix1;
+    iy1 = iy1 >= h ? iy1 - h : iy1;
+    const uchar4 *d = S.tex_data + ti.x;
+    const uchar4 t00 = d[iy0 * w + ix0], t10 = d[iy0 * w + ix1], t01 = d[iy1 * w + ix0], t11 = d[iy1 * w + ix1];
+    const uint8_t c00[3] = {t00.x, t00.y, t00.z}, c10[3] = {t10.x, t10.y, t10.z}, c01[3] = {t01.x, t01.y, t01.z},
+                  c11[3] = {t11.x, t11.y, t11.z};
+    for (int c = 0; c < 3; ++c) {
+        const float top = srgb_to_linear(c00[c]) * (1.0f - fx) + srgb_to_linear(c10[c]) * fx;
+        const float bot = srgb_to_linear(c01[c]) * (1.0f - fx) + srgb_to_linear(c11[c]) * fx;
+        out[c] = top * (1.0f - fy) + bot * fy;
+    }
+}
+
 struct DevRender {
     DevScene S;
     const float *pos;            // 3 per vertex (original)
@@ -601,7 +640,13 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
             ng = nrm(cross3(sub(v1, v0), sub(v2, v0)));
             mat_id = R.tri_mat[t];
         }
-        const pg_material m = R.mats[mat_id];
+        pg_material m = R.mats[mat_id];
+        if (m.texture > 0 && !(h.prim & PG_SPHERE_BIT) && (m.type == PG_MAT_DIFFUSE || m.type == PG_MAT_PHONG)) {
+            // diffuse reflectance times the texture (raytrace.rgen:233-249)
+            float tc[3];
+            tex_rgb(R.S, h.prim, (uint32_t)m.texture - 1u, h.u, h.v, tc);
+            for (int c = 0; c < 3; ++c) m.albedo[c] *= tc[c];
+        }
         const bool front = dot3(d, ng) < 0.0f;  // raytrace.rchit:42-48
         const V n = front ? ng : mul(ng, -1.0f);
         const V wi = mul(d, -1.0f);
@@ -1010,6 +1055,9 @@ struct pg_scene {
     float *d_light_cdf = nullptr;
     int32_t *d_tri_light = nullptr;
     float *d_env = nullptr;
+    float *d_tri_uv = nullptr;
+    uint4 *d_tex_info = nullptr;
+    uchar4 *d_tex_data = nullptr;
     unsigned long long *d_stats = nullptr;
     uint32_t n_lights = 0;
     bool uploaded = false;
@@ -1142,6 +1190,18 @@ int ensure_uploaded(pg_scene *sc) {
     if (!st) st = upload(&sc->d_light_cdf, sc->h_light_cdf);
     if (!st) st = upload(&sc->d_tri_light, sc->h_tri_light);
     if (!st) st = upload(&sc->d_env, s.env);
+    if (!st) st = upload(&sc->d_tri_uv, s.tri_uv);
+    if (!st && !s.textures.empty()) {
+        std::vector<uint4> info;
+        std::vector<uchar4> texels;
+        for (const auto &t : s.textures) {
+            info.push_back(make_uint4((uint32_t)texels.size(), t.w, t.h, 0u));
+            for (size_t i = 0; i < (size_t)t.w * t.h; ++i)
+                texels.push_back(make_uchar4(t.rgba[4 * i], t.rgba[4 * i + 1], t.rgba[4 * i + 2], t.rgba[4 * i + 3]));
+        }
+        st = upload(&sc->d_tex_info, info);
+        if (!st) st = upload(&sc->d_tex_data, texels);
+    }
     if (!st && cudaMalloc(&sc->d_counters, sizeof(uint32_t) * 16) != cudaSuccess) st = PG_ERR_CUDA;
     if (!st && cudaMalloc(&sc->d_stats, sizeof(unsigned long long) * kNumStats) != cudaSuccess) st = PG_ERR_CUDA;
     if (st) return scene_error(st, "scene upload failed (CUDA)");
@@ -1206,6 +1266,10 @@ DevScene dev_scene(const pg_scene *sc) {
     S.spheres = sc->d_spheres;
     S.n_spheres = (uint32_t)sc->host.spheres.size();
     S.n_triangles = (uint32_t)sc->host.tri_mat.size();
+    S.tri_uv = sc->d_tri_uv;
+    S.tex_info = sc->d_tex_info;
+    S.tex_data = sc->d_tex_data;
+    S.alpha_salt = 0u;
     return S;
 }
 
@@ -1318,10 +1382,56 @@ int pg_scene_destroy(pg_scene *sc) {
     cudaFree(sc->d_light_cdf);
     cudaFree(sc->d_tri_light);
     cudaFree(sc->d_env);
+    cudaFree(sc->d_tri_uv);
+    cudaFree(sc->d_tex_info);
+    cudaFree(sc->d_tex_data);
     cudaFree(sc->d_stats);
     cudaFree(sc->d_counters);
     for (void *b : sc->bufs) cudaFree(b);
     delete sc;
+    return PG_OK;
+}
+
+int pg_scene_texture_sizes(const pg_scene *sc, uint32_t *n_textures, uint64_t *n_texels) {
+    if (!sc) return PG_ERR_ARG;
+    uint64_t n = 0;
+    for (const auto &t : sc->host.textures) n += (uint64_t)t.w * t.h;
+    if (n_textures) *n_textures = (uint32_t)sc->host.textures.size();
+    if (n_texels) *n_texels = n;
+    return PG_OK;
+}
+
+int pg_scene_export_textures(const pg_scene *sc, float *tri_uv, uint32_t *tex_info, uint8_t *texels) {
+    if (!sc) return PG_ERR_ARG;
+    const SceneData &s = sc->host;
+    if (tri_uv) memcpy(tri_uv, s.tri_uv.data(), sizeof(float) * s.tri_uv.size());
+    uint64_t first = 0;
+    for (size_t i = 0; i < s.textures.size(); ++i) {
+        const auto &t = s.textures[i];
+        if (tex_info) {
+            tex_info[4 * i] = (uint32_t)first;
+            tex_info[4 * i + 1] = t.w;
+            tex_info[4 * i + 2] = t.h;
+            tex_info[4 * i + 3] = 0;
+        }
+        if (texels) memcpy(texels + 4 * first, t.rgba.data(), t.rgba.size());
+        first += (uint64_t)t.w * t.h;
+    }
+    return PG_OK;
+}
+
+int pg_png_read(const char *path, uint8_t *rgba_out, uint64_t capacity, uint32_t *width, uint32_t *height) {
+    if (!path || !width || !height) return PG_ERR_ARG;
+    uint32_t w = 0, h = 0;
+    std::vector<uint8_t> rgba;
+    std::string err;
+    if (!pg::read_png(path, w, h, rgba, err))
+        return set_error(nullptr, err.rfind("cannot open", 0) == 0 ? PG_ERR_IO : PG_ERR_PARSE, err);
+    *width = w;
+    *height = h;
+    if (!rgba_out) return PG_OK;  // size query
+    if (capacity < rgba.size()) return set_error(nullptr, PG_ERR_ARG, "PNG output buffer too small");
+    memcpy(rgba_out, rgba.data(), rgba.size());
     return PG_OK;
 }
 
@@ -1472,6 +1582,7 @@ int pg_render(pg_scene *sc, const pg_render_params *rp, pg_ctx *guide, float *im
         R.tan_half = tanf(cam.vfov_deg * 0.5f * 3.14159265f / 180.0f);
     }
     R.rp = *rp;
+    R.S.alpha_salt = alpha_salt(rp->seed);
     R.image = image;
     R.counters = sc->d_counters;
     R.guiding = rp->use_guiding ? 1 : 0;

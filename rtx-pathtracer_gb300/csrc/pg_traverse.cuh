@@ -27,11 +27,75 @@ static_assert(sizeof(DevBvhNode) == 128, "node layout");
 
 struct DevScene {
     const DevBvhNode *nodes;
-    const float4 *tris;           // 3 float4 per triangle in BVH order; tris[3i].w = original id (bits)
+    const float4 *tris;           // 3 float4 per triangle in BVH order; tris[3i].w = original id (bits),
+                                  // tris[3i+1].w = the material's texture (bits; 0 none)
     const pg_sphere *spheres;
     uint32_t n_spheres;
     uint32_t n_triangles;
+    const float *tri_uv;          // 6 per original triangle
+    const uint4 *tex_info;        // per texture: first texel, width, height
+    const uchar4 *tex_data;       // RGBA8 texels, rows from the top
+    uint32_t alpha_salt;          // per-frame salt of the alpha test's hash
 };
+
+// ---- alpha-tested hits (raytrace.rahit:21-46) --------------------------------
+// A hit on a textured triangle is ignored when a hash of (texture u, origin.x *
+// t) and the frame's salt, as a number in [0, 1), exceeds the texture's alpha
+// at the hit.  The arithmetic is spelled out with round-to-nearest operations
+// so the CPU traversal twin reproduces every decision.
+__host__ __device__ __forceinline__ uint32_t tea16(uint32_t v0, uint32_t v1) {
+    uint32_t s0 = 0;
+    for (int n = 0; n < 16; ++n) {
+        s0 += 0x9e3779b9u;
+        v0 += ((v1 << 4) + 0xa341316cu) ^ (v1 + s0) ^ ((v1 >> 5) + 0xc8013ea4u);
+        v1 += ((v0 << 4) + 0xad90777du) ^ (v0 + s0) ^ ((v0 >> 5) + 0x7e95761eu);
+    }
+    return v0;
+}
+
+// Bilinear alpha (repeat addressing, texel centres at half-integers) of texture
+// info {first, w, h} at (u, v).
+__device__ __forceinline__ float tex_alpha(const DevScene &S, uint32_t tex, float u, float v) {
+    const uint4 ti = __ldg(&S.tex_info[tex]);
+    const int w = (int)ti.y, h = (int)ti.z;
+    u = __fsub_rn(u, floorf(u));
+    v = __fsub_rn(v, floorf(v));
+    const float x = __fsub_rn(__fmul_rn(u, (float)w), 0.5f), y = __fsub_rn(__fmul_rn(v, (float)h), 0.5f);
+    const float x0 = floorf(x), y0 = floorf(y);
+    const float fx = __fsub_rn(x, x0), fy = __fsub_rn(y, y0);
+    int ix0 = (int)x0, iy0 = (int)y0;
+    int ix1 = ix0 + 1, iy1 = iy0 + 1;
+    ix0 = ix0 < 0 ? ix0 + w : ix0;
+    iy0 = iy0 < 0 ? iy0 + h : iy0;
+    ix1 = ix1 >= w ? ix1 - w : ix1;
+    iy1 = iy1 >= h ? iy1 - h : iy1;
+    const uchar4 *d = S.tex_data + ti.x;
+    const float k = 1.0f / 255.0f;
+    const float a00 = __fmul_rn((float)__ldg(&d[iy0 * w + ix0]).w, k), a10 = __fmul_rn((float)__ldg(&d[iy0 * w + ix1]).w, k);
+    const float a01 = __fmul_rn((float)__ldg(&d[iy1 * w + ix0]).w, k), a11 = __fmul_rn((float)__ldg(&d[iy1 * w + ix1]).w, k);
+    const float gx = __fsub_rn(1.0f, fx), gy = __fsub_rn(1.0f, fy);
+    const float top = __fadd_rn(__fmul_rn(a00, gx), __fmul_rn(a10, fx));
+    const float bot = __fadd_rn(__fmul_rn(a01, gx), __fmul_rn(a11, fx));
+    return __fadd_rn(__fmul_rn(top, gy), __fmul_rn(bot, fy));
+}
+
+// Whether the hit (barycentrics bu, bv of v1, v2; distance t) on original
+// triangle `id` with texture `tex` (1-based) stands.
+__device__ __forceinline__ bool alpha_keep(const DevScene &S, const float org_x, uint32_t id, uint32_t tex, float bu,
+                                           float bv, float t) {
+    const float *uv = S.tri_uv + 6 * (size_t)id;
+    const float w0 = __fsub_rn(__fsub_rn(1.0f, bu), bv);
+    const float tu = __fadd_rn(__fadd_rn(__fmul_rn(__ldg(uv), w0), __fmul_rn(__ldg(uv + 2), bu)), __fmul_rn(__ldg(uv + 4), bv));
+    const float tv = __fadd_rn(__fadd_rn(__fmul_rn(__ldg(uv + 1), w0), __fmul_rn(__ldg(uv + 3), bu)), __fmul_rn(__ldg(uv + 5), bv));
+    const float a = tex_alpha(S, tex - 1u, tu, tv);
+    // uint(textureUV * 1e8 + origin.x * t): the first component, converted through a
+    // clamped 64-bit integer (the shader's conversion is undefined out of range)
+    const float sx = fminf(fmaxf(__fadd_rn(__fmul_rn(tu, 100000000.0f), __fmul_rn(org_x, t)), -4.0e18f), 4.0e18f);
+    uint32_t seed = tea16((uint32_t)(long long)sx, S.alpha_salt);
+    seed = 1664525u * seed + 1013904223u;  // lcg, then rnd in [0, 1)
+    const float r = (float)(seed & 0x00FFFFFFu) * (1.0f / 16777216.0f);
+    return !(r > a);
+}
 
 struct RayPre {
     float org[3], dir[3], inv[3];
@@ -237,8 +301,10 @@ __device__ __forceinline__ bool trav_step(const DevScene &S, TravState &st, int 
             const float4 v0 = __ldg(&S.tris[3 * ti]), v1 = __ldg(&S.tris[3 * ti + 1]), v2 = __ldg(&S.tris[3 * ti + 2]);
             ctr.tri();
             float t, u, v;
+            const uint32_t tex = __float_as_uint(v1.w);
             if (kAny) {
-                if (tri_intersect(st.r, v0, v1, v2, st.tmin, st.tmax, t, u, v)) {
+                if (tri_intersect(st.r, v0, v1, v2, st.tmin, st.tmax, t, u, v) &&
+                    (tex == 0u || alpha_keep(S, st.r.org[0], __float_as_uint(v0.w), tex, u, v, t))) {
                     st.best_id = __float_as_uint(v0.w);
                     return true;
                 }
@@ -247,7 +313,8 @@ __device__ __forceinline__ bool trav_step(const DevScene &S, TravState &st, int 
                 // one ulp above the best t, so an equal t is seen and the lower id wins
                 const float lim = st.best_id == PG_NO_HIT ? st.tmax : __uint_as_float(__float_as_uint(st.tmax) + 1u);
                 if (tri_intersect(st.r, v0, v1, v2, st.tmin, lim, t, u, v) &&
-                    (t < st.tmax || (t == st.tmax && id < st.best_id))) {
+                    (t < st.tmax || (t == st.tmax && id < st.best_id)) &&
+                    (tex == 0u || alpha_keep(S, st.r.org[0], id, tex, u, v, t))) {
                     st.tmax = t;
                     st.best_id = id;
                     st.best_u = u;

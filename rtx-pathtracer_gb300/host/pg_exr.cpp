@@ -450,4 +450,6 @@ bool write_exr(const std::string &path, const float *rgb, uint32_t width, uint32
     return true;
 }
 
+bool zlib_inflate(const uint8_t *src, size_t n, std::vector<uint8_t> &out) { return inflate_zlib(src, n, out); }
+
 }  // namespace pg

@@ -2,6 +2,7 @@
 // binned-SAH BVH builder (host side of the tracer).
 #include "pg_scene.h"
 #include "pg_exr.h"
+#include "pg_png.h"
 
 #include <math.h>
 #include <stdio.h>
@@ -56,6 +57,7 @@ void add_tri(SceneData &s, uint32_t a, uint32_t b, uint32_t c, uint32_t m) {
     s.idx.push_back(b);
     s.idx.push_back(c);
     s.tri_mat.push_back(m);
+    s.tri_uv.insert(s.tri_uv.end(), 6, 0.0f);
 }
 
 }  // namespace
@@ -496,6 +498,11 @@ void build_bvh(SceneData &s, int max_leaf) {
         }
         uint32_t id = t;
         memcpy(&s.tri_verts[12 * (size_t)i + 3], &id, 4);
+        // v1.w: the material's texture (0 none), so traversal knows which hits to alpha-test
+        // without another load
+        const uint32_t m = s.tri_mat[t];
+        const int32_t tex = m < s.mats.size() ? s.mats[m].texture : 0;
+        memcpy(&s.tri_verts[12 * (size_t)i + 7], &tex, 4);
     }
 }
 
@@ -528,7 +535,7 @@ bool load_obj(SceneData &s, const std::string &path, const float *to_world, uint
         s.error = "cannot open OBJ file " + path;
         return false;
     }
-    std::vector<float> vp;
+    std::vector<float> vt;  // u, 1 - v (src/SceneLoader.cpp:288-291)
     std::string line;
     const uint32_t base_tri = (uint32_t)s.tri_mat.size();
     std::vector<uint32_t> local_to_global;
@@ -544,19 +551,46 @@ bool load_obj(SceneData &s, const std::string &path, const float *to_world, uint
             else
                 memcpy(o, p, sizeof o);
             local_to_global.push_back(add_vertex(s, v3(o[0], o[1], o[2])));
+        } else if (tag == "vt") {
+            float u = 0.0f, v = 0.0f;
+            ls >> u >> v;
+            vt.push_back(u);
+            vt.push_back(1.0f - v);
         } else if (tag == "f") {
             std::vector<uint32_t> ids;
+            std::vector<long> tex;  // texture coordinate index per corner, -1 without one
             std::string tok;
             while (ls >> tok) {
-                long v = strtol(tok.c_str(), nullptr, 10);
+                char *endp = nullptr;
+                long v = strtol(tok.c_str(), &endp, 10);
                 if (v < 0) v = (long)local_to_global.size() + v + 1;
                 if (v < 1 || (size_t)v > local_to_global.size()) {
                     s.error = "OBJ face index out of range in " + path;
                     return false;
                 }
                 ids.push_back(local_to_global[(size_t)v - 1]);
+                long t = -1;
+                if (endp && *endp == '/' && endp[1] != '/' && endp[1] != 0) {
+                    t = strtol(endp + 1, nullptr, 10);
+                    if (t < 0) t = (long)(vt.size() / 2) + t + 1;
+                    if (t < 1 || (size_t)t > vt.size() / 2) {
+                        s.error = "OBJ texture coordinate index out of range in " + path;
+                        return false;
+                    }
+                    --t;
+                }
+                tex.push_back(t);
             }
-            for (size_t k = 2; k < ids.size(); ++k) add_tri(s, ids[0], ids[k - 1], ids[k], material);
+            for (size_t k = 2; k < ids.size(); ++k) {
+                add_tri(s, ids[0], ids[k - 1], ids[k], material);
+                const long c[3] = {tex[0], tex[k - 1], tex[k]};
+                float *uv = &s.tri_uv[s.tri_uv.size() - 6];
+                for (int q = 0; q < 3; ++q)
+                    if (c[q] >= 0) {
+                        uv[2 * q] = vt[2 * (size_t)c[q]];
+                        uv[2 * q + 1] = vt[2 * (size_t)c[q] + 1];
+                    }
+            }
         }
     }
     if (s.tri_mat.size() == base_tri) {
@@ -746,7 +780,7 @@ std::string read_string(const XNode &n, const std::string &name) {
 // parseXmlBSDF (src/SceneLoader.cpp:558-611): diffuse, phong, dielectric,
 // conductor (a mirror when its material is "none"), roughconductor (Beckmann);
 // roughplastic as GGX, anything else diffuse.
-uint32_t bsdf_material(SceneData &s, const XNode &b) {
+uint32_t bsdf_material(SceneData &s, const XNode &b, const std::map<std::string, int32_t> &textures) {
     const XNode *bb = &b;
     if (b.attr.count("type") && b.attr.at("type") == "twosided" && !b.kids.empty()) {
         for (auto &k : b.kids)
@@ -783,6 +817,15 @@ uint32_t bsdf_material(SceneData &s, const XNode &b) {
     if (type == "roughplastic")
         return add_material(s, PG_MAT_GGX, read_rgb(*bb, "specularReflectance", v3(1, 1, 1)), v3(0, 0, 0),
                             read_float(*bb, "alpha", 0.1f), 1);
+    // a diffuse reflectance given by a texture reference: white, scaled by the
+    // texture (src/SceneLoader.cpp:574-587)
+    for (auto &k : bb->kids)
+        if (k.name == "ref" && k.attr.count("name") && k.attr.at("name") == "reflectance" && k.attr.count("id") &&
+            textures.count(k.attr.at("id"))) {
+            const uint32_t id = add_material(s, PG_MAT_DIFFUSE, v3(1, 1, 1), v3(0, 0, 0), 0, 1);
+            s.mats[id].texture = textures.at(k.attr.at("id")) + 1;
+            return id;
+        }
     return add_material(s, PG_MAT_DIFFUSE, read_rgb(*bb, "reflectance", v3(0.5f, 0.5f, 0.5f)), v3(0, 0, 0), 0, 1);
 }
 
@@ -831,8 +874,27 @@ bool load_mitsuba(SceneData &s, const std::string &path, uint32_t width, uint32_
             }
         }
     }
+    // bitmap textures (SceneLoader::parseXmlTextures, src/SceneLoader.cpp:515-533)
+    std::map<std::string, int32_t> textures;
+    for (auto &k : scene->kids) {
+        if (k.name != "texture" || !k.attr.count("id")) continue;
+        if (textures.count(k.attr.at("id"))) {
+            s.error = "duplicate texture id " + k.attr.at("id") + " in " + path;
+            return false;
+        }
+        const std::string file = read_string(k, "filename");
+        const std::string full = (!file.empty() && file[0] == '/') ? file : dir + file;
+        SceneData::Texture tex;
+        std::string terr;
+        if (!read_png(full, tex.w, tex.h, tex.rgba, terr)) {
+            s.error = "texture " + k.attr.at("id") + ": " + terr;
+            return false;
+        }
+        textures[k.attr.at("id")] = (int32_t)s.textures.size();
+        s.textures.push_back(std::move(tex));
+    }
     for (auto &k : scene->kids)
-        if (k.name == "bsdf" && k.attr.count("id")) named[k.attr.at("id")] = bsdf_material(s, k);
+        if (k.name == "bsdf" && k.attr.count("id")) named[k.attr.at("id")] = bsdf_material(s, k, textures);
     // SceneLoader::parseEnvMap (src/SceneLoader.cpp:370-401): an envmap emitter's EXR image
     for (auto &k : scene->kids) {
         if (k.name != "emitter" || !k.attr.count("type") || k.attr.at("type") != "envmap") continue;
@@ -864,7 +926,7 @@ bool load_mitsuba(SceneData &s, const std::string &path, uint32_t width, uint32_
                 }
                 mat = named.at(k.attr.at("id"));
             } else if (k.name == "bsdf") {
-                mat = bsdf_material(s, k);
+                mat = bsdf_material(s, k, textures);
             }
         }
         if (const XNode *em = sh.child("emitter")) {

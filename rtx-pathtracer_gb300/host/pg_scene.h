@@ -40,6 +40,16 @@ struct SceneData {
     // environment map (the reference's envmap emitter): lat-long RGB, row 0 = up
     uint32_t env_w = 0, env_h = 0;
     std::vector<float> env;
+    // texture coordinates: 6 floats (u, v of the three corners) per triangle,
+    // v flipped as the reference flips it (src/SceneLoader.cpp:288-291)
+    std::vector<float> tri_uv;
+    // material textures (RGBA8, sRGB colour, linear alpha; rows from the top);
+    // pg_material::texture = index + 1
+    struct Texture {
+        uint32_t w = 0, h = 0;
+        std::vector<uint8_t> rgba;
+    };
+    std::vector<Texture> textures;
     // built
     std::vector<BvhNode> nodes;
     std::vector<float> tri_verts;  // 12 floats per triangle in BVH order: v0.xyz id, v1.xyz 0, v2.xyz 0
