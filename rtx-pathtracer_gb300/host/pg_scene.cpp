@@ -2,6 +2,7 @@
 // binned-SAH BVH builder (host side of the tracer).
 #include "pg_scene.h"
 #include "pg_exr.h"
+#include "pg_jpeg.h"
 #include "pg_png.h"
 
 #include <math.h>
@@ -11,6 +12,7 @@
 #include <algorithm>
 #include <array>
 #include <fstream>
+#include <iterator>
 #include <map>
 #include <sstream>
 
@@ -777,6 +779,24 @@ std::string read_string(const XNode &n, const std::string &name) {
     return "";
 }
 
+// A texture file (stbi_load with 4 channels, src/SceneLoader.cpp:200): PNG or
+// baseline JPEG by signature, as RGBA8.
+bool read_texture(const std::string &path, uint32_t &w, uint32_t &h, std::vector<uint8_t> &rgba, std::string &err) {
+    std::ifstream in(path, std::ios::binary);
+    if (!in) {
+        err = "cannot open " + path;
+        return false;
+    }
+    const std::vector<uint8_t> data((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
+    bool ok;
+    if (data.size() >= 2 && data[0] == 0xFF && data[1] == 0xD8)
+        ok = decode_jpeg(data.data(), data.size(), w, h, rgba, err);
+    else
+        ok = decode_png(data.data(), data.size(), w, h, rgba, err);
+    if (!ok) err = path + ": " + err;
+    return ok;
+}
+
 // parseXmlBSDF (src/SceneLoader.cpp:558-611): diffuse, phong, dielectric,
 // conductor (a mirror when its material is "none"), roughconductor (Beckmann);
 // roughplastic as GGX, anything else diffuse.
@@ -886,7 +906,7 @@ bool load_mitsuba(SceneData &s, const std::string &path, uint32_t width, uint32_
         const std::string full = (!file.empty() && file[0] == '/') ? file : dir + file;
         SceneData::Texture tex;
         std::string terr;
-        if (!read_png(full, tex.w, tex.h, tex.rgba, terr)) {
+        if (!read_texture(full, tex.w, tex.h, tex.rgba, terr)) {
             s.error = "texture " + k.attr.at("id") + ": " + terr;
             return false;
         }

@@ -67,11 +67,46 @@ def test_mitsuba_bitmap_texture(pkg, abi, tmp_path):
     assert (tex_bits[np.isin(ids, tri)] == 1).all() and (tex_bits[~np.isin(ids, tri)] == 0).all()
 
 
-def test_jpeg_texture_is_reported(pkg, abi, tmp_path):
+def test_unreadable_textures_are_reported(pkg, abi, tmp_path):
     write_texture_scene(tmp_path)
-    (tmp_path / "leaf.jpg").write_bytes(b"\xff\xd8\xff\xe0" + b"\0" * 64)
-    text = (tmp_path / "scene.xml").read_text().replace("leaf.png", "leaf.jpg")
-    (tmp_path / "scene.xml").write_text(text)
-    with pytest.raises(pkg.PathGuideError) as e:
-        pkg.Scene.load(tmp_path / "scene.xml", 8, 8)
-    assert "PNG" in str(e.value)
+    (tmp_path / "trunc.jpg").write_bytes(b"\xff\xd8\xff\xe0" + b"\0" * 64)
+    (tmp_path / "prog.jpg").write_bytes(b"\xff\xd8\xff\xc2\x00\x11" + b"\x08" + b"\0" * 16)
+    (tmp_path / "junk.tga").write_bytes(b"\0" * 64)
+    for name, words in (("trunc.jpg", "JPEG"), ("prog.jpg", "progressive"), ("junk.tga", "PNG")):
+        text = (tmp_path / "scene.xml").read_text()
+        (tmp_path / "s2.xml").write_text(text.replace("leaf.png", name))
+        with pytest.raises(pkg.PathGuideError) as e:
+            pkg.Scene.load(tmp_path / "s2.xml", 8, 8)
+        assert words in str(e.value), str(e.value)
+
+
+@pytest.mark.parametrize("mode", ["grey", "444", "420", "420_restart"])
+def test_jpeg_baseline(mode, pkg, tmp_path):
+    """Baseline JPEG decoding against the pixels the test's own encoder implies:
+    at most one level off (float IDCT and colour rounding), almost always exact."""
+    from jpegutil import write_jpeg
+    rng = np.random.default_rng(len(mode))
+    H, W = 37, 53  # partial MCUs on both edges
+    y, x = np.mgrid[0:H, 0:W]
+    Y = np.clip(128 + 80 * np.sin(x / 5.0) * np.cos(y / 7.0) + rng.normal(0, 6, (H, W)), 0, 255).astype(np.uint8)
+    Cb = np.clip(128 + 40 * np.cos(x / 9.0), 0, 255).astype(np.uint8)
+    Cr = np.clip(128 + 30 * np.sin(y / 6.0), 0, 255).astype(np.uint8)
+    u, v = np.meshgrid(np.arange(8), np.arange(8))
+    ql, qc = (1 + (u + v)).reshape(-1), (2 + 2 * (u + v)).reshape(-1)
+    if mode == "grey":
+        data, want = write_jpeg([Y], [(1, 1)], [ql])
+    elif mode == "444":
+        data, want = write_jpeg([Y, Cb, Cr], [(1, 1)] * 3, [ql, qc, qc])
+    else:
+        data, want = write_jpeg([Y, Cb, Cr], [(2, 2), (1, 1), (1, 1)], [ql, qc, qc],
+                                restart=3 if mode.endswith("restart") else 0)
+    (tmp_path / "t.jpg").write_bytes(data)
+    # through a scene texture (the decoder is reached by signature)
+    write_texture_scene(tmp_path)
+    (tmp_path / "scene.xml").write_text((tmp_path / "scene.xml").read_text().replace("leaf.png", "t.jpg"))
+    sc = pkg.Scene.load(tmp_path / "scene.xml", 8, 8)
+    exp = sc.export()
+    assert list(exp["tex_info"][0][1:3]) == [W, H]
+    got = exp["tex_data"].reshape(H, W, 4).astype(np.int32)
+    diff = np.abs(got - want.astype(np.int32))
+    assert diff.max() <= 1 and (diff > 0).mean() < 0.02, (diff.max(), (diff > 0).mean())
