@@ -540,7 +540,7 @@ __global__ void k_camera(DevRender R) {
 // slowest ray.  One BVH node per lane per loop trip (trav_step).
 // kCount: also add the traversal work to stats[2] (nodes) and stats[3] (triangles).
 template <bool kCount>
-__global__ void __launch_bounds__(128) k_extend(DevRender R) {
+__global__ void __launch_bounds__(128, 8) k_extend(DevRender R) {
     const uint32_t n = R.counters[0];
     const int lane = threadIdx.x & 31;
     TravState st;
@@ -916,7 +916,7 @@ __device__ __forceinline__ void shadow_finish(const DevRender &R, uint32_t i) {
 // scheduled like k_extend.
 // kCount: also add the traversal work to stats[4] (nodes) and stats[5] (triangles).
 template <bool kCount>
-__global__ void __launch_bounds__(128) k_shadow(DevRender R) {
+__global__ void __launch_bounds__(128, 8) k_shadow(DevRender R) {
     const uint32_t n = R.counters[2];
     const int lane = threadIdx.x & 31;
     TravState st;

@@ -81,7 +81,7 @@ __device__ __forceinline__ float tex_alpha(const DevScene &S, uint32_t tex, floa
 
 // Whether the hit (barycentrics bu, bv of v1, v2; distance t) on original
 // triangle `id` with texture `tex` (1-based) stands.
-__device__ __forceinline__ bool alpha_keep(const DevScene &S, const float org_x, uint32_t id, uint32_t tex, float bu,
+__device__ __noinline__ bool alpha_keep(const DevScene &S, const float org_x, uint32_t id, uint32_t tex, float bu,
                                            float bv, float t) {
     const float *uv = S.tri_uv + 6 * (size_t)id;
     const float w0 = __fsub_rn(__fsub_rn(1.0f, bu), bv);
