@@ -1,11 +1,13 @@
 // pg_exr.cpp - OpenEXR scanline images, the subset the reference's scenes and
 // golden renders use (CommonOps.cpp:12-65 reads and writes them through the
 // OpenEXR library, which this build does not have): HALF / FLOAT / UINT
-// channels, NONE, ZIPS and ZIP compression, increasing or decreasing line
-// order.  ZIP blocks are zlib streams; they are inflated here by a
+// channels, NONE, ZIPS, ZIP and PIZ compression, increasing or decreasing
+// line order.  ZIP blocks are zlib streams; they are inflated here by a
 // project-written decoder of the DEFLATE format (RFC 1950 / 1951), then the
-// EXR byte predictor and the two-half interleave are undone.  The writer
-// stores FLOAT channels without compression.
+// EXR byte predictor and the two-half interleave are undone.  PIZ blocks go
+// through the project's restatement of OpenEXR's Huffman, wavelet and value
+// table steps (piz_decode).  The writer stores FLOAT channels without
+// compression.
 #include "pg_exr.h"
 
 #include <cmath>
@@ -225,7 +227,225 @@ struct Channel {
 
 int pixel_bytes(int32_t type) { return type == 1 ? 2 : 4; }
 
+// ---------------------------------------------------------------------------
+// PIZ (OpenEXR's wavelet + Huffman compression of 32-line chunks)
+//
+// Chunk layout: the bitmap of 16-bit values present (first and last non-zero
+// byte, then those bytes), the length of the Huffman stream, the stream.  The
+// stream holds the code lengths of symbols [im, iM] (6-bit fields, with runs
+// of zero lengths coded as 59..62 for 2..5 zeros and 63 + 8 bits for 6..261
+// zeros), codes assigned longest-first in symbol order, then nBits of codes;
+// symbol iM repeats the previous value (8-bit count).  The decoded values are,
+// per channel, a 2-D Haar-like wavelet transform (14-bit or modular 16-bit
+// lifting) of the channel's lines, over indices of the values present.
+// ---------------------------------------------------------------------------
+struct PizBits {
+    const uint8_t *p, *end;
+    uint64_t c = 0;
+    int lc = 0;
+    bool get(int nb, uint32_t &v) {
+        while (lc < nb) {
+            if (p >= end) return false;
+            c = (c << 8) | *p++;
+            lc += 8;
+        }
+        lc -= nb;
+        v = (uint32_t)((c >> lc) & ((1ull << nb) - 1));
+        return true;
+    }
+};
+
+bool huf_decode(const uint8_t *d, size_t n, uint16_t *out, size_t nout) {
+    constexpr uint32_t kEncSize = 65537;
+    if (n == 0) return nout == 0;
+    if (n < 20) return false;
+    const uint32_t im = rd<uint32_t>(d), iM = rd<uint32_t>(d + 4), nbits = rd<uint32_t>(d + 12);
+    if (im >= kEncSize || iM >= kEncSize || im > iM) return false;
+    std::vector<uint8_t> len(kEncSize, 0);
+    PizBits tb{d + 20, d + n};
+    for (uint32_t i = im; i <= iM; ++i) {
+        uint32_t l;
+        if (!tb.get(6, l)) return false;
+        if (l >= 59) {
+            uint32_t run;
+            if (l == 63) {
+                uint32_t z;
+                if (!tb.get(8, z)) return false;
+                run = z + 6;
+            } else {
+                run = l - 59 + 2;
+            }
+            if (i + run > iM + 1) return false;
+            i += run - 1;  // lengths stay 0
+        } else {
+            len[i] = (uint8_t)l;
+        }
+    }
+    // codes: per length, the first code, longest lengths taking the smallest values
+    uint64_t cnt[59] = {0}, base[59] = {0};
+    for (uint32_t i = 0; i < kEncSize; ++i) cnt[len[i]]++;
+    uint64_t c = 0;
+    for (int l = 58; l > 0; --l) {
+        base[l] = c;
+        c = (c + cnt[l]) >> 1;
+    }
+    std::vector<std::vector<uint32_t>> sym(59);
+    for (uint32_t i = 0; i < kEncSize; ++i)
+        if (len[i]) sym[len[i]].push_back(i);  // symbol order within a length
+    const uint8_t *ds = tb.p;  // the code stream starts at the next whole byte
+    if ((uint64_t)(d + n - ds) * 8 < nbits) return false;
+    uint64_t pos = 0;
+    auto bit = [&]() -> uint32_t {
+        const uint32_t b = (ds[pos >> 3] >> (7 - (pos & 7))) & 1u;
+        ++pos;
+        return b;
+    };
+    size_t o = 0;
+    while (pos < nbits) {
+        uint64_t code = 0;
+        int l = 0;
+        uint32_t s = 0xFFFFFFFFu;
+        while (pos < nbits && l < 58) {
+            code = (code << 1) | bit();
+            ++l;
+            if (!sym[l].empty() && code >= base[l] && code < base[l] + sym[l].size()) {
+                s = sym[l][code - base[l]];
+                break;
+            }
+        }
+        if (s == 0xFFFFFFFFu) return false;
+        if (s == iM) {  // run of the previous value
+            if (pos + 8 > nbits || o == 0) return false;
+            uint32_t r = 0;
+            for (int k = 0; k < 8; ++k) r = (r << 1) | bit();
+            if (o + r > nout) return false;
+            const uint16_t prev = out[o - 1];
+            for (uint32_t k = 0; k < r; ++k) out[o++] = prev;
+        } else {
+            if (o >= nout) return false;
+            out[o++] = (uint16_t)s;
+        }
+    }
+    return o == nout;
+}
+
+inline void wdec14(uint16_t l, uint16_t h, uint16_t &a, uint16_t &b) {
+    const int ls = (int16_t)l, hi = (int16_t)h;
+    const int ai = ls + (hi & 1) + (hi >> 1);
+    a = (uint16_t)(int16_t)ai;
+    b = (uint16_t)(int16_t)(ai - hi);
+}
+inline void wdec16(uint16_t l, uint16_t h, uint16_t &a, uint16_t &b) {
+    const int m = l, dd = h;
+    const int bb = (m - (dd >> 1)) & 0xFFFF;
+    const int aa = (dd + bb - 0x8000) & 0xFFFF;
+    b = (uint16_t)bb;
+    a = (uint16_t)aa;
+}
+
+// Inverse wavelet of an nx x ny array (element strides ox, oy) whose values
+// index at most mx.
+void wav2_decode(uint16_t *in, int nx, int ox, int ny, int oy, int mx) {
+    const bool w14 = mx < (1 << 14);
+    auto dec = [&](uint16_t l, uint16_t h, uint16_t &a, uint16_t &b) {
+        if (w14)
+            wdec14(l, h, a, b);
+        else
+            wdec16(l, h, a, b);
+    };
+    const int n = nx > ny ? ny : nx;
+    int p = 1;
+    while (p <= n) p <<= 1;
+    p >>= 1;
+    int p2 = p;
+    p >>= 1;
+    while (p >= 1) {
+        long py = 0;
+        const long ey = (long)oy * (ny - p2);
+        const long oy1 = (long)oy * p, oy2 = (long)oy * p2, ox1 = (long)ox * p, ox2 = (long)ox * p2;
+        uint16_t i00, i01, i10, i11;
+        for (; py <= ey; py += oy2) {
+            long px = py;
+            const long ex = py + (long)ox * (nx - p2);
+            for (; px <= ex; px += ox2) {
+                const long p01 = px + ox1, p10 = px + oy1, p11 = p10 + ox1;
+                dec(in[px], in[p10], i00, i10);
+                dec(in[p01], in[p11], i01, i11);
+                dec(i00, i01, in[px], in[p01]);
+                dec(i10, i11, in[p10], in[p11]);
+            }
+            if (nx & p) {
+                const long p10 = px + oy1;
+                dec(in[px], in[p10], i00, in[p10]);
+                in[px] = i00;
+            }
+        }
+        if (ny & p) {
+            long px = py;
+            const long ex = py + (long)ox * (nx - p2);
+            for (; px <= ex; px += ox2) {
+                const long p01 = px + ox1;
+                dec(in[px], in[p01], i00, in[p01]);
+                in[px] = i00;
+            }
+        }
+        p2 = p;
+        p >>= 1;
+    }
+}
+
+// One PIZ chunk of nl lines of width W into the uncompressed line layout
+// (per line, each channel's W samples), `want` bytes.
+bool piz_decode(const uint8_t *src, size_t n, const std::vector<Channel> &chans, int W, int nl, size_t want,
+                std::vector<uint8_t> &out) {
+    if (n < 4) return false;
+    const uint16_t mn = rd<uint16_t>(src), mxz = rd<uint16_t>(src + 2);
+    size_t p = 4;
+    std::vector<uint8_t> bitmap(8192, 0);
+    if (mxz >= 8192) return false;
+    if (mn <= mxz) {
+        const size_t k = (size_t)mxz - mn + 1;
+        if (p + k > n) return false;
+        memcpy(&bitmap[mn], src + p, k);
+        p += k;
+    }
+    std::vector<uint16_t> lut(65536, 0);
+    int k = 0;
+    for (int i = 0; i < 65536; ++i)
+        if (i == 0 || (bitmap[i >> 3] & (1 << (i & 7)))) lut[k++] = (uint16_t)i;
+    const int max_value = k - 1;
+    if (p + 4 > n) return false;
+    const int32_t len = rd<int32_t>(src + p);
+    p += 4;
+    if (len < 0 || p + (size_t)len > n || want % 2) return false;
+    std::vector<uint16_t> buf(want / 2);
+    if (!huf_decode(src + p, (size_t)len, buf.data(), buf.size())) return false;
+    std::vector<size_t> start;
+    size_t at = 0;
+    for (auto &c : chans) {
+        const int size = pixel_bytes(c.type) / 2;
+        start.push_back(at);
+        for (int j = 0; j < size; ++j) wav2_decode(&buf[at + j], W, size, nl, W * size, max_value);
+        at += (size_t)W * nl * size;
+    }
+    if (at != buf.size()) return false;
+    for (auto &v : buf) v = lut[v];
+    out.resize(want);
+    size_t o = 0;
+    for (int l = 0; l < nl; ++l)
+        for (size_t c = 0; c < chans.size(); ++c) {
+            const size_t cnt = (size_t)W * (pixel_bytes(chans[c].type) / 2);
+            for (size_t i = 0; i < cnt; ++i) {
+                const uint16_t v = buf[start[c] + (size_t)l * cnt + i];
+                out[o++] = (uint8_t)(v & 0xFF);
+                out[o++] = (uint8_t)(v >> 8);
+            }
+        }
+    return true;
+}
+
 }  // namespace
+
 
 bool read_exr(const std::string &path, ExrImage &img, std::string &err) {
     std::ifstream f(path, std::ios::binary);
@@ -308,8 +528,9 @@ bool read_exr(const std::string &path, ExrImage &img, std::string &err) {
     int lines;
     if (compression == 0 || compression == 2) lines = 1;       // NONE, ZIPS
     else if (compression == 3) lines = 16;                      // ZIP
+    else if (compression == 4) lines = 32;                      // PIZ
     else {
-        err = path + ": compression " + std::to_string(compression) + " is not supported (NONE, ZIPS, ZIP are)";
+        err = path + ": compression " + std::to_string(compression) + " is not supported (NONE, ZIPS, ZIP, PIZ are)";
         return false;
     }
     (void)line_order;  // chunks carry their own y
@@ -352,6 +573,11 @@ bool read_exr(const std::string &path, ExrImage &img, std::string &err) {
         const uint8_t *src = &d[off + 8];
         if ((size_t)size == want) {  // stored uncompressed (also allowed for ZIP chunks)
             raw.assign(src, src + want);
+        } else if (compression == 4) {
+            if (!piz_decode(src, (size_t)size, chans, W, nl, want, raw)) {
+                err = path + ": cannot decode PIZ chunk " + std::to_string(c);
+                return false;
+            }
         } else {
             tmp.clear();
             if (compression == 0 || !inflate_zlib(src, (size_t)size, tmp) || tmp.size() != want) {

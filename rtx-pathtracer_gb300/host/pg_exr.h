@@ -1,4 +1,4 @@
-// pg_exr.h - OpenEXR scanline images (read: NONE / ZIPS / ZIP, HALF / FLOAT /
+// pg_exr.h - OpenEXR scanline images (read: NONE / ZIPS / ZIP / PIZ, HALF / FLOAT /
 // UINT; write: FLOAT, no compression), RGB floats row-major from the top row.
 #pragma once
 

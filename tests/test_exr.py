@@ -9,6 +9,7 @@ import glob
 import os
 import struct
 import zlib
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -192,3 +193,22 @@ def test_envmap_emitter_loads(pkg, tmp_path):
     with pytest.raises(pkg.PathGuideError) as e:
         pkg.Scene.load(tmp_path / "scene2.xml", 8, 8)
     assert e.value.status == pkg.abi.PG_ERR_IO
+
+
+REF_SCENES = Path("/root/reference/scenes")
+
+
+@pytest.mark.skipif(not (REF_SCENES / "envMap" / "envmap.exr").exists(), reason="reference scenes absent")
+def test_piz_reference_envmap(pkg):
+    """The reference's PIZ-compressed environment map (half RGB, 512 x 256): the
+    decoded panorama was inspected (a gallery interior with windows); its
+    checksum pins the decoder.  The scenes that use it load."""
+    import hashlib
+    a = pkg.read_exr(REF_SCENES / "envMap" / "envmap.exr")
+    assert a.shape == (256, 512, 3) and np.isfinite(a).all() and a.min() >= 0.0
+    assert hashlib.sha256(np.ascontiguousarray(a, dtype=np.float32).tobytes()).hexdigest() == \
+        "b55a24c28fe07a55e325eaccd7b917c055c5cf8af09412421f4486d2d8807ba5"
+    for name in ("envMap/envMap.xml", "testSpheres/testSpheres.xml"):
+        sc = pkg.Scene.load(REF_SCENES / name, 32, 24)
+        assert sc.envmap() is not None
+        sc.close()
