@@ -575,8 +575,8 @@ int pg_scene_set_envmap(pg_scene *scene, const float *rgb, uint32_t width, uint3
 int pg_scene_get_envmap(const pg_scene *scene, float *rgb_out, uint32_t *width, uint32_t *height);
 
 /* OpenEXR images (writeEXR / readEXR, src/CommonOps.cpp:12-65): scanline
- * files with HALF, FLOAT or UINT channels, uncompressed, ZIPS or ZIP
- * compressed (the project inflates ZIP itself); RGB floats row-major from the
+ * files with HALF, FLOAT or UINT channels, uncompressed, ZIPS, ZIP or PIZ
+ * compressed (the project decodes both itself); RGB floats row-major from the
  * top row (a Y-only image fills all three).  With rgb_out NULL only the size
  * is returned; capacity counts floats.  The writer stores FLOAT R, G, B
  * without compression. */
