@@ -468,6 +468,32 @@ CONFIG1_WORKLOAD = ("plain CPU-runnable guiding fit: 64 regions x 16384 samples,
                     "weights lognormal(0,1), K=8, 20 EM iterations")
 
 
+def bench_converged(pkg, abi, torch, stream, dirw_d, offs_d, counts, R, tuned, fits: int = 5):
+    """The same workload fitted as the reference fits it by default: the
+    relative log-likelihood test (gain < 0.005 after one iteration) with at
+    most 100 iterations; sample-iterations counted from each region's
+    iteration count."""
+    ctx = pkg.FitContext(abi.default_fit_config(num_initial_components=K), max_regions=R)
+    if tuned:
+        ctx.set_tuning(**tuned)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        ctx.fit(dirw_d, offs_d, R, abi.PG_FIT_INIT, stream=stream)
+        ev0.record(stream)
+        for _ in range(fits):
+            ctx.fit(dirw_d, offs_d, R, abi.PG_FIT_INIT, stream=stream)
+        ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / fits
+    iters = ctx.states(R)["iters_last"].astype(np.int64)
+    ctx.close()
+    si = int((counts * iters).sum())
+    fitted = iters > 0
+    return {"ms_per_fit": ms, "value": si / (ms * 1e-3) / 1e6, "unit": UNIT, "sample_iterations": si,
+            "mean_iterations": float(iters[fitted].mean()), "max_iterations": int(iters.max()),
+            "config": "relative log-likelihood threshold 0.005, at most 100 iterations (the reference's defaults)"}
+
+
 def bench_config1(pkg, abi, torch, stream, steps: int, cpu: bool):
     """The reference's CPU-runnable fit configuration on the GPU, with the
     bit-exact lightpmm port on the host cores beside it."""
@@ -823,6 +849,8 @@ def main():
     if graph is not None:
         graph.close()
     ctx.close()
+    if not args.sweep:
+        line["converged_mode"] = bench_converged(pkg, abi, torch, stream, dirw_d, offs_d, counts, R, tuned)
     if args.workload == "all" and not args.small:
         line["cpu_runnable_config"] = bench_config1(pkg, abi, torch, stream, args.steps,
                                                     cpu=rank == 0 and not args.no_cpu_baseline)
