@@ -187,7 +187,8 @@ int pg_fit_regions_host(pg_ctx *ctx, const float *dirw_host, const uint32_t *off
     // One copy, then one fit.  Fitting chunks of regions while later chunks
     // copy was measured slower: every chunk's largest region adds its own
     // tail, which costs more than the copy (about 200 GB/s from page-locked
-    // memory) that it hides.
+    // memory) that it hides.  Four concurrent copies of quarters of the
+    // samples were slower than one copy as well.
     if (total) {
         st = check_cuda(ctx, cudaMemcpyAsync(ctx->h2d_dirw, dirw_host, sizeof(float4) * total, cudaMemcpyHostToDevice,
                                              ctx->h2d_stream), "samples upload");
