@@ -686,6 +686,8 @@ struct TrainArgs {
     float *partials;            // gridDim.x x NPARAM weight / bias gradient sums
     float *loss_partials;       // gridDim.x x {sum w (-log q), sum w}
     uint32_t *err;              // PG_DEV_ERR_TIMEOUT if a wait ran out
+    const float *pos;           // inference: positions (3 floats each)
+    float *mix_out;             // inference: n x 80 mixture parameters
 };
 
 // Waits for the MMAs committed to `bar` (phase `phase`), bounded.
@@ -780,7 +782,9 @@ __device__ __forceinline__ void backward_epilogue(uint32_t tacc, int c0, uint32_
 // encoding chunk.  The output layer goes through shared memory (sO, one
 // column-major row of 80 floats per record) so the component split does not
 // follow the tensor-memory column blocks.
-template <int TPR>
+// kInfer: the forward pass only, writing each position's mixture parameters
+// {pi, mu, kappa} per component (pg_mlp_infer).
+template <int TPR, bool kInfer = false>
 __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
     constexpr int NT = TILE * TPR, HC = 64 / TPR, NCMP = NC / TPR;
     extern __shared__ __align__(1024) unsigned char sm[];
@@ -847,13 +851,17 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
         const uint32_t r = tile * TILE + (uint32_t)rec;
         float x[3] = {0.0f, 0.0f, 0.0f}, d[3] = {0.0f, 0.0f, 1.0f}, w = 0.0f;
         if (r < A.n) {
-            const pg_directional_data &rc = A.rec[r];
-            for (int k = 0; k < 3; ++k) {
-                x[k] = (rc.position[k] - A.lo[k]) * A.inv_ext[k];
-                d[k] = rc.direction[k];
+            if constexpr (kInfer) {
+                for (int k = 0; k < 3; ++k) x[k] = (A.pos[3 * (size_t)r + k] - A.lo[k]) * A.inv_ext[k];
+            } else {
+                const pg_directional_data &rc = A.rec[r];
+                for (int k = 0; k < 3; ++k) {
+                    x[k] = (rc.position[k] - A.lo[k]) * A.inv_ext[k];
+                    d[k] = rc.direction[k];
+                }
+                w = rc.flags == PG_INVALID_REGION ? 0.0f : rc.weight;
+                if (!(w > 0.0f) || !isfinite(w)) w = 0.0f;
             }
-            w = rc.flags == PG_INVALID_REGION ? 0.0f : rc.weight;
-            if (!(w > 0.0f) || !isfinite(w)) w = 0.0f;
         }
         // encoding -> X1: 112 features, the ones column, zeros to 128 (chunks h, h + TPR, ...)
         for (int ch = h; ch < KC1; ch += TPR) {
@@ -928,148 +936,172 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
 #pragma unroll
         for (int g = 0; g < TPR; ++g) lsm += sXs[g * TILE + rec] * __expf(sXm[g * TILE + rec] - lmax);
         const float lse = lmax + __logf(lsm);
-        float lp[NCMP], kq[NCMP], csq[NCMP], mu[NCMP][3], fin[NCMP];
+        if constexpr (kInfer) {
+            if (r < A.n) {
+                float *mo = A.mix_out + (size_t)r * NOUT;
 #pragma unroll
-        for (int q = 0; q < NCMP; ++q) {
-            const int j = j0 + q;
-            const float mx = sO[(5 * j + 1) * TILE + rec], my = sO[(5 * j + 2) * TILE + rec],
-                        mz = sO[(5 * j + 3) * TILE + rec];
-            const float mn = sqrtf(mx * mx + my * my + mz * mz);
-            const float inv = mn > 0.0f ? 1.0f / mn : 0.0f;
-            const float k = __expf(fminf(fmaxf(sO[(5 * j + 4) * TILE + rec], S_MIN), S_MAX));
-            mu[q][0] = mx * inv;
-            mu[q][1] = my * inv;
-            mu[q][2] = mz * inv;
-            const float cs = mu[q][0] * d[0] + mu[q][1] * d[1] + mu[q][2] * d[2];
-            const float om = -expm1f(-2.0f * k);  // 1 - e^{-2k}
-            const float lognorm = __logf(k) - __logf(2.0f * kPi) - __logf(om);
-            lp[q] = (sO[(5 * j) * TILE + rec] - lse) + lognorm + k * (cs - 1.0f);
-            kq[q] = k;
-            csq[q] = cs;
-            fin[q] = inv * k;  // kappa / |m|
-        }
-        float mq = -INFINITY;
-#pragma unroll
-        for (int q = 0; q < NCMP; ++q) mq = fmaxf(mq, lp[q]);
-        float sq = 0.0f;
-#pragma unroll
-        for (int q = 0; q < NCMP; ++q) sq += __expf(lp[q] - mq);
-        __syncthreads();  // everyone has read the logit maxima
-        sXm[h * TILE + rec] = mq;
-        sXs[h * TILE + rec] = sq;
-        __syncthreads();
-        float qmax = -INFINITY;
-#pragma unroll
-        for (int g = 0; g < TPR; ++g) qmax = fmaxf(qmax, sXm[g * TILE + rec]);
-        float qs = 0.0f;
-#pragma unroll
-        for (int g = 0; g < TPR; ++g) qs += sXs[g * TILE + rec] * __expf(sXm[g * TILE + rec] - qmax);
-        const float logq = qmax + __logf(qs);
-        if (h == 0 && w > 0.0f) {
-            lsum += w * -logq;
-            wsum += w;
-        }
-#pragma unroll
-        for (int q = 0; q < NCMP; ++q) {
-            const int j = j0 + q;
-            float *o = sO + (5 * j) * TILE + rec;
-            const float sraw = o[4 * TILE];
-            const float k = kq[q], cs = csq[q];
-            const float rr = __expf(lp[q] - logq);  // responsibility
-            const float pi = __expf(o[0] - lse);
-            const float f = -w * rr * fin[q];
-            o[0] = w * (pi - rr);
-            o[TILE] = f * (d[0] - cs * mu[q][0]);
-            o[2 * TILE] = f * (d[1] - cs * mu[q][1]);
-            o[3 * TILE] = f * (d[2] - cs * mu[q][2]);
-            const bool inside = sraw > S_MIN && sraw < S_MAX;
-            const float e = __expf(-2.0f * k);
-            const float tt = 2.0f * k * e / -expm1f(-2.0f * k);
-            o[4 * TILE] = inside ? -w * rr * (1.0f - tt + k * (cs - 1.0f)) : 0.0f;
-        }
-        __syncthreads();
-        for (int ch = h; ch < NOUT / 8; ch += TPR) {
-            const float *o = sO + (8 * ch) * TILE + rec;
-            *reinterpret_cast<uint4 *>(sDY + elem(rec, 8 * ch, KCH)) =
-                make_uint4(pack2(o[0], o[TILE]), pack2(o[2 * TILE], o[3 * TILE]), pack2(o[4 * TILE], o[5 * TILE]),
-                           pack2(o[6 * TILE], o[7 * TILE]));
-        }
-        // ---- backward: weight gradients of layer l and dH_{l-1} from one commit
-        operands_ready();
-        if (tid == 0) {
-            fence_after();
-            gemm(tm + TM_G4, gX4, gDY, TILE / 16, idesc(128, NOUT, 1, 1), !first);
-            gemm(tm + TM_ACT, bDY, bW4, NOUT / 16, idesc(128, NH, 0, 1), false);
-            commit(&s_bar);
-        }
-        mma_wait(&s_bar, phase, A.err);
-        backward_epilogue<HC>(tl + TM_ACT, hc0, m3, sDY, rec);
-        operands_ready();
-        if (tid == 0) {
-            fence_after();
-            gemm(tm + TM_G3, gX3, gDY, TILE / 16, idesc(128, NH, 1, 1), !first);
-            gemm(tm + TM_ACT, bDY, bW3, NH / 16, idesc(128, NH, 0, 1), false);
-            commit(&s_bar);
-        }
-        mma_wait(&s_bar, phase, A.err);
-        backward_epilogue<HC>(tl + TM_ACT, hc0, m2, sDY, rec);
-        operands_ready();
-        if (tid == 0) {
-            fence_after();
-            gemm(tm + TM_G2, gX2, gDY, TILE / 16, idesc(128, NH, 1, 1), !first);
-            gemm(tm + TM_ACT, bDY, bW2, NH / 16, idesc(128, NH, 0, 1), false);
-            commit(&s_bar);
-        }
-        mma_wait(&s_bar, phase, A.err);
-        backward_epilogue<HC>(tl + TM_ACT, hc0, m1, sDY, rec);
-        operands_ready();
-        if (tid == 0) {
-            fence_after();
-            gemm(tm + TM_G1, gX1, gDY, TILE / 16, idesc(128, NH, 1, 1), !first);
-            commit(&s_bar);
-        }
-        mma_wait(&s_bar, phase, A.err);
-        first = false;
-    }
-    // ---- this CTA's gradient sums: lane = input row (bias row = the ones column);
-    // column blocks h, h + TPR, ...
-    float *out = A.partials + (size_t)blockIdx.x * NPARAM;
-    const int i = rec;
-    auto dump = [&](uint32_t tcol, int nout, int nin, int ow, int ob) {
-        for (int c = 16 * h; c < nout; c += 16 * TPR) {
-            float v[16];
-            tld16(tl + tcol + c, v);
-            tld_wait();
-            if (first) {  // no tile: zero sums
-#pragma unroll
-                for (int j = 0; j < 16; ++j) v[j] = 0.0f;
+                for (int q = 0; q < NCMP; ++q) {
+                    const int j = j0 + q;
+                    const float *o = sO + (5 * j) * TILE + rec;
+                    const float mx = o[TILE], my = o[2 * TILE], mz = o[3 * TILE];
+                    const float mn = sqrtf(mx * mx + my * my + mz * mz);
+                    const float inv = mn > 0.0f ? 1.0f / mn : 0.0f;
+                    mo[5 * j] = __expf(o[0] - lse);
+                    mo[5 * j + 1] = mx * inv;
+                    mo[5 * j + 2] = my * inv;
+                    mo[5 * j + 3] = mz * inv;
+                    mo[5 * j + 4] = __expf(fminf(fmaxf(o[4 * TILE], S_MIN), S_MAX));
+                }
             }
-            if (i < nin) {
-#pragma unroll
-                for (int j = 0; j < 16; ++j) out[ow + (c + j) * nin + i] = v[j];
-            } else if (i == nin) {
-#pragma unroll
-                for (int j = 0; j < 16; ++j) out[ob + c + j] = v[j];
+        } else {
+            float lp[NCMP], kq[NCMP], csq[NCMP], mu[NCMP][3], fin[NCMP];
+    #pragma unroll
+            for (int q = 0; q < NCMP; ++q) {
+                const int j = j0 + q;
+                const float mx = sO[(5 * j + 1) * TILE + rec], my = sO[(5 * j + 2) * TILE + rec],
+                            mz = sO[(5 * j + 3) * TILE + rec];
+                const float mn = sqrtf(mx * mx + my * my + mz * mz);
+                const float inv = mn > 0.0f ? 1.0f / mn : 0.0f;
+                const float k = __expf(fminf(fmaxf(sO[(5 * j + 4) * TILE + rec], S_MIN), S_MAX));
+                mu[q][0] = mx * inv;
+                mu[q][1] = my * inv;
+                mu[q][2] = mz * inv;
+                const float cs = mu[q][0] * d[0] + mu[q][1] * d[1] + mu[q][2] * d[2];
+                const float om = -expm1f(-2.0f * k);  // 1 - e^{-2k}
+                const float lognorm = __logf(k) - __logf(2.0f * kPi) - __logf(om);
+                lp[q] = (sO[(5 * j) * TILE + rec] - lse) + lognorm + k * (cs - 1.0f);
+                kq[q] = k;
+                csq[q] = cs;
+                fin[q] = inv * k;  // kappa / |m|
             }
+            float mq = -INFINITY;
+    #pragma unroll
+            for (int q = 0; q < NCMP; ++q) mq = fmaxf(mq, lp[q]);
+            float sq = 0.0f;
+    #pragma unroll
+            for (int q = 0; q < NCMP; ++q) sq += __expf(lp[q] - mq);
+            __syncthreads();  // everyone has read the logit maxima
+            sXm[h * TILE + rec] = mq;
+            sXs[h * TILE + rec] = sq;
+            __syncthreads();
+            float qmax = -INFINITY;
+    #pragma unroll
+            for (int g = 0; g < TPR; ++g) qmax = fmaxf(qmax, sXm[g * TILE + rec]);
+            float qs = 0.0f;
+    #pragma unroll
+            for (int g = 0; g < TPR; ++g) qs += sXs[g * TILE + rec] * __expf(sXm[g * TILE + rec] - qmax);
+            const float logq = qmax + __logf(qs);
+            if (h == 0 && w > 0.0f) {
+                lsum += w * -logq;
+                wsum += w;
+            }
+    #pragma unroll
+            for (int q = 0; q < NCMP; ++q) {
+                const int j = j0 + q;
+                float *o = sO + (5 * j) * TILE + rec;
+                const float sraw = o[4 * TILE];
+                const float k = kq[q], cs = csq[q];
+                const float rr = __expf(lp[q] - logq);  // responsibility
+                const float pi = __expf(o[0] - lse);
+                const float f = -w * rr * fin[q];
+                o[0] = w * (pi - rr);
+                o[TILE] = f * (d[0] - cs * mu[q][0]);
+                o[2 * TILE] = f * (d[1] - cs * mu[q][1]);
+                o[3 * TILE] = f * (d[2] - cs * mu[q][2]);
+                const bool inside = sraw > S_MIN && sraw < S_MAX;
+                const float e = __expf(-2.0f * k);
+                const float tt = 2.0f * k * e / -expm1f(-2.0f * k);
+                o[4 * TILE] = inside ? -w * rr * (1.0f - tt + k * (cs - 1.0f)) : 0.0f;
+            }
+            __syncthreads();
+            for (int ch = h; ch < NOUT / 8; ch += TPR) {
+                const float *o = sO + (8 * ch) * TILE + rec;
+                *reinterpret_cast<uint4 *>(sDY + elem(rec, 8 * ch, KCH)) =
+                    make_uint4(pack2(o[0], o[TILE]), pack2(o[2 * TILE], o[3 * TILE]), pack2(o[4 * TILE], o[5 * TILE]),
+                               pack2(o[6 * TILE], o[7 * TILE]));
+            }
+            // ---- backward: weight gradients of layer l and dH_{l-1} from one commit
+            operands_ready();
+            if (tid == 0) {
+                fence_after();
+                gemm(tm + TM_G4, gX4, gDY, TILE / 16, idesc(128, NOUT, 1, 1), !first);
+                gemm(tm + TM_ACT, bDY, bW4, NOUT / 16, idesc(128, NH, 0, 1), false);
+                commit(&s_bar);
+            }
+            mma_wait(&s_bar, phase, A.err);
+            backward_epilogue<HC>(tl + TM_ACT, hc0, m3, sDY, rec);
+            operands_ready();
+            if (tid == 0) {
+                fence_after();
+                gemm(tm + TM_G3, gX3, gDY, TILE / 16, idesc(128, NH, 1, 1), !first);
+                gemm(tm + TM_ACT, bDY, bW3, NH / 16, idesc(128, NH, 0, 1), false);
+                commit(&s_bar);
+            }
+            mma_wait(&s_bar, phase, A.err);
+            backward_epilogue<HC>(tl + TM_ACT, hc0, m2, sDY, rec);
+            operands_ready();
+            if (tid == 0) {
+                fence_after();
+                gemm(tm + TM_G2, gX2, gDY, TILE / 16, idesc(128, NH, 1, 1), !first);
+                gemm(tm + TM_ACT, bDY, bW2, NH / 16, idesc(128, NH, 0, 1), false);
+                commit(&s_bar);
+            }
+            mma_wait(&s_bar, phase, A.err);
+            backward_epilogue<HC>(tl + TM_ACT, hc0, m1, sDY, rec);
+            operands_ready();
+            if (tid == 0) {
+                fence_after();
+                gemm(tm + TM_G1, gX1, gDY, TILE / 16, idesc(128, NH, 1, 1), !first);
+                commit(&s_bar);
+            }
+            mma_wait(&s_bar, phase, A.err);
+            first = false;
         }
-    };
-    dump(TM_G1, NH, NIN, OW1, OB1);
-    dump(TM_G2, NH, NH, OW2, OB2);
-    dump(TM_G3, NH, NH, OW3, OB3);
-    dump(TM_G4, NOUT, NH, OW4, OB4);
-    for (int off = 16; off > 0; off >>= 1) {
-        lsum += __shfl_xor_sync(0xffffffffu, lsum, off);
-        wsum += __shfl_xor_sync(0xffffffffu, wsum, off);
     }
-    if (lane == 0) {
-        s_red[2 * warp] = lsum;
-        s_red[2 * warp + 1] = wsum;
-    }
-    fence_before();
-    __syncthreads();
-    if (tid == 0) {  // only share 0 (warps 0-3) carries loss sums
-        A.loss_partials[2 * blockIdx.x] = (s_red[0] + s_red[2]) + (s_red[4] + s_red[6]);
-        A.loss_partials[2 * blockIdx.x + 1] = (s_red[1] + s_red[3]) + (s_red[5] + s_red[7]);
+    if constexpr (!kInfer) {
+        // ---- this CTA's gradient sums: lane = input row (bias row = the ones column);
+        // column blocks h, h + TPR, ...
+        float *out = A.partials + (size_t)blockIdx.x * NPARAM;
+        const int i = rec;
+        auto dump = [&](uint32_t tcol, int nout, int nin, int ow, int ob) {
+            for (int c = 16 * h; c < nout; c += 16 * TPR) {
+                float v[16];
+                tld16(tl + tcol + c, v);
+                tld_wait();
+                if (first) {  // no tile: zero sums
+    #pragma unroll
+                    for (int j = 0; j < 16; ++j) v[j] = 0.0f;
+                }
+                if (i < nin) {
+    #pragma unroll
+                    for (int j = 0; j < 16; ++j) out[ow + (c + j) * nin + i] = v[j];
+                } else if (i == nin) {
+    #pragma unroll
+                    for (int j = 0; j < 16; ++j) out[ob + c + j] = v[j];
+                }
+            }
+        };
+        dump(TM_G1, NH, NIN, OW1, OB1);
+        dump(TM_G2, NH, NH, OW2, OB2);
+        dump(TM_G3, NH, NH, OW3, OB3);
+        dump(TM_G4, NOUT, NH, OW4, OB4);
+        for (int off = 16; off > 0; off >>= 1) {
+            lsum += __shfl_xor_sync(0xffffffffu, lsum, off);
+            wsum += __shfl_xor_sync(0xffffffffu, wsum, off);
+        }
+        if (lane == 0) {
+            s_red[2 * warp] = lsum;
+            s_red[2 * warp + 1] = wsum;
+        }
+        fence_before();
+        __syncthreads();
+        if (tid == 0) {  // only share 0 (warps 0-3) carries loss sums
+            A.loss_partials[2 * blockIdx.x] = (s_red[0] + s_red[2]) + (s_red[4] + s_red[6]);
+            A.loss_partials[2 * blockIdx.x + 1] = (s_red[1] + s_red[3]) + (s_red[5] + s_red[7]);
+        }
+    } else {
+        fence_before();
+        __syncthreads();
     }
     if (warp == 0) {
         fence_after();
@@ -1426,6 +1458,8 @@ int pg_mlp_create(const pg_mlp_config *cfg, pg_mlp **out) {
          cudaFuncSetAttribute(k_fwd_bwd<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)M->smem) ==
              cudaSuccess &&
          cudaFuncSetAttribute(tc::k_train_tc<tc::kTpr>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              tc::SM_TOTAL) == cudaSuccess &&
+         cudaFuncSetAttribute(tc::k_train_tc<tc::kTpr, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               tc::SM_TOTAL) == cudaSuccess;
     if (!ok) {
         pg_mlp_destroy(M);
@@ -1568,6 +1602,24 @@ int pg_mlp_set_path(pg_mlp *M, int path) {
 int pg_mlp_infer(pg_mlp *M, const float *positions, uint32_t n, float *mixtures_out, void *stream) {
     if (!M || (n && (!positions || !mixtures_out))) return PG_ERR_ARG;
     if (n == 0) return PG_OK;
+    if (M->path == PG_MLP_PATH_TCGEN05) {
+        const uint32_t tiles = (n + tc::TILE - 1) / tc::TILE;
+        const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)M->sm_count);
+        tc::TrainArgs T{};
+        const FwdArgs F = fwd_args(M);
+        for (int i = 0; i < 3; ++i) {
+            T.lo[i] = F.lo[i];
+            T.inv_ext[i] = F.inv_ext[i];
+        }
+        T.n = n;
+        T.pos = positions;
+        T.mix_out = mixtures_out;
+        T.wimg = M->img;
+        T.theta = M->theta;
+        T.err = M->err;
+        tc::k_train_tc<tc::kTpr, true><<<grid, tc::TILE * tc::kTpr, tc::SM_TOTAL, (cudaStream_t)stream>>>(T);
+        return cudaGetLastError() == cudaSuccess ? PG_OK : mlp_error(PG_ERR_CUDA, "surrogate inference launch");
+    }
     FwdArgs A = fwd_args(M);
     A.pos = positions;
     A.n = n;
