@@ -112,6 +112,12 @@ typedef struct pg_region_state {
 
 #define PG_STATE_FITTED 1u     /* region has been fitted at least once        */
 #define PG_STATE_NONFINITE 2u  /* last fit produced a non-finite parameter    */
+/* Set by pg_fit_regions_noalloc on every region of a call in which a bounded
+ * device wait ran out or an index check failed (the fit of those regions is
+ * incomplete); that entry point clears it on a clean call, the others leave it
+ * as they find it.  Context-based fits report the same events through their
+ * status codes instead. */
+#define PG_STATE_FIT_FAILED 4u
 
 /* VMF_Theta / VMM_Theta as uploaded to the tracer (src/PathGuiding.h:36-75,
  * shaders/guiding.glsl:14-51): 40 and 720 bytes, scalar layout. */
@@ -611,21 +617,25 @@ int pg_render(pg_scene *scene, const pg_render_params *params, pg_ctx *guide, fl
 /* No counterpart in the reference: the reference fits on the host.
  *
  * pg_fit_regions_noalloc runs the same batched fit as pg_fit_regions for
- * callers that cannot allocate device memory - renderers that own all device
- * memory through their own arena, code recording a CUDA graph (a cudaMalloc
- * breaks the capture), or plugin hosts that hand the guiding step only its own
- * buffers.  It needs no pg_ctx: the caller passes the fit properties, the
- * device array of n_regions mixture states (read and written in place) and the
- * samples and offsets as for pg_fit_regions.  The fit's scratch lives in one
- * static device array of the library, sized for PG_NOALLOC_MAX_REGIONS
- * regions (about 257 KB per GPU, held until the process exits); nothing is
- * allocated.  The first call on a device looks up that array's device address
- * (cudaGetSymbolAddress), so make it before any stream capture.  All calls
- * share the array: calls whose work may overlap on the GPU race and must be
- * ordered (same stream or events).  Returns PG_ERR_NOMEM when n_regions
- * exceeds PG_NOALLOC_MAX_REGIONS, PG_ERR_ARG for bad arguments, PG_ERR_CUDA
- * when a CUDA call fails; non-finite results are flagged in the states
- * (PG_STATE_NONFINITE). */
+ * callers that cannot allocate device memory: renderers that own all device
+ * memory through their own arena (another allocator would fragment it and
+ * defeat its accounting), and plugin hosts that hand the guiding step only its
+ * own buffers and no right to allocate.  It needs no pg_ctx: the caller passes
+ * the fit properties, the device array of n_regions mixture states (read and
+ * written in place) and the samples and offsets as for pg_fit_regions.  The
+ * fit's scratch lives in one static device array of the library, sized for
+ * PG_NOALLOC_MAX_REGIONS regions (about 257 KB per GPU, held until the process
+ * exits); nothing is allocated and nothing is read from host memory after the
+ * call returns.  The first call on a device looks up that array's device
+ * address (cudaGetSymbolAddress) and keeps it for the life of the process; a
+ * device reset (cudaDeviceReset) invalidates the kept address, so do not call
+ * this entry point after one.  All calls share the array: calls whose work may
+ * overlap on the GPU race and must be ordered (same stream or events).
+ * Returns PG_ERR_NOMEM when n_regions exceeds PG_NOALLOC_MAX_REGIONS,
+ * PG_ERR_ARG for bad arguments, PG_ERR_CUDA when a CUDA call fails.  Errors
+ * found on the device are reported in the states, stream-ordered: non-finite
+ * results per region (PG_STATE_NONFINITE), and a bounded wait that ran out or
+ * a failed index check on every region of the call (PG_STATE_FIT_FAILED). */
 #define PG_NOALLOC_MAX_REGIONS 65536u
 int pg_fit_regions_noalloc(const pg_fit_config *cfg, pg_region_state *states, const float *dirw,
                            const uint32_t *offsets, uint32_t n_regions, int mode, void *stream);
@@ -685,7 +695,12 @@ int pg_mlp_train(pg_mlp *mlp, const pg_directional_data *records, uint64_t n, fl
 #define PG_MLP_PATH_WARP_MMA 1
 int pg_mlp_set_path(pg_mlp *mlp, int path);
 /* Mixture parameters at n positions (device, 3 floats each): per position 16
- * components of {weight, mu x, mu y, mu z, kappa} (80 floats, device). */
+ * components of {weight, mu x, mu y, mu z, kappa} (80 floats, device).
+ * Stream-ordered and not synchronised: a bounded tensor-core wait that ran out
+ * is reported (PG_ERR_TIMEOUT) by the next call of this surrogate that
+ * synchronises - pg_mlp_loss_grad / pg_mlp_train with a loss, or
+ * pg_mlp_write_guide / pg_mlp_judge_guide, which check right after their own
+ * inference. */
 int pg_mlp_infer(pg_mlp *mlp, const float *positions, uint32_t n, float *mixtures_out, void *stream);
 /* Evaluates the network at the centres of the regions of a guiding context
  * (after pg_set_regions) and installs the mixtures as the context's packed

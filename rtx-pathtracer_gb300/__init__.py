@@ -449,9 +449,11 @@ NOALLOC_MAX_REGIONS = 65536
 def fit_regions_noalloc(cfg: abi.FitConfig, states_dev, dirw, offsets, n_regions: int,
                         mode: int = abi.PG_FIT_INIT, stream=None) -> int:
     """pg_fit_regions_noalloc: the batched fit without a context and without any
-    device allocation, for callers that may not allocate (own memory arenas,
-    graph capture, plugin hosts).  states_dev is the caller's device array of
-    n_regions pg_region_state records, updated in place.  Returns the status."""
+    device allocation, for callers that may not allocate (renderers with their
+    own memory arena, plugin hosts given only their own buffers).  states_dev is
+    the caller's device array of n_regions pg_region_state records, updated in
+    place; device-side failures are flagged in the states (PG_STATE_*).
+    Returns the status."""
     return library().pg_fit_regions_noalloc(C.byref(cfg), _dptr(states_dev), _dptr(dirw), _dptr(offsets),
                                             n_regions, mode, _stream_handle(stream))
 

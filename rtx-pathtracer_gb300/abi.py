@@ -11,6 +11,7 @@ INVALID_REGION = 0xFFFFFFFF
 PG_OK, PG_ERR_ARG, PG_ERR_CUDA, PG_ERR_TIMEOUT, PG_ERR_NUMERIC, PG_ERR_NOMEM, PG_ERR_IO, \
     PG_ERR_PARSE, PG_ERR_STATE = range(9)
 PG_FIT_INIT, PG_FIT_CONTINUE, PG_FIT_UPDATE = 0, 1, 2
+PG_STATE_FITTED, PG_STATE_NONFINITE, PG_STATE_FIT_FAILED = 1, 2, 4
 
 STATE_DTYPE = np.dtype([
     ("weight", "<f4", (16,)), ("mu_x", "<f4", (16,)), ("mu_y", "<f4", (16,)),

@@ -1406,7 +1406,7 @@ int check_device_error(pg_mlp *M) {
         return mlp_error(PG_ERR_CUDA, "surrogate error word");
     if (e) {
         cudaMemset(M->err, 0, sizeof(uint32_t));
-        return mlp_error(PG_ERR_TIMEOUT, "surrogate training: a tensor-core wait timed out");
+        return mlp_error(PG_ERR_TIMEOUT, "surrogate tensor-core kernel (training or inference): a bounded wait timed out");
     }
     return PG_OK;
 }
@@ -1652,6 +1652,10 @@ int net_guide(pg_mlp *M, const GuideTarget &T, bool to_ctx, cudaStream_t s) {
     }
     k_region_centres<<<(T.n_regions + 255) / 256, 256, 0, s>>>(T.aabbs, T.n_regions, M->pos);
     if (int st = pg_mlp_infer(M, M->pos, T.n_regions, M->mix, s)) return st;
+    // a tensor-core wait that ran out leaves mixtures unwritten: check before
+    // they become a guide
+    if (cudaStreamSynchronize(s) != cudaSuccess) return mlp_error(PG_ERR_CUDA, "surrogate inference");
+    if (int st = check_device_error(M)) return st;
     k_pack_guide<<<T.n_regions, NC, 0, s>>>(M->mix, M->pos, T.n_regions, to_ctx ? T.vmm : M->net_vmm);
     return cudaGetLastError() == cudaSuccess ? PG_OK : mlp_error(PG_ERR_CUDA, "guide pack launch");
 }

@@ -2,10 +2,10 @@
 // cannot allocate device memory.
 //
 // Some callers of this library cannot call cudaMalloc: a renderer that
-// hands out all device memory from its own arena and forbids other allocators,
-// code running while a stream is being captured into a CUDA graph (a
-// cudaMalloc there breaks the capture), or a plugin host that gives the
-// guiding step only the buffers it owns.  pg_ctx_create allocates the fit's
+// hands out all device memory from its own arena and forbids other allocators
+// (a second allocator fragments the arena and breaks its accounting), or a
+// plugin host that gives the guiding step only the buffers it owns and no
+// allocation rights of its own.  pg_ctx_create allocates the fit's
 // scratch (work-queue counters, the largest-first region order and the initial
 // mixture table), so those callers cannot use pg_fit_regions.  This entry point
 // runs the same fit kernel with its scratch in one file-scope device array
@@ -18,11 +18,20 @@
 // Two calls whose work overlaps on the GPU (different streams, no ordering)
 // race on the array and give wrong results: order them on one stream or with
 // events.
+//
+// Nothing of a call goes through host memory: the initial mixture table
+// travels as a kernel argument, and a bounded wait that ran out or a failed
+// index check inside the fit is reported in the caller's states
+// (PG_STATE_FIT_FAILED on every region of the call) by a last small kernel.
 #include <atomic>
 
 #include "pg_em_kernels.cuh"
 
 namespace {
+
+struct InitTable {
+    float v[64];  // initial means x[16] y[16] z[16], initial mean cosines[16]
+};
 
 struct NoAllocScratch {
     uint32_t counters[64];                     // work queues, error word, cluster count
@@ -75,6 +84,29 @@ void initial_table(uint32_t K, float kap, float *t) {
         const double kd = kap < 1e-3f ? 0.0 : (double)kap;
         t[48 + n] = kd > 0.0 ? (float)(1.0 / tanh(kd) - 1.0 / kd) : 0.0f;
     }
+}
+
+// Clears the work counters and error word and stores the initial table; the
+// table is a kernel argument, so the launch copies it and no host buffer has to
+// outlive the call.
+__global__ void noalloc_prepare_kernel(InitTable table, NoAllocScratch *scr) {
+    const int t = threadIdx.x;
+    if (t < 64) {
+        scr->counters[t] = 0u;
+        scr->init_table[t] = table.v[t];
+    }
+}
+
+// Maps the fit's device error word into the states of the call: a wait that
+// ran out or a failed index check leaves regions unfitted or partly fitted, so
+// every region of the call is marked; a clean call clears the mark.
+// Non-finite parameters are flagged per region by the fit itself.
+__global__ void noalloc_finish_kernel(pg_region_state *states, uint32_t n_regions, const uint32_t *error_word) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_regions) return;
+    const bool failed = (*error_word & (PG_DEV_ERR_TIMEOUT | PG_DEV_ERR_BOUNDS)) != 0u;
+    const uint32_t f = states[r].flags;
+    states[r].flags = failed ? (f | PG_STATE_FIT_FAILED) : (f & ~PG_STATE_FIT_FAILED);
 }
 
 // K <= 16: the register-capped build at three CTAs per SM (E-step constants in
@@ -130,14 +162,12 @@ extern "C" int pg_fit_regions_noalloc(const pg_fit_config *cfg, pg_region_state 
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return PG_ERR_CUDA;
     cudaStream_t s = (cudaStream_t)stream;
-    // The table goes from a host stack buffer; a pageable copy is staged
-    // before cudaMemcpyAsync returns.
-    float table[64];
-    initial_table(cfg->num_initial_components, cfg->init_kappa, table);
-    if (cudaMemcpyAsync(scr->init_table, table, sizeof(table), cudaMemcpyHostToDevice, s) != cudaSuccess)
-        return PG_ERR_CUDA;
-    // Work queues and the error word start at zero; the order is rewritten below.
-    if (cudaMemsetAsync(scr->counters, 0, sizeof(scr->counters), s) != cudaSuccess) return PG_ERR_CUDA;
+    // Work queues and the error word start at zero, the initial table is
+    // rewritten (by value: no host buffer), and the order is rewritten below.
+    InitTable table;
+    initial_table(cfg->num_initial_components, cfg->init_kappa, table.v);
+    noalloc_prepare_kernel<<<1, 64, 0, s>>>(table, scr);
+    if (cudaGetLastError() != cudaSuccess) return PG_ERR_CUDA;
     const uint32_t cluster = 2u, cap = 4096u, large_threshold = 24576u;
     order_regions_kernel<128><<<1, 1024, 0, s>>>(offsets, n_regions, scr->order, large_threshold, scr->counters + 3);
     if (cudaGetLastError() != cudaSuccess) return PG_ERR_CUDA;
@@ -158,6 +188,9 @@ extern "C" int pg_fit_regions_noalloc(const pg_fit_config *cfg, pg_region_state 
     args.ll_out = nullptr;
     args.stages = 2u;
     const bool wide = (mode == PG_FIT_INIT) ? (cfg->num_initial_components > 8) : true;
-    return wide ? launch_noalloc<16, 3, true>(args, s, cluster, cap, sms)
-                : launch_noalloc<8, 0, false>(args, s, cluster, cap, sms);
+    st = wide ? launch_noalloc<16, 3, true>(args, s, cluster, cap, sms)
+              : launch_noalloc<8, 0, false>(args, s, cluster, cap, sms);
+    if (st) return st;
+    noalloc_finish_kernel<<<(n_regions + 255) / 256, 256, 0, s>>>(states, n_regions, scr->counters + 2);
+    return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ERR_CUDA;
 }
