@@ -406,10 +406,6 @@ int pg_update(pg_ctx *ctx, const pg_directional_data *records, uint64_t n_record
 /* Scenes, traversal and the wavefront path tracer                       */
 /* ------------------------------------------------------------------ */
 
-/* Material types: MAT_DIFFUSE, MAT_SPECULAR, MAT_DIELECTRIC, MAT_LIGHT of
- * shaders/raytrace.rgen:21-27.  PG_MAT_GGX is a GGX microfacet conductor; it
- * takes the place of the reference's Beckmann MAT_ROUGH_CONDUCTOR
- * (raytrace.rgen:222-236). */
 /* Material types: the reference's EMatType (src/SceneLoader.h:31-39) - diffuse,
  * specular, dielectric, light, Phong, conductor - plus GGX (the project's
  * glossy lobe) and the reference's Beckmann rough conductor. */
@@ -517,6 +513,11 @@ typedef struct pg_render_params {
 /* Time each stage with CUDA events on the render stream (the call then
  * synchronises the stream before returning). */
 #define PG_RENDER_TIME_STAGES 2u
+/* Guide near-specular lobes too (Beckmann / GGX roughness <= 0.3, Phong
+ * exponent >= 250), as the reference does: it mixes the guide into every
+ * non-discrete material (raytrace.rgen:926) while recording only the others
+ * (:962-964, 1180).  Off by default: guiding then follows the recording rule. */
+#define PG_RENDER_GUIDE_ALMOST_DISCRETE 4u
 
 enum pg_render_stage {
     PG_STAGE_CAMERA = 0, PG_STAGE_EXTEND, PG_STAGE_SHADE, PG_STAGE_SHADOW, PG_STAGE_ADVANCE, PG_STAGE_COMMIT,
@@ -609,6 +610,67 @@ int pg_trace_closest_counted(pg_scene *scene, const pg_ray *rays, uint32_t n, pg
  * written to records (device, width * height * 16), INVALID where empty. */
 int pg_render(pg_scene *scene, const pg_render_params *params, pg_ctx *guide, float *image,
               pg_directional_data *records, pg_render_stats *stats, void *stream);
+
+/* Shading-function probes (diagnostics; no counterpart in the reference,
+ * whose functions run inside its ray-generation shader).  Each probe runs one
+ * of the renderer's own device functions on explicit inputs and random
+ * numbers, so the functions can be compared with the reference's shader
+ * functions (shaders/raytrace.rgen, guiding.glsl, random.glsl) one call at a
+ * time:
+ *   PG_PROBE_FRESNEL            fresnel(a = eta, b = cos_i)            raytrace.rgen:145-160
+ *   PG_PROBE_FRESNEL_CONDUCTOR  fresnelConductor(a = cos_i, b = eta, c = k)  :163-175
+ *   PG_PROBE_BSDF_EVAL          evalBsdf * and pdfBSDF at (n, wi, wo)   :284-332, 557-599
+ *   PG_PROBE_BSDF_SAMPLE        sampleBSDF with u[1..3]; v[3] = its pdf :483-552
+ *   PG_PROBE_VMM_PDF            VMM(wo) of mixture `vmm` seen from x     guiding.glsl:53-60
+ *   PG_PROBE_VMM_SAMPLE         sampleVMM from x with u[4], u[2], u[3]  guiding.glsl:62-96
+ *   PG_PROBE_CONTINUE           getNewDirection and evalBsdf / pdf      raytrace.rgen:923-960, 1176
+ *                               (u = choice, lobe/ul, u1, u2, lobe choice; c = guiding prob;
+ *                               result: direction, pdf, throughput change)
+ *   PG_PROBE_TO_WORLD           toWorld(wo, n)                          transform.glsl:7-38
+ * (* the library's BSDF value includes the cosine, as evalBsdf's does.)
+ * flags: bit 0 front face, bit 1 parallax re-aiming, bit 2 the vertex is
+ * guided, bit 3 its region exists (else the path ends), bit 4 the guide-all
+ * rule (PG_RENDER_GUIDE_ALMOST_DISCRETE).  mats, vmms, probes and out are
+ * device arrays; a probe whose material or mixture index is out of range
+ * writes NaN results. */
+enum {
+    PG_PROBE_FRESNEL = 0, PG_PROBE_FRESNEL_CONDUCTOR = 1, PG_PROBE_BSDF_EVAL = 2, PG_PROBE_BSDF_SAMPLE = 3,
+    PG_PROBE_VMM_PDF = 4, PG_PROBE_VMM_SAMPLE = 5, PG_PROBE_CONTINUE = 6, PG_PROBE_TO_WORLD = 7
+};
+typedef struct pg_shading_probe {
+    int32_t op;
+    uint32_t material;  /* index into mats */
+    uint32_t vmm;       /* index into vmms */
+    uint32_t flags;
+    float n[3], wi[3], wo[3], x[3];
+    float u[5];
+    float a, b, c;
+} pg_shading_probe;
+typedef struct pg_shading_result {
+    float v[8];  /* direction or value (3), pdf, throughput change (3), unused */
+} pg_shading_result;
+int pg_probe_shading(const pg_material *mats, uint32_t n_mats, const pg_vmm_theta *vmms, uint32_t n_vmms,
+                     const pg_shading_probe *probes, uint32_t n, pg_shading_result *out, void *stream);
+
+/* Sample-recording probe (diagnostics; no counterpart in the reference):
+ * replays paths through the renderer's record functions - radiance reaching
+ * a path is added to its earlier records through their throughput changes
+ * (updateSamples, raytrace.rgen:973-978), then each record is committed with
+ * weight |L| / pdf or marked invalid (commitSamples, :980-990).  Path p's
+ * events are events[path_offsets[p] .. path_offsets[p + 1]); kind 0 records a
+ * vertex (pdf, throughput change tc, region id; at most 16 per path, later
+ * ones dropped), kind 1 is radiance `light` reaching the path.  Per path:
+ * counts[p] records, weights / flags [p * 16 + k] (flags = region id or
+ * PG_INVALID_REGION).  All arrays are device arrays. */
+typedef struct pg_record_event {
+    int32_t kind;
+    float pdf;
+    float tc[3];
+    uint32_t region;
+    float light[3];
+} pg_record_event;
+int pg_probe_records(const pg_record_event *events, const uint32_t *path_offsets, uint32_t n_paths, float *weights,
+                     uint32_t *flags, uint32_t *counts, void *stream);
 
 /* ------------------------------------------------------------------ */
 /* Allocation-free fit                                                 */

@@ -1,0 +1,208 @@
+"""TEST INFRASTRUCTURE: ctypes access to the reference's shader functions
+compiled as host C++ (oracle/_ref/libglslref.so, built by
+oracle/build_glsl_ref.py where the reference tree is present).
+
+The functions are the reference's own (shaders/raytrace.rgen, guiding.glsl,
+random.glsl, transform.glsl); this module maps the library's material and
+mixture records onto the reference's, and turns the random state a sampling
+function leaves behind into the list of numbers it drew, so the same numbers
+can be handed to the project's implementations.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_ref" / "libglslref.so"
+
+# the reference's MAT_* numbers (raytrace.rgen:21-27)
+MAT_DIFFUSE, MAT_SPECULAR, MAT_DIELECTRIC, MAT_LIGHT, MAT_PHONG, MAT_CONDUCTOR, MAT_ROUGH_CONDUCTOR = range(7)
+# the library's PG_MAT_* numbers (include/pathguide.h)
+PG_MAT = dict(DIFFUSE=0, SPECULAR=1, DIELECTRIC=2, LIGHT=3, PHONG=4, CONDUCTOR=5, GGX=6, BECKMANN=7)
+_PG_TO_REF = {0: MAT_DIFFUSE, 1: MAT_SPECULAR, 2: MAT_DIELECTRIC, 3: MAT_LIGHT, 4: MAT_PHONG, 5: MAT_CONDUCTOR,
+              7: MAT_ROUGH_CONDUCTOR}
+
+
+class RefMaterial(C.Structure):
+    _fields_ = [("type", C.c_int32), ("light", C.c_float * 3), ("diffuse", C.c_float * 3),
+                ("specular", C.c_float * 3), ("specular_highlight", C.c_float), ("refraction_index", C.c_float),
+                ("eta", C.c_float), ("k", C.c_float), ("roughness", C.c_float)]
+
+
+def ref_material(pg: np.void) -> RefMaterial:
+    """The reference's Material for a library pg_material record (fields as
+    the reference's SceneLoader fills them, src/SceneLoader.cpp:558-648)."""
+    t = int(pg["type"])
+    m = RefMaterial()
+    m.type = _PG_TO_REF[t]
+    m.light[:] = [float(x) for x in pg["emission"]]
+    if t in (PG_MAT["SPECULAR"], PG_MAT["DIELECTRIC"]):
+        m.specular[:] = [float(x) for x in pg["albedo"]]
+    else:
+        m.diffuse[:] = [float(x) for x in pg["albedo"]]
+    if t == PG_MAT["PHONG"]:
+        m.specular[:] = [float(x) for x in pg["specular"]]
+    m.specular_highlight = float(pg["exponent"])
+    m.refraction_index = float(pg["ior"]) if float(pg["ior"]) > 0 else 1.0
+    m.eta, m.k, m.roughness = float(pg["eta"]), float(pg["k"]), float(pg["roughness"])
+    return m
+
+
+def available() -> bool:
+    return LIB_PATH.exists()
+
+
+class GlslRef:
+    def __init__(self, path: Path = LIB_PATH):
+        self.lib = C.CDLL(str(path))
+        f, p, u, i = C.c_float, C.c_void_p, C.c_uint32, C.c_int
+        P = C.POINTER
+        sig = {
+            "glslref_rnd_sequence": (None, [u, u, p]),
+            "glslref_fresnel": (f, [f, f]),
+            "glslref_fresnel_conductor": (f, [f, f, f]),
+            "glslref_beckmann_D": (f, [p, p, p]),
+            "glslref_beckmann_G1": (f, [p, p, p, p]),
+            "glslref_power_heuristic": (f, [f, f]),
+            "glslref_eval_bsdf": (f, [p, p, p, p, i, p]),
+            "glslref_sample_bsdf": (f, [p, p, p, i, u, p, P(u)]),
+            "glslref_vmm_pdf": (f, [p, p, p, i]),
+            "glslref_sample_vmm": (None, [p, p, i, u, p, P(u)]),
+            "glslref_new_direction": (f, [p, p, p, p, i, p, C.c_int32, i, f, i, u, p, p, P(u)]),
+            "glslref_cosine_hemisphere": (None, [p, u, p, P(u)]),
+            "glslref_cosine_power": (None, [p, f, u, p, P(u)]),
+            "glslref_beckmann_normal": (None, [p, p, u, p, P(u)]),
+            "glslref_to_world": (None, [p, p, p]),
+            "glslref_almost_discrete": (i, [p]),
+            "glslref_discrete": (i, [p]),
+            "glslref_record_path": (u, [u, p, p, p, p, p, p, p]),
+            "glslref_weight_window": (f, [p, p, p, f, u, P(C.c_int32), P(u)]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(self.lib, name)
+            fn.restype = res
+            fn.argtypes = args
+
+    # ---- random numbers -------------------------------------------------
+    def drawn(self, state: int, state_after: int, limit: int = 64) -> np.ndarray:
+        """The rnd() values a call drew between two generator states."""
+        seq = np.zeros(limit, dtype=np.float32)
+        self.lib.glslref_rnd_sequence(state, limit, seq.ctypes.data)
+        s = state
+        for n in range(limit + 1):
+            if s == state_after:
+                return seq[:n].copy()
+            s = (1664525 * s + 1013904223) & 0xFFFFFFFF
+        raise RuntimeError("random state not reached")
+
+    @staticmethod
+    def _v(x) -> np.ndarray:
+        return np.ascontiguousarray(x, dtype=np.float32)
+
+    # ---- functions --------------------------------------------------------
+    def fresnel(self, eta, cos_i):
+        return self.lib.glslref_fresnel(eta, cos_i)
+
+    def fresnel_conductor(self, cos_i, eta, k):
+        return self.lib.glslref_fresnel_conductor(cos_i, eta, k)
+
+    def eval_bsdf(self, mat: RefMaterial, n, wi, wo, front=True):
+        """(evalBsdf, pdfBSDF)."""
+        out = np.zeros(3, np.float32)
+        n, wi, wo = self._v(n), self._v(wi), self._v(wo)
+        pdf = self.lib.glslref_eval_bsdf(C.byref(mat), n.ctypes.data, wi.ctypes.data, wo.ctypes.data,
+                                         int(front), out.ctypes.data)
+        return out, pdf
+
+    def sample_bsdf(self, mat: RefMaterial, wi, n, front, state):
+        """(direction, pdf, numbers drawn)."""
+        d = np.zeros(3, np.float32)
+        after = C.c_uint32()
+        wi, n = self._v(wi), self._v(n)
+        pdf = self.lib.glslref_sample_bsdf(C.byref(mat), wi.ctypes.data, n.ctypes.data, int(front), state,
+                                           d.ctypes.data, C.byref(after))
+        return d, pdf, self.drawn(state, after.value)
+
+    def vmm_pdf(self, vmm: np.ndarray, wo, pos, parallax):
+        wo, pos = self._v(wo), self._v(pos)
+        return self.lib.glslref_vmm_pdf(vmm.ctypes.data, wo.ctypes.data, pos.ctypes.data, int(parallax))
+
+    def sample_vmm(self, vmm: np.ndarray, pos, parallax, state):
+        d = np.zeros(3, np.float32)
+        after = C.c_uint32()
+        pos = self._v(pos)
+        self.lib.glslref_sample_vmm(vmm.ctypes.data, pos.ctypes.data, int(parallax), state, d.ctypes.data,
+                                    C.byref(after))
+        return d, self.drawn(state, after.value)
+
+    def new_direction(self, mat: RefMaterial, origin, n, wi, front, vmm, region, use_guiding, guiding_prob,
+                      parallax, state):
+        """getNewDirection: (direction, pdf, throughput change, numbers drawn)."""
+        d = np.zeros(3, np.float32)
+        tc = np.zeros(3, np.float32)
+        after = C.c_uint32()
+        origin, n, wi = self._v(origin), self._v(n), self._v(wi)
+        pdf = self.lib.glslref_new_direction(C.byref(mat), origin.ctypes.data, n.ctypes.data, wi.ctypes.data,
+                                             int(front), vmm.ctypes.data, int(region), int(use_guiding),
+                                             guiding_prob, int(parallax), state, d.ctypes.data, tc.ctypes.data,
+                                             C.byref(after))
+        return d, pdf, tc, self.drawn(state, after.value)
+
+    def cosine_hemisphere(self, n, state):
+        d = np.zeros(3, np.float32)
+        after = C.c_uint32()
+        n = self._v(n)
+        self.lib.glslref_cosine_hemisphere(n.ctypes.data, state, d.ctypes.data, C.byref(after))
+        return d, self.drawn(state, after.value)
+
+    def cosine_power(self, axis, p, state):
+        d = np.zeros(3, np.float32)
+        after = C.c_uint32()
+        axis = self._v(axis)
+        self.lib.glslref_cosine_power(axis.ctypes.data, p, state, d.ctypes.data, C.byref(after))
+        return d, self.drawn(state, after.value)
+
+    def beckmann_normal(self, mat, n, state):
+        d = np.zeros(3, np.float32)
+        after = C.c_uint32()
+        n = self._v(n)
+        self.lib.glslref_beckmann_normal(C.byref(mat), n.ctypes.data, state, d.ctypes.data, C.byref(after))
+        return d, self.drawn(state, after.value)
+
+    def to_world(self, v, n):
+        out = np.zeros(3, np.float32)
+        v, n = self._v(v), self._v(n)
+        self.lib.glslref_to_world(v.ctypes.data, n.ctypes.data, out.ctypes.data)
+        return out
+
+    def almost_discrete(self, mat) -> bool:
+        return bool(self.lib.glslref_almost_discrete(C.byref(mat)))
+
+    def discrete(self, mat) -> bool:
+        return bool(self.lib.glslref_discrete(C.byref(mat)))
+
+    def record_path(self, kinds, pdfs, tcs, regions, lights):
+        """Committed (weights, flags) of one path's recorded vertices."""
+        n = len(kinds)
+        k = np.ascontiguousarray(kinds, np.int32)
+        p = np.ascontiguousarray(pdfs, np.float32)
+        t = np.ascontiguousarray(tcs, np.float32).reshape(n, 3)
+        r = np.ascontiguousarray(regions, np.uint32)
+        L = np.ascontiguousarray(lights, np.float32).reshape(n, 3)
+        w = np.zeros(16, np.float32)
+        fl = np.zeros(16, np.uint32)
+        m = self.lib.glslref_record_path(n, k.ctypes.data, p.ctypes.data, t.ctypes.data, r.ctypes.data,
+                                         L.ctypes.data, w.ctypes.data, fl.ctypes.data)
+        return w[:m].copy(), fl[:m].copy()
+
+    def weight_window(self, estimate, throughput, adjoint, s, state):
+        """applyWeightWindow: (q, n, numbers drawn)."""
+        n = C.c_int32()
+        after = C.c_uint32()
+        e, t, a = self._v(estimate), self._v(throughput), self._v(adjoint)
+        q = self.lib.glslref_weight_window(e.ctypes.data, t.ctypes.data, a.ctypes.data, s, state, C.byref(n),
+                                           C.byref(after))
+        return q, n.value, self.drawn(state, after.value)

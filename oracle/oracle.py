@@ -299,6 +299,18 @@ class TraceOracle:
                                      _U32, _I]
         L.pgo_rnd.argtypes = [_U32, _U32, _U32, _U32]
         L.pgo_rnd.restype = C.c_float
+        L.pgo_probe_shading.argtypes = [_P, _U32, _P, _U32, _P, _U32, _P]
+
+    def probe_shading(self, mats: np.ndarray, vmms: np.ndarray, probes: np.ndarray) -> np.ndarray:
+        """The FP64 restatement of the renderer's shading functions on
+        pg_probe_shading records; (n, 8) float64."""
+        m = np.ascontiguousarray(mats, dtype=abi.MATERIAL_DTYPE)
+        v = np.ascontiguousarray(vmms, dtype=abi.VMM_THETA_DTYPE)
+        p = np.ascontiguousarray(probes, dtype=abi.PROBE_DTYPE)
+        out = np.zeros((max(len(p), 1), 8), dtype=np.float64)
+        self.lib.pgo_probe_shading(m.ctypes.data, len(m), v.ctypes.data, len(v), p.ctypes.data, len(p),
+                                   out.ctypes.data)
+        return out[:len(p)]
 
     @staticmethod
     def scene(exp: dict, camera: "abi.Camera | None" = None) -> tuple:

@@ -612,8 +612,11 @@ bool almost_delta(const pg_material &m) {
     return ((m.type == PG_MAT_GGX || m.type == PG_MAT_BECKMANN) && m.roughness <= 0.3f) ||
            (m.type == PG_MAT_PHONG && m.exponent >= 250.0f);
 }
-// guiding follows the recording rule: not on discrete or almost-discrete lobes
-bool guided_material(const pg_material &m) { return !is_delta(m) && !almost_delta(m); }
+// guiding follows the recording rule (not on discrete or almost-discrete
+// lobes) unless PG_RENDER_GUIDE_ALMOST_DISCRETE asks for the reference's rule
+bool guided_material(const pg_material &m, uint32_t flags) {
+    return !is_delta(m) && ((flags & PG_RENDER_GUIDE_ALMOST_DISCRETE) || !almost_delta(m));
+}
 
 D3 sample_bsdf(const pg_material &m, D3 d, D3 n, double ul, double u1, double u2) {
     if (m.type == PG_MAT_PHONG) {
@@ -694,6 +697,78 @@ D3 vmm_sample(const pg_vmm_theta &v, D3 x, int par, double ul, double u1, double
     }
     const double z = 1.0 - 2.0 * u1, r = sqrt(std::max(0.0, 1.0 - z * z)), ph = 2.0 * PI * u2;
     return d3(r * cos(ph), r * sin(ph), z);
+}
+
+// The continuation of a path at a vertex: getNewDirection (raytrace.rgen:
+// 923-960) and the throughput change evalBsdf / pdf (:1176), the estimator's
+// choices as the device makes them (delta materials reflect or refract, a
+// guided vertex without a region ends the path, draw_ua() supplies the lobe
+// choice only when the guide is sampled).
+struct Continuation {
+    D3 wo;
+    double pdf;
+    D3 tc;
+    bool delta;
+};
+template <typename DrawUa>
+Continuation continue_path(const pg_material &m, D3 d, D3 n, bool front, D3 x, bool gm, const pg_vmm_theta *mix,
+                           int par, double guiding_prob, double uch, double ul, double u1, double u2,
+                           DrawUa draw_ua) {
+    Continuation c{d3(0, 0, 1), 0.0, d3(0, 0, 0), false};
+    const D3 wi = d * -1.0;
+    if (m.type == PG_MAT_DIELECTRIC) {
+        const double eta = front ? 1.0 / m.ior : m.ior;
+        const double ci = dot(wi, n);
+        const double F = fresnel(eta, ci);
+        if (ul > F) {
+            const double k = 1.0 - eta * eta * (1.0 - ci * ci);
+            c.wo = k < 0.0 ? reflect(d, n) : unit(d * eta - n * (eta * (-ci) + sqrt(std::max(k, 0.0))));
+        } else {
+            c.wo = reflect(d, n);
+        }
+        c.pdf = 1.0;
+        c.tc = fv(m.albedo);
+        c.delta = true;
+    } else if (m.type == PG_MAT_SPECULAR) {
+        c.wo = reflect(d, n);
+        c.pdf = 1.0;
+        c.tc = fv(m.albedo);
+        c.delta = true;
+    } else if (m.type == PG_MAT_CONDUCTOR) {
+        c.wo = reflect(d, n);
+        c.pdf = 1.0;
+        const double F = fresnel_conductor(dot(wi, n), m.eta, m.k);
+        c.tc = d3(F, F, F);
+        c.delta = true;
+    } else {
+        if (gm && !mix) return c;
+        const bool use_guide = gm && uch < guiding_prob;
+        D3 wo = use_guide ? vmm_sample(*mix, x, par, draw_ua(), u1, u2) : sample_bsdf(m, d, n, ul, u1, u2);
+        Eval me = bsdf(m, n, wi, wo);
+        double pdf = me.pdf;
+        if (gm) {
+            if (dot(wo, n) < 0.0 || me.pdf <= 0.0) {
+                pdf = 0.0;
+            } else {
+                const double pg = vmm_pdf(*mix, wo, x, par);
+                if (std::isnan(pg)) {
+                    if (use_guide) {
+                        wo = sample_bsdf(m, d, n, ul, u1, u2);
+                        me = bsdf(m, n, wi, wo);
+                    }
+                    pdf = me.pdf;
+                } else {
+                    pdf = (1.0 - guiding_prob) * me.pdf + guiding_prob * pg;
+                }
+            }
+        }
+        c.wo = wo;
+        if (dot(wo, n) > 0.0 && pdf > 0.0 && me.pdf > 0.0) {
+            c.tc = me.f * (1.0 / pdf);
+            c.pdf = pdf;
+        }
+    }
+    return c;
 }
 
 // the lat-long environment along d (raytrace.rmiss), bilinear with wrap-around
@@ -800,7 +875,7 @@ D3 render_pixel(const Scene64 &sc, const pg_render_params &rp, const pgo_guide *
                 const Eval me = bsdf(m, n, wi, wl);
                 if (mx(me.f) > 0.0) {
                     double pb = me.pdf;
-                    if (rp.use_guiding && g && guided_material(m)) {
+                    if (rp.use_guiding && g && guided_material(m, rp.flags)) {
                         const uint32_t reg = region_of(*g, x);
                         if (reg != PG_INVALID_REGION) {
                             const double pg = vmm_pdf(g->vmm[reg], wl, x, par);
@@ -839,7 +914,7 @@ D3 render_pixel(const Scene64 &sc, const pg_render_params &rp, const pgo_guide *
                 const Eval me = bsdf(m, n, wi, wl);
                 if (mx(me.f) > 0.0) {
                     double pb = me.pdf;
-                    if (rp.use_guiding && g && guided_material(m)) {
+                    if (rp.use_guiding && g && guided_material(m, rp.flags)) {
                         const uint32_t reg = region_of(*g, x);
                         if (reg != PG_INVALID_REGION) {
                             const double pg = vmm_pdf(g->vmm[reg], wl, x, par);
@@ -853,73 +928,19 @@ D3 render_pixel(const Scene64 &sc, const pg_render_params &rp, const pgo_guide *
             }
             }
         }
-        D3 wo = d3(0, 0, 1), tc = d3(0, 0, 0);
-        double pdf = 0.0;
-        bool delta = false;
         const double uch = rnd(rp.seed, pix, smp, dimb(b, 3)), ul = rnd(rp.seed, pix, smp, dimb(b, 4));
         const double u1 = rnd(rp.seed, pix, smp, dimb(b, 5)), u2 = rnd(rp.seed, pix, smp, dimb(b, 6));
-        if (m.type == PG_MAT_DIELECTRIC) {
-            const double eta = front ? 1.0 / m.ior : m.ior;
-            const double ci = dot(wi, n);
-            const double F = fresnel(eta, ci);
-            if (ul > F) {
-                const double k = 1.0 - eta * eta * (1.0 - ci * ci);
-                wo = k < 0.0 ? reflect(d, n) : unit(d * eta - n * (eta * (-ci) + sqrt(std::max(k, 0.0))));
-            } else {
-                wo = reflect(d, n);
-            }
-            pdf = 1.0;
-            tc = fv(m.albedo);
-            delta = true;
-        } else if (m.type == PG_MAT_SPECULAR) {
-            wo = reflect(d, n);
-            pdf = 1.0;
-            tc = fv(m.albedo);
-            delta = true;
-        } else if (m.type == PG_MAT_CONDUCTOR) {
-            wo = reflect(d, n);
-            pdf = 1.0;
-            const double F = fresnel_conductor(dot(wi, n), m.eta, m.k);
-            tc = d3(F, F, F);
-            delta = true;
-        } else {
-            const bool gm = rp.use_guiding && g && guided_material(m);
-            bool use_guide = false, terminate = false;
-            uint32_t reg = PG_INVALID_REGION;
-            if (gm) {
-                reg = region_of(*g, x);
-                if (reg == PG_INVALID_REGION) terminate = true;
-                use_guide = uch < rp.guiding_prob;
-            }
-            if (!terminate) {
-                if (use_guide)
-                    wo = vmm_sample(g->vmm[reg], x, par, rnd(rp.seed, pix, smp, dimb(b, 7)), u1, u2);
-                else
-                    wo = sample_bsdf(m, d, n, ul, u1, u2);
-                Eval me = bsdf(m, n, wi, wo);
-                pdf = me.pdf;
-                if (gm) {
-                    if (dot(wo, n) < 0.0 || me.pdf <= 0.0) {
-                        pdf = 0.0;
-                    } else {
-                        const double pg = vmm_pdf(g->vmm[reg], wo, x, par);
-                        if (std::isnan(pg)) {
-                            if (use_guide) {
-                                wo = sample_bsdf(m, d, n, ul, u1, u2);
-                                me = bsdf(m, n, wi, wo);
-                            }
-                            pdf = me.pdf;
-                        } else {
-                            pdf = (1.0 - rp.guiding_prob) * me.pdf + rp.guiding_prob * pg;
-                        }
-                    }
-                }
-                if (dot(wo, n) > 0.0 && pdf > 0.0 && me.pdf > 0.0)
-                    tc = me.f * (1.0 / pdf);
-                else
-                    pdf = 0.0;
-            }
+        const bool gm = rp.use_guiding && g && guided_material(m, rp.flags);
+        const pg_vmm_theta *mix = nullptr;
+        if (gm) {
+            const uint32_t reg = region_of(*g, x);
+            if (reg != PG_INVALID_REGION) mix = &g->vmm[reg];
         }
+        const Continuation cn = continue_path(m, d, n, front, x, gm, mix, par, rp.guiding_prob, uch, ul, u1, u2,
+                                              [&] { return rnd(rp.seed, pix, smp, dimb(b, 7)); });
+        const D3 wo = cn.wo, tc = cn.tc;
+        const double pdf = cn.pdf;
+        const bool delta = cn.delta;
         if (!(pdf > 0.0 && mx(tc) > 0.0)) break;
         thr = hm(thr, tc);
         o = x;
@@ -932,6 +953,75 @@ D3 render_pixel(const Scene64 &sc, const pg_render_params &rp, const pgo_guide *
 }  // namespace
 
 extern "C" {
+
+void pgo_probe_shading(const pg_material *mats, uint32_t n_mats, const pg_vmm_theta *vmms, uint32_t n_vmms,
+                       const pg_shading_probe *P, uint32_t count, double *out) {
+    for (uint32_t i = 0; i < count; ++i) {
+        const pg_shading_probe &q = P[i];
+        double *r = out + 8 * i;
+        for (int k = 0; k < 8; ++k) r[k] = 0.0;
+        const bool uses_mat = q.op == PG_PROBE_BSDF_EVAL || q.op == PG_PROBE_BSDF_SAMPLE || q.op == PG_PROBE_CONTINUE;
+        const bool uses_vmm = q.op == PG_PROBE_VMM_PDF || q.op == PG_PROBE_VMM_SAMPLE ||
+                              (q.op == PG_PROBE_CONTINUE && (q.flags & 8u));
+        if ((uses_mat && q.material >= n_mats) || (uses_vmm && q.vmm >= n_vmms)) {
+            for (int k = 0; k < 8; ++k) r[k] = NAN;
+            continue;
+        }
+        const D3 n = fv(q.n), wi = fv(q.wi), wo = fv(q.wo), x = fv(q.x);
+        const bool front = (q.flags & 1u) != 0;
+        const int par = (q.flags & 2u) ? 1 : 0;
+        auto put = [&](int at, D3 v) {
+            r[at] = v.x;
+            r[at + 1] = v.y;
+            r[at + 2] = v.z;
+        };
+        switch (q.op) {
+            case PG_PROBE_FRESNEL:
+                r[0] = fresnel(q.a, q.b);
+                break;
+            case PG_PROBE_FRESNEL_CONDUCTOR:
+                r[0] = fresnel_conductor(q.a, q.b, q.c);
+                break;
+            case PG_PROBE_BSDF_EVAL: {
+                const Eval e = bsdf(mats[q.material], n, wi, wo);
+                put(0, e.f);
+                r[3] = e.pdf;
+                break;
+            }
+            case PG_PROBE_BSDF_SAMPLE: {
+                const pg_material &m = mats[q.material];
+                const D3 w = sample_bsdf(m, wi * -1.0, n, q.u[1], q.u[2], q.u[3]);
+                put(0, w);
+                r[3] = bsdf(m, n, wi, w).pdf;
+                break;
+            }
+            case PG_PROBE_VMM_PDF:
+                r[0] = vmm_pdf(vmms[q.vmm], wo, x, par);
+                break;
+            case PG_PROBE_VMM_SAMPLE:
+                put(0, vmm_sample(vmms[q.vmm], x, par, q.u[4], q.u[2], q.u[3]));
+                break;
+            case PG_PROBE_CONTINUE: {
+                const pg_material &m = mats[q.material];
+                const uint32_t rf = (q.flags & 16u) ? PG_RENDER_GUIDE_ALMOST_DISCRETE : 0u;
+                const bool gm = (q.flags & 4u) && guided_material(m, rf);
+                const pg_vmm_theta *mix = (q.flags & 8u) ? &vmms[q.vmm] : nullptr;
+                const double ua = q.u[4];
+                const Continuation c = continue_path(m, wi * -1.0, n, front, x, gm, mix, par, q.c, q.u[0], q.u[1],
+                                                     q.u[2], q.u[3], [&] { return ua; });
+                put(0, c.wo);
+                r[3] = c.pdf;
+                put(4, c.tc);
+                break;
+            }
+            case PG_PROBE_TO_WORLD:
+                put(0, to_world(wo, n));
+                break;
+            default:
+                break;
+        }
+    }
+}
 
 float pgo_rnd(uint32_t seed, uint32_t pixel, uint32_t sample, uint32_t dim) { return (float)rnd(seed, pixel, sample, dim); }
 

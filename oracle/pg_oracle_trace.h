@@ -63,6 +63,11 @@ void pgo_trace_any(const pgo_scene *s, const pg_ray *rays, uint32_t n, uint32_t 
 void pgo_render_f64(const pgo_scene *s, const pg_render_params *params, const pgo_guide *guide, double *image,
                     uint32_t row_begin, uint32_t row_end, int n_threads);
 
+/* The renderer's shading functions in double precision on the probes of
+ * pg_probe_shading (same records and result layout: 8 values per probe). */
+void pgo_probe_shading(const pg_material *mats, uint32_t n_mats, const pg_vmm_theta *vmms, uint32_t n_vmms,
+                       const pg_shading_probe *probes, uint32_t n, double *out);
+
 /* The renderer's random number (seed, pixel, sample, dimension). */
 float pgo_rnd(uint32_t seed, uint32_t pixel, uint32_t sample, uint32_t dim);
 

@@ -103,6 +103,8 @@ SIGNATURES = {
     "pg_trace_closest": (_I, [_P, _P, _U32, _P, _P]),
     "pg_trace_any": (_I, [_P, _P, _U32, _P, _P]),
     "pg_trace_closest_counted": (_I, [_P, _P, _U32, _P, _P, _P, _P]),
+    "pg_probe_shading": (_I, [_P, _U32, _P, _U32, _P, _U32, _P, _P]),
+    "pg_probe_records": (_I, [_P, _P, _U32, _P, _P, _P, _P]),
     "pg_render": (_I, [_P, C.POINTER(abi.RenderParams), _P, _P, _P, C.POINTER(abi.RenderStats), _P]),
 }
 
@@ -456,6 +458,42 @@ def fit_regions_noalloc(cfg: abi.FitConfig, states_dev, dirw, offsets, n_regions
     Returns the status."""
     return library().pg_fit_regions_noalloc(C.byref(cfg), _dptr(states_dev), _dptr(dirw), _dptr(offsets),
                                             n_regions, mode, _stream_handle(stream))
+
+
+def probe_shading(mats: np.ndarray, vmms: np.ndarray, probes: np.ndarray) -> np.ndarray:
+    """pg_probe_shading on the current CUDA device: the renderer's shading
+    functions on explicit inputs (probes: abi.PROBE_DTYPE records; mats:
+    abi.MATERIAL_DTYPE; vmms: abi.VMM_THETA_DTYPE).  Returns (n, 8) float32."""
+    import torch
+    dev = lambda a: torch.from_numpy(np.frombuffer(np.ascontiguousarray(a).tobytes(), dtype=np.uint8).copy()).cuda()
+    n = len(probes)
+    dm, dv, dp = dev(mats), dev(vmms), dev(probes)
+    out = torch.zeros((max(n, 1), 8), dtype=torch.float32, device="cuda")
+    st = library().pg_probe_shading(_dptr(dm), len(mats), _dptr(dv), len(vmms), _dptr(dp), n, _dptr(out), None)
+    if st != abi.PG_OK:
+        raise PathGuideError(st, "pg_probe_shading")
+    torch.cuda.synchronize()
+    return out[:n].cpu().numpy()
+
+
+def probe_records(events: np.ndarray, path_offsets: np.ndarray):
+    """pg_probe_records on the current CUDA device: the renderer's sample
+    recording replayed over paths of abi.RECORD_EVENT_DTYPE events.  Returns
+    (weights (P, 16), flags (P, 16), counts (P,))."""
+    import torch
+    ev = np.ascontiguousarray(events, dtype=abi.RECORD_EVENT_DTYPE)
+    offs = np.ascontiguousarray(path_offsets, dtype=np.uint32)
+    P = len(offs) - 1
+    d_ev = torch.from_numpy(np.frombuffer(ev.tobytes(), dtype=np.uint8).copy()).cuda()
+    d_off = torch.from_numpy(offs.view(np.int32).copy()).cuda()
+    w = torch.zeros((max(P, 1), 16), dtype=torch.float32, device="cuda")
+    f = torch.zeros((max(P, 1), 16), dtype=torch.int32, device="cuda")
+    c = torch.zeros(max(P, 1), dtype=torch.int32, device="cuda")
+    st = library().pg_probe_records(_dptr(d_ev), _dptr(d_off), P, _dptr(w), _dptr(f), _dptr(c), None)
+    if st != abi.PG_OK:
+        raise PathGuideError(st, "pg_probe_records")
+    torch.cuda.synchronize()
+    return w[:P].cpu().numpy(), f[:P].cpu().numpy().view(np.uint32), c[:P].cpu().numpy().view(np.uint32)
 
 
 def read_png(path) -> np.ndarray:

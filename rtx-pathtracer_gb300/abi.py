@@ -90,6 +90,18 @@ NODE_DTYPE = np.dtype([("lo", "<f4", (3, 4)), ("hi", "<f4", (3, 4)), ("child", "
 assert MATERIAL_DTYPE.itemsize == 64 and SPHERE_DTYPE.itemsize == 32 and RAY_DTYPE.itemsize == 32
 assert HIT_DTYPE.itemsize == 16 and NODE_DTYPE.itemsize == 128
 
+# shading-function probes (pg_probe_shading)
+PG_PROBE_FRESNEL, PG_PROBE_FRESNEL_CONDUCTOR, PG_PROBE_BSDF_EVAL, PG_PROBE_BSDF_SAMPLE, PG_PROBE_VMM_PDF, \
+    PG_PROBE_VMM_SAMPLE, PG_PROBE_CONTINUE, PG_PROBE_TO_WORLD = range(8)
+PROBE_FRONT, PROBE_PARALLAX, PROBE_GUIDED, PROBE_REGION, PROBE_GUIDE_ALL = 1, 2, 4, 8, 16
+PROBE_DTYPE = np.dtype([("op", "<i4"), ("material", "<u4"), ("vmm", "<u4"), ("flags", "<u4"),
+                        ("n", "<f4", (3,)), ("wi", "<f4", (3,)), ("wo", "<f4", (3,)), ("x", "<f4", (3,)),
+                        ("u", "<f4", (5,)), ("a", "<f4"), ("b", "<f4"), ("c", "<f4")])
+assert PROBE_DTYPE.itemsize == 96
+RECORD_EVENT_DTYPE = np.dtype([("kind", "<i4"), ("pdf", "<f4"), ("tc", "<f4", (3,)), ("region", "<u4"),
+                               ("light", "<f4", (3,))])
+assert RECORD_EVENT_DTYPE.itemsize == 36
+
 
 class Camera(C.Structure):
     _fields_ = [("origin", C.c_float * 3), ("target", C.c_float * 3), ("up", C.c_float * 3),
@@ -160,6 +172,7 @@ class RenderParams(C.Structure):
 
 PG_RENDER_COUNT_WORK = 1
 PG_RENDER_TIME_STAGES = 2
+PG_RENDER_GUIDE_ALMOST_DISCRETE = 4
 STAGES = ("camera", "extend", "shade", "shadow", "advance", "commit")
 
 

@@ -216,10 +216,13 @@ __device__ __forceinline__ bool almost_delta(const pg_material &m) {
 }
 // Vertices whose continuation mixes in the guide.  The reference guides every
 // non-discrete material (raytrace.rgen:926) but records only the ones that
-// are not almost discrete; here guiding follows the recording rule, so a
-// near-specular lobe is never sampled from a mixture learned at other
-// surfaces of its region.
-__device__ __forceinline__ bool guided_material(const pg_material &m) { return !is_delta(m) && !almost_delta(m); }
+// are not almost discrete; by default guiding here follows the recording
+// rule, so a near-specular lobe is never sampled from a mixture learned at
+// other surfaces of its region.  PG_RENDER_GUIDE_ALMOST_DISCRETE restores the
+// reference's rule.
+__device__ __forceinline__ bool guided_material(const pg_material &m, uint32_t render_flags) {
+    return !is_delta(m) && ((render_flags & PG_RENDER_GUIDE_ALMOST_DISCRETE) || !almost_delta(m));
+}
 
 // Lambert (cosine), Phong (a lobe chosen by ul, sampleBSDF raytrace.rgen:
 // 491-517), Beckmann (randomBeckmannNormal, random.glsl:127-136) or GGX
@@ -357,6 +360,85 @@ __device__ V vmm_sample(const pg_vmm_theta &v, V x, int par, float u_lobe, float
     return mk(r * cosf(ph), r * sinf(ph), z);
 }
 
+// The continuation of a path at a vertex (getNewDirection, raytrace.rgen:
+// 923-960, and the throughput change evalBsdf / pdf of :1176): delta
+// materials reflect or refract (a dielectric picks by Fresnel with ul);
+// others sample the BSDF or, with probability guiding_prob at a guided
+// vertex (gm), the region's mixture `mix`, and weight by the one-sample
+// mixture pdf.  A guided vertex without a region (mix null) ends the path
+// (pdf 0).  draw_ua() supplies the lobe-choice number, drawn only when the
+// guide is sampled.
+struct Continuation {
+    V wo;
+    float pdf;
+    V tc;        // throughput change f cos / pdf
+    bool delta;  // discrete direction
+};
+template <typename DrawUa>
+__device__ __forceinline__ Continuation continue_path(const pg_material &m, V d, V n, bool front, V x, bool gm,
+                                                      const pg_vmm_theta *mix, int par, float guiding_prob,
+                                                      float uch, float ul, float u1, float u2, DrawUa draw_ua) {
+    Continuation c{mk(0, 0, 1), 0.0f, mk(0, 0, 0), false};
+    const V wi = mul(d, -1.0f);
+    if (m.type == PG_MAT_DIELECTRIC) {
+        const float eta = front ? 1.0f / m.ior : m.ior;  // refractionIndexInv in front
+        const float ci = dot3(wi, n);
+        const float F = fresnel_dielectric(eta, ci);
+        if (ul > F) {
+            // refract(-wi, n, eta)
+            const float k = 1.0f - eta * eta * (1.0f - ci * ci);
+            c.wo = k < 0.0f ? reflect3(d, n) : sub(mul(d, eta), mul(n, eta * (-ci) + sqrtf(fmaxf(k, 0.0f))));
+            c.wo = nrm(c.wo);
+        } else {
+            c.wo = reflect3(d, n);
+        }
+        c.pdf = 1.0f;
+        c.tc = mk(m.albedo[0], m.albedo[1], m.albedo[2]);
+        c.delta = true;
+    } else if (m.type == PG_MAT_SPECULAR) {
+        c.wo = reflect3(d, n);
+        c.pdf = 1.0f;
+        c.tc = mk(m.albedo[0], m.albedo[1], m.albedo[2]);
+        c.delta = true;
+    } else if (m.type == PG_MAT_CONDUCTOR) {
+        // evalBsdf MAT_CONDUCTOR (raytrace.rgen:588-592)
+        c.wo = reflect3(d, n);
+        c.pdf = 1.0f;
+        const float F = fresnel_conductor(dot3(wi, n), m.eta, m.k);
+        c.tc = mk(F, F, F);
+        c.delta = true;
+    } else {
+        if (gm && !mix) return c;  // no region: the path ends
+        const bool use_guide = gm && uch < guiding_prob;
+        V wo = use_guide ? vmm_sample(*mix, x, par, draw_ua(), u1, u2) : sample_bsdf(m, d, n, ul, u1, u2);
+        MatEval me = bsdf_eval(m, n, wi, wo);
+        float pdf = me.pdf;
+        if (gm) {
+            if (dot3(wo, n) < 0.0f || me.pdf <= 0.0f) {
+                pdf = 0.0f;
+            } else {
+                const float pg = vmm_pdf(*mix, wo, x, par);
+                if (isnan(pg)) {
+                    // unusable mixture: a plain BSDF sample (raytrace.rgen:951-953)
+                    if (use_guide) {
+                        wo = sample_bsdf(m, d, n, ul, u1, u2);
+                        me = bsdf_eval(m, n, wi, wo);
+                    }
+                    pdf = me.pdf;
+                } else {
+                    pdf = (1.0f - guiding_prob) * me.pdf + guiding_prob * pg;
+                }
+            }
+        }
+        c.wo = wo;
+        if (dot3(wo, n) > 0.0f && pdf > 0.0f && me.pdf > 0.0f) {
+            c.tc = mul(me.f, 1.0f / pdf);
+            c.pdf = pdf;
+        }
+    }
+    return c;
+}
+
 // ---------------------------------------------------------------------------
 // Device scene and render state
 // ---------------------------------------------------------------------------
@@ -460,16 +542,25 @@ __device__ __forceinline__ void warp_append(uint32_t *counter, uint32_t *queue, 
 
 // updateSamples (raytrace.rgen:973-978): radiance L arriving at the vertex
 // after record slot n-1 flows back through the recorded throughput changes.
-__device__ __forceinline__ void update_records(const DevRender &R, uint32_t pix, uint32_t n, V L) {
-    const uint32_t start = R.rec_start[pix];
+// Radiance L reaching a path: added to the light sums of its records
+// [start, n), scaled back through each record's throughput change
+// (updateSamples, raytrace.rgen:973-978).  lsum and tc are the path's
+// record slots (3 floats each).
+__device__ __forceinline__ void add_record_radiance(float *lsum, const float *tc, uint32_t start, uint32_t n, V L) {
     for (int i = (int)n - 1; i >= (int)start; --i) {
-        const uint32_t s = pix * kMaxRecords + (uint32_t)i;
-        R.rec_lsum[3 * s] += L.x;
-        R.rec_lsum[3 * s + 1] += L.y;
-        R.rec_lsum[3 * s + 2] += L.z;
-        L = hmul(L, ld3(R.rec_tc, s));
+        lsum[3 * i] += L.x;
+        lsum[3 * i + 1] += L.y;
+        lsum[3 * i + 2] += L.z;
+        L = hmul(L, ld3(tc, (uint32_t)i));
     }
 }
+__device__ __forceinline__ void update_records(const DevRender &R, uint32_t pix, uint32_t n, V L) {
+    const uint32_t base = pix * kMaxRecords;
+    add_record_radiance(R.rec_lsum + 3 * (size_t)base, R.rec_tc + 3 * (size_t)base, R.rec_start[pix], n, L);
+}
+// A record's weight |L| / pdf (commitSamples, raytrace.rgen:980-990); a
+// weight that is not positive leaves the record invalid.
+__device__ __forceinline__ float record_weight(V lsum, float pdf) { return sqrtf(dot3(lsum, lsum)) / pdf; }
 
 // Environment radiance along a direction (raytrace.rmiss): the lat-long map
 // at u = atan2(x, -z) / 2 pi, v = acos(y) / pi, bilinear with wrap-around in
@@ -706,7 +797,7 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
                     const MatEval me = bsdf_eval(m, n, wi, wl);
                     if (maxc(me.f) > 0.0f) {
                         float pb = me.pdf;
-                        if (R.guiding && guided_material(m)) {
+                        if (R.guiding && guided_material(m, R.rp.flags)) {
                             const uint32_t reg = region_of(R.guide, x);
                             if (reg != PG_INVALID_REGION) {
                                 const float pg = vmm_pdf(R.guide.vmm[reg], wl, x, R.guide.use_parallax);
@@ -761,7 +852,7 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
                         if (maxc(me.f) > 0.0f) {
                             // pdf of the continuation sampler for this direction (MIS)
                             float pb = me.pdf;
-                            if (R.guiding && guided_material(m)) {
+                            if (R.guiding && guided_material(m, R.rp.flags)) {
                                 const uint32_t reg = region_of(R.guide, x);
                                 if (reg != PG_INVALID_REGION) {
                                     const float pg = vmm_pdf(R.guide.vmm[reg], wl, x, R.guide.use_parallax);
@@ -783,80 +874,21 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
                 }
             }
             // --- continuation (getNewDirection, raytrace.rgen:923-960)
-            V wo = mk(0, 0, 1);
-            float pdf = 0.0f;
-            V tc = mk(0, 0, 0);  // throughput change f cos / pdf
-            bool delta = false;
             const float uch = rnd(R.rp.seed, p, R.sample, dimb(b, 3));
             const float ul = rnd(R.rp.seed, p, R.sample, dimb(b, 4));
             const float u1 = rnd(R.rp.seed, p, R.sample, dimb(b, 5)), u2 = rnd(R.rp.seed, p, R.sample, dimb(b, 6));
-            if (m.type == PG_MAT_DIELECTRIC) {
-                const float eta = front ? 1.0f / m.ior : m.ior;  // refractionIndexInv in front
-                const float ci = dot3(wi, n);
-                const float F = fresnel_dielectric(eta, ci);
-                if (ul > F) {
-                    // refract(-wi, n, eta)
-                    const float k = 1.0f - eta * eta * (1.0f - ci * ci);
-                    wo = k < 0.0f ? reflect3(d, n) : sub(mul(d, eta), mul(n, eta * (-ci) + sqrtf(fmaxf(k, 0.0f))));
-                    wo = nrm(wo);
-                } else {
-                    wo = reflect3(d, n);
-                }
-                pdf = 1.0f;
-                tc = mk(m.albedo[0], m.albedo[1], m.albedo[2]);
-                delta = true;
-            } else if (m.type == PG_MAT_SPECULAR) {
-                wo = reflect3(d, n);
-                pdf = 1.0f;
-                tc = mk(m.albedo[0], m.albedo[1], m.albedo[2]);
-                delta = true;
-            } else if (m.type == PG_MAT_CONDUCTOR) {
-                // evalBsdf MAT_CONDUCTOR (raytrace.rgen:588-592)
-                wo = reflect3(d, n);
-                pdf = 1.0f;
-                const float F = fresnel_conductor(dot3(wi, n), m.eta, m.k);
-                tc = mk(F, F, F);
-                delta = true;
-            } else {
-                const bool gm = R.guiding && guided_material(m);
-                bool use_guide = false;
-                uint32_t reg = PG_INVALID_REGION;
-                bool terminate = false;
-                if (gm) {
-                    reg = region_of(R.guide, x);
-                    if (reg == PG_INVALID_REGION) terminate = true;  // no region: the path ends
-                    use_guide = uch < R.rp.guiding_prob;
-                }
-                if (!terminate) {
-                    if (use_guide) {
-                        const float ua = rnd(R.rp.seed, p, R.sample, dimb(b, 7));
-                        wo = vmm_sample(R.guide.vmm[reg], x, R.guide.use_parallax, ua, u1, u2);
-                    } else {
-                        wo = sample_bsdf(m, d, n, ul, u1, u2);
-                    }
-                    MatEval me = bsdf_eval(m, n, wi, wo);
-                    pdf = me.pdf;
-                    if (gm) {
-                        if (dot3(wo, n) < 0.0f || me.pdf <= 0.0f) {
-                            pdf = 0.0f;
-                        } else {
-                            const float pg = vmm_pdf(R.guide.vmm[reg], wo, x, R.guide.use_parallax);
-                            if (isnan(pg)) {
-                                // unusable mixture: a plain BSDF sample (raytrace.rgen:951-953)
-                                if (use_guide) {
-                                    wo = sample_bsdf(m, d, n, ul, u1, u2);
-                                    me = bsdf_eval(m, n, wi, wo);
-                                }
-                                pdf = me.pdf;
-                            } else {
-                                pdf = (1.0f - R.rp.guiding_prob) * me.pdf + R.rp.guiding_prob * pg;
-                            }
-                        }
-                    }
-                    if (dot3(wo, n) > 0.0f && pdf > 0.0f && me.pdf > 0.0f) tc = mul(me.f, 1.0f / pdf);
-                    else pdf = 0.0f;
-                }
+            const bool gm = R.guiding && guided_material(m, R.rp.flags);
+            const pg_vmm_theta *mix = nullptr;
+            if (gm) {
+                const uint32_t reg = region_of(R.guide, x);
+                if (reg != PG_INVALID_REGION) mix = &R.guide.vmm[reg];
             }
+            const Continuation cn = continue_path(m, d, n, front, x, gm, mix, R.guide.use_parallax,
+                                                  R.rp.guiding_prob, uch, ul, u1, u2,
+                                                  [&] { return rnd(R.rp.seed, p, R.sample, dimb(b, 7)); });
+            const V wo = cn.wo, tc = cn.tc;
+            const float pdf = cn.pdf;
+            const bool delta = cn.delta;
             if (pdf > 0.0f && maxc(tc) > 0.0f) {
                 thr = hmul(thr, tc);
                 cont = true;
@@ -970,8 +1002,7 @@ __global__ void k_commit(DevRender R, uint32_t n_pix) {
     for (uint32_t k = start; k < cnt; ++k) {
         const uint32_t s = p * kMaxRecords + k;
         pg_directional_data &rd = R.rec[s];
-        const V L = ld3(R.rec_lsum, s);
-        const float w = sqrtf(dot3(L, L)) / rd.pdf;
+        const float w = record_weight(ld3(R.rec_lsum, s), rd.pdf);
         if (!(w > 0.0f) || rd.flags == PG_INVALID_REGION) {
             rd.flags = PG_INVALID_REGION;
         } else {
@@ -1003,6 +1034,111 @@ __global__ void k_reset_records(pg_directional_data *rec, uint32_t n_slots, uint
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n_slots) rec[i].flags = PG_INVALID_REGION;
     if (i < n_pix) rec_start[i] = 0;
+}
+
+// One shading-function call per probe (pg_probe_shading).
+__global__ void k_probe_shading(const pg_material *mats, uint32_t n_mats, const pg_vmm_theta *vmms,
+                                uint32_t n_vmms, const pg_shading_probe *P, uint32_t count, pg_shading_result *out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const pg_shading_probe q = P[i];
+    pg_shading_result r;
+    const bool uses_mat = q.op == PG_PROBE_BSDF_EVAL || q.op == PG_PROBE_BSDF_SAMPLE || q.op == PG_PROBE_CONTINUE;
+    const bool uses_vmm = q.op == PG_PROBE_VMM_PDF || q.op == PG_PROBE_VMM_SAMPLE ||
+                          (q.op == PG_PROBE_CONTINUE && (q.flags & 8u));
+    const bool bad = (uses_mat && q.material >= n_mats) || (uses_vmm && q.vmm >= n_vmms);
+    for (int k = 0; k < 8; ++k) r.v[k] = bad ? __int_as_float(0x7fc00000) : 0.0f;
+    if (bad) {
+        out[i] = r;
+        return;
+    }
+    const V n = mk(q.n[0], q.n[1], q.n[2]), wi = mk(q.wi[0], q.wi[1], q.wi[2]);
+    const V wo = mk(q.wo[0], q.wo[1], q.wo[2]), x = mk(q.x[0], q.x[1], q.x[2]);
+    const bool front = (q.flags & 1u) != 0;
+    const int par = (q.flags & 2u) ? 1 : 0;
+    auto put = [&](int at, V v) {
+        r.v[at] = v.x;
+        r.v[at + 1] = v.y;
+        r.v[at + 2] = v.z;
+    };
+    switch (q.op) {
+        case PG_PROBE_FRESNEL:
+            r.v[0] = fresnel_dielectric(q.a, q.b);
+            break;
+        case PG_PROBE_FRESNEL_CONDUCTOR:
+            r.v[0] = fresnel_conductor(q.a, q.b, q.c);
+            break;
+        case PG_PROBE_BSDF_EVAL: {
+            const MatEval e = bsdf_eval(mats[q.material], n, wi, wo);
+            put(0, e.f);
+            r.v[3] = e.pdf;
+            break;
+        }
+        case PG_PROBE_BSDF_SAMPLE: {
+            const pg_material &m = mats[q.material];
+            const V w = sample_bsdf(m, mul(wi, -1.0f), n, q.u[1], q.u[2], q.u[3]);
+            put(0, w);
+            r.v[3] = bsdf_eval(m, n, wi, w).pdf;
+            break;
+        }
+        case PG_PROBE_VMM_PDF:
+            r.v[0] = vmm_pdf(vmms[q.vmm], wo, x, par);
+            break;
+        case PG_PROBE_VMM_SAMPLE:
+            put(0, vmm_sample(vmms[q.vmm], x, par, q.u[4], q.u[2], q.u[3]));
+            break;
+        case PG_PROBE_CONTINUE: {
+            const pg_material &m = mats[q.material];
+            const uint32_t rf = (q.flags & 16u) ? PG_RENDER_GUIDE_ALMOST_DISCRETE : 0u;
+            const bool gm = (q.flags & 4u) && guided_material(m, rf);
+            const pg_vmm_theta *mix = (q.flags & 8u) ? &vmms[q.vmm] : nullptr;
+            const Continuation c = continue_path(m, mul(wi, -1.0f), n, front, x, gm, mix, par, q.c, q.u[0], q.u[1],
+                                                 q.u[2], q.u[3], [&] { return q.u[4]; });
+            put(0, c.wo);
+            r.v[3] = c.pdf;
+            put(4, c.tc);
+            break;
+        }
+        case PG_PROBE_TO_WORLD:
+            put(0, to_world(wo, n));
+            break;
+        default:
+            break;
+    }
+    out[i] = r;
+}
+
+// Sample recording of one path per thread (pg_probe_records): the events in
+// order through the renderer's record functions, then the commit.
+__global__ void k_probe_records(const pg_record_event *ev, const uint32_t *offsets, uint32_t n_paths, float *weights,
+                                uint32_t *flags, uint32_t *counts) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_paths) return;
+    float lsum[3 * kMaxRecords], tc[3 * kMaxRecords], pdf[kMaxRecords];
+    uint32_t region[kMaxRecords];
+    uint32_t cnt = 0;
+    for (uint32_t e = offsets[p]; e < offsets[p + 1]; ++e) {
+        const pg_record_event q = ev[e];
+        if (q.kind == 0) {
+            if (cnt >= (uint32_t)kMaxRecords) continue;
+            for (int c = 0; c < 3; ++c) {
+                lsum[3 * cnt + c] = 0.0f;
+                tc[3 * cnt + c] = q.tc[c];
+            }
+            pdf[cnt] = q.pdf;
+            region[cnt] = q.region;
+            ++cnt;
+        } else {
+            add_record_radiance(lsum, tc, 0u, cnt, mk(q.light[0], q.light[1], q.light[2]));
+        }
+    }
+    for (uint32_t k = 0; k < cnt; ++k) {
+        const float w = record_weight(ld3(lsum, k), pdf[k]);
+        const bool valid = w > 0.0f && region[k] != PG_INVALID_REGION;
+        weights[p * kMaxRecords + k] = valid ? w : 0.0f;
+        flags[p * kMaxRecords + k] = valid ? region[k] : PG_INVALID_REGION;
+    }
+    counts[p] = cnt;
 }
 
 __global__ void k_trace_closest(DevScene S, const pg_ray *rays, uint32_t n, pg_hit *hits) {
@@ -1473,6 +1609,23 @@ int pg_scene_export_mesh(const pg_scene *sc, float *positions, uint32_t *indices
     if (positions) memcpy(positions, s.pos.data(), sizeof(float) * s.pos.size());
     if (indices) memcpy(indices, s.idx.data(), sizeof(uint32_t) * s.idx.size());
     return PG_OK;
+}
+
+int pg_probe_shading(const pg_material *mats, uint32_t n_mats, const pg_vmm_theta *vmms, uint32_t n_vmms,
+                     const pg_shading_probe *probes, uint32_t n, pg_shading_result *out, void *stream) {
+    if (n == 0) return PG_OK;
+    if (!probes || !out || (n_mats && !mats) || (n_vmms && !vmms)) return PG_ERR_ARG;
+    k_probe_shading<<<(n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(mats, n_mats, vmms, n_vmms, probes, n, out);
+    return cudaGetLastError() == cudaSuccess ? PG_OK : scene_error(PG_ERR_CUDA, "probe launch");
+}
+
+int pg_probe_records(const pg_record_event *events, const uint32_t *path_offsets, uint32_t n_paths, float *weights,
+                     uint32_t *flags, uint32_t *counts, void *stream) {
+    if (n_paths == 0) return PG_OK;
+    if (!events || !path_offsets || !weights || !flags || !counts) return PG_ERR_ARG;
+    k_probe_records<<<(n_paths + 127) / 128, 128, 0, (cudaStream_t)stream>>>(events, path_offsets, n_paths, weights,
+                                                                           flags, counts);
+    return cudaGetLastError() == cudaSuccess ? PG_OK : scene_error(PG_ERR_CUDA, "probe launch");
 }
 
 int pg_trace_closest(pg_scene *sc, const pg_ray *rays, uint32_t n, pg_hit *hits, void *stream) {

@@ -1,0 +1,62 @@
+"""The tracer's shading functions against the reference's own shader
+functions (shaders/raytrace.rgen, guiding.glsl, random.glsl, transform.glsl),
+which oracle/build_glsl_ref.py compiles as host C++ where the reference tree is
+present.
+
+* The committed fixture (tests/golden/shader_ref.npz) is what that build
+  computes: regenerated and compared bit for bit where the tree is present.
+* The FP64 restatement of the renderer (oracle/pg_oracle_trace.cpp, the
+  image oracle of the GPU tests) evaluates every fixture case within the
+  tolerances of tests/shader_cmp.py.  The GPU's functions are compared in
+  tests/test_shader_ref_gpu.py.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from shader_cmp import compare
+
+from conftest import GOLDEN
+
+
+@pytest.fixture(scope="module")
+def fixture():
+    return np.load(GOLDEN / "shader_ref.npz")
+
+
+def test_fixture_is_what_the_reference_functions_compute(tmp_path, fixture):
+    from oracle import build_glsl_ref
+    if build_glsl_ref.build_glsl_ref() is None:
+        pytest.skip("reference tree absent: the fixture stands as committed")
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_shader_golden", GOLDEN / "make_shader_golden.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    out = tmp_path / "shader_ref.npz"
+    mod.main(out)
+    fresh = np.load(out)
+    for k in fixture.files:
+        assert fresh[k].dtype == fixture[k].dtype and fresh[k].tobytes() == fixture[k].tobytes(), k
+
+
+def test_fp64_oracle_matches_reference_shader_functions(fixture):
+    from oracle import build_oracle
+    build_oracle.build_oracle()
+    from oracle.oracle import TraceOracle
+    got = TraceOracle().probe_shading(fixture["mats"], fixture["vmms"], fixture["probes"])
+    report, failures = compare(fixture, got)
+    assert not failures, "\n".join(failures[:20])
+    # every family was exercised
+    for name in ("fresnel", "eval", "sample_dir", "sample_pdf", "vmm_pdf", "vmm_sample", "continue_dir",
+                 "continue_tc", "continue_pdf", "to_world"):
+        assert report[name][0] > 100, name
+
+
+def test_reference_function_families_cover_the_materials(fixture):
+    tags = set(str(t) for t in fixture["tags"])
+    for mi in range(len(fixture["mats"])):
+        assert any(t.startswith(f"continue_{mi}_") for t in tags)
+    # guided with a region, guided without one, unguided
+    for suffix in ("_01", "_10", "_11"):
+        assert any(t.endswith(suffix) for t in tags if t.startswith("continue"))
