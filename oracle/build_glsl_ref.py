@@ -10,11 +10,16 @@ rewrites only -
 
   * ``in`` parameter qualifiers dropped, ``out``/``inout T x`` become ``T &x``;
   * unsuffixed floating literals get an ``f`` suffix (GLSL literals are float);
-  * a scalar swizzle ``(expr).xxx`` becomes ``xxx(expr)``;
+  * a scalar swizzle ``(expr).xxx`` becomes ``xxx(expr)``, and the identity
+    swizzle ``origin.xyz`` / ``direction.xyz`` / ``normal.xyz`` of a vec3 the
+    vec3 itself;
   * ``T f = f(...)`` (a variable named after the function that initialises
     it, legal in GLSL) calls ``glsl::f`` by its qualified name;
   * each switch case's statements are put in braces (GLSL allows
     declarations between case labels);
+  * variables declared at file scope become ``thread_local`` (each shader
+    invocation has its own), and a shader's ``main()`` body becomes a named
+    function;
   * ``#include`` / ``#version`` / ``#extension`` lines are dropped;
 
 and writes oracle/_ref/glsl_ref_gen.cpp, which wraps the text in namespace
@@ -42,7 +47,7 @@ PART_A = [
     ("limits.glsl", 1, 7),            # SIZE_LIGHT_RANDOM, MAX_DISTRIBUTIONS, MAX_DIRECTIONAL_DATA_PER_PIXEL
     ("raycommon.glsl", 1, 76),        # hitInfo, shadowCheck, pushConstant, sphere
     ("raycommon.glsl", 83, 103),      # cacheHeader, cacheData, cacheHits
-    ("wavefront.glsl", 9, 45),        # Material, InstanceInfo, Light, FaceSample
+    ("wavefront.glsl", 1, 45),        # Vertex, Material, InstanceInfo, Light, FaceSample
     ("random_fwd.glsl", 1, 40),       # forward declarations of random.glsl
     ("transform_fwd.glsl", 1, 11),    # forward declarations of transform.glsl
     ("guiding.glsl", 5, 113),         # VMF_Theta, vMF, VMM_Theta, VMM, sampleVMF, sampleVMM, DirectionalData
@@ -58,11 +63,31 @@ PART_B = [
     ("raytrace.rgen", 806, 869),      # isICCapable, approxDiffuse, applyWeightWindow
     ("raytrace.rgen", 923, 990),      # getNewDirection, isMatAlmostDiscrete, getBaseIndex, updateSamples, commitSamples
 ]
+# the estimator: the per-invocation state of the ray-generation shader, the
+# hit / miss shaders (their main() bodies become the named functions) and the
+# path loop with next-event estimation
+PART_C_STATE = [
+    ("raytrace.rgen", 56, 84),        # ray flags, new irradiance-cache entries, the split queue
+]
+SHADERS_AS_FUNCTIONS = [
+    ("raytrace.rchit", 17, 58, "closestHitTriangle"),
+    ("raytrace.sphere.rchit", 14, 35, "closestHitSphere"),
+    ("raytrace.rmiss", 16, 30, "missShader"),
+    ("raytrace.shadow.rmiss", 8, 10, "shadowMissShader"),
+]
+PART_C = [
+    ("raytrace.rgen", 358, 473),      # sampleLights
+    ("raytrace.rgen", 601, 731),      # nextEventEstimation
+    ("raytrace.rgen", 745, 804),      # queryIrradianceCache(Gradients)
+    ("raytrace.rgen", 871, 902),      # multipleNEE, split
+    ("raytrace.rgen", 992, 1226),     # raytrace: the path loop, NEE, guiding, sample recording
+]
 
 _QUAL_OUT = re.compile(r"\b(?:out|inout)\s+(\w+)\s+(\w+)")
 _QUAL_IN = re.compile(r"\bin\s+(\w+)\s+(\w+)")
 _SIGNATURE = re.compile(r"^\s*\w+\s+\w+\s*\(.*\)\s*[{;]?\s*$")
 _LABEL = re.compile(r"^\s*(case\s+[^:]+|default\s*):\s*$")
+_VEC3_XYZ = re.compile(r"\b(origin|direction|normal)\.xyz\b")
 _SELF_INIT = re.compile(r"\b(\w+)\s+(\w+)\s*=\s*\2\s*\(")
 _FLOAT_LIT = re.compile(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])")
 
@@ -115,9 +140,23 @@ def _scope_cases(lines):
     return out
 
 
+_GLOBAL_VAR = re.compile(r"^(?!\s*(?:const|struct|return|#|typedef)\b)(\w+\s+\w+\s*(?:\[[^\]]*\])?\s*(?:=[^;]*)?;)\s*$")
+
+
+def _thread_local_globals(lines):
+    out, depth = [], 0
+    for line in lines:
+        code = line.partition("//")[0]
+        if depth == 0 and _GLOBAL_VAR.match(code) and "(" not in code:
+            line = "thread_local " + line
+        depth += code.count("{") - code.count("}")
+        out.append(line)
+    return out
+
+
 def transform(text: str) -> str:
     out = []
-    for line in _scope_cases(text.splitlines()):
+    for line in _thread_local_globals(_scope_cases(text.splitlines())):
         s = line.strip()
         if s.startswith("#include") or s.startswith("#version") or s.startswith("#extension"):
             out.append("")
@@ -129,6 +168,7 @@ def transform(text: str) -> str:
             code, sep, comment = line.partition("//")
             code = _FLOAT_LIT.sub(lambda m: m.group(1) + "f", code)
             code = _swizzle_xxx(code)
+            code = _VEC3_XYZ.sub(r"\1", code)
             code = _SELF_INIT.sub(lambda m: f"{m.group(1)} {m.group(2)} = glsl::{m.group(2)}(", code)
             line = code + sep + comment
         out.append(line)
@@ -143,6 +183,15 @@ def _excerpt(parts) -> str:
     return "\n".join(chunks)
 
 
+def _shaders_as_functions() -> str:
+    chunks = []
+    for name, a, b, fn in SHADERS_AS_FUNCTIONS:
+        lines = (SHADERS / name).read_text().splitlines()
+        body = "\n".join(lines[a - 1:b])
+        chunks.append(f"void {fn}() {{\n#line {a} \"{name}\"\n" + transform(body) + "\n}")
+    return "\n".join(chunks)
+
+
 def generate() -> Path:
     OUT_DIR.mkdir(exist_ok=True)
     src = "\n".join([
@@ -154,8 +203,14 @@ def generate() -> Path:
         '#line 1 "glsl_ref_stubs.inc"',
         '#include "glsl_ref_stubs.inc"',
         _excerpt(PART_B),
+        _excerpt(PART_C_STATE),
+        '#line 1 "glsl_ref_scene.inc"',
+        '#include "glsl_ref_scene.inc"',
+        _shaders_as_functions(),
+        _excerpt(PART_C),
         "}  // namespace glsl",
         '#include "glsl_ref_harness.inc"',
+        '#include "glsl_ref_render.inc"',
         "",
     ])
     out = OUT_DIR / "glsl_ref_gen.cpp"
@@ -167,13 +222,19 @@ def generate() -> Path:
 def build_glsl_ref(force: bool = False):
     if not (SHADERS / "raytrace.rgen").exists():
         return None
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_pg_oracle_build", HERE / "build_oracle.py")
+    ob = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(ob)
+    ob.build_oracle()  # the traversal twin the estimator's ray queries run on
     gen = generate()
     lib = OUT_DIR / "libglslref.so"
     deps = [gen, HERE / "glsl_shim.hpp", HERE / "glsl_ref_stubs.inc", HERE / "glsl_ref_harness.inc",
-            Path(__file__)]
+            HERE / "glsl_ref_scene.inc", HERE / "glsl_ref_render.inc", HERE / "liboracle.so", Path(__file__)]
     if force or not lib.exists() or any(d.stat().st_mtime > lib.stat().st_mtime for d in deps):
-        cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-fpermissive", "-w",
-               f"-I{HERE}", f"-I{HERE.parent / 'include'}", str(gen), "-o", str(lib)]
+        cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-fpermissive", "-w", "-pthread",
+               f"-I{HERE}", f"-I{HERE.parent / 'include'}", str(gen), "-o", str(lib),
+               f"-L{HERE}", "-loracle", "-Wl,-rpath,$ORIGIN/.."]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)

@@ -55,6 +55,13 @@ def available() -> bool:
     return LIB_PATH.exists()
 
 
+class RenderConfig(C.Structure):
+    _fields_ = [("spp", C.c_uint32), ("max_depth", C.c_uint32), ("max_follow_discrete", C.c_uint32),
+                ("use_nee", C.c_uint32), ("use_mis", C.c_uint32), ("use_guiding", C.c_uint32),
+                ("guiding_prob", C.c_float), ("use_parallax", C.c_uint32), ("frame_seed", C.c_uint32),
+                ("region_splits", C.c_uint32), ("region_root", C.c_float * 6)]
+
+
 class GlslRef:
     def __init__(self, path: Path = LIB_PATH):
         self.lib = C.CDLL(str(path))
@@ -80,6 +87,7 @@ class GlslRef:
             "glslref_discrete": (i, [p]),
             "glslref_record_path": (u, [u, p, p, p, p, p, p, p]),
             "glslref_weight_window": (f, [p, p, p, f, u, P(C.c_int32), P(u)]),
+            "glslref_render": (i, [p, P(RenderConfig), p, u, u, i, p]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(self.lib, name)
@@ -197,6 +205,35 @@ class GlslRef:
         m = self.lib.glslref_record_path(n, k.ctypes.data, p.ctypes.data, t.ctypes.data, r.ctypes.data,
                                          L.ctypes.data, w.ctypes.data, fl.ctypes.data)
         return w[:m].copy(), fl[:m].copy()
+
+    def render(self, exp: dict, path_length: int, spp: int, frame_seed: int, use_nee=True, use_mis=True,
+               guide: dict | None = None, guiding_prob=0.5, rows=None, threads=None) -> np.ndarray:
+        """The reference's estimator (raytrace() and the hit shaders compiled as
+        C++) over an exported library scene: radiance sums (H, W, 3).
+        path_length is the library's max_depth (paths of at most that many
+        segments); the reference's maxDepth counts two fewer (its next-event
+        estimation runs at the vertex after maxDepth)."""
+        import os
+        from oracle.oracle import TraceOracle
+        s, keep = TraceOracle.scene(exp)
+        cam = exp["info"].camera
+        W, H = cam.width, cam.height
+        img = np.zeros((H, W, 3), dtype=np.float64)
+        cfg = RenderConfig(spp=spp, max_depth=max(path_length - 2, 0), max_follow_discrete=0,
+                           use_nee=int(use_nee), use_mis=int(use_mis), use_guiding=int(guide is not None),
+                           guiding_prob=guiding_prob, frame_seed=frame_seed)
+        vmm = None
+        if guide is not None:
+            cfg.use_parallax = int(guide["use_parallax"])
+            cfg.region_splits = int(guide["split_count"])
+            cfg.region_root[:] = [float(x) for x in guide["root"]]
+            vmm = np.ascontiguousarray(guide["vmm"])
+        r0, r1 = rows if rows is not None else (0, H)
+        st = self.lib.glslref_render(C.byref(s), C.byref(cfg), vmm.ctypes.data if vmm is not None else None, r0, r1,
+                                     threads or os.cpu_count() or 1, img.ctypes.data)
+        if st != 0:
+            raise RuntimeError("glslref_render failed")
+        return img
 
     def weight_window(self, estimate, throughput, adjoint, s, state):
         """applyWeightWindow: (q, n, numbers drawn)."""

@@ -52,9 +52,19 @@ struct vec4 {
     vec4(const vec3 &v, float d) : x(v.x), y(v.y), z(v.z), w(d), xyz(v) {}
 };
 
-struct mat4 {
-    float m[16];
+struct ivec3 {
+    int x, y, z;
+    ivec3(int a, int b, int c) : x(a), y(b), z(c) {}
 };
+
+struct mat4 {
+    float m[16];  // column-major, as GLSL: m[4 * column + row]
+};
+inline vec4 operator*(const mat4 &a, const vec4 &v) {
+    float r[4];
+    for (int i = 0; i < 4; ++i) r[i] = a.m[i] * v.x + a.m[4 + i] * v.y + a.m[8 + i] * v.z + a.m[12 + i] * v.w;
+    return vec4(r[0], r[1], r[2], r[3]);
+}
 
 inline vec3 operator+(vec3 a, vec3 b) { return vec3(a.x + b.x, a.y + b.y, a.z + b.z); }
 inline vec3 operator-(vec3 a, vec3 b) { return vec3(a.x - b.x, a.y - b.y, a.z - b.z); }
@@ -66,6 +76,7 @@ inline vec3 operator/(vec3 a, float s) { return vec3(a.x / s, a.y / s, a.z / s);
 inline vec3 operator+(vec3 a, float s) { return vec3(a.x + s, a.y + s, a.z + s); }
 inline vec3 operator-(vec3 a) { return vec3(-a.x, -a.y, -a.z); }
 inline vec2 operator*(vec2 a, float s) { return vec2(a.x * s, a.y * s); }
+inline vec2 operator+(vec2 a, vec2 b) { return vec2(a.x + b.x, a.y + b.y); }
 
 // scalar functions, single precision as in GLSL
 inline float abs(float x) { return std::fabs(x); }
@@ -107,8 +118,10 @@ inline vec3 mix(vec3 a, vec3 b, float t) { return a * (1.0f - t) + b * t; }
 // `expr.xxx` of a scalar expression
 inline vec3 xxx(float s) { return vec3(s); }
 
-// Texture lookups: the tests use untextured materials only; a lookup reads white.
+// Texture lookups: sampler 0 is the environment map (raytrace.rmiss,
+// raytrace.rgen:406-421), answered by the estimator harness; the tests use
+// untextured materials, so no other sampler is read.
 extern int textureSamplers[64];
-inline vec4 texture(int, vec2) { return vec4(1.0f); }
+vec4 texture(int sampler, vec2 uv);
 
 }  // namespace glsl

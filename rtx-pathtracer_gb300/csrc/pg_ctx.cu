@@ -192,6 +192,7 @@ int pg_set_region_states(pg_ctx *ctx, const pg_region_state *host_in, uint32_t f
     if (!ctx || (!host_in && count)) return PG_ERR_ARG;
     if ((uint64_t)first + count > ctx->max_regions) return set_error(ctx, PG_ERR_ARG, "region range out of bounds");
     cudaStream_t s = (cudaStream_t)stream;
+    guide_mark_stale(ctx);
     int st = check_cuda(ctx,
                         cudaMemcpyAsync(ctx->d_states + first, host_in, sizeof(pg_region_state) * (size_t)count,
                                         cudaMemcpyHostToDevice, s),

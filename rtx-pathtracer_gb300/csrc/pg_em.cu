@@ -72,6 +72,7 @@ int pg_init_regions(pg_ctx *ctx, uint32_t n_regions, void *stream) {
     if (!ctx) return PG_ERR_ARG;
     if (n_regions > ctx->max_regions) return set_error(ctx, PG_ERR_ARG, "n_regions exceeds context capacity");
     if (n_regions == 0) return PG_OK;
+    guide_mark_stale(ctx);
     // All-zero offsets: every region is empty, so only initialisation runs and
     // no sample is read (the sample pointer is never dereferenced).
     int st = pg_fit_regions(ctx, reinterpret_cast<const float *>(ctx->d_init), ctx->d_zero_offsets, n_regions,
@@ -91,6 +92,7 @@ int fit_range(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t 
               cudaStream_t s) {
     ctx->last_launches = 0;
     if (n_regions == 0) return PG_OK;
+    guide_mark_stale(ctx);
     int st = upload_init_table(ctx, s);
     if (st) return st;
     st = check_cuda(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(uint32_t) * 4, s), "queue reset");

@@ -14,6 +14,7 @@
 struct pg_fit_graph {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    pg_ctx *ctx = nullptr;  // whose states a replay refits
 };
 
 namespace {
@@ -134,6 +135,7 @@ int pg_fit_graph_create(pg_ctx *ctx, const float *dirw, const uint32_t *offsets,
     if (ce != cudaSuccess || !graph) return set_error(ctx, PG_ERR_CUDA, "stream capture of the fit failed");
     pg_fit_graph *g = new pg_fit_graph();
     g->graph = graph;
+    g->ctx = ctx;
     if (cudaGraphInstantiate(&g->exec, graph, 0) != cudaSuccess) {
         cudaGraphDestroy(graph);
         delete g;
@@ -145,6 +147,7 @@ int pg_fit_graph_create(pg_ctx *ctx, const float *dirw, const uint32_t *offsets,
 
 int pg_fit_graph_launch(pg_fit_graph *g, void *stream) {
     if (!g || !g->exec) return PG_ERR_ARG;
+    pg::guide_mark_stale(g->ctx);
     return cudaGraphLaunch(g->exec, (cudaStream_t)stream) == cudaSuccess
                ? PG_OK
                : pg::set_error(nullptr, PG_ERR_CUDA, "graph launch failed");

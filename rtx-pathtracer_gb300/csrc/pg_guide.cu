@@ -672,6 +672,9 @@ int guide_target(pg_ctx *ctx, GuideTarget *out) {
 }
 
 void guide_mark_written(pg_ctx *ctx) { guide(ctx).vmm_fresh = true; }
+void guide_mark_stale(pg_ctx *ctx) {
+    if (ctx && ctx->guide) static_cast<GuideScratch *>(ctx->guide)->vmm_fresh = false;
+}
 
 int guide_view(pg_ctx *ctx, GuideView *out, cudaStream_t s) {
     GuideScratch &g = guide(ctx);

@@ -60,6 +60,9 @@ int fit_range(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t 
 int order_regions(pg_ctx *ctx, const uint32_t *offsets, uint32_t n_regions, uint32_t large_threshold,
                   uint32_t *n_large_out, cudaStream_t s);
 void guide_release(pg_ctx *ctx);
+// The packed guide (VMM_Theta) is repacked from the states before the next
+// guided render: called by every call that changes mixture states.
+void guide_mark_stale(pg_ctx *ctx);
 // split/merge statistics: allocated (zeroed) on first use, zeroed again when
 // regions are initialised
 int extras_ensure(pg_ctx *ctx, cudaStream_t s);

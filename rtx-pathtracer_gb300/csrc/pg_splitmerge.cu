@@ -1017,6 +1017,7 @@ int pg_split_merge(pg_ctx *ctx, const float *dirw, const float *pdf, const uint3
     if (n_regions > ctx->max_regions) return set_error(ctx, PG_ERR_ARG, "n_regions exceeds context capacity");
     if (n_regions == 0) return PG_OK;
     cudaStream_t s = (cudaStream_t)stream;
+    guide_mark_stale(ctx);
     if (int st = extras_ensure(ctx, s)) return st;
     sm::Args A;
     A.states = ctx->d_states;

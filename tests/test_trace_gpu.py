@@ -63,6 +63,9 @@ def make_rays(abi, rng, exp, n):
 SCENES = {
     "cornell": lambda pkg: pkg.Scene.cornell(64, 48, ico_level=5),
     "plates": lambda pkg: pkg.Scene.plates(64, 36, occluder_grid=64, seed=4),
+    # the guided-rendering benchmark's geometry: a 707 x 707 displaced grid,
+    # 999,698 occluder triangles, a deep tree (stack depth, overflow guard)
+    "plates_1m": lambda pkg: pkg.Scene.plates(64, 36, occluder_grid=707, seed=4),
 }
 
 
@@ -79,6 +82,8 @@ def test_closest_hit_bit_exact(name, cuda, pkg, abi, tracer):
     got = host(d_hits, abi.HIT_DTYPE)
     want = tracer.closest(exp, rays)
     assert (want["prim"] != 0xFFFFFFFF).mean() > 0.15  # the plates scene is open: most random rays escape
+    if name == "plates_1m":
+        assert exp["tri_mat"].shape[0] > 999_000
     same = got.view(np.uint32).reshape(-1, 4) == want.view(np.uint32).reshape(-1, 4)
     bad = np.where(~same.all(axis=1))[0]
     assert bad.size == 0, f"{bad.size} hits differ; first {bad[:5]}: gpu {got[bad[:3]]} cpu {want[bad[:3]]}"
