@@ -127,12 +127,25 @@ def make_workload(small: bool, args=None, boxes=None):
     return wl.fit_batched(seed=3)
 
 
+def cpu_fitter(threads: int):
+    """The CPU fit the baselines time: the reference's own lightpmm
+    (oracle/_ref, built from the reference's headers: with its vectorclass on
+    x86-64, with the portable vectorclass stand-in on the Arm host) when it
+    was built, else the bit-exact C port of it (oracle/pg_oracle.c)."""
+    from oracle.oracle import Oracle, ReferenceFit
+    if ReferenceFit.available():
+        ref = ReferenceFit()
+        return "reference", lambda cfg, d, o: ref.fit(cfg, d, o, threads=threads)
+    port = Oracle()
+    return "port", lambda cfg, d, o: port.fit(cfg, d, o, f64=False, threads=threads)
+
+
 def cpu_baseline(w, seconds: float = 12.0, threads: int | None = None):
-    """The reference's CPU fit (bit-exact C restatement of lightpmm, oracle/)
-    on a bounded sample of the workload's regions, over `threads` host threads."""
-    from oracle.oracle import Oracle, abi
-    o = Oracle()
+    """The reference's CPU fit (cpu_fitter) on a bounded sample of the
+    workload's regions, over `threads` host threads (regions in parallel)."""
+    from oracle.oracle import abi
     threads = threads or (os.cpu_count() or 1)
+    kind, fit = cpu_fitter(threads)
     offsets = w["offsets"].astype(np.int64)
     counts = np.diff(offsets)
     cfg = abi.forced_iterations(ITERS, num_initial_components=K)
@@ -140,19 +153,21 @@ def cpu_baseline(w, seconds: float = 12.0, threads: int | None = None):
     n_try = 64
     t0 = time.perf_counter()
     sub = slice(0, n_try)
-    o.fit(cfg, w["dirw"][offsets[0]:offsets[n_try]], (offsets[:n_try + 1] - offsets[0]).astype(np.uint32),
-          f64=False, threads=threads)
+    fit(cfg, w["dirw"][offsets[0]:offsets[n_try]], (offsets[:n_try + 1] - offsets[0]).astype(np.uint32))
     dt = time.perf_counter() - t0
     rate = counts[sub].sum() * ITERS / max(dt, 1e-6)
     target = rate * seconds / ITERS
     n = int(np.searchsorted(np.cumsum(counts), target)) + 1
     n = max(n_try, min(n, len(counts)))
     t0 = time.perf_counter()
-    o.fit(cfg, w["dirw"][:offsets[n]], offsets[:n + 1].astype(np.uint32), f64=False, threads=threads)
+    fit(cfg, w["dirw"][:offsets[n]], offsets[:n + 1].astype(np.uint32))
     dt = time.perf_counter() - t0
     si = counts[:n].sum() * ITERS
-    return {"value": si / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"first {n} of {len(counts)} regions ({int(counts[:n].sum())} samples), {ITERS} iterations",
+    what = ("the reference's lightpmm VMMFactory::fit" if kind == "reference"
+            else "the bit-exact C port of lightpmm")
+    return {"value": si / dt / 1e6, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": f"first {n} of {len(counts)} regions ({int(counts[:n].sum())} samples), {ITERS} iterations, "
+                      f"{what}, regions over {threads} threads",
             "seconds": dt}
 
 
@@ -585,13 +600,20 @@ def bench_config1(pkg, abi, torch, stream, steps: int, cpu: bool):
            "config": {"workload": CONFIG1_WORKLOAD, "l2": "1 M samples (16 MB) stay in L2 and shared memory",
                       "tuning": {f: int(getattr(best, f)) for f, _ in abi.FitTuning._fields_}}}
     if cpu:
-        from oracle.oracle import Oracle
         threads = os.cpu_count() or 1
+        kind, fit = cpu_fitter(threads)
         t0 = time.perf_counter()
-        Oracle().fit(cfg, w["dirw"], w["offsets"], f64=False, threads=threads)
+        fit(cfg, w["dirw"], w["offsets"])
         dt = time.perf_counter() - t0
-        out["cpu_baseline"] = {"value": si / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+        out["cpu_baseline"] = {"value": si / dt / 1e6, "unit": UNIT, "cores": threads, "kind": kind,
                                "sample": "the whole configuration (64 regions, 20 iterations)"}
+        kind1, fit1 = cpu_fitter(1)
+        t0 = time.perf_counter()
+        fit1(cfg, w["dirw"], w["offsets"])
+        dt1 = time.perf_counter() - t0
+        out["cpu_baseline_one_core"] = {"value": si / dt1 / 1e6, "unit": UNIT, "cores": 1, "kind": kind1,
+                                        "sample": "the whole configuration, regions serial as the reference "
+                                                  "fits them (src/PathGuiding.cpp:281-288)"}
     ctx.close()
     return out
 

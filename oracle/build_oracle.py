@@ -3,11 +3,17 @@
 * ``oracle/liboracle.so`` - the plain-C restatement (pg_oracle.c, and the
   tracer restatement pg_oracle_trace.cpp), built on whichever machine runs it.
 * ``oracle/_ref/liblightpmm_ref.so`` - the reference's own vendored lightpmm fit
-  compiled from its sources where they lie (REFERENCE_ROOT), through
-  lightpmm_harness.cpp and a project-written glm stand-in (glm_shim/).  It is
-  built only when the reference tree is present and the host is x86-64 (the
-  vendored vectorclass library has no other SIMD back end); its flags are the
-  reference's own (CMakeLists.txt: C++20, -O4, no -march).
+  compiled through lightpmm_harness.cpp and a project-written glm stand-in
+  (glm_shim/), with the reference's flags (CMakeLists.txt: C++20, -O4, no
+  -march).  Where the reference tree is present its lightpmm and guiding
+  headers are read where they lie, and also staged (copied, not committed:
+  oracle/_ref is git-ignored) into oracle/_ref/src so that a host without the
+  tree - the Arm GPU host - can build the same fit.  On x86-64 with the tree
+  the build uses the vendored vectorclass library (SSE); elsewhere it uses the
+  project-written portable stand-in for that library (vcl_shim/: lane loops,
+  and SSE type stand-ins on hosts without x86 intrinsics), which
+  ``oracle/_ref/liblightpmm_ref_portable.so`` also builds on x86-64 so the two
+  can be compared.
 """
 from __future__ import annotations
 
@@ -59,20 +65,54 @@ def build_oracle(force: bool = False) -> Path:
     return out
 
 
+STAGED = HERE / "_ref" / "src"
+X86 = platform.machine() in ("x86_64", "AMD64")
+
+
+def stage_reference_sources():
+    """Copies the reference's lightpmm and guiding headers into oracle/_ref/src
+    (where the tree is present); returns the staged directory, or None."""
+    pmm = REFERENCE_ROOT / "external" / "lightpmm" / "include" / "pmm"
+    guiding = REFERENCE_ROOT / "external" / "guiding"
+    if pmm.exists() and guiding.exists():
+        for src_dir, name in ((pmm, "pmm"), (guiding, "guiding")):
+            dst = STAGED / name
+            dst.mkdir(parents=True, exist_ok=True)
+            for f in sorted(src_dir.glob("*.h")):
+                t = dst / f.name
+                data = f.read_bytes()
+                if not t.exists() or t.read_bytes() != data:
+                    t.write_bytes(data)
+    return STAGED if (STAGED / "pmm" / "VMMFactory.h").exists() else None
+
+
+def _build_lightpmm(out: Path, include_dirs, force: bool):
+    srcs = [HERE / "lightpmm_harness.cpp", ROOT / "include" / "pathguide.h"]
+    if force or _stale(out, srcs + sorted((HERE / "vcl_shim").rglob("*.h"))):
+        _run(["g++", "-std=c++20", "-O3", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", "-w"] +
+             [f"-I{d}" for d in include_dirs] +
+             [f"-I{ROOT / 'include'}", str(HERE / "lightpmm_harness.cpp"), "-o", str(out)])
+    return out
+
+
 def build_reference(force: bool = False):
-    """Compile the reference's lightpmm fit into oracle/_ref (x86-64 hosts with the tree only)."""
+    """Compile the reference's lightpmm fit into oracle/_ref: from the tree
+    with its vectorclass on x86-64, else from the staged headers with the
+    portable vectorclass stand-in (the Arm host).  None if neither source is
+    there."""
+    staged = stage_reference_sources()
     inc = REFERENCE_ROOT / "external" / "lightpmm" / "include"
-    if not inc.exists() or platform.machine() not in ("x86_64", "AMD64"):
-        return None
     out_dir = HERE / "_ref"
     out_dir.mkdir(exist_ok=True)
-    out = out_dir / "liblightpmm_ref.so"
-    srcs = [HERE / "lightpmm_harness.cpp", ROOT / "include" / "pathguide.h"]
-    if force or _stale(out, srcs):
-        _run(["g++", "-std=c++20", "-O3", "-fPIC", "-shared", "-w",
-              f"-I{HERE / 'glm_shim'}", f"-I{inc}", f"-I{REFERENCE_ROOT / 'external'}",
-              f"-I{ROOT / 'include'}", str(HERE / "lightpmm_harness.cpp"), "-o", str(out)])
-    return out
+    shim = [HERE / "vcl_shim"] + ([] if X86 else [HERE / "vcl_shim" / "noarch"])
+    if inc.exists() and X86:
+        out = _build_lightpmm(out_dir / "liblightpmm_ref.so",
+                              [HERE / "glm_shim", inc, REFERENCE_ROOT / "external"], force)
+        _build_lightpmm(out_dir / "liblightpmm_ref_portable.so", shim + [HERE / "glm_shim", staged], force)
+        return out
+    if staged is not None:
+        return _build_lightpmm(out_dir / "liblightpmm_ref.so", shim + [HERE / "glm_shim", staged], force)
+    return None
 
 
 if __name__ == "__main__":

@@ -18,6 +18,8 @@
 // not vendored): the principal eigenvector of the symmetric covariance in
 // closed form.
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -447,6 +449,51 @@ int lpmm_ref_init(const pg_fit_config *cfg, uint32_t n, pg_region_state *states)
     return 0;
 }
 
+}  // extern "C"
+
+namespace {
+// One region of lpmm_ref_fit: the reference's VMMFactory::initialize / fit /
+// updateFit on the region's samples.
+void fit_region(Factory &factory, std::vector<DData> &data, const pg_fit_config *cfg, int mode, uint32_t r,
+                const float *dirw, const uint32_t *offsets, pg_region_state *states, float *ll_final) {
+    (void)cfg;
+    const uint32_t b = offsets[r], e = offsets[r + 1];
+    data.resize(e - b);
+    for (uint32_t i = b; i < e; ++i) {
+        const float *p = dirw + 4 * size_t(i);
+        data[i - b] = DData(lightpmm::Point3(0.f, 0.f, 0.f), lightpmm::Vector3(p[0], p[1], p[2]), p[3], 1.0f, 1.0f,
+                            r);
+    }
+    PMM pmm{};
+    if (mode == PG_FIT_INIT) {
+        factory.initialize(pmm);
+    } else {
+        state_to_pmm(states[r], pmm);
+    }
+    const uint32_t before = pmm.m_numEMIterations;
+    if (e > b) {
+        if (mode == PG_FIT_UPDATE)
+            factory.updateFit(data.begin(), data.end(), pmm);
+        else
+            factory.fit(data.begin(), data.end(), pmm, false);
+    }
+    pg_region_state &s = states[r];
+    if (mode == PG_FIT_INIT) {
+        std::memset(&s, 0, sizeof(s));
+        for (int c = 0; c < 16; ++c) s.distance[c] = std::numeric_limits<float>::infinity();
+    }
+    pmm_to_state(pmm, s);
+    s.iters_last = pmm.m_numEMIterations - before;
+    if (ll_final) {
+        float ll = 0.0f;
+        if (e > b) factory.computeSufficentStatsFromSamples(data.begin(), data.end(), pmm, nullptr, &ll);
+        ll_final[r] = ll;
+    }
+}
+}  // namespace
+
+extern "C" {
+
 // Fits each region with the reference's VMMFactory.  `dirw` holds float4
 // {dir.xyz, weight} per sample grouped by region (offsets[n_regions+1]).
 // mode: PG_FIT_INIT / PG_FIT_CONTINUE / PG_FIT_UPDATE.  ll_final[r] receives
@@ -456,40 +503,27 @@ int lpmm_ref_fit(const pg_fit_config *cfg, int mode, uint32_t n_regions, const f
                  const uint32_t *offsets, pg_region_state *states, float *ll_final) {
     Factory factory(props_from(cfg));
     std::vector<DData> data;
-    for (uint32_t r = 0; r < n_regions; ++r) {
-        const uint32_t b = offsets[r], e = offsets[r + 1];
-        data.resize(e - b);
-        for (uint32_t i = b; i < e; ++i) {
-            const float *p = dirw + 4 * size_t(i);
-            data[i - b] = DData(lightpmm::Point3(0.f, 0.f, 0.f), lightpmm::Vector3(p[0], p[1], p[2]),
-                                p[3], 1.0f, 1.0f, r);
-        }
-        PMM pmm{};
-        if (mode == PG_FIT_INIT) {
-            factory.initialize(pmm);
-        } else {
-            state_to_pmm(states[r], pmm);
-        }
-        const uint32_t before = pmm.m_numEMIterations;
-        if (e > b) {
-            if (mode == PG_FIT_UPDATE)
-                factory.updateFit(data.begin(), data.end(), pmm);
-            else
-                factory.fit(data.begin(), data.end(), pmm, false);
-        }
-        pg_region_state &s = states[r];
-        if (mode == PG_FIT_INIT) {
-            std::memset(&s, 0, sizeof(s));
-            for (int c = 0; c < 16; ++c) s.distance[c] = std::numeric_limits<float>::infinity();
-        }
-        pmm_to_state(pmm, s);
-        s.iters_last = pmm.m_numEMIterations - before;
-        if (ll_final) {
-            float ll = 0.0f;
-            if (e > b) factory.computeSufficentStatsFromSamples(data.begin(), data.end(), pmm, nullptr, &ll);
-            ll_final[r] = ll;
-        }
-    }
+    for (uint32_t r = 0; r < n_regions; ++r) fit_region(factory, data, cfg, mode, r, dirw, offsets, states, ll_final);
+    return 0;
+}
+
+// lpmm_ref_fit with the regions spread over n_threads host threads (each with
+// its own factory), taking the next region from a shared counter - the
+// reference's per-region fit run region-parallel, as a multi-core host would.
+int lpmm_ref_fit_threads(const pg_fit_config *cfg, int mode, uint32_t n_regions, const float *dirw,
+                         const uint32_t *offsets, pg_region_state *states, float *ll_final, int n_threads) {
+    std::atomic<uint32_t> next{0};
+    auto body = [&] {
+        Factory factory(props_from(cfg));
+        std::vector<DData> data;
+        for (uint32_t r = next.fetch_add(1); r < n_regions; r = next.fetch_add(1))
+            fit_region(factory, data, cfg, mode, r, dirw, offsets, states, ll_final);
+    };
+    const int T = std::max(1, n_threads);
+    std::vector<std::thread> pool;
+    for (int t = 1; t < T; ++t) pool.emplace_back(body);
+    body();
+    for (auto &th : pool) th.join();
     return 0;
 }
 

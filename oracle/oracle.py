@@ -197,19 +197,23 @@ class Oracle:
 
 
 class ReferenceFit:
-    """The reference's own lightpmm fit compiled in place (oracle/_ref)."""
+    """The reference's own lightpmm fit (oracle/_ref/liblightpmm_ref.so, built by
+    oracle/build_oracle.py: on x86-64 from the tree with the vendored
+    vectorclass, elsewhere from the staged headers with the portable
+    vectorclass stand-in)."""
 
     PATH = HERE / "_ref" / "liblightpmm_ref.so"
 
     @classmethod
-    def available(cls) -> bool:
-        return cls.PATH.exists()
+    def available(cls, path: Path | None = None) -> bool:
+        return (path or cls.PATH).exists()
 
-    def __init__(self):
-        self.lib = C.CDLL(str(self.PATH))
+    def __init__(self, path: Path | None = None):
+        self.lib = C.CDLL(str(path or self.PATH))
         L = self.lib
         L.lpmm_ref_init.argtypes = [C.POINTER(abi.FitConfig), _U32, _P]
         L.lpmm_ref_fit.argtypes = [C.POINTER(abi.FitConfig), _I, _U32, _P, _P, _P, _P]
+        L.lpmm_ref_fit_threads.argtypes = [C.POINTER(abi.FitConfig), _I, _U32, _P, _P, _P, _P, _I]
         L.lpmm_ref_update_distances.argtypes = [_U32, _P, _P, _P, _P]
         L.lpmm_ref_reposition.argtypes = [_P, _P]
         L.lpmm_ref_fastexp.argtypes = [_P, _P, _U32]
@@ -223,14 +227,20 @@ class ReferenceFit:
         self.lib.lpmm_ref_init(C.byref(cfg), n, abi.ptr(s))
         return s
 
-    def fit(self, cfg, dirw, offsets, states=None, mode=abi.PG_FIT_INIT):
+    def fit(self, cfg, dirw, offsets, states=None, mode=abi.PG_FIT_INIT, threads: int = 1):
+        """Regions serial as the reference fits them (threads 1), or spread
+        over host threads."""
         dirw = _f32(dirw)
         offsets = np.ascontiguousarray(offsets, dtype=np.uint32)
         R = offsets.shape[0] - 1
         st = np.zeros(R, dtype=abi.STATE_DTYPE) if states is None else states.copy()
         ll = np.zeros(R, dtype=np.float32)
-        self.lib.lpmm_ref_fit(C.byref(cfg), mode, R, abi.ptr(dirw), abi.ptr(offsets), abi.ptr(st),
-                              abi.ptr(ll))
+        if threads > 1:
+            self.lib.lpmm_ref_fit_threads(C.byref(cfg), mode, R, abi.ptr(dirw), abi.ptr(offsets), abi.ptr(st),
+                                          abi.ptr(ll), threads)
+        else:
+            self.lib.lpmm_ref_fit(C.byref(cfg), mode, R, abi.ptr(dirw), abi.ptr(offsets), abi.ptr(st),
+                                  abi.ptr(ll))
         return st, ll
 
     def postfit(self, cfg, sm, dirw, pdf, dist, offsets, states, extras):
