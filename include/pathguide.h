@@ -387,7 +387,11 @@ int pg_prefit_parallax(pg_ctx *ctx, const pg_directional_data *sorted, const uin
 /* Harmonic-mean lobe distances over one pass of samples (the statistic of
  * external/guiding/incrementaldistance.h:57-107, PathGuiding::postFit,
  * src/PathGuiding.cpp:445-448).  Regions without samples are left unchanged,
- * as PathGuiding::update runs postFit only for non-empty regions. */
+ * as PathGuiding::update runs postFit only for non-empty regions.  The pass
+ * takes up to the context's max_samples, or as many samples as the largest
+ * record set sorted by the context (pg_sort_samples, pg_update); more than
+ * that leave every distance unchanged and report a bounds error through
+ * pg_sync_status. */
 int pg_update_distances(pg_ctx *ctx, const float *dirw, const float *dist, const uint32_t *offsets,
                         uint32_t n_regions, void *stream);
 

@@ -287,67 +287,110 @@ __global__ void parallax_means_kernel(pg_region_state *states, const float *aabb
 
 // Harmonic-mean distance per lobe, weighted by w * gamma_k * pdf_k over the
 // samples with distance > 0 (the statistic of incrementaldistance.h:57-107),
-// merged with the previous estimate.  One CTA per region; per-thread FP32
-// partial sums, warp shuffles, Neumaier merge across warps.
-template <int NT>
-__global__ void __launch_bounds__(NT) distance_kernel(pg_region_state *states, const float4 *dirw,
-                                                      const float *dist, const uint32_t *offsets,
-                                                      uint32_t n_regions) {
-    constexpr int NW = NT / 32;
-    __shared__ float c_ax[16], c_ay[16], c_az[16], c_c0[16], c_cm[16], c_lk[16];
+// merged with the previous estimate.  The samples are cut into work items of
+// at most kDistChunk samples of one region, so a large region is spread over
+// many CTAs: distance_items_kernel numbers the items (region-major),
+// distance_partial_kernel sums each item's 32 statistics, and
+// distance_finalize_kernel adds a region's items in item order (Neumaier) and
+// updates the lobes - deterministic whatever the launch shape.
+constexpr uint32_t kDistChunk = 2048;
+constexpr int kDistThreads = 256;
+
+// item_offsets[r] = first work item of region r (empty regions have none);
+// item_offsets[n_regions] = the item count.  One CTA.
+__global__ void __launch_bounds__(kScanThreads) distance_items_kernel(const uint32_t *offsets, uint32_t n_regions,
+                                                                      uint32_t *item_offsets) {
+    __shared__ uint32_t carry, tot;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < n_regions; base += kScanThreads) {
+        const uint32_t r = base + threadIdx.x;
+        const uint32_t n = r < n_regions ? offsets[r + 1] - offsets[r] : 0u;
+        const uint32_t e = block_exclusive_scan((n + kDistChunk - 1) / kDistChunk, &tot);
+        if (r < n_regions) item_offsets[r] = carry + e;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) item_offsets[n_regions] = carry;
+}
+
+// Per work item: the sums over its samples of a_k = w gamma_k pdf_k and
+// a_k / t.  With e_k = pi_k pdf_k (one ex2 per lobe; the exponent
+// kl (mu.d - 1) + log2(norm) is clamped at log2(norm), cos <= 1) and
+// p = sum_k e_k: a_k = (w / p) e_k^2 / pi_k.  partial[item] = {sum a[16],
+// sum a / t[16]}.  More items than the scratch holds: nothing is written and
+// PG_DEV_ERR_BOUNDS is reported.
+__global__ void __launch_bounds__(kDistThreads) distance_partial_kernel(const pg_region_state *states,
+                                                                        const float4 *dirw, const float *dist,
+                                                                        const uint32_t *offsets, uint32_t n_regions,
+                                                                        const uint32_t *item_offsets, float *partial,
+                                                                        uint64_t cap_items, uint32_t *error_word) {
+    constexpr int NW = kDistThreads / 32;
+    __shared__ float c_ax[16], c_ay[16], c_az[16], c_c0[16], c_cm[16], c_lk[16], c_ipi[16];
     __shared__ float red[NW][32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (uint32_t r = blockIdx.x; r < n_regions; r += gridDim.x) {
-        // regions without samples are not updated (postFit runs only for
-        // non-empty regions, src/PathGuiding.cpp:281-288): an empty batch
-        // would turn the initial infinite distance into 0/0
-        if (offsets[r + 1] == offsets[r]) continue;
-        pg_region_state *s = states + r;
-        const uint32_t K = min(s->k, 16u);
+    const uint32_t n_items = item_offsets[n_regions];
+    if (n_items > cap_items) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(error_word, PG_DEV_ERR_BOUNDS);
+        return;
+    }
+    for (uint32_t item = blockIdx.x; item < n_items; item += gridDim.x) {
+        // the region of this item: the last r with item_offsets[r] <= item
+        uint32_t lo = 0, hi = n_regions - 1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) / 2;
+            if (item_offsets[mid] <= item)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const uint32_t r = lo;
+        const pg_region_state *s = states + r;
         if (tid < 16) {
             const int c = tid;
-            // log2 of pdf_k = kl (mu.d - 1) + log2(norm); log2 of pi_k pdf_k adds log2(pi)
+            const uint32_t K = min(s->k, 16u);
+            const bool on = c < (int)K && s->norm[c] > 0.0f && s->weight[c] > 0.0f;
             const float kl = s->kappa[c] * kLog2e;
-            const float ln = (c < (int)K && s->norm[c] > 0.0f) ? log2f(s->norm[c]) : -INFINITY;
-            const float lw = (c < (int)K && s->weight[c] > 0.0f) ? log2f(s->weight[c]) : -INFINITY;
+            const float ln = on ? log2f(s->norm[c]) : -INFINITY;
             c_ax[c] = kl * s->mu_x[c];
             c_ay[c] = kl * s->mu_y[c];
             c_az[c] = kl * s->mu_z[c];
-            c_c0[c] = ln - kl;  // log2 pdf_k before the clamp
-            c_cm[c] = ln;       // clamp: cos <= 1
-            c_lk[c] = lw;
+            c_c0[c] = ln - kl;
+            c_cm[c] = ln;
+            c_lk[c] = on ? log2f(s->weight[c]) : -INFINITY;
+            c_ipi[c] = on ? 1.0f / s->weight[c] : 0.0f;
         }
         __syncthreads();
         float bw[16], bwd[16];
 #pragma unroll
         for (int c = 0; c < 16; ++c) bw[c] = bwd[c] = 0.0f;
-        const uint32_t b = offsets[r], e = offsets[r + 1];
-        for (uint32_t i = b + tid; i < e; i += NT) {
+        const uint32_t b = offsets[r] + (item - item_offsets[r]) * kDistChunk;
+        const uint32_t e = min(offsets[r + 1], b + kDistChunk);
+        for (uint32_t i = b + tid; i < e; i += kDistThreads) {
             const float t = dist[i];
             if (!(t > 0.0f)) continue;
             const float4 d = dirw[i];
-            float lp[16];
+            float ek[16];
             float p = 0.0f;
 #pragma unroll
             for (int c = 0; c < 16; ++c) {
                 float a = fmaf(c_az[c], d.z, c_c0[c]);
                 a = fmaf(c_ay[c], d.y, a);
                 a = fmaf(c_ax[c], d.x, a);
-                lp[c] = fminf(a, c_cm[c]);
-                p += exp2f(lp[c] + c_lk[c]);
+                ek[c] = ex2_approx(fminf(a, c_cm[c]) + c_lk[c]);
+                p += ek[c];
             }
             if (!(p > kPmmEps)) continue;
             const float sc = d.w / p;
             const float it = 1.0f / t;
 #pragma unroll
             for (int c = 0; c < 16; ++c) {
-                // w * gamma_k * pdf_k = w/p * pi_k pdf_k * pdf_k
-                const float a = exp2f(2.0f * lp[c] + c_lk[c]) * sc;
+                const float a = ek[c] * ek[c] * c_ipi[c] * sc;
                 bw[c] += a;
                 bwd[c] += a * it;
             }
         }
-        // reduce: lanes hold 32 values (bw[16], bwd[16]); warp sums then Neumaier over warps
 #pragma unroll
         for (int c = 0; c < 16; ++c) {
             float x = bw[c], y = bwd[c];
@@ -361,21 +404,39 @@ __global__ void __launch_bounds__(NT) distance_kernel(pg_region_state *states, c
             }
         }
         __syncthreads();
-        // every lane of the active 4-lane groups, as the reference's SIMD update does
-        if (tid < 16 && tid < (int)((K + 3u) & ~3u)) {
-            const int c = tid;
-            float wh = 0.f, wl = 0.f, dh = 0.f, dl = 0.f;
-            for (int w = 0; w < NW; ++w) {
-                neumaier_add(wh, wl, red[w][c]);
-                neumaier_add(dh, dl, red[w][16 + c]);
-            }
-            const float batch_w = wh + wl, batch_wd = dh + dl;
-            const float old_w = s->dist_sum_w[c];
-            const float new_w = old_w + batch_w;
-            s->distance[c] = new_w / (old_w / s->distance[c] + batch_wd);
-            s->dist_sum_w[c] = new_w;
+        if (tid < 32) {
+            float h = 0.f, l = 0.f;
+            for (int w = 0; w < NW; ++w) neumaier_add(h, l, red[w][tid]);
+            partial[(size_t)item * 32 + tid] = h + l;
         }
         __syncthreads();
+    }
+}
+
+// One warp per region: the items' sums added in item order, then the
+// harmonic-mean update of every lane of the active 4-lane groups, as the
+// reference's SIMD update does.  Regions without samples are not updated
+// (postFit runs only for non-empty regions, src/PathGuiding.cpp:281-288): an
+// empty batch would turn the initial infinite distance into 0/0.
+__global__ void distance_finalize_kernel(pg_region_state *states, const uint32_t *item_offsets, uint32_t n_regions,
+                                         const float *partial, uint64_t cap_items) {
+    const uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (r >= n_regions || item_offsets[n_regions] > cap_items) return;
+    const uint32_t i0 = item_offsets[r], i1 = item_offsets[r + 1];
+    if (i0 == i1) return;
+    float h = 0.f, l = 0.f;
+    for (uint32_t it = i0; it < i1; ++it) neumaier_add(h, l, partial[(size_t)it * 32 + lane]);
+    const float sum = h + l;
+    const float wd = __shfl_down_sync(0xffffffffu, sum, 16);  // lane c: the sum of a_c / t
+    pg_region_state *s = states + r;
+    const uint32_t K = min(s->k, 16u);
+    if (lane < 16 && lane < (int)((K + 3u) & ~3u)) {
+        const int c = lane;
+        const float old_w = s->dist_sum_w[c];
+        const float new_w = old_w + sum;
+        s->distance[c] = new_w / (old_w / s->distance[c] + wd);
+        s->dist_sum_w[c] = new_w;
     }
 }
 
@@ -556,6 +617,11 @@ struct GuideScratch {
     bool tree_split = false;       // a region was split: the renderer descends the node array
     uint32_t *split_out = nullptr; // device: new region and node counts
     pg_region_split_config rs{};
+    // distance pass: work-item offsets per region and the items' partial sums
+    uint32_t *dist_items = nullptr;
+    float *dist_partial = nullptr;
+    uint32_t cap_dist_regions = 0;
+    uint64_t cap_dist_items = 0;
 };
 
 static GuideScratch &guide(pg_ctx *ctx) {
@@ -583,6 +649,8 @@ void guide_release(pg_ctx *ctx) {
     cudaFree(g.nodes);
     cudaFree(g.leaf_of);
     cudaFree(g.split_out);
+    cudaFree(g.dist_items);
+    cudaFree(g.dist_partial);
     delete static_cast<GuideScratch *>(ctx->guide);
     ctx->guide = nullptr;
 }
@@ -625,6 +693,41 @@ static void exclusive_scan(uint32_t *v, uint32_t n, uint32_t *sums, cudaStream_t
     scan_chunk_sums<<<chunks, kScanThreads, 0, s>>>(v, n, sums);
     scan_sums_single<<<1, kScanThreads, 0, s>>>(sums, chunks);
     scan_chunks_apply<<<chunks, kScanThreads, 0, s>>>(v, n, sums);
+}
+
+// The distance pass: the work items, their partial sums, the per-region
+// update.  The scratch holds the items of as many samples as the larger of the
+// context's max_samples and the largest record set sorted so far; more
+// samples than that are reported as PG_DEV_ERR_BOUNDS and leave the distances
+// untouched.
+static int update_distances(pg_ctx *ctx, const float4 *dirw, const float *dist, const uint32_t *offsets,
+                            uint32_t n_regions, cudaStream_t s) {
+    GuideScratch &g = guide(ctx);
+    const uint64_t max_samples = std::max<uint64_t>(ctx->max_samples, g.cap_n);
+    const uint64_t items = max_samples / kDistChunk + n_regions + 1;
+    if (n_regions + 1 > g.cap_dist_regions) {
+        cudaFree(g.dist_items);
+        g.dist_items = nullptr;
+        if (int st = check_cuda(ctx, cudaMalloc(&g.dist_items, sizeof(uint32_t) * (n_regions + 1)), "distance items"))
+            return st;
+        g.cap_dist_regions = n_regions + 1;
+    }
+    if (items > g.cap_dist_items) {
+        cudaFree(g.dist_partial);
+        g.dist_partial = nullptr;
+        g.cap_dist_items = 0;
+        if (int st = check_cuda(ctx, cudaMalloc(&g.dist_partial, sizeof(float) * 32 * items), "distance sums"))
+            return st;
+        g.cap_dist_items = items;
+    }
+    distance_items_kernel<<<1, kScanThreads, 0, s>>>(offsets, n_regions, g.dist_items);
+    const uint32_t grid = (uint32_t)std::min<uint64_t>(items, (uint64_t)ctx->sm_count * 8u);
+    distance_partial_kernel<<<grid, kDistThreads, 0, s>>>(ctx->d_states, dirw, dist, offsets, n_regions,
+                                                          g.dist_items, g.dist_partial, g.cap_dist_items,
+                                                          ctx->d_counters + 2);
+    distance_finalize_kernel<<<(n_regions + 7) / 8, 256, 0, s>>>(ctx->d_states, g.dist_items, n_regions,
+                                                                  g.dist_partial, g.cap_dist_items);
+    return check_cuda(ctx, cudaGetLastError(), "distance launch");
 }
 
 // Sorts the (region id, index) pairs of n records; leaves the sorted indices in
@@ -814,10 +917,8 @@ int pg_update_distances(pg_ctx *ctx, const float *dirw, const float *dist, const
     if (!ctx || !dirw || !dist || !offsets) return PG_ERR_ARG;
     if (n_regions > ctx->max_regions) return set_error(ctx, PG_ERR_ARG, "n_regions exceeds context capacity");
     if (n_regions == 0) return PG_OK;
-    cudaStream_t s = (cudaStream_t)stream;
-    distance_kernel<256><<<std::min<uint32_t>(n_regions, (uint32_t)ctx->sm_count * 8u), 256, 0, s>>>(
-        ctx->d_states, reinterpret_cast<const float4 *>(dirw), dist, offsets, n_regions);
-    return check_cuda(ctx, cudaGetLastError(), "distance launch");
+    return update_distances(ctx, reinterpret_cast<const float4 *>(dirw), dist, offsets, n_regions,
+                            (cudaStream_t)stream);
 }
 
 int pg_pack_vmm_theta(pg_ctx *ctx, uint32_t n_regions, pg_vmm_theta *out, void *stream) {

@@ -102,7 +102,7 @@ def relmse(img: np.ndarray, ref: np.ndarray, eps: float = 1e-2) -> float:
 def guided_sequence(scene: Scene, guiding: PathGuiding, collector: SampleCollector, image, train_spp=(1, 2, 4, 8, 16, 32),
                     final_spp: int = 64, max_depth: int = 10, seed: int = 1, guiding_prob: float = 0.5,
                     accumulate_training: bool = True, surrogate=None, judge_min_records: int = 32,
-                    stream=None) -> dict:
+                    stream=None, render_flags: int = 0) -> dict:
     """Training passes (render with recording, then PathGuiding::update; the
     first pass is unguided), then a guided render of final_spp samples.  The
     image (cleared first) receives radiance sums: of every pass when
@@ -112,7 +112,9 @@ def guided_sequence(scene: Scene, guiding: PathGuiding, collector: SampleCollect
     network online (one epoch each), and before the final render the network
     is judged against the fit region by region on the last pass's records
     (pg_mlp_judge_guide).  Returns CUDA-event times in ms and the number of
-    samples per pixel summed."""
+    samples per pixel summed.  render_flags go to every render
+    (PG_RENDER_GUIDE_ALMOST_DISCRETE: the reference's rule of guiding every
+    non-discrete material)."""
     torch = _torch()
     s = stream or torch.cuda.current_stream()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
@@ -127,7 +129,8 @@ def guided_sequence(scene: Scene, guiding: PathGuiding, collector: SampleCollect
         ev[0].record(s)
         for i, spp in enumerate(train_spp):
             p = abi.render_params(spp=spp, max_depth=max_depth, seed=seed + 1000 * (i + 1),
-                                  use_guiding=1 if i > 0 else 0, guiding_prob=guiding_prob, record_samples=1)
+                                  use_guiding=1 if i > 0 else 0, guiding_prob=guiding_prob, record_samples=1,
+                                  flags=render_flags)
             scene.render(p, scratch, guide=guiding.ctx, records_dev=collector.buffer, stream=s, stats=False)
             guiding.update(collector, stream=s)
             if surrogate is not None:
@@ -138,7 +141,7 @@ def guided_sequence(scene: Scene, guiding: PathGuiding, collector: SampleCollect
             switched = surrogate.judge_guide(guiding.ctx, srt, n_valid, min_records=judge_min_records, stream=s)
         ev[1].record(s)
         p = abi.render_params(spp=final_spp, max_depth=max_depth, seed=seed, use_guiding=1,
-                              guiding_prob=guiding_prob)
+                              guiding_prob=guiding_prob, flags=render_flags)
         scene.render(p, image, guide=guiding.ctx, stream=s, stats=False)
         ev[2].record(s)
     torch.cuda.synchronize()
