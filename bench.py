@@ -375,6 +375,52 @@ GUIDED_CORNELL_WORKLOAD = ("guided PT on the Cornell box of the tracer workload 
                            "(12 splits), 8-component parallax-aware mixtures")
 
 
+def first_hit_classes(pkg, abi, torch, sc):
+    """Per pixel, what the pixel-centre camera ray hits first: a GGX plate
+    (by roughness), another surface (by material index), a light, or nothing."""
+    info = sc.info()
+    cam = info.camera
+    W, H = cam.width, cam.height
+    o, t, up = (np.array(x, dtype=np.float64) for x in (cam.origin, cam.target, cam.up))
+    f = (t - o) / np.linalg.norm(t - o)
+    r = np.cross(f, up)
+    r /= np.linalg.norm(r)
+    u = np.cross(r, f)
+    th = np.tan(np.radians(cam.vfov_deg) / 2)
+    px, py = np.meshgrid(np.arange(W) + 0.5, np.arange(H) + 0.5)
+    d = f[None, None] + ((2 * px / W - 1) * th * W / H)[..., None] * r + ((1 - 2 * py / H) * th)[..., None] * u
+    d /= np.linalg.norm(d, axis=2, keepdims=True)
+    rays = np.zeros(W * H, abi.RAY_DTYPE)
+    rays["org"], rays["dir"], rays["tmin"], rays["tmax"] = o, d.reshape(-1, 3), 1e-4, 1e30
+    d_rays = torch.from_numpy(rays.view(np.uint8).copy()).cuda()
+    d_hits = torch.zeros(W * H * abi.HIT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    sc.trace_closest(d_rays, W * H, d_hits)
+    torch.cuda.synchronize()
+    prim = np.frombuffer(d_hits.cpu().numpy().tobytes(), abi.HIT_DTYPE)["prim"]
+    exp = sc.export()
+    mats = exp["mats"]
+    cls = np.full(W * H, "miss", dtype=object)
+    sphere = (prim != abi.NO_HIT) & ((prim & abi.SPHERE_BIT) != 0)
+    tri = (prim != abi.NO_HIT) & ~sphere
+    cls[sphere] = "light"
+    names = []
+    for m in exp["tri_mat"][prim[tri]]:
+        mm = mats[m]
+        names.append(f"ggx_{mm['roughness']:.3f}" if mm["type"] == abi.PG_MAT_GGX else
+                     ("light" if mm["type"] == abi.PG_MAT_LIGHT else f"material_{int(m)}"))
+    cls[tri] = names
+    return cls.reshape(H, W)
+
+
+def relmse_by_class(img, ref, cls, eps=1e-2):
+    """Each first-hit class's share of the relMSE (sums to the image's relMSE)."""
+    e = (img - ref) ** 2 / (ref * ref + eps)
+    out = {"all": float(e.mean())}
+    for c in sorted(set(cls.ravel().tolist())):
+        out[c] = float(e[cls == c].sum() / e.size)
+    return out
+
+
 def bench_guided(pkg, abi, torch, stream, ref_spp: int = 4096, scene: str = "plates"):
     """Equal-time relMSE of guided and plain NEE+MIS path tracing against a
     high-spp plain render (relMSE = mean (x - r)^2 / (r^2 + 1e-2))."""
@@ -460,6 +506,11 @@ def bench_guided(pkg, abi, torch, stream, ref_spp: int = 4096, scene: str = "pla
                             "plain_ms": p64_ms}}
     out["value"] = out["guided"]["relmse"] / out["plain_equal_time"]["relmse"]
     out["value_meaning"] = "guided relMSE / plain relMSE at equal time (< 1: guiding wins)"
+    cls = first_hit_classes(pkg, abi, torch, sc)
+    out["relmse_by_first_hit"] = {
+        "pixels": {c: int((cls == c).sum()) for c in sorted(set(cls.ravel().tolist()))},
+        "guided": relmse_by_class(guided, ref, cls), "plain_equal_time": relmse_by_class(peq, ref, cls),
+        "guided_64spp": relmse_by_class(g64, ref, cls), "plain_64spp": relmse_by_class(p64, ref, cls)}
     if sur is not None:
         out["surrogate_beside_fit"] = sur
         out["region_splitting"] = region_splits
