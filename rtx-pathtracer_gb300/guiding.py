@@ -124,6 +124,7 @@ def guided_sequence(scene: Scene, guiding: PathGuiding, collector: SampleCollect
         srt = torch.empty(collector.n_slots * RECORD_BYTES, dtype=torch.uint8, device="cuda")
         offs = torch.empty(R + 1, dtype=torch.int32, device="cuda")
     switched = None
+    trained = []
     with torch.cuda.stream(s):
         image.zero_()
         ev[0].record(s)
@@ -136,6 +137,7 @@ def guided_sequence(scene: Scene, guiding: PathGuiding, collector: SampleCollect
             if surrogate is not None:
                 guiding.ctx.sort_samples(collector.buffer, collector.n_slots, R, srt, offs, stream=s)
                 n_valid = int(offs[R].item())
+                trained.append(n_valid)
                 surrogate.train(srt, n_valid, stream=s, want_loss=False)
         if surrogate is not None:
             switched = surrogate.judge_guide(guiding.ctx, srt, n_valid, min_records=judge_min_records, stream=s)
@@ -150,4 +152,5 @@ def guided_sequence(scene: Scene, guiding: PathGuiding, collector: SampleCollect
            "total_ms": ev[0].elapsed_time(ev[2]), "spp": total}
     if switched is not None:
         out["regions_switched"] = switched
+        out["records_trained_per_pass"] = trained
     return out
