@@ -908,7 +908,7 @@ def main():
     ap.add_argument("--sigma", type=float, default=-1.0, help="override the region-size sigma")
     ap.add_argument("--sweep", action="store_true", help="time the tuning grid and print one line per point")
     ap.add_argument("--workload", default="all",
-                    choices=["all", "em", "tracer", "guided", "surrogate", "splitmerge"],
+                    choices=["all", "em", "tracer", "guided", "surrogate", "splitmerge", "update"],
                     help="all: the EM line with the tracer, guided and surrogate blocks; or one of them alone")
     ap.add_argument("--sm-cluster-threshold", type=int, default=0,
                     help="split/merge: regions above this many samples use a cluster (0: library default)")
@@ -959,6 +959,16 @@ def main():
             print(json.dumps(line), flush=True)
         return
     w = make_workload(args.small, args, boxes=None if args.small else region_boxes(pkg, abi))
+    if args.workload == "update":
+        stream = torch.cuda.Stream()
+        sampler = ClockSampler(local)
+        with sampler:
+            line = bench_update_step(pkg, abi, torch, stream, w, args.steps, args.warmup, None)
+        line.update(n_gpus=world, scaling="weak", vs_baseline=None, data="synthetic (seeded vMF mixtures)",
+                    clocks=sampler.summary())
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        return
     if args.workload == "splitmerge":
         stream = torch.cuda.Stream()
         sampler = ClockSampler(local)

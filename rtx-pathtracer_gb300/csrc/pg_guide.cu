@@ -294,7 +294,7 @@ __global__ void parallax_means_kernel(pg_region_state *states, const float *aabb
 // distance_finalize_kernel adds a region's items in item order (Neumaier) and
 // updates the lobes - deterministic whatever the launch shape.
 constexpr uint32_t kDistChunk = 2048;
-constexpr int kDistThreads = 256;
+constexpr int kDistThreads = 64;
 
 // item_offsets[r] = first work item of region r (empty regions have none);
 // item_offsets[n_regions] = the item count.  One CTA.
@@ -721,7 +721,14 @@ static int update_distances(pg_ctx *ctx, const float4 *dirw, const float *dist, 
         g.cap_dist_items = items;
     }
     distance_items_kernel<<<1, kScanThreads, 0, s>>>(offsets, n_regions, g.dist_items);
-    const uint32_t grid = (uint32_t)std::min<uint64_t>(items, (uint64_t)ctx->sm_count * 8u);
+    // persistent: as many CTAs as are resident (each thread sums 32 samples of
+    // an item; several items in flight per SM hide the per-item latency)
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, distance_partial_kernel, kDistThreads, 0) !=
+            cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    const uint32_t grid = (uint32_t)std::min<uint64_t>(items, (uint64_t)ctx->sm_count * (uint64_t)per_sm);
     distance_partial_kernel<<<grid, kDistThreads, 0, s>>>(ctx->d_states, dirw, dist, offsets, n_regions,
                                                           g.dist_items, g.dist_partial, g.cap_dist_items,
                                                           ctx->d_counters + 2);
