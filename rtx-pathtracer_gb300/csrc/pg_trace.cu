@@ -635,7 +635,7 @@ __global__ void __launch_bounds__(128, 8) k_extend(DevRender R) {
     const uint32_t n = R.counters[0];
     const int lane = threadIdx.x & 31;
     TravState st;
-    int stack[kStackSize];
+    int deep[kDeepStack];
     WorkCount wc;
     NoCount nc;
     uint32_t p = 0;
@@ -663,7 +663,7 @@ __global__ void __launch_bounds__(128, 8) k_extend(DevRender R) {
         }
         if (!__any_sync(0xffffffffu, have)) break;
         if (have) {
-            const bool done = kCount ? trav_step<false>(R.S, st, stack, wc) : trav_step<false>(R.S, st, stack, nc);
+            const bool done = kCount ? trav_step<false>(R.S, st, deep, wc) : trav_step<false>(R.S, st, deep, nc);
             if (done) {
                 pg_hit h;
                 h.t = st.tmax;
@@ -952,7 +952,7 @@ __global__ void __launch_bounds__(128, 8) k_shadow(DevRender R) {
     const uint32_t n = R.counters[2];
     const int lane = threadIdx.x & 31;
     TravState st;
-    int stack[kStackSize];
+    int deep[kDeepStack];
     WorkCount wc;
     NoCount nc;
     uint32_t i = 0;
@@ -980,7 +980,7 @@ __global__ void __launch_bounds__(128, 8) k_shadow(DevRender R) {
         }
         if (!__any_sync(0xffffffffu, have)) break;
         if (have) {
-            const bool done = kCount ? trav_step<true>(R.S, st, stack, wc) : trav_step<true>(R.S, st, stack, nc);
+            const bool done = kCount ? trav_step<true>(R.S, st, deep, wc) : trav_step<true>(R.S, st, deep, nc);
             if (done) {
                 if (st.best_id == PG_NO_HIT) shadow_finish(R, i);
                 have = false;

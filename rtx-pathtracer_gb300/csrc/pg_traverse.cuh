@@ -218,6 +218,13 @@ __device__ __forceinline__ bool sphere_intersect(const RayPre &r, const pg_spher
 // most three pushes per four-wide level); a full stack drops the push, which
 // the CPU twin does identically.
 constexpr int kStackSize = 128;
+// The short stack: the top kRegStack entries live in registers as a shift
+// register (a push shifts them down, a pop up); only deeper entries go to the
+// local-memory part of kStackSize - kRegStack.  The logical stack - order of
+// entries and the dropped push when full - is that of one array of
+// kStackSize, so the traversal order, and the CPU twin, do not change.
+constexpr int kRegStack = 4;
+constexpr int kDeepStack = kStackSize - kRegStack;
 
 // Work counters of one traversal: NoCount compiles to nothing; WorkCount
 // tallies the BVH nodes fetched and the triangles tested.
@@ -240,8 +247,28 @@ struct TravState {
     float tmin, tmax;  // tmax: best t so far for closest-hit queries
     float best_u, best_v;
     uint32_t best_id;
-    int node, sp;
+    int node, sp;          // sp: entries on the stack
+    int top[kRegStack];    // the stack's top entries, top[0] uppermost
 };
+
+// Push onto the short stack (deep: the local-memory part, kDeepStack entries).
+__device__ __forceinline__ void stack_push(TravState &st, int *deep, int x) {
+    if (st.sp >= kStackSize) return;
+    if (st.sp >= kRegStack) deep[st.sp - kRegStack] = st.top[kRegStack - 1];
+#pragma unroll
+    for (int i = kRegStack - 1; i > 0; --i) st.top[i] = st.top[i - 1];
+    st.top[0] = x;
+    ++st.sp;
+}
+// Pop (the stack is not empty).
+__device__ __forceinline__ int stack_pop(TravState &st, const int *deep) {
+    const int x = st.top[0];
+#pragma unroll
+    for (int i = 0; i < kRegStack - 1; ++i) st.top[i] = st.top[i + 1];
+    if (st.sp > kRegStack) st.top[kRegStack - 1] = deep[st.sp - 1 - kRegStack];
+    --st.sp;
+    return x;
+}
 
 // Spheres first (closest: they set the initial best; any: a hit ends the
 // query), then the BVH from the root.  Returns true when the query is
@@ -280,7 +307,7 @@ __device__ __forceinline__ int i4(const int4 &v, int i) { return i == 0 ? v.x : 
 // so the next nearest is on top.  Returns true when the traversal is over; for
 // any-hit, st.best_id != PG_NO_HIT then means occluded.
 template <bool kAny, class Ctr>
-__device__ __forceinline__ bool trav_step(const DevScene &S, TravState &st, int *stack, Ctr &ctr) {
+__device__ __forceinline__ bool trav_step(const DevScene &S, TravState &st, int *deep, Ctr &ctr) {
     // read-only path: the scene never changes during a launch
     const DevBvhNode *np = S.nodes + st.node;
     const float4 lox = __ldg(&np->lox), loy = __ldg(&np->loy), loz = __ldg(&np->loz);
@@ -341,13 +368,12 @@ __device__ __forceinline__ bool trav_step(const DevScene &S, TravState &st, int 
         ++nn;
     }
     if (nn > 0) {
-        for (int q = nn - 1; q >= 1; --q)
-            if (st.sp < kStackSize) stack[st.sp++] = cand[q];
+        for (int q = nn - 1; q >= 1; --q) stack_push(st, deep, cand[q]);
         st.node = cand[0];
         return false;
     }
     if (st.sp == 0) return true;
-    st.node = stack[--st.sp];
+    st.node = stack_pop(st, deep);
     return false;
 }
 
@@ -356,9 +382,9 @@ template <class Ctr = NoCount>
 __device__ __forceinline__ bool trace_closest(const DevScene &S, const float o[3], const float d[3], float tmin,
                                               float tmax, pg_hit &hit, Ctr &&ctr = Ctr()) {
     TravState st;
-    int stack[kStackSize];
+    int deep[kDeepStack];
     trav_begin<false>(S, st, o, d, tmin, tmax);
-    while (!trav_step<false>(S, st, stack, ctr)) {
+    while (!trav_step<false>(S, st, deep, ctr)) {
     }
     hit.t = st.tmax;
     hit.u = st.best_u;
@@ -372,9 +398,9 @@ template <class Ctr = NoCount>
 __device__ __forceinline__ bool trace_any(const DevScene &S, const float o[3], const float d[3], float tmin,
                                           float tmax, Ctr &&ctr = Ctr()) {
     TravState st;
-    int stack[kStackSize];
+    int deep[kDeepStack];
     if (trav_begin<true>(S, st, o, d, tmin, tmax)) return true;
-    while (!trav_step<true>(S, st, stack, ctr)) {
+    while (!trav_step<true>(S, st, deep, ctr)) {
     }
     return st.best_id != PG_NO_HIT;
 }
