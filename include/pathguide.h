@@ -523,6 +523,24 @@ typedef struct pg_render_params {
  * (:962-964, 1180).  Off by default: guiding then follows the recording rule. */
 #define PG_RENDER_GUIDE_ALMOST_DISCRETE 4u
 
+/* Irradiance cache (raytrace.rgen:745-813, 1231-1421; raytrace.irradiance.rint,
+ * raytrace.irradiance.rahit): with a cache set on the scene
+ * (pg_scene_set_irradiance_cache), a path that reaches a diffuse vertex (or any
+ * non-discrete one with use_on_glossy) inside cached spheres takes the cached
+ * irradiance there times the surface's diffuse reflectance / pi, adds one
+ * next-event sample and ends.  Elsewhere the vertex queues a new entry with
+ * probability create_prob (at most 5 per pixel and pass), and every pixel
+ * queues an update of the next entry (round robin) with probability
+ * update_prob.  The queued entries are computed after each sample pass (20 x 10
+ * stratified hemisphere paths each), written in pixel order, and used from the
+ * next pass on: one pass here is one frame of the reference at one sample per
+ * pixel.  A render call that grows the cache synchronizes its stream once at
+ * the end.  Requires a cache on the scene. */
+#define PG_RENDER_IRRADIANCE_CACHE 8u
+/* With PG_RENDER_IRRADIANCE_CACHE: query the cache only (no creation, no
+ * update, no synchronization). */
+#define PG_RENDER_IC_FROZEN 16u
+
 enum pg_render_stage {
     PG_STAGE_CAMERA = 0, PG_STAGE_EXTEND, PG_STAGE_SHADE, PG_STAGE_SHADOW, PG_STAGE_ADVANCE, PG_STAGE_COMMIT,
     PG_STAGE_COUNT
@@ -593,6 +611,72 @@ int pg_scene_get_envmap(const pg_scene *scene, float *rgb_out, uint32_t *width, 
  * without compression. */
 int pg_exr_read(const char *path, float *rgb_out, uint64_t capacity, uint32_t *width, uint32_t *height);
 int pg_exr_write(const char *path, const float *rgb, uint32_t width, uint32_t height);
+
+/* The irradiance cache of a scene: the reference's push constants
+ * (src/RayTracingApp.h:97-113) and IC_SIZE.  Defaults: a 0.2, min_radius 0.1,
+ * create_prob 0.0005, update_prob 0.00001, gradients off (max length 5),
+ * visibility check off, one NEE sample, diffuse surfaces only. */
+typedef struct pg_irradiance_cache_config {
+    uint32_t capacity;            /* IC_SIZE: maximum entries (0 removes the cache) */
+    float a;                      /* irradianceA: sphere radius = a * harmonic mean distance */
+    float min_radius;             /* irradianceCacheMinRadius: lower bound of the harmonic distance */
+    float create_prob;            /* irradianceCreateProb, per vertex without a cache hit */
+    float update_prob;            /* irradianceUpdateProb, per pixel sample */
+    uint32_t use_gradients;       /* useIrradianceGradients */
+    float gradients_max_length;   /* irradianceGradientsMaxLength */
+    uint32_t visibility_check;    /* irradianceCachePerformVisibilityCheck */
+    uint32_t use_on_glossy;       /* useIrradianceCacheOnGlossy */
+    uint32_t reserved[3];
+} pg_irradiance_cache_config;
+
+/* One cache entry (cacheSpheres[i] and cache[i] of raytrace.rgen:118-119): the
+ * sphere (centre, radius = a * harmonic_r), the surface normal, the cached
+ * irradiance and its rotation and translation gradients. */
+typedef struct pg_ic_entry {
+    float center[3];
+    float radius;
+    float normal[3];
+    float harmonic_r;
+    float color[3];
+    uint32_t num_updates;
+    float rot_grad[3];
+    float trans_grad[3];
+} pg_ic_entry;
+
+void pg_default_irradiance_cache_config(pg_irradiance_cache_config *out);
+/* Sets (and empties) the scene's irradiance cache; capacity 0 removes it. */
+int pg_scene_set_irradiance_cache(pg_scene *scene, const pg_irradiance_cache_config *cfg);
+/* The entries (host copy; NULL out: count only) and their count. */
+int pg_scene_get_irradiance_cache(pg_scene *scene, pg_ic_entry *out, uint32_t capacity, uint32_t *n_entries);
+/* Replaces the entries (host array, at most the capacity) - e.g. a cache
+ * computed elsewhere, for rendering with PG_RENDER_IC_FROZEN - and restarts
+ * the round-robin update position. */
+int pg_scene_set_irradiance_cache_entries(pg_scene *scene, const pg_ic_entry *entries, uint32_t n);
+
+/* Cache queries at n points with their surface normals (device arrays, 3
+ * floats each): rgb the weighted mean of the applicable entries
+ * (queryIrradianceCache, raytrace.rgen:748-773), found 1 where one applied. */
+int pg_ic_query(pg_scene *scene, const float *positions, const float *normals, uint32_t n, float *rgb,
+                uint32_t *found, void *stream);
+
+/* A request for a cache entry at a surface point.  pixel, bounce and pass
+ * name the random numbers its paths use: a render queues the request of the
+ * vertex at `bounce` of the path `pixel` (a camera path: its pixel) in sample
+ * pass `pass` (bounce 255: the update request of that pixel). */
+typedef struct pg_ic_request {
+    float position[3];
+    float normal[3];
+    uint32_t pixel, bounce, pass, reserved;
+} pg_ic_request;
+
+/* The entries calculateCacheData (raytrace.rgen:1231-1316) and
+ * createIrradianceCache (:1383-1421) make at n requests (device arrays), with
+ * the render settings rp (seed, next-event estimation, guiding with `guide`)
+ * and the scene's cache for the lookups of their paths; the cache is not
+ * changed.  A request whose hemisphere saw nothing gets harmonic_r -1 and
+ * num_updates 0 (no entry would be made). */
+int pg_ic_compute(pg_scene *scene, const pg_render_params *rp, pg_ctx *guide, const pg_ic_request *requests,
+                  uint32_t n, pg_ic_entry *out, void *stream);
 
 /* Closest hit / any hit of n rays (device arrays).  Traversal: four-wide BVH,
  * near child first, watertight FP32 ray-triangle test (Woop, Benthin and

@@ -20,6 +20,12 @@ rewrites only -
   * variables declared at file scope become ``thread_local`` (each shader
     invocation has its own), and a shader's ``main()`` body becomes a named
     function;
+  * an identifier swizzle ``name.xxx`` becomes ``xxx(name)`` too;
+  * in the irradiance cache's intersection shader its buffer name
+    ``spheres`` becomes ``cacheSpheres`` (the name raytrace.rgen binds the
+    same buffer under), and in its any-hit shader the local ``E`` becomes
+    ``E_`` (raytrace.rgen defines a macro ``E``, which the separately
+    compiled shader does not see);
   * ``#include`` / ``#version`` / ``#extension`` lines are dropped;
 
 and writes oracle/_ref/glsl_ref_gen.cpp, which wraps the text in namespace
@@ -46,6 +52,7 @@ OUT_DIR = HERE / "_ref"
 PART_A = [
     ("limits.glsl", 1, 7),            # SIZE_LIGHT_RANDOM, MAX_DISTRIBUTIONS, MAX_DIRECTIONAL_DATA_PER_PIXEL
     ("raycommon.glsl", 1, 76),        # hitInfo, shadowCheck, pushConstant, sphere
+    ("raycommon.glsl", 78, 81),       # aabb
     ("raycommon.glsl", 83, 103),      # cacheHeader, cacheData, cacheHits
     ("wavefront.glsl", 1, 45),        # Vertex, Material, InstanceInfo, Light, FaceSample
     ("random_fwd.glsl", 1, 40),       # forward declarations of random.glsl
@@ -69,11 +76,22 @@ PART_B = [
 PART_C_STATE = [
     ("raytrace.rgen", 56, 84),        # ray flags, new irradiance-cache entries, the split queue
 ]
+# the irradiance cache's any-hit helpers, after the cache buffers (glsl_ref_scene.inc)
+PART_IC_HELPERS = [
+    ("raytrace.irradiance.rahit", 18, 25),  # irradianceWeight, visibilityCheck
+]
+# (file, first, last, function name[, renames]): a renamed identifier is a
+# buffer the shader binds under another name than raytrace.rgen does (binding
+# 12 is `spheres` in the cache's intersection shader, `cacheSpheres` in
+# raytrace.rgen:118), or a local variable named like a macro of
+# raytrace.rgen (`E`, :19), which a separate shader does not see
 SHADERS_AS_FUNCTIONS = [
     ("raytrace.rchit", 17, 58, "closestHitTriangle"),
     ("raytrace.sphere.rchit", 14, 35, "closestHitSphere"),
     ("raytrace.rmiss", 16, 30, "missShader"),
     ("raytrace.shadow.rmiss", 8, 10, "shadowMissShader"),
+    ("raytrace.irradiance.rint", 13, 20, "icIntersectionShader", {"spheres": "cacheSpheres"}),
+    ("raytrace.irradiance.rahit", 28, 50, "icAnyHitShader", {"E": "E_"}),
 ]
 PART_C = [
     ("raytrace.rgen", 358, 473),      # sampleLights
@@ -81,12 +99,14 @@ PART_C = [
     ("raytrace.rgen", 745, 804),      # queryIrradianceCache(Gradients)
     ("raytrace.rgen", 871, 902),      # multipleNEE, split
     ("raytrace.rgen", 992, 1226),     # raytrace: the path loop, NEE, guiding, sample recording
+    ("raytrace.rgen", 1231, 1421),    # calculateCacheData, clampGradients, update- / createIrradianceCache
 ]
 
 _QUAL_OUT = re.compile(r"\b(?:out|inout)\s+(\w+)\s+(\w+)")
 _QUAL_IN = re.compile(r"\bin\s+(\w+)\s+(\w+)")
 _SIGNATURE = re.compile(r"^\s*\w+\s+\w+\s*\(.*\)\s*[{;]?\s*$")
 _LABEL = re.compile(r"^\s*(case\s+[^:]+|default\s*):\s*$")
+_NAME_XXX = re.compile(r"\b([A-Za-z_]\w*)\.xxx\b")
 _VEC3_XYZ = re.compile(r"\b(origin|direction|normal)\.xyz\b")
 _SELF_INIT = re.compile(r"\b(\w+)\s+(\w+)\s*=\s*\2\s*\(")
 _FLOAT_LIT = re.compile(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])")
@@ -168,6 +188,7 @@ def transform(text: str) -> str:
             code, sep, comment = line.partition("//")
             code = _FLOAT_LIT.sub(lambda m: m.group(1) + "f", code)
             code = _swizzle_xxx(code)
+            code = _NAME_XXX.sub(r"xxx(\1)", code)
             code = _VEC3_XYZ.sub(r"\1", code)
             code = _SELF_INIT.sub(lambda m: f"{m.group(1)} {m.group(2)} = glsl::{m.group(2)}(", code)
             line = code + sep + comment
@@ -185,9 +206,11 @@ def _excerpt(parts) -> str:
 
 def _shaders_as_functions() -> str:
     chunks = []
-    for name, a, b, fn in SHADERS_AS_FUNCTIONS:
+    for name, a, b, fn, *rest in SHADERS_AS_FUNCTIONS:
         lines = (SHADERS / name).read_text().splitlines()
         body = "\n".join(lines[a - 1:b])
+        for old, new in (rest[0] if rest else {}).items():
+            body = re.sub(rf"\b{old}\b", new, body)
         chunks.append(f"void {fn}() {{\n#line {a} \"{name}\"\n" + transform(body) + "\n}")
     return "\n".join(chunks)
 
@@ -206,6 +229,7 @@ def generate() -> Path:
         _excerpt(PART_C_STATE),
         '#line 1 "glsl_ref_scene.inc"',
         '#include "glsl_ref_scene.inc"',
+        _excerpt(PART_IC_HELPERS),
         _shaders_as_functions(),
         _excerpt(PART_C),
         "}  // namespace glsl",

@@ -59,7 +59,18 @@ class RenderConfig(C.Structure):
     _fields_ = [("spp", C.c_uint32), ("max_depth", C.c_uint32), ("max_follow_discrete", C.c_uint32),
                 ("use_nee", C.c_uint32), ("use_mis", C.c_uint32), ("use_guiding", C.c_uint32),
                 ("guiding_prob", C.c_float), ("use_parallax", C.c_uint32), ("frame_seed", C.c_uint32),
-                ("region_splits", C.c_uint32), ("region_root", C.c_float * 6)]
+                ("region_splits", C.c_uint32), ("region_root", C.c_float * 6), ("use_ic", C.c_uint32)]
+
+
+class IcConfig(C.Structure):
+    _fields_ = [("a", C.c_float), ("min_radius", C.c_float), ("gradients_max_length", C.c_float),
+                ("use_gradients", C.c_uint32), ("visibility_check", C.c_uint32), ("use_on_glossy", C.c_uint32),
+                ("capacity", C.c_uint32)]
+
+
+def ic_config(capacity, a=0.2, min_radius=0.1, gradients_max_length=5.0, use_gradients=0, visibility_check=0,
+              use_on_glossy=0) -> IcConfig:
+    return IcConfig(a, min_radius, gradients_max_length, use_gradients, visibility_check, use_on_glossy, capacity)
 
 
 class GlslRef:
@@ -88,6 +99,11 @@ class GlslRef:
             "glslref_record_path": (u, [u, p, p, p, p, p, p, p]),
             "glslref_weight_window": (f, [p, p, p, f, u, P(C.c_int32), P(u)]),
             "glslref_render": (i, [p, P(RenderConfig), p, u, u, i, p]),
+            "glslref_ic_set": (i, [p, u, P(IcConfig)]),
+            "glslref_ic_get": (u, [p, u, P(u)]),
+            "glslref_ic_query": (None, [p, p, u, p, p]),
+            "glslref_ic_compute": (i, [p, P(RenderConfig), p, p, p, p, u, i, p]),
+            "glslref_ic_create_update": (i, [p, P(RenderConfig), p, p, u, u]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(self.lib, name)
@@ -207,12 +223,13 @@ class GlslRef:
         return w[:m].copy(), fl[:m].copy()
 
     def render(self, exp: dict, path_length: int, spp: int, frame_seed: int, use_nee=True, use_mis=True,
-               guide: dict | None = None, guiding_prob=0.5, rows=None, threads=None) -> np.ndarray:
+               guide: dict | None = None, guiding_prob=0.5, rows=None, threads=None, use_ic=False) -> np.ndarray:
         """The reference's estimator (raytrace() and the hit shaders compiled as
         C++) over an exported library scene: radiance sums (H, W, 3).
         path_length is the library's max_depth (paths of at most that many
         segments); the reference's maxDepth counts two fewer (its next-event
-        estimation runs at the vertex after maxDepth)."""
+        estimation runs at the vertex after maxDepth).  use_ic: query the
+        cache of ic_set at every cache-capable vertex (no entries are made)."""
         import os
         from oracle.oracle import TraceOracle
         s, keep = TraceOracle.scene(exp)
@@ -221,7 +238,7 @@ class GlslRef:
         img = np.zeros((H, W, 3), dtype=np.float64)
         cfg = RenderConfig(spp=spp, max_depth=max(path_length - 2, 0), max_follow_discrete=0,
                            use_nee=int(use_nee), use_mis=int(use_mis), use_guiding=int(guide is not None),
-                           guiding_prob=guiding_prob, frame_seed=frame_seed)
+                           guiding_prob=guiding_prob, frame_seed=frame_seed, use_ic=int(use_ic))
         vmm = None
         if guide is not None:
             cfg.use_parallax = int(guide["use_parallax"])
@@ -234,6 +251,74 @@ class GlslRef:
         if st != 0:
             raise RuntimeError("glslref_render failed")
         return img
+
+    # --- irradiance cache
+    def ic_set(self, entries: np.ndarray, cfg: IcConfig):
+        """The cache the reference's functions see (entries: pg_ic_entry rows)."""
+        e = np.ascontiguousarray(entries)
+        assert e.dtype.itemsize == 72
+        if self.lib.glslref_ic_set(e.ctypes.data if len(e) else None, len(e), C.byref(cfg)) != 0:
+            raise RuntimeError("glslref_ic_set failed")
+
+    def ic_get(self, dtype) -> tuple[np.ndarray, int]:
+        """The reference cache's entries and its round-robin update position."""
+        nxt = C.c_uint32()
+        n = self.lib.glslref_ic_get(None, 0, C.byref(nxt))
+        out = np.zeros(n, dtype=dtype)
+        self.lib.glslref_ic_get(out.ctypes.data if n else None, n, C.byref(nxt))
+        return out, nxt.value
+
+    def ic_query(self, pos, nrm):
+        pos = np.ascontiguousarray(pos, dtype=np.float32)
+        nrm = np.ascontiguousarray(nrm, dtype=np.float32)
+        n = len(pos)
+        rgb = np.zeros((n, 3), dtype=np.float32)
+        found = np.zeros(n, dtype=np.uint32)
+        self.lib.glslref_ic_query(pos.ctypes.data, nrm.ctypes.data, n, rgb.ctypes.data, found.ctypes.data)
+        return rgb, found
+
+    @staticmethod
+    def _config(exp, use_nee, use_mis, guide, guiding_prob, frame_seed=0, spp=1, path_length=2, use_ic=0):
+        cfg = RenderConfig(spp=spp, max_depth=max(path_length - 2, 0), max_follow_discrete=0,
+                           use_nee=int(use_nee), use_mis=int(use_mis), use_guiding=int(guide is not None),
+                           guiding_prob=guiding_prob, frame_seed=frame_seed, use_ic=int(use_ic))
+        vmm = None
+        if guide is not None:
+            cfg.use_parallax = int(guide["use_parallax"])
+            cfg.region_splits = int(guide["split_count"])
+            cfg.region_root[:] = [float(x) for x in guide["root"]]
+            vmm = np.ascontiguousarray(guide["vmm"])
+        return cfg, vmm
+
+    def ic_compute(self, exp: dict, pos, nrm, seeds, use_nee=True, use_mis=True, guide=None, guiding_prob=0.5,
+                   threads=None) -> np.ndarray:
+        """calculateCacheData at each (pos, nrm) with random state seeds[i]:
+        (n, 10) colour, rotation gradient, translation gradient, harmonicR."""
+        import os
+        from oracle.oracle import TraceOracle
+        s, keep = TraceOracle.scene(exp)
+        cfg, vmm = self._config(exp, use_nee, use_mis, guide, guiding_prob)
+        pos = np.ascontiguousarray(pos, dtype=np.float32)
+        nrm = np.ascontiguousarray(nrm, dtype=np.float32)
+        seeds = np.ascontiguousarray(seeds, dtype=np.uint32)
+        out = np.zeros((len(pos), 10), dtype=np.float32)
+        st = self.lib.glslref_ic_compute(C.byref(s), C.byref(cfg), vmm.ctypes.data if vmm is not None else None,
+                                         pos.ctypes.data, nrm.ctypes.data, seeds.ctypes.data, len(pos),
+                                         threads or os.cpu_count() or 1, out.ctypes.data)
+        if st != 0:
+            raise RuntimeError("glslref_ic_compute failed")
+        return out
+
+    def ic_create_update(self, exp: dict, pos=None, nrm=None, updates=0, seed=1, use_nee=True, use_mis=True) -> int:
+        """createIrradianceCache at (pos, nrm) (if given), then `updates`
+        calls of updateIrradianceCache, on the cache of ic_set."""
+        from oracle.oracle import TraceOracle
+        s, keep = TraceOracle.scene(exp)
+        cfg, _ = self._config(exp, use_nee, use_mis, None, 0.5)
+        p = np.ascontiguousarray(pos, dtype=np.float32) if pos is not None else None
+        q = np.ascontiguousarray(nrm, dtype=np.float32) if nrm is not None else None
+        return self.lib.glslref_ic_create_update(C.byref(s), C.byref(cfg), p.ctypes.data if p is not None else None,
+                                                 q.ctypes.data if q is not None else None, updates, seed)
 
     def weight_window(self, estimate, throughput, adjoint, s, state):
         """applyWeightWindow: (q, n, numbers drawn)."""

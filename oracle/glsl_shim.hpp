@@ -115,6 +115,14 @@ inline vec3 abs(vec3 a) { return vec3(abs(a.x), abs(a.y), abs(a.z)); }
 inline vec3 max(vec3 a, vec3 b) { return vec3(max(a.x, b.x), max(a.y, b.y), max(a.z, b.z)); }
 inline vec3 mix(vec3 a, vec3 b, float t) { return a * (1.0f - t) + b * t; }
 
+// atomicAdd on a buffer member: the old value (the tests run the cache's
+// create / update functions on one thread)
+inline uint atomicAdd(uint &x, uint v) {
+    const uint old = x;
+    x += v;
+    return old;
+}
+
 // `expr.xxx` of a scalar expression
 inline vec3 xxx(float s) { return vec3(s); }
 

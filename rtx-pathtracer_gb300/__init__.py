@@ -106,6 +106,12 @@ SIGNATURES = {
     "pg_probe_shading": (_I, [_P, _U32, _P, _U32, _P, _U32, _P, _P]),
     "pg_probe_records": (_I, [_P, _P, _U32, _P, _P, _P, _P]),
     "pg_render": (_I, [_P, C.POINTER(abi.RenderParams), _P, _P, _P, C.POINTER(abi.RenderStats), _P]),
+    "pg_default_irradiance_cache_config": (None, [C.POINTER(abi.IrradianceCacheConfig)]),
+    "pg_scene_set_irradiance_cache": (_I, [_P, C.POINTER(abi.IrradianceCacheConfig)]),
+    "pg_scene_get_irradiance_cache": (_I, [_P, _P, _U32, C.POINTER(_U32)]),
+    "pg_scene_set_irradiance_cache_entries": (_I, [_P, _P, _U32]),
+    "pg_ic_query": (_I, [_P, _P, _P, _U32, _P, _P, _P]),
+    "pg_ic_compute": (_I, [_P, C.POINTER(abi.RenderParams), _P, _P, _U32, _P, _P]),
 }
 
 _LIB = None
@@ -656,6 +662,57 @@ class Scene:
                                        _dptr(image_dev), _dptr(records_dev) if records_dev is not None else None,
                                        C.byref(st) if st is not None else None, _stream_handle(stream)))
         return st
+
+    # --- irradiance cache
+    def set_irradiance_cache(self, cfg: "abi.IrradianceCacheConfig | None" = None, **fields):
+        """Sets (and empties) the scene's irradiance cache: the defaults of
+        pg_default_irradiance_cache_config, or cfg, with `fields` overriding."""
+        if cfg is None:
+            cfg = abi.IrradianceCacheConfig()
+            self.lib.pg_default_irradiance_cache_config(C.byref(cfg))
+        for k, v in fields.items():
+            setattr(cfg, k, v)
+        self._check(self.lib.pg_scene_set_irradiance_cache(self.h, C.byref(cfg)))
+        return cfg
+
+    def irradiance_cache(self) -> np.ndarray:
+        """The cache's entries (IC_ENTRY_DTYPE)."""
+        n = C.c_uint32()
+        self._check(self.lib.pg_scene_get_irradiance_cache(self.h, None, 0, C.byref(n)))
+        out = np.zeros(n.value, dtype=abi.IC_ENTRY_DTYPE)
+        if n.value:
+            self._check(self.lib.pg_scene_get_irradiance_cache(self.h, out.ctypes.data, n.value, C.byref(n)))
+        return out
+
+    def set_irradiance_cache_entries(self, entries: np.ndarray):
+        e = np.ascontiguousarray(entries, dtype=abi.IC_ENTRY_DTYPE)
+        self._check(self.lib.pg_scene_set_irradiance_cache_entries(self.h, e.ctypes.data if len(e) else None,
+                                                                   len(e)))
+
+    def ic_query(self, positions, normals):
+        """Cache queries at (n, 3) points with normals: (rgb (n, 3), found (n,))."""
+        import torch
+        pos = torch.as_tensor(np.ascontiguousarray(positions, dtype=np.float32)).cuda()
+        nrm = torch.as_tensor(np.ascontiguousarray(normals, dtype=np.float32)).cuda()
+        n = pos.shape[0]
+        rgb = torch.zeros((n, 3), dtype=torch.float32, device="cuda")
+        found = torch.zeros(n, dtype=torch.int32, device="cuda")
+        self._check(self.lib.pg_ic_query(self.h, _dptr(pos), _dptr(nrm), n, _dptr(rgb), _dptr(found),
+                                         _stream_handle(None)))
+        torch.cuda.synchronize()
+        return rgb.cpu().numpy(), found.cpu().numpy().astype(np.uint32)
+
+    def ic_compute(self, params: abi.RenderParams, requests: np.ndarray,
+                   guide: "FitContext | None" = None) -> np.ndarray:
+        """The entries calculateCacheData makes at the requests (IC_REQUEST_DTYPE)."""
+        import torch
+        req = np.ascontiguousarray(requests, dtype=abi.IC_REQUEST_DTYPE)
+        n = len(req)
+        d_req = torch.from_numpy(req.view(np.uint8).copy()).cuda()
+        d_out = torch.zeros(n * abi.IC_ENTRY_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+        self._check(self.lib.pg_ic_compute(self.h, C.byref(params), guide.h if guide is not None else None,
+                                           _dptr(d_req), n, _dptr(d_out), _stream_handle(None)))
+        return d_out.cpu().numpy().view(abi.IC_ENTRY_DTYPE)
 
     def get_scene_size(self):
         """SceneLoader::getSceneSize (src/SceneLoader.h:118): the scene box (min xyz, max xyz)."""

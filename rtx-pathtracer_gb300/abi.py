@@ -173,6 +173,8 @@ class RenderParams(C.Structure):
 PG_RENDER_COUNT_WORK = 1
 PG_RENDER_TIME_STAGES = 2
 PG_RENDER_GUIDE_ALMOST_DISCRETE = 4
+PG_RENDER_IRRADIANCE_CACHE = 8
+PG_RENDER_IC_FROZEN = 16
 STAGES = ("camera", "extend", "shade", "shadow", "advance", "commit")
 
 
@@ -182,6 +184,23 @@ class RenderStats(C.Structure):
                 ("extension_triangle_tests", C.c_uint64), ("shadow_node_visits", C.c_uint64),
                 ("shadow_triangle_tests", C.c_uint64), ("stage_ms", C.c_float * 6),
                 ("stage_launches", C.c_uint32 * 6)]
+
+
+class IrradianceCacheConfig(C.Structure):
+    _fields_ = [("capacity", C.c_uint32), ("a", C.c_float), ("min_radius", C.c_float), ("create_prob", C.c_float),
+                ("update_prob", C.c_float), ("use_gradients", C.c_uint32), ("gradients_max_length", C.c_float),
+                ("visibility_check", C.c_uint32), ("use_on_glossy", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+
+
+# pg_ic_entry (72 bytes) and pg_ic_request (40 bytes)
+IC_ENTRY_DTYPE = np.dtype([("center", "<f4", 3), ("radius", "<f4"), ("normal", "<f4", 3), ("harmonic_r", "<f4"),
+                           ("color", "<f4", 3), ("num_updates", "<u4"), ("rot_grad", "<f4", 3),
+                           ("trans_grad", "<f4", 3)])
+assert IC_ENTRY_DTYPE.itemsize == 72
+IC_REQUEST_DTYPE = np.dtype([("position", "<f4", 3), ("normal", "<f4", 3), ("pixel", "<u4"), ("bounce", "<u4"),
+                             ("pass", "<u4"), ("reserved", "<u4")])
+assert IC_REQUEST_DTYPE.itemsize == 40
+IC_UPDATE_BOUNCE = 255
 
 
 def render_params(spp=1, max_depth=8, seed=1, use_nee=1, use_mis=1, use_guiding=0, guiding_prob=0.5,

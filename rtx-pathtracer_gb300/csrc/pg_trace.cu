@@ -480,6 +480,12 @@ __device__ __forceinline__ void tex_rgb(const DevScene &S, uint32_t prim, uint32
     }
 }
 
+}  // namespace pg
+
+#include "pg_icache.cuh"
+
+namespace pg {
+
 struct DevRender {
     DevScene S;
     const float *pos;            // 3 per vertex (original)
@@ -520,6 +526,7 @@ struct DevRender {
     int32_t *rec_pending;        // slot awaiting its distance, -1 if none
     float *rec_factor;           // apparent-distance factor through refraction
     float *image;
+    DevIc ic;                    // irradiance cache (query / grow off: unused)
 };
 
 __device__ __forceinline__ V ld3(const float *a, uint32_t i) { return mk(a[3 * i], a[3 * i + 1], a[3 * i + 2]); }
@@ -587,6 +594,84 @@ __device__ __forceinline__ float light_pdf(const DevRender &R, uint32_t light, f
     return (t * t) / (fmaxf(cos_l, 1e-12f) * L.area) / (float)R.n_lights;
 }
 
+// One next-event sample from x (sampleLights, raytrace.rgen:358-473): a light
+// picked uniformly by ul, then a point on it (u1, u2): the environment by a
+// uniform direction in the hemisphere of n, a sphere uniformly over its
+// surface, a mesh by area and uniformly within the triangle.  Returns false
+// when the sample contributes nothing; else the direction, the shadow ray's
+// extent, BSDF * cos * emitted radiance (fLe, to be divided by pl and weighted
+// by the caller), the light pdf pl and the BSDF's pdf pb of the direction.
+struct NeeSample {
+    V wl;
+    float tmax;
+    V fLe;
+    float pl, pb;
+};
+__device__ __forceinline__ bool nee_sample(const DevRender &R, const pg_material &m, V x, V n, V wi, float ul,
+                                           float u1, float u2, NeeSample &ns) {
+    const uint32_t l = min((uint32_t)(ul * (float)R.n_lights), R.n_lights - 1);
+    const DevLight &L = R.lights[l];
+    if (L.type == 2) {
+        // environment: a uniform direction in the hemisphere (raytrace.rgen:406-421)
+        const float ct = u1, st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct)), ph = 2.0f * kPi * u2;
+        const V wl = to_world(mk(st * cosf(ph), st * sinf(ph), ct), n);
+        const MatEval me = bsdf_eval(m, n, wi, wl);
+        if (!(maxc(me.f) > 0.0f)) return false;
+        ns.wl = wl;
+        ns.tmax = 1e30f;
+        ns.pl = 0.15915494309189535f / (float)R.n_lights;
+        ns.pb = me.pdf;
+        ns.fLe = hmul(me.f, env_radiance(R, wl));
+        return true;
+    }
+    V lp, ln;
+    if (L.type == 1) {
+        const pg_sphere &sp = R.S.spheres[L.sphere];
+        const float z = 1.0f - 2.0f * u1, rr = sqrtf(fmaxf(0.0f, 1.0f - z * z)), ph = 2.0f * kPi * u2;
+        ln = mk(rr * cosf(ph), rr * sinf(ph), z);
+        lp = add(mk(sp.center[0], sp.center[1], sp.center[2]), mul(ln, sp.radius));
+    } else {
+        // triangle by area, then a uniform point (raytrace.rgen:445-456)
+        uint32_t lo = 0, hi = L.count - 1;
+        const float uc = u1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) / 2;
+            if (R.light_cdf[L.first + mid] < uc)
+                lo = mid + 1;
+            else
+                hi = mid;
+        }
+        const float c0 = lo == 0 ? 0.0f : R.light_cdf[L.first + lo - 1];
+        const float c1 = R.light_cdf[L.first + lo];
+        const float ur = c1 > c0 ? fminf((uc - c0) / (c1 - c0), 0.99999994f) : 0.5f;
+        const uint32_t t = R.light_tris[L.first + lo];
+        const V a = ld3(R.pos, R.idx[3 * t]), bb = ld3(R.pos, R.idx[3 * t + 1]), c = ld3(R.pos, R.idx[3 * t + 2]);
+        const float sx = sqrtf(ur);
+        lp = add(add(mul(a, 1.0f - sx), mul(bb, sx * (1.0f - u2))), mul(c, u2 * sx));
+        ln = nrm(cross3(sub(bb, a), sub(c, a)));
+    }
+    V tl = sub(lp, x);
+    const float dist2 = dot3(tl, tl), dist = sqrtf(dist2);
+    const V wl = mul(tl, 1.0f / dist);
+    float cl = -dot3(wl, ln);
+    if (L.type == 0) cl = fabsf(cl);  // two-sided mesh lights (raytrace.rgen:463-466)
+    if (!(cl > 0.0f && dot3(n, wl) > 0.0f)) return false;
+    const MatEval me = bsdf_eval(m, n, wi, wl);
+    if (!(maxc(me.f) > 0.0f)) return false;
+    ns.wl = wl;
+    ns.tmax = dist * (1.0f - 0.0001f);
+    ns.pl = dist2 / (cl * L.area) / (float)R.n_lights;
+    ns.pb = me.pdf;
+    ns.fLe = hmul(me.f, mk(L.emission[0], L.emission[1], L.emission[2]));
+    return true;
+}
+
+}  // namespace pg
+
+#include "pg_icache_paths.cuh"
+
+namespace pg {
+
 __global__ void k_camera(DevRender R) {
     const uint32_t W = R.cam.width, H = R.cam.height;
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
@@ -619,6 +704,12 @@ __global__ void k_camera(DevRender R) {
         R.rec_count[pix] = R.rec_start[pix];
         R.rec_pending[pix] = -1;
         R.rec_factor[pix] = 1.0f;
+    }
+    if (R.ic.grow) {
+        // main() of raytrace.rgen:1639-1641: an update of the next entry with probability update_prob
+        R.ic.created[pix] = 0;
+        if (rnd(R.rp.seed ^ kIcSalt, pix, R.sample, 1023u) < R.ic.update_prob)
+            ic_push(R.ic, mk(0, 0, 0), mk(0, 0, 1), -1, pix, kIcUpdateBounce, R.sample);
     }
 }
 
@@ -741,8 +832,25 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
         const bool front = dot3(d, ng) < 0.0f;  // raytrace.rchit:42-48
         const V n = front ? ng : mul(ng, -1.0f);
         const V wi = mul(d, -1.0f);
-        // distance of a pending record (raytrace.rgen:1149-1156, 1201-1212)
-        if (rec_on && R.rec_pending[p] >= 0) {
+        // irradiance cache (raytrace.rgen:1080-1139): a vertex inside cached
+        // spheres takes their irradiance, adds next-event estimation and ends
+        // the path; elsewhere it may queue a new entry
+        bool ic_end = false;
+        V ic_L = mk(0, 0, 0);
+        if (R.ic.query && !last && m.type != PG_MAT_LIGHT && ic_capable(R.ic, m)) {
+            V E;
+            if (ic_query(R.ic, x, n, E)) {
+                ic_end = true;
+                ic_L = hmul(approx_diffuse(m, n, wi), E);
+            } else if (R.ic.grow && rnd(R.rp.seed, p, R.sample, dimb(bounce, 8)) < R.ic.create_prob &&
+                       R.ic.state[2] < R.ic.capacity && R.ic.created[p] < kIcMaxNewPerPixel) {
+                R.ic.created[p] += 1;
+                ic_push(R.ic, x, n, -1, p, (uint32_t)bounce, R.sample);
+            }
+        }
+        // distance of a pending record (raytrace.rgen:1149-1156, 1201-1212); a
+        // path that ends at the cache leaves it as it is
+        if (rec_on && R.rec_pending[p] >= 0 && !ic_end) {
             pg_directional_data &rd = R.rec[p * kMaxRecords + (uint32_t)R.rec_pending[p]];
             rd.distance += h.t * R.rec_factor[p];
             if (!is_delta(m) && !almost_delta(m)) R.rec_pending[p] = -1;
@@ -782,151 +890,100 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
             }
         } else if (!last) {
             const int b = bounce;
-            // --- next-event estimation (raytrace.rgen:601-731)
-            if (R.rp.use_nee && !is_delta(m) && R.n_lights > 0) {
-                const uint32_t l =
-                    min((uint32_t)(rnd(R.rp.seed, p, R.sample, dimb(b, 0)) * (float)R.n_lights), R.n_lights - 1);
-                const DevLight &L = R.lights[l];
-                const float u1 = rnd(R.rp.seed, p, R.sample, dimb(b, 1)), u2 = rnd(R.rp.seed, p, R.sample, dimb(b, 2));
-                V lp, ln;
-                if (L.type == 2) {
-                    // environment: a uniform direction in the hemisphere (raytrace.rgen:406-421)
-                    const float ct = u1, st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct)), ph = 2.0f * kPi * u2;
-                    const V wl = to_world(mk(st * cosf(ph), st * sinf(ph), ct), n);
-                    const float pl = 0.15915494309189535f / (float)R.n_lights;
-                    const MatEval me = bsdf_eval(m, n, wi, wl);
-                    if (maxc(me.f) > 0.0f) {
-                        float pb = me.pdf;
-                        if (R.guiding && guided_material(m, R.rp.flags)) {
-                            const uint32_t reg = region_of(R.guide, x);
-                            if (reg != PG_INVALID_REGION) {
-                                const float pg = vmm_pdf(R.guide.vmm[reg], wl, x, R.guide.use_parallax);
-                                if (!isnan(pg)) pb = (1.0f - R.rp.guiding_prob) * pb + R.rp.guiding_prob * pg;
-                            }
-                        }
-                        const float w = R.rp.use_mis ? pl * pl / (pl * pl + pb * pb) : 1.0f;
-                        const V Lnee = mul(hmul(me.f, env_radiance(R, wl)), w / pl);
-                        const uint32_t s = atomicAdd(&R.counters[2], 1u);
-                        st3(R.sh_o, s, x);
-                        st3(R.sh_d, s, wl);
-                        R.sh_tmax[s] = 1e30f;
-                        st3(R.sh_c, s, hmul(thr, Lnee));
-                        st3(R.sh_l, s, Lnee);
-                        R.sh_pix[s] = p;
-                        R.sh_nrec[s] = rec_on ? R.rec_count[p] : 0u;
-                    }
-                } else {
-                    if (L.type == 1) {
-                        const pg_sphere &sp = R.S.spheres[L.sphere];
-                        const float z = 1.0f - 2.0f * u1, rr = sqrtf(fmaxf(0.0f, 1.0f - z * z)), ph = 2.0f * kPi * u2;
-                        ln = mk(rr * cosf(ph), rr * sinf(ph), z);
-                        lp = add(mk(sp.center[0], sp.center[1], sp.center[2]), mul(ln, sp.radius));
-                    } else {
-                        // triangle by area, then a uniform point (raytrace.rgen:445-456)
-                        uint32_t lo = 0, hi = L.count - 1;
-                        const float uc = u1;
-                        while (lo < hi) {
-                            const uint32_t mid = (lo + hi) / 2;
-                            if (R.light_cdf[L.first + mid] < uc)
-                                lo = mid + 1;
-                            else
-                                hi = mid;
-                        }
-                        const float c0 = lo == 0 ? 0.0f : R.light_cdf[L.first + lo - 1];
-                        const float c1 = R.light_cdf[L.first + lo];
-                        const float ur = c1 > c0 ? fminf((uc - c0) / (c1 - c0), 0.99999994f) : 0.5f;
-                        const uint32_t t = R.light_tris[L.first + lo];
-                        const V a = ld3(R.pos, R.idx[3 * t]), bb = ld3(R.pos, R.idx[3 * t + 1]), c = ld3(R.pos, R.idx[3 * t + 2]);
-                        const float sx = sqrtf(ur);
-                        lp = add(add(mul(a, 1.0f - sx), mul(bb, sx * (1.0f - u2))), mul(c, u2 * sx));
-                        ln = nrm(cross3(sub(bb, a), sub(c, a)));
-                    }
-                    V tl = sub(lp, x);
-                    const float dist2 = dot3(tl, tl), dist = sqrtf(dist2);
-                    const V wl = mul(tl, 1.0f / dist);
-                    float cl = -dot3(wl, ln);
-                    if (L.type == 0) cl = fabsf(cl);  // two-sided mesh lights (raytrace.rgen:463-466)
-                    if (cl > 0.0f && dot3(n, wl) > 0.0f) {
-                        const float pl = dist2 / (cl * L.area) / (float)R.n_lights;
-                        const MatEval me = bsdf_eval(m, n, wi, wl);
-                        if (maxc(me.f) > 0.0f) {
-                            // pdf of the continuation sampler for this direction (MIS)
-                            float pb = me.pdf;
-                            if (R.guiding && guided_material(m, R.rp.flags)) {
-                                const uint32_t reg = region_of(R.guide, x);
-                                if (reg != PG_INVALID_REGION) {
-                                    const float pg = vmm_pdf(R.guide.vmm[reg], wl, x, R.guide.use_parallax);
-                                    if (!isnan(pg)) pb = (1.0f - R.rp.guiding_prob) * pb + R.rp.guiding_prob * pg;
-                                }
-                            }
-                            const float w = R.rp.use_mis ? pl * pl / (pl * pl + pb * pb) : 1.0f;
-                            const V Lnee = mul(hmul(me.f, mk(L.emission[0], L.emission[1], L.emission[2])), w / pl);
-                            const uint32_t s = atomicAdd(&R.counters[2], 1u);
-                            st3(R.sh_o, s, x);
-                            st3(R.sh_d, s, wl);
-                            R.sh_tmax[s] = dist * (1.0f - 0.0001f);
-                            st3(R.sh_c, s, hmul(thr, Lnee));
-                            st3(R.sh_l, s, Lnee);
-                            R.sh_pix[s] = p;
-                            R.sh_nrec[s] = rec_on ? R.rec_count[p] : 0u;
+            if (ic_end) {
+                // the cached irradiance; it reaches no guiding record (raytrace.rgen:1119)
+                const V c = hmul(thr, ic_L);
+                if (maxc(c) > 0.0f) {
+                    atomicAdd(&R.image[3 * p], c.x);
+                    atomicAdd(&R.image[3 * p + 1], c.y);
+                    atomicAdd(&R.image[3 * p + 2], c.z);
+                    R.found[p] = 1;
+                }
+            }
+            // --- next-event estimation (raytrace.rgen:601-731), always at a cache end (:1122)
+            if ((R.rp.use_nee || ic_end) && !is_delta(m) && R.n_lights > 0) {
+                NeeSample ns;
+                if (nee_sample(R, m, x, n, wi, rnd(R.rp.seed, p, R.sample, dimb(b, 0)),
+                               rnd(R.rp.seed, p, R.sample, dimb(b, 1)), rnd(R.rp.seed, p, R.sample, dimb(b, 2)), ns)) {
+                    // pdf of the continuation sampler for this direction (MIS)
+                    float pb = ns.pb;
+                    if (R.guiding && guided_material(m, R.rp.flags)) {
+                        const uint32_t reg = region_of(R.guide, x);
+                        if (reg != PG_INVALID_REGION) {
+                            const float pg = vmm_pdf(R.guide.vmm[reg], ns.wl, x, R.guide.use_parallax);
+                            if (!isnan(pg)) pb = (1.0f - R.rp.guiding_prob) * pb + R.rp.guiding_prob * pg;
                         }
                     }
+                    // a vertex whose path ends at the irradiance cache has no continuation to pair with
+                    const float pl = ns.pl;
+                    const float w = (R.rp.use_mis && !ic_end) ? pl * pl / (pl * pl + pb * pb) : 1.0f;
+                    const V Lnee = mul(ns.fLe, w / pl);
+                    const uint32_t s = atomicAdd(&R.counters[2], 1u);
+                    st3(R.sh_o, s, x);
+                    st3(R.sh_d, s, ns.wl);
+                    R.sh_tmax[s] = ns.tmax;
+                    st3(R.sh_c, s, hmul(thr, Lnee));
+                    st3(R.sh_l, s, Lnee);
+                    R.sh_pix[s] = p;
+                    R.sh_nrec[s] = (rec_on && !ic_end) ? R.rec_count[p] : 0u;
                 }
             }
             // --- continuation (getNewDirection, raytrace.rgen:923-960)
-            const float uch = rnd(R.rp.seed, p, R.sample, dimb(b, 3));
-            const float ul = rnd(R.rp.seed, p, R.sample, dimb(b, 4));
-            const float u1 = rnd(R.rp.seed, p, R.sample, dimb(b, 5)), u2 = rnd(R.rp.seed, p, R.sample, dimb(b, 6));
-            const bool gm = R.guiding && guided_material(m, R.rp.flags);
-            const pg_vmm_theta *mix = nullptr;
-            if (gm) {
-                const uint32_t reg = region_of(R.guide, x);
-                if (reg != PG_INVALID_REGION) mix = &R.guide.vmm[reg];
-            }
-            const Continuation cn = continue_path(m, d, n, front, x, gm, mix, R.guide.use_parallax,
-                                                  R.rp.guiding_prob, uch, ul, u1, u2,
-                                                  [&] { return rnd(R.rp.seed, p, R.sample, dimb(b, 7)); });
-            const V wo = cn.wo, tc = cn.tc;
-            const float pdf = cn.pdf;
-            const bool delta = cn.delta;
-            if (pdf > 0.0f && maxc(tc) > 0.0f) {
-                thr = hmul(thr, tc);
-                cont = true;
-                // guiding record of this vertex (raytrace.rgen:1179-1200)
-                if (rec_on) {
-                    const uint32_t cnt = R.rec_count[p];
-                    if (cnt < (uint32_t)kMaxRecords) {
-                        const uint32_t s = p * kMaxRecords + cnt;
-                        pg_directional_data rd;
-                        rd.position[0] = x.x;
-                        rd.position[1] = x.y;
-                        rd.position[2] = x.z;
-                        rd.direction[0] = wo.x;
-                        rd.direction[1] = wo.y;
-                        rd.direction[2] = wo.z;
-                        rd.weight = 0.0f;
-                        rd.pdf = pdf;
-                        rd.distance = 0.0f;
-                        if (delta || almost_delta(m)) {
-                            rd.flags = PG_INVALID_REGION;
-                        } else {
-                            rd.flags = region_of(R.guide, x);
-                            R.rec_pending[p] = (int32_t)cnt;
-                            R.rec_factor[p] = 1.0f;
-                        }
-                        R.rec[s] = rd;
-                        st3(R.rec_lsum, s, mk(0, 0, 0));
-                        st3(R.rec_tc, s, tc);
-                        R.rec_count[p] = cnt + 1;
-                    } else if (R.rec_pending[p] >= 0 && m.type == PG_MAT_DIELECTRIC && dot3(wo, n) < 0.0f) {
-                        const float eta = front ? m.ior : 1.0f / m.ior;
-                        R.rec_factor[p] = fabsf(dot3(n, d) / dot3(n, wo)) * eta;
-                    }
+            if (!ic_end) {
+                const float uch = rnd(R.rp.seed, p, R.sample, dimb(b, 3));
+                const float ul = rnd(R.rp.seed, p, R.sample, dimb(b, 4));
+                const float u1 = rnd(R.rp.seed, p, R.sample, dimb(b, 5)), u2 = rnd(R.rp.seed, p, R.sample, dimb(b, 6));
+                const bool gm = R.guiding && guided_material(m, R.rp.flags);
+                const pg_vmm_theta *mix = nullptr;
+                if (gm) {
+                    const uint32_t reg = region_of(R.guide, x);
+                    if (reg != PG_INVALID_REGION) mix = &R.guide.vmm[reg];
                 }
-                st3(R.ro, p, x);
-                st3(R.rd, p, wo);
-                st3(R.thr, p, thr);
-                R.prev_pdf[p] = delta ? 0.0f : pdf;
+                const Continuation cn = continue_path(m, d, n, front, x, gm, mix, R.guide.use_parallax,
+                                                      R.rp.guiding_prob, uch, ul, u1, u2,
+                                                      [&] { return rnd(R.rp.seed, p, R.sample, dimb(b, 7)); });
+                const V wo = cn.wo, tc = cn.tc;
+                const float pdf = cn.pdf;
+                const bool delta = cn.delta;
+                if (pdf > 0.0f && maxc(tc) > 0.0f) {
+                    thr = hmul(thr, tc);
+                    cont = true;
+                    // guiding record of this vertex (raytrace.rgen:1179-1200)
+                    if (rec_on) {
+                        const uint32_t cnt = R.rec_count[p];
+                        if (cnt < (uint32_t)kMaxRecords) {
+                            const uint32_t s = p * kMaxRecords + cnt;
+                            pg_directional_data rd;
+                            rd.position[0] = x.x;
+                            rd.position[1] = x.y;
+                            rd.position[2] = x.z;
+                            rd.direction[0] = wo.x;
+                            rd.direction[1] = wo.y;
+                            rd.direction[2] = wo.z;
+                            rd.weight = 0.0f;
+                            rd.pdf = pdf;
+                            rd.distance = 0.0f;
+                            if (delta || almost_delta(m)) {
+                                rd.flags = PG_INVALID_REGION;
+                            } else {
+                                rd.flags = region_of(R.guide, x);
+                                R.rec_pending[p] = (int32_t)cnt;
+                                R.rec_factor[p] = 1.0f;
+                            }
+                            R.rec[s] = rd;
+                            st3(R.rec_lsum, s, mk(0, 0, 0));
+                            st3(R.rec_tc, s, tc);
+                            R.rec_count[p] = cnt + 1;
+                        } else if (R.rec_pending[p] >= 0 && m.type == PG_MAT_DIELECTRIC && dot3(wo, n) < 0.0f) {
+                            const float eta = front ? m.ior : 1.0f / m.ior;
+                            R.rec_factor[p] = fabsf(dot3(n, d) / dot3(n, wo)) * eta;
+                        }
+                    }
+                    st3(R.ro, p, x);
+                    st3(R.rd, p, wo);
+                    st3(R.thr, p, thr);
+                    R.prev_pdf[p] = delta ? 0.0f : pdf;
+                }
             }
         }
     }
@@ -1208,6 +1265,25 @@ struct pg_scene {
     std::vector<void *> bufs;
     DevRender R{};
     uint32_t *d_counters = nullptr;
+    // irradiance cache
+    struct IcStore {
+        bool on = false;
+        pg_irradiance_cache_config cfg{};
+        pg_ic_entry *entries = nullptr;   // capacity
+        uint32_t *state = nullptr;        // 4 words (DevIc::state)
+        uint32_t *cell_start = nullptr;   // kIcCells + 1
+        uint32_t *cell_count = nullptr;   // kIcCells
+        uint32_t *cell_fill = nullptr;    // kIcCells
+        uint32_t *refs = nullptr;
+        uint32_t cap_refs = 0;
+        IcRequest *requests = nullptr;    // req_cap
+        IcResult *results = nullptr;      // req_cap
+        float4 *samples = nullptr;        // req_cap x 200
+        uint32_t req_cap = 0;
+        uint8_t *created = nullptr;       // per pixel
+        uint32_t cap_created = 0;
+        bool grid_stale = true;
+    } ic;
 };
 
 namespace {
@@ -1409,6 +1485,147 @@ DevScene dev_scene(const pg_scene *sc) {
     return S;
 }
 
+// The state a render call shares with the cache's paths: the scene, the
+// camera basis, the settings and the guide.  Path buffers are left as they are.
+int setup_render(pg_scene *sc, const pg_render_params *rp, pg_ctx *guide, cudaStream_t s, DevRender &R) {
+    R.S = dev_scene(sc);
+    R.pos = sc->d_pos;
+    R.idx = sc->d_idx;
+    R.tri_mat = sc->d_tri_mat;
+    R.mats = sc->d_mats;
+    R.lights = sc->d_lights;
+    R.n_lights = sc->n_lights;
+    R.light_tris = sc->d_light_tris;
+    R.light_cdf = sc->d_light_cdf;
+    R.tri_light = sc->d_tri_light;
+    R.env = sc->d_env;
+    R.env_w = sc->host.env_w;
+    R.env_h = sc->host.env_h;
+    const pg_camera cam = sc->host.camera;
+    R.cam = cam;
+    {
+        float f[3] = {cam.target[0] - cam.origin[0], cam.target[1] - cam.origin[1], cam.target[2] - cam.origin[2]};
+        float l = sqrtf(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+        for (int i = 0; i < 3; ++i) f[i] /= l;
+        float r[3] = {f[1] * cam.up[2] - f[2] * cam.up[1], f[2] * cam.up[0] - f[0] * cam.up[2],
+                      f[0] * cam.up[1] - f[1] * cam.up[0]};
+        l = sqrtf(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+        for (int i = 0; i < 3; ++i) r[i] /= l;
+        const float u[3] = {r[1] * f[2] - r[2] * f[1], r[2] * f[0] - r[0] * f[2], r[0] * f[1] - r[1] * f[0]};
+        for (int i = 0; i < 3; ++i) {
+            R.cam_fwd[i] = f[i];
+            R.cam_right[i] = r[i];
+            R.cam_up[i] = u[i];
+        }
+        R.tan_half = tanf(cam.vfov_deg * 0.5f * 3.14159265f / 180.0f);
+    }
+    R.rp = *rp;
+    R.S.alpha_salt = alpha_salt(rp->seed);
+    R.guiding = rp->use_guiding ? 1 : 0;
+    R.recording = rp->record_samples ? 1 : 0;
+    memset(&R.guide, 0, sizeof R.guide);
+    if (guide) {
+        GuideView gv;
+        const int st = guide_view(guide, &gv, s);
+        if (st) return scene_error(st, pg_last_error(guide));
+        for (int i = 0; i < 6; ++i) R.guide.root[i] = gv.root[i];
+        R.guide.split_count = gv.split_count;
+        R.guide.nodes = gv.nodes;
+        R.guide.vmm = gv.vmm;
+        R.guide.use_parallax = gv.use_parallax;
+    }
+    memset(&R.ic, 0, sizeof R.ic);
+    return PG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Irradiance cache (host side)
+// ---------------------------------------------------------------------------
+constexpr uint32_t kIcRequestCap = 16384;  // requests one pass can queue
+
+void ic_free(pg_scene::IcStore &c) {
+    cudaFree(c.entries);
+    cudaFree(c.state);
+    cudaFree(c.cell_start);
+    cudaFree(c.cell_count);
+    cudaFree(c.cell_fill);
+    cudaFree(c.refs);
+    cudaFree(c.requests);
+    cudaFree(c.results);
+    cudaFree(c.samples);
+    cudaFree(c.created);
+    c = pg_scene::IcStore{};
+}
+
+// The device view of the scene's cache; the grid spans the scene box.
+void ic_view(const pg_scene *sc, DevIc &D) {
+    const auto &c = sc->ic;
+    memset(&D, 0, sizeof D);
+    D.entries = c.entries;
+    D.cell_start = c.cell_start;
+    D.cell_refs = c.refs;
+    D.cap_refs = c.cap_refs;
+    for (int i = 0; i < 3; ++i) {
+        const float lo = sc->aabb[i], hi = sc->aabb[3 + i];
+        const float ext = hi - lo, margin = 1e-3f * std::max(ext, 1e-3f);
+        D.lo[i] = lo - margin;
+        D.inv_cell[i] = (float)kIcGrid / (ext + 2.0f * margin);
+    }
+    D.a = c.cfg.a;
+    D.min_radius = c.cfg.min_radius;
+    D.create_prob = c.cfg.create_prob;
+    D.update_prob = c.cfg.update_prob;
+    D.grad_max = c.cfg.gradients_max_length;
+    D.use_gradients = c.cfg.use_gradients ? 1 : 0;
+    D.visibility = c.cfg.visibility_check ? 1 : 0;
+    D.on_glossy = c.cfg.use_on_glossy ? 1 : 0;
+    D.requests = c.requests;
+    D.req_cap = c.req_cap;
+    D.capacity = c.cfg.capacity;
+    D.created = c.created;
+    D.state = c.state;
+}
+
+uint32_t sm_count() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return (uint32_t)std::max(1, sms);
+}
+
+// Rebuilds the cell lists over the current entries (all on the stream).
+int ic_build_grid(pg_scene *sc, const DevIc &D, cudaStream_t s) {
+    auto &c = sc->ic;
+    if (cudaMemsetAsync(c.cell_count, 0, sizeof(uint32_t) * kIcCells, s) != cudaSuccess ||
+        cudaMemsetAsync(c.cell_fill, 0, sizeof(uint32_t) * kIcCells, s) != cudaSuccess)
+        return scene_error(PG_ERR_CUDA, "irradiance cache grid reset");
+    const uint32_t G = std::min((c.cfg.capacity + 127) / 128, 4u * sm_count());
+    k_ic_grid_count<<<G, 128, 0, s>>>(D, c.cell_count);
+    k_ic_grid_scan<<<1, 1024, 0, s>>>(c.cell_count, c.cell_start);
+    k_ic_grid_fill<<<G, 128, 0, s>>>(D, c.cell_start, c.cell_fill, c.refs);
+    k_ic_grid_sort<<<kIcCells / 128, 128, 0, s>>>(c.cell_start, c.refs, c.cap_refs);
+    if (cudaGetLastError() != cudaSuccess) return scene_error(PG_ERR_CUDA, "irradiance cache grid launch failed");
+    c.grid_stale = false;
+    return PG_OK;
+}
+
+// After a sample pass: the queued requests' entries computed and written, the
+// grid rebuilt.  No host synchronization.
+int ic_process(pg_scene *sc, const DevRender &R, cudaStream_t s) {
+    auto &c = sc->ic;
+    const DevIc &D = R.ic;
+    const uint32_t sms = sm_count();
+    const uint32_t gq = (c.req_cap + 127) / 128;
+    k_ic_assign<<<gq, 128, 0, s>>>(D);
+    k_ic_paths<<<8 * sms, 128, 0, s>>>(R, c.samples);
+    k_ic_reduce<<<std::min((c.req_cap + 3) / 4, 8 * sms), 128, 0, s>>>(R, c.samples, c.results);
+    k_ic_slots<<<gq, 128, 0, s>>>(D, c.results);
+    k_ic_commit<<<gq, 128, 0, s>>>(D, c.results);
+    k_ic_finish<<<1, 1, 0, s>>>(D);
+    if (cudaGetLastError() != cudaSuccess) return scene_error(PG_ERR_CUDA, "irradiance cache launch failed");
+    return ic_build_grid(sc, D, s);
+}
+
 int create_common(pg_scene *sc, pg_scene **out) {
     build_host(sc);
     *out = sc;
@@ -1524,8 +1741,164 @@ int pg_scene_destroy(pg_scene *sc) {
     cudaFree(sc->d_stats);
     cudaFree(sc->d_counters);
     for (void *b : sc->bufs) cudaFree(b);
+    ic_free(sc->ic);
     delete sc;
     return PG_OK;
+}
+
+void pg_default_irradiance_cache_config(pg_irradiance_cache_config *out) {
+    if (!out) return;
+    memset(out, 0, sizeof *out);
+    out->capacity = 100000;
+    out->a = 0.2f;
+    out->min_radius = 0.1f;
+    out->create_prob = 0.0005f;
+    out->update_prob = 0.00001f;
+    out->use_gradients = 0;
+    out->gradients_max_length = 5.0f;
+    out->visibility_check = 0;
+    out->use_on_glossy = 0;
+}
+
+int pg_scene_set_irradiance_cache(pg_scene *sc, const pg_irradiance_cache_config *cfg) {
+    if (!sc || !cfg) return PG_ERR_ARG;
+    if (cfg->capacity > (1u << 24)) return scene_error(PG_ERR_ARG, "irradiance cache capacity above 2^24 entries");
+    if (cfg->capacity && (!(cfg->a > 0.0f) || !std::isfinite(cfg->a) || !(cfg->min_radius >= 0.0f) ||
+                          !(cfg->create_prob >= 0.0f && cfg->create_prob <= 1.0f) ||
+                          !(cfg->update_prob >= 0.0f && cfg->update_prob <= 1.0f) ||
+                          !(cfg->gradients_max_length >= 0.0f)))
+        return scene_error(PG_ERR_ARG, "irradiance cache: a > 0, min_radius >= 0, probabilities in [0, 1], "
+                                       "gradients_max_length >= 0");
+    if (sc->ic.on) cudaDeviceSynchronize();  // a render may still read the old cache
+    ic_free(sc->ic);
+    if (cfg->capacity == 0) return PG_OK;
+    auto &c = sc->ic;
+    c.req_cap = kIcRequestCap;
+    c.cap_refs = std::max(1u << 20, 8u * cfg->capacity);
+    bool ok = cudaMalloc(&c.entries, sizeof(pg_ic_entry) * cfg->capacity) == cudaSuccess &&
+              cudaMalloc(&c.state, 4 * sizeof(uint32_t)) == cudaSuccess &&
+              cudaMalloc(&c.cell_start, sizeof(uint32_t) * (kIcCells + 1)) == cudaSuccess &&
+              cudaMalloc(&c.cell_count, sizeof(uint32_t) * kIcCells) == cudaSuccess &&
+              cudaMalloc(&c.cell_fill, sizeof(uint32_t) * kIcCells) == cudaSuccess &&
+              cudaMalloc(&c.refs, sizeof(uint32_t) * c.cap_refs) == cudaSuccess &&
+              cudaMalloc(&c.requests, sizeof(IcRequest) * c.req_cap) == cudaSuccess &&
+              cudaMalloc(&c.results, sizeof(IcResult) * c.req_cap) == cudaSuccess &&
+              cudaMalloc(&c.samples, sizeof(float4) * kIcSamples * (size_t)c.req_cap) == cudaSuccess;
+    ok = ok && cudaMemset(c.state, 0, 4 * sizeof(uint32_t)) == cudaSuccess &&
+         cudaMemset(c.cell_start, 0, sizeof(uint32_t) * (kIcCells + 1)) == cudaSuccess &&
+         cudaDeviceSynchronize() == cudaSuccess;
+    if (!ok) {
+        ic_free(c);
+        return scene_error(PG_ERR_NOMEM, "irradiance cache: out of device memory");
+    }
+    c.cfg = *cfg;
+    c.on = true;
+    c.grid_stale = false;  // empty lists
+    return PG_OK;
+}
+
+int pg_scene_get_irradiance_cache(pg_scene *sc, pg_ic_entry *out, uint32_t capacity, uint32_t *n_entries) {
+    if (!sc || !n_entries) return PG_ERR_ARG;
+    *n_entries = 0;
+    if (!sc->ic.on) return PG_OK;
+    uint32_t st[4];
+    if (cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(st, sc->ic.state, sizeof st, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return scene_error(PG_ERR_CUDA, "irradiance cache read");
+    *n_entries = st[2];
+    if (out && st[2]) {
+        if (capacity < st[2]) return scene_error(PG_ERR_ARG, "irradiance cache: output holds fewer entries than the cache");
+        if (cudaMemcpy(out, sc->ic.entries, sizeof(pg_ic_entry) * st[2], cudaMemcpyDeviceToHost) != cudaSuccess)
+            return scene_error(PG_ERR_CUDA, "irradiance cache read");
+    }
+    return PG_OK;
+}
+
+int pg_scene_set_irradiance_cache_entries(pg_scene *sc, const pg_ic_entry *entries, uint32_t n) {
+    if (!sc || (n && !entries)) return PG_ERR_ARG;
+    if (!sc->ic.on) return scene_error(PG_ERR_ARG, "no irradiance cache on the scene (pg_scene_set_irradiance_cache)");
+    if (n > sc->ic.cfg.capacity) return scene_error(PG_ERR_ARG, "more entries than the cache's capacity");
+    const uint32_t st[4] = {0, 0, n, 0};
+    if (cudaDeviceSynchronize() != cudaSuccess ||
+        (n && cudaMemcpy(sc->ic.entries, entries, sizeof(pg_ic_entry) * n, cudaMemcpyHostToDevice) != cudaSuccess) ||
+        cudaMemcpy(sc->ic.state, st, sizeof st, cudaMemcpyHostToDevice) != cudaSuccess)
+        return scene_error(PG_ERR_CUDA, "irradiance cache write");
+    sc->ic.grid_stale = true;
+    // grow the reference list to what the grid will need
+    DevIc D;
+    ic_view(sc, D);
+    if (int st2 = ic_build_grid(sc, D, nullptr)) return st2;
+    uint32_t total = 0;
+    if (cudaMemcpy(&total, sc->ic.cell_start + kIcCells, sizeof total, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return scene_error(PG_ERR_CUDA, "irradiance cache grid size");
+    if (total > sc->ic.cap_refs) {
+        cudaFree(sc->ic.refs);
+        sc->ic.refs = nullptr;
+        const uint64_t want = std::min<uint64_t>(2ull * total, 0xFFFFFFF0ull);
+        if (cudaMalloc(&sc->ic.refs, sizeof(uint32_t) * want) != cudaSuccess) {
+            sc->ic.cap_refs = 0;
+            sc->ic.grid_stale = true;
+            return scene_error(PG_ERR_NOMEM, "irradiance cache grid: out of device memory");
+        }
+        sc->ic.cap_refs = (uint32_t)want;
+        ic_view(sc, D);
+        if (int st2 = ic_build_grid(sc, D, nullptr)) return st2;
+    }
+    return cudaDeviceSynchronize() == cudaSuccess ? PG_OK : scene_error(PG_ERR_CUDA, "irradiance cache grid build");
+}
+
+int pg_ic_query(pg_scene *sc, const float *positions, const float *normals, uint32_t n, float *rgb, uint32_t *found,
+                void *stream) {
+    if (!sc || (n && (!positions || !normals || !rgb || !found))) return PG_ERR_ARG;
+    if (!sc->ic.on) return scene_error(PG_ERR_ARG, "no irradiance cache on the scene (pg_scene_set_irradiance_cache)");
+    if (n == 0) return PG_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    DevIc D;
+    ic_view(sc, D);
+    if (sc->ic.grid_stale)
+        if (int st = ic_build_grid(sc, D, s)) return st;
+    k_ic_query_probe<<<(n + 127) / 128, 128, 0, s>>>(D, positions, normals, n, rgb, found);
+    return cudaGetLastError() == cudaSuccess ? PG_OK : scene_error(PG_ERR_CUDA, "irradiance cache query launch");
+}
+
+int pg_ic_compute(pg_scene *sc, const pg_render_params *rp, pg_ctx *guide, const pg_ic_request *requests, uint32_t n,
+                  pg_ic_entry *out, void *stream) {
+    if (!sc || !rp || (n && (!requests || !out))) return PG_ERR_ARG;
+    if (!sc->ic.on) return scene_error(PG_ERR_ARG, "no irradiance cache on the scene (pg_scene_set_irradiance_cache)");
+    if (rp->use_guiding && !guide) return scene_error(PG_ERR_ARG, "guiding needs a guiding context");
+    if (n > 65536u) return scene_error(PG_ERR_ARG, "at most 65536 requests per call");
+    if (n == 0) return PG_OK;
+    if (int st = ensure_uploaded(sc)) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    DevRender R{};
+    if (int st = setup_render(sc, rp, guide, s, R)) return st;
+    ic_view(sc, R.ic);
+    R.ic.query = 1;
+    if (sc->ic.grid_stale)
+        if (int st = ic_build_grid(sc, R.ic, s)) return st;
+    IcRequest *req = nullptr;
+    float4 *smp = nullptr;
+    uint32_t *state = nullptr;
+    const uint32_t st_host[4] = {n, 0, 0, 0};
+    bool ok = cudaMalloc(&req, sizeof(IcRequest) * n) == cudaSuccess &&
+              cudaMalloc(&smp, sizeof(float4) * kIcSamples * (size_t)n) == cudaSuccess &&
+              cudaMalloc(&state, sizeof st_host) == cudaSuccess &&
+              cudaMemcpyAsync(state, st_host, sizeof st_host, cudaMemcpyHostToDevice, s) == cudaSuccess;
+    if (ok) {
+        R.ic.requests = req;
+        R.ic.req_cap = n;
+        R.ic.state = state;
+        R.ic.grow = 0;
+        const uint32_t sms = sm_count();
+        k_ic_load_requests<<<(n + 127) / 128, 128, 0, s>>>(requests, n, req);
+        k_ic_paths<<<8 * sms, 128, 0, s>>>(R, smp);
+        k_ic_compute_probe_reduce<<<std::min((n + 3) / 4, 8 * sms), 128, 0, s>>>(R, smp, n, out);
+        ok = cudaGetLastError() == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
+    }
+    cudaFree(req);
+    cudaFree(smp);
+    cudaFree(state);
+    return ok ? PG_OK : scene_error(PG_ERR_CUDA, "irradiance cache compute");
 }
 
 int pg_scene_texture_sizes(const pg_scene *sc, uint32_t *n_textures, uint64_t *n_texels) {
@@ -1704,53 +2077,26 @@ int pg_render(pg_scene *sc, const pg_render_params *rp, pg_ctx *guide, float *im
         sc->cap_pix = P;
     }
     DevRender R = sc->R;
-    R.S = dev_scene(sc);
-    R.pos = sc->d_pos;
-    R.idx = sc->d_idx;
-    R.tri_mat = sc->d_tri_mat;
-    R.mats = sc->d_mats;
-    R.lights = sc->d_lights;
-    R.n_lights = sc->n_lights;
-    R.light_tris = sc->d_light_tris;
-    R.light_cdf = sc->d_light_cdf;
-    R.tri_light = sc->d_tri_light;
-    R.env = sc->d_env;
-    R.env_w = sc->host.env_w;
-    R.env_h = sc->host.env_h;
-    R.cam = cam;
-    {
-        float f[3] = {cam.target[0] - cam.origin[0], cam.target[1] - cam.origin[1], cam.target[2] - cam.origin[2]};
-        float l = sqrtf(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
-        for (int i = 0; i < 3; ++i) f[i] /= l;
-        float r[3] = {f[1] * cam.up[2] - f[2] * cam.up[1], f[2] * cam.up[0] - f[0] * cam.up[2],
-                      f[0] * cam.up[1] - f[1] * cam.up[0]};
-        l = sqrtf(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
-        for (int i = 0; i < 3; ++i) r[i] /= l;
-        const float u[3] = {r[1] * f[2] - r[2] * f[1], r[2] * f[0] - r[0] * f[2], r[0] * f[1] - r[1] * f[0]};
-        for (int i = 0; i < 3; ++i) {
-            R.cam_fwd[i] = f[i];
-            R.cam_right[i] = r[i];
-            R.cam_up[i] = u[i];
-        }
-        R.tan_half = tanf(cam.vfov_deg * 0.5f * 3.14159265f / 180.0f);
-    }
-    R.rp = *rp;
-    R.S.alpha_salt = alpha_salt(rp->seed);
+    if (int st = setup_render(sc, rp, guide, s, R)) return st;
     R.image = image;
     R.counters = sc->d_counters;
-    R.guiding = rp->use_guiding ? 1 : 0;
-    R.recording = rp->record_samples ? 1 : 0;
     R.rec = records;
-    memset(&R.guide, 0, sizeof R.guide);
-    if (guide) {
-        GuideView gv;
-        const int st = guide_view(guide, &gv, s);
-        if (st) return scene_error(st, pg_last_error(guide));
-        for (int i = 0; i < 6; ++i) R.guide.root[i] = gv.root[i];
-        R.guide.split_count = gv.split_count;
-        R.guide.nodes = gv.nodes;
-        R.guide.vmm = gv.vmm;
-        R.guide.use_parallax = gv.use_parallax;
+    const bool ic_on = (rp->flags & PG_RENDER_IRRADIANCE_CACHE) != 0;
+    if (ic_on) {
+        auto &c = sc->ic;
+        if (!c.on) return scene_error(PG_ERR_ARG, "PG_RENDER_IRRADIANCE_CACHE needs a cache (pg_scene_set_irradiance_cache)");
+        if (P > c.cap_created) {
+            cudaFree(c.created);
+            c.created = nullptr;
+            c.cap_created = 0;
+            if (cudaMalloc(&c.created, P) != cudaSuccess) return scene_error(PG_ERR_NOMEM, "irradiance cache pixel counters");
+            c.cap_created = P;
+        }
+        ic_view(sc, R.ic);
+        R.ic.query = 1;
+        R.ic.grow = !(rp->flags & PG_RENDER_IC_FROZEN) && (c.cfg.create_prob > 0.0f || c.cfg.update_prob > 0.0f);
+        if (c.grid_stale)
+            if (int st = ic_build_grid(sc, R.ic, s)) return st;
     }
     if (cudaMemsetAsync(sc->d_counters, 0, sizeof(uint32_t) * 16, s) != cudaSuccess)
         return scene_error(PG_ERR_CUDA, "counter reset");
@@ -1808,6 +2154,29 @@ int pg_render(pg_scene *sc, const pg_render_params *rp, pg_ctx *guide, float *im
             tm.begin(PG_STAGE_COMMIT);
             k_commit<<<G, T, 0, s>>>(R, P);
             tm.end();
+        }
+        if (R.ic.grow)
+            if (int st = ic_process(sc, Rb, s)) return st;
+    }
+    if (R.ic.grow) {
+        // grow the grid's reference list if the last build did not fit in it
+        auto &c = sc->ic;
+        uint32_t total = 0;
+        if (cudaMemcpyAsync(&total, c.cell_start + kIcCells, sizeof total, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return scene_error(PG_ERR_CUDA, "irradiance cache grid size");
+        if (total > c.cap_refs) {
+            cudaFree(c.refs);
+            c.refs = nullptr;
+            const uint64_t want = std::min<uint64_t>(2ull * total, 0xFFFFFFF0ull);
+            if (cudaMalloc(&c.refs, sizeof(uint32_t) * want) != cudaSuccess) {
+                c.cap_refs = 0;
+                c.grid_stale = true;
+                return scene_error(PG_ERR_NOMEM, "irradiance cache grid: out of device memory");
+            }
+            c.cap_refs = (uint32_t)want;
+            ic_view(sc, R.ic);
+            if (int st = ic_build_grid(sc, R.ic, s)) return st;
         }
     }
     if (cudaGetLastError() != cudaSuccess) return scene_error(PG_ERR_CUDA, "render launch failed");
