@@ -18,6 +18,7 @@ back.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import subprocess
@@ -359,6 +360,81 @@ def bench_tracer(pkg, abi, torch, stream, steps: int, warmup: int, cpu: bool, sc
         out["cpu_baseline"] = {k: v for k, v in cb.items() if k != "seconds"}
         if scene == "cornell":
             out["image_vs_fp64"] = image_relmse_vs_fp64(pkg, abi, torch, stream, sc, params)
+    sc.close()
+    return out
+
+
+IC_WORKLOAD = ("irradiance cache and ADRRS on the tracer's Cornell box (1280x720, depth 8, NEE + MIS): the "
+               "reference's 50 prepare frames of 1 spp growing the cache (IC_SIZE 100000, irradianceA 0.2, create "
+               "0.0005, update 0.00001, min radius 0.1), then 16-spp frames querying it (paths end at the cache), "
+               "and ADRRS (weight window s 5, splitting) against a 16-spp estimate; relMSE against a 4096-spp "
+               "plain render")
+
+
+def bench_irradiance(pkg, abi, torch, stream, ref_spp: int = 4096):
+    """The irradiance cache's cost and effect: prepare frames (a 1-spp frame
+    plus the cache's entry computation and grid rebuild after it), frames
+    that end paths at the cache, ADRRS frames; each with its relMSE against a
+    converged plain render and the plain frame's relMSE at equal time."""
+    guiding = entry.load_submodule("guiding")
+    sc = pkg.Scene.cornell(1280, 720, ico_level=5)
+    info = sc.info()
+    P = info.camera.width * info.camera.height
+    depth, spp = 8, 16
+    img = torch.zeros(P * 3, dtype=torch.float32, device="cuda")
+
+    def timed(params, frames=1):
+        img.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for f in range(frames):
+                params.seed = params.seed + 1
+                sc.render(params, img, stream=stream, stats=False)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / frames
+
+    ref_params = abi.render_params(spp=ref_spp, max_depth=depth, seed=424242)
+    img.zero_()
+    with torch.cuda.stream(stream):
+        sc.render(ref_params, img, stream=stream, stats=False)
+    torch.cuda.synchronize()
+    ref = img.cpu().numpy().reshape(-1, 3).astype(np.float64) / ref_spp
+
+    def relmse(spp_):
+        a = img.cpu().numpy().reshape(-1, 3).astype(np.float64) / spp_
+        return float(((a - ref) ** 2 / (ref * ref + 1e-2)).mean())
+
+    out = {"metric": "irradiance cache and ADRRS frame times and relMSE", "config": {"workload": IC_WORKLOAD}}
+    plain_ms = timed(abi.render_params(spp=1, max_depth=depth, seed=1))
+    cfg = abi.IrradianceCacheConfig()
+    sc.lib.pg_default_irradiance_cache_config(ctypes.byref(cfg))
+    sc.set_irradiance_cache(cfg)
+    prep = abi.render_params(spp=1, max_depth=depth, seed=10, flags=abi.PG_RENDER_IRRADIANCE_CACHE)
+    prep_ms = timed(prep, guiding.IRRADIANCE_PREPARE_FRAMES)
+    n_entries = len(sc.irradiance_cache())
+    out["prepare_frames"] = {"frames": guiding.IRRADIANCE_PREPARE_FRAMES, "ms_per_frame": prep_ms,
+                             "plain_1spp_frame_ms": plain_ms, "entries_after": n_entries,
+                             "note": "a prepare frame is a 1-spp frame plus the entries it queued (20 x 10 "
+                                     "hemisphere paths each) and the grid rebuild; it synchronizes once at the end"}
+    rows = {}
+    for name, flags in (("plain", 0), ("cache", abi.PG_RENDER_IRRADIANCE_CACHE | abi.PG_RENDER_IC_FROZEN)):
+        ms = timed(abi.render_params(spp=spp, max_depth=depth, seed=2000, flags=flags))
+        rows[name] = {"ms": ms, "relmse": relmse(spp)}
+    # ADRRS: the estimate frame, then frames with roulette and splitting
+    est = guiding.adrrs_estimate(sc, stream=stream)
+    for name, split in (("adrrs_rr", False), ("adrrs_split", True)):
+        sc.set_adrrs(est, s=5.0, split=split)
+        ms = timed(abi.render_params(spp=spp, max_depth=depth, seed=3000, flags=abi.PG_RENDER_ADRRS))
+        rows[name] = {"ms": ms, "relmse": relmse(spp)}
+    # equal time: relMSE x time (lower is better), relative to the plain frame
+    base = rows["plain"]["ms"] * rows["plain"]["relmse"]
+    for r in rows.values():
+        r["time_x_relmse_vs_plain"] = r["ms"] * r["relmse"] / base
+    out["frames_16spp"] = rows
+    out["reference"] = f"plain NEE+MIS, {ref_spp} spp"
     sc.close()
     return out
 
@@ -948,6 +1024,7 @@ def main():
                     if args.scene == "both":
                         line["plates"] = bench_tracer(pkg, abi, torch, stream, min(args.steps, 5), 2, cpu=False,
                                                       scene="plates")
+                        line["irradiance_cache"] = bench_irradiance(pkg, abi, torch, stream)
             elif args.workload == "surrogate":
                 line = bench_surrogate(pkg, abi, torch, stream)
             else:
@@ -1142,6 +1219,11 @@ def main():
             tp = bench_tracer(pkg, abi, torch, stream, min(args.steps, 5), 2, cpu=False, scene="plates")
         tp["clocks"] = psampler.summary()
         line["tracer_plates"] = tp
+        isampler = ClockSampler(local)
+        with isampler:
+            ic = bench_irradiance(pkg, abi, torch, stream)
+        ic["clocks"] = isampler.summary()
+        line["irradiance_cache"] = ic
         gsampler = ClockSampler(local)
         with gsampler:
             gd = bench_guided(pkg, abi, torch, stream)

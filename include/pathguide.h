@@ -540,6 +540,19 @@ typedef struct pg_render_params {
 /* With PG_RENDER_IRRADIANCE_CACHE: query the cache only (no creation, no
  * update, no synchronization). */
 #define PG_RENDER_IC_FROZEN 16u
+/* ADRRS, adjoint-driven Russian roulette and splitting (raytrace.rgen:830-869,
+ * 883-902, 1080-1117, 1684-1708): at a cache-capable vertex after the first bounce
+ * where the scene's irradiance cache applies, the path's throughput is
+ * compared with a weight window centred on |estimate / cached irradiance|
+ * (estimate: the pixel's value from pg_scene_set_adrrs).  Below the window
+ * the path continues with probability max(v / lower, 0.1) and its
+ * throughput is divided by it; above it, with split set, it is split into
+ * about v / upper copies (at most 10 copies per pixel and pass) that share
+ * the throughput and continue independently.  The cache is only read (a path
+ * does not end at it).  Requires a cache and an estimate on the scene; not
+ * with record_samples when splitting (the reference collects no samples
+ * then either). */
+#define PG_RENDER_ADRRS 32u
 
 enum pg_render_stage {
     PG_STAGE_CAMERA = 0, PG_STAGE_EXTEND, PG_STAGE_SHADE, PG_STAGE_SHADOW, PG_STAGE_ADVANCE, PG_STAGE_COMMIT,
@@ -653,6 +666,21 @@ int pg_scene_get_irradiance_cache(pg_scene *scene, pg_ic_entry *out, uint32_t ca
  * the round-robin update position. */
 int pg_scene_set_irradiance_cache_entries(pg_scene *scene, const pg_ic_entry *entries, uint32_t n);
 
+/* ADRRS settings (src/RayTracingApp.h:111-113).  estimate: a device array
+ * of width * height * 3 floats for the scene's camera, each pixel's mean
+ * radiance (the reference renders it with its estimate settings,
+ * src/RayTracingApp.cpp:1206-1217), owned by the caller and read by every
+ * render with PG_RENDER_ADRRS until replaced.  s: the window's ratio
+ * upper / lower (adrrsS, default 5).  split: split paths above the window
+ * (adrrsSplit, default 1). */
+typedef struct pg_adrrs_config {
+    const float *estimate;
+    float s;
+    uint32_t split;
+    uint32_t reserved[4];
+} pg_adrrs_config;
+int pg_scene_set_adrrs(pg_scene *scene, const pg_adrrs_config *cfg);
+
 /* Cache queries at n points with their surface normals (device arrays, 3
  * floats each): rgb the weighted mean of the applicable entries
  * (queryIrradianceCache, raytrace.rgen:748-773), found 1 where one applied. */
@@ -715,6 +743,9 @@ int pg_render(pg_scene *scene, const pg_render_params *params, pg_ctx *guide, fl
  *                               (u = choice, lobe/ul, u1, u2, lobe choice; c = guiding prob;
  *                               result: direction, pdf, throughput change)
  *   PG_PROBE_TO_WORLD           toWorld(wo, n)                          transform.glsl:7-38
+ *   PG_PROBE_WEIGHT_WINDOW      applyWeightWindow(throughput = wi, adjoint = wo, estimate = x,
+ *                               s = a, rounding number u[0]): v[0] = q, v[1] = n   raytrace.rgen:830-869
+ *   PG_PROBE_APPROX_DIFFUSE     approxDiffuse(material, n, wi)          raytrace.rgen:815-828
  * (* the library's BSDF value includes the cosine, as evalBsdf's does.)
  * flags: bit 0 front face, bit 1 parallax re-aiming, bit 2 the vertex is
  * guided, bit 3 its region exists (else the path ends), bit 4 the guide-all
@@ -723,7 +754,8 @@ int pg_render(pg_scene *scene, const pg_render_params *params, pg_ctx *guide, fl
  * writes NaN results. */
 enum {
     PG_PROBE_FRESNEL = 0, PG_PROBE_FRESNEL_CONDUCTOR = 1, PG_PROBE_BSDF_EVAL = 2, PG_PROBE_BSDF_SAMPLE = 3,
-    PG_PROBE_VMM_PDF = 4, PG_PROBE_VMM_SAMPLE = 5, PG_PROBE_CONTINUE = 6, PG_PROBE_TO_WORLD = 7
+    PG_PROBE_VMM_PDF = 4, PG_PROBE_VMM_SAMPLE = 5, PG_PROBE_CONTINUE = 6, PG_PROBE_TO_WORLD = 7,
+    PG_PROBE_WEIGHT_WINDOW = 8, PG_PROBE_APPROX_DIFFUSE = 9
 };
 typedef struct pg_shading_probe {
     int32_t op;

@@ -312,6 +312,38 @@ private:
     cudaStream_t stream_;
 };
 
+// ---------------------------------------------------------------------------
+// IrradianceCache(maxCaches) (src/IrradianceCache.h:33-64): the scene's
+// irradiance cache with the reference's push-constant defaults; entries are
+// made and updated by renders with PG_RENDER_IRRADIANCE_CACHE.
+// ---------------------------------------------------------------------------
+class IrradianceCache {
+public:
+    IrradianceCache(const SceneLoader &scene, uint32_t maxCaches, bool onGlossy = false) : scene_(&scene) {
+        pg_default_irradiance_cache_config(&cfg_);
+        cfg_.capacity = maxCaches;
+        cfg_.use_on_glossy = onGlossy ? 1u : 0u;
+        check(pg_scene_set_irradiance_cache(scene.handle(), &cfg_));
+    }
+    uint32_t size() const {
+        uint32_t n = 0;
+        check(pg_scene_get_irradiance_cache(scene_->handle(), nullptr, 0, &n));
+        return n;
+    }
+    std::vector<pg_ic_entry> entries() const {
+        std::vector<pg_ic_entry> out(size());
+        uint32_t n = 0;
+        check(pg_scene_get_irradiance_cache(scene_->handle(), out.data(), (uint32_t)out.size(), &n));
+        out.resize(n);
+        return out;
+    }
+    const pg_irradiance_cache_config &config() const { return cfg_; }
+
+private:
+    const SceneLoader *scene_;
+    pg_irradiance_cache_config cfg_{};
+};
+
 inline pg_render_params render_params(uint32_t spp, uint32_t max_depth, uint32_t seed, bool guiding = false,
                                       bool record = false, float guiding_prob = 0.5f) {
     pg_render_params p{};

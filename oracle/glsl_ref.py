@@ -59,7 +59,9 @@ class RenderConfig(C.Structure):
     _fields_ = [("spp", C.c_uint32), ("max_depth", C.c_uint32), ("max_follow_discrete", C.c_uint32),
                 ("use_nee", C.c_uint32), ("use_mis", C.c_uint32), ("use_guiding", C.c_uint32),
                 ("guiding_prob", C.c_float), ("use_parallax", C.c_uint32), ("frame_seed", C.c_uint32),
-                ("region_splits", C.c_uint32), ("region_root", C.c_float * 6), ("use_ic", C.c_uint32)]
+                ("region_splits", C.c_uint32), ("region_root", C.c_float * 6), ("use_ic", C.c_uint32),
+                ("use_adrrs", C.c_uint32), ("adrrs_split", C.c_uint32), ("adrrs_s", C.c_float),
+                ("estimate", C.c_void_p)]
 
 
 class IcConfig(C.Structure):
@@ -98,6 +100,7 @@ class GlslRef:
             "glslref_discrete": (i, [p]),
             "glslref_record_path": (u, [u, p, p, p, p, p, p, p]),
             "glslref_weight_window": (f, [p, p, p, f, u, P(C.c_int32), P(u)]),
+            "glslref_approx_diffuse": (None, [p, p, p, p]),
             "glslref_render": (i, [p, P(RenderConfig), p, u, u, i, p]),
             "glslref_ic_set": (i, [p, u, P(IcConfig)]),
             "glslref_ic_get": (u, [p, u, P(u)]),
@@ -223,13 +226,16 @@ class GlslRef:
         return w[:m].copy(), fl[:m].copy()
 
     def render(self, exp: dict, path_length: int, spp: int, frame_seed: int, use_nee=True, use_mis=True,
-               guide: dict | None = None, guiding_prob=0.5, rows=None, threads=None, use_ic=False) -> np.ndarray:
+               guide: dict | None = None, guiding_prob=0.5, rows=None, threads=None, use_ic=False,
+               adrrs: dict | None = None) -> np.ndarray:
         """The reference's estimator (raytrace() and the hit shaders compiled as
         C++) over an exported library scene: radiance sums (H, W, 3).
         path_length is the library's max_depth (paths of at most that many
         segments); the reference's maxDepth counts two fewer (its next-event
         estimation runs at the vertex after maxDepth).  use_ic: query the
-        cache of ic_set at every cache-capable vertex (no entries are made)."""
+        cache of ic_set at every cache-capable vertex (no entries are made).
+        adrrs: {"estimate": (H, W, 3) mean radiance, "s", "split"} - ADRRS
+        with the cache of ic_set."""
         import os
         from oracle.oracle import TraceOracle
         s, keep = TraceOracle.scene(exp)
@@ -239,6 +245,11 @@ class GlslRef:
         cfg = RenderConfig(spp=spp, max_depth=max(path_length - 2, 0), max_follow_discrete=0,
                            use_nee=int(use_nee), use_mis=int(use_mis), use_guiding=int(guide is not None),
                            guiding_prob=guiding_prob, frame_seed=frame_seed, use_ic=int(use_ic))
+        est = None
+        if adrrs is not None:
+            est = np.ascontiguousarray(adrrs["estimate"], dtype=np.float32)
+            cfg.use_adrrs, cfg.adrrs_split, cfg.adrrs_s = 1, int(adrrs["split"]), float(adrrs["s"])
+            cfg.estimate = est.ctypes.data
         vmm = None
         if guide is not None:
             cfg.use_parallax = int(guide["use_parallax"])
@@ -319,6 +330,12 @@ class GlslRef:
         q = np.ascontiguousarray(nrm, dtype=np.float32) if nrm is not None else None
         return self.lib.glslref_ic_create_update(C.byref(s), C.byref(cfg), p.ctypes.data if p is not None else None,
                                                  q.ctypes.data if q is not None else None, updates, seed)
+
+    def approx_diffuse(self, mat: RefMaterial, n, wi) -> np.ndarray:
+        out = np.zeros(3, np.float32)
+        n, wi = self._v(n), self._v(wi)
+        self.lib.glslref_approx_diffuse(C.byref(mat), n.ctypes.data, wi.ctypes.data, out.ctypes.data)
+        return out
 
     def weight_window(self, estimate, throughput, adjoint, s, state):
         """applyWeightWindow: (q, n, numbers drawn)."""

@@ -960,7 +960,8 @@ void pgo_probe_shading(const pg_material *mats, uint32_t n_mats, const pg_vmm_th
         const pg_shading_probe &q = P[i];
         double *r = out + 8 * i;
         for (int k = 0; k < 8; ++k) r[k] = 0.0;
-        const bool uses_mat = q.op == PG_PROBE_BSDF_EVAL || q.op == PG_PROBE_BSDF_SAMPLE || q.op == PG_PROBE_CONTINUE;
+        const bool uses_mat = q.op == PG_PROBE_BSDF_EVAL || q.op == PG_PROBE_BSDF_SAMPLE || q.op == PG_PROBE_CONTINUE ||
+                              q.op == PG_PROBE_APPROX_DIFFUSE;
         const bool uses_vmm = q.op == PG_PROBE_VMM_PDF || q.op == PG_PROBE_VMM_SAMPLE ||
                               (q.op == PG_PROBE_CONTINUE && (q.flags & 8u));
         if ((uses_mat && q.material >= n_mats) || (uses_vmm && q.vmm >= n_vmms)) {
@@ -1017,6 +1018,38 @@ void pgo_probe_shading(const pg_material *mats, uint32_t n_mats, const pg_vmm_th
             case PG_PROBE_TO_WORLD:
                 put(0, to_world(wo, n));
                 break;
+            case PG_PROBE_WEIGHT_WINDOW: {
+                // applyWeightWindow (raytrace.rgen:830-869)
+                const D3 r3 = d3(x.x / wo.x, x.y / wo.y, x.z / wo.z);
+                const double center = sqrt(dot(r3, r3));
+                const double s = q.a, lower = 2.0 * center / (1.0 + s), upper = s * lower;
+                const double v = sqrt(dot(wi, wi));
+                double qq = 1.0;
+                int nn = 1;
+                if (std::isnan(lower) || lower <= 0.0 || (lower <= v && v <= upper)) {
+                    qq = 1.0;
+                } else if (v <= lower) {
+                    qq = std::max(v / lower, 0.1);
+                } else {
+                    qq = v / upper;
+                    nn = (int)qq;
+                    if (q.u[0] > (double)(nn + 1) - qq) ++nn;
+                }
+                r[0] = qq;
+                r[1] = nn;
+                break;
+            }
+            case PG_PROBE_APPROX_DIFFUSE: {
+                // approxDiffuse (raytrace.rgen:815-828); GGX: its tint / pi
+                const pg_material &m = mats[q.material];
+                if (m.type == PG_MAT_BECKMANN) {
+                    const double F = fresnel_conductor(dot(wi, n), m.eta, m.k) / PI;
+                    put(0, d3(F, F, F));
+                } else {
+                    put(0, d3(m.albedo[0] / PI, m.albedo[1] / PI, m.albedo[2] / PI));
+                }
+                break;
+            }
             default:
                 break;
         }

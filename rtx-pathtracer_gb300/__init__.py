@@ -111,6 +111,7 @@ SIGNATURES = {
     "pg_scene_get_irradiance_cache": (_I, [_P, _P, _U32, C.POINTER(_U32)]),
     "pg_scene_set_irradiance_cache_entries": (_I, [_P, _P, _U32]),
     "pg_ic_query": (_I, [_P, _P, _P, _U32, _P, _P, _P]),
+    "pg_scene_set_adrrs": (_I, [_P, C.POINTER(abi.AdrrsConfig)]),
     "pg_ic_compute": (_I, [_P, C.POINTER(abi.RenderParams), _P, _P, _U32, _P, _P]),
 }
 
@@ -674,6 +675,13 @@ class Scene:
             setattr(cfg, k, v)
         self._check(self.lib.pg_scene_set_irradiance_cache(self.h, C.byref(cfg)))
         return cfg
+
+    def set_adrrs(self, estimate_dev, s: float = 5.0, split: bool = True):
+        """The pixel estimate (device float32, H*W*3 mean radiance, kept alive
+        by the caller) and window of PG_RENDER_ADRRS renders."""
+        self._adrrs_estimate = estimate_dev
+        cfg = abi.AdrrsConfig(_dptr(estimate_dev), s, int(split))
+        self._check(self.lib.pg_scene_set_adrrs(self.h, C.byref(cfg)))
 
     def irradiance_cache(self) -> np.ndarray:
         """The cache's entries (IC_ENTRY_DTYPE)."""

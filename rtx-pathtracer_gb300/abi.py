@@ -92,7 +92,7 @@ assert HIT_DTYPE.itemsize == 16 and NODE_DTYPE.itemsize == 128
 
 # shading-function probes (pg_probe_shading)
 PG_PROBE_FRESNEL, PG_PROBE_FRESNEL_CONDUCTOR, PG_PROBE_BSDF_EVAL, PG_PROBE_BSDF_SAMPLE, PG_PROBE_VMM_PDF, \
-    PG_PROBE_VMM_SAMPLE, PG_PROBE_CONTINUE, PG_PROBE_TO_WORLD = range(8)
+    PG_PROBE_VMM_SAMPLE, PG_PROBE_CONTINUE, PG_PROBE_TO_WORLD, PG_PROBE_WEIGHT_WINDOW, PG_PROBE_APPROX_DIFFUSE = range(10)
 PROBE_FRONT, PROBE_PARALLAX, PROBE_GUIDED, PROBE_REGION, PROBE_GUIDE_ALL = 1, 2, 4, 8, 16
 PROBE_DTYPE = np.dtype([("op", "<i4"), ("material", "<u4"), ("vmm", "<u4"), ("flags", "<u4"),
                         ("n", "<f4", (3,)), ("wi", "<f4", (3,)), ("wo", "<f4", (3,)), ("x", "<f4", (3,)),
@@ -175,6 +175,7 @@ PG_RENDER_TIME_STAGES = 2
 PG_RENDER_GUIDE_ALMOST_DISCRETE = 4
 PG_RENDER_IRRADIANCE_CACHE = 8
 PG_RENDER_IC_FROZEN = 16
+PG_RENDER_ADRRS = 32
 STAGES = ("camera", "extend", "shade", "shadow", "advance", "commit")
 
 
@@ -184,6 +185,10 @@ class RenderStats(C.Structure):
                 ("extension_triangle_tests", C.c_uint64), ("shadow_node_visits", C.c_uint64),
                 ("shadow_triangle_tests", C.c_uint64), ("stage_ms", C.c_float * 6),
                 ("stage_launches", C.c_uint32 * 6)]
+
+
+class AdrrsConfig(C.Structure):
+    _fields_ = [("estimate", C.c_void_p), ("s", C.c_float), ("split", C.c_uint32), ("reserved", C.c_uint32 * 4)]
 
 
 class IrradianceCacheConfig(C.Structure):

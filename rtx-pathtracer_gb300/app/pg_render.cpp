@@ -2,9 +2,9 @@
 // facades of pathguiding.hpp.
 //
 // Arguments follow the reference's main (src/main.cpp:8-33): WIDTH HEIGHT
-// IC_SIZE GUIDING_SPLITS SCENE.  IC_SIZE (irradiance cache) is accepted and
-// unused.  SCENE is a Mitsuba-XML file, or "cornell" / "plates" for the
-// procedural scenes.  The frame loop restates RayTracingApp's guiding phase
+// IC_SIZE GUIDING_SPLITS SCENE.  IC_SIZE is the irradiance cache's capacity,
+// used with --irradiance-cache or --adrrs.  SCENE is a Mitsuba-XML file, or
+// "cornell" / "plates" for the procedural scenes.  The frame loop restates RayTracingApp's guiding phase
 // (src/RayTracingApp.cpp:125-157): numGuidingOptimizations training frames
 // that record samples and call PathGuiding::update, each accumulated into the
 // image, then the remaining samples with guiding.  The mean radiance is
@@ -15,13 +15,18 @@
 // Options: --spp N (final guided samples, default 64), --train LIST (training
 // samples per frame, default 1,2,4,8,16,32), --depth N (10), --seed N (1),
 // --prob P (guiding probability 0.5), --no-guiding (plain NEE + MIS with the
-// same total samples), --no-parallax, --no-split-merge, --out FILE.
+// same total samples), --no-parallax, --no-split-merge, --out FILE,
+// --irradiance-cache (the cache's prepare frames, then every frame queries
+// and grows it), --adrrs (prepare frames on glossy surfaces too, the
+// estimate frame, then adjoint-driven roulette and splitting,
+// src/RayTracingApp.cpp:1129-1170, 1206-1217), --prepare-frames N (50).
 #include <cuda_runtime.h>
 
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -57,7 +62,7 @@ bool write_pfm(const std::string &path, const std::vector<float> &rgb, uint32_t 
 int usage() {
     fprintf(stderr, "Required parameters: WIDTH HEIGHT IC_SIZE GUIDING_SPLITS SCENE [--spp N] [--train LIST] "
                     "[--depth N] [--seed N] [--prob P] [--no-guiding] [--no-parallax] [--no-split-merge] "
-                    "[--split-regions SAMPLES] [--out FILE]\n");
+                    "[--split-regions SAMPLES] [--out FILE] [--irradiance-cache] [--adrrs] [--prepare-frames N]\n");
     return EXIT_FAILURE;
 }
 
@@ -70,7 +75,8 @@ int main(int argc, char **argv) {
     const std::string scene_arg = argv[5];
     uint32_t spp = 64, depth = 10, seed = 1;
     float prob = 0.5f;
-    bool guiding = true, parallax = true, split_merge = true;
+    bool guiding = true, parallax = true, split_merge = true, use_ic = false, adrrs = false;
+    uint32_t prepare_frames = 50;  // irradianceCachePrepareFrames (src/RayTracingApp.h:175)
     float split_regions = 0.0f;  // samplesForRegionSplit; 0: regions are not split (the reference's default)
     std::vector<uint32_t> train = {1, 2, 4, 8, 16, 32};
     std::string out;
@@ -87,9 +93,17 @@ int main(int argc, char **argv) {
         else if (a == "--no-split-merge") split_merge = false;
         else if (a == "--split-regions") split_regions = strtof(next(), nullptr);
         else if (a == "--out") out = next();
+        else if (a == "--irradiance-cache") use_ic = true;
+        else if (a == "--adrrs") adrrs = true;
+        else if (a == "--prepare-frames") prepare_frames = (uint32_t)strtoul(next(), nullptr, 10);
         else return usage();
     }
     if (W == 0 || H == 0) return usage();
+    const uint32_t ic_size = (uint32_t)strtoul(argv[3], nullptr, 10);
+    if ((use_ic || adrrs) && ic_size == 0) {
+        fprintf(stderr, "--irradiance-cache and --adrrs need IC_SIZE > 0\n");
+        return EXIT_FAILURE;
+    }
     try {
         pg::SceneLoader scene = scene_arg == "cornell"  ? pg::SceneLoader::cornell(W, H)
                                 : scene_arg == "plates" ? pg::SceneLoader::plates(W, H)
@@ -101,6 +115,47 @@ int main(int argc, char **argv) {
         pg::check_cuda(cudaMalloc(&image, n * sizeof(float)), "image");
         pg::check_cuda(cudaMemsetAsync(image, 0, n * sizeof(float), stream), "image clear");
         pg::Tracer tracer(scene, stream);
+        // irradiance cache: prepare frames of one sample per pixel into a scratch image
+        // (isIrradiancePrepareFrame), for ADRRS on glossy surfaces too, then the estimate
+        uint32_t flags = 0, ic_entries = 0;
+        float *estimate = nullptr;
+        std::unique_ptr<pg::IrradianceCache> ic;
+        if (use_ic || adrrs) {
+            ic.reset(new pg::IrradianceCache(scene, ic_size, adrrs));
+            float *scratch = nullptr;
+            pg::check_cuda(cudaMalloc(&scratch, n * sizeof(float)), "scratch image");
+            for (uint32_t f = 0; f < prepare_frames; ++f) {
+                pg_render_params p = pg::render_params(1, depth, seed + 7777u * (f + 1));
+                p.flags = PG_RENDER_IRRADIANCE_CACHE;
+                tracer.render(p, scratch);
+            }
+            if (adrrs) {
+                // setEstimateRTSettings: 16 samples, the cache used, maxDepth 1
+                pg::check_cuda(cudaMemsetAsync(scratch, 0, n * sizeof(float), stream), "estimate clear");
+                pg_render_params p = pg::render_params(16, 3, seed + 99u);
+                p.flags = PG_RENDER_IRRADIANCE_CACHE | PG_RENDER_IC_FROZEN;
+                tracer.render(p, scratch);
+                std::vector<float> est(n);
+                pg::check_cuda(cudaMemcpyAsync(est.data(), scratch, n * sizeof(float), cudaMemcpyDeviceToHost, stream),
+                               "estimate download");
+                pg::check_cuda(cudaStreamSynchronize(stream), "estimate");
+                for (float &v : est) v /= 16.0f;
+                pg::check_cuda(cudaMalloc(&estimate, n * sizeof(float)), "estimate");
+                pg::check_cuda(cudaMemcpy(estimate, est.data(), n * sizeof(float), cudaMemcpyHostToDevice),
+                               "estimate upload");
+                pg_adrrs_config ac{};
+                ac.estimate = estimate;
+                ac.s = 5.0f;
+                ac.split = 1;
+                pg::check(pg_scene_set_adrrs(scene.handle(), &ac));
+                flags = PG_RENDER_ADRRS;
+            } else {
+                flags = PG_RENDER_IRRADIANCE_CACHE;
+            }
+            pg::check_cuda(cudaStreamSynchronize(stream), "prepare frames");
+            cudaFree(scratch);
+            ic_entries = ic->size();
+        }
         cudaEvent_t e0, e1, e2;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
@@ -116,15 +171,18 @@ int main(int argc, char **argv) {
             if (split_regions > 0.0f) pg.setSplitRegions(true, split_regions);
             pg::SampleCollector collector(pg.getRegionCount(), W, H, stream);
             for (size_t f = 0; f < train.size(); ++f) {
-                tracer.render(pg::render_params(train[f], depth, seed + 1000u * (uint32_t)(f + 1), f > 0, true, prob),
-                              image, &pg, &collector);
+                pg_render_params p = pg::render_params(train[f], depth, seed + 1000u * (uint32_t)(f + 1), f > 0, true, prob);
+                p.flags = flags;
+                tracer.render(p, image, &pg, &collector);
                 // RayTracingApp rebuilds its buffers when update reports split regions
                 if (pg.update(collector)) collector.setRegionCount(pg.getRegionCount());
                 total += train[f];
             }
             regions = pg.getRegionCount();
             cudaEventRecord(e1, stream);
-            tracer.render(pg::render_params(spp, depth, seed, true, false, prob), image, &pg);
+            pg_render_params p = pg::render_params(spp, depth, seed, true, false, prob);
+            p.flags = flags;
+            tracer.render(p, image, &pg);
             total += spp;
             cudaEventRecord(e2, stream);
             pg.synchronize();
@@ -137,7 +195,9 @@ int main(int argc, char **argv) {
             uint32_t all = spp;
             for (uint32_t t : train) all += t;
             cudaEventRecord(e1, stream);
-            tracer.render(pg::render_params(all, depth, seed), image);
+            pg_render_params p = pg::render_params(all, depth, seed);
+            p.flags = flags;
+            tracer.render(p, image);
             total = all;
             cudaEventRecord(e2, stream);
         }
@@ -166,10 +226,12 @@ int main(int argc, char **argv) {
         }
         printf("{\"scene\": \"%s\", \"width\": %u, \"height\": %u, \"guiding\": %s, \"spp\": %u, "
                "\"train_ms\": %.3f, \"render_ms\": %.3f, \"mean\": %.9g, \"sorted_records\": %llu, "
-               "\"regions_with_samples\": %llu, \"regions\": %u}\n",
+               "\"regions_with_samples\": %llu, \"regions\": %u, \"irradiance_cache_entries\": %u, \"adrrs\": %s}\n",
                scene_arg.c_str(), W, H, guiding ? "true" : "false", total, train_ms, render_ms, mean,
-               (unsigned long long)sorted_records, (unsigned long long)regions_with_samples, regions);
+               (unsigned long long)sorted_records, (unsigned long long)regions_with_samples, regions, ic_entries,
+               adrrs ? "true" : "false");
         cudaFree(image);
+        cudaFree(estimate);
         cudaStreamDestroy(stream);
     } catch (const pg::Error &e) {
         fprintf(stderr, "pg_render: %s\n", e.what());

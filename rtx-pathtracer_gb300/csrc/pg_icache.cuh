@@ -36,8 +36,9 @@ constexpr uint32_t kIcUpdateBounce = 255;  // bounce field of an update request
 constexpr uint32_t kIcSalt = 0x1c0ffee1u;  // seed salt of the cache's random numbers
 
 // A queued request: a new entry at (o, n) (target -1) or an update of an
-// entry (target >= 0 once assigned; -2: nothing to do).  pixel / bounce /
-// pass name its random-number stream and its place in the commit order.
+// entry (target >= 0 once assigned; -2: nothing to do).  pixel (the
+// requesting path's stream: its pixel for a camera path) / bounce / pass name
+// its random numbers and its place in the commit order.
 struct IcRequest {
     float o[3], n[3];
     int32_t target;
@@ -62,7 +63,7 @@ struct DevIc {
     int query, grow;             // what this render call does: query; create and update
     IcRequest *requests;
     uint32_t req_cap, capacity;
-    uint8_t *created;            // per pixel: new-entry requests of this pass
+    uint32_t *created;           // per pixel: new-entry requests of this pass
     uint32_t *state;             // [0] requests queued, [1] round-robin update position, [2] entries,
                                  // [3] new entries written this pass
 };

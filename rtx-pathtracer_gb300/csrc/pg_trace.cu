@@ -527,6 +527,15 @@ struct DevRender {
     float *rec_factor;           // apparent-distance factor through refraction
     float *image;
     DevIc ic;                    // irradiance cache (query / grow off: unused)
+    // ADRRS and the split copies it makes: path ids below n_pix are camera
+    // paths (their pixel); ids n_pix + k are split slot k
+    const float *adrrs_est;      // pixels' mean radiance (null: ADRRS off)
+    float adrrs_s;
+    int adrrs_split;
+    uint32_t n_pix, split_cap;
+    uint32_t *split_pix, *split_stream;  // per split slot: pixel, random stream
+    uint32_t *split_count;       // per pixel: copies made this pass
+    uint32_t *q_copy;            // split copies made at this bounce (counters[9])
 };
 
 __device__ __forceinline__ V ld3(const float *a, uint32_t i) { return mk(a[3 * i], a[3 * i + 1], a[3 * i + 2]); }
@@ -534,6 +543,40 @@ __device__ __forceinline__ void st3(float *a, uint32_t i, V v) {
     a[3 * i] = v.x;
     a[3 * i + 1] = v.y;
     a[3 * i + 2] = v.z;
+}
+
+// A path's pixel and random stream: a camera path's are its id; a split
+// copy's are recorded with its slot.
+__device__ __forceinline__ uint32_t pixel_of(const DevRender &R, uint32_t p) {
+    return p < R.n_pix ? p : R.split_pix[p - R.n_pix];
+}
+__device__ __forceinline__ uint32_t stream_of(const DevRender &R, uint32_t p) {
+    return p < R.n_pix ? p : R.split_stream[p - R.n_pix];
+}
+__device__ __forceinline__ void add_image(const DevRender &R, uint32_t px, V c) {
+    atomicAdd(&R.image[3 * px], c.x);
+    atomicAdd(&R.image[3 * px + 1], c.y);
+    atomicAdd(&R.image[3 * px + 2], c.z);
+}
+
+// applyWeightWindow (raytrace.rgen:830-869): the window around
+// |estimate / adjoint| with upper = s * lower; returns q and the number of
+// paths n (1: Russian roulette with survival probability q; more: an
+// expected-value split into q paths, u deciding the rounding).
+__device__ __forceinline__ float weight_window(V thr, V adjoint, V est, float s, float u, int &n) {
+    const V r = mk(est.x / adjoint.x, est.y / adjoint.y, est.z / adjoint.z);
+    const float center = sqrtf(dot3(r, r));
+    const float lower = 2.0f * center / (1.0f + s);
+    const float upper = s * lower;
+    const float v = sqrtf(dot3(thr, thr));
+    n = 1;
+    if (isnan(lower) || lower <= 0.0f) return 1.0f;
+    if (lower <= v && v <= upper) return 1.0f;
+    if (v <= lower) return fmaxf(v / lower, 0.1f);
+    const float q = v / upper;
+    n = (int)q;
+    if (u > (float)(n + 1) - q) ++n;
+    return q;
 }
 
 __device__ __forceinline__ void warp_append(uint32_t *counter, uint32_t *queue, uint32_t value, bool pred) {
@@ -705,6 +748,8 @@ __global__ void k_camera(DevRender R) {
         R.rec_pending[pix] = -1;
         R.rec_factor[pix] = 1.0f;
     }
+    if (R.adrrs_split) R.split_count[pix] = 0;
+    if (pix == 0) R.counters[8] = 0;  // split slots taken this pass
     if (R.ic.grow) {
         // main() of raytrace.rgen:1639-1641: an update of the next entry with probability update_prob
         R.ic.created[pix] = 0;
@@ -772,15 +817,152 @@ __global__ void __launch_bounds__(128, 8) k_extend(DevRender R) {
     }
 }
 
-__global__ void k_shade(DevRender R, int bounce, int last) {
+// Next-event estimation and the continuation at a non-emitting vertex x of
+// path p (random stream `stream`, throughput thr before the vertex).  The
+// shadow ray is queued with the radiance it would bring; the continuation
+// (getNewDirection, raytrace.rgen:923-960) writes p's next ray and, with
+// rec_on, the vertex's guiding record.  ic_end: the path ends at the
+// irradiance cache here (next-event estimation always, unweighted: there is
+// no continuation to pair it with).  Returns whether p continues.
+__device__ bool shade_vertex(const DevRender &R, uint32_t p, uint32_t stream, int b, bool rec_on, bool ic_end,
+                             const pg_material &m, V x, V n, V d, bool front, V thr) {
+    const V wi = mul(d, -1.0f);
+    // --- next-event estimation (raytrace.rgen:601-731), always at a cache end (:1122)
+    if ((R.rp.use_nee || ic_end) && !is_delta(m) && R.n_lights > 0) {
+        NeeSample ns;
+        if (nee_sample(R, m, x, n, wi, rnd(R.rp.seed, stream, R.sample, dimb(b, 0)),
+                       rnd(R.rp.seed, stream, R.sample, dimb(b, 1)), rnd(R.rp.seed, stream, R.sample, dimb(b, 2)),
+                       ns)) {
+            // pdf of the continuation sampler for this direction (MIS)
+            float pb = ns.pb;
+            if (R.guiding && guided_material(m, R.rp.flags)) {
+                const uint32_t reg = region_of(R.guide, x);
+                if (reg != PG_INVALID_REGION) {
+                    const float pg = vmm_pdf(R.guide.vmm[reg], ns.wl, x, R.guide.use_parallax);
+                    if (!isnan(pg)) pb = (1.0f - R.rp.guiding_prob) * pb + R.rp.guiding_prob * pg;
+                }
+            }
+            const float pl = ns.pl;
+            const float w = (R.rp.use_mis && !ic_end) ? pl * pl / (pl * pl + pb * pb) : 1.0f;
+            const V Lnee = mul(ns.fLe, w / pl);
+            const uint32_t s = atomicAdd(&R.counters[2], 1u);
+            st3(R.sh_o, s, x);
+            st3(R.sh_d, s, ns.wl);
+            R.sh_tmax[s] = ns.tmax;
+            st3(R.sh_c, s, hmul(thr, Lnee));
+            st3(R.sh_l, s, Lnee);
+            R.sh_pix[s] = p;
+            R.sh_nrec[s] = (rec_on && !ic_end) ? R.rec_count[p] : 0u;
+        }
+    }
+    if (ic_end) return false;
+    // --- continuation (getNewDirection, raytrace.rgen:923-960)
+    const float uch = rnd(R.rp.seed, stream, R.sample, dimb(b, 3));
+    const float ul = rnd(R.rp.seed, stream, R.sample, dimb(b, 4));
+    const float u1 = rnd(R.rp.seed, stream, R.sample, dimb(b, 5)), u2 = rnd(R.rp.seed, stream, R.sample, dimb(b, 6));
+    const bool gm = R.guiding && guided_material(m, R.rp.flags);
+    const pg_vmm_theta *mix = nullptr;
+    if (gm) {
+        const uint32_t reg = region_of(R.guide, x);
+        if (reg != PG_INVALID_REGION) mix = &R.guide.vmm[reg];
+    }
+    const Continuation cn = continue_path(m, d, n, front, x, gm, mix, R.guide.use_parallax, R.rp.guiding_prob, uch,
+                                          ul, u1, u2, [&] { return rnd(R.rp.seed, stream, R.sample, dimb(b, 7)); });
+    const V wo = cn.wo, tc = cn.tc;
+    const float pdf = cn.pdf;
+    const bool delta = cn.delta;
+    if (!(pdf > 0.0f && maxc(tc) > 0.0f)) return false;
+    thr = hmul(thr, tc);
+    // guiding record of this vertex (raytrace.rgen:1179-1200)
+    if (rec_on) {
+        const uint32_t cnt = R.rec_count[p];
+        if (cnt < (uint32_t)kMaxRecords) {
+            const uint32_t s = p * kMaxRecords + cnt;
+            pg_directional_data rd;
+            rd.position[0] = x.x;
+            rd.position[1] = x.y;
+            rd.position[2] = x.z;
+            rd.direction[0] = wo.x;
+            rd.direction[1] = wo.y;
+            rd.direction[2] = wo.z;
+            rd.weight = 0.0f;
+            rd.pdf = pdf;
+            rd.distance = 0.0f;
+            if (delta || almost_delta(m)) {
+                rd.flags = PG_INVALID_REGION;
+            } else {
+                rd.flags = region_of(R.guide, x);
+                R.rec_pending[p] = (int32_t)cnt;
+                R.rec_factor[p] = 1.0f;
+            }
+            R.rec[s] = rd;
+            st3(R.rec_lsum, s, mk(0, 0, 0));
+            st3(R.rec_tc, s, tc);
+            R.rec_count[p] = cnt + 1;
+        } else if (R.rec_pending[p] >= 0 && m.type == PG_MAT_DIELECTRIC && dot3(wo, n) < 0.0f) {
+            const float eta = front ? m.ior : 1.0f / m.ior;
+            R.rec_factor[p] = fabsf(dot3(n, d) / dot3(n, wo)) * eta;
+        }
+    }
+    st3(R.ro, p, x);
+    st3(R.rd, p, wo);
+    st3(R.thr, p, thr);
+    R.prev_pdf[p] = delta ? 0.0f : pdf;
+    return true;
+}
+
+constexpr uint32_t kMaxSplits = 10;  // MAX_SPLITS (raytrace.rgen:82): copies per pixel and pass
+
+// ADRRS at a vertex where the cache gives irradiance E (raytrace.rgen:
+// 1086-1117): the weight window of the path's throughput thr against the
+// pixel's estimate; Russian roulette (returns true when the path ends,
+// otherwise divides thr by the survival probability) or splitting into
+// `copies` paths (thr divided by their expected number; copies - 1 split
+// slots from split_base, fewer within the pixel's budget and the slots, the
+// throughput then shared by their number, raytrace.rgen:1103-1109).  Out of
+// line: the shading kernel's registers stay with its common path.
+__device__ __noinline__ bool adrrs_vertex(const DevRender &R, uint32_t px, uint32_t stream, int b, V E, V &thr,
+                                          int &copies, uint32_t &split_base) {
+    int nn;
+    float q = weight_window(thr, E, ld3(R.adrrs_est, px), R.adrrs_s, rnd(R.rp.seed, stream, R.sample, dimb(b, 10)),
+                            nn);
+    if (nn == 1) {
+        if (rnd(R.rp.seed, stream, R.sample, dimb(b, 9)) > q) return true;
+        thr = mul(thr, 1.0f / q);
+    } else if (R.adrrs_split) {
+        const uint32_t want = (uint32_t)nn - 1u;
+        const uint32_t used = atomicAdd(&R.split_count[px], want);
+        uint32_t k = used < kMaxSplits ? min(want, kMaxSplits - used) : 0u;
+        if (k) {
+            split_base = atomicAdd(&R.counters[8], k);
+            k = split_base < R.split_cap ? min(k, R.split_cap - split_base) : 0u;
+        }
+        if (k < want) {
+            nn = (int)k + 1;
+            q = (float)nn;
+        }
+        thr = mul(thr, 1.0f / q);
+        copies = nn;
+    }
+    return false;
+}
+
+// One bounce of the paths in the current queue (copies 0), or of the split
+// copies made at this bounce (copies 1: counters[9] of them in q_copy, each
+// at its parent's vertex with the parent's ray and shared throughput; they
+// take no roulette or split decision there again).  kCache: the irradiance
+// cache or ADRRS is on (a render without them runs the leaner instance).
+template <bool kCache>
+__global__ void k_shade(DevRender R, int bounce, int last, int copies_pass) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= R.counters[0]) return;
-    const uint32_t p = R.q_cur[i];
+    if (i >= R.counters[copies_pass ? 9 : 0]) return;
+    const uint32_t p = copies_pass ? R.q_copy[i] : R.q_cur[i];
+    const uint32_t px = kCache ? pixel_of(R, p) : p, stream = kCache ? stream_of(R, p) : p;
     const pg_hit h = R.hits[p];
     const V d = ld3(R.rd, p);
     V thr = ld3(R.thr, p);
     bool cont = false;
-    const bool rec_on = R.recording != 0;
+    const bool rec_on = R.recording != 0;  // camera paths only: no split copies while recording
     if (h.prim == PG_NO_HIT) {
         // miss: a pending record saw infinity (distance 0)
         if (rec_on && R.rec_pending[p] >= 0) {
@@ -798,10 +980,7 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
             }
             const V Le = mul(env_radiance(R, d), w);
             if (maxc(Le) > 0.0f) {
-                const V c = hmul(thr, Le);
-                atomicAdd(&R.image[3 * p], c.x);
-                atomicAdd(&R.image[3 * p + 1], c.y);
-                atomicAdd(&R.image[3 * p + 2], c.z);
+                add_image(R, px, hmul(thr, Le));
                 R.found[p] = 1;
                 if (rec_on) update_records(R, p, R.rec_count[p], Le);
             }
@@ -832,25 +1011,34 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
         const bool front = dot3(d, ng) < 0.0f;  // raytrace.rchit:42-48
         const V n = front ? ng : mul(ng, -1.0f);
         const V wi = mul(d, -1.0f);
-        // irradiance cache (raytrace.rgen:1080-1139): a vertex inside cached
-        // spheres takes their irradiance, adds next-event estimation and ends
-        // the path; elsewhere it may queue a new entry
-        bool ic_end = false;
+        // irradiance cache and ADRRS (raytrace.rgen:1080-1139): a vertex inside
+        // cached spheres either takes their irradiance, adds next-event
+        // estimation and ends the path, or (ADRRS) compares the path's
+        // throughput with the weight window the cached irradiance gives:
+        // Russian roulette below it, splitting above; a vertex outside every
+        // sphere may queue a new entry
+        bool ic_end = false, rr_end = false;
         V ic_L = mk(0, 0, 0);
-        if (R.ic.query && !last && m.type != PG_MAT_LIGHT && ic_capable(R.ic, m)) {
+        int copies = 1;
+        uint32_t split_base = 0;
+        if (kCache && (R.ic.query || (R.adrrs_est && bounce >= 1)) && !copies_pass && !last &&
+            m.type != PG_MAT_LIGHT && ic_capable(R.ic, m)) {
             V E;
             if (ic_query(R.ic, x, n, E)) {
-                ic_end = true;
-                ic_L = hmul(approx_diffuse(m, n, wi), E);
-            } else if (R.ic.grow && rnd(R.rp.seed, p, R.sample, dimb(bounce, 8)) < R.ic.create_prob &&
-                       R.ic.state[2] < R.ic.capacity && R.ic.created[p] < kIcMaxNewPerPixel) {
-                R.ic.created[p] += 1;
-                ic_push(R.ic, x, n, -1, p, (uint32_t)bounce, R.sample);
+                if (R.adrrs_est) {
+                    rr_end = adrrs_vertex(R, px, stream, bounce, E, thr, copies, split_base);
+                } else {
+                    ic_end = true;
+                    ic_L = hmul(approx_diffuse(m, n, wi), E);
+                }
+            } else if (R.ic.grow && rnd(R.rp.seed, stream, R.sample, dimb(bounce, 8)) < R.ic.create_prob &&
+                       R.ic.state[2] < R.ic.capacity && atomicAdd(&R.ic.created[px], 1u) < kIcMaxNewPerPixel) {
+                ic_push(R.ic, x, n, -1, stream, (uint32_t)bounce, R.sample);
             }
         }
         // distance of a pending record (raytrace.rgen:1149-1156, 1201-1212); a
-        // path that ends at the cache leaves it as it is
-        if (rec_on && R.rec_pending[p] >= 0 && !ic_end) {
+        // path that ends at the cache or in the roulette leaves it as it is
+        if (rec_on && R.rec_pending[p] >= 0 && !ic_end && !rr_end) {
             pg_directional_data &rd = R.rec[p * kMaxRecords + (uint32_t)R.rec_pending[p]];
             rd.distance += h.t * R.rec_factor[p];
             if (!is_delta(m) && !almost_delta(m)) R.rec_pending[p] = -1;
@@ -880,111 +1068,36 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
             if (front || (h.prim & PG_SPHERE_BIT) == 0) {
                 const V Le = mul(mk(m.emission[0], m.emission[1], m.emission[2]), w);
                 if (maxc(Le) > 0.0f) {
-                    const V c = hmul(thr, Le);
-                    atomicAdd(&R.image[3 * p], c.x);
-                    atomicAdd(&R.image[3 * p + 1], c.y);
-                    atomicAdd(&R.image[3 * p + 2], c.z);
+                    add_image(R, px, hmul(thr, Le));
                     R.found[p] = 1;
                     if (rec_on) update_records(R, p, R.rec_count[p], Le);
                 }
             }
-        } else if (!last) {
-            const int b = bounce;
-            if (ic_end) {
+        } else if (!last && !rr_end) {
+            if (kCache && ic_end) {
                 // the cached irradiance; it reaches no guiding record (raytrace.rgen:1119)
                 const V c = hmul(thr, ic_L);
                 if (maxc(c) > 0.0f) {
-                    atomicAdd(&R.image[3 * p], c.x);
-                    atomicAdd(&R.image[3 * p + 1], c.y);
-                    atomicAdd(&R.image[3 * p + 2], c.z);
+                    add_image(R, px, c);
                     R.found[p] = 1;
                 }
             }
-            // --- next-event estimation (raytrace.rgen:601-731), always at a cache end (:1122)
-            if ((R.rp.use_nee || ic_end) && !is_delta(m) && R.n_lights > 0) {
-                NeeSample ns;
-                if (nee_sample(R, m, x, n, wi, rnd(R.rp.seed, p, R.sample, dimb(b, 0)),
-                               rnd(R.rp.seed, p, R.sample, dimb(b, 1)), rnd(R.rp.seed, p, R.sample, dimb(b, 2)), ns)) {
-                    // pdf of the continuation sampler for this direction (MIS)
-                    float pb = ns.pb;
-                    if (R.guiding && guided_material(m, R.rp.flags)) {
-                        const uint32_t reg = region_of(R.guide, x);
-                        if (reg != PG_INVALID_REGION) {
-                            const float pg = vmm_pdf(R.guide.vmm[reg], ns.wl, x, R.guide.use_parallax);
-                            if (!isnan(pg)) pb = (1.0f - R.rp.guiding_prob) * pb + R.rp.guiding_prob * pg;
-                        }
-                    }
-                    // a vertex whose path ends at the irradiance cache has no continuation to pair with
-                    const float pl = ns.pl;
-                    const float w = (R.rp.use_mis && !ic_end) ? pl * pl / (pl * pl + pb * pb) : 1.0f;
-                    const V Lnee = mul(ns.fLe, w / pl);
-                    const uint32_t s = atomicAdd(&R.counters[2], 1u);
-                    st3(R.sh_o, s, x);
-                    st3(R.sh_d, s, ns.wl);
-                    R.sh_tmax[s] = ns.tmax;
-                    st3(R.sh_c, s, hmul(thr, Lnee));
-                    st3(R.sh_l, s, Lnee);
-                    R.sh_pix[s] = p;
-                    R.sh_nrec[s] = (rec_on && !ic_end) ? R.rec_count[p] : 0u;
-                }
+            // split copies (raytrace.rgen:883-902, 1684-1708): paths of their own at
+            // this vertex, shaded by the copies pass of this bounce with their own
+            // next-event sample and continuation
+            for (int c = 1; kCache && c < copies; ++c) {
+                const uint32_t slot = split_base + (uint32_t)c - 1u, q2 = R.n_pix + slot;
+                R.split_pix[slot] = px;
+                R.split_stream[slot] = fmix32(stream * 0x9e3779b1u + (uint32_t)(bounce * (int)kMaxSplits + c));
+                st3(R.ro, q2, o);
+                st3(R.rd, q2, d);
+                st3(R.thr, q2, thr);
+                R.hits[q2] = h;
+                R.prev_pdf[q2] = R.prev_pdf[p];
+                R.found[q2] = 0;
+                R.q_copy[atomicAdd(&R.counters[9], 1u)] = q2;
             }
-            // --- continuation (getNewDirection, raytrace.rgen:923-960)
-            if (!ic_end) {
-                const float uch = rnd(R.rp.seed, p, R.sample, dimb(b, 3));
-                const float ul = rnd(R.rp.seed, p, R.sample, dimb(b, 4));
-                const float u1 = rnd(R.rp.seed, p, R.sample, dimb(b, 5)), u2 = rnd(R.rp.seed, p, R.sample, dimb(b, 6));
-                const bool gm = R.guiding && guided_material(m, R.rp.flags);
-                const pg_vmm_theta *mix = nullptr;
-                if (gm) {
-                    const uint32_t reg = region_of(R.guide, x);
-                    if (reg != PG_INVALID_REGION) mix = &R.guide.vmm[reg];
-                }
-                const Continuation cn = continue_path(m, d, n, front, x, gm, mix, R.guide.use_parallax,
-                                                      R.rp.guiding_prob, uch, ul, u1, u2,
-                                                      [&] { return rnd(R.rp.seed, p, R.sample, dimb(b, 7)); });
-                const V wo = cn.wo, tc = cn.tc;
-                const float pdf = cn.pdf;
-                const bool delta = cn.delta;
-                if (pdf > 0.0f && maxc(tc) > 0.0f) {
-                    thr = hmul(thr, tc);
-                    cont = true;
-                    // guiding record of this vertex (raytrace.rgen:1179-1200)
-                    if (rec_on) {
-                        const uint32_t cnt = R.rec_count[p];
-                        if (cnt < (uint32_t)kMaxRecords) {
-                            const uint32_t s = p * kMaxRecords + cnt;
-                            pg_directional_data rd;
-                            rd.position[0] = x.x;
-                            rd.position[1] = x.y;
-                            rd.position[2] = x.z;
-                            rd.direction[0] = wo.x;
-                            rd.direction[1] = wo.y;
-                            rd.direction[2] = wo.z;
-                            rd.weight = 0.0f;
-                            rd.pdf = pdf;
-                            rd.distance = 0.0f;
-                            if (delta || almost_delta(m)) {
-                                rd.flags = PG_INVALID_REGION;
-                            } else {
-                                rd.flags = region_of(R.guide, x);
-                                R.rec_pending[p] = (int32_t)cnt;
-                                R.rec_factor[p] = 1.0f;
-                            }
-                            R.rec[s] = rd;
-                            st3(R.rec_lsum, s, mk(0, 0, 0));
-                            st3(R.rec_tc, s, tc);
-                            R.rec_count[p] = cnt + 1;
-                        } else if (R.rec_pending[p] >= 0 && m.type == PG_MAT_DIELECTRIC && dot3(wo, n) < 0.0f) {
-                            const float eta = front ? m.ior : 1.0f / m.ior;
-                            R.rec_factor[p] = fabsf(dot3(n, d) / dot3(n, wo)) * eta;
-                        }
-                    }
-                    st3(R.ro, p, x);
-                    st3(R.rd, p, wo);
-                    st3(R.thr, p, thr);
-                    R.prev_pdf[p] = delta ? 0.0f : pdf;
-                }
-            }
+            cont = shade_vertex(R, p, stream, bounce, rec_on, ic_end, m, x, n, d, front, thr);
         }
     }
     warp_append(&R.counters[1], R.q_next, p, cont);
@@ -994,9 +1107,7 @@ __global__ void k_shade(DevRender R, int bounce, int last) {
 // path's guiding records.
 __device__ __forceinline__ void shadow_finish(const DevRender &R, uint32_t i) {
     const uint32_t p = R.sh_pix[i];
-    atomicAdd(&R.image[3 * p], R.sh_c[3 * i]);
-    atomicAdd(&R.image[3 * p + 1], R.sh_c[3 * i + 1]);
-    atomicAdd(&R.image[3 * p + 2], R.sh_c[3 * i + 2]);
+    add_image(R, pixel_of(R, p), ld3(R.sh_c, i));
     R.found[p] = 1;
     if (R.recording) update_records(R, p, R.sh_nrec[i], ld3(R.sh_l, i));
 }
@@ -1085,6 +1196,7 @@ __global__ void k_advance(DevRender R) {
     R.counters[2] = 0;
     R.counters[6] = 0;
     R.counters[7] = 0;
+    R.counters[9] = 0;
 }
 
 __global__ void k_reset_records(pg_directional_data *rec, uint32_t n_slots, uint32_t *rec_start, uint32_t n_pix) {
@@ -1100,7 +1212,8 @@ __global__ void k_probe_shading(const pg_material *mats, uint32_t n_mats, const 
     if (i >= count) return;
     const pg_shading_probe q = P[i];
     pg_shading_result r;
-    const bool uses_mat = q.op == PG_PROBE_BSDF_EVAL || q.op == PG_PROBE_BSDF_SAMPLE || q.op == PG_PROBE_CONTINUE;
+    const bool uses_mat = q.op == PG_PROBE_BSDF_EVAL || q.op == PG_PROBE_BSDF_SAMPLE || q.op == PG_PROBE_CONTINUE ||
+                          q.op == PG_PROBE_APPROX_DIFFUSE;
     const bool uses_vmm = q.op == PG_PROBE_VMM_PDF || q.op == PG_PROBE_VMM_SAMPLE ||
                           (q.op == PG_PROBE_CONTINUE && (q.flags & 8u));
     const bool bad = (uses_mat && q.material >= n_mats) || (uses_vmm && q.vmm >= n_vmms);
@@ -1158,6 +1271,15 @@ __global__ void k_probe_shading(const pg_material *mats, uint32_t n_mats, const 
         }
         case PG_PROBE_TO_WORLD:
             put(0, to_world(wo, n));
+            break;
+        case PG_PROBE_WEIGHT_WINDOW: {
+            int nn;
+            r.v[0] = weight_window(wi, wo, x, q.a, q.u[0], nn);
+            r.v[1] = (float)nn;
+            break;
+        }
+        case PG_PROBE_APPROX_DIFFUSE:
+            put(0, approx_diffuse(mats[q.material], n, wi));
             break;
         default:
             break;
@@ -1261,10 +1383,12 @@ struct pg_scene {
     float aabb[6] = {0, 0, 0, 0, 0, 0};
     // render scratch
     uint32_t cap_pix = 0;
+    uint32_t cap_paths = 0;       // path slots: pixels plus split copies
     uint32_t persist_blocks = 0;  // resident CTAs of the persistent traversal stages (all SMs)
     std::vector<void *> bufs;
     DevRender R{};
     uint32_t *d_counters = nullptr;
+    pg_adrrs_config adrrs{nullptr, 5.0f, 1, {0, 0, 0, 0}};
     // irradiance cache
     struct IcStore {
         bool on = false;
@@ -1280,7 +1404,7 @@ struct pg_scene {
         IcResult *results = nullptr;      // req_cap
         float4 *samples = nullptr;        // req_cap x 200
         uint32_t req_cap = 0;
-        uint8_t *created = nullptr;       // per pixel
+        uint32_t *created = nullptr;      // per pixel
         uint32_t cap_created = 0;
         bool grid_stale = true;
     } ic;
@@ -1847,6 +1971,13 @@ int pg_scene_set_irradiance_cache_entries(pg_scene *sc, const pg_ic_entry *entri
     return cudaDeviceSynchronize() == cudaSuccess ? PG_OK : scene_error(PG_ERR_CUDA, "irradiance cache grid build");
 }
 
+int pg_scene_set_adrrs(pg_scene *sc, const pg_adrrs_config *cfg) {
+    if (!sc || !cfg) return PG_ERR_ARG;
+    if (!(cfg->s > 1.0f) || !std::isfinite(cfg->s)) return scene_error(PG_ERR_ARG, "ADRRS: s must be above 1");
+    sc->adrrs = *cfg;
+    return PG_OK;
+}
+
 int pg_ic_query(pg_scene *sc, const float *positions, const float *normals, uint32_t n, float *rgb, uint32_t *found,
                 void *stream) {
     if (!sc || (n && (!positions || !normals || !rgb || !found))) return PG_ERR_ARG;
@@ -2038,63 +2169,89 @@ int pg_render(pg_scene *sc, const pg_render_params *rp, pg_ctx *guide, float *im
     cudaStream_t s = (cudaStream_t)stream;
     const pg_camera cam = sc->host.camera;
     const uint32_t P = cam.width * cam.height;
+    const bool adrrs = (rp->flags & PG_RENDER_ADRRS) != 0;
+    if (adrrs && !sc->adrrs.estimate)
+        return scene_error(PG_ERR_ARG, "PG_RENDER_ADRRS needs an estimate (pg_scene_set_adrrs)");
+    if (adrrs && !sc->ic.on) return scene_error(PG_ERR_ARG, "PG_RENDER_ADRRS needs an irradiance cache");
+    const bool splitting = adrrs && sc->adrrs.split;
+    if (splitting && rp->record_samples)
+        return scene_error(PG_ERR_ARG, "ADRRS splitting and record_samples exclude each other");
+    // paths: one per pixel, plus up to two split copies per pixel and pass
+    const uint32_t split_cap = splitting ? 2u * P : 0u;
+    const uint32_t NP = P + split_cap;
     // grow the path and queue buffers
-    if (P > sc->cap_pix) {
+    if (P > sc->cap_pix || NP > sc->cap_paths) {
         for (void *b : sc->bufs) cudaFree(b);
         sc->bufs.clear();
+        sc->cap_pix = 0;
+        sc->cap_paths = 0;
+        size_t want = 0;
         auto alloc = [&](size_t bytes) -> void * {
+            ++want;
             void *p = nullptr;
-            if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+            if (cudaMalloc(&p, std::max<size_t>(bytes, 4)) != cudaSuccess) return nullptr;
             sc->bufs.push_back(p);
             return p;
         };
         DevRender &R = sc->R;
-        R.ro = (float *)alloc(12ull * P);
-        R.rd = (float *)alloc(12ull * P);
-        R.thr = (float *)alloc(12ull * P);
-        R.prev_pdf = (float *)alloc(4ull * P);
-        R.alive = (uint8_t *)alloc(P);
-        R.found = (uint8_t *)alloc(P);
-        R.hits = (pg_hit *)alloc(sizeof(pg_hit) * (size_t)P);
-        R.q_cur = (uint32_t *)alloc(4ull * P);
-        R.q_next = (uint32_t *)alloc(4ull * P);
-        R.sh_o = (float *)alloc(12ull * P);
-        R.sh_d = (float *)alloc(12ull * P);
-        R.sh_tmax = (float *)alloc(4ull * P);
-        R.sh_c = (float *)alloc(12ull * P);
-        R.sh_l = (float *)alloc(12ull * P);
-        R.sh_pix = (uint32_t *)alloc(4ull * P);
-        R.sh_nrec = (uint32_t *)alloc(4ull * P);
+        // per path
+        R.ro = (float *)alloc(12ull * NP);
+        R.rd = (float *)alloc(12ull * NP);
+        R.thr = (float *)alloc(12ull * NP);
+        R.prev_pdf = (float *)alloc(4ull * NP);
+        R.alive = (uint8_t *)alloc(NP);
+        R.found = (uint8_t *)alloc(NP);
+        R.hits = (pg_hit *)alloc(sizeof(pg_hit) * (size_t)NP);
+        R.q_cur = (uint32_t *)alloc(4ull * NP);
+        R.q_next = (uint32_t *)alloc(4ull * NP);
+        R.sh_o = (float *)alloc(12ull * NP);
+        R.sh_d = (float *)alloc(12ull * NP);
+        R.sh_tmax = (float *)alloc(4ull * NP);
+        R.sh_c = (float *)alloc(12ull * NP);
+        R.sh_l = (float *)alloc(12ull * NP);
+        R.sh_pix = (uint32_t *)alloc(4ull * NP);
+        R.sh_nrec = (uint32_t *)alloc(4ull * NP);
+        // per pixel
         R.rec_lsum = (float *)alloc(12ull * P * kMaxRecords);
         R.rec_tc = (float *)alloc(12ull * P * kMaxRecords);
         R.rec_count = (uint32_t *)alloc(4ull * P);
         R.rec_start = (uint32_t *)alloc(4ull * P);
         R.rec_pending = (int32_t *)alloc(4ull * P);
         R.rec_factor = (float *)alloc(4ull * P);
-        for (void *b : sc->bufs)
-            if (!b) return scene_error(PG_ERR_NOMEM, "render buffers: out of device memory");
-        if (sc->bufs.size() != 22) return scene_error(PG_ERR_NOMEM, "render buffers: out of device memory");
+        R.split_count = (uint32_t *)alloc(4ull * P);
+        // per split slot
+        R.split_pix = (uint32_t *)alloc(4ull * (NP - P));
+        R.split_stream = (uint32_t *)alloc(4ull * (NP - P));
+        R.q_copy = (uint32_t *)alloc(4ull * (NP - P));
+        if (sc->bufs.size() != want) return scene_error(PG_ERR_NOMEM, "render buffers: out of device memory");
         sc->cap_pix = P;
+        sc->cap_paths = NP;
     }
     DevRender R = sc->R;
     if (int st = setup_render(sc, rp, guide, s, R)) return st;
     R.image = image;
     R.counters = sc->d_counters;
     R.rec = records;
+    R.n_pix = P;
+    R.split_cap = split_cap;
+    R.adrrs_est = adrrs ? sc->adrrs.estimate : nullptr;
+    R.adrrs_s = sc->adrrs.s;
+    R.adrrs_split = splitting ? 1 : 0;
     const bool ic_on = (rp->flags & PG_RENDER_IRRADIANCE_CACHE) != 0;
-    if (ic_on) {
+    if (ic_on || adrrs) {
         auto &c = sc->ic;
         if (!c.on) return scene_error(PG_ERR_ARG, "PG_RENDER_IRRADIANCE_CACHE needs a cache (pg_scene_set_irradiance_cache)");
         if (P > c.cap_created) {
             cudaFree(c.created);
             c.created = nullptr;
             c.cap_created = 0;
-            if (cudaMalloc(&c.created, P) != cudaSuccess) return scene_error(PG_ERR_NOMEM, "irradiance cache pixel counters");
+            if (cudaMalloc(&c.created, sizeof(uint32_t) * P) != cudaSuccess)
+                return scene_error(PG_ERR_NOMEM, "irradiance cache pixel counters");
             c.cap_created = P;
         }
         ic_view(sc, R.ic);
-        R.ic.query = 1;
-        R.ic.grow = !(rp->flags & PG_RENDER_IC_FROZEN) && (c.cfg.create_prob > 0.0f || c.cfg.update_prob > 0.0f);
+        R.ic.query = ic_on ? 1 : 0;
+        R.ic.grow = ic_on && !(rp->flags & PG_RENDER_IC_FROZEN) && (c.cfg.create_prob > 0.0f || c.cfg.update_prob > 0.0f);
         if (c.grid_stale)
             if (int st = ic_build_grid(sc, R.ic, s)) return st;
     }
@@ -2112,6 +2269,9 @@ int pg_render(pg_scene *sc, const pg_render_params *rp, pg_ctx *guide, float *im
     if (!tm.init((rp->flags & PG_RENDER_TIME_STAGES) != 0, s)) return scene_error(PG_ERR_CUDA, "stage timer events");
     const uint32_t T = 128;
     const uint32_t G = (P + T - 1) / T;
+    const uint32_t GS = (NP + T - 1) / T;                        // shading: camera paths and split copies
+    const bool cache_paths = ic_on || adrrs;
+    const uint32_t GC = std::max(1u, (split_cap + T - 1) / T);  // the copies made at a bounce
     if (sc->persist_blocks == 0) {
         int dev = 0, sms = 0, b_ext = 0, b_sh = 0;
         cudaGetDevice(&dev);
@@ -2137,7 +2297,12 @@ int pg_render(pg_scene *sc, const pg_render_params *rp, pg_ctx *guide, float *im
             tm.end();
             const int last = (b + 1 == rp->max_depth) ? 1 : 0;
             tm.begin(PG_STAGE_SHADE);
-            k_shade<<<G, T, 0, s>>>(Rb, (int)b, last);
+            if (cache_paths) {
+                k_shade<true><<<GS, T, 0, s>>>(Rb, (int)b, last, 0);
+                if (splitting) k_shade<true><<<GC, T, 0, s>>>(Rb, (int)b, last, 1);
+            } else {
+                k_shade<false><<<GS, T, 0, s>>>(Rb, (int)b, last, 0);
+            }
             tm.end();
             tm.begin(PG_STAGE_SHADOW);
             if (count)

@@ -9,11 +9,16 @@
 - guided_sequence: the headless form of RayTracingApp's frame loop
   (src/RayTracingApp.cpp:125-157): training passes that render with sample
   recording and call PathGuiding::update, then a guided render.
+- prepare_irradiance_cache / adrrs_estimate / adrrs_frames: the irradiance
+  cache's prepare frames, the ADRRS estimate frame and the ADRRS frames
+  (src/RayTracingApp.cpp:1129-1170, 1206-1217).
 
 Device buffers are torch tensors (allocation and streams only); all work is in
 the library.
 """
 from __future__ import annotations
+
+import ctypes
 
 import numpy as np
 
@@ -154,3 +159,62 @@ def guided_sequence(scene: Scene, guiding: PathGuiding, collector: SampleCollect
         out["regions_switched"] = switched
         out["records_trained_per_pass"] = trained
     return out
+
+
+# --- irradiance cache and ADRRS frames (src/RayTracingApp.cpp:1129-1170, 1206-1217)
+IRRADIANCE_PREPARE_FRAMES = 50  # irradianceCachePrepareFrames (src/RayTracingApp.h:175)
+
+
+def prepare_irradiance_cache(scene: Scene, frames: int = IRRADIANCE_PREPARE_FRAMES, max_depth: int = 10, seed: int = 1,
+                             cfg: "abi.IrradianceCacheConfig | None" = None, use_on_glossy: bool = False,
+                             stream=None) -> np.ndarray:
+    """The reference's prepare frames: `frames` frames of one sample per pixel
+    that grow the scene's irradiance cache and whose images are not kept
+    (isIrradiancePrepareFrame).  Sets a cache on the scene (cfg or the
+    defaults, use_on_glossy as ADRRS's prepare frames set it) and returns its
+    entries."""
+    torch = _torch()
+    if cfg is None:
+        cfg = abi.IrradianceCacheConfig()
+        scene.lib.pg_default_irradiance_cache_config(ctypes.byref(cfg))
+    cfg.use_on_glossy = int(use_on_glossy)
+    scene.set_irradiance_cache(cfg)
+    cam = scene.info().camera
+    scratch = torch.zeros(cam.width * cam.height * 3, dtype=torch.float32, device="cuda")
+    for f in range(frames):
+        params = abi.render_params(spp=1, max_depth=max_depth, seed=seed + f, use_nee=1, use_mis=1,
+                                   flags=abi.PG_RENDER_IRRADIANCE_CACHE)
+        scene.render(params, scratch, stream=stream, stats=False)
+    torch.cuda.synchronize()
+    return scene.irradiance_cache()
+
+
+def adrrs_estimate(scene: Scene, spp: int = 16, max_depth: int = 3, seed: int = 7, stream=None):
+    """The pixel estimate ADRRS compares against, rendered with the
+    reference's estimate settings (setEstimateRTSettings: 16 samples per
+    pixel, the irradiance cache used, next-event estimation, maxDepth 1 - a
+    path length of 3 here): a device tensor of per-pixel mean radiance."""
+    torch = _torch()
+    cam = scene.info().camera
+    img = torch.zeros(cam.width * cam.height * 3, dtype=torch.float32, device="cuda")
+    params = abi.render_params(spp=spp, max_depth=max_depth, seed=seed, use_nee=1, use_mis=1,
+                               flags=abi.PG_RENDER_IRRADIANCE_CACHE | abi.PG_RENDER_IC_FROZEN)
+    scene.render(params, img, stream=stream, stats=False)
+    torch.cuda.synchronize()
+    return img / spp
+
+
+def adrrs_frames(scene: Scene, image, frames: int, spp: int = 1, max_depth: int = 30, seed: int = 100,
+                 s: float = 5.0, split: bool = True, prepare_frames: int = IRRADIANCE_PREPARE_FRAMES, stream=None):
+    """RayTracingApp's ADRRS sequence: prepare frames growing the cache (on
+    glossy surfaces too), the estimate frame, then `frames` frames of `spp`
+    samples with adjoint-driven roulette and splitting added into image.
+    Returns the estimate tensor (kept alive with the scene's ADRRS settings)."""
+    prepare_irradiance_cache(scene, prepare_frames, seed=seed, use_on_glossy=True, stream=stream)
+    est = adrrs_estimate(scene, stream=stream)
+    scene.set_adrrs(est, s=s, split=split)
+    for f in range(frames):
+        params = abi.render_params(spp=spp, max_depth=max_depth, seed=seed + prepare_frames + f, use_nee=1,
+                                   use_mis=1, flags=abi.PG_RENDER_ADRRS)
+        scene.render(params, image, stream=stream, stats=False)
+    return est

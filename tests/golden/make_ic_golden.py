@@ -15,7 +15,10 @@ C++ by oracle/build_glsl_ref.py - on seeded inputs, for the GPU cache to match
   * render__*: a cache of entries createIrradianceCache made at surface
     points the camera sees and their next bounce, and the reference's
     estimator querying it (no entries made while rendering): PARTS parts of
-    SPP samples per pixel as 4 x 4 block means.
+    SPP samples per pixel as 4 x 4 block means;
+  * adrrs__*: the reference's estimator with ADRRS over that cache (its
+    weight windows, roulette and split paths as main() runs them), against
+    an estimate the plain estimator rendered, with and without splitting.
 
 Run from the repository root:
 
@@ -39,8 +42,8 @@ abi = pkg.abi
 
 from oracle import build_glsl_ref  # noqa: E402
 from oracle.glsl_ref import GlslRef, ic_config  # noqa: E402
-from ic_scenes import (COMPUTE_POINTS, COMPUTE_RUNS, IC_A, IC_CAPACITY, PATH_LENGTH, PARTS, SPP, blocks,  # noqa: E402
-                       query_case, surface_points, cornell)
+from ic_scenes import (ADRRS_S, COMPUTE_POINTS, COMPUTE_RUNS, ESTIMATE_SPP, IC_A, IC_CAPACITY, PATH_LENGTH,  # noqa: E402
+                       PARTS, SPP, blocks, query_case, surface_points, cornell)
 
 OUT = Path(__file__).resolve().parent / "ic_ref.npz"
 
@@ -89,6 +92,20 @@ def main(out: Path = OUT):
     arrays["render__blocks"] = np.stack(res)
     b = arrays["render__blocks"]
     print(f"render: mean {b.mean():.5f}, part spread {b.mean(axis=(1, 2, 3)).std() / b.mean():.4f}")
+    # ADRRS with that cache against an estimate of the plain estimator, with
+    # and without splitting
+    est = (g.render(exp, path_length=PATH_LENGTH, spp=ESTIMATE_SPP, frame_seed=777, use_nee=True, use_mis=True)
+           / ESTIMATE_SPP).astype(np.float32)
+    arrays["adrrs__estimate"] = est
+    for split in (0, 1):
+        res = []
+        for p in range(PARTS):
+            img = g.render(exp, path_length=PATH_LENGTH, spp=SPP, frame_seed=100 + p, use_nee=True, use_mis=True,
+                           adrrs={"estimate": est, "s": ADRRS_S, "split": split}) / SPP
+            res.append(blocks(img).astype(np.float32))
+        arrays[f"adrrs__blocks_split{split}"] = np.stack(res)
+        b = arrays[f"adrrs__blocks_split{split}"]
+        print(f"adrrs split {split}: mean {b.mean():.5f}, part spread {b.mean(axis=(1, 2, 3)).std() / b.mean():.4f}")
     sc.close()
     np.savez_compressed(out, compute_points=cp, compute_normals=cn, **arrays)
     print(out)

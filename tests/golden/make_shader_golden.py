@@ -250,6 +250,41 @@ def main(out: Path = OUT):
         rec_events.append(ev)
         rec_want.append(np.stack([w, fl.view(np.float32)], axis=1) if len(w) else np.zeros((0, 2), np.float32))
 
+    # ADRRS weight window (raytrace.rgen:830-869) and approxDiffuse (:815-828),
+    # from a random sequence of their own; window cases whose decisions sit
+    # within 1e-4 of a boundary are skipped (FP32 rounding could flip them)
+    rng2 = np.random.default_rng(20261204)
+    made = 0
+    while made < 600:
+        est = (rng2.uniform(0.0, 2.0, 3) * (rng2.random() < 0.95)).astype(np.float32)
+        adj = rng2.uniform(0.01, 2.0, 3).astype(np.float32)
+        thr = (rng2.uniform(0.0, 1.0, 3) * np.exp(rng2.uniform(-4, 4))).astype(np.float32)
+        s_ = float(rng2.choice([2.0, 5.0, 10.0]))
+        state = int(rng2.integers(1, 2 ** 31))
+        q, nn, drawn = g.weight_window(est, thr, adj, s_, state)
+        e64, a64, t64 = est.astype(np.float64), adj.astype(np.float64), thr.astype(np.float64)
+        center = np.linalg.norm(e64 / a64)
+        lower, v = 2 * center / (1 + s_), np.linalg.norm(t64)
+        upper = s_ * lower
+        if lower > 0 and (abs(v - lower) < 1e-4 * lower or abs(v - upper) < 1e-4 * upper):
+            continue
+        if len(drawn) and abs(float(drawn[0]) - (int(v / upper) + 1 - v / upper)) < 1e-4:
+            continue
+        p = base(abi.PG_PROBE_WEIGHT_WINDOW)
+        p["wi"], p["wo"], p["x"], p["a"] = thr, adj, est, s_
+        if len(drawn):
+            p["u"][0] = drawn[0]
+        add(p, [q, nn] + [0] * 6, "weight_window")
+        made += 1
+    for mi, m in enumerate(mats):
+        if int(m["type"]) not in (abi.PG_MAT_DIFFUSE, abi.PG_MAT_PHONG, abi.PG_MAT_BECKMANN):
+            continue
+        for n, w in zip(unit(rng2, 60), unit(rng2, 60)):
+            w = w if w @ n > 0 else -w
+            p = base(abi.PG_PROBE_APPROX_DIFFUSE, mi)
+            p["n"], p["wi"] = n, w
+            add(p, list(g.approx_diffuse(refm[mi], n, w)) + [0] * 5, "approx_diffuse")
+
     np.savez_compressed(
         out, mats=mats, vmms=vmms, probes=np.array(probes, dtype=P), want=np.array(want), tags=np.array(tags),
         rec_offsets=np.cumsum([0] + [len(e) for e in rec_events]).astype(np.int64),

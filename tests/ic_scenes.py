@@ -16,6 +16,8 @@ PARTS, SPP = 8, 1024
 IC_A = 0.5          # irradianceA: larger spheres than the default 0.2, so most paths meet the cache
 IC_CAPACITY = 4096
 COMPUTE_RUNS = 1024
+ESTIMATE_SPP = 256  # the ADRRS estimate: the plain estimator's mean
+ADRRS_S = 5.0       # adrrsS
 # (point, normal) on the Cornell box's diffuse walls: left, right, back, ceiling, floor (twice)
 COMPUTE_POINTS = [
     ((0.0, 0.5, 0.5), (1.0, 0.0, 0.0)),

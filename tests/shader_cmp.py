@@ -29,7 +29,7 @@ DISCRETE_TYPES = (1, 2, 5)  # PG_MAT_SPECULAR, PG_MAT_DIELECTRIC, PG_MAT_CONDUCT
 
 TOL = {
     "fresnel": 2e-5, "fresnel_conductor": 2e-5, "eval": 5e-5, "sample_pdf": 3e-4,
-    "vmm_pdf": 4e-4, "continue": 4e-4, "angle": 3e-5, "vmm_angle": 3e-5,
+    "vmm_pdf": 4e-4, "continue": 4e-4, "angle": 3e-5, "vmm_angle": 3e-5, "weight_window": 1e-5,
 }
 
 
@@ -56,12 +56,19 @@ def compare(fx, got, tol=TOL, scale=1.0):
             failures.append(f"{name}: case {int(idx[i])} error {float(err[i]):.3g} > {bound * scale:.3g} "
                             f"(got {got[idx[i], :7]}, want {want[idx[i], :7]})")
 
-    fam = np.array([t.split("_")[0] if not t.startswith(("fresnel", "vmm", "to_world")) else t for t in tags])
+    fam = np.array([t.split("_")[0] if not t.startswith(("fresnel", "vmm", "to_world", "weight_window",
+                                                          "approx_diffuse")) else t for t in tags])
     for name in ("fresnel", "fresnel_conductor", "vmm_pdf"):
         idx = np.where(fam == name)[0]
         check(name, _rel(got[idx, 0], want[idx, 0]), tol[name], idx)
     idx = np.where(fam == "eval")[0]
     check("eval", np.max(_rel(got[idx, :4], want[idx, :4]), axis=1), tol["eval"], idx)
+    # ADRRS weight window: the number of paths exactly, q to FP32 rounding
+    idx = np.where(fam == "weight_window")[0]
+    check("weight_window_n", np.abs(got[idx, 1] - want[idx, 1]), 0.0, idx)
+    check("weight_window_q", _rel(got[idx, 0], want[idx, 0]), tol["weight_window"], idx)
+    idx = np.where(fam == "approx_diffuse")[0]
+    check("approx_diffuse", np.max(_rel(got[idx, :3], want[idx, :3]), axis=1), tol["fresnel_conductor"], idx)
     idx = np.where(fam == "to_world")[0]
     check("to_world", _angle(got[idx, :3], want[idx, :3]), tol["angle"], idx)
     idx = np.where(fam == "vmm_sample")[0]

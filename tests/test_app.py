@@ -79,3 +79,36 @@ def test_guided_and_plain_renders(exe, tmp_path, cuda, pkg, abi):
                         str(exr)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     np.testing.assert_array_equal(pkg.read_exr(exr), out["plain"][0])
+
+
+def test_cache_modes_need_a_capacity(exe):
+    for flag in ("--irradiance-cache", "--adrrs"):
+        r = subprocess.run([str(exe), "8", "8", "0", "4", "cornell", flag], capture_output=True, text=True)
+        assert r.returncode != 0 and "IC_SIZE" in r.stderr
+
+
+@pytest.mark.gpu
+def test_irradiance_cache_and_adrrs_renders(exe, tmp_path, cuda, pkg, abi):
+    """IC_SIZE with --irradiance-cache (prepare frames, then frames that use and
+    grow the cache) and with --adrrs (the estimate frame, then roulette and
+    splitting): images of the Cornell box near the plain render's mean (the
+    cache's irradiance is an approximation: within 10 %; ADRRS is unbiased:
+    within 3 %)."""
+    W, H = 96, 54
+    torch = cuda
+    sc = pkg.Scene.cornell(W, H)
+    img = torch.zeros(W * H * 3, dtype=torch.float32, device="cuda")
+    sc.render(abi.render_params(spp=1024, max_depth=10, seed=99), img)
+    ref = float(img.mean()) / 1024
+    sc.close()
+    for mode, tol in (("--irradiance-cache", 0.10), ("--adrrs", 0.03)):
+        pfm = tmp_path / "ic.pfm"
+        r = subprocess.run([str(exe), str(W), str(H), "20000", "8", "cornell", "--spp", "256", "--no-guiding",
+                            "--prepare-frames", "20", mode, "--out", str(pfm)], capture_output=True, text=True,
+                           timeout=300)
+        assert r.returncode == 0, r.stderr
+        info = json.loads(r.stdout.strip().splitlines()[-1])
+        assert info["irradiance_cache_entries"] > 20 and info["adrrs"] == (mode == "--adrrs")
+        got = read_pfm(pfm)
+        assert np.isfinite(got).all()
+        assert abs(got.mean() - ref) / ref < tol, (mode, got.mean(), ref)

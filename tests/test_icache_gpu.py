@@ -194,3 +194,76 @@ def test_grown_cache_is_repeatable_and_well_formed(cuda, pkg, abi):
     assert (np.linalg.norm(a["rot_grad"], axis=1) <= 5.0 + 1e-4).all()
     assert (np.linalg.norm(a["trans_grad"], axis=1) <= 5.0 + 1e-4).all()
     assert (a["num_updates"] > 1).any()  # some entries were updated
+
+
+def _adrrs_setup(torch, fixture, abi, split, s=S.ADRRS_S):
+    """The Cornell box of the estimator comparison with the reference-made
+    cache and the fixture's pixel estimate (the reference's plain estimator)."""
+    sc = S.cornell()
+    sc.set_irradiance_cache(capacity=S.IC_CAPACITY, a=S.IC_A, create_prob=0.0, update_prob=0.0)
+    sc.set_irradiance_cache_entries(fixture["render__entries"])
+    est = torch.from_numpy(np.ascontiguousarray(fixture["adrrs__estimate"], dtype=np.float32).reshape(-1)).cuda()
+    sc.set_adrrs(est, s=s, split=bool(split))
+    return sc, est
+
+
+@pytest.mark.parametrize("split", [0, 1])
+def test_adrrs_render_converges_to_reference_adrrs(split, fixture, cuda, pkg, abi):
+    """The ADRRS image converges to the reference's own estimator with ADRRS
+    (its weight windows, roulette and split paths, in the fixture) - with
+    splitting also to the plain estimator, since roulette and splitting then
+    change only the noise.  Without splitting the reference's rule is biased:
+    a path the window would split in two keeps its whole throughput while one
+    kept single is divided by q (raytrace.rgen:1094-1101); the library keeps
+    that rule."""
+    torch = cuda
+    sc, est = _adrrs_setup(torch, fixture, abi, split)
+    parts = []
+    for p in range(S.PARTS):
+        params = abi.render_params(spp=S.SPP, max_depth=S.PATH_LENGTH, seed=3000 + p, use_nee=1, use_mis=1,
+                                   flags=abi.PG_RENDER_ADRRS)
+        img, _ = render_gpu(torch, sc, params)
+        parts.append(S.blocks(img / S.SPP))
+    got = np.stack(parts)
+    import estimator_scenes as E
+    z, ratio, ok = E.compare_blocks(fixture[f"adrrs__blocks_split{split}"], got)
+    assert ok, f"split {split}: block |z| {z:.2f}, mean ratio {ratio:.4f} against the reference's ADRRS"
+    if split:
+        plain = np.load(GOLDEN / "estimator_ref.npz")["cornell_mis__blocks"]
+        z, ratio, ok = E.compare_blocks(plain, got)
+        assert ok, f"block |z| {z:.2f}, mean ratio {ratio:.4f} against the plain estimator"
+    sc.close()
+
+
+def test_adrrs_roulette_and_splitting_change_the_work(fixture, cuda, pkg, abi):
+    torch = cuda
+    rays = {}
+    for name, flags, split, s in (("plain", 0, 0, 1.5), ("rr", abi.PG_RENDER_ADRRS, 0, 1.5),
+                                  ("split", abi.PG_RENDER_ADRRS, 1, 1.5)):
+        sc, est = _adrrs_setup(torch, fixture, abi, split, s)
+        params = abi.render_params(spp=64, max_depth=S.PATH_LENGTH, seed=7, use_nee=1, use_mis=1, flags=flags)
+        _, st = render_gpu(torch, sc, params)
+        rays[name] = st.extension_rays
+        sc.close()
+    # with a narrow window roulette ends paths early, and splitting adds copies to the same decisions
+    assert rays["rr"] < 0.95 * rays["plain"], rays
+    assert rays["split"] > rays["rr"], rays
+
+
+def test_adrrs_rejects_missing_estimate_and_recording_with_splits(cuda, pkg, abi):
+    torch = cuda
+    sc = S.cornell()
+    sc.set_irradiance_cache(capacity=16, create_prob=0.0, update_prob=0.0)
+    img = torch.zeros(S.W * S.H * 3, dtype=torch.float32, device="cuda")
+    with pytest.raises(pkg.PathGuideError):
+        sc.render(abi.render_params(spp=1, max_depth=4, flags=abi.PG_RENDER_ADRRS), img)
+    est = torch.ones(S.W * S.H * 3, dtype=torch.float32, device="cuda")
+    sc.set_adrrs(est, s=5.0, split=True)
+    rec = torch.zeros(S.W * S.H * 16 * 10, dtype=torch.float32, device="cuda")
+    ctx = pkg.FitContext(abi.default_fit_config(), max_regions=8)
+    ctx.set_regions(2, np.array(sc.info().aabb, dtype=np.float32))
+    with pytest.raises(pkg.PathGuideError):
+        sc.render(abi.render_params(spp=1, max_depth=4, record_samples=1, flags=abi.PG_RENDER_ADRRS), img,
+                  guide=ctx, records_dev=rec)
+    ctx.close()
+    sc.close()

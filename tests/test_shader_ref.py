@@ -49,7 +49,7 @@ def test_fp64_oracle_matches_reference_shader_functions(fixture):
     assert not failures, "\n".join(failures[:20])
     # every family was exercised
     for name in ("fresnel", "eval", "sample_dir", "sample_pdf", "vmm_pdf", "vmm_sample", "continue_dir",
-                 "continue_tc", "continue_pdf", "to_world"):
+                 "continue_tc", "continue_pdf", "to_world", "weight_window_n", "weight_window_q", "approx_diffuse"):
         assert report[name][0] > 100, name
 
 
