@@ -327,7 +327,9 @@ __global__ void __launch_bounds__(kDistThreads) distance_partial_kernel(const pg
                                                                         const uint32_t *item_offsets, float *partial,
                                                                         uint64_t cap_items, uint32_t *error_word) {
     constexpr int NW = kDistThreads / 32;
-    __shared__ float c_ax[16], c_ay[16], c_az[16], c_c0[16], c_cm[16], c_lk[16], c_ipi[16];
+    // component constants as pairs (component 2j in .x, 2j + 1 in .y): the
+    // per-sample arithmetic runs on packed FP32x2 instructions
+    __shared__ float2 c_ax[8], c_ay[8], c_az[8], c_c0[8], c_cm[8], c_lk[8], c_ipi[8];
     __shared__ float red[NW][32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t n_items = item_offsets[n_regions];
@@ -353,47 +355,56 @@ __global__ void __launch_bounds__(kDistThreads) distance_partial_kernel(const pg
             const bool on = c < (int)K && s->norm[c] > 0.0f && s->weight[c] > 0.0f;
             const float kl = s->kappa[c] * kLog2e;
             const float ln = on ? log2f(s->norm[c]) : -INFINITY;
-            c_ax[c] = kl * s->mu_x[c];
-            c_ay[c] = kl * s->mu_y[c];
-            c_az[c] = kl * s->mu_z[c];
-            c_c0[c] = ln - kl;
-            c_cm[c] = ln;
-            c_lk[c] = on ? log2f(s->weight[c]) : -INFINITY;
-            c_ipi[c] = on ? 1.0f / s->weight[c] : 0.0f;
+            float *ax = reinterpret_cast<float *>(c_ax), *ay = reinterpret_cast<float *>(c_ay),
+                  *az = reinterpret_cast<float *>(c_az), *c0 = reinterpret_cast<float *>(c_c0),
+                  *cm = reinterpret_cast<float *>(c_cm), *lk = reinterpret_cast<float *>(c_lk),
+                  *ipi = reinterpret_cast<float *>(c_ipi);
+            ax[c] = kl * s->mu_x[c];
+            ay[c] = kl * s->mu_y[c];
+            az[c] = kl * s->mu_z[c];
+            c0[c] = ln - kl;
+            cm[c] = ln;
+            lk[c] = on ? log2f(s->weight[c]) : -INFINITY;
+            ipi[c] = on ? 1.0f / s->weight[c] : 0.0f;
         }
         __syncthreads();
-        float bw[16], bwd[16];
+        float2 bw[8], bwd[8];
 #pragma unroll
-        for (int c = 0; c < 16; ++c) bw[c] = bwd[c] = 0.0f;
+        for (int j = 0; j < 8; ++j) bw[j] = bwd[j] = make_float2(0.0f, 0.0f);
         const uint32_t b = offsets[r] + (item - item_offsets[r]) * kDistChunk;
         const uint32_t e = min(offsets[r + 1], b + kDistChunk);
         for (uint32_t i = b + tid; i < e; i += kDistThreads) {
             const float t = dist[i];
             if (!(t > 0.0f)) continue;
             const float4 d = dirw[i];
-            float ek[16];
+            const float2 dx2 = make_float2(d.x, d.x), dy2 = make_float2(d.y, d.y), dz2 = make_float2(d.z, d.z);
+            float2 ek[8];
             float p = 0.0f;
 #pragma unroll
-            for (int c = 0; c < 16; ++c) {
-                float a = fmaf(c_az[c], d.z, c_c0[c]);
-                a = fmaf(c_ay[c], d.y, a);
-                a = fmaf(c_ax[c], d.x, a);
-                ek[c] = ex2_approx(fminf(a, c_cm[c]) + c_lk[c]);
-                p += ek[c];
+            for (int j = 0; j < 8; ++j) {
+                float2 a = __ffma2_rn(c_az[j], dz2, c_c0[j]);
+                a = __ffma2_rn(c_ay[j], dy2, a);
+                a = __ffma2_rn(c_ax[j], dx2, a);
+                const float2 m = c_cm[j], l = c_lk[j];
+                ek[j].x = ex2_approx(fminf(a.x, m.x) + l.x);
+                ek[j].y = ex2_approx(fminf(a.y, m.y) + l.y);
+                p += ek[j].x;
+                p += ek[j].y;
             }
             if (!(p > kPmmEps)) continue;
             const float sc = d.w / p;
             const float it = 1.0f / t;
+            const float2 sc2 = make_float2(sc, sc), it2 = make_float2(it, it);
 #pragma unroll
-            for (int c = 0; c < 16; ++c) {
-                const float a = ek[c] * ek[c] * c_ipi[c] * sc;
-                bw[c] += a;
-                bwd[c] += a * it;
+            for (int j = 0; j < 8; ++j) {
+                const float2 a = __fmul2_rn(__fmul2_rn(__fmul2_rn(ek[j], ek[j]), c_ipi[j]), sc2);
+                bw[j] = __fadd2_rn(bw[j], a);
+                bwd[j] = __ffma2_rn(a, it2, bwd[j]);
             }
         }
 #pragma unroll
         for (int c = 0; c < 16; ++c) {
-            float x = bw[c], y = bwd[c];
+            float x = (c & 1) ? bw[c >> 1].y : bw[c >> 1].x, y = (c & 1) ? bwd[c >> 1].y : bwd[c >> 1].x;
             for (int o = 16; o > 0; o >>= 1) {
                 x += __shfl_xor_sync(0xffffffffu, x, o);
                 y += __shfl_xor_sync(0xffffffffu, y, o);

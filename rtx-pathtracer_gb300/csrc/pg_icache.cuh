@@ -168,69 +168,87 @@ __device__ __forceinline__ void ic_push(const DevIc &ic, V o, V n, int32_t targe
     ic.requests[q] = r;
 }
 
+// The number of queued requests i with sel(i) whose key is below `key`,
+// counted by the CTA through shared-memory tiles of keys (every thread of
+// the CTA takes part; `active` threads use the count).
+constexpr uint32_t kIcRankTile = 512;
+template <class Sel>
+__device__ __forceinline__ uint32_t ic_rank(const DevIc &ic, uint32_t n_req, uint64_t key, bool active, Sel sel) {
+    __shared__ uint64_t tk[kIcRankTile];
+    uint32_t rank = 0;
+    for (uint32_t base = 0; base < n_req; base += kIcRankTile) {
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < kIcRankTile; j += blockDim.x) {
+            const uint32_t i = base + j;
+            tk[j] = (i < n_req && sel(i)) ? ic_key(ic.requests[i]) : ~0ull;
+        }
+        __syncthreads();
+        if (active) {
+            const uint32_t m = min(kIcRankTile, n_req - base);
+            for (uint32_t j = 0; j < m; ++j) rank += tk[j] < key ? 1u : 0u;
+        }
+    }
+    return rank;
+}
+
 // Update requests take their entries in request order from the round-robin
 // position (updateIrradianceCache, raytrace.rgen:1334-1345: the position
 // advances by one per request, and a request that finds it past the last
 // entry sets it back to 0 and updates nothing).  An entry that an earlier
-// request of the same pass already updates is skipped.  Ranks by counting:
-// O(requests^2) over at most req_cap requests.
+// request of the same pass already updates is skipped.  One thread per
+// request (the grid covers req_cap); ranks by counting, O(requests^2).
 __global__ void __launch_bounds__(128) k_ic_assign(DevIc ic) {
     const uint32_t n_req = min(ic.state[0], ic.req_cap);
+    if (blockIdx.x * blockDim.x >= n_req) return;  // the whole CTA
     const uint32_t n = ic.state[2], start = ic.state[1];
     const uint32_t first = n > start ? n - start : 0u;  // requests before the first reset
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n_req; q += gridDim.x * blockDim.x) {
-        IcRequest &rq = ic.requests[q];
-        if (rq.bounce != kIcUpdateBounce) continue;
-        const uint64_t key = ic_key(rq);
-        uint32_t rank = 0;
-        for (uint32_t i = 0; i < n_req; ++i) {
-            const IcRequest &o = ic.requests[i];
-            rank += (o.bounce == kIcUpdateBounce && ic_key(o) < key) ? 1u : 0u;
-        }
-        int32_t target = -2;
-        if (rank < first) {
-            target = (int32_t)(start + rank);
-        } else if (n > 0) {
-            const uint32_t r = rank - first, pos = r % (n + 1u);
-            const uint32_t t = pos - 1u;
-            // pos 0: the reset; a second cycle, or an entry of the first stretch: already updated
-            if (pos != 0 && r < n + 1u && (first == 0 || t < start)) target = (int32_t)t;
-        }
-        if (target >= 0) {
-            const pg_ic_entry &e = ic.entries[target];
-            if (e.num_updates < 1u) {
-                target = -2;
-            } else {
-                for (int c = 0; c < 3; ++c) {
-                    rq.o[c] = e.center[c];
-                    rq.n[c] = e.normal[c];
-                }
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = q < n_req && ic.requests[q].bounce == kIcUpdateBounce;
+    const uint64_t key = active ? ic_key(ic.requests[q]) : 0ull;
+    const uint32_t rank = ic_rank(ic, n_req, key, active,
+                                  [&](uint32_t i) { return ic.requests[i].bounce == kIcUpdateBounce; });
+    if (!active) return;
+    IcRequest &rq = ic.requests[q];
+    int32_t target = -2;
+    if (rank < first) {
+        target = (int32_t)(start + rank);
+    } else if (n > 0) {
+        const uint32_t r = rank - first, pos = r % (n + 1u);
+        const uint32_t t = pos - 1u;
+        // pos 0: the reset; a second cycle, or an entry of the first stretch: already updated
+        if (pos != 0 && r < n + 1u && (first == 0 || t < start)) target = (int32_t)t;
+    }
+    if (target >= 0) {
+        const pg_ic_entry &e = ic.entries[target];
+        if (e.num_updates < 1u) {
+            target = -2;
+        } else {
+            for (int c = 0; c < 3; ++c) {
+                rq.o[c] = e.center[c];
+                rq.n[c] = e.normal[c];
             }
         }
-        rq.target = target;
     }
+    rq.target = target;
 }
 
 // New entries take consecutive slots after the existing ones in request
 // order, counting only requests whose hemisphere saw something
-// (createIrradianceCache, raytrace.rgen:1383-1421).
+// (createIrradianceCache, raytrace.rgen:1383-1421).  One thread per request.
 __global__ void __launch_bounds__(128) k_ic_slots(DevIc ic, const IcResult *res) {
     const uint32_t n_req = min(ic.state[0], ic.req_cap);
+    if (blockIdx.x * blockDim.x >= n_req) return;  // the whole CTA
     const uint32_t n = ic.state[2];
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n_req; q += gridDim.x * blockDim.x) {
-        IcRequest &rq = ic.requests[q];
-        if (rq.target != -1 || !(res[q].harmonic_r >= 0.0f)) continue;
-        const uint64_t key = ic_key(rq);
-        uint32_t rank = 0;
-        for (uint32_t i = 0; i < n_req; ++i) {
-            const IcRequest &o = ic.requests[i];
-            rank += (o.target == -1 && res[i].harmonic_r >= 0.0f && ic_key(o) < key) ? 1u : 0u;
-        }
-        const uint32_t slot = n + rank;
-        if (slot < ic.capacity) {
-            rq.slot = slot;
-            atomicAdd(&ic.state[3], 1u);
-        }
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    auto creates = [&](uint32_t i) { return ic.requests[i].target == -1 && res[i].harmonic_r >= 0.0f; };
+    const bool active = q < n_req && creates(q);
+    const uint64_t key = active ? ic_key(ic.requests[q]) : 0ull;
+    const uint32_t rank = ic_rank(ic, n_req, key, active, creates);
+    if (!active) return;
+    const uint32_t slot = n + rank;
+    if (slot < ic.capacity) {
+        ic.requests[q].slot = slot;
+        atomicAdd(&ic.state[3], 1u);
     }
 }
 
@@ -323,52 +341,66 @@ __device__ __forceinline__ void ic_cell_range(const DevIc &ic, const pg_ic_entry
         hi[c] = ic_cell_coord(e.center[c] + e.radius, ic.lo[c], ic.inv_cell[c]);
     }
 }
+// One thread per (entry, z) slab of cells: an entry's box (it can cover
+// thousands of cells) spreads over up to 32 threads.
 __global__ void __launch_bounds__(128) k_ic_grid_count(DevIc ic, uint32_t *count) {
     const uint32_t n = ic.state[2];
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint64_t slabs = (uint64_t)n * kIcGrid;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < slabs;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t i = (uint32_t)(t / kIcGrid);
+        const int z = (int)(t % kIcGrid);
         int lo[3], hi[3];
         ic_cell_range(ic, ic.entries[i], lo, hi);
-        for (int z = lo[2]; z <= hi[2]; ++z)
-            for (int y = lo[1]; y <= hi[1]; ++y)
-                for (int x = lo[0]; x <= hi[0]; ++x) atomicAdd(&count[(z * kIcGrid + y) * kIcGrid + x], 1u);
+        if (z < lo[2] || z > hi[2]) continue;
+        for (int y = lo[1]; y <= hi[1]; ++y)
+            for (int x = lo[0]; x <= hi[0]; ++x) atomicAdd(&count[(z * kIcGrid + y) * kIcGrid + x], 1u);
     }
 }
-// Exclusive scan of the cell counts into start (one CTA of 1024 threads,
-// 32 cells each); start[kIcCells] is the total.
+// Exclusive scan of the cell counts into start, one CTA of 32 warps: warp w
+// scans cells [1024 w, 1024 (w + 1)) in coalesced 32-cell chunks;
+// start[kIcCells] is the total.
 __global__ void __launch_bounds__(1024) k_ic_grid_scan(const uint32_t *count, uint32_t *start) {
-    constexpr uint32_t per = kIcCells / 1024;
-    __shared__ uint32_t part[1024];
-    const uint32_t t = threadIdx.x;
-    uint32_t s = 0;
-    for (uint32_t i = 0; i < per; ++i) s += count[t * per + i];
-    part[t] = s;
+    constexpr uint32_t per_warp = kIcCells / 32;
+    __shared__ uint32_t wsum[32];
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t *c = count + w * per_warp;
+    uint32_t tot = 0;
+    for (uint32_t k = lane; k < per_warp; k += 32) tot += c[k];
+    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    if (lane == 0) wsum[w] = tot;
     __syncthreads();
-    for (uint32_t o = 1; o < 1024; o <<= 1) {
-        const uint32_t v = t >= o ? part[t - o] : 0u;
-        __syncthreads();
-        part[t] += v;
-        __syncthreads();
+    uint32_t base = 0;
+    for (uint32_t k = 0; k < w; ++k) base += wsum[k];
+    for (uint32_t k0 = 0; k0 < per_warp; k0 += 32) {
+        const uint32_t v = c[k0 + lane];
+        uint32_t inc = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= (uint32_t)o) inc += u;
+        }
+        start[w * per_warp + k0 + lane] = base + inc - v;
+        base += __shfl_sync(0xffffffffu, inc, 31);
     }
-    uint32_t base = part[t] - s;
-    for (uint32_t i = 0; i < per; ++i) {
-        start[t * per + i] = base;
-        base += count[t * per + i];
-    }
-    if (t == 1023) start[kIcCells] = part[1023];
+    if (threadIdx.x == 1023) start[kIcCells] = base;
 }
 __global__ void __launch_bounds__(128) k_ic_grid_fill(DevIc ic, const uint32_t *start, uint32_t *fill,
                                                       uint32_t *refs) {
     const uint32_t n = ic.state[2];
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint64_t slabs = (uint64_t)n * kIcGrid;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < slabs;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t i = (uint32_t)(t / kIcGrid);
+        const int z = (int)(t % kIcGrid);
         int lo[3], hi[3];
         ic_cell_range(ic, ic.entries[i], lo, hi);
-        for (int z = lo[2]; z <= hi[2]; ++z)
-            for (int y = lo[1]; y <= hi[1]; ++y)
-                for (int x = lo[0]; x <= hi[0]; ++x) {
-                    const uint32_t c = (z * kIcGrid + y) * kIcGrid + x;
-                    const uint32_t slot = start[c] + atomicAdd(&fill[c], 1u);
-                    if (slot < ic.cap_refs) refs[slot] = i;
-                }
+        if (z < lo[2] || z > hi[2]) continue;
+        for (int y = lo[1]; y <= hi[1]; ++y)
+            for (int x = lo[0]; x <= hi[0]; ++x) {
+                const uint32_t cc = (z * kIcGrid + y) * kIcGrid + x;
+                const uint32_t slot = start[cc] + atomicAdd(&fill[cc], 1u);
+                if (slot < ic.cap_refs) refs[slot] = i;
+            }
     }
 }
 // Each cell's list in entry order (insertion sort; lists are short), so a

@@ -1723,7 +1723,8 @@ int ic_build_grid(pg_scene *sc, const DevIc &D, cudaStream_t s) {
     if (cudaMemsetAsync(c.cell_count, 0, sizeof(uint32_t) * kIcCells, s) != cudaSuccess ||
         cudaMemsetAsync(c.cell_fill, 0, sizeof(uint32_t) * kIcCells, s) != cudaSuccess)
         return scene_error(PG_ERR_CUDA, "irradiance cache grid reset");
-    const uint32_t G = std::min((c.cfg.capacity + 127) / 128, 4u * sm_count());
+    // (entry, z) slabs, grid-stride over the entries the device holds
+    const uint32_t G = 16u * sm_count();
     k_ic_grid_count<<<G, 128, 0, s>>>(D, c.cell_count);
     k_ic_grid_scan<<<1, 1024, 0, s>>>(c.cell_count, c.cell_start);
     k_ic_grid_fill<<<G, 128, 0, s>>>(D, c.cell_start, c.cell_fill, c.refs);
