@@ -188,7 +188,12 @@ int pg_region_states_device(pg_ctx *ctx, pg_region_state **dev_out);
  * launch.  `dirw` (device, 16-byte aligned) holds one float4
  * {direction.xyz, weight} per sample, grouped by region; `offsets` (device)
  * holds n_regions+1 sample offsets.  Regions run different iteration counts
- * (relative log-likelihood test per region).  Replaces the serial loop
+ * (relative log-likelihood test per region).  The launch takes regions in
+ * order of expected work - samples times the iteration count of the region's
+ * last fit (20 where it has none) - and gives those above the tuning's
+ * large_threshold (in samples at 20 iterations) a cluster of CTAs, so a
+ * region's team, and with it the low bits of its statistics' sums, follows
+ * its state's last iteration count.  Replaces the serial loop
  * PathGuiding::update -> updateRegion -> VMMFactory::fit / updateFit
  * (src/PathGuiding.cpp:281-288, 350-368; VMMFactory.h:157-216, 305-362). */
 int pg_fit_regions(pg_ctx *ctx, const float *dirw, const uint32_t *offsets,
@@ -226,8 +231,9 @@ typedef struct pg_fit_tuning {
     uint32_t components_per_thread; /* 8 or 16: K=16 mixtures use 2 or 1 threads per sample */
     uint32_t unroll;                /* samples per loop trip: 1, 2 or 4 (4: 128
                                        threads per CTA)                         */
-    uint32_t large_threshold;       /* regions with more samples are shared by a
-                                       cluster (0: smem_samples)                */
+    uint32_t large_threshold;       /* regions with more expected work (samples
+                                       x last iterations / 20) are shared by a
+                                       cluster (0: 24576)                       */
     uint32_t stream_stages;         /* slices larger than smem_samples stream
                                        from L2 through a ring of this many
                                        TMA-filled shared-memory stages (0: 2; at

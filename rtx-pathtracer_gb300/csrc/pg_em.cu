@@ -106,7 +106,8 @@ int fit_range(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t 
     const uint32_t cap = t.smem_samples ? t.smem_samples : 4096u;
     const uint32_t large_threshold =
         cluster > 1 ? (t.large_threshold ? t.large_threshold : 24576u) : 0xFFFFFFFFu;
-    order_regions_kernel<128><<<1, 1024, 0, s>>>(offsets, n_regions, ctx->d_order, large_threshold, ctx->d_counters + 3);
+    order_regions_kernel<128><<<1, 1024, 0, s>>>(offsets, n_regions, ctx->d_order, large_threshold, ctx->d_counters + 3,
+                                                 ctx->d_states + first);
     st = check_cuda(ctx, cudaGetLastError(), "order_regions launch");
     if (st) return st;
     EmArgs args;

@@ -976,21 +976,33 @@ static int launch_fit(pg_ctx *ctx, const EmArgs &args_in, cudaStream_t s, uint32
 }
 
 
-// Orders region ids by sample count, largest first (LPT), with a stable
-// counting sort over 128 logarithmic size buckets (4 per octave).  One CTA of
-// 1024 threads; n_regions of any size.  NB = 128 buckets.
+// Orders region ids by expected work, largest first (LPT), with a stable
+// counting sort over 128 logarithmic buckets (4 per octave).  The work of a
+// region is its sample count times its iteration count over 20: a fitted
+// region's last fit's count (states, may be null) predicts this fit's, others
+// count 20 - so with forced iterations (always 20) the order is by sample
+// count, and with the convergence test a region that iterated long last time
+// starts early and, above the threshold, gets a cluster (the tail of a
+// 100-iteration region on one CTA otherwise outlasts the rest of the fit).
+// One CTA of 1024 threads; n_regions of any size.  NB = 128 buckets.
 template <int NB>
 __global__ void __launch_bounds__(1024) order_regions_kernel(const uint32_t *offsets, uint32_t n_regions,
                                                              uint32_t *order, uint32_t large_threshold,
-                                                             uint32_t *n_large_out) {
+                                                             uint32_t *n_large_out,
+                                                             const pg_region_state *states = nullptr) {
     __shared__ uint32_t hist[NB];
     __shared__ uint32_t base[NB];
     __shared__ uint32_t warp_cnt[32][NB];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     auto bucket_of = [&](uint32_t r) -> int {
-        const uint32_t n = offsets[r + 1] - offsets[r];
+        float n = (float)(offsets[r + 1] - offsets[r]);
+        if (states) {
+            const pg_region_state &st = states[r];
+            const uint32_t it = (st.flags & PG_STATE_FITTED) ? st.iters_last : 0u;
+            if (it > 0) n = n * (float)it * (1.0f / 20.0f);
+        }
         // descending: bucket 0 = largest
-        const float l = log2f((float)n + 1.0f) * 4.0f;
+        const float l = log2f(n + 1.0f) * 4.0f;
         int k = (int)l;
         k = k < 0 ? 0 : (k > NB - 1 ? NB - 1 : k);
         return NB - 1 - k;

@@ -169,7 +169,8 @@ extern "C" int pg_fit_regions_noalloc(const pg_fit_config *cfg, pg_region_state 
     noalloc_prepare_kernel<<<1, 64, 0, s>>>(table, scr);
     if (cudaGetLastError() != cudaSuccess) return PG_ERR_CUDA;
     const uint32_t cluster = 2u, cap = 4096u, large_threshold = 24576u;
-    order_regions_kernel<128><<<1, 1024, 0, s>>>(offsets, n_regions, scr->order, large_threshold, scr->counters + 3);
+    order_regions_kernel<128><<<1, 1024, 0, s>>>(offsets, n_regions, scr->order, large_threshold, scr->counters + 3,
+                                                 states);
     if (cudaGetLastError() != cudaSuccess) return PG_ERR_CUDA;
     EmArgs args;
     args.states = states;
