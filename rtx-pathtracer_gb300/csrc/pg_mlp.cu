@@ -503,7 +503,9 @@ __global__ void __launch_bounds__(32 * kWarps) k_wgrad(WgradArgs A) {
 struct AdamArgs {
     const float *partials;
     uint32_t n_blocks;
-    const double *scalars;   // {sum w (-log q), sum w}
+    double *scalars;         // {sum w (-log q), sum w}
+    const float *loss_partials;  // not null: the scalars are summed here from these
+    uint32_t n_loss;             // (pairs), as k_tc_scalars sums them, and written
     float *theta, *m, *v;
     __nv_bfloat16 *wb;
     __nv_bfloat16 *img;      // the tensor-core kernel's weight image
@@ -537,8 +539,31 @@ __device__ __forceinline__ int wb_index(int p) {
 constexpr int kAdamGroups = 8;
 __global__ void __launch_bounds__(32 * kAdamGroups) k_reduce_adam(AdamArgs A) {
     __shared__ float ps[kAdamGroups][32], pc[kAdamGroups][32];
+    __shared__ double sl[32 * kAdamGroups], sw[32 * kAdamGroups];
     const int lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
     const int p = blockIdx.x * 32 + lane;
+    if (A.loss_partials) {
+        // the batch's loss and weight sums, in k_tc_scalars' order (same block size)
+        double l = 0.0, w = 0.0;
+        for (uint32_t i = threadIdx.x; i < A.n_loss; i += blockDim.x) {
+            l += A.loss_partials[2 * i];
+            w += A.loss_partials[2 * i + 1];
+        }
+        sl[threadIdx.x] = l;
+        sw[threadIdx.x] = w;
+        __syncthreads();
+        for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+            if ((int)threadIdx.x < st) {
+                sl[threadIdx.x] += sl[threadIdx.x + st];
+                sw[threadIdx.x] += sw[threadIdx.x + st];
+            }
+            __syncthreads();
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            A.scalars[0] = sl[0];
+            A.scalars[1] = sw[0];
+        }
+    }
     {
         float s = 0.0f, c = 0.0f;
         if (p < NPARAM)
@@ -555,7 +580,7 @@ __global__ void __launch_bounds__(32 * kAdamGroups) k_reduce_adam(AdamArgs A) {
         neumaier_add(s, c, ps[g][lane]);
         c += pc[g][lane];
     }
-    const double W = A.scalars[1];
+    const double W = A.loss_partials ? sw[0] : A.scalars[1];
     const float gr = W > 0.0 ? (float)((double)(s + c) / W) : 0.0f;
     if (A.grad_out) {
         A.grad_out[p] = gr;
@@ -1276,6 +1301,7 @@ struct pg_mlp {
     uint32_t cap_batches = 0;
     uint32_t wg_blocks = 0;
     uint32_t wg_used = 0;            // row blocks of the last weight-gradient launch
+    uint32_t loss_pending = 0;       // loss partials of the last batch the update still sums
     uint32_t step = 0;
     size_t smem = 0;
     __nv_bfloat16 *img = nullptr;    // tensor-core kernel's weight image
@@ -1301,7 +1327,8 @@ FwdArgs fwd_args(const pg_mlp *M) {
 
 // forward + backward + weight gradients of one batch; leaves the partials and
 // the batch's scalars in scalars[2 * slot]
-int batch_gradients(pg_mlp *M, const pg_directional_data *rec, uint32_t n, uint32_t slot, cudaStream_t s) {
+int batch_gradients(pg_mlp *M, const pg_directional_data *rec, uint32_t n, uint32_t slot, cudaStream_t s,
+                    bool scalars_now = true) {
     if (M->path == PG_MLP_PATH_TCGEN05) {
         const uint32_t tiles = (n + tc::TILE - 1) / tc::TILE;
         const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)M->sm_count);
@@ -1319,7 +1346,9 @@ int batch_gradients(pg_mlp *M, const pg_directional_data *rec, uint32_t n, uint3
         T.loss_partials = M->fwd_partials;
         T.err = M->err;
         tc::k_train_tc<tc::kTpr><<<grid, tc::TILE * tc::kTpr, tc::SM_TOTAL, s>>>(T);
-        tc::k_tc_scalars<<<1, 256, 0, s>>>(M->fwd_partials, grid, M->scalars + 2 * slot);
+        // the batch's scalars: now, or summed by the update that follows (one launch fewer)
+        M->loss_pending = scalars_now ? 0u : grid;
+        if (scalars_now) tc::k_tc_scalars<<<1, 256, 0, s>>>(M->fwd_partials, grid, M->scalars + 2 * slot);
         if (cudaGetLastError() != cudaSuccess) return mlp_error(PG_ERR_CUDA, "surrogate gradient launch");
         M->wg_used = grid;
         return PG_OK;
@@ -1353,6 +1382,11 @@ int reduce_step(pg_mlp *M, uint32_t slot, float *grad_out, cudaStream_t s) {
     A.partials = M->wg_partials;
     A.n_blocks = M->wg_used;
     A.scalars = M->scalars + 2 * slot;
+    if (M->loss_pending) {
+        A.loss_partials = M->fwd_partials;
+        A.n_loss = M->loss_pending;
+        M->loss_pending = 0;
+    }
     A.theta = M->theta;
     A.m = M->m;
     A.v = M->v;
@@ -1576,7 +1610,7 @@ int pg_mlp_train(pg_mlp *M, const pg_directional_data *records, uint64_t n, floa
     for (uint32_t b = 0; b < batches; ++b) {
         const uint64_t first = (uint64_t)b * B;
         const uint32_t cnt = (uint32_t)std::min<uint64_t>(B, n - first);
-        if (int st = batch_gradients(M, records + first, cnt, b, s)) return st;
+        if (int st = batch_gradients(M, records + first, cnt, b, s, false)) return st;
         if (int st = reduce_step(M, b, nullptr, s)) return st;
     }
     if (loss_out) {
