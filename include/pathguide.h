@@ -204,11 +204,16 @@ int pg_fit_regions(pg_ctx *ctx, const float *dirw, const uint32_t *offsets,
  * 276-312): dirw_host holds float4 {direction, weight} per sample grouped by
  * region, offsets_host n_regions + 1 sample offsets.  The samples go to a
  * context-owned device buffer on a copy stream that starts behind the work
- * already queued on `stream`, then the fit runs on `stream` (page-locked host
- * memory copies asynchronously; pageable memory works through staging).
+ * already queued on `stream`, in up to 16 chunks cut at region boundaries,
+ * the chunks holding the largest regions first; the fit runs on `stream` from
+ * the start and each region waits for its chunk (page-locked host memory
+ * copies asynchronously; pageable memory works through staging).  A region
+ * whose chunk has not arrived after about two seconds stops waiting and
+ * pg_sync_status then reports PG_ERR_TIMEOUT.
  * Same results as pg_fit_regions on the same samples; the states stay on the
  * device (pg_get_region_states).  Both buffers must stay valid until the
- * stream reaches the fit. */
+ * stream reaches the fit; work queued on `stream` afterwards runs after
+ * every copy. */
 int pg_fit_regions_host(pg_ctx *ctx, const float *dirw_host, const uint32_t *offsets_host, uint32_t n_regions,
                         int mode, void *stream);
 

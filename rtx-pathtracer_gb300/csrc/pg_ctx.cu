@@ -129,6 +129,8 @@ int pg_ctx_destroy(pg_ctx *ctx) {
     extras_release(ctx);
     cudaFree(ctx->h2d_dirw);
     cudaFree(ctx->h2d_offsets);
+    cudaFree(ctx->h2d_ready);
+    if (ctx->h2d_ones) cudaFreeHost(ctx->h2d_ones);
     if (ctx->h2d_stream) cudaStreamDestroy(ctx->h2d_stream);
     for (cudaEvent_t e : ctx->h2d_events)
         if (e) cudaEventDestroy(e);

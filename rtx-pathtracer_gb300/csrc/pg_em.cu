@@ -1,6 +1,7 @@
 // pg_em.cu - host side of the batched EM fit (C ABI entry points), the
 // largest-first region ordering and the log-likelihood evaluation kernel.
 #include <algorithm>
+#include <vector>
 
 #include "pg_em_kernels.cuh"
 
@@ -89,7 +90,7 @@ namespace pg {
 // The fit of regions [first, first + n_regions): offsets points at region
 // first's entry, the states written are first's onwards.
 int fit_range(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t first, uint32_t n_regions, int mode,
-              cudaStream_t s) {
+              cudaStream_t s, const SampleArrival *arrival) {
     ctx->last_launches = 0;
     if (n_regions == 0) return PG_OK;
     guide_mark_stale(ctx);
@@ -110,7 +111,7 @@ int fit_range(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t 
                                                  ctx->d_states + first);
     st = check_cuda(ctx, cudaGetLastError(), "order_regions launch");
     if (st) return st;
-    EmArgs args;
+    EmArgs args{};
     args.states = ctx->d_states + first;
     args.dirw = reinterpret_cast<const float4 *>(dirw);
     args.offsets = offsets;
@@ -126,6 +127,10 @@ int fit_range(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t 
     args.ll_out = nullptr;
     args.smem_cap = cap;
     args.stages = t.stream_stages ? t.stream_stages : 2u;
+    if (arrival)
+        args.arrival = *arrival;
+    else
+        memset(&args.arrival, 0, sizeof args.arrival);
     const uint32_t K = ctx->cfg.num_initial_components;
     // The component count of an existing state is read from the state; size
     // for the widest case unless the mixtures are initialised here.
@@ -180,26 +185,68 @@ int pg_fit_regions_host(pg_ctx *ctx, const float *dirw_host, const uint32_t *off
             st = check_cuda(ctx, cudaEventCreateWithFlags(&ctx->h2d_events[i], cudaEventDisableTiming), "copy events");
         if (st) return st;
     }
+    if (!ctx->h2d_ready) {
+        int st = check_cuda(ctx, cudaMalloc(&ctx->h2d_ready, sizeof(uint32_t) * kMaxArrivalChunks), "arrival flags");
+        if (!st) st = check_cuda(ctx, cudaHostAlloc(&ctx->h2d_ones, sizeof(uint32_t) * kMaxArrivalChunks,
+                                                    cudaHostAllocDefault),
+                                 "arrival flag source");
+        if (st) return st;
+        for (uint32_t c = 0; c < kMaxArrivalChunks; ++c) ctx->h2d_ones[c] = 1u;
+    }
+    // The samples travel in chunks cut at region boundaries, the chunks holding
+    // the largest regions first (the fit starts with the largest), and the fit
+    // runs from the start: each region waits for its chunk's flag, which a
+    // 4-byte copy behind the chunk's copy sets.  Everything else the fit does
+    // overlaps the copy (page-locked host memory reaches about 210 GB/s, as
+    // fast as the SMs can read it themselves).
+    SampleArrival arr;
+    memset(&arr, 0, sizeof arr);
+    std::vector<uint32_t> prio;
+    {
+        const uint32_t C = std::min<uint32_t>(kMaxArrivalChunks, n_regions);
+        arr.start[0] = 0;
+        uint32_t c = 0, biggest = 0;
+        for (uint32_t r = 0; r < n_regions; ++r) {
+            biggest = std::max(biggest, offsets_host[r + 1] - offsets_host[r]);
+            const bool cut = (uint64_t)offsets_host[r + 1] * C >= (uint64_t)(c + 1) * total;
+            if ((cut && c + 1 < C) || r + 1 == n_regions) {
+                arr.start[++c] = offsets_host[r + 1];
+                prio.push_back(biggest);
+                biggest = 0;
+            }
+        }
+        arr.n_chunks = c;
+        arr.ready = ctx->h2d_ready;
+    }
+    std::vector<uint32_t> copy_order(arr.n_chunks);
+    for (uint32_t c = 0; c < arr.n_chunks; ++c) copy_order[c] = c;
+    std::stable_sort(copy_order.begin(), copy_order.end(), [&](uint32_t x, uint32_t y) { return prio[x] > prio[y]; });
     int st = check_cuda(ctx, cudaMemcpyAsync(ctx->h2d_offsets, offsets_host, sizeof(uint32_t) * (n_regions + 1),
                                              cudaMemcpyHostToDevice, s), "offsets upload");
+    if (!st) st = check_cuda(ctx, cudaMemsetAsync(ctx->h2d_ready, 0, sizeof(uint32_t) * kMaxArrivalChunks, s),
+                             "arrival flags reset");
     // the copy stream starts after everything queued on the caller's stream
     // (an earlier fit may still read the sample buffer)
     if (!st) st = check_cuda(ctx, cudaEventRecord(ctx->h2d_events[1], s), "copy fork");
     if (!st) st = check_cuda(ctx, cudaStreamWaitEvent(ctx->h2d_stream, ctx->h2d_events[1], 0), "copy fork");
-    if (st) return st;
-    // One copy, then one fit.  Fitting chunks of regions while later chunks
-    // copy was measured slower: every chunk's largest region adds its own
-    // tail, which costs more than the copy (about 200 GB/s from page-locked
-    // memory) that it hides.  Four concurrent copies of quarters of the
-    // samples were slower than one copy as well.
-    if (total) {
-        st = check_cuda(ctx, cudaMemcpyAsync(ctx->h2d_dirw, dirw_host, sizeof(float4) * total, cudaMemcpyHostToDevice,
-                                             ctx->h2d_stream), "samples upload");
-        if (!st) st = check_cuda(ctx, cudaEventRecord(ctx->h2d_events[0], ctx->h2d_stream), "copy event");
-        if (!st) st = check_cuda(ctx, cudaStreamWaitEvent(s, ctx->h2d_events[0], 0), "copy join");
-        if (st) return st;
+    for (uint32_t k = 0; !st && k < arr.n_chunks; ++k) {
+        const uint32_t c = copy_order[k];
+        const uint64_t n0 = arr.start[c], n1 = arr.start[c + 1];
+        if (n1 > n0)
+            st = check_cuda(ctx, cudaMemcpyAsync(ctx->h2d_dirw + n0, reinterpret_cast<const float4 *>(dirw_host) + n0,
+                                                 sizeof(float4) * (n1 - n0), cudaMemcpyHostToDevice, ctx->h2d_stream),
+                            "samples upload");
+        if (!st)
+            st = check_cuda(ctx, cudaMemcpyAsync(ctx->h2d_ready + c, ctx->h2d_ones + c, sizeof(uint32_t),
+                                                 cudaMemcpyHostToDevice, ctx->h2d_stream),
+                            "arrival flag");
     }
-    return fit_range(ctx, reinterpret_cast<const float *>(ctx->h2d_dirw), ctx->h2d_offsets, 0, n_regions, mode, s);
+    if (!st) st = check_cuda(ctx, cudaEventRecord(ctx->h2d_events[0], ctx->h2d_stream), "copy event");
+    if (st) return st;
+    st = fit_range(ctx, reinterpret_cast<const float *>(ctx->h2d_dirw), ctx->h2d_offsets, 0, n_regions, mode, s, &arr);
+    // work queued behind the fit also waits for every copy (a chunk no region waited on included)
+    if (!st) st = check_cuda(ctx, cudaStreamWaitEvent(s, ctx->h2d_events[0], 0), "copy join");
+    return st;
 }
 
 int pg_eval_loglik(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t n_regions, double *ll_out,

@@ -62,7 +62,31 @@ struct EmArgs {
     const uint32_t *n_large;     // number of regions fitted by a whole cluster
     uint32_t stages;             // ring stages for streamed slices (>= 1)
     uint32_t stage_n;            // samples per ring stage: a multiple of the E-step trip width
+    SampleArrival arrival;       // arrival.ready null: every sample is in place
 };
+
+// Waits (one thread, bounded: about 2 s) until the chunk of samples holding
+// offset b has arrived from the host; a wait that runs out reports
+// PG_DEV_ERR_TIMEOUT.  The flags are written by host-to-device copies behind
+// each chunk's copy on the copy stream, so the chunk's samples are in device
+// memory once its flag reads non-zero.
+__device__ __forceinline__ void wait_samples(const EmArgs &a, uint32_t b) {
+    const SampleArrival &ar = a.arrival;
+    uint32_t c = 0;
+    while (c + 1 < ar.n_chunks && ar.start[c + 1] <= b) ++c;
+    const long long t0 = clock64();
+    for (;;) {
+        uint32_t v;
+        asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(ar.ready + c) : "memory");
+        if (v != 0u) break;
+        if (clock64() - t0 > 4000000000LL) {
+            atomicOr(a.error_word, PG_DEV_ERR_TIMEOUT);
+            break;
+        }
+        __nanosleep(200);
+    }
+    __threadfence();
+}
 
 constexpr uint32_t kMaxStages = 8;
 
@@ -662,6 +686,11 @@ __device__ void process_region(const EmArgs &a, EmShared<KMAX, NT / 32> &S, floa
     const uint32_t b = a.offsets[r], e = a.offsets[r + 1];
     const uint32_t N = e > b ? e - b : 0u;
     pg_region_state *st = a.states + r;
+    if (a.arrival.ready) {
+        // samples copied from the host while the fit runs: wait for this region's chunk
+        if (tid == 0) wait_samples(a, b);
+        __syncthreads();
+    }
     // this CTA's slice [sb, se)
     const uint32_t chunk = (N + csize - 1) / csize;
     const uint32_t sb = min(e, b + crank * chunk);

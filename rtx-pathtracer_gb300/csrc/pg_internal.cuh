@@ -41,6 +41,8 @@ struct pg_ctx {
     uint32_t *h2d_offsets = nullptr;
     cudaStream_t h2d_stream = nullptr;
     cudaEvent_t h2d_events[2] = {nullptr, nullptr};  // copy done, caller's stream fork
+    uint32_t *h2d_ready = nullptr;                     // per chunk: its samples are in place (device)
+    uint32_t *h2d_ones = nullptr;                      // page-locked source of the ready flags
     pg_region_extra *d_extras = nullptr;  // split/merge statistics per region (pg_splitmerge.cu)
     cudaStream_t sm_aux = nullptr;        // split/merge: the clustered launch runs beside the per-CTA one
     cudaEvent_t sm_fork = nullptr, sm_join = nullptr;
@@ -53,10 +55,18 @@ namespace pg {
 int set_error(pg_ctx *ctx, int status, const std::string &msg);
 int check_cuda(pg_ctx *ctx, cudaError_t e, const char *what);
 int upload_init_table(pg_ctx *ctx, cudaStream_t s);
+// Samples of a fit still arriving from the host: chunk c, samples
+// [start[c], start[c + 1]) (region boundaries), is in place once ready[c] != 0.
+constexpr uint32_t kMaxArrivalChunks = 16;
+struct SampleArrival {
+    const uint32_t *ready;
+    uint32_t n_chunks;
+    uint32_t start[kMaxArrivalChunks + 1];
+};
+int fit_range(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t first, uint32_t n_regions, int mode,
+              cudaStream_t s, const SampleArrival *arrival = nullptr);
 // region ids into ctx->d_order, largest sample count first; *n_large_out
 // (device) = regions in size buckets at or above large_threshold
-int fit_range(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t first, uint32_t n_regions, int mode,
-              cudaStream_t s);
 int order_regions(pg_ctx *ctx, const uint32_t *offsets, uint32_t n_regions, uint32_t large_threshold,
                   uint32_t *n_large_out, cudaStream_t s);
 void guide_release(pg_ctx *ctx);

@@ -172,7 +172,7 @@ extern "C" int pg_fit_regions_noalloc(const pg_fit_config *cfg, pg_region_state 
     order_regions_kernel<128><<<1, 1024, 0, s>>>(offsets, n_regions, scr->order, large_threshold, scr->counters + 3,
                                                  states);
     if (cudaGetLastError() != cudaSuccess) return PG_ERR_CUDA;
-    EmArgs args;
+    EmArgs args{};
     args.states = states;
     args.dirw = reinterpret_cast<const float4 *>(dirw);
     args.offsets = offsets;
