@@ -202,18 +202,20 @@ int pg_fit_regions(pg_ctx *ctx, const float *dirw, const uint32_t *offsets,
 /* VMMFactory::fit / updateFit over regions whose samples are in HOST memory
  * (the reference fits the host copy of the records, src/PathGuiding.cpp:
  * 276-312): dirw_host holds float4 {direction, weight} per sample grouped by
- * region, offsets_host n_regions + 1 sample offsets.  The samples go to a
- * context-owned device buffer on a copy stream that starts behind the work
- * already queued on `stream`, in up to 16 chunks cut at region boundaries,
- * the chunks holding the largest regions first; the fit runs on `stream` from
- * the start and each region waits for its chunk (page-locked host memory
- * copies asynchronously; pageable memory works through staging).  A region
- * whose chunk has not arrived after about two seconds stops waiting and
- * pg_sync_status then reports PG_ERR_TIMEOUT.
- * Same results as pg_fit_regions on the same samples; the states stay on the
- * device (pg_get_region_states).  Both buffers must stay valid until the
- * stream reaches the fit; work queued on `stream` afterwards runs after
- * every copy. */
+ * region, offsets_host n_regions + 1 sample offsets.  Page-locked samples
+ * (cudaHostAlloc, cudaHostRegister, a pinned torch tensor) at a 16-byte aligned
+ * address are read by the fit itself: each region's samples are read from host
+ * memory when the fit reaches the region (largest regions first), so the
+ * transfer overlaps the fit; slices larger than the staging capacity are
+ * copied once to a context-owned device buffer.  Other host memory goes to
+ * that buffer on a copy stream that starts behind the work already queued on
+ * `stream`, in up to 16 chunks cut at region boundaries, the chunks holding
+ * the largest regions first, while the fit runs: each region waits for its
+ * chunk, and a region whose chunk has not arrived after about two seconds
+ * stops waiting and pg_sync_status then reports PG_ERR_TIMEOUT.  Same results
+ * as pg_fit_regions on the same samples; the states stay on the device
+ * (pg_get_region_states).  Both buffers must stay valid and unchanged until
+ * the stream has completed the fit. */
 int pg_fit_regions_host(pg_ctx *ctx, const float *dirw_host, const uint32_t *offsets_host, uint32_t n_regions,
                         int mode, void *stream);
 

@@ -90,7 +90,7 @@ namespace pg {
 // The fit of regions [first, first + n_regions): offsets points at region
 // first's entry, the states written are first's onwards.
 int fit_range(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t first, uint32_t n_regions, int mode,
-              cudaStream_t s, const SampleArrival *arrival) {
+              cudaStream_t s, const HostSamples *host) {
     ctx->last_launches = 0;
     if (n_regions == 0) return PG_OK;
     guide_mark_stale(ctx);
@@ -127,10 +127,10 @@ int fit_range(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t 
     args.ll_out = nullptr;
     args.smem_cap = cap;
     args.stages = t.stream_stages ? t.stream_stages : 2u;
-    if (arrival)
-        args.arrival = *arrival;
+    if (host)
+        args.host = *host;
     else
-        memset(&args.arrival, 0, sizeof args.arrival);
+        memset(&args.host, 0, sizeof args.host);
     const uint32_t K = ctx->cfg.num_initial_components;
     // The component count of an existing state is read from the state; size
     // for the widest case unless the mixtures are initialised here.
@@ -185,21 +185,38 @@ int pg_fit_regions_host(pg_ctx *ctx, const float *dirw_host, const uint32_t *off
             st = check_cuda(ctx, cudaEventCreateWithFlags(&ctx->h2d_events[i], cudaEventDisableTiming), "copy events");
         if (st) return st;
     }
+    int st = check_cuda(ctx, cudaMemcpyAsync(ctx->h2d_offsets, offsets_host, sizeof(uint32_t) * (n_regions + 1),
+                                             cudaMemcpyHostToDevice, s), "offsets upload");
+    if (st) return st;
+    // Page-locked samples are read by the fit itself: each CTA reads a region's
+    // slice from host memory when it reaches the region, so the transfer follows
+    // the fit's own order (largest regions first) and overlaps the rest of the
+    // fit; slices above the staging capacity are copied once to the device
+    // buffer, from which their iterations stream.
+    cudaPointerAttributes pa{};
+    const cudaError_t ae = cudaPointerGetAttributes(&pa, dirw_host);
+    if (ae != cudaSuccess) (void)cudaGetLastError();
+    if (ae == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer &&
+        reinterpret_cast<uintptr_t>(pa.devicePointer) % 16u == 0) {  // 16-byte sample loads
+        HostSamples hs;
+        memset(&hs, 0, sizeof hs);
+        hs.mapped = static_cast<const float4 *>(pa.devicePointer);
+        return fit_range(ctx, reinterpret_cast<const float *>(ctx->h2d_dirw), ctx->h2d_offsets, 0, n_regions, mode,
+                         s, &hs);
+    }
     if (!ctx->h2d_ready) {
-        int st = check_cuda(ctx, cudaMalloc(&ctx->h2d_ready, sizeof(uint32_t) * kMaxArrivalChunks), "arrival flags");
+        st = check_cuda(ctx, cudaMalloc(&ctx->h2d_ready, sizeof(uint32_t) * kMaxArrivalChunks), "arrival flags");
         if (!st) st = check_cuda(ctx, cudaHostAlloc(&ctx->h2d_ones, sizeof(uint32_t) * kMaxArrivalChunks,
                                                     cudaHostAllocDefault),
                                  "arrival flag source");
         if (st) return st;
         for (uint32_t c = 0; c < kMaxArrivalChunks; ++c) ctx->h2d_ones[c] = 1u;
     }
-    // The samples travel in chunks cut at region boundaries, the chunks holding
-    // the largest regions first (the fit starts with the largest), and the fit
-    // runs from the start: each region waits for its chunk's flag, which a
-    // 4-byte copy behind the chunk's copy sets.  Everything else the fit does
-    // overlaps the copy (page-locked host memory reaches about 210 GB/s, as
-    // fast as the SMs can read it themselves).
-    SampleArrival arr;
+    // Pageable samples travel in chunks cut at region boundaries, the chunks
+    // holding the largest regions first (the fit starts with the largest), and
+    // the fit runs from the start: each region waits for its chunk's flag, which
+    // a 4-byte copy behind the chunk's copy sets.
+    HostSamples arr;
     memset(&arr, 0, sizeof arr);
     std::vector<uint32_t> prio;
     {
@@ -221,10 +238,8 @@ int pg_fit_regions_host(pg_ctx *ctx, const float *dirw_host, const uint32_t *off
     std::vector<uint32_t> copy_order(arr.n_chunks);
     for (uint32_t c = 0; c < arr.n_chunks; ++c) copy_order[c] = c;
     std::stable_sort(copy_order.begin(), copy_order.end(), [&](uint32_t x, uint32_t y) { return prio[x] > prio[y]; });
-    int st = check_cuda(ctx, cudaMemcpyAsync(ctx->h2d_offsets, offsets_host, sizeof(uint32_t) * (n_regions + 1),
-                                             cudaMemcpyHostToDevice, s), "offsets upload");
-    if (!st) st = check_cuda(ctx, cudaMemsetAsync(ctx->h2d_ready, 0, sizeof(uint32_t) * kMaxArrivalChunks, s),
-                             "arrival flags reset");
+    st = check_cuda(ctx, cudaMemsetAsync(ctx->h2d_ready, 0, sizeof(uint32_t) * kMaxArrivalChunks, s),
+                    "arrival flags reset");
     // the copy stream starts after everything queued on the caller's stream
     // (an earlier fit may still read the sample buffer)
     if (!st) st = check_cuda(ctx, cudaEventRecord(ctx->h2d_events[1], s), "copy fork");

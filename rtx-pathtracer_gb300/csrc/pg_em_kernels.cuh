@@ -62,7 +62,7 @@ struct EmArgs {
     const uint32_t *n_large;     // number of regions fitted by a whole cluster
     uint32_t stages;             // ring stages for streamed slices (>= 1)
     uint32_t stage_n;            // samples per ring stage: a multiple of the E-step trip width
-    SampleArrival arrival;       // arrival.ready null: every sample is in place
+    HostSamples host;            // all null: every sample is in place in dirw
 };
 
 // Waits (one thread, bounded: about 2 s) until the chunk of samples holding
@@ -71,7 +71,7 @@ struct EmArgs {
 // each chunk's copy on the copy stream, so the chunk's samples are in device
 // memory once its flag reads non-zero.
 __device__ __forceinline__ void wait_samples(const EmArgs &a, uint32_t b) {
-    const SampleArrival &ar = a.arrival;
+    const HostSamples &ar = a.host;
     uint32_t c = 0;
     while (c + 1 < ar.n_chunks && ar.start[c + 1] <= b) ++c;
     const long long t0 = clock64();
@@ -86,6 +86,23 @@ __device__ __forceinline__ void wait_samples(const EmArgs &a, uint32_t b) {
         __nanosleep(200);
     }
     __threadfence();
+}
+
+// The CTA's threads copy samples [0, n) from src (page-locked host memory the
+// device addresses) to dst (shared or device memory), eight 16-byte loads in
+// flight per thread.
+__device__ __forceinline__ void pull_samples(const float4 *__restrict__ src, float4 *__restrict__ dst, uint32_t n,
+                                             uint32_t tid, uint32_t nt) {
+    constexpr uint32_t D = 8;
+    uint32_t i = tid;
+    for (; i + (D - 1) * nt < n; i += D * nt) {
+        float4 v[D];
+#pragma unroll
+        for (uint32_t k = 0; k < D; ++k) v[k] = __ldcs(src + i + k * nt);
+#pragma unroll
+        for (uint32_t k = 0; k < D; ++k) dst[i + k * nt] = v[k];
+    }
+    for (; i < n; i += nt) dst[i] = __ldcs(src + i);
 }
 
 constexpr uint32_t kMaxStages = 8;
@@ -686,7 +703,7 @@ __device__ void process_region(const EmArgs &a, EmShared<KMAX, NT / 32> &S, floa
     const uint32_t b = a.offsets[r], e = a.offsets[r + 1];
     const uint32_t N = e > b ? e - b : 0u;
     pg_region_state *st = a.states + r;
-    if (a.arrival.ready) {
+    if (a.host.ready) {
         // samples copied from the host while the fit runs: wait for this region's chunk
         if (tid == 0) wait_samples(a, b);
         __syncthreads();
@@ -706,7 +723,12 @@ __device__ void process_region(const EmArgs &a, EmShared<KMAX, NT / 32> &S, floa
     const uint32_t max_itr = S.max_itr;
     const bool resident = n_local <= a.smem_cap;
     bool ok = true;
-    if (resident && max_itr > 0 && n_local > 0) {
+    if (resident && max_itr > 0 && n_local > 0 && a.host.mapped) {
+        // samples in page-locked host memory: the CTA reads its slice itself
+        pull_samples(a.host.mapped + sb, s_samp, n_local, tid, NT);
+        fence_proxy_async_smem();  // later TMA writes to this shared memory come after these stores
+        __syncthreads();
+    } else if (resident && max_itr > 0 && n_local > 0) {
         if (tid == 0) {
             fence_proxy_async_smem();
             const uint32_t bytes = n_local * 16u;
@@ -738,6 +760,13 @@ __device__ void process_region(const EmArgs &a, EmShared<KMAX, NT / 32> &S, floa
     const uint32_t nch = ring ? (n_local + stage_n - 1) / stage_n : 1u;
     const unsigned long long uses = ring ? (unsigned long long)nch * max_itr : 0ull;
     uint32_t consumed = 0;  // ring uses completed
+    if (ring && a.host.mapped) {
+        // streamed slice from host memory: copy it once to its place in the
+        // device sample buffer, which the ring's TMA copies then read
+        pull_samples(a.host.mapped + sb, const_cast<float4 *>(a.dirw) + sb, n_local, tid, NT);
+        fence_proxy_async_global();
+        __syncthreads();
+    }
     if (ring && tid == 0) {
         fence_proxy_async_smem();
         const uint32_t first = (uint32_t)min(uses, (unsigned long long)stages);

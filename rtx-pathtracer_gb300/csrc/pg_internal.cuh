@@ -35,7 +35,8 @@ struct pg_ctx {
     float init_kappa = -1.0f;
     uint32_t last_launches = 0;
     void *guide = nullptr;           // sort / parallax / distance scratch (pg_guide.cu)
-    // pg_fit_regions_host: device copies of host samples, filled on a copy stream
+    // pg_fit_regions_host: device copies of host samples (streamed slices of page-locked
+    // samples, or every sample of pageable ones, filled on a copy stream)
     float4 *h2d_dirw = nullptr;
     uint64_t h2d_cap = 0;
     uint32_t *h2d_offsets = nullptr;
@@ -55,16 +56,21 @@ namespace pg {
 int set_error(pg_ctx *ctx, int status, const std::string &msg);
 int check_cuda(pg_ctx *ctx, cudaError_t e, const char *what);
 int upload_init_table(pg_ctx *ctx, cudaStream_t s);
-// Samples of a fit still arriving from the host: chunk c, samples
-// [start[c], start[c + 1]) (region boundaries), is in place once ready[c] != 0.
+// Samples of a fit that start in host memory.  mapped non-null: page-locked
+// host samples at this device address, read by each CTA as it reaches a region
+// (slices above the staging capacity are first copied to the same offsets of
+// the device sample buffer).  ready non-null: the samples are being copied to
+// the device buffer in chunks; chunk c, samples [start[c], start[c + 1]) (region
+// boundaries), is in place once ready[c] != 0.
 constexpr uint32_t kMaxArrivalChunks = 16;
-struct SampleArrival {
+struct HostSamples {
+    const float4 *mapped;
     const uint32_t *ready;
     uint32_t n_chunks;
     uint32_t start[kMaxArrivalChunks + 1];
 };
 int fit_range(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t first, uint32_t n_regions, int mode,
-              cudaStream_t s, const SampleArrival *arrival = nullptr);
+              cudaStream_t s, const HostSamples *host = nullptr);
 // region ids into ctx->d_order, largest sample count first; *n_large_out
 // (device) = regions in size buckets at or above large_threshold
 int order_regions(pg_ctx *ctx, const uint32_t *offsets, uint32_t n_regions, uint32_t large_threshold,
@@ -138,6 +144,9 @@ __device__ __forceinline__ void fence_mbar_init() {
 }
 __device__ __forceinline__ void fence_proxy_async_smem() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_global() {
+    asm volatile("fence.proxy.async.global;" ::: "memory");
 }
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)

@@ -222,15 +222,22 @@ def test_argument_errors(cuda, pkg, abi):
     ctx.close()
 
 
-@pytest.mark.parametrize("mode", ["init", "update"])
+@pytest.mark.parametrize("mode", ["init", "update", "forced16"])
 def test_fit_from_host_memory_equals_device_fit(mode, cuda, pkg, abi, workloads):
     """pg_fit_regions_host (the fit from host memory) gives the same states,
-    bit for bit, as pg_fit_regions on device copies of the samples."""
+    bit for bit, as pg_fit_regions on device copies of the samples: page-locked
+    samples read by the fit itself (resident slices, streamed slices above the
+    staging capacity, cluster slices; early stops in the converged modes),
+    a page-locked view that starts inside its allocation, and pageable samples
+    copied in chunks."""
     torch = cuda
     w = workloads.fit_batched(seed=12, n_regions=300, median=3000, sigma=1.0, lo=64, hi=40000)
     R = len(w["offsets"]) - 1
-    cfg = abi.default_fit_config(num_initial_components=8)
-    m = abi.PG_FIT_INIT if mode == "init" else abi.PG_FIT_UPDATE
+    if mode == "forced16":
+        cfg = abi.forced_iterations(20, num_initial_components=16)
+    else:
+        cfg = abi.default_fit_config(num_initial_components=8)
+    m = abi.PG_FIT_UPDATE if mode == "update" else abi.PG_FIT_INIT
     start = None
     if mode == "update":
         start, _ = run_fit(cuda, pkg, cfg, w["dirw"], w["offsets"])
@@ -255,3 +262,16 @@ def test_fit_from_host_memory_equals_device_fit(mode, cuda, pkg, abi, workloads)
     c_ctx.fit_host(np.ascontiguousarray(w["dirw"], dtype=np.float32), w["offsets"].astype(np.uint32), R, m)
     c_ctx.sync()
     assert a_ctx.states(R).tobytes() == c_ctx.states(R).tobytes()
+    # a page-locked view 16 bytes into its allocation, and one 4 bytes in (not
+    # aligned for 16-byte loads: copied instead)
+    for shift in (4, 1):
+        e_ctx = pkg.FitContext(cfg, max_regions=R)
+        if start is not None:
+            e_ctx.set_states(start)
+        flat = np.ascontiguousarray(w["dirw"], dtype=np.float32).reshape(-1)
+        big = torch.zeros(flat.size + 8, dtype=torch.float32).pin_memory()
+        big[shift:shift + flat.size] = torch.from_numpy(flat)
+        e_ctx.fit_host(big[shift:shift + flat.size], offs_h, R, m)
+        e_ctx.sync()
+        assert a_ctx.states(R).tobytes() == e_ctx.states(R).tobytes(), shift
+        e_ctx.close()
