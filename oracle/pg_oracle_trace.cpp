@@ -1,6 +1,7 @@
 // pg_oracle_trace.cpp - TEST INFRASTRUCTURE (see pg_oracle_trace.h).
 // Compiled with -ffp-contract=off: every FP32 operation of the traversal twin
-// rounds exactly where the device code's explicit _rn intrinsics round.
+// rounds exactly where the device code's explicit _rn intrinsics round (fmaf
+// where the device uses __fmaf_rn).
 #include "pg_oracle_trace.h"
 #include "pg_oracle.h"
 
@@ -62,12 +63,12 @@ bool tri_intersect(const RayPre &r, const float *v0, const float *v1, const floa
     const float B[3] = {v1[0] - r.org[0], v1[1] - r.org[1], v1[2] - r.org[2]};
     const float C[3] = {v2[0] - r.org[0], v2[1] - r.org[1], v2[2] - r.org[2]};
     const float Akz = A[r.kz], Bkz = B[r.kz], Ckz = C[r.kz];
-    const float Ax = A[r.kx] - r.Sx * Akz;
-    const float Ay = A[r.ky] - r.Sy * Akz;
-    const float Bx = B[r.kx] - r.Sx * Bkz;
-    const float By = B[r.ky] - r.Sy * Bkz;
-    const float Cx = C[r.kx] - r.Sx * Ckz;
-    const float Cy = C[r.ky] - r.Sy * Ckz;
+    const float Ax = fmaf(-r.Sx, Akz, A[r.kx]);  // fused where the device fuses
+    const float Ay = fmaf(-r.Sy, Akz, A[r.ky]);
+    const float Bx = fmaf(-r.Sx, Bkz, B[r.kx]);
+    const float By = fmaf(-r.Sy, Bkz, B[r.ky]);
+    const float Cx = fmaf(-r.Sx, Ckz, C[r.kx]);
+    const float Cy = fmaf(-r.Sy, Ckz, C[r.ky]);
     float U = Cx * By - Cy * Bx;
     float V = Ax * Cy - Ay * Cx;
     float W = Bx * Ay - By * Ax;
@@ -80,7 +81,7 @@ bool tri_intersect(const RayPre &r, const float *v0, const float *v1, const floa
     const float det = (U + V) + W;
     if (det == 0.0f) return false;
     const float Az = r.Sz * Akz, Bz = r.Sz * Bkz, Cz = r.Sz * Ckz;
-    const float T = ((U * Az) + (V * Bz)) + (W * Cz);
+    const float T = fmaf(W, Cz, fmaf(V, Bz, U * Az));
     const float t = T / det;
     if (!(t > tmin && t < tmax)) return false;
     t_out = t;

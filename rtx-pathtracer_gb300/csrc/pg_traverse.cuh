@@ -2,11 +2,15 @@
 //
 // Closest hit and any hit over the four-wide BVH of host/pg_scene.cpp.  The
 // triangle test is the watertight algorithm of Woop, Benthin and Wald (JCGT
-// 2013).  Every product, sum and quotient of the triangle and box tests is an
-// explicit round-to-nearest operation (__fmul_rn, __fadd_rn, __fdiv_rn, ...),
-// so no FMA contraction happens and a CPU restatement with the same operation
-// order reproduces the hit (triangle id and t) bit for bit.  Ties in t go to
-// the lower triangle id.
+// 2013).  Every operation of the triangle and box tests is an explicit
+// round-to-nearest one (__fmul_rn, __fadd_rn, __fmaf_rn, __fdiv_rn, ...), so the
+// compiler contracts nothing and a CPU restatement with the same operations in
+// the same order (fmaf where these use __fmaf_rn) reproduces the hit (triangle
+// id and t) bit for bit.  The per-vertex shear and the numerator of t are fused
+// multiply-adds; the edge functions are not, so an edge shared by two triangles
+// gives exactly negated values in both (watertightness), nor is the slab test,
+// whose widening bounds the error of a subtraction and a product.  Ties in t go
+// to the lower triangle id.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -140,12 +144,12 @@ __device__ __forceinline__ bool tri_intersect(const RayPre &r, const float4 &v0,
     const float B[3] = {__fsub_rn(v1.x, r.org[0]), __fsub_rn(v1.y, r.org[1]), __fsub_rn(v1.z, r.org[2])};
     const float C[3] = {__fsub_rn(v2.x, r.org[0]), __fsub_rn(v2.y, r.org[1]), __fsub_rn(v2.z, r.org[2])};
     const float Akz = A[r.kz], Bkz = B[r.kz], Ckz = C[r.kz];
-    const float Ax = __fsub_rn(A[r.kx], __fmul_rn(r.Sx, Akz));
-    const float Ay = __fsub_rn(A[r.ky], __fmul_rn(r.Sy, Akz));
-    const float Bx = __fsub_rn(B[r.kx], __fmul_rn(r.Sx, Bkz));
-    const float By = __fsub_rn(B[r.ky], __fmul_rn(r.Sy, Bkz));
-    const float Cx = __fsub_rn(C[r.kx], __fmul_rn(r.Sx, Ckz));
-    const float Cy = __fsub_rn(C[r.ky], __fmul_rn(r.Sy, Ckz));
+    const float Ax = __fmaf_rn(-r.Sx, Akz, A[r.kx]);
+    const float Ay = __fmaf_rn(-r.Sy, Akz, A[r.ky]);
+    const float Bx = __fmaf_rn(-r.Sx, Bkz, B[r.kx]);
+    const float By = __fmaf_rn(-r.Sy, Bkz, B[r.ky]);
+    const float Cx = __fmaf_rn(-r.Sx, Ckz, C[r.kx]);
+    const float Cy = __fmaf_rn(-r.Sy, Ckz, C[r.ky]);
     float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
     float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
     float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
@@ -161,7 +165,7 @@ __device__ __forceinline__ bool tri_intersect(const RayPre &r, const float4 &v0,
     const float Az = __fmul_rn(r.Sz, Akz);
     const float Bz = __fmul_rn(r.Sz, Bkz);
     const float Cz = __fmul_rn(r.Sz, Ckz);
-    const float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
+    const float T = __fmaf_rn(W, Cz, __fmaf_rn(V, Bz, __fmul_rn(U, Az)));
     const float t = __fdiv_rn(T, det);
     if (!(t > tmin && t < tmax)) return false;
     t_out = t;
