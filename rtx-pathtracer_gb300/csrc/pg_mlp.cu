@@ -639,8 +639,8 @@ constexpr int IW1 = 0, IW2 = IW1 + NH * K1, IW3 = IW2 + NH * KH, IW4 = IW3 + NH 
 // shared memory (bytes)
 constexpr int SM_W = 0, SM_X1 = SM_W + NIMG * 2, SM_X2 = SM_X1 + TILE * K1 * 2, SM_X3 = SM_X2 + TILE * KH * 2,
               SM_X4 = SM_X3 + TILE * KH * 2, SM_DY = SM_X4 + TILE * KH * 2, SM_SLACK = SM_DY + TILE * KH * 2,
-              SM_BIAS = SM_SLACK + 2048, SM_O = SM_BIAS + (3 * NH + NOUT) * 4, SM_XCH = SM_O + NOUT * TILE * 4,
-              SM_TOTAL = SM_XCH + 2 * 4 * TILE * 4;
+              SM_BIAS = SM_SLACK + 2048, SM_XCH = SM_BIAS + (3 * NH + NOUT) * 4,
+              SM_REC = SM_XCH + 2 * 4 * TILE * 4, SM_TOTAL = SM_REC + TILE * 40;
 // The weight GEMMs of layers 2-4 use M = 128 over 81 meaningful rows: rows 81..127
 // read past the end of X_l (at most 767 bytes) into the next buffer or the slack.
 static_assert(SM_X1 % 128 == 0 && SM_TOTAL <= 227 * 1024, "shared memory layout");
@@ -701,6 +701,17 @@ __device__ __forceinline__ void tld16(uint32_t taddr, float (&v)[16]) {
     for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 __device__ __forceinline__ void tld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+// 4 consecutive FP32 columns of this thread's tensor-memory lane (column a multiple of 4)
+__device__ __forceinline__ void tld4(uint32_t taddr, float *v) {
+    uint32_t r0, r1, r2, r3;
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(taddr));
+    v[0] = __uint_as_float(r0);
+    v[1] = __uint_as_float(r1);
+    v[2] = __uint_as_float(r2);
+    v[3] = __uint_as_float(r3);
+}
 
 struct TrainArgs {
     const pg_directional_data *rec;
@@ -737,7 +748,7 @@ __device__ __forceinline__ void operands_ready() {
 __device__ __forceinline__ uint32_t enc_pair_fast(const float x[3], int c) {
     if (c < 96) {
         const int i = c >> 1, d = i % 3, k = i / 3;
-        const float y = ldexpf(x[d], k);
+        const float y = ldexpf(d == 0 ? x[0] : (d == 1 ? x[1] : x[2]), k);  // selects: x stays in registers
         const float r = y - 2.0f * rintf(0.5f * y);
         float sn, cs;
         __sincosf(kPi * r, &sn, &cs);
@@ -801,12 +812,27 @@ __device__ __forceinline__ void backward_epilogue(uint32_t tacc, int c0, uint32_
     }
 }
 
+// Queues asynchronous 4-byte copies of tile `tile`'s inputs (its records, or
+// its positions for inference) into shared memory: the copies of the next tile
+// run while this one computes.  tile < number of tiles.
+template <bool kInfer>
+__device__ __forceinline__ void prefetch_tile(const TrainArgs &A, uint32_t tile, uint32_t *dst, int tid, int nt) {
+    const uint32_t first = tile * TILE;
+    const uint32_t nrec = min((uint32_t)TILE, A.n - first);
+    const uint32_t words = nrec * (kInfer ? 3u : 10u);
+    const uint32_t *src = kInfer ? reinterpret_cast<const uint32_t *>(A.pos + 3 * (size_t)first)
+                                 : reinterpret_cast<const uint32_t *>(A.rec + first);
+    for (uint32_t i = (uint32_t)tid; i < words; i += (uint32_t)nt)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst + i)), "l"(src + i) : "memory");
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
 // TPR threads per record: warps w, w + 4, ... share tensor-memory lanes
 // 32 (w % 4) .. + 31, i.e. the same 32 records; share h = warp / 4 takes 64 / TPR
 // of a layer's columns, 16 / TPR of the mixture components and every TPR-th
-// encoding chunk.  The output layer goes through shared memory (sO, one
-// column-major row of 80 floats per record) so the component split does not
-// follow the tensor-memory column blocks.
+// encoding chunk.  The output layer's columns 5 j .. 5 j + 4 hold component
+// j (logit, mean, log kappa): share h reads its components' 5 NC / TPR columns
+// straight from tensor memory and writes their gradient into dY.
 // kInfer: the forward pass only, writing each position's mixture parameters
 // {pi, mu, kappa} per component (pg_mlp_infer).
 template <int TPR, bool kInfer = false>
@@ -824,9 +850,10 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
     __nv_bfloat16 *sX4 = reinterpret_cast<__nv_bfloat16 *>(sm + SM_X4);
     __nv_bfloat16 *sDY = reinterpret_cast<__nv_bfloat16 *>(sm + SM_DY);
     float *sB = reinterpret_cast<float *>(sm + SM_BIAS);
-    float *sO = reinterpret_cast<float *>(sm + SM_O);      // [NOUT][TILE]
     float *sXm = reinterpret_cast<float *>(sm + SM_XCH);   // [TPR][TILE] partial maxima
     float *sXs = sXm + TPR * TILE;                          // [TPR][TILE] partial sums
+    uint32_t *sRec = reinterpret_cast<uint32_t *>(sm + SM_REC);  // the tile's records (10 words each)
+    static_assert(sizeof(pg_directional_data) == 40, "record words");
     {
         const uint4 *src = reinterpret_cast<const uint4 *>(A.wimg);
         uint4 *dst = reinterpret_cast<uint4 *>(sm + SM_W);
@@ -872,19 +899,24 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
     bool first = true;
     const uint32_t tiles = (A.n + TILE - 1) / TILE;
     const int hc0 = h * HC;  // this share's hidden columns
+    if (blockIdx.x < tiles) prefetch_tile<kInfer>(A, blockIdx.x, sRec, tid, NT);
     for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const uint32_t r = tile * TILE + (uint32_t)rec;
         float x[3] = {0.0f, 0.0f, 0.0f}, d[3] = {0.0f, 0.0f, 1.0f}, w = 0.0f;
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        __syncthreads();  // the tile's inputs are in shared memory
         if (r < A.n) {
             if constexpr (kInfer) {
-                for (int k = 0; k < 3; ++k) x[k] = (A.pos[3 * (size_t)r + k] - A.lo[k]) * A.inv_ext[k];
+                const float *p = reinterpret_cast<const float *>(sRec) + 3 * rec;
+                for (int k = 0; k < 3; ++k) x[k] = (p[k] - A.lo[k]) * A.inv_ext[k];
             } else {
-                const pg_directional_data &rc = A.rec[r];
+                const float *rc = reinterpret_cast<const float *>(sRec) + 10 * rec;
                 for (int k = 0; k < 3; ++k) {
-                    x[k] = (rc.position[k] - A.lo[k]) * A.inv_ext[k];
-                    d[k] = rc.direction[k];
+                    x[k] = (rc[k] - A.lo[k]) * A.inv_ext[k];  // position
+                    d[k] = rc[3 + k];                          // direction
                 }
-                w = rc.flags == PG_INVALID_REGION ? 0.0f : rc.weight;
+                const uint32_t flags = sRec[10 * rec + 9];
+                w = flags == PG_INVALID_REGION ? 0.0f : rc[6];  // weight
                 if (!(w > 0.0f) || !isfinite(w)) w = 0.0f;
             }
         }
@@ -901,7 +933,8 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
         }
         uint32_t m1, m2, m3;
         // ---- forward
-        operands_ready();
+        operands_ready();  // also: every thread has read its record
+        if (tile + gridDim.x < tiles) prefetch_tile<kInfer>(A, tile + gridDim.x, sRec, tid, NT);
         if (tid == 0) {
             fence_after();
             gemm(tm + TM_ACT, fX1, fW1, K1 / 16, idesc(128, NH, 0, 0), false);
@@ -932,25 +965,25 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
             commit(&s_bar);
         }
         mma_wait(&s_bar, phase, A.err);
-        // ---- mixture, loss and output gradient: outputs + bias -> sO (column blocks h, h + TPR, ...)
-        for (int q = h; q < NOUT / 16; q += TPR) {
-            float v[16];
-            tld16(tl + TM_ACT + 16 * q, v);
-            tld_wait();
-#pragma unroll
-            for (int j = 0; j < 16; ++j) sO[(16 * q + j) * TILE + rec] = v[j] + sB[3 * NH + 16 * q + j];
-        }
-        __syncthreads();
+        // ---- mixture, loss and output gradient, from tensor memory (outputs + bias)
+        static_assert((5 * NCMP) % 4 == 0 && (5 * NCMP) % 2 == 0, "share columns");
         const int j0 = h * NCMP;  // this share's components
+        const int oc0 = 5 * j0;   // and their first output column
+        float o[5 * NCMP];
+#pragma unroll
+        for (int q = 0; q < 5 * NCMP / 4; ++q) tld4(tl + TM_ACT + oc0 + 4 * q, &o[4 * q]);
+        tld_wait();
+#pragma unroll
+        for (int c = 0; c < 5 * NCMP; ++c) o[c] += sB[3 * NH + oc0 + c];
         // Fast exponentials and logarithms (relative error ~1e-6): the loss and
         // gradient are sums over many records of terms that are rounded to
         // BF16 on the way back.
         float ml = -INFINITY;
 #pragma unroll
-        for (int q = 0; q < NCMP; ++q) ml = fmaxf(ml, sO[(5 * (j0 + q)) * TILE + rec]);
+        for (int q = 0; q < NCMP; ++q) ml = fmaxf(ml, o[5 * q]);
         float sl = 0.0f;
 #pragma unroll
-        for (int q = 0; q < NCMP; ++q) sl += __expf(sO[(5 * (j0 + q)) * TILE + rec] - ml);
+        for (int q = 0; q < NCMP; ++q) sl += __expf(o[5 * q] - ml);
         sXm[h * TILE + rec] = ml;
         sXs[h * TILE + rec] = sl;
         __syncthreads();
@@ -967,34 +1000,34 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
 #pragma unroll
                 for (int q = 0; q < NCMP; ++q) {
                     const int j = j0 + q;
-                    const float *o = sO + (5 * j) * TILE + rec;
-                    const float mx = o[TILE], my = o[2 * TILE], mz = o[3 * TILE];
+                    const float mx = o[5 * q + 1], my = o[5 * q + 2], mz = o[5 * q + 3];
                     const float mn = sqrtf(mx * mx + my * my + mz * mz);
                     const float inv = mn > 0.0f ? 1.0f / mn : 0.0f;
-                    mo[5 * j] = __expf(o[0] - lse);
+                    mo[5 * j] = __expf(o[5 * q] - lse);
                     mo[5 * j + 1] = mx * inv;
                     mo[5 * j + 2] = my * inv;
                     mo[5 * j + 3] = mz * inv;
-                    mo[5 * j + 4] = __expf(fminf(fmaxf(o[4 * TILE], S_MIN), S_MAX));
+                    mo[5 * j + 4] = __expf(fminf(fmaxf(o[5 * q + 4], S_MIN), S_MAX));
                 }
             }
         } else {
-            float lp[NCMP], kq[NCMP], csq[NCMP], mu[NCMP][3], fin[NCMP];
+            float lp[NCMP], kq[NCMP], csq[NCMP], mu[NCMP][3], fin[NCMP], pq[NCMP];
+            uint32_t inside = 0u;  // bit q: log kappa strictly inside its clamp
     #pragma unroll
             for (int q = 0; q < NCMP; ++q) {
-                const int j = j0 + q;
-                const float mx = sO[(5 * j + 1) * TILE + rec], my = sO[(5 * j + 2) * TILE + rec],
-                            mz = sO[(5 * j + 3) * TILE + rec];
+                const float mx = o[5 * q + 1], my = o[5 * q + 2], mz = o[5 * q + 3];
+                pq[q] = __expf(o[5 * q] - lse);
+                inside |= (o[5 * q + 4] > S_MIN && o[5 * q + 4] < S_MAX) ? 1u << q : 0u;
                 const float mn = sqrtf(mx * mx + my * my + mz * mz);
                 const float inv = mn > 0.0f ? 1.0f / mn : 0.0f;
-                const float k = __expf(fminf(fmaxf(sO[(5 * j + 4) * TILE + rec], S_MIN), S_MAX));
+                const float k = __expf(fminf(fmaxf(o[5 * q + 4], S_MIN), S_MAX));
                 mu[q][0] = mx * inv;
                 mu[q][1] = my * inv;
                 mu[q][2] = mz * inv;
                 const float cs = mu[q][0] * d[0] + mu[q][1] * d[1] + mu[q][2] * d[2];
                 const float om = -expm1f(-2.0f * k);  // 1 - e^{-2k}
                 const float lognorm = __logf(k) - __logf(2.0f * kPi) - __logf(om);
-                lp[q] = (sO[(5 * j) * TILE + rec] - lse) + lognorm + k * (cs - 1.0f);
+                lp[q] = (o[5 * q] - lse) + lognorm + k * (cs - 1.0f);
                 kq[q] = k;
                 csq[q] = cs;
                 fin[q] = inv * k;  // kappa / |m|
@@ -1020,31 +1053,25 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
                 lsum += w * -logq;
                 wsum += w;
             }
+            // the gradient of this share's outputs, BF16 pairs into dY
+            float gq[5 * NCMP];
     #pragma unroll
             for (int q = 0; q < NCMP; ++q) {
-                const int j = j0 + q;
-                float *o = sO + (5 * j) * TILE + rec;
-                const float sraw = o[4 * TILE];
                 const float k = kq[q], cs = csq[q];
                 const float rr = __expf(lp[q] - logq);  // responsibility
-                const float pi = __expf(o[0] - lse);
+                const float pi = pq[q];
                 const float f = -w * rr * fin[q];
-                o[0] = w * (pi - rr);
-                o[TILE] = f * (d[0] - cs * mu[q][0]);
-                o[2 * TILE] = f * (d[1] - cs * mu[q][1]);
-                o[3 * TILE] = f * (d[2] - cs * mu[q][2]);
-                const bool inside = sraw > S_MIN && sraw < S_MAX;
+                gq[5 * q] = w * (pi - rr);
+                gq[5 * q + 1] = f * (d[0] - cs * mu[q][0]);
+                gq[5 * q + 2] = f * (d[1] - cs * mu[q][1]);
+                gq[5 * q + 3] = f * (d[2] - cs * mu[q][2]);
                 const float e = __expf(-2.0f * k);
                 const float tt = 2.0f * k * e / -expm1f(-2.0f * k);
-                o[4 * TILE] = inside ? -w * rr * (1.0f - tt + k * (cs - 1.0f)) : 0.0f;
+                gq[5 * q + 4] = ((inside >> q) & 1u) ? -w * rr * (1.0f - tt + k * (cs - 1.0f)) : 0.0f;
             }
-            __syncthreads();
-            for (int ch = h; ch < NOUT / 8; ch += TPR) {
-                const float *o = sO + (8 * ch) * TILE + rec;
-                *reinterpret_cast<uint4 *>(sDY + elem(rec, 8 * ch, KCH)) =
-                    make_uint4(pack2(o[0], o[TILE]), pack2(o[2 * TILE], o[3 * TILE]), pack2(o[4 * TILE], o[5 * TILE]),
-                               pack2(o[6 * TILE], o[7 * TILE]));
-            }
+    #pragma unroll
+            for (int c = 0; c < 5 * NCMP; c += 2)
+                *reinterpret_cast<uint32_t *>(sDY + elem(rec, oc0 + c, KCH)) = pack2(gq[c], gq[c + 1]);
             // ---- backward: weight gradients of layer l and dH_{l-1} from one commit
             operands_ready();
             if (tid == 0) {
