@@ -640,10 +640,11 @@ constexpr int IW1 = 0, IW2 = IW1 + NH * K1, IW3 = IW2 + NH * KH, IW4 = IW3 + NH 
 constexpr int SM_W = 0, SM_X1 = SM_W + NIMG * 2, SM_X2 = SM_X1 + TILE * K1 * 2, SM_X3 = SM_X2 + TILE * KH * 2,
               SM_X4 = SM_X3 + TILE * KH * 2, SM_DY = SM_X4 + TILE * KH * 2, SM_SLACK = SM_DY + TILE * KH * 2,
               SM_BIAS = SM_SLACK + 2048, SM_XCH = SM_BIAS + (3 * NH + NOUT) * 4,
-              SM_REC = SM_XCH + 2 * 4 * TILE * 4, SM_TOTAL = SM_REC + TILE * 40;
+              SM_REC = SM_XCH + 2 * 4 * TILE * 4, SM_X1B = (SM_REC + TILE * 40 + 127) / 128 * 128,
+              SM_TOTAL = SM_X1B + TILE * K1 * 2;
 // The weight GEMMs of layers 2-4 use M = 128 over 81 meaningful rows: rows 81..127
 // read past the end of X_l (at most 767 bytes) into the next buffer or the slack.
-static_assert(SM_X1 % 128 == 0 && SM_TOTAL <= 227 * 1024, "shared memory layout");
+static_assert(SM_X1 % 128 == 0 && SM_X1B % 128 == 0 && SM_TOTAL <= 227 * 1024, "shared memory layout");
 // tensor-memory columns: layer accumulator, then the four weight-gradient blocks
 constexpr uint32_t TM_ACT = 0, TM_G1 = 128, TM_G2 = 192, TM_G3 = 256, TM_G4 = 320, TM_COLS = 512;
 constexpr int kTpr = 4;  // threads per record
@@ -844,7 +845,9 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
     __shared__ float s_red[2 * NT / 32];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int rec = tid & (TILE - 1), h = tid / TILE;  // record within the tile, share
-    __nv_bfloat16 *sX1 = reinterpret_cast<__nv_bfloat16 *>(sm + SM_X1);
+    // two X1 buffers: a tile's encoding is written while the tile before it runs its backward GEMMs
+    __nv_bfloat16 *const sX1a = reinterpret_cast<__nv_bfloat16 *>(sm + SM_X1);
+    __nv_bfloat16 *const sX1b = reinterpret_cast<__nv_bfloat16 *>(sm + SM_X1B);
     __nv_bfloat16 *sX2 = reinterpret_cast<__nv_bfloat16 *>(sm + SM_X2);
     __nv_bfloat16 *sX3 = reinterpret_cast<__nv_bfloat16 *>(sm + SM_X3);
     __nv_bfloat16 *sX4 = reinterpret_cast<__nv_bfloat16 *>(sm + SM_X4);
@@ -880,18 +883,19 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
     fence_after();
     const uint32_t tm = s_tmem;
     const uint32_t tl = tm + ((uint32_t)((warp & 3) * 32) << 16);  // this warp's lanes
-    const uint32_t aW = smem_u32(sm + SM_W), aX1 = smem_u32(sX1), aX2 = smem_u32(sX2), aX3 = smem_u32(sX3),
+    const uint32_t aW = smem_u32(sm + SM_W), aX1 = smem_u32(sX1a), aX1b = smem_u32(sX1b),
+                   aX2 = smem_u32(sX2), aX3 = smem_u32(sX3),
                    aX4 = smem_u32(sX4), aDY = smem_u32(sDY);
     // operand walks (bytes): K-major tiles advance 2 chunks (256 B) per K-step of 16,
     // MN-major ones 2 row groups
-    const Opnd fX1{aX1, 128, KC1 * 128, 256}, fX2{aX2, 128, KCH * 128, 256}, fX3{aX3, 128, KCH * 128, 256},
+    const Opnd fX2{aX2, 128, KCH * 128, 256}, fX3{aX3, 128, KCH * 128, 256},
         fX4{aX4, 128, KCH * 128, 256};
     const Opnd fW1{aW + IW1 * 2, 128, KC1 * 128, 256}, fW2{aW + IW2 * 2, 128, KCH * 128, 256},
         fW3{aW + IW3 * 2, 128, KCH * 128, 256}, fW4{aW + IW4 * 2, 128, KCH * 128, 256};
     const Opnd bDY{aDY, 128, KCH * 128, 256};
     const Opnd bW2{aW + IW2 * 2, KCH * 128, 128, 2 * KCH * 128}, bW3{aW + IW3 * 2, KCH * 128, 128, 2 * KCH * 128},
         bW4{aW + IW4 * 2, KCH * 128, 128, 2 * KCH * 128};
-    const Opnd gX1{aX1, KC1 * 128, 128, 2 * KC1 * 128}, gX2{aX2, KCH * 128, 128, 2 * KCH * 128},
+    const Opnd gX2{aX2, KCH * 128, 128, 2 * KCH * 128},
         gX3{aX3, KCH * 128, 128, 2 * KCH * 128}, gX4{aX4, KCH * 128, 128, 2 * KCH * 128};
     const Opnd gDY{aDY, KCH * 128, 128, 2 * KCH * 128};
     uint32_t phase = 0;
@@ -899,6 +903,20 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
     bool first = true;
     const uint32_t tiles = (A.n + TILE - 1) / TILE;
     const int hc0 = h * HC;  // this share's hidden columns
+    // encoding chunk ch of a record at x into the X1 tile dst: 112 features, the
+    // ones column, zeros to 128 (this thread's chunks are h, h + TPR, ...)
+    auto encode_chunk = [&](const float *xx, int ch, __nv_bfloat16 *dst) {
+        const int c = 8 * ch;
+        uint4 v;
+        if (ch < 14)
+            v = make_uint4(enc_pair_fast(xx, c), enc_pair_fast(xx, c + 2), enc_pair_fast(xx, c + 4),
+                           enc_pair_fast(xx, c + 6));
+        else
+            v = make_uint4(ch == 14 ? pack2(1.0f, 0.0f) : 0u, 0u, 0u, 0u);
+        *reinterpret_cast<uint4 *>(dst + elem(rec, c, KC1)) = v;
+    };
+    int xb = 0;            // this tile's X1 buffer
+    bool encoded = false;  // this tile's X1 was written during the tile before
     if (blockIdx.x < tiles) prefetch_tile<kInfer>(A, blockIdx.x, sRec, tid, NT);
     for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const uint32_t r = tile * TILE + (uint32_t)rec;
@@ -920,24 +938,15 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
                 if (!(w > 0.0f) || !isfinite(w)) w = 0.0f;
             }
         }
-        // encoding -> X1: 112 features, the ones column, zeros to 128 (chunks h, h + TPR, ...)
-        for (int ch = h; ch < KC1; ch += TPR) {
-            const int c = 8 * ch;
-            uint4 v;
-            if (ch < 14)
-                v = make_uint4(enc_pair_fast(x, c), enc_pair_fast(x, c + 2), enc_pair_fast(x, c + 4),
-                               enc_pair_fast(x, c + 6));
-            else
-                v = make_uint4(ch == 14 ? pack2(1.0f, 0.0f) : 0u, 0u, 0u, 0u);
-            *reinterpret_cast<uint4 *>(sX1 + elem(rec, c, KC1)) = v;
-        }
+        if (!encoded)
+            for (int ch = h; ch < KC1; ch += TPR) encode_chunk(x, ch, xb ? sX1b : sX1a);
         uint32_t m1, m2, m3;
         // ---- forward
         operands_ready();  // also: every thread has read its record
         if (tile + gridDim.x < tiles) prefetch_tile<kInfer>(A, tile + gridDim.x, sRec, tid, NT);
         if (tid == 0) {
             fence_after();
-            gemm(tm + TM_ACT, fX1, fW1, K1 / 16, idesc(128, NH, 0, 0), false);
+            gemm(tm + TM_ACT, Opnd{xb ? aX1b : aX1, 128, KC1 * 128, 256}, fW1, K1 / 16, idesc(128, NH, 0, 0), false);
             commit(&s_bar);
         }
         mma_wait(&s_bar, phase, A.err);
@@ -1072,14 +1081,26 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
     #pragma unroll
             for (int c = 0; c < 5 * NCMP; c += 2)
                 *reinterpret_cast<uint32_t *>(sDY + elem(rec, oc0 + c, KCH)) = pack2(gq[c], gq[c + 1]);
-            // ---- backward: weight gradients of layer l and dH_{l-1} from one commit
+            // ---- backward: weight gradients of layer l and dH_{l-1} from one commit.
+            // While each commit runs, the threads encode a quarter of the next
+            // tile into the other X1 buffer (its records arrived during this tile).
+            const uint32_t ntile = tile + gridDim.x;
+            const bool has_next = ntile < tiles;
+            __nv_bfloat16 *xn1 = xb ? sX1a : sX1b;  // the other X1 buffer
+            asm volatile("cp.async.wait_group 0;" ::: "memory");  // the barrier below publishes them
             operands_ready();
+            float xn[3] = {0.0f, 0.0f, 0.0f};
+            if (has_next && ntile * TILE + (uint32_t)rec < A.n) {
+                const float *rc = reinterpret_cast<const float *>(sRec) + 10 * rec;
+                for (int k = 0; k < 3; ++k) xn[k] = (rc[k] - A.lo[k]) * A.inv_ext[k];
+            }
             if (tid == 0) {
                 fence_after();
                 gemm(tm + TM_G4, gX4, gDY, TILE / 16, idesc(128, NOUT, 1, 1), !first);
                 gemm(tm + TM_ACT, bDY, bW4, NOUT / 16, idesc(128, NH, 0, 1), false);
                 commit(&s_bar);
             }
+            if (has_next) encode_chunk(xn, h, xn1);
             mma_wait(&s_bar, phase, A.err);
             backward_epilogue<HC>(tl + TM_ACT, hc0, m3, sDY, rec);
             operands_ready();
@@ -1089,6 +1110,7 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
                 gemm(tm + TM_ACT, bDY, bW3, NH / 16, idesc(128, NH, 0, 1), false);
                 commit(&s_bar);
             }
+            if (has_next) encode_chunk(xn, h + TPR, xn1);
             mma_wait(&s_bar, phase, A.err);
             backward_epilogue<HC>(tl + TM_ACT, hc0, m2, sDY, rec);
             operands_ready();
@@ -1098,16 +1120,22 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
                 gemm(tm + TM_ACT, bDY, bW2, NH / 16, idesc(128, NH, 0, 1), false);
                 commit(&s_bar);
             }
+            if (has_next) encode_chunk(xn, h + 2 * TPR, xn1);
             mma_wait(&s_bar, phase, A.err);
             backward_epilogue<HC>(tl + TM_ACT, hc0, m1, sDY, rec);
             operands_ready();
             if (tid == 0) {
                 fence_after();
-                gemm(tm + TM_G1, gX1, gDY, TILE / 16, idesc(128, NH, 1, 1), !first);
+                gemm(tm + TM_G1, Opnd{xb ? aX1b : aX1, KC1 * 128, 128, 2 * KC1 * 128}, gDY, TILE / 16,
+                     idesc(128, NH, 1, 1), !first);
                 commit(&s_bar);
             }
+            if (has_next)
+                for (int ch = h + 3 * TPR; ch < KC1; ch += TPR) encode_chunk(xn, ch, xn1);
             mma_wait(&s_bar, phase, A.err);
             first = false;
+            encoded = has_next;
+            xb ^= 1;
         }
     }
     if constexpr (!kInfer) {
