@@ -540,6 +540,9 @@ constexpr int kAdamGroups = 8;
 __global__ void __launch_bounds__(32 * kAdamGroups) k_reduce_adam(AdamArgs A) {
     __shared__ float ps[kAdamGroups][32], pc[kAdamGroups][32];
     __shared__ double sl[32 * kAdamGroups], sw[32 * kAdamGroups];
+    // the next batch's training kernel may launch now; it waits for this grid
+    // before it reads the weights
+    asm volatile("griddepcontrol.launch_dependents;");
     const int lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
     const int p = blockIdx.x * 32 + lane;
     if (A.loss_partials) {
@@ -857,6 +860,12 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
     float *sXs = sXm + TPR * TILE;                          // [TPR][TILE] partial sums
     uint32_t *sRec = reinterpret_cast<uint32_t *>(sm + SM_REC);  // the tile's records (10 words each)
     static_assert(sizeof(pg_directional_data) == 40, "record words");
+    const uint32_t tiles = (A.n + TILE - 1) / TILE;
+    // The first tile's inputs; then, when launched behind the previous batch's
+    // update kernel (programmatic dependent launch), wait for its weights: the
+    // records are not written by that kernel.
+    if (blockIdx.x < tiles) prefetch_tile<kInfer>(A, blockIdx.x, sRec, tid, NT);
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     {
         const uint4 *src = reinterpret_cast<const uint4 *>(A.wimg);
         uint4 *dst = reinterpret_cast<uint4 *>(sm + SM_W);
@@ -901,7 +910,6 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
     uint32_t phase = 0;
     float lsum = 0.0f, wsum = 0.0f;
     bool first = true;
-    const uint32_t tiles = (A.n + TILE - 1) / TILE;
     const int hc0 = h * HC;  // this share's hidden columns
     // encoding chunk ch of a record at x into the X1 tile dst: 112 features, the
     // ones column, zeros to 128 (this thread's chunks are h, h + TPR, ...)
@@ -917,7 +925,6 @@ __global__ void __launch_bounds__(TILE * TPR, 1) k_train_tc(TrainArgs A) {
     };
     int xb = 0;            // this tile's X1 buffer
     bool encoded = false;  // this tile's X1 was written during the tile before
-    if (blockIdx.x < tiles) prefetch_tile<kInfer>(A, blockIdx.x, sRec, tid, NT);
     for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const uint32_t r = tile * TILE + (uint32_t)rec;
         float x[3] = {0.0f, 0.0f, 0.0f}, d[3] = {0.0f, 0.0f, 1.0f}, w = 0.0f;
@@ -1383,7 +1390,7 @@ FwdArgs fwd_args(const pg_mlp *M) {
 // forward + backward + weight gradients of one batch; leaves the partials and
 // the batch's scalars in scalars[2 * slot]
 int batch_gradients(pg_mlp *M, const pg_directional_data *rec, uint32_t n, uint32_t slot, cudaStream_t s,
-                    bool scalars_now = true) {
+                    bool scalars_now = true, bool after_update = false) {
     if (M->path == PG_MLP_PATH_TCGEN05) {
         const uint32_t tiles = (n + tc::TILE - 1) / tc::TILE;
         const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)M->sm_count);
@@ -1400,7 +1407,20 @@ int batch_gradients(pg_mlp *M, const pg_directional_data *rec, uint32_t n, uint3
         T.partials = M->wg_partials;
         T.loss_partials = M->fwd_partials;
         T.err = M->err;
-        tc::k_train_tc<tc::kTpr><<<grid, tc::TILE * tc::kTpr, tc::SM_TOTAL, s>>>(T);
+        // behind the previous batch's update kernel: a programmatic dependent
+        // launch (the prologue and the first records overlap that kernel)
+        cudaLaunchConfig_t lc = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        lc.gridDim = dim3(grid, 1, 1);
+        lc.blockDim = dim3(tc::TILE * tc::kTpr, 1, 1);
+        lc.dynamicSmemBytes = tc::SM_TOTAL;
+        lc.stream = s;
+        lc.attrs = at;
+        lc.numAttrs = after_update ? 1 : 0;
+        if (cudaLaunchKernelEx(&lc, tc::k_train_tc<tc::kTpr>, T) != cudaSuccess)
+            return mlp_error(PG_ERR_CUDA, "surrogate gradient launch");
         // the batch's scalars: now, or summed by the update that follows (one launch fewer)
         M->loss_pending = scalars_now ? 0u : grid;
         if (scalars_now) tc::k_tc_scalars<<<1, 256, 0, s>>>(M->fwd_partials, grid, M->scalars + 2 * slot);
@@ -1665,7 +1685,7 @@ int pg_mlp_train(pg_mlp *M, const pg_directional_data *records, uint64_t n, floa
     for (uint32_t b = 0; b < batches; ++b) {
         const uint64_t first = (uint64_t)b * B;
         const uint32_t cnt = (uint32_t)std::min<uint64_t>(B, n - first);
-        if (int st = batch_gradients(M, records + first, cnt, b, s, false)) return st;
+        if (int st = batch_gradients(M, records + first, cnt, b, s, false, b > 0)) return st;
         if (int st = reduce_step(M, b, nullptr, s)) return st;
     }
     if (loss_out) {
