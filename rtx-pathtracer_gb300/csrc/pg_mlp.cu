@@ -539,39 +539,75 @@ __device__ __forceinline__ int wb_index(int p) {
 constexpr int kAdamGroups = 8;
 __global__ void __launch_bounds__(32 * kAdamGroups) k_reduce_adam(AdamArgs A) {
     __shared__ float ps[kAdamGroups][32], pc[kAdamGroups][32];
-    __shared__ double sl[32 * kAdamGroups], sw[32 * kAdamGroups];
+    __shared__ double sl[1], sw[1];  // the batch's loss and weight sums
     // the next batch's training kernel may launch now; it waits for this grid
     // before it reads the weights
     asm volatile("griddepcontrol.launch_dependents;");
     const int lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
     const int p = blockIdx.x * 32 + lane;
-    if (A.loss_partials) {
-        // the batch's loss and weight sums, in k_tc_scalars' order (same block size)
-        double l = 0.0, w = 0.0;
-        for (uint32_t i = threadIdx.x; i < A.n_loss; i += blockDim.x) {
-            l += A.loss_partials[2 * i];
-            w += A.loss_partials[2 * i + 1];
+    if (A.loss_partials && grp == 0) {
+        // The batch's loss and weight sums in k_tc_scalars' order, by one warp:
+        // lane l holds that kernel's threads l + 32 k (k < 8), whose tree steps
+        // 128, 64 and 32 stay in the lane and steps 16 .. 1 are shuffles.
+        double l[8], w[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {  // the first element of each thread's sum (0 + x = x): loads in flight together
+            const uint32_t i = lane + 32u * k;
+            l[k] = i < A.n_loss ? (double)A.loss_partials[2 * i] : 0.0;
+            w[k] = i < A.n_loss ? (double)A.loss_partials[2 * i + 1] : 0.0;
         }
-        sl[threadIdx.x] = l;
-        sw[threadIdx.x] = w;
-        __syncthreads();
-        for (int st = blockDim.x / 2; st > 0; st >>= 1) {
-            if ((int)threadIdx.x < st) {
-                sl[threadIdx.x] += sl[threadIdx.x + st];
-                sw[threadIdx.x] += sw[threadIdx.x + st];
+        for (uint32_t i0 = 256u + lane; i0 < A.n_loss; i0 += 256u)  // more than 256 partials
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const uint32_t i = i0 + 32u * k;
+                if (i < A.n_loss) {
+                    l[k] += A.loss_partials[2 * i];
+                    w[k] += A.loss_partials[2 * i + 1];
+                }
             }
-            __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            l[k] += l[k + 4];
+            w[k] += w[k + 4];
         }
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            A.scalars[0] = sl[0];
-            A.scalars[1] = sw[0];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            l[k] += l[k + 2];
+            w[k] += w[k + 2];
+        }
+        l[0] += l[1];
+        w[0] += w[1];
+        for (int st = 16; st > 0; st >>= 1) {
+            const double lo = __shfl_down_sync(0xffffffffu, l[0], st), wo = __shfl_down_sync(0xffffffffu, w[0], st);
+            if (lane < st) {
+                l[0] += lo;
+                w[0] += wo;
+            }
+        }
+        if (lane == 0) {
+            sl[0] = l[0];
+            sw[0] = w[0];
+            if (blockIdx.x == 0) {
+                A.scalars[0] = l[0];
+                A.scalars[1] = w[0];
+            }
         }
     }
     {
+        // this warp's partials, eight loads in flight, added in block order
         float s = 0.0f, c = 0.0f;
         if (p < NPARAM)
-            for (uint32_t b = grp; b < A.n_blocks; b += kAdamGroups)
-                neumaier_add(s, c, A.partials[(size_t)b * NPARAM + p]);
+            for (uint32_t b0 = grp; b0 < A.n_blocks; b0 += 8u * kAdamGroups) {
+                float v[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const uint32_t b = b0 + (uint32_t)k * kAdamGroups;
+                    v[k] = b < A.n_blocks ? A.partials[(size_t)b * NPARAM + p] : 0.0f;
+                }
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if (b0 + (uint32_t)k * kAdamGroups < A.n_blocks) neumaier_add(s, c, v[k]);
+            }
         ps[grp][lane] = s;
         pc[grp][lane] = c;
     }

@@ -210,6 +210,24 @@ def test_training_reduces_loss(cuda, pkg, abi, workloads):
     net.close()
 
 
+def test_training_reports_its_batch_loss_bit_for_bit(cuda, pkg, abi, workloads):
+    """pg_mlp_train sums each batch's loss partials inside its update kernel (one
+    warp, in the pairing order of the separate kernel pg_mlp_loss_grad uses): for a
+    one-batch pass the loss it reports equals pg_mlp_loss_grad's on the same
+    weights exactly.  40000 records: 313 tiles over every SM's partial."""
+    torch = cuda
+    rng = np.random.default_rng(23)
+    n = 40000
+    rec = records(workloads, rng, n, kappa=20.0)
+    rec["flags"][0] = 0
+    net = pkg.Surrogate(BOX, batch=1 << 16)
+    d = dev(torch, rec)
+    la = net.loss_grad(d, n)
+    lb = net.train(d, n)
+    assert np.isfinite(la) and la == lb, (la, lb)
+    net.close()
+
+
 def collect(torch, pkg, abi, G, sc, pg, col, spp_list, seed0, guided_after_first=True):
     """Training passes with recording; returns the valid records of all passes
     (host, bucketed by region per pass)."""
