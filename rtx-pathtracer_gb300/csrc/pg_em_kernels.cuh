@@ -487,15 +487,35 @@ __device__ __forceinline__ void merge_totals(const EmShared<KMAX, NW> &S, float 
     }
 }
 
-// Warp 0 of the CTA that owns the region: M-step of iteration `it` from merged
-// statistics m (lane c < KMAX) and region totals (lane 0).
+// The log-likelihood of iteration `it` (FP64) and the relative log-likelihood
+// test (VMMFactory.h:201-212): one thread of a warp other than the M-step's, so
+// this FP64 chain runs beside the component updates.
+template <int KMAX, int NW>
+__device__ void mstep_loglik(const EmArgs &a, EmShared<KMAX, NW> &S, uint32_t it, float llh, float llc) {
+    const pg_fit_config &cfg = a.cfg;
+    S.ll = ((double)llh + (double)llc) * 0.6931471805599453;
+    uint32_t stop = 0;
+    if (it >= cfg.min_itr) {
+        if (it > cfg.min_itr) {
+            // (LL - last) * (1/|last|) < thr, evaluated without the division:
+            // (LL - last) < thr * |last| gives the same decision for every
+            // finite or infinite operand (|last| = 0 included).
+            if ((S.ll - S.last_ll) < (double)cfg.rel_ll_threshold * fabs(S.last_ll)) stop = 1;
+        }
+        if (!stop) S.last_ll = S.ll;
+    }
+    S.stop = stop;
+}
+
+// Warp 0 of the CTA that owns the region: the component updates of iteration
+// `it` from merged statistics m (lane c < KMAX) and the region's valid weight
+// (lane 0); the log-likelihood and the stopping test are mstep_loglik's.
 template <int KMAX, int NW>
 __device__ void mstep_apply(const EmArgs &a, EmShared<KMAX, NW> &S, int lane, uint32_t it, uint32_t N, Stats4 m,
-                            float llh, float llc, float swh, float swc) {
+                            float swh, float swc) {
     const pg_fit_config &cfg = a.cfg;
     const uint32_t K = S.K;
     if (lane == 0) {
-        S.ll = ((double)llh + (double)llc) * 0.6931471805599453;
         if (it == 0) {
             const float sum_w = swh + swc;
             if (a.mode == PG_FIT_UPDATE) {
@@ -586,20 +606,6 @@ __device__ void mstep_apply(const EmArgs &a, EmShared<KMAX, NW> &S, int lane, ui
         S.nrm[c] = nrm;
         S.em2k[c] = em2k;
         make_consts(S, c, K);
-    }
-    if (lane == 0) {
-        // relative log-likelihood test (VMMFactory.h:201-212), FP64
-        uint32_t stop = 0;
-        if (it >= cfg.min_itr) {
-            if (it > cfg.min_itr) {
-                // (LL - last) * (1/|last|) < thr, evaluated without the division:
-                // (LL - last) < thr * |last| gives the same decision for every
-                // finite or infinite operand (|last| = 0 included).
-                if ((S.ll - S.last_ll) < (double)cfg.rel_ll_threshold * fabs(S.last_ll)) stop = 1;
-            }
-            if (!stop) S.last_ll = S.ll;
-        }
-        S.stop = stop;
     }
 }
 
@@ -857,8 +863,12 @@ __device__ void process_region(const EmArgs &a, EmShared<KMAX, NT / 32> &S, floa
                 Stats4 m = stats_zero();
                 if (lane < KMAX) m = merge_warps(S, lane);
                 float llh = 0.f, llc = 0.f, swh = 0.f, swc = 0.f;
-                if (lane == 0) merge_totals(S, llh, llc, swh, swc);
-                mstep_apply(a, S, lane, it, N, m, llh, llc, swh, swc);
+                if (lane == 0 && it == 0) merge_totals(S, llh, llc, swh, swc);
+                mstep_apply(a, S, lane, it, N, m, swh, swc);
+            } else if (warp == 1 && lane == 0) {
+                float llh, llc, swh, swc;
+                merge_totals(S, llh, llc, swh, swc);
+                mstep_loglik(a, S, it, llh, llc);
             }
             __syncthreads();
         } else {
@@ -880,7 +890,7 @@ __device__ void process_region(const EmArgs &a, EmShared<KMAX, NT / 32> &S, floa
             cluster.sync();
             if (owner && warp == 0) {
                 Stats4 m = stats_zero();
-                float llh = 0.f, llc = 0.f, swh = 0.f, swc = 0.f;
+                float swh = 0.f, swc = 0.f;
                 for (uint32_t q = 0; q < csize; ++q) {
                     const EmShared<KMAX, NW> *P = cluster.map_shared_rank(&S, q);
                     if (lane < KMAX) {
@@ -889,12 +899,16 @@ __device__ void process_region(const EmArgs &a, EmShared<KMAX, NT / 32> &S, floa
                         neumaier_add2(m.szh, m.szc, P->part[4][lane], P->part[5][lane]);
                         neumaier_add2(m.wh, m.wc, P->part[6][lane], P->part[7][lane]);
                     }
-                    if (lane == 0) {
-                        neumaier_add2(llh, llc, P->ptot[0], P->ptot[1]);
-                        neumaier_add2(swh, swc, P->ptot[2], P->ptot[3]);
-                    }
+                    if (lane == 0 && it == 0) neumaier_add2(swh, swc, P->ptot[2], P->ptot[3]);
                 }
-                mstep_apply(a, S, lane, it, N, m, llh, llc, swh, swc);
+                mstep_apply(a, S, lane, it, N, m, swh, swc);
+            } else if (owner && warp == 1 && lane == 0) {
+                float llh = 0.f, llc = 0.f;
+                for (uint32_t q = 0; q < csize; ++q) {
+                    const EmShared<KMAX, NW> *P = cluster.map_shared_rank(&S, q);
+                    neumaier_add2(llh, llc, P->ptot[0], P->ptot[1]);
+                }
+                mstep_loglik(a, S, it, llh, llc);
             }
             cluster.sync();
             if (!owner && warp == 0) pull_consts(cluster, S, lane);
