@@ -298,16 +298,23 @@ constexpr int kDistThreads = 64;
 
 // item_offsets[r] = first work item of region r (empty regions have none);
 // item_offsets[n_regions] = the item count.  One CTA.
+// item_region[i] = the region of work item i (items beyond cap_items are not
+// written; the partial kernel then reports the overflow).
 __global__ void __launch_bounds__(kScanThreads) distance_items_kernel(const uint32_t *offsets, uint32_t n_regions,
-                                                                      uint32_t *item_offsets) {
+                                                                      uint32_t *item_offsets, uint32_t *item_region,
+                                                                      uint64_t cap_items) {
     __shared__ uint32_t carry, tot;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
     for (uint32_t base = 0; base < n_regions; base += kScanThreads) {
         const uint32_t r = base + threadIdx.x;
         const uint32_t n = r < n_regions ? offsets[r + 1] - offsets[r] : 0u;
-        const uint32_t e = block_exclusive_scan((n + kDistChunk - 1) / kDistChunk, &tot);
-        if (r < n_regions) item_offsets[r] = carry + e;
+        const uint32_t cnt = (n + kDistChunk - 1) / kDistChunk;
+        const uint32_t e = block_exclusive_scan(cnt, &tot);
+        if (r < n_regions) {
+            item_offsets[r] = carry + e;
+            for (uint32_t i = carry + e; i < carry + e + cnt && i < cap_items; ++i) item_region[i] = r;
+        }
         __syncthreads();
         if (threadIdx.x == 0) carry += tot;
         __syncthreads();
@@ -324,7 +331,8 @@ __global__ void __launch_bounds__(kScanThreads) distance_items_kernel(const uint
 __global__ void __launch_bounds__(kDistThreads) distance_partial_kernel(const pg_region_state *states,
                                                                         const float4 *dirw, const float *dist,
                                                                         const uint32_t *offsets, uint32_t n_regions,
-                                                                        const uint32_t *item_offsets, float *partial,
+                                                                        const uint32_t *item_offsets,
+                                                                        const uint32_t *item_region, float *partial,
                                                                         uint64_t cap_items, uint32_t *error_word) {
     constexpr int NW = kDistThreads / 32;
     // component constants as pairs (component 2j in .x, 2j + 1 in .y): the
@@ -338,16 +346,7 @@ __global__ void __launch_bounds__(kDistThreads) distance_partial_kernel(const pg
         return;
     }
     for (uint32_t item = blockIdx.x; item < n_items; item += gridDim.x) {
-        // the region of this item: the last r with item_offsets[r] <= item
-        uint32_t lo = 0, hi = n_regions - 1;
-        while (lo < hi) {
-            const uint32_t mid = (lo + hi + 1) / 2;
-            if (item_offsets[mid] <= item)
-                lo = mid;
-            else
-                hi = mid - 1;
-        }
-        const uint32_t r = lo;
+        const uint32_t r = item_region[item];
         const pg_region_state *s = states + r;
         if (tid < 16) {
             const int c = tid;
@@ -373,10 +372,18 @@ __global__ void __launch_bounds__(kDistThreads) distance_partial_kernel(const pg
         for (int j = 0; j < 8; ++j) bw[j] = bwd[j] = make_float2(0.0f, 0.0f);
         const uint32_t b = offsets[r] + (item - item_offsets[r]) * kDistChunk;
         const uint32_t e = min(offsets[r + 1], b + kDistChunk);
-        for (uint32_t i = b + tid; i < e; i += kDistThreads) {
-            const float t = dist[i];
+        // the next sample's distance and direction load while this one computes
+        uint32_t i = b + tid;
+        float t_nx = i < e ? dist[i] : 0.0f;
+        float4 d_nx = i < e ? dirw[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        for (; i < e; i += kDistThreads) {
+            const float t = t_nx;
+            const float4 d = d_nx;
+            if (i + kDistThreads < e) {
+                t_nx = dist[i + kDistThreads];
+                d_nx = dirw[i + kDistThreads];
+            }
             if (!(t > 0.0f)) continue;
-            const float4 d = dirw[i];
             const float2 dx2 = make_float2(d.x, d.x), dy2 = make_float2(d.y, d.y), dz2 = make_float2(d.z, d.z);
             float2 ek[8];
             float p = 0.0f;
@@ -630,6 +637,7 @@ struct GuideScratch {
     pg_region_split_config rs{};
     // distance pass: work-item offsets per region and the items' partial sums
     uint32_t *dist_items = nullptr;
+    uint32_t *dist_item_region = nullptr;  // per work item: its region
     float *dist_partial = nullptr;
     uint32_t cap_dist_regions = 0;
     uint64_t cap_dist_items = 0;
@@ -661,6 +669,7 @@ void guide_release(pg_ctx *ctx) {
     cudaFree(g.leaf_of);
     cudaFree(g.split_out);
     cudaFree(g.dist_items);
+    cudaFree(g.dist_item_region);
     cudaFree(g.dist_partial);
     delete static_cast<GuideScratch *>(ctx->guide);
     ctx->guide = nullptr;
@@ -725,13 +734,18 @@ static int update_distances(pg_ctx *ctx, const float4 *dirw, const float *dist, 
     }
     if (items > g.cap_dist_items) {
         cudaFree(g.dist_partial);
+        cudaFree(g.dist_item_region);
         g.dist_partial = nullptr;
+        g.dist_item_region = nullptr;
         g.cap_dist_items = 0;
         if (int st = check_cuda(ctx, cudaMalloc(&g.dist_partial, sizeof(float) * 32 * items), "distance sums"))
             return st;
+        if (int st = check_cuda(ctx, cudaMalloc(&g.dist_item_region, sizeof(uint32_t) * items), "distance items"))
+            return st;
         g.cap_dist_items = items;
     }
-    distance_items_kernel<<<1, kScanThreads, 0, s>>>(offsets, n_regions, g.dist_items);
+    distance_items_kernel<<<1, kScanThreads, 0, s>>>(offsets, n_regions, g.dist_items, g.dist_item_region,
+                                                     g.cap_dist_items);
     // persistent: as many CTAs as are resident (each thread sums 32 samples of
     // an item; several items in flight per SM hide the per-item latency)
     int per_sm = 0;
@@ -741,7 +755,8 @@ static int update_distances(pg_ctx *ctx, const float4 *dirw, const float *dist, 
         per_sm = 1;
     const uint32_t grid = (uint32_t)std::min<uint64_t>(items, (uint64_t)ctx->sm_count * (uint64_t)per_sm);
     distance_partial_kernel<<<grid, kDistThreads, 0, s>>>(ctx->d_states, dirw, dist, offsets, n_regions,
-                                                          g.dist_items, g.dist_partial, g.cap_dist_items,
+                                                          g.dist_items, g.dist_item_region, g.dist_partial,
+                                                          g.cap_dist_items,
                                                           ctx->d_counters + 2);
     distance_finalize_kernel<<<(n_regions + 7) / 8, 256, 0, s>>>(ctx->d_states, g.dist_items, n_regions,
                                                                   g.dist_partial, g.cap_dist_items);
