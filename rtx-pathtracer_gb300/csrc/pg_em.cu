@@ -96,7 +96,7 @@ int fit_range(pg_ctx *ctx, const float *dirw, const uint32_t *offsets, uint32_t 
     guide_mark_stale(ctx);
     int st = upload_init_table(ctx, s);
     if (st) return st;
-    st = check_cuda(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(uint32_t) * 4, s), "queue reset");
+    st = check_cuda(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(uint32_t) * 6, s), "queue reset");
     if (st) return st;
     const pg_fit_tuning &t = ctx->tuning;
     // Defaults: the best point of the tuning sweep on the 4096-region K=16
@@ -201,6 +201,7 @@ int pg_fit_regions_host(pg_ctx *ctx, const float *dirw_host, const uint32_t *off
         HostSamples hs;
         memset(&hs, 0, sizeof hs);
         hs.mapped = static_cast<const float4 *>(pa.devicePointer);
+        hs.pulls = ctx->d_counters + 4;  // zeroed with the fit's queue counters
         return fit_range(ctx, reinterpret_cast<const float *>(ctx->h2d_dirw), ctx->h2d_offsets, 0, n_regions, mode,
                          s, &hs);
     }

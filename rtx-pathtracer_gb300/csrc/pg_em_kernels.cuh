@@ -88,6 +88,27 @@ __device__ __forceinline__ void wait_samples(const EmArgs &a, uint32_t b) {
     __threadfence();
 }
 
+// At most kPullers CTAs read their slices from host memory at once, in the
+// order they ask (about the fit's largest-first order): the host link then
+// serves the first regions' samples first instead of sharing its bandwidth
+// among every CTA of the first wave.  Thread 0; a wait that runs out (about
+// 2 s) reports PG_DEV_ERR_TIMEOUT and reads anyway.
+constexpr uint32_t kPullers = 32;
+__device__ __forceinline__ void pull_gate_enter(const EmArgs &a) {
+    const uint32_t t = atomicAdd(a.host.pulls, 1u);
+    const long long t0 = clock64();
+    for (;;) {
+        uint32_t done;
+        asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(done) : "l"(a.host.pulls + 1) : "memory");
+        if (done + kPullers > t) break;
+        if (clock64() - t0 > 4000000000LL) {
+            atomicOr(a.error_word, PG_DEV_ERR_TIMEOUT);
+            break;
+        }
+        __nanosleep(256);
+    }
+}
+
 // The CTA's threads copy samples [0, n) from src (page-locked host memory the
 // device addresses) to dst (shared or device memory), eight 16-byte loads in
 // flight per thread.
@@ -731,9 +752,12 @@ __device__ void process_region(const EmArgs &a, EmShared<KMAX, NT / 32> &S, floa
     bool ok = true;
     if (resident && max_itr > 0 && n_local > 0 && a.host.mapped) {
         // samples in page-locked host memory: the CTA reads its slice itself
+        if (tid == 0) pull_gate_enter(a);
+        __syncthreads();
         pull_samples(a.host.mapped + sb, s_samp, n_local, tid, NT);
         fence_proxy_async_smem();  // later TMA writes to this shared memory come after these stores
         __syncthreads();
+        if (tid == 0) atomicAdd(a.host.pulls + 1, 1u);
     } else if (resident && max_itr > 0 && n_local > 0) {
         if (tid == 0) {
             fence_proxy_async_smem();
@@ -769,9 +793,12 @@ __device__ void process_region(const EmArgs &a, EmShared<KMAX, NT / 32> &S, floa
     if (ring && a.host.mapped) {
         // streamed slice from host memory: copy it once to its place in the
         // device sample buffer, which the ring's TMA copies then read
+        if (tid == 0) pull_gate_enter(a);
+        __syncthreads();
         pull_samples(a.host.mapped + sb, const_cast<float4 *>(a.dirw) + sb, n_local, tid, NT);
         fence_proxy_async_global();
         __syncthreads();
+        if (tid == 0) atomicAdd(a.host.pulls + 1, 1u);
     }
     if (ring && tid == 0) {
         fence_proxy_async_smem();

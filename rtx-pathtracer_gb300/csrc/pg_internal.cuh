@@ -65,6 +65,7 @@ int upload_init_table(pg_ctx *ctx, cudaStream_t s);
 constexpr uint32_t kMaxArrivalChunks = 16;
 struct HostSamples {
     const float4 *mapped;
+    uint32_t *pulls;  // mapped: [0] tickets handed out, [1] slices read (device counters, zeroed per fit)
     const uint32_t *ready;
     uint32_t n_chunks;
     uint32_t start[kMaxArrivalChunks + 1];
