@@ -1172,19 +1172,44 @@ def main():
     h2d = dirw_h.numel() * 4 + offs_h.numel() * 4
     d2h = R * abi.STATE_DTYPE.itemsize
     offs_np = offs_h  # pinned: the offsets copy is asynchronous too
+
+    def host_step():
+        ctx.fit_host(dirw_h, offs_np, R, abi.PG_FIT_INIT, stream=stream)
+        ctx.states(R, stream=stream)  # D2H of the fitted states + stream sync
+
+    # A host-fed region's first iteration waits for its samples to cross the host
+    # link, and a larger cluster splits that wait among its CTAs: the host path
+    # keeps the tuned shape or the same shape with 4-CTA clusters, whichever is
+    # faster on this machine (three untimed steps each).
+    e2e_tuning = None
+    if tuned is not None and tuned["cluster_size"] not in (1, 4):
+        best_e2e = None
+        for cl in sorted({tuned["cluster_size"], 4}):
+            cand = dict(tuned, cluster_size=cl)
+            ctx.set_tuning(**cand)
+            with torch.cuda.stream(stream):
+                host_step()
+                t1 = time.perf_counter()
+                for _ in range(3):
+                    host_step()
+                t1 = time.perf_counter() - t1
+            if best_e2e is None or t1 < best_e2e[0]:
+                best_e2e = (t1, cand)
+        e2e_tuning = best_e2e[1]
+        ctx.set_tuning(**e2e_tuning)
     with torch.cuda.stream(stream):
         for _ in range(max(1, args.warmup)):
-            ctx.fit_host(dirw_h, offs_np, R, abi.PG_FIT_INIT, stream=stream)
-            ctx.states(R, stream=stream)
+            host_step()
     torch.cuda.synchronize()
     e2e_steps = max(1, args.steps)
     t0 = time.perf_counter()
     with torch.cuda.stream(stream):
         for _ in range(e2e_steps):
-            ctx.fit_host(dirw_h, offs_np, R, abi.PG_FIT_INIT, stream=stream)
-            ctx.states(R, stream=stream)  # D2H of the fitted states + stream sync
+            host_step()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
     e2e_value = si_per_step * world / (e2e_ms * 1e-3) / 1e6
+    if e2e_tuning is not None:
+        ctx.set_tuning(**tuned)  # the later blocks use the device fit's shape
 
     hbm, peak_src = measured_peaks()
     alg_bytes = 16.0 * si_per_step
@@ -1211,7 +1236,8 @@ def main():
                        "launch": "captured CUDA graph" if graph is not None else "direct",
                        "tuning": tuned if tuned is not None else "manual", "autotuned_ms": tune_ms},
             "gpu_launches": launches * args.steps,
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "cluster_size": (e2e_tuning or tuned or {}).get("cluster_size")},
             "roofline": roofline, "clocks": sampler.summary()}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(w).items() if k != "seconds"}
