@@ -222,6 +222,37 @@ def test_argument_errors(cuda, pkg, abi):
     ctx.close()
 
 
+
+def test_fit_from_host_memory_with_empty_regions(cuda, pkg, abi, workloads):
+    """Host-fed fits with empty regions between full ones, and with every region
+    empty: page-locked (read by the fit) and pageable (copied in chunks) samples
+    give the device fit's states bit for bit."""
+    torch = cuda
+    w = workloads.fit_batched(seed=31, n_regions=120, median=3000, sigma=1.0, lo=64, hi=30000)
+    counts = np.diff(w["offsets"].astype(np.int64))
+    counts[::3] = 0  # every third region empty
+    counts[-1] = 0
+    keep = np.concatenate([np.arange(w["offsets"][r], w["offsets"][r] + counts[r]) for r in range(len(counts))])
+    dirw = np.ascontiguousarray(w["dirw"][keep], dtype=np.float32)
+    offsets = np.concatenate([[0], np.cumsum(counts)]).astype(np.uint32)
+    R = len(counts)
+    cfg = abi.forced_iterations(20, num_initial_components=16)
+    for dw, off in ((dirw, offsets), (np.zeros((0, 4), np.float32), np.zeros(R + 1, np.uint32))):
+        a = pkg.FitContext(cfg, max_regions=R)
+        d = torch.from_numpy(dw.reshape(-1, 4) if dw.size else np.zeros((1, 4), np.float32)).cuda()
+        o = torch.from_numpy(off.view(np.int32)).cuda()
+        a.fit(d, o, R, abi.PG_FIT_INIT)
+        a.sync()
+        want = a.states(R)
+        for host in (torch.from_numpy(dw.reshape(-1) if dw.size else np.zeros(4, np.float32)).pin_memory(),
+                     np.ascontiguousarray(dw.reshape(-1) if dw.size else np.zeros(4, np.float32))):
+            b = pkg.FitContext(cfg, max_regions=R)
+            b.fit_host(host, torch.from_numpy(off.view(np.int32)).pin_memory(), R, abi.PG_FIT_INIT)
+            b.sync()
+            assert want.tobytes() == b.states(R).tobytes()
+            b.close()
+        a.close()
+
 @pytest.mark.parametrize("mode", ["init", "update", "forced16"])
 def test_fit_from_host_memory_equals_device_fit(mode, cuda, pkg, abi, workloads):
     """pg_fit_regions_host (the fit from host memory) gives the same states,
