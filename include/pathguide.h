@@ -652,7 +652,9 @@ typedef struct pg_irradiance_cache_config {
     float gradients_max_length;   /* irradianceGradientsMaxLength */
     uint32_t visibility_check;    /* irradianceCachePerformVisibilityCheck */
     uint32_t use_on_glossy;       /* useIrradianceCacheOnGlossy */
-    uint32_t reserved[3];
+    uint32_t num_nee;             /* irradianceNumNEE: light samples averaged at each
+                                     vertex of an entry's hemisphere paths (0: 1; at most 64) */
+    uint32_t reserved[2];
 } pg_irradiance_cache_config;
 
 /* One cache entry (cacheSpheres[i] and cache[i] of raytrace.rgen:118-119): the

@@ -67,12 +67,13 @@ class RenderConfig(C.Structure):
 class IcConfig(C.Structure):
     _fields_ = [("a", C.c_float), ("min_radius", C.c_float), ("gradients_max_length", C.c_float),
                 ("use_gradients", C.c_uint32), ("visibility_check", C.c_uint32), ("use_on_glossy", C.c_uint32),
-                ("capacity", C.c_uint32)]
+                ("capacity", C.c_uint32), ("num_nee", C.c_uint32)]
 
 
 def ic_config(capacity, a=0.2, min_radius=0.1, gradients_max_length=5.0, use_gradients=0, visibility_check=0,
-              use_on_glossy=0) -> IcConfig:
-    return IcConfig(a, min_radius, gradients_max_length, use_gradients, visibility_check, use_on_glossy, capacity)
+              use_on_glossy=0, num_nee=0) -> IcConfig:
+    return IcConfig(a, min_radius, gradients_max_length, use_gradients, visibility_check, use_on_glossy, capacity,
+                    num_nee)
 
 
 class GlslRef:

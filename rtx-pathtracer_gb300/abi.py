@@ -194,7 +194,8 @@ class AdrrsConfig(C.Structure):
 class IrradianceCacheConfig(C.Structure):
     _fields_ = [("capacity", C.c_uint32), ("a", C.c_float), ("min_radius", C.c_float), ("create_prob", C.c_float),
                 ("update_prob", C.c_float), ("use_gradients", C.c_uint32), ("gradients_max_length", C.c_float),
-                ("visibility_check", C.c_uint32), ("use_on_glossy", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+                ("visibility_check", C.c_uint32), ("use_on_glossy", C.c_uint32), ("num_nee", C.c_uint32),
+                ("reserved", C.c_uint32 * 2)]
 
 
 # pg_ic_entry (72 bytes) and pg_ic_request (40 bytes)

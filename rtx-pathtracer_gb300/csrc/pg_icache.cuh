@@ -60,6 +60,7 @@ struct DevIc {
     float lo[3], inv_cell[3];
     float a, min_radius, create_prob, update_prob, grad_max;
     int use_gradients, visibility, on_glossy;
+    uint32_t num_nee;            // light samples averaged per vertex of an entry's paths (>= 1)
     int query, grow;             // what this render call does: query; create and update
     IcRequest *requests;
     uint32_t req_cap, capacity;

@@ -100,8 +100,18 @@ __device__ V ic_stratum_path(const DevRender &R, uint32_t seed, uint32_t stream,
             ++follow_count;  // depth >= maxDepth (1) always holds
         } else {
             add_next = false;
-            const V direct = ic_direct(R, m, x, n, wi, rnd(seed, stream, (uint32_t)s, dim),
-                                       rnd(seed, stream, (uint32_t)s, dim + 1), rnd(seed, stream, (uint32_t)s, dim + 2));
+            // multipleNEE (raytrace.rgen:871-877): the mean of irradianceNumNEE light
+            // samples; sample q > 0 draws from the stratum's stream at index s + 256 q
+            V direct = ic_direct(R, m, x, n, wi, rnd(seed, stream, (uint32_t)s, dim),
+                                 rnd(seed, stream, (uint32_t)s, dim + 1), rnd(seed, stream, (uint32_t)s, dim + 2));
+            if (R.ic.num_nee > 1) {
+                for (uint32_t q = 1; q < R.ic.num_nee; ++q) {
+                    const uint32_t sq = (uint32_t)s + 256u * q;
+                    direct = add(direct, ic_direct(R, m, x, n, wi, rnd(seed, stream, sq, dim),
+                                                   rnd(seed, stream, sq, dim + 1), rnd(seed, stream, sq, dim + 2)));
+                }
+                direct = mul(direct, 1.0f / (float)R.ic.num_nee);
+            }
             V E;
             if (R.ic.query && ic_capable(R.ic, m) && ic_query(R.ic, x, n, E)) {
                 L = add(L, hmul(thr, add(hmul(approx_diffuse(m, n, wi), E), direct)));

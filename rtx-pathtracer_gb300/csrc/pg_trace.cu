@@ -1703,6 +1703,7 @@ void ic_view(const pg_scene *sc, DevIc &D) {
     D.use_gradients = c.cfg.use_gradients ? 1 : 0;
     D.visibility = c.cfg.visibility_check ? 1 : 0;
     D.on_glossy = c.cfg.use_on_glossy ? 1 : 0;
+    D.num_nee = c.cfg.num_nee ? c.cfg.num_nee : 1u;
     D.requests = c.requests;
     D.req_cap = c.req_cap;
     D.capacity = c.cfg.capacity;
@@ -1883,11 +1884,13 @@ void pg_default_irradiance_cache_config(pg_irradiance_cache_config *out) {
     out->gradients_max_length = 5.0f;
     out->visibility_check = 0;
     out->use_on_glossy = 0;
+    out->num_nee = 1;
 }
 
 int pg_scene_set_irradiance_cache(pg_scene *sc, const pg_irradiance_cache_config *cfg) {
     if (!sc || !cfg) return PG_ERR_ARG;
     if (cfg->capacity > (1u << 24)) return scene_error(PG_ERR_ARG, "irradiance cache capacity above 2^24 entries");
+    if (cfg->num_nee > 64) return scene_error(PG_ERR_ARG, "irradiance cache: num_nee above 64");
     if (cfg->capacity && (!(cfg->a > 0.0f) || !std::isfinite(cfg->a) || !(cfg->min_radius >= 0.0f) ||
                           !(cfg->create_prob >= 0.0f && cfg->create_prob <= 1.0f) ||
                           !(cfg->update_prob >= 0.0f && cfg->update_prob <= 1.0f) ||

@@ -11,7 +11,8 @@ C++ by oracle/build_glsl_ref.py - on seeded inputs, for the GPU cache to match
     visibility test;
   * compute__*: calculateCacheData at six surface points of the Cornell box,
     COMPUTE_RUNS runs each (random states 1..), with an empty cache and with
-    the cache of render__entries;
+    the cache of render__entries, and with an empty cache and three light
+    samples per vertex (irradianceNumNEE 3, compute__empty_nee3);
   * render__*: a cache of entries createIrradianceCache made at surface
     points the camera sees and their next bounce, and the reference's
     estimator querying it (no entries made while rendering): PARTS parts of
@@ -77,8 +78,9 @@ def main(out: Path = OUT):
     pos_r = np.repeat(cp, COMPUTE_RUNS, axis=0)
     nrm_r = np.repeat(cn, COMPUTE_RUNS, axis=0)
     seeds = np.tile(np.arange(1, COMPUTE_RUNS + 1, dtype=np.uint32), len(cp))
-    for name, ent in (("empty", np.zeros(0, dtype=abi.IC_ENTRY_DTYPE)), ("cache", cache)):
-        g.ic_set(ent, ic_config(IC_CAPACITY, a=IC_A))
+    empty = np.zeros(0, dtype=abi.IC_ENTRY_DTYPE)
+    for name, ent, nee in (("empty", empty, 0), ("cache", cache, 0), ("empty_nee3", empty, 3)):
+        g.ic_set(ent, ic_config(IC_CAPACITY, a=IC_A, num_nee=nee))
         res = g.ic_compute(exp, pos_r, nrm_r, seeds).reshape(len(cp), COMPUTE_RUNS, 10)
         arrays[f"compute__{name}"] = res
         print(name, np.round(res.mean(1)[:, [0, 1, 2, 9]], 4))

@@ -69,10 +69,13 @@ def _gpu_compute(sc, abi, points, normals, runs, seed=1):
     return sc.ic_compute(params, req).reshape(len(points), runs)
 
 
-@pytest.mark.parametrize("cache", ["empty", "cache"])
+@pytest.mark.parametrize("cache", ["empty", "cache", "empty_nee3"])
 def test_compute_matches_reference(cache, fixture, cuda, pkg, abi):
+    """calculateCacheData: the GPU's entries against the reference's over many
+    runs (empty_nee3: three light samples per vertex, irradianceNumNEE 3)."""
     sc = S.cornell()
-    sc.set_irradiance_cache(capacity=S.IC_CAPACITY, a=S.IC_A, create_prob=0.0, update_prob=0.0)
+    sc.set_irradiance_cache(capacity=S.IC_CAPACITY, a=S.IC_A, create_prob=0.0, update_prob=0.0,
+                            num_nee=3 if cache == "empty_nee3" else 1)
     if cache == "cache":
         sc.set_irradiance_cache_entries(fixture["render__entries"])
     runs = 4096
